@@ -1,0 +1,223 @@
+/*
+ * libnqcuda -- GB300 (sm_103a) engine for the variational Monte Carlo step of
+ * NeuralQuantum.jl.  C ABI only: plain pointers, sizes and enums.
+ *
+ * The reference plugs GPU support in through Julia multiple dispatch on
+ * GPUArray state types (src/GPU/Base/GPUstates.jl:1-7).  This library
+ * replaces that layer with coarse-grained calls, one per stage of the
+ * reference's iterative interface:
+ *
+ *   reference call                                        entry point here
+ *   ---------------------------------------------------   --------------------
+ *   BatchedSampler(net, sampler, prob, algo; batch_sz)     nq_create +
+ *     (src/IterativeInterface/build_Batched.jl:1-14)         nq_set_params +
+ *                                                            nq_set_operator
+ *   _sample_state!(is)  (BaseIterativeSampler.jl:5-17)     nq_sample
+ *     init_sampler!/samplenext! (Metropolis.jl:101-167)
+ *     propose_step!(LocalRule) (LocalRuleGPU.jl:23-36)
+ *   logψ!/logψ_and_∇logψ! (RBMBatched.jl:37-91,           nq_logpsi, nq_logpsi_grad
+ *     NDMBatched.jl:94-280)
+ *   sample!(is) minus sampling: estimator loop, stats,     nq_estimate
+ *     centring, gradient, setup_algorithm!
+ *     (BatchedValSampler.jl:117-139,
+ *      BatchedGradSampler.jl:77-123, SRDirect.jl:26-48)
+ *   precondition!(prec, SR, iter) (SRDirect.jl:51-90)      nq_precondition
+ *   Optimisers.update!(Descent(η), net, Δw)                nq_update_descent
+ *     (src/Optimisers/apply.jl:25-32)
+ *   one full iteration of the examples' loop               nq_vmc_step
+ *     (examples/ising1d.jl:32-42)
+ *
+ * Conventions (the reference's own, so the Julia side needs no reshaping):
+ *   - parameters cross the ABI as one flat vector in the reference order
+ *     (functor field order, each array column-major; src/tuple_logic.jl:31-72):
+ *     RBM: a, b, W (M x N).  NDM: b_mu, h_mu, w_mu, u_mu, b_la, h_la, d_la,
+ *     w_la, u_la.  RBM parameters are complex, NDM parameters real.
+ *   - configurations cross the ABI as int8 site values (spin: -1/+1, Fock:
+ *     0/1), N x B x L column-major (the reference's samples array); doubled
+ *     (density-matrix) states are the row array followed by the column array.
+ *   - complex numbers are interleaved (re, im) pairs.
+ *
+ * Errors: every call returns an nq_status; the message of the last failure on
+ * a handle is available from nq_last_error.  No C++ exception crosses the ABI.
+ * Threading: a handle is not thread-safe; distinct handles are independent
+ * (each owns its CUDA stream and device buffers).
+ */
+#ifndef NQCUDA_H
+#define NQCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NQCUDA_ABI_VERSION 1
+
+typedef enum {
+  NQ_OK = 0,
+  NQ_ERR_ARG = 1,          /* invalid argument or size */
+  NQ_ERR_CUDA = 2,         /* CUDA runtime error */
+  NQ_ERR_NOT_PD = 3,       /* SR matrix not positive definite */
+  NQ_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+  NQ_ERR_NAN = 5,          /* non-finite values detected */
+  NQ_ERR_STATE = 6,        /* call order violated (e.g. no operator set) */
+  NQ_ERR_UNSUPPORTED = 7   /* configuration outside the supported envelope */
+} nq_status;
+
+typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1 } nq_network;
+typedef enum { NQ_ACT_LOGCOSH = 0, NQ_ACT_SOFTPLUS = 1 } nq_activation;
+typedef enum { NQ_HILB_SPIN = 0, NQ_HILB_FOCK = 1 } nq_hilbert;
+typedef enum { NQ_DTYPE_C64 = 0, NQ_DTYPE_C128 = 1, NQ_DTYPE_F32 = 2, NQ_DTYPE_F64 = 3 } nq_dtype;
+
+/* Precision of the network evaluation (θ contraction + estimator). */
+typedef enum {
+  NQ_EVAL_F32 = 0,         /* FP32 CUDA cores */
+  NQ_EVAL_TC_BF16X2 = 1,   /* θ = Wσ+b on tcgen05, W split in bf16 hi+lo, FP32 accumulate */
+  NQ_EVAL_F64 = 2          /* FP64 (small reference-precision runs) */
+} nq_eval_precision;
+
+/* Precision of the S = O_c O_c† accumulation. */
+typedef enum {
+  NQ_S_F32 = 0,            /* FP32 CUDA cores */
+  NQ_S_TF32 = 1,           /* tcgen05 kind::tf32, FP32 accumulate */
+  NQ_S_TF32X3 = 2,         /* tcgen05 kind::tf32 with hi/lo split (3 products) */
+  NQ_S_F64 = 3             /* FP64 CUDA cores */
+} nq_s_precision;
+
+/* Reference quirks that can be reproduced exactly (off by default). */
+#define NQ_QUIRK_STALE_LAST_SLOT 0x1u  /* BaseIterativeSampler.jl:11-16 never writes slot L */
+
+typedef struct {
+  int32_t network;         /* nq_network */
+  int32_t activation;      /* nq_activation */
+  int32_t hilbert;         /* nq_hilbert (local dimension 2) */
+  int32_t n_sites;         /* N (physical sites) */
+  int32_t n_hidden;        /* RBM: M = αN; NDM: hidden units αN */
+  int32_t n_ancilla;       /* NDM: βN; ignored for the RBM */
+  int32_t n_chains;        /* batch_sz: independent Metropolis chains */
+  int32_t chain_length;    /* samples recorded per chain per nq_sample */
+  int32_t burn;            /* burn-in sweeps */
+  int32_t passes;          /* Metropolis steps per sweep (even -> +1, Metropolis.jl:30-38) */
+  uint64_t seed;           /* Philox key */
+  int32_t eval_precision;  /* nq_eval_precision */
+  int32_t s_precision;     /* nq_s_precision */
+  uint32_t quirks;         /* NQ_QUIRK_* bits */
+  int32_t reserved[7];
+} nq_config;
+
+/* Statistics of the local estimator (src/utils/stats.jl:1-50). */
+typedef struct {
+  double mean_re, mean_im;
+  double error;
+  double variance;
+  double tau;
+  double R;
+  double acceptance;       /* accepted / proposed Metropolis steps of the last nq_sample */
+} nq_measurement;
+
+/*
+ * A flattened k-local operator (KLocalOperatorSum, or the three operator
+ * lists of a KLocalLiouvillian) in the order accumulate_connections! visits
+ * them (KLocalOperatorSum.jl:65-72, KLocalLiouvillian.jl:46-52).  Sites index
+ * the full configuration: 0..N-1 for a ket or the row (σ) of a doubled state,
+ * N..2N-1 for its column (η).  One entry per local operator o:
+ *   op_n_sites[o]        number of digit sites (1..8)
+ *   op_sites[8*o + i]    site of digit i (first digit least significant,
+ *                        KLocalOperator.jl local_index)
+ *   op_row_offset[o]     first global row of this operator
+ * A left-right tensor KLocalOperatorTensor(L, conj L) is one operator whose
+ * digits are its row sites followed by its column sites; its rows list the
+ * products mel_l * mel_r of all pairs (KLocalOperatorTensor.jl:149-156).
+ *   row_conn_offset[r]   first connection of global row r (length n_rows + 1)
+ *   conn_mel[2*c]        complex matrix element (re, im)
+ *   conn_n_changes[c]    number of changed sites (0..8)
+ *   conn_change_site[8*c + i]   changed site (0..2N-1)
+ *   conn_change_value[8*c + i]  new site value (-1/+1 or 0/1)
+ */
+typedef struct {
+  int32_t n_ops;
+  int32_t n_rows;
+  int32_t n_conns;
+  const int32_t* op_n_sites;
+  const int32_t* op_sites;
+  const int32_t* op_row_offset;
+  const int32_t* row_conn_offset;
+  const double* conn_mel;
+  const int32_t* conn_n_changes;
+  const int32_t* conn_change_site;
+  const int8_t* conn_change_value;
+} nq_op_table;
+
+typedef struct nq_handle nq_handle;
+
+/* ---- lifecycle ----------------------------------------------------------- */
+const char* nq_version(void);
+int32_t nq_abi_version(void);
+nq_status nq_create(const nq_config* cfg, nq_handle** out);
+void nq_destroy(nq_handle* h);
+nq_status nq_last_error(const nq_handle* h, char* buf, size_t len);
+int64_t nq_n_params(const nq_handle* h);
+
+/* ---- parameters: BatchedSampler(net, ...) / load_from_dict! ---------------- */
+nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype);
+nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype);
+
+/* ---- operator: the `prob` argument of BatchedSampler ----------------------- */
+nq_status nq_set_operator(nq_handle* h, const nq_op_table* op);
+
+/* ---- _sample_state!: Metropolis sampling of all chains --------------------
+ * call_index selects the Philox stream of this call (the reference re-seeds
+ * nothing; each call continues its MersenneTwister).  samples_out (nullable)
+ * receives N x B x L (doubled: 2N x B x L) int8 values.  accept_bits (nullable,
+ * testing aid) receives one byte per (step, chain), step-major. */
+nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out,
+                    uint8_t* accept_bits);
+/* Replace the sample buffer (N x B x L int8), e.g. to evaluate given states. */
+nq_status nq_set_samples(nq_handle* h, const int8_t* samples);
+
+/* ---- logψ! / logψ_and_∇logψ! on arbitrary host batches --------------------
+ * sigma: n configurations, int8, column-major (N x n; doubled: row block
+ * 2N x n with rows 0..N-1 = σ, N..2N-1 = η).  out: n complex128.
+ * grad (nullable): P x n complex128, column-major. */
+nq_status nq_logpsi(nq_handle* h, const int8_t* sigma, int64_t n, double* out);
+nq_status nq_logpsi_grad(nq_handle* h, const int8_t* sigma, int64_t n, double* out,
+                         double* grad);
+
+/* ---- sample!(is) after sampling -------------------------------------------
+ * Evaluates logψ and ∇logψ on the sample buffer, the local estimator of the
+ * operator (E_loc, or L_loc and ∇L_loc for a Liouvillian), its statistics,
+ * the centred gradient, the force F and the SR matrix S.
+ * loc_out (nullable): B x L complex128 local values.  force_out (nullable):
+ * P complex128 (real parameters: P float64). */
+nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out,
+                      double* force_out);
+/* S (nullable out): P x P column-major complex128 (real parameters: float64). */
+nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
+
+/* ---- precondition!(prec, SR, iter) ----------------------------------------
+ * kind: 0 = sr_shift (S_ii += eps), 1 = sr_multiplicative
+ * (S + max(lam0*b^iter, lam_min) diag S), 2 = sr_none.  Cholesky solve of
+ * S Δw = F.  dw_out (nullable) receives Δw (complex128 or float64). */
+nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0,
+                          double b, double lam_min, int32_t iter, double* dw_out);
+
+/* ---- Optimisers.update!(Descent(lr), net, Δw): w .-= lr Δw on device ------- */
+nq_status nq_update_descent(nq_handle* h, double lr);
+
+/* ---- one full VMC iteration: sample + estimate + precondition(shift) + update.
+ * Replays a captured CUDA graph after the first call. */
+nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
+                      nq_measurement* stats);
+
+/* ---- timing/diagnostics ----------------------------------------------------
+ * Milliseconds of the last call per stage: [sample, eval+estimator, stats+force,
+ * S, solve, update]. */
+nq_status nq_stage_times(nq_handle* h, float* ms6);
+/* Number of kernel launches issued by this handle since creation. */
+int64_t nq_kernel_launches(const nq_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NQCUDA_H */

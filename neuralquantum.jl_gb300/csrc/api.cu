@@ -1,0 +1,711 @@
+// C-ABI of libnqcuda: handle lifecycle, device buffers, the stage sequence of
+// one VMC iteration and its CUDA-graph replay.  See include/nqcuda.h for the
+// mapping of every entry point onto the reference interface it replaces.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/nqcuda.h"
+#include "nq_kernels.cuh"
+
+struct nq_handle {
+  nq_config cfg{};
+  int N = 0, M = 0, Ma = 0, nst = 0, P = 0, B = 0, L = 0, Ns = 0, passes = 1;
+  int n_record = 0, write_last = 0;
+  bool doubled = false, complex_params = true, f64 = false;
+  int hilb = 0, act = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int64_t launches = 0;
+
+  double* d_master = nullptr;      // FP64 master parameters (complex interleaved or real)
+  float* d_p32 = nullptr;          // FP32 working copy (RBM, complex)
+  void* d_tab[3] = {nullptr, nullptr, nullptr};
+  uint64_t* d_samples = nullptr;   // [L][B]
+  unsigned long long* d_accepted = nullptr;
+  uint32_t* d_call = nullptr;
+  void* d_logpsi = nullptr;        // cpx<R>[Ns]
+  void* d_g = nullptr;             // cpx<R>[M][Ns]
+  void* d_eloc = nullptr;          // cpx<R>[Ns]
+  float2* d_g32 = nullptr;         // FP32 view of g for the S stage
+  ForceBufs fb;
+  int force_nblk = 0;
+  double* d_stats = nullptr;       // 6 doubles
+  float* d_G = nullptr;
+  float* d_Gpart = nullptr;
+  int gram_ksplit = 1;
+  float* d_X = nullptr;
+  int Ns_pad = 0;
+  double* d_S = nullptr;
+  SolveBufs sb;
+  double* d_dw = nullptr;          // Δw as stored for the update (complex or real)
+  DevOp op;
+  bool has_op = false;
+  std::vector<void*> op_allocs;
+
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_kernels = 0;
+  double graph_eps = -1, graph_lr = -1;
+  uint32_t* h_call = nullptr;      // pinned
+  double* h_stats = nullptr;       // pinned [8]
+  unsigned long long* h_acc = nullptr;
+  cudaEvent_t ev[7] = {};
+  float stage_ms[6] = {};
+  bool timing = true;
+};
+
+namespace {
+
+nq_status fail(nq_handle* h, nq_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  return code;
+}
+
+#define CK(expr)                                                                          \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess)                                                                \
+      return fail(h, NQ_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                  __FILE__, __LINE__);                                                    \
+  } while (0)
+
+#define CKL(expr)       \
+  do {                  \
+    ++h->launches;      \
+    CK(expr);           \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  return cudaMalloc((void**)p, count * sizeof(T) + 16);
+}
+
+template <typename R>
+RbmDev<R> rbm_dev(nq_handle* h) {
+  RbmDev<R> d;
+  d.N = h->N; d.M = h->M; d.act = h->act; d.hilb = h->hilb;
+  const cpx<R>* base;
+  if (h->f64) base = reinterpret_cast<const cpx<R>*>(h->d_master);
+  else base = reinterpret_cast<const cpx<R>*>(h->d_p32);
+  d.a = base;
+  d.b = base + h->N;
+  d.W = base + h->N + h->M;
+  d.t0 = reinterpret_cast<const cpx<R>*>(h->d_tab[0]);
+  d.t1 = reinterpret_cast<const cpx<R>*>(h->d_tab[1]);
+  d.t2 = reinterpret_cast<const cpx<R>*>(h->d_tab[2]);
+  return d;
+}
+
+// refresh FP32 copies and the per-flip tables after a parameter change
+nq_status refresh_params(nq_handle* h) {
+  if (!h->f64) CKL(launch_rbm_params_from_master(h->d_master, h->N, h->M, h->d_p32, h->st));
+  if (h->f64) {
+    RbmDev<double> d = rbm_dev<double>(h);
+    CKL(launch_rbm_tables<double>(d, (cpx<double>*)h->d_tab[0], (cpx<double>*)h->d_tab[1],
+                                  (cpx<double>*)h->d_tab[2], h->st));
+  } else {
+    RbmDev<float> d = rbm_dev<float>(h);
+    CKL(launch_rbm_tables<float>(d, (cpx<float>*)h->d_tab[0], (cpx<float>*)h->d_tab[1],
+                                 (cpx<float>*)h->d_tab[2], h->st));
+  }
+  return NQ_OK;
+}
+
+nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_dev,
+                       const uint32_t* call_ptr = nullptr) {
+  SamplerRun run;
+  run.B = h->B; run.L = h->L; run.burn = h->cfg.burn; run.passes = h->passes;
+  run.n_record = h->n_record; run.write_last_at_end = h->write_last;
+  run.k0 = (uint32_t)(h->cfg.seed & 0xffffffffu);
+  run.k1 = (uint32_t)(h->cfg.seed >> 32);
+  run.call = call;
+  run.call_ptr = call_ptr;
+  run.samples = h->d_samples;
+  run.accepted = h->d_accepted;
+  run.accept_bits = accept_bits_dev;
+  CK(cudaMemsetAsync(h->d_accepted, 0, sizeof(unsigned long long), h->st));
+  if (h->f64) CKL(launch_rbm_sampler<double>(rbm_dev<double>(h), run, h->st));
+  else CKL(launch_rbm_sampler<float>(rbm_dev<float>(h), run, h->st));
+  return NQ_OK;
+}
+
+nq_status stage_eval(nq_handle* h) {
+  const DevOp* op = h->has_op ? &h->op : nullptr;
+  if (h->f64) {
+    CKL(launch_rbm_eval<double>(rbm_dev<double>(h), h->d_samples, h->Ns, op, (cpx<double>*)h->d_logpsi,
+                                (cpx<double>*)h->d_g, (cpx<double>*)h->d_eloc, h->st));
+  } else {
+    CKL(launch_rbm_eval<float>(rbm_dev<float>(h), h->d_samples, h->Ns, op, (cpx<float>*)h->d_logpsi,
+                               (cpx<float>*)h->d_g, (cpx<float>*)h->d_eloc, h->st));
+  }
+  return NQ_OK;
+}
+
+__global__ void g64_to_32_kernel(const double* g, long n, float2* out) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_float2((float)g[2 * i], (float)g[2 * i + 1]);
+}
+
+nq_status stage_force(nq_handle* h) {
+  if (h->f64) {
+    CKL(launch_rbm_force<double>(rbm_dev<double>(h), h->d_samples, h->Ns, (cpx<double>*)h->d_g,
+                                 (cpx<double>*)h->d_eloc, h->fb, h->st));
+    CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_stats, h->st));
+  } else {
+    CKL(launch_rbm_force<float>(rbm_dev<float>(h), h->d_samples, h->Ns, (cpx<float>*)h->d_g,
+                                (cpx<float>*)h->d_eloc, h->fb, h->st));
+    CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 0, h->d_stats, h->st));
+  }
+  return NQ_OK;
+}
+
+nq_status stage_S(nq_handle* h) {
+  RbmOSource src;
+  src.N = h->N; src.M = h->M; src.hilb = h->hilb; src.Ns = h->Ns;
+  src.samples = h->d_samples;
+  if (h->f64) {
+    long n = (long)h->M * h->Ns;
+    ++h->launches;
+    g64_to_32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>((const double*)h->d_g, n, h->d_g32);
+    CK(cudaGetLastError());
+    src.g = h->d_g32;
+  } else {
+    src.g = reinterpret_cast<const float2*>(h->d_g);
+  }
+  src.meanO = h->fb.meanO;
+  const int sp = h->cfg.s_precision;
+  if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
+    CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, h->st));
+    CKL(launch_gram_tc(h->d_X, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
+                       h->gram_ksplit, h->st));
+  } else {
+    CKL(launch_gram_simt(src, h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
+  }
+  CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, !h->complex_params, h->d_S, h->st));
+  return NQ_OK;
+}
+
+nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
+  CKL(launch_sr_solve(h->sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, 2, h->st));
+  h->launches += 4L * ((h->P + 31) / 32) + 12;
+  return NQ_OK;
+}
+
+nq_status stage_update(nq_handle* h, double lr) {
+  long nd = h->complex_params ? 2L * h->P : h->P;
+  CKL(launch_descent(h->d_master, h->sb.x, nd, lr, h->st));
+  return refresh_params(h);
+}
+
+nq_status check_status_word(nq_handle* h) {
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, h->sb.status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (st != 0) {
+    CK(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st));
+    return fail(h, NQ_ERR_NOT_PD, "SR matrix is not positive definite after the diagonal shift");
+  }
+  return NQ_OK;
+}
+
+void fill_measurement(nq_handle* h, nq_measurement* m) {
+  if (!m) return;
+  m->mean_re = h->h_stats[0];
+  m->mean_im = h->h_stats[1];
+  m->error = h->h_stats[2];
+  m->variance = h->h_stats[3];
+  m->tau = h->h_stats[4];
+  m->R = h->h_stats[5];
+  double steps = (double)h->B * h->passes * (h->cfg.burn + h->n_record);
+  m->acceptance = steps > 0 ? (double)(*h->h_acc) / steps : 0.0;
+}
+
+void free_op(nq_handle* h) {
+  for (void* p : h->op_allocs) cudaFree(p);
+  h->op_allocs.clear();
+  h->has_op = false;
+  h->op = DevOp();
+}
+
+template <typename T>
+nq_status upload(nq_handle* h, const T* src, size_t count, const T** dst) {
+  if (count == 0) count = 1;
+  T* d = nullptr;
+  CK(cudaMalloc((void**)&d, count * sizeof(T)));
+  h->op_allocs.push_back(d);
+  if (src) CK(cudaMemcpy(d, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = d;
+  return NQ_OK;
+}
+
+}  // namespace
+
+// =============================== C ABI ======================================
+extern "C" {
+
+const char* nq_version(void) { return "libnqcuda 0.1.0 (sm_103a)"; }
+int32_t nq_abi_version(void) { return NQCUDA_ABI_VERSION; }
+
+nq_status nq_create(const nq_config* cfg, nq_handle** out) {
+  if (!cfg || !out) return NQ_ERR_ARG;
+  *out = nullptr;
+  nq_handle* h = new nq_handle();
+  h->cfg = *cfg;
+  const nq_config& c = *cfg;
+  auto bad = [&](const char* msg) {
+    fprintf(stderr, "nq_create: %s\n", msg);
+    delete h;
+    return NQ_ERR_ARG;
+  };
+  if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM) return bad("unknown network");
+  if (c.network == NQ_NET_NDM) {
+    delete h;
+    return NQ_ERR_UNSUPPORTED;
+  }
+  if (c.activation != NQ_ACT_LOGCOSH && c.activation != NQ_ACT_SOFTPLUS) return bad("unknown activation");
+  if (c.hilbert != NQ_HILB_SPIN && c.hilbert != NQ_HILB_FOCK) return bad("unknown hilbert space");
+  if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
+  if (c.n_hidden < 1 || c.n_hidden > 256) return bad("n_hidden must be in 1..256");
+  if (c.n_chains < 2 || c.chain_length < 1 || c.burn < 0 || c.passes < 1) return bad("bad sampler sizes");
+  if (c.eval_precision != NQ_EVAL_F32 && c.eval_precision != NQ_EVAL_F64) {
+    delete h;
+    return NQ_ERR_UNSUPPORTED;
+  }
+  if (c.s_precision == NQ_S_F64) { delete h; return NQ_ERR_UNSUPPORTED; }
+  if ((c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) && !gram_tc_supported()) {
+    delete h;
+    return NQ_ERR_UNSUPPORTED;
+  }
+  h->N = c.n_sites;
+  h->M = c.n_hidden;
+  h->nst = h->N;
+  h->P = h->N + h->M + h->M * h->N;
+  h->B = c.n_chains;
+  h->L = c.chain_length;
+  h->Ns = h->B * h->L;
+  h->passes = (c.passes % 2 == 0) ? c.passes + 1 : c.passes;
+  const bool stale = (c.quirks & NQ_QUIRK_STALE_LAST_SLOT) != 0;
+  h->n_record = stale ? (h->L > 1 ? h->L - 1 : 0) : h->L;
+  h->write_last = (stale && h->L == 1) ? 1 : 0;
+  h->hilb = c.hilbert;
+  h->act = c.activation;
+  h->f64 = c.eval_precision == NQ_EVAL_F64;
+  h->complex_params = true;
+  if ((long)h->Ns * h->M > (1L << 31)) return bad("B*L*M too large");
+
+  nq_status s = NQ_OK;
+  auto step = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && s == NQ_OK) {
+      fprintf(stderr, "nq_create: %s: %s\n", what, cudaGetErrorString(e));
+      s = NQ_ERR_CUDA;
+    }
+  };
+  step(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking), "stream");
+  const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
+  const int P = h->P;
+  step(dalloc(&h->d_master, 2 * (size_t)P), "params");
+  step(dalloc(&h->d_p32, 2 * (size_t)P), "params32");
+  for (int k = 0; k < 3; ++k) step(cudaMalloc(&h->d_tab[k], (size_t)h->N * h->M * csz + 16), "tables");
+  step(dalloc(&h->d_samples, (size_t)h->Ns), "samples");
+  step(dalloc(&h->d_accepted, 1), "accepted");
+  step(dalloc(&h->d_call, 1), "call");
+  step(cudaMalloc(&h->d_logpsi, (size_t)h->Ns * csz), "logpsi");
+  step(cudaMalloc(&h->d_g, (size_t)h->Ns * h->M * csz), "g");
+  step(cudaMalloc(&h->d_eloc, (size_t)h->Ns * csz), "eloc");
+  if (h->f64) step(dalloc(&h->d_g32, (size_t)h->Ns * h->M), "g32");
+  h->force_nblk = rbm_force_nblocks(h->Ns, h->N, h->M, (int)csz);
+  step(dalloc(&h->fb.partial, (size_t)h->force_nblk * 4 * P), "force partial");
+  step(dalloc(&h->fb.partialE, 2 * (size_t)h->force_nblk), "force partialE");
+  step(dalloc(&h->fb.meanO, 2 * (size_t)P), "meanO");
+  step(dalloc(&h->fb.force, 2 * (size_t)P), "force");
+  step(dalloc(&h->fb.meanE, 2), "meanE");
+  step(dalloc(&h->d_stats, 8), "stats");
+  const int rows = 2 * P;
+  const int rp = ((rows + 127) / 128) * 128;
+  // split-K so that the S stage fills the GPU with ~2 waves of tiles
+  {
+    const int nt = (rows + 63) / 64;
+    const int tiles = nt * (nt + 1) / 2;
+    int ks = 1;
+    while (tiles * ks < 2 * 152 && ks < 16 && h->Ns / (ks * 2) >= 256) ks *= 2;
+    h->gram_ksplit = ks;
+  }
+  step(dalloc(&h->d_G, (size_t)rows * rows), "G");
+  step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
+  if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) {
+    h->Ns_pad = ((h->Ns + 127) / 128) * 128;
+    step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
+  }
+  step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
+  step(dalloc(&h->sb.Lf, (size_t)P * P), "Lf");
+  step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
+  step(dalloc(&h->sb.r, 2 * (size_t)P), "r");
+  step(dalloc(&h->sb.rf, (size_t)P), "rf");
+  step(dalloc(&h->sb.status, 1), "status");
+  h->sb.S = h->d_S;
+  step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
+  step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
+  step(cudaMallocHost((void**)&h->h_acc, sizeof(unsigned long long)), "pinned");
+  for (int k = 0; k < 7; ++k) step(cudaEventCreate(&h->ev[k]), "event");
+  if (s == NQ_OK) {
+    step(cudaMemsetAsync(h->d_master, 0, 2 * sizeof(double) * P, h->st), "memset");
+    step(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st), "memset");
+    // sample buffer starts as the state() fill: all sites at local index 0
+    step(cudaMemsetAsync(h->d_samples, 0, sizeof(uint64_t) * h->Ns, h->st), "memset");
+    step(cudaMemsetAsync(h->d_S, 0, 2 * sizeof(double) * P * P, h->st), "memset");
+    if (refresh_params(h) != NQ_OK) s = NQ_ERR_CUDA;
+    step(cudaStreamSynchronize(h->st), "sync");
+  }
+  if (s != NQ_OK) {
+    nq_destroy(h);
+    return s;
+  }
+  *out = h;
+  return NQ_OK;
+}
+
+void nq_destroy(nq_handle* h) {
+  if (!h) return;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  free_op(h);
+  void* bufs[] = {h->d_master, h->d_p32, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
+                  h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
+                  h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE,
+                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_S, h->sb.Lf, h->sb.x, h->sb.r,
+                  h->sb.rf, h->sb.status, h->d_dw};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (h->h_call) cudaFreeHost(h->h_call);
+  if (h->h_stats) cudaFreeHost(h->h_stats);
+  if (h->h_acc) cudaFreeHost(h->h_acc);
+  for (int k = 0; k < 7; ++k)
+    if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+nq_status nq_last_error(const nq_handle* h, char* buf, size_t len) {
+  if (!h || !buf || len == 0) return NQ_ERR_ARG;
+  snprintf(buf, len, "%s", h->err.c_str());
+  return NQ_OK;
+}
+
+int64_t nq_n_params(const nq_handle* h) { return h ? h->P : -1; }
+int64_t nq_kernel_launches(const nq_handle* h) { return h ? h->launches : -1; }
+
+nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype) {
+  if (!h || !flat) return NQ_ERR_ARG;
+  if (n != h->P) return fail(h, NQ_ERR_ARG, "expected %d parameters, got %lld", h->P, (long long)n);
+  std::vector<double> buf(2 * (size_t)h->P, 0.0);
+  if (dtype == NQ_DTYPE_C128) memcpy(buf.data(), flat, buf.size() * sizeof(double));
+  else if (dtype == NQ_DTYPE_C64) {
+    const float* f = (const float*)flat;
+    for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
+  } else return fail(h, NQ_ERR_ARG, "RBM parameters are complex (dtype c64 or c128)");
+  for (double v : buf)
+    if (!std::isfinite(v)) return fail(h, NQ_ERR_NAN, "non-finite parameter");
+  CK(cudaMemcpyAsync(h->d_master, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  nq_status s = refresh_params(h);
+  if (s != NQ_OK) return s;
+  CK(cudaStreamSynchronize(h->st));
+  return NQ_OK;
+}
+
+nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
+  if (!h || !flat) return NQ_ERR_ARG;
+  if (n != h->P) return fail(h, NQ_ERR_ARG, "expected %d parameters, got %lld", h->P, (long long)n);
+  std::vector<double> buf(2 * (size_t)h->P);
+  CK(cudaMemcpyAsync(buf.data(), h->d_master, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (dtype == NQ_DTYPE_C128) memcpy(flat, buf.data(), buf.size() * sizeof(double));
+  else if (dtype == NQ_DTYPE_C64) {
+    float* f = (float*)flat;
+    for (size_t i = 0; i < buf.size(); ++i) f[i] = (float)buf[i];
+  } else return fail(h, NQ_ERR_ARG, "RBM parameters are complex (dtype c64 or c128)");
+  return NQ_OK;
+}
+
+nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
+  if (!h || !t) return NQ_ERR_ARG;
+  if (t->n_ops < 1 || t->n_rows < 1 || t->n_conns < 0) return fail(h, NQ_ERR_ARG, "empty operator");
+  // validate on the host
+  for (int o = 0; o < t->n_ops; ++o) {
+    int k = t->op_n_sites[o];
+    if (k < 1 || k > 8) return fail(h, NQ_ERR_ARG, "operator %d: %d sites (1..8 supported)", o, k);
+    for (int d = 0; d < k; ++d)
+      if (t->op_sites[8 * o + d] < 0 || t->op_sites[8 * o + d] >= h->nst)
+        return fail(h, NQ_ERR_ARG, "operator %d: site out of range", o);
+    if (t->op_row_offset[o] < 0 || t->op_row_offset[o] + (1 << k) > t->n_rows)
+      return fail(h, NQ_ERR_ARG, "operator %d: row offset out of range", o);
+  }
+  for (int r = 0; r < t->n_rows; ++r)
+    if (t->row_conn_offset[r] > t->row_conn_offset[r + 1] || t->row_conn_offset[r] < 0)
+      return fail(h, NQ_ERR_ARG, "row offsets not monotone");
+  if (t->row_conn_offset[t->n_rows] != t->n_conns) return fail(h, NQ_ERR_ARG, "row offsets do not end at n_conns");
+  for (int c = 0; c < t->n_conns; ++c) {
+    int nc = t->conn_n_changes[c];
+    if (nc < 0 || nc > 8) return fail(h, NQ_ERR_ARG, "connection %d: bad change count", c);
+    for (int q = 0; q < nc; ++q) {
+      int s = t->conn_change_site[8 * c + q];
+      int v = t->conn_change_value[8 * c + q];
+      if (s < 0 || s >= h->nst) return fail(h, NQ_ERR_ARG, "connection %d: site out of range", c);
+      bool ok = h->hilb == NQ_HILB_SPIN ? (v == 1 || v == -1) : (v == 0 || v == 1);
+      if (!ok) return fail(h, NQ_ERR_ARG, "connection %d: invalid site value %d", c, v);
+    }
+  }
+  CK(cudaStreamSynchronize(h->st));
+  free_op(h);
+  DevOp d;
+  d.n_ops = t->n_ops; d.n_rows = t->n_rows; d.n_conns = t->n_conns;
+  nq_status s;
+  if ((s = upload(h, t->op_n_sites, t->n_ops, &d.op_n_sites)) != NQ_OK) return s;
+  if ((s = upload(h, t->op_sites, 8 * (size_t)t->n_ops, &d.op_sites)) != NQ_OK) return s;
+  if ((s = upload(h, t->op_row_offset, t->n_ops, &d.op_row_offset)) != NQ_OK) return s;
+  if ((s = upload(h, t->row_conn_offset, (size_t)t->n_rows + 1, &d.row_conn_offset)) != NQ_OK) return s;
+  if ((s = upload(h, t->conn_mel, 2 * (size_t)t->n_conns, &d.conn_mel)) != NQ_OK) return s;
+  if ((s = upload(h, t->conn_n_changes, (size_t)t->n_conns, &d.conn_n_changes)) != NQ_OK) return s;
+  if ((s = upload(h, t->conn_change_site, 8 * (size_t)t->n_conns, &d.conn_change_site)) != NQ_OK) return s;
+  if ((s = upload(h, (const signed char*)t->conn_change_value, 8 * (size_t)t->n_conns, &d.conn_change_value)) != NQ_OK)
+    return s;
+  h->op = d;
+  h->has_op = true;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NQ_OK;
+}
+
+nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out, uint8_t* accept_bits) {
+  if (!h) return NQ_ERR_ARG;
+  unsigned char* d_bits = nullptr;
+  size_t nbits = (size_t)h->B * h->passes * (h->cfg.burn + h->n_record);
+  if (accept_bits) CK(cudaMalloc(&d_bits, nbits));
+  CK(cudaEventRecord(h->ev[0], h->st));
+  nq_status s = stage_sample(h, (uint32_t)call_index, d_bits);
+  if (s != NQ_OK) { if (d_bits) cudaFree(d_bits); return s; }
+  CK(cudaEventRecord(h->ev[1], h->st));
+  CK(cudaMemcpyAsync(h->h_acc, h->d_accepted, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st));
+  if (samples_out) {
+    signed char* d_v = nullptr;
+    CK(cudaMalloc(&d_v, (size_t)h->Ns * h->nst));
+    ++h->launches;
+    CK(launch_unpack_int8(h->d_samples, h->nst, h->Ns, h->hilb, d_v, h->st));
+    CK(cudaMemcpyAsync(samples_out, d_v, (size_t)h->Ns * h->nst, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    cudaFree(d_v);
+  }
+  if (d_bits) {
+    CK(cudaMemcpyAsync(accept_bits, d_bits, nbits, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    cudaFree(d_bits);
+  }
+  CK(cudaStreamSynchronize(h->st));
+  cudaEventElapsedTime(&h->stage_ms[0], h->ev[0], h->ev[1]);
+  return NQ_OK;
+}
+
+nq_status nq_set_samples(nq_handle* h, const int8_t* samples) {
+  if (!h || !samples) return NQ_ERR_ARG;
+  signed char* d_v = nullptr;
+  CK(cudaMalloc(&d_v, (size_t)h->Ns * h->nst));
+  CK(cudaMemcpyAsync(d_v, samples, (size_t)h->Ns * h->nst, cudaMemcpyHostToDevice, h->st));
+  ++h->launches;
+  CK(launch_pack_int8(d_v, h->nst, h->Ns, h->hilb, h->d_samples, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  cudaFree(d_v);
+  return NQ_OK;
+}
+
+static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, double* out, double* grad) {
+  if (!h || !sigma || !out || n < 1) return NQ_ERR_ARG;
+  for (int64_t i = 0; i < n * h->nst; ++i) {
+    int v = sigma[i];
+    bool ok = h->hilb == NQ_HILB_SPIN ? (v == 1 || v == -1) : (v == 0 || v == 1);
+    if (!ok) return fail(h, NQ_ERR_ARG, "invalid site value %d at %lld", v, (long long)i);
+  }
+  const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
+  signed char* d_v = nullptr;
+  uint64_t* d_bits = nullptr;
+  void *d_lp = nullptr, *d_g = nullptr;
+  double* d_out = nullptr;
+  CK(cudaMalloc(&d_v, (size_t)n * h->nst));
+  CK(cudaMalloc(&d_bits, (size_t)n * sizeof(uint64_t)));
+  CK(cudaMalloc(&d_lp, (size_t)n * csz));
+  CK(cudaMalloc(&d_g, (size_t)n * h->M * csz));
+  CK(cudaMemcpyAsync(d_v, sigma, (size_t)n * h->nst, cudaMemcpyHostToDevice, h->st));
+  ++h->launches;
+  CK(launch_pack_int8(d_v, h->nst, n, h->hilb, d_bits, h->st));
+  if (h->f64) CKL(launch_rbm_eval<double>(rbm_dev<double>(h), d_bits, (int)n, nullptr, (cpx<double>*)d_lp, (cpx<double>*)d_g, nullptr, h->st));
+  else CKL(launch_rbm_eval<float>(rbm_dev<float>(h), d_bits, (int)n, nullptr, (cpx<float>*)d_lp, (cpx<float>*)d_g, nullptr, h->st));
+  std::vector<double> lp(2 * n);
+  if (h->f64) CK(cudaMemcpyAsync(lp.data(), d_lp, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  else {
+    std::vector<float> f(2 * n);
+    CK(cudaMemcpyAsync(f.data(), d_lp, 2 * n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int64_t i = 0; i < 2 * n; ++i) lp[i] = f[i];
+  }
+  if (grad) {
+    CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
+    if (h->f64) CKL(launch_rbm_grad_matrix<double>(d_bits, (int)n, h->N, h->M, h->hilb, (cpx<double>*)d_g, d_out, h->st));
+    else CKL(launch_rbm_grad_matrix<float>(d_bits, (int)n, h->N, h->M, h->hilb, (cpx<float>*)d_g, d_out, h->st));
+    CK(cudaMemcpyAsync(grad, d_out, (size_t)2 * h->P * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
+  memcpy(out, lp.data(), 2 * n * sizeof(double));
+  cudaFree(d_v); cudaFree(d_bits); cudaFree(d_lp); cudaFree(d_g);
+  if (d_out) cudaFree(d_out);
+  return NQ_OK;
+}
+
+nq_status nq_logpsi(nq_handle* h, const int8_t* sigma, int64_t n, double* out) {
+  return eval_host_batch(h, sigma, n, out, nullptr);
+}
+
+nq_status nq_logpsi_grad(nq_handle* h, const int8_t* sigma, int64_t n, double* out, double* grad) {
+  return eval_host_batch(h, sigma, n, out, grad);
+}
+
+nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, double* force_out) {
+  if (!h) return NQ_ERR_ARG;
+  if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
+  nq_status s;
+  CK(cudaEventRecord(h->ev[1], h->st));
+  if ((s = stage_eval(h)) != NQ_OK) return s;
+  CK(cudaEventRecord(h->ev[2], h->st));
+  if ((s = stage_force(h)) != NQ_OK) return s;
+  CK(cudaEventRecord(h->ev[3], h->st));
+  if ((s = stage_S(h)) != NQ_OK) return s;
+  CK(cudaEventRecord(h->ev[4], h->st));
+  CK(cudaMemcpyAsync(h->h_stats, h->d_stats, 6 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  cudaEventElapsedTime(&h->stage_ms[1], h->ev[1], h->ev[2]);
+  cudaEventElapsedTime(&h->stage_ms[2], h->ev[2], h->ev[3]);
+  cudaEventElapsedTime(&h->stage_ms[3], h->ev[3], h->ev[4]);
+  fill_measurement(h, stats);
+  const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
+  if (loc_out) {
+    std::vector<char> buf((size_t)h->Ns * csz);
+    CK(cudaMemcpy(buf.data(), h->d_eloc, buf.size(), cudaMemcpyDeviceToHost));
+    if (h->f64) memcpy(loc_out, buf.data(), buf.size());
+    else {
+      const float* f = (const float*)buf.data();
+      for (size_t i = 0; i < 2 * (size_t)h->Ns; ++i) loc_out[i] = f[i];
+    }
+  }
+  if (force_out) {
+    std::vector<double> f(2 * (size_t)h->P);
+    CK(cudaMemcpy(f.data(), h->fb.force, f.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->complex_params) memcpy(force_out, f.data(), f.size() * sizeof(double));
+    else
+      for (int i = 0; i < h->P; ++i) force_out[i] = f[2 * i];
+  }
+  return NQ_OK;
+}
+
+nq_status nq_get_sr_matrix(nq_handle* h, double* s_out) {
+  if (!h || !s_out) return NQ_ERR_ARG;
+  std::vector<double> S(2 * (size_t)h->P * h->P);
+  CK(cudaMemcpyAsync(S.data(), h->d_S, S.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (h->complex_params) memcpy(s_out, S.data(), S.size() * sizeof(double));
+  else
+    for (size_t i = 0; i < (size_t)h->P * h->P; ++i) s_out[i] = S[2 * i];
+  return NQ_OK;
+}
+
+nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0, double b,
+                          double lam_min, int32_t iter, double* dw_out) {
+  if (!h) return NQ_ERR_ARG;
+  if (kind < 0 || kind > 2) return fail(h, NQ_ERR_ARG, "unknown precondition kind %d", kind);
+  double lam = 0.0;
+  if (kind == 1) lam = std::max(lam0 * std::pow(b, (double)iter), lam_min);
+  CK(cudaEventRecord(h->ev[4], h->st));
+  nq_status s = stage_solve(h, kind, eps, lam);
+  if (s != NQ_OK) return s;
+  CK(cudaEventRecord(h->ev[5], h->st));
+  if ((s = check_status_word(h)) != NQ_OK) return s;
+  cudaEventElapsedTime(&h->stage_ms[4], h->ev[4], h->ev[5]);
+  if (dw_out) {
+    std::vector<double> x(2 * (size_t)h->P);
+    CK(cudaMemcpy(x.data(), h->sb.x, x.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->complex_params) memcpy(dw_out, x.data(), x.size() * sizeof(double));
+    else
+      for (int i = 0; i < h->P; ++i) dw_out[i] = x[2 * i];
+  }
+  return NQ_OK;
+}
+
+nq_status nq_update_descent(nq_handle* h, double lr) {
+  if (!h) return NQ_ERR_ARG;
+  CK(cudaEventRecord(h->ev[5], h->st));
+  nq_status s = stage_update(h, lr);
+  if (s != NQ_OK) return s;
+  CK(cudaEventRecord(h->ev[6], h->st));
+  CK(cudaStreamSynchronize(h->st));
+  cudaEventElapsedTime(&h->stage_ms[5], h->ev[5], h->ev[6]);
+  if (h->graph) { /* parameters live on the device; the graph stays valid */ }
+  return NQ_OK;
+}
+
+// Whole iteration; replays a captured graph once built.  The call index
+// reaches the sampler through a pinned host word copied by the first graph
+// node, so one graph serves every iteration.
+nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, nq_measurement* stats) {
+  if (!h) return NQ_ERR_ARG;
+  if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
+  if (h->graph && (h->graph_eps != eps || h->graph_lr != lr)) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  CK(cudaStreamSynchronize(h->st));
+  *h->h_call = (uint32_t)call_index;
+  if (!h->graph) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = h->launches;
+    nq_status s = NQ_OK;
+    cudaError_t ce = cudaMemcpyAsync(h->d_call, h->h_call, sizeof(uint32_t), cudaMemcpyHostToDevice, h->st);
+    if (ce != cudaSuccess) s = fail(h, NQ_ERR_CUDA, "capture memcpy: %s", cudaGetErrorString(ce));
+    if (s == NQ_OK) s = stage_sample(h, 0, nullptr, h->d_call);
+    if (s == NQ_OK) s = stage_eval(h);
+    if (s == NQ_OK) s = stage_force(h);
+    if (s == NQ_OK) s = stage_S(h);
+    if (s == NQ_OK) s = stage_solve(h, 0, eps, 0.0);
+    if (s == NQ_OK) s = stage_update(h, lr);
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    h->graph_kernels = h->launches - before;
+    h->launches = before;
+    if (s != NQ_OK) { if (g) cudaGraphDestroy(g); return s; }
+    CK(e);
+    CK(cudaGraphInstantiate(&h->graph, g, 0));
+    cudaGraphDestroy(g);
+    h->graph_eps = eps;
+    h->graph_lr = lr;
+  }
+  CK(cudaGraphLaunch(h->graph, h->st));
+  h->launches += h->graph_kernels;
+  CK(cudaMemcpyAsync(h->h_stats, h->d_stats, 6 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_acc, h->d_accepted, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  nq_status s = check_status_word(h);
+  if (s != NQ_OK) return s;
+  fill_measurement(h, stats);
+  return NQ_OK;
+}
+
+nq_status nq_stage_times(nq_handle* h, float* ms6) {
+  if (!h || !ms6) return NQ_ERR_ARG;
+  memcpy(ms6, h->stage_ms, sizeof(h->stage_ms));
+  return NQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Kernel launch interfaces shared between the translation units of
+// libnqcuda.  Every launcher returns a cudaError_t and enqueues on `st`.
+#pragma once
+#include "nq_common.cuh"
+
+// Flattened operator on the device (see nq_op_table in include/nqcuda.h).
+struct DevOp {
+  int n_ops = 0, n_rows = 0, n_conns = 0;
+  const int* op_n_sites = nullptr;      // [n_ops]
+  const int* op_sites = nullptr;        // [8*n_ops]
+  const int* op_row_offset = nullptr;   // [n_ops]
+  const int* row_conn_offset = nullptr; // [n_rows+1]
+  const double* conn_mel = nullptr;     // [2*n_conns]
+  const int* conn_n_changes = nullptr;  // [n_conns]
+  const int* conn_change_site = nullptr;// [8*n_conns]
+  const signed char* conn_change_value = nullptr; // [8*n_conns]
+};
+
+// ------------------------------- RBM ------------------------------------
+// Per-(site i, hidden h) tables, index i*M + h, |Δσ| = d (2 spin, 1 Fock):
+//   logcosh:  t0 = cosh(W d), t1 = sinh(W d), t2 = tanh(W d)
+//   softplus: t0 = exp(W d) - 1, t1 = exp(-W d) - 1, t2 = 0
+// With g = f'(θ), the ratio cosh(θ+Δ)/cosh(θ) (resp. (1+e^{θ+Δ})/(1+e^θ))
+// of a single flip with Δ = W dv is t0 + g*sign(dv)*t1 (resp. 1 + g*t0|t1).
+template <typename R> struct RbmDev {
+  int N = 0, M = 0, act = 0, hilb = 0;
+  const cpx<R>* a = nullptr;   // [N]
+  const cpx<R>* b = nullptr;   // [M]
+  const cpx<R>* W = nullptr;   // [M*N] column-major
+  const cpx<R>* t0 = nullptr;  // [N*M]
+  const cpx<R>* t1 = nullptr;
+  const cpx<R>* t2 = nullptr;
+};
+
+cudaError_t launch_rbm_params_from_master(const double* master, int N, int M, float* f32_out,
+                                          cudaStream_t st);
+template <typename R>
+cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2,
+                              cudaStream_t st);
+
+struct SamplerRun {
+  int B = 0, L = 0, burn = 0, passes = 1, n_record = 0, write_last_at_end = 0;
+  uint32_t k0 = 0, k1 = 0, call = 0;
+  const uint32_t* call_ptr = nullptr;          // if set, the call index is read here
+  uint64_t* samples = nullptr;                 // [L][B]
+  unsigned long long* accepted = nullptr;      // scalar counter
+  unsigned char* accept_bits = nullptr;        // nullable [steps][B]
+};
+template <typename R>
+cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st);
+
+// logψ, g = f'(θ) (hidden-major [M][Ns]) and the local estimator on Ns samples.
+template <typename R>
+cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int Ns,
+                            const DevOp* op, cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc,
+                            cudaStream_t st);
+
+// Per-block partial sums of O, E conj(O) and E over sample chunks, then a
+// deterministic FP64 reduction into <O> (meanO) and F.
+struct ForceBufs {
+  double* partial = nullptr;   // [nblk][2*P] complex (O, EO)
+  double* partialE = nullptr;  // [nblk] complex
+  double* meanO = nullptr;     // [P] complex
+  double* force = nullptr;     // [P] complex
+  double* meanE = nullptr;     // complex scalar
+};
+int rbm_force_nblocks(int Ns, int N, int M, int csize);
+template <typename R>
+cudaError_t launch_rbm_force(const RbmDev<R>& net, const uint64_t* samples, int Ns, const cpx<R>* g,
+                             const cpx<R>* eloc, const ForceBufs& fb, cudaStream_t st);
+
+// ------------------------------- SR -------------------------------------
+// Structured O rows for the S accumulation: parameter k of the RBM vector
+// [a (N), b (M), W (M x N)] at sample s is v_j(s), g_h(s), g_h(s) v_j(s).
+struct RbmOSource {
+  int N = 0, M = 0, hilb = 0, Ns = 0;
+  const uint64_t* samples = nullptr;
+  const float2* g = nullptr;       // [M][Ns] (FP32 storage)
+  const double* meanO = nullptr;   // [P] complex
+};
+// G = X X^T over the real rows X = [Re O_c; Im O_c] interleaved (2P x Ns),
+// upper tiles only, FP32 CUDA cores.  G is 2P x 2P row-major.
+cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* partial, int ksplit,
+                             cudaStream_t st);
+// materialise X (2P x Ns_pad, row-major, zero padded) in FP32 for tcgen05
+cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, cudaStream_t st);
+// tcgen05 kind::tf32 SYRK: G = X X^T (upper tiles), split-K partials reduced.
+cudaError_t launch_gram_tc(const float* X, int rows, int Ns_pad, int split3, float* G,
+                           float* partial, int ksplit, cudaStream_t st);
+int gram_tc_supported();
+// S (P x P complex double, full Hermitian) = combine(G)/Ns
+cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_params, double* S,
+                              cudaStream_t st);
+
+// shifted FP32 factorisation + FP64 iterative refinement solve of S x = F.
+struct SolveBufs {
+  double* S = nullptr;        // [P*P] complex (input, untouched)
+  float2* Lf = nullptr;       // [P*P] complex float factor workspace
+  double* x = nullptr;        // [P] complex solution
+  double* r = nullptr;        // [P] complex residual
+  float2* rf = nullptr;       // [P] complex float rhs workspace
+  int* status = nullptr;      // device status word
+};
+cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
+                            double lam, bool real_params, int refine_iters, cudaStream_t st);
+
+// w -= lr * dw on the FP64 master vector (complex: 2P doubles, real: P)
+cudaError_t launch_descent(double* master, const double* dw, long n_doubles, double lr,
+                           cudaStream_t st);
+
+// Measurement statistics (stats.jl:26-50) of a chains x samples matrix stored
+// sample-major (value index s = chain + B*slot); mode 0: complex values,
+// mode 1: |value|^2 (the Liouvillian cost).
+template <typename R>
+cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* out6,
+                         cudaStream_t st);
+
+// bit-packed configurations <-> int8 site values (N x n column-major)
+cudaError_t launch_pack_int8(const signed char* v, int nsites, long n, int hilb, uint64_t* bits,
+                             cudaStream_t st);
+cudaError_t launch_unpack_int8(const uint64_t* bits, int nsites, long n, int hilb, signed char* v,
+                               cudaStream_t st);
+// O matrix (P x n complex double, column-major) for logψ_and_∇logψ!
+template <typename R>
+cudaError_t launch_rbm_grad_matrix(const uint64_t* samples, int n, int N, int M, int hilb,
+                                   const cpx<R>* g, double* out, cudaStream_t st);

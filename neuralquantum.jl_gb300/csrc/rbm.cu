@@ -1,0 +1,606 @@
+// RBM hot path: per-flip tables, the persistent Metropolis sampler with an
+// incremental θ-cache, batched logψ / f'(θ) / local-estimator evaluation and
+// the force partial sums.
+//
+// Reference: src/Networks/ClosedSystems/RBM.jl:40-105, RBMBatched.jl:37-91
+// (network), src/Samplers/Metropolis.jl:101-167 + MCMCRules/LocalRule.jl:19-28
+// (sampler), src/IterativeInterface/Accumulators/AccumulatorObsScalar.jl:52-137
+// (estimator), src/IterativeInterface/Samplers/CostFun/BatchedValSampler.jl:97-115
+// and BaseIterativeSampler.jl:19-26 (centring and force).
+#include "nq_kernels.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// parameters: FP64 master (interleaved complex, reference order a, b, W) ->
+// FP32 working copy
+// ---------------------------------------------------------------------------
+__global__ void master_to_f32_kernel(const double* m, long n, float* out) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)m[i];
+}
+
+template <typename R>
+__global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;   // idx = i*M + h
+  if (idx >= net.N * net.M) return;
+  int i = idx / net.M, h = idx % net.M;
+  // compute in double for accuracy, store as R
+  cpx<R> w = net.W[h + net.M * i];
+  double d = net.hilb == HILB_SPIN ? 2.0 : 1.0;
+  cpx<double> z = mk((double)w.x * d, (double)w.y * d);
+  cpx<double> c0, c1, c2;
+  if (net.act == ACT_LOGCOSH) {
+    c0 = ccoshc(z);
+    c1 = csinhc(z);
+    c2 = act_df<ACT_LOGCOSH>(z);  // tanh(z)
+  } else {
+    cpx<double> ep = cexpc(z), em = cexpc(mk(-z.x, -z.y));
+    c0 = mk(ep.x - 1.0, ep.y);
+    c1 = mk(em.x - 1.0, em.y);
+    c2 = mk(0.0, 0.0);
+  }
+  t0[idx] = mk((R)c0.x, (R)c0.y);
+  t1[idx] = mk((R)c1.x, (R)c1.y);
+  t2[idx] = mk((R)c2.x, (R)c2.y);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent Metropolis sampler.  G lanes advance one chain; lane l owns the
+// hidden units h = l + G*k (k < HPL) and keeps θ_h and g_h = f'(θ_h) in
+// registers.  A proposal flipping site i costs HPL complex FMAs per lane
+// (ratio t0 + g*t1 per unit) plus a log2(G)-step shuffle reduction; an
+// accepted flip updates θ additively and g by the Möbius map of the
+// single-flip tables.  g is recomputed from θ at the end of every sweep, so
+// rounding drift is bounded by one sweep.
+// ---------------------------------------------------------------------------
+template <typename R, int G, int HPL, int ACT>
+__global__ void __launch_bounds__(256)
+rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = net.N, M = net.M;
+  cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* s_t1 = s_t0 + N * M;
+  cpx<R>* s_t2 = s_t1 + N * M;
+  R* s_are = reinterpret_cast<R*>(s_t2 + N * M);      // Re a_i
+  for (int k = threadIdx.x; k < N * M; k += blockDim.x) {
+    s_t0[k] = net.t0[k];
+    s_t1[k] = net.t1[k];
+    if (ACT == ACT_LOGCOSH) s_t2[k] = net.t2[k];
+  }
+  for (int k = threadIdx.x; k < N; k += blockDim.x) s_are[k] = net.a[k].x;
+  __syncthreads();
+
+  const int lane = threadIdx.x % G;
+  const int chain_raw = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const bool active = chain_raw < run.B;
+  const int chain = active ? chain_raw : run.B - 1;
+  const int hilb = net.hilb;
+  if (run.call_ptr) run.call = *run.call_ptr;
+
+  // random initial configuration (rand!, HomogeneousSpin.jl:130-135)
+  uint64_t bits = 0;
+  for (int q = 0; q < N; q += 4) {
+    u32x4 w = philox4x32_10((uint32_t)(q >> 2), run.call, (uint32_t)chain, TAG_INIT, run.k0, run.k1);
+    uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (q + k < N && (ws[k] >> 31)) bits |= 1ull << (q + k);
+  }
+
+  cpx<R> th[HPL], g[HPL];
+  // θ = b + W v
+#pragma unroll
+  for (int k = 0; k < HPL; ++k) {
+    int h = lane + G * k;
+    th[k] = mk(R(0), R(0));
+    g[k] = mk(R(0), R(0));
+    if (h < M) {
+      cpx<R> t = net.b[h];
+      for (int j = 0; j < N; ++j) {
+        R v = site_value<R>(bits, j, hilb);
+        cpx<R> w = net.W[h + M * j];
+        t.x += w.x * v;
+        t.y += w.y * v;
+      }
+      th[k] = t;
+      g[k] = act_df<ACT>(t);
+    }
+  }
+
+  unsigned long long naccept = 0;
+  const int nsweeps = run.burn + run.n_record;
+  uint32_t t = 0;
+  for (int sweep = 0; sweep < nsweeps; ++sweep) {
+    for (int pass = 0; pass < run.passes; ++pass, ++t) {
+      u32x4 r = philox4x32_10(t, run.call, (uint32_t)chain, TAG_MH, run.k0, run.k1);
+      const int i = (int)uniform_site(r.x, (uint32_t)N);
+      const R u = (R)uniform24(r.y);
+      const int bit = (int)((bits >> i) & 1ull);
+      R dv;
+      if (hilb == HILB_SPIN) dv = bit ? R(-2) : R(2);
+      else dv = bit ? R(-1) : R(1);
+      const bool pos = dv > 0;
+      R prod = R(1);
+#pragma unroll
+      for (int k = 0; k < HPL; ++k) {
+        int h = lane + G * k;
+        if (h < M) {
+          cpx<R> rr;
+          if (ACT == ACT_LOGCOSH) {
+            cpx<R> c1 = s_t1[i * M + h];
+            if (!pos) c1 = mk(-c1.x, -c1.y);
+            rr = cfma(g[k], c1, s_t0[i * M + h]);
+          } else {
+            cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
+            rr = cfma(g[k], bb, mk(R(1), R(0)));
+          }
+          prod *= abs2c(rr);
+        }
+      }
+      R lsum = r_log(prod);
+#pragma unroll
+      for (int off = G / 2; off > 0; off >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+      const R logA = R(2) * s_are[i] * dv + lsum;
+      const bool acc = (logA >= R(0)) || (u < r_exp(logA));
+      if (acc) {
+#pragma unroll
+        for (int k = 0; k < HPL; ++k) {
+          int h = lane + G * k;
+          if (h < M) {
+            cpx<R> w = net.W[h + M * i];
+            th[k].x += w.x * dv;
+            th[k].y += w.y * dv;
+            if (ACT == ACT_LOGCOSH) {
+              cpx<R> tau = s_t2[i * M + h];
+              if (!pos) tau = mk(-tau.x, -tau.y);
+              g[k] = divc(g[k] + tau, cfma(g[k], tau, mk(R(1), R(0))));
+            } else {
+              cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
+              cpx<R> num = g[k] * mk(R(1) + bb.x, bb.y);
+              g[k] = divc(num, cfma(g[k], bb, mk(R(1), R(0))));
+            }
+          }
+        }
+        bits ^= 1ull << i;
+        ++naccept;
+      }
+      if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = acc ? 1 : 0;
+    }
+    // end of sweep: record and resynchronise g with θ
+    const int slot = sweep - run.burn;
+    if (slot >= 0 && active && lane == 0) run.samples[(size_t)slot * run.B + chain] = bits;
+#pragma unroll
+    for (int k = 0; k < HPL; ++k)
+      if (lane + G * k < M) g[k] = act_df<ACT>(th[k]);
+  }
+  if (run.write_last_at_end && active && lane == 0) run.samples[chain] = bits;
+  if (active && lane == 0) atomicAdd(run.accepted, naccept);
+}
+
+// ---------------------------------------------------------------------------
+// Batched evaluation, one thread per sample: θ = Wσ + b, logψ = aᵀσ + Σ f(θ),
+// g = f'(θ) and, if an operator is given, the local estimator
+//   E_loc(σ) = Σ_diag mel + Σ_{σ'≠σ} mel ψ(σ')/ψ(σ)
+// with ψ(σ')/ψ(σ) = exp(aᵀΔσ) Π_h [t0 + g t1] for single flips (table path)
+// and exp(aᵀΔσ) Π_h [cosh Δθ + g sinh Δθ] (softplus: 1 + g (e^Δθ - 1)) for
+// multi-site changes.  Zero matrix elements are skipped
+// (AccumulatorObsScalar.jl:92).
+// ---------------------------------------------------------------------------
+template <typename R, int ACT>
+__global__ void __launch_bounds__(128)
+rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, DevOp op,
+                int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
+                cpx<R>* __restrict__ eloc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = net.N, M = net.M, T = blockDim.x;
+  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(smem_raw);     // [M*N]
+  cpx<R>* s_b = s_W + M * N;                              // [M]
+  cpx<R>* s_a = s_b + M;                                  // [N]
+  cpx<R>* s_g = s_a + N;                                  // [M][T]
+  cpx<R>* s_t0 = s_g + (size_t)M * T;                     // [N*M] (if has_op)
+  cpx<R>* s_t1 = s_t0 + (has_op ? N * M : 0);
+  for (int k = threadIdx.x; k < M * N; k += T) s_W[k] = net.W[k];
+  for (int k = threadIdx.x; k < M; k += T) s_b[k] = net.b[k];
+  for (int k = threadIdx.x; k < N; k += T) s_a[k] = net.a[k];
+  if (has_op)
+    for (int k = threadIdx.x; k < N * M; k += T) { s_t0[k] = net.t0[k]; s_t1[k] = net.t1[k]; }
+  __syncthreads();
+  const int s = blockIdx.x * T + threadIdx.x;
+  if (s >= Ns) return;
+  const int hilb = net.hilb;
+  const uint64_t bits = samples[s];
+
+  cpx<R> lp = mk(R(0), R(0));
+  for (int j = 0; j < N; ++j) {
+    R v = site_value<R>(bits, j, hilb);
+    lp.x += s_a[j].x * v;
+    lp.y += s_a[j].y * v;
+  }
+  for (int h = 0; h < M; ++h) {
+    cpx<R> th = s_b[h];
+    for (int j = 0; j < N; ++j) {
+      R v = site_value<R>(bits, j, hilb);
+      th.x += s_W[h + M * j].x * v;
+      th.y += s_W[h + M * j].y * v;
+    }
+    lp = lp + act_f<ACT>(th);
+    cpx<R> gh = act_df<ACT>(th);
+    s_g[h * T + threadIdx.x] = gh;
+    if (gout) gout[(size_t)h * Ns + s] = gh;
+  }
+  logpsi[s] = lp;
+  if (!has_op) return;
+
+  const R dmag = hilb == HILB_SPIN ? R(2) : R(1);
+  cpx<R> E = mk(R(0), R(0));
+  for (int o = 0; o < op.n_ops; ++o) {
+    const int ns_o = __ldg(op.op_n_sites + o);
+    int r = 0;
+    for (int d = 0; d < ns_o; ++d) {
+      int site = __ldg(op.op_sites + 8 * o + d);
+      r |= (int)((bits >> site) & 1ull) << d;
+    }
+    const int row = __ldg(op.op_row_offset + o) + r;
+    const int c0 = __ldg(op.row_conn_offset + row), c1 = __ldg(op.row_conn_offset + row + 1);
+    for (int c = c0; c < c1; ++c) {
+      const double mre = __ldg(op.conn_mel + 2 * c), mim = __ldg(op.conn_mel + 2 * c + 1);
+      if (mre == 0.0 && mim == 0.0) continue;
+      const cpx<R> mel = mk((R)mre, (R)mim);
+      const int nch = __ldg(op.conn_n_changes + c);
+      if (nch == 0) { E = E + mel; continue; }
+      // exp(aᵀΔσ)
+      cpx<R> aexp = mk(R(0), R(0));
+      int i1 = -1; R dv1 = 0;
+      for (int q = 0; q < nch; ++q) {
+        int site = __ldg(op.conn_change_site + 8 * c + q);
+        R nv = (R)__ldg(op.conn_change_value + 8 * c + q);
+        R dv = nv - site_value<R>(bits, site, hilb);
+        aexp.x += s_a[site].x * dv;
+        aexp.y += s_a[site].y * dv;
+        i1 = site; dv1 = dv;
+      }
+      cpx<R> prod = mk(R(1), R(0));
+      R logscale = R(0);
+      if (nch == 1) {
+        const bool pos = dv1 > 0;
+        for (int h = 0; h < M; ++h) {
+          cpx<R> gh = s_g[h * T + threadIdx.x];
+          cpx<R> rr;
+          if (ACT == ACT_LOGCOSH) {
+            cpx<R> t1 = s_t1[i1 * M + h];
+            if (!pos) t1 = mk(-t1.x, -t1.y);
+            rr = cfma(gh, t1, s_t0[i1 * M + h]);
+          } else {
+            cpx<R> bb = pos ? s_t0[i1 * M + h] : s_t1[i1 * M + h];
+            rr = cfma(gh, bb, mk(R(1), R(0)));
+          }
+          prod = prod * rr;
+          R m2 = abs2c(prod);
+          if (m2 > R(1e20) || m2 < R(1e-20)) {
+            R m = sqrt(m2);
+            logscale += r_log(m);
+            prod = (R(1) / m) * prod;
+          }
+        }
+      } else {
+        for (int h = 0; h < M; ++h) {
+          cpx<R> dth = mk(R(0), R(0));
+          for (int q = 0; q < nch; ++q) {
+            int site = __ldg(op.conn_change_site + 8 * c + q);
+            R nv = (R)__ldg(op.conn_change_value + 8 * c + q);
+            R dv = nv - site_value<R>(bits, site, hilb);
+            cpx<R> w = s_W[h + M * site];
+            dth.x += w.x * dv;
+            dth.y += w.y * dv;
+          }
+          cpx<R> gh = s_g[h * T + threadIdx.x];
+          cpx<R> rr;
+          if (ACT == ACT_LOGCOSH) rr = cfma(gh, csinhc(dth), ccoshc(dth));
+          else {
+            cpx<R> e = cexpc(dth);
+            rr = cfma(gh, mk(e.x - R(1), e.y), mk(R(1), R(0)));
+          }
+          prod = prod * rr;
+          R m2 = abs2c(prod);
+          if (m2 > R(1e20) || m2 < R(1e-20)) {
+            R m = sqrt(m2);
+            logscale += r_log(m);
+            prod = (R(1) / m) * prod;
+          }
+        }
+      }
+      (void)dmag;
+      cpx<R> ea = cexpc(mk(aexp.x + logscale, aexp.y));
+      E = E + mel * (ea * prod);
+    }
+  }
+  eloc[s] = E;
+}
+
+// ---------------------------------------------------------------------------
+// Force partial sums over chunks of CH samples (one block per chunk):
+//   O_s  = [v(s), g(s), g(s) v(s)ᵀ]          (P = N + M + M N entries)
+//   ΣO, Σ E conj(O), Σ E
+// accumulated in FP32 with Kahan compensation inside a chunk, emitted in FP64.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256)
+rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ samples, int Ns,
+                         const cpx<R>* __restrict__ g, const cpx<R>* __restrict__ eloc, int CH,
+                         double* __restrict__ partial, double* __restrict__ partialE) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int P = N + M + M * N;
+  const int s0 = blockIdx.x * CH;
+  const int n = min(CH, Ns - s0);
+  cpx<R>* s_g = reinterpret_cast<cpx<R>*>(smem_raw);   // [M][CH]
+  cpx<R>* s_e = s_g + (size_t)M * CH;                  // [CH]
+  R* s_v = reinterpret_cast<R*>(s_e + CH);             // [N][CH]
+  for (int k = threadIdx.x; k < M * CH; k += blockDim.x) {
+    int h = k / CH, t = k % CH;
+    s_g[k] = t < n ? g[(size_t)h * Ns + s0 + t] : mk(R(0), R(0));
+  }
+  for (int t = threadIdx.x; t < CH; t += blockDim.x) {
+    uint64_t bits = t < n ? samples[s0 + t] : 0;
+    s_e[t] = t < n ? eloc[s0 + t] : mk(R(0), R(0));
+    for (int j = 0; j < N; ++j) s_v[j * CH + t] = t < n ? site_value<R>(bits, j, hilb) : R(0);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    cpx<R> so = mk(R(0), R(0)), co = mk(R(0), R(0));   // Kahan sum of O
+    cpx<R> se = mk(R(0), R(0));
+    int kind, h = 0, j = 0;
+    if (p < N) { kind = 0; j = p; }
+    else if (p < N + M) { kind = 1; h = p - N; }
+    else { kind = 2; h = (p - N - M) % M; j = (p - N - M) / M; }
+    for (int t = 0; t < n; ++t) {
+      cpx<R> o;
+      if (kind == 0) o = mk(s_v[j * CH + t], R(0));
+      else if (kind == 1) o = s_g[h * CH + t];
+      else o = s_v[j * CH + t] * s_g[h * CH + t];
+      // Kahan
+      cpx<R> y = o - co;
+      cpx<R> tt = so + y;
+      co = (tt - so) - y;
+      so = tt;
+      se = se + s_e[t] * conjc(o);
+    }
+    double* dst = partial + (size_t)blockIdx.x * 4 * P;
+    dst[2 * p] = (double)so.x;
+    dst[2 * p + 1] = (double)so.y;
+    dst[2 * P + 2 * p] = (double)se.x;
+    dst[2 * P + 2 * p + 1] = (double)se.y;
+  }
+  if (threadIdx.x == 0) {
+    double ex = 0, ey = 0;
+    for (int t = 0; t < n; ++t) { ex += (double)s_e[t].x; ey += (double)s_e[t].y; }
+    partialE[2 * blockIdx.x] = ex;
+    partialE[2 * blockIdx.x + 1] = ey;
+  }
+}
+
+// F = ΣE conj(O)/Ns - <E> conj(<O>),  <O> = ΣO/Ns   (FP64, fixed order)
+__global__ void force_reduce_kernel(int P, int nblk, int Ns, const double* __restrict__ partial,
+                                    const double* __restrict__ partialE, double* meanO,
+                                    double* force, double* meanE) {
+  __shared__ double sE[2];
+  if (threadIdx.x == 0) {
+    double ex = 0, ey = 0;
+    for (int b = 0; b < nblk; ++b) { ex += partialE[2 * b]; ey += partialE[2 * b + 1]; }
+    sE[0] = ex / Ns; sE[1] = ey / Ns;
+    if (blockIdx.x == 0) { meanE[0] = sE[0]; meanE[1] = sE[1]; }
+  }
+  __syncthreads();
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double ox = 0, oy = 0, fx = 0, fy = 0;
+  for (int b = 0; b < nblk; ++b) {
+    const double* src = partial + (size_t)b * 4 * P;
+    ox += src[2 * p]; oy += src[2 * p + 1];
+    fx += src[2 * P + 2 * p]; fy += src[2 * P + 2 * p + 1];
+  }
+  ox /= Ns; oy /= Ns; fx /= Ns; fy /= Ns;
+  meanO[2 * p] = ox; meanO[2 * p + 1] = oy;
+  // - <E> conj(<O>)
+  fx -= sE[0] * ox + sE[1] * oy;
+  fy -= sE[1] * ox - sE[0] * oy;
+  force[2 * p] = fx; force[2 * p + 1] = fy;
+}
+
+template <typename R>
+__global__ void rbm_grad_matrix_kernel(const uint64_t* samples, int n, int N, int M, int hilb,
+                                       const cpx<R>* g, double* out) {
+  const int P = N + M + M * N;
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)P * n) return;
+  int s = (int)(idx / P), p = (int)(idx % P);
+  uint64_t bits = samples[s];
+  cpx<R> o;
+  if (p < N) o = mk(site_value<R>(bits, p, hilb), R(0));
+  else if (p < N + M) o = g[(size_t)(p - N) * n + s];
+  else {
+    int q = p - N - M, h = q % M, j = q / M;
+    o = site_value<R>(bits, j, hilb) * g[(size_t)h * n + s];
+  }
+  out[2 * idx] = (double)o.x;
+  out[2 * idx + 1] = (double)o.y;
+}
+
+__global__ void pack_kernel(const signed char* v, int nsites, long n, int hilb, uint64_t* bits) {
+  long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  uint64_t b = 0;
+  for (int j = 0; j < nsites; ++j) {
+    int x = v[s * nsites + j];
+    int bit = hilb == HILB_SPIN ? (x > 0) : (x != 0);
+    b |= (uint64_t)bit << j;
+  }
+  bits[s] = b;
+}
+
+__global__ void unpack_kernel(const uint64_t* bits, int nsites, long n, int hilb, signed char* v) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= n * nsites) return;
+  long s = idx / nsites;
+  int j = (int)(idx % nsites);
+  int bit = (int)((bits[s] >> j) & 1ull);
+  v[idx] = (signed char)(hilb == HILB_SPIN ? 2 * bit - 1 : bit);
+}
+
+}  // namespace
+
+// ------------------------------- launchers ---------------------------------
+
+cudaError_t launch_rbm_params_from_master(const double* master, int N, int M, float* f32_out,
+                                          cudaStream_t st) {
+  long n = 2L * (N + M + (long)M * N);
+  master_to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(master, n, f32_out);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2,
+                              cudaStream_t st) {
+  int n = net.N * net.M;
+  rbm_tables_kernel<R><<<(n + 127) / 128, 128, 0, st>>>(net, t0, t1, t2);
+  return cudaGetLastError();
+}
+
+template <typename R, int G, int HPL, int ACT>
+static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
+  const int threads = 256;
+  const int chains_per_block = threads / G;
+  const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
+  size_t smem = (size_t)3 * net.N * net.M * sizeof(cpx<R>) + net.N * sizeof(R);
+  auto kern = rbm_sampler_kernel<R, G, HPL, ACT>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<blocks, threads, smem, st>>>(net, run);
+  return cudaGetLastError();
+}
+
+template <typename R, int G, int ACT>
+static cudaError_t sampler_hpl(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
+  const int hpl = (net.M + G - 1) / G;
+  switch (hpl) {
+    case 1: return sampler_inst<R, G, 1, ACT>(net, run, st);
+    case 2: return sampler_inst<R, G, 2, ACT>(net, run, st);
+    case 3: return sampler_inst<R, G, 3, ACT>(net, run, st);
+    case 4: return sampler_inst<R, G, 4, ACT>(net, run, st);
+    case 5: return sampler_inst<R, G, 5, ACT>(net, run, st);
+    case 6: return sampler_inst<R, G, 6, ACT>(net, run, st);
+    case 7: return sampler_inst<R, G, 7, ACT>(net, run, st);
+    case 8: return sampler_inst<R, G, 8, ACT>(net, run, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
+  if (net.N > 64 || net.M > 256) return cudaErrorInvalidValue;
+  const bool small = net.M <= 64;
+  if (net.act == ACT_LOGCOSH)
+    return small ? sampler_hpl<R, 8, ACT_LOGCOSH>(net, run, st) : sampler_hpl<R, 32, ACT_LOGCOSH>(net, run, st);
+  return small ? sampler_hpl<R, 8, ACT_SOFTPLUS>(net, run, st) : sampler_hpl<R, 32, ACT_SOFTPLUS>(net, run, st);
+}
+
+static int eval_threads(int M, size_t csize) {
+  int T = 128;
+  while (T > 32 && (size_t)M * T * csize > 96 * 1024) T /= 2;
+  return T;
+}
+
+template <typename R>
+cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int Ns, const DevOp* op,
+                            cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc, cudaStream_t st) {
+  const int T = eval_threads(net.M, sizeof(cpx<R>));
+  const int has_op = op != nullptr && eloc != nullptr;
+  size_t smem = ((size_t)net.M * net.N + net.M + net.N + (size_t)net.M * T +
+                 (has_op ? 2 * (size_t)net.N * net.M : 0)) * sizeof(cpx<R>);
+  DevOp dop;
+  if (has_op) dop = *op;
+  const int blocks = (Ns + T - 1) / T;
+  if (net.act == ACT_LOGCOSH) {
+    auto kern = rbm_eval_kernel<R, ACT_LOGCOSH>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<blocks, T, smem, st>>>(net, samples, Ns, dop, has_op, logpsi, g, eloc);
+  } else {
+    auto kern = rbm_eval_kernel<R, ACT_SOFTPLUS>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<blocks, T, smem, st>>>(net, samples, Ns, dop, has_op, logpsi, g, eloc);
+  }
+  return cudaGetLastError();
+}
+
+static int force_chunk(int N, int M, int csize) {
+  int CH = 256;
+  while (CH > 32 && ((size_t)(M + 1) * CH * csize + (size_t)N * CH * (csize / 2)) > 64 * 1024) CH /= 2;
+  return CH;
+}
+
+int rbm_force_nblocks(int Ns, int N, int M, int csize) {
+  int CH = force_chunk(N, M, csize);
+  return (Ns + CH - 1) / CH;
+}
+
+template <typename R>
+cudaError_t launch_rbm_force(const RbmDev<R>& net, const uint64_t* samples, int Ns, const cpx<R>* g,
+                             const cpx<R>* eloc, const ForceBufs& fb, cudaStream_t st) {
+  const int CH = force_chunk(net.N, net.M, (int)sizeof(cpx<R>));
+  const int nblk = (Ns + CH - 1) / CH;
+  size_t smem = ((size_t)net.M * CH + CH) * sizeof(cpx<R>) + (size_t)net.N * CH * sizeof(R);
+  auto kern = rbm_force_partial_kernel<R>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<nblk, 256, smem, st>>>(net.N, net.M, net.hilb, samples, Ns, g, eloc, CH, fb.partial,
+                                fb.partialE);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int P = net.N + net.M + net.M * net.N;
+  force_reduce_kernel<<<(P + 127) / 128, 128, 0, st>>>(P, nblk, Ns, fb.partial, fb.partialE,
+                                                        fb.meanO, fb.force, fb.meanE);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_rbm_grad_matrix(const uint64_t* samples, int n, int N, int M, int hilb,
+                                   const cpx<R>* g, double* out, cudaStream_t st) {
+  long tot = (long)(N + M + M * N) * n;
+  rbm_grad_matrix_kernel<R><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(samples, n, N, M, hilb, g, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_int8(const signed char* v, int nsites, long n, int hilb, uint64_t* bits,
+                             cudaStream_t st) {
+  pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(v, nsites, n, hilb, bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_int8(const uint64_t* bits, int nsites, long n, int hilb, signed char* v,
+                               cudaStream_t st) {
+  long tot = n * nsites;
+  unpack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(bits, nsites, n, hilb, v);
+  return cudaGetLastError();
+}
+
+// explicit instantiations
+template cudaError_t launch_rbm_tables<float>(const RbmDev<float>&, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
+template cudaError_t launch_rbm_tables<double>(const RbmDev<double>&, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
+template cudaError_t launch_rbm_sampler<float>(const RbmDev<float>&, const SamplerRun&, cudaStream_t);
+template cudaError_t launch_rbm_sampler<double>(const RbmDev<double>&, const SamplerRun&, cudaStream_t);
+template cudaError_t launch_rbm_eval<float>(const RbmDev<float>&, const uint64_t*, int, const DevOp*, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
+template cudaError_t launch_rbm_eval<double>(const RbmDev<double>&, const uint64_t*, int, const DevOp*, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
+template cudaError_t launch_rbm_force<float>(const RbmDev<float>&, const uint64_t*, int, const cpx<float>*, const cpx<float>*, const ForceBufs&, cudaStream_t);
+template cudaError_t launch_rbm_force<double>(const RbmDev<double>&, const uint64_t*, int, const cpx<double>*, const cpx<double>*, const ForceBufs&, cudaStream_t);
+template cudaError_t launch_rbm_grad_matrix<float>(const uint64_t*, int, int, int, int, const cpx<float>*, double*, cudaStream_t);
+template cudaError_t launch_rbm_grad_matrix<double>(const uint64_t*, int, int, int, int, const cpx<double>*, double*, cudaStream_t);

@@ -1,0 +1,514 @@
+// Stochastic reconfiguration: the S = O_c O_c† accumulation (FP32 CUDA-core
+// variant and the X materialisation for the tcgen05 variant), assembly of the
+// Hermitian S, the diagonally shifted solve (FP32 blocked Cholesky with FP64
+// iterative refinement, so the returned Δw solves the FP64 system), the
+// Descent update and the Measurement statistics.
+//
+// Reference: src/Algorithms/SR/SRDirect.jl:26-90 (S, F, shift, Cholesky),
+// src/Optimisers/apply.jl:25-32 + rules.jl:15-17 (Descent),
+// src/utils/stats.jl:26-50 (Measurement).
+#include "nq_kernels.cuh"
+
+namespace {
+
+// value of real row `row` of X = [Re O_c; Im O_c] (interleaved) at sample s
+__device__ __forceinline__ float x_value(const RbmOSource& src, int row, int s, uint64_t bits) {
+  const int N = src.N, M = src.M;
+  const int k = row >> 1, part = row & 1;
+  float ox, oy;
+  if (k < N) { ox = site_valuef(bits, k, src.hilb); oy = 0.f; }
+  else if (k < N + M) { float2 g = src.g[(size_t)(k - N) * src.Ns + s]; ox = g.x; oy = g.y; }
+  else {
+    int q = k - N - M, h = q % M, j = q / M;
+    float2 g = src.g[(size_t)h * src.Ns + s];
+    float v = site_valuef(bits, j, src.hilb);
+    ox = g.x * v; oy = g.y * v;
+  }
+  ox -= (float)src.meanO[2 * k];
+  oy -= (float)src.meanO[2 * k + 1];
+  return part ? oy : ox;
+}
+
+__device__ __forceinline__ void tile_of(int t, int nt, int* ti, int* tj) {
+  // enumerate upper tiles row by row: (0,0),(0,1),...,(0,nt-1),(1,1),...
+  int i = 0, rem = t;
+  while (rem >= nt - i) { rem -= nt - i; ++i; }
+  *ti = i; *tj = i + rem;
+}
+
+// 64x64 output tile per block, 16x16 threads with 4x4 micro tiles, K chunks of
+// 16 samples generated on the fly from (σ, g, <O>).
+constexpr int GT = 64, GK = 16;
+__global__ void __launch_bounds__(256)
+gram_simt_kernel(RbmOSource src, int rows, int nt, int ksplit, float* __restrict__ partial) {
+  __shared__ float As[GK][GT + 4];
+  __shared__ float Bs[GK][GT + 4];
+  int ti, tj;
+  tile_of(blockIdx.x, nt, &ti, &tj);
+  const int kz = blockIdx.y;
+  const int per = (src.Ns + ksplit - 1) / ksplit;
+  const int kb = kz * per, ke = min(src.Ns, kb + per);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  float acc[4][4] = {};
+  for (int k0 = kb; k0 < ke; k0 += GK) {
+    // generate: thread -> (sample t = tid % 16, rows tid/16 + 16 q)
+    {
+      const int t = threadIdx.x % GK;
+      const int s = k0 + t;
+      const bool ok = s < ke;
+      const uint64_t bits = ok ? src.samples[s] : 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        int r = threadIdx.x / GK + 16 * q;
+        int ra = ti * GT + r, rb = tj * GT + r;
+        As[t][r] = (ok && ra < rows) ? x_value(src, ra, s, bits) : 0.f;
+        Bs[t][r] = (ok && rb < rows) ? x_value(src, rb, s, bits) : 0.f;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { a[i] = As[kk][ty * 4 + i]; b[i] = Bs[kk][tx * 4 + i]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  // partial layout: [ksplit][rows_pad][rows_pad] with rows_pad = nt*64
+  const int rp = nt * GT;
+  float* dst = partial + (size_t)kz * rp * rp;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      dst[(size_t)(ti * GT + ty * 4 + i) * rp + tj * GT + tx * 4 + j] = acc[i][j];
+}
+
+// sum split-K partials of the upper tiles into G (rows x rows, row-major)
+__global__ void gram_reduce_kernel(const float* __restrict__ partial, int rows, int rp, int tile,
+                                   int ksplit, float* __restrict__ G) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)rows * rows) return;
+  int a = (int)(idx / rows), b = (int)(idx % rows);
+  if (a / tile > b / tile) return;   // lower tiles were not computed
+  float s = 0.f;
+  for (int z = 0; z < ksplit; ++z) s += partial[(size_t)z * rp * rp + (size_t)a * rp + b];
+  G[idx] = s;
+}
+
+__global__ void build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)rows * Ns_pad) return;
+  int row = (int)(idx / Ns_pad), s = (int)(idx % Ns_pad);
+  float v = 0.f;
+  if (s < src.Ns) v = x_value(src, row, s, src.samples[s]);
+  X[idx] = v;
+}
+
+__device__ __forceinline__ float gsym(const float* G, int rows, int a, int b) {
+  return a <= b ? G[(size_t)a * rows + b] : G[(size_t)b * rows + a];
+}
+
+// S[k + P l] (column-major, complex double):
+//   Re = (G[2k][2l] + G[2k+1][2l+1]) / Ns,  Im = (G[2k][2l+1] - G[2k+1][2l]) / Ns
+// which is conj(O_c O_c†)/Ns (SRDirect.jl:41-43); real parameters keep Re only.
+__global__ void assemble_S_kernel(const float* __restrict__ G, int P, double inv_ns, int real_params,
+                                  double* __restrict__ S) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)P * P) return;
+  int k = (int)(idx % P), l = (int)(idx / P);
+  const int rows = 2 * P;
+  double re = ((double)gsym(G, rows, 2 * k, 2 * l) + (double)gsym(G, rows, 2 * k + 1, 2 * l + 1)) * inv_ns;
+  double im = real_params ? 0.0
+                          : ((double)gsym(G, rows, 2 * k, 2 * l + 1) - (double)gsym(G, rows, 2 * k + 1, 2 * l)) * inv_ns;
+  S[2 * idx] = re;
+  S[2 * idx + 1] = im;
+}
+
+// ---------------------------------------------------------------------------
+// Shifted copy into the FP32 factor workspace (lower triangle, column-major).
+// kind 0: S_ii += eps;  kind 1: S_ii += lam * S_ii;  kind 2: none.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double diag_shift(const double* S, int P, int i, int kind, double eps,
+                                             double lam) {
+  if (kind == 0) return eps;
+  if (kind == 1) return lam * S[2 * ((size_t)i + (size_t)P * i)];
+  return 0.0;
+}
+
+__global__ void shift_copy_kernel(const double* __restrict__ S, int P, int kind, double eps,
+                                  double lam, float2* __restrict__ Lf) {
+  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)P * P) return;
+  int i = (int)(idx % P), j = (int)(idx / P);
+  double re = S[2 * idx], im = S[2 * idx + 1];
+  if (i == j) { re += diag_shift(S, P, i, kind, eps, lam); im = 0.0; }
+  Lf[idx] = make_float2((float)re, (float)im);
+}
+
+constexpr int CB = 32;   // Cholesky block size
+
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 f2mulconj(float2 a, float2 b) {  // a * conj(b)
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+// factor the nb x nb diagonal block at k0 in shared memory
+__global__ void __launch_bounds__(1024) potrf_diag_kernel(float2* A, int P, int k0, int nb, int* status) {
+  __shared__ float2 D[CB][CB + 1];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    int i = e % nb, j = e / nb;
+    D[i][j] = A[(size_t)(k0 + i) + (size_t)P * (k0 + j)];
+  }
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    __shared__ float piv;
+    if (tid == 0) {
+      float d = D[j][j].x;
+      if (!(d > 0.f)) { atomicExch(status, 1); d = 1.0f; }
+      piv = sqrtf(d);
+      D[j][j] = make_float2(piv, 0.f);
+    }
+    __syncthreads();
+    const float inv = 1.0f / piv;
+    for (int i = j + 1 + tid; i < nb; i += blockDim.x) D[i][j] = make_float2(D[i][j].x * inv, D[i][j].y * inv);
+    __syncthreads();
+    // trailing update of the lower part: D[i][c] -= D[i][j] conj(D[c][j]), i >= c > j
+    const int m = nb - j - 1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      int i = j + 1 + e % m, c = j + 1 + e / m;
+      if (i >= c) {
+        float2 p = f2mulconj(D[i][j], D[c][j]);
+        D[i][c].x -= p.x;
+        D[i][c].y -= p.y;
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    int i = e % nb, j = e / nb;
+    if (i >= j) A[(size_t)(k0 + i) + (size_t)P * (k0 + j)] = D[i][j];
+  }
+}
+
+// rows i >= k0+nb of the panel: X L_kkᴴ = A_ik  (forward substitution per row)
+__global__ void __launch_bounds__(128) trsm_panel_kernel(float2* A, int P, int k0, int nb) {
+  __shared__ float2 Lk[CB][CB + 1];
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    int i = e % nb, j = e / nb;
+    Lk[i][j] = A[(size_t)(k0 + i) + (size_t)P * (k0 + j)];
+  }
+  __syncthreads();
+  const int i = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  float2 x[CB];
+#pragma unroll
+  for (int j = 0; j < CB; ++j) {
+    if (j < nb) {
+      float2 a = A[(size_t)i + (size_t)P * (k0 + j)];
+      for (int p = 0; p < j; ++p) {
+        float2 q = f2mulconj(x[p], Lk[j][p]);
+        a.x -= q.x;
+        a.y -= q.y;
+      }
+      const float inv = 1.0f / Lk[j][j].x;
+      x[j] = make_float2(a.x * inv, a.y * inv);
+      A[(size_t)i + (size_t)P * (k0 + j)] = x[j];
+    }
+  }
+}
+
+// trailing update A[i][j] -= Σ_p L[i][k0+p] conj(L[j][k0+p]) on lower tiles of
+// the trailing matrix (rows/cols >= t0 = k0 + nb), 32x32 tiles, 256 threads
+__global__ void __launch_bounds__(256) herk_update_kernel(float2* A, int P, int k0, int nb, int t0, int ntt) {
+  __shared__ float2 Li[CB][CB + 1];
+  __shared__ float2 Lj[CB][CB + 1];
+  int ti, tj;
+  {
+    // lower tiles enumerated column by column: (0,0),(1,0),..,(ntt-1,0),(1,1),...
+    int c = 0, rem = blockIdx.x;
+    while (rem >= ntt - c) { rem -= ntt - c; ++c; }
+    tj = c; ti = c + rem;
+  }
+  const int r0 = t0 + ti * CB, c0 = t0 + tj * CB;
+  for (int e = threadIdx.x; e < CB * nb; e += blockDim.x) {
+    int r = e % CB, p = e / CB;
+    int gi = r0 + r, gj = c0 + r;
+    Li[r][p] = gi < P ? A[(size_t)gi + (size_t)P * (k0 + p)] : make_float2(0.f, 0.f);
+    Lj[r][p] = gj < P ? A[(size_t)gj + (size_t)P * (k0 + p)] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int tr = threadIdx.x % CB, tc4 = threadIdx.x / CB;   // 8 column groups of 4
+  for (int q = 0; q < 4; ++q) {
+    int c = tc4 * 4 + q;
+    int gi = r0 + tr, gj = c0 + c;
+    if (gi >= P || gj >= P || gi < gj) continue;
+    float2 s = make_float2(0.f, 0.f);
+    for (int p = 0; p < nb; ++p) {
+      float2 m = f2mulconj(Li[tr][p], Lj[c][p]);
+      s.x += m.x;
+      s.y += m.y;
+    }
+    float2* a = A + (size_t)gi + (size_t)P * gj;
+    a->x -= s.x;
+    a->y -= s.y;
+  }
+}
+
+// single-block triangular solves with the FP32 factor: L y = b, Lᴴ x = y
+__global__ void __launch_bounds__(1024) trsv_kernel(const float2* __restrict__ L, int P, float2* b) {
+  __shared__ float2 xj;
+  for (int j = 0; j < P; ++j) {
+    if (threadIdx.x == 0) {
+      float2 v = b[j];
+      float inv = 1.0f / L[(size_t)j + (size_t)P * j].x;
+      xj = make_float2(v.x * inv, v.y * inv);
+      b[j] = xj;
+    }
+    __syncthreads();
+    float2 x = xj;
+    for (int i = j + 1 + threadIdx.x; i < P; i += blockDim.x) {
+      float2 m = f2mul(L[(size_t)i + (size_t)P * j], x);
+      b[i].x -= m.x;
+      b[i].y -= m.y;
+    }
+    __syncthreads();
+  }
+  // backward: x_j = (y_j - Σ_{i>j} conj(L[i][j]) x_i) / L_jj
+  __shared__ float red[2][32];
+  for (int j = P - 1; j >= 0; --j) {
+    float sx = 0.f, sy = 0.f;
+    for (int i = j + 1 + threadIdx.x; i < P; i += blockDim.x) {
+      float2 l = L[(size_t)i + (size_t)P * j];
+      float2 x = b[i];
+      // conj(l) * x
+      sx += l.x * x.x + l.y * x.y;
+      sy += l.x * x.y - l.y * x.x;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, off);
+      sy += __shfl_xor_sync(0xffffffffu, sy, off);
+    }
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = sx; red[1][threadIdx.x >> 5] = sy; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float tx = 0.f, ty = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tx += red[0][w]; ty += red[1][w]; }
+      float2 y = b[j];
+      float inv = 1.0f / L[(size_t)j + (size_t)P * j].x;
+      b[j] = make_float2((y.x - tx) * inv, (y.y - ty) * inv);
+    }
+    __syncthreads();
+  }
+}
+
+// FP64 residual r = F - (S + D) x with x updated by the FP32 correction d
+__global__ void refine_update_kernel(double* x, const float2* __restrict__ d, int P, int first) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  if (first) { x[2 * i] = 0.0; x[2 * i + 1] = 0.0; }
+  x[2 * i] += (double)d[i].x;
+  x[2 * i + 1] += (double)d[i].y;
+}
+
+__global__ void __launch_bounds__(128)
+residual_kernel(const double* __restrict__ S, int P, const double* __restrict__ F,
+                const double* __restrict__ x, int kind, double eps, double lam, int real_params,
+                double* __restrict__ r, float2* __restrict__ rf) {
+  const int k = blockIdx.x;
+  // (S x)_k = Σ_l S[k][l] x_l = Σ_l conj(S[l][k]) x_l (Hermitian; column k contiguous)
+  double sx = 0.0, sy = 0.0;
+  for (int l = threadIdx.x; l < P; l += blockDim.x) {
+    double ar = S[2 * ((size_t)l + (size_t)P * k)], ai = -S[2 * ((size_t)l + (size_t)P * k) + 1];
+    if (l == k) ai = 0.0;
+    double xr = x[2 * l], xi = x[2 * l + 1];
+    sx += ar * xr - ai * xi;
+    sy += ar * xi + ai * xr;
+  }
+  __shared__ double red[2][4];
+  for (int off = 16; off > 0; off >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, off);
+    sy += __shfl_xor_sync(0xffffffffu, sy, off);
+  }
+  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = sx; red[1][threadIdx.x >> 5] = sy; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tx = red[0][0] + red[0][1] + red[0][2] + red[0][3];
+    double ty = red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    double dsh = diag_shift(S, P, k, kind, eps, lam);
+    tx += dsh * x[2 * k];
+    ty += dsh * x[2 * k + 1];
+    double fx = F[2 * k], fy = real_params ? 0.0 : F[2 * k + 1];
+    double rx = fx - tx, ry = fy - ty;
+    r[2 * k] = rx;
+    r[2 * k + 1] = ry;
+    rf[k] = make_float2((float)rx, (float)ry);
+  }
+}
+
+__global__ void rhs_init_kernel(const double* F, int P, int real_params, float2* rf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  rf[i] = make_float2((float)F[2 * i], real_params ? 0.f : (float)F[2 * i + 1]);
+}
+
+__global__ void descent_kernel(double* w, const double* dw, long n, double lr) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) w[i] -= lr * dw[i];
+}
+
+// ---------------------------------------------------------------------------
+// Measurement statistics, one block; FP64 with fixed reduction order.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ cpx<double> stat_val(const cpx<R>* v, long i, int mode) {
+  cpx<R> a = v[i];
+  if (mode == 1) return mk((double)a.x * a.x + (double)a.y * a.y, 0.0);
+  return mk((double)a.x, (double)a.y);
+}
+
+__device__ void block_sum2(double& a, double& b, double* sh) {
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    b += __shfl_xor_sync(0xffffffffu, b, off);
+  }
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { sh[2 * w] = a; sh[2 * w + 1] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0, y = 0;
+    for (int i = 0; i < nw; ++i) { x += sh[2 * i]; y += sh[2 * i + 1]; }
+    sh[64] = x; sh[65] = y;
+  }
+  __syncthreads();
+  a = sh[64]; b = sh[65];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(1024) stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
+                                                     double* __restrict__ out) {
+  __shared__ double sh[66];
+  // pass 1: μ = mean of chain means, mean of chain variances
+  double smx = 0, smy = 0, svar = 0, dummy = 0;
+  for (int c = threadIdx.x; c < B; c += blockDim.x) {
+    double mx = 0, my = 0;
+    for (int l = 0; l < L; ++l) { cpx<double> x = stat_val(v, c + (long)B * l, mode); mx += x.x; my += x.y; }
+    mx /= L; my /= L;
+    double vv = 0;
+    for (int l = 0; l < L; ++l) {
+      cpx<double> x = stat_val(v, c + (long)B * l, mode);
+      vv += (x.x - mx) * (x.x - mx) + (x.y - my) * (x.y - my);
+    }
+    svar += L > 1 ? vv / (L - 1) : 0.0;
+    smx += mx; smy += my;
+  }
+  block_sum2(smx, smy, sh);
+  block_sum2(svar, dummy, sh);
+  const double mux = smx / B, muy = smy / B;
+  // pass 2: variance of chain means and of all values around μ
+  double vmc = 0, vall = 0;
+  for (int c = threadIdx.x; c < B; c += blockDim.x) {
+    double mx = 0, my = 0;
+    for (int l = 0; l < L; ++l) {
+      cpx<double> x = stat_val(v, c + (long)B * l, mode);
+      mx += x.x; my += x.y;
+      vall += (x.x - mux) * (x.x - mux) + (x.y - muy) * (x.y - muy);
+    }
+    mx /= L; my /= L;
+    vmc += (mx - mux) * (mx - mux) + (my - muy) * (my - muy);
+  }
+  block_sum2(vmc, vall, sh);
+  if (threadIdx.x == 0) {
+    double var_mu_ch = vmc / (B - 1);
+    double var_mu = vall / ((double)B * L - 1);
+    double t = var_mu_ch / var_mu;
+    out[0] = mux;
+    out[1] = muy;
+    out[2] = sqrt(var_mu_ch / B);
+    out[3] = svar / B;
+    out[4] = fmax(0.0, 0.5 * (t * L - 1.0));
+    out[5] = sqrt((double)(L - 1) / L + t);
+  }
+}
+
+}  // namespace
+
+// ------------------------------- launchers ---------------------------------
+
+cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* partial, int ksplit,
+                             cudaStream_t st) {
+  const int rows = 2 * P;
+  const int nt = (rows + GT - 1) / GT;
+  const int ntiles = nt * (nt + 1) / 2;
+  dim3 grid(ntiles, ksplit);
+  gram_simt_kernel<<<grid, 256, 0, st>>>(src, rows, nt, ksplit, partial);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  long tot = (long)rows * rows;
+  gram_reduce_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(partial, rows, nt * GT, GT, ksplit, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, cudaStream_t st) {
+  long tot = 2L * P * Ns_pad;
+  build_X_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(src, 2 * P, Ns_pad, X);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_params, double* S,
+                              cudaStream_t st) {
+  long tot = (long)P * P;
+  assemble_S_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(G, P, inv_ns, real_params ? 1 : 0, S);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
+                            double lam, bool real_params, int refine_iters, cudaStream_t st) {
+  long tot = (long)P * P;
+  shift_copy_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(sb.S, P, kind, eps, lam, sb.Lf);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  for (int k0 = 0; k0 < P; k0 += CB) {
+    const int nb = min(CB, P - k0);
+    potrf_diag_kernel<<<1, 1024, 0, st>>>(sb.Lf, P, k0, nb, sb.status);
+    const int rem = P - k0 - nb;
+    if (rem > 0) {
+      trsm_panel_kernel<<<(rem + 127) / 128, 128, 0, st>>>(sb.Lf, P, k0, nb);
+      const int ntt = (rem + CB - 1) / CB;
+      herk_update_kernel<<<ntt * (ntt + 1) / 2, 256, 0, st>>>(sb.Lf, P, k0, nb, k0 + nb, ntt);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  rhs_init_kernel<<<(P + 255) / 256, 256, 0, st>>>(F, P, real_params ? 1 : 0, sb.rf);
+  for (int it = 0; it <= refine_iters; ++it) {
+    trsv_kernel<<<1, 1024, 0, st>>>(sb.Lf, P, sb.rf);
+    refine_update_kernel<<<(P + 255) / 256, 256, 0, st>>>(sb.x, sb.rf, P, it == 0);
+    residual_kernel<<<P, 128, 0, st>>>(sb.S, P, F, sb.x, kind, eps, lam, real_params ? 1 : 0, sb.r, sb.rf);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_descent(double* master, const double* dw, long n_doubles, double lr,
+                           cudaStream_t st) {
+  descent_kernel<<<(unsigned)((n_doubles + 255) / 256), 256, 0, st>>>(master, dw, n_doubles, lr);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* out6, cudaStream_t st) {
+  stats_kernel<R><<<1, 1024, 0, st>>>(vals, B, L, mode, out6);
+  return cudaGetLastError();
+}
+template cudaError_t launch_stats<float>(const cpx<float>*, int, int, int, double*, cudaStream_t);
+template cudaError_t launch_stats<double>(const cpx<double>*, int, int, int, double*, cudaStream_t);

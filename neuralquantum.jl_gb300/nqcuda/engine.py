@@ -1,0 +1,154 @@
+"""Thin object wrapper of one libnqcuda handle (include/nqcuda.h)."""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .hilbert import SuperOpSpace, physical
+from .networks import RBM, NDM, af_logcosh
+
+
+class Engine:
+    def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
+                 eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0):
+        L = _lib.lib()
+        cfg = _lib.NqConfig()
+        ph = physical(hilb)
+        if isinstance(net, RBM):
+            cfg.network = _lib.NQ_NET_RBM
+            cfg.n_hidden = net.M
+            cfg.n_ancilla = 0
+            self.complex_params = True
+        elif isinstance(net, NDM):
+            cfg.network = _lib.NQ_NET_NDM
+            cfg.n_hidden = net.Mh
+            cfg.n_ancilla = net.Ma
+            self.complex_params = False
+        else:
+            raise TypeError(f"unsupported network {type(net)}")
+        cfg.activation = _lib.NQ_ACT_LOGCOSH if net.f == af_logcosh else _lib.NQ_ACT_SOFTPLUS
+        cfg.hilbert = _lib.NQ_HILB_SPIN if ph.kind == "spin" else _lib.NQ_HILB_FOCK
+        cfg.n_sites = ph.n_sites
+        cfg.n_chains = n_chains
+        cfg.chain_length = chain_length
+        cfg.burn = burn
+        cfg.passes = passes
+        cfg.seed = seed
+        cfg.eval_precision = eval_precision
+        cfg.s_precision = s_precision
+        cfg.quirks = quirks
+        self.cfg = cfg
+        self.lib = L
+        self.h = ctypes.c_void_p()
+        st = L.nq_create(ctypes.byref(cfg), ctypes.byref(self.h))
+        if st != _lib.NQ_OK:
+            raise _lib.NqError(st, "nq_create failed (see stderr)")
+        self.P = int(L.nq_n_params(self.h))
+        self.N = ph.n_sites
+        self.nsites = 2 * ph.n_sites if isinstance(hilb, SuperOpSpace) else ph.n_sites
+        self.B, self.L = n_chains, chain_length
+        self.passes = passes + 1 if passes % 2 == 0 else passes
+        self._op = None
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.nq_destroy(self.h)
+                self.h = ctypes.c_void_p()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != _lib.NQ_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.nq_last_error(self.h, buf, 512)
+            raise _lib.NqError(st, buf.value.decode(errors="replace"))
+
+    # ---- parameters -------------------------------------------------------
+    def set_params(self, flat):
+        if self.complex_params:
+            v = np.ascontiguousarray(flat, dtype=np.complex128)
+            self._check(self.lib.nq_set_params(self.h, v.ctypes.data, self.P, _lib.NQ_DTYPE_C128))
+        else:
+            v = np.ascontiguousarray(np.real(flat), dtype=np.float64)
+            self._check(self.lib.nq_set_params(self.h, v.ctypes.data, self.P, _lib.NQ_DTYPE_F64))
+
+    def get_params(self):
+        if self.complex_params:
+            v = np.empty(self.P, np.complex128)
+            self._check(self.lib.nq_get_params(self.h, v.ctypes.data, self.P, _lib.NQ_DTYPE_C128))
+        else:
+            v = np.empty(self.P, np.float64)
+            self._check(self.lib.nq_get_params(self.h, v.ctypes.data, self.P, _lib.NQ_DTYPE_F64))
+        return v
+
+    def set_operator(self, table):
+        self._op = table           # keep the arrays alive
+        st = table.struct()
+        self._check(self.lib.nq_set_operator(self.h, ctypes.byref(st)))
+
+    # ---- stages -------------------------------------------------------------
+    def sample(self, call_index, want_samples=True, want_accept_bits=False):
+        out = np.empty((self.L, self.B, self.nsites), np.int8) if want_samples else None
+        steps = self.passes * (self.cfg.burn + self.L)
+        bits = np.empty((steps, self.B), np.uint8) if want_accept_bits else None
+        self._check(self.lib.nq_sample(self.h, call_index,
+                                       out.ctypes.data if out is not None else None,
+                                       bits.ctypes.data if bits is not None else None))
+        return out, bits
+
+    def set_samples(self, samples):
+        v = np.ascontiguousarray(samples, dtype=np.int8)
+        if v.size != self.L * self.B * self.nsites:
+            raise ValueError("samples must hold L x B x nsites values")
+        self._check(self.lib.nq_set_samples(self.h, v.ctypes.data))
+
+    def logpsi(self, sigma, with_grad=False):
+        """sigma: (n, nsites) site values -> logψ (n,) [, grad (n, P)]."""
+        v = np.ascontiguousarray(sigma, dtype=np.int8)
+        n = v.shape[0]
+        out = np.empty(n, np.complex128)
+        if with_grad:
+            g = np.empty((n, self.P), np.complex128)
+            self._check(self.lib.nq_logpsi_grad(self.h, v.ctypes.data, n, out.ctypes.data, g.ctypes.data))
+            return out, g
+        self._check(self.lib.nq_logpsi(self.h, v.ctypes.data, n, out.ctypes.data))
+        return out
+
+    def estimate(self, want_loc=False, want_force=False):
+        m = _lib.NqMeasurement()
+        loc = np.empty((self.L, self.B), np.complex128) if want_loc else None
+        if want_force:
+            force = np.empty(self.P, np.complex128 if self.complex_params else np.float64)
+        else:
+            force = None
+        self._check(self.lib.nq_estimate(self.h, ctypes.byref(m),
+                                         loc.ctypes.data if loc is not None else None,
+                                         force.ctypes.data if force is not None else None))
+        return m, loc, force
+
+    def sr_matrix(self):
+        S = np.empty((self.P, self.P), np.complex128 if self.complex_params else np.float64, order="F")
+        self._check(self.lib.nq_get_sr_matrix(self.h, S.ctypes.data))
+        return S
+
+    def precondition(self, kind=0, eps=0.001, lam0=100.0, b=0.95, lam_min=1e-4, it=1):
+        dw = np.empty(self.P, np.complex128 if self.complex_params else np.float64)
+        self._check(self.lib.nq_precondition(self.h, kind, eps, lam0, b, lam_min, it, dw.ctypes.data))
+        return dw
+
+    def update_descent(self, lr):
+        self._check(self.lib.nq_update_descent(self.h, lr))
+
+    def vmc_step(self, call_index, eps, lr):
+        m = _lib.NqMeasurement()
+        self._check(self.lib.nq_vmc_step(self.h, call_index, eps, lr, ctypes.byref(m)))
+        return m
+
+    def stage_times(self):
+        a = (ctypes.c_float * 6)()
+        self._check(self.lib.nq_stage_times(self.h, a))
+        return list(a)
+
+    def kernel_launches(self):
+        return int(self.lib.nq_kernel_launches(self.h))

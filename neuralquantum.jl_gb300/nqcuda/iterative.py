@@ -1,0 +1,117 @@
+"""The reference's user loop on top of libnqcuda.
+
+    is = BatchedSampler(net, sampler, H, SR(ϵ=0.01); batch_sz=4096)
+    for i in range(1, 301):
+        ldata, prec = sample_(is)            # sample!(is)
+        grad = precondition_(prec, algo, i)  # precondition!(prec, algo, i)
+        update_(Descent(0.01), net, grad)    # Optimisers.update!(opt, net, grad)
+
+Reference: src/IterativeInterface/build_Batched.jl:1-14 (BatchedSampler),
+Samplers/CostFun/BatchedValSampler.jl:117-139 and BatchedGradSampler.jl:77-123
+(sample!), src/Algorithms/SR/SR.jl:50-57 and SRDirect.jl:51-90
+(SR / precondition!), src/Optimisers/rules.jl:11-17 and apply.jl:25-32
+(Descent / update!).
+"""
+import numpy as np
+
+from . import _lib
+from .engine import Engine
+from .operators import KLocalLiouvillian, op_table
+from .hilbert import SuperOpSpace
+from .stats import Measurement
+
+sr_shift, sr_multiplicative, sr_none = 0, 1, 2
+sr_cholesky = "sr_cholesky"
+
+
+class SR:
+    """``SR(T; ϵ=0.001, precondition_type=sr_shift, algorithm=sr_cholesky,
+    λ0=100, b=0.95, λmin=1e-4)``.  Only the direct Cholesky algorithm is
+    provided by the engine."""
+
+    def __init__(self, eps=0.001, precondition_type=sr_shift, algorithm=sr_cholesky,
+                 lam0=100.0, b=0.95, lam_min=1e-4):
+        if algorithm != sr_cholesky:
+            raise NotImplementedError("the engine implements the sr_cholesky algorithm")
+        self.eps, self.precondition_type = float(eps), precondition_type
+        self.lam0, self.b, self.lam_min = float(lam0), float(b), float(lam_min)
+
+
+class Descent:
+    def __init__(self, eta):
+        self.eta = float(eta)
+
+
+class SRCache:
+    """What ``sample!`` returns as the preconditioner cache: S and F live on
+    the device inside the engine."""
+
+    def __init__(self, sampler):
+        self.sampler = sampler
+
+
+class Gradient:
+    """Δw returned by ``precondition_``; the values also stay on the device."""
+
+    def __init__(self, sampler, values):
+        self.sampler = sampler
+        self.values = values
+
+
+class BatchedSampler:
+    def __init__(self, net, sampler, prob, algo=None, batch_sz=16, eval_precision=_lib.NQ_EVAL_F32,
+                 s_precision=_lib.NQ_S_F32, reference_quirks=False):
+        self.net = net
+        self.sampler = sampler
+        self.prob = prob
+        self.algo = algo if algo is not None else SR()
+        self.liouvillian = isinstance(prob, KLocalLiouvillian)
+        hilb = prob.hilb if not self.liouvillian else prob.hilb
+        quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
+        self.engine = Engine(net, hilb, batch_sz, sampler.chain_length, sampler.burn_length,
+                             sampler.passes, sampler.seed, eval_precision, s_precision, quirks)
+        self.engine.set_params(net.flat())
+        self.engine.set_operator(op_table(prob))
+        self.calls = 0
+        self.last_samples = None
+
+    def sample_(self, keep_samples=False):
+        out, _ = self.engine.sample(self.calls, want_samples=keep_samples)
+        self.calls += 1
+        if keep_samples:
+            self.last_samples = out
+        m, _, _ = self.engine.estimate()
+        mean = complex(m.mean_re, m.mean_im) if not self.liouvillian else m.mean_re
+        return Measurement(mean, m.error, m.variance, m.tau, m.R), SRCache(self)
+
+    def step(self, lr, eps=None):
+        """One whole iteration (sample!, precondition! with sr_shift, update!)
+        replayed from a captured CUDA graph."""
+        eps = self.algo.eps if eps is None else eps
+        m = self.engine.vmc_step(self.calls, eps, lr)
+        self.calls += 1
+        mean = complex(m.mean_re, m.mean_im) if not self.liouvillian else m.mean_re
+        return Measurement(mean, m.error, m.variance, m.tau, m.R)
+
+    def sync_net(self):
+        self.net.set_flat(self.engine.get_params())
+        return self.net
+
+
+def sample_(is_):
+    return is_.sample_()
+
+
+def precondition_(prec, algo, it):
+    eng = prec.sampler.engine
+    dw = eng.precondition(algo.precondition_type, algo.eps, algo.lam0, algo.b, algo.lam_min, it)
+    return Gradient(prec.sampler, dw)
+
+
+def update_(opt, net, grad):
+    s = grad.sampler
+    if s.net is not net:
+        raise ValueError("the gradient belongs to another network")
+    s.engine.update_descent(opt.eta)
+    s.sync_net()
+    return net

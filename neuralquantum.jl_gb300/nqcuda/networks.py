@@ -1,0 +1,90 @@
+"""Network parameter containers of the reference API (host side).
+
+``RBM(T, N, α, f)`` (src/Networks/ClosedSystems/RBM.jl:40-48) and
+``NDM(T, N, αh, αa, f)`` (src/Networks/MixedDensityMatrix/NDM.jl:50-63) hold
+their arrays on the host in the reference layout; the engine keeps the
+authoritative FP64 copy on the device while a ``BatchedSampler`` is bound and
+writes it back after every ``update_``.  The flat parameter vector is the
+functor field order with column-major arrays (src/tuple_logic.jl:31-72).
+"""
+import numpy as np
+
+af_logcosh = "logcosh"
+af_softplus = "softplus"
+
+
+class RBM:
+    def __init__(self, T, N, alpha, f=af_softplus):
+        self.dtype = np.dtype(T)
+        if self.dtype.kind != "c":
+            raise ValueError("the RBM takes complex weights (ComplexF32 / ComplexF64)")
+        self.N = int(N)
+        self.M = int(round(alpha * N))
+        self.f = f
+        self.a = np.zeros(self.N, self.dtype)
+        self.b = np.zeros(self.M, self.dtype)
+        self.W = np.zeros((self.M, self.N), self.dtype)
+
+    @property
+    def n_params(self):
+        return self.N + self.M + self.M * self.N
+
+    def flat(self):
+        return np.concatenate([self.a, self.b, self.W.reshape(-1, order="F")]).astype(np.complex128)
+
+    def set_flat(self, v):
+        v = np.asarray(v)
+        N, M = self.N, self.M
+        self.a = v[:N].astype(self.dtype)
+        self.b = v[N:N + M].astype(self.dtype)
+        self.W = v[N + M:].reshape((M, N), order="F").astype(self.dtype)
+
+    def __repr__(self):
+        return f"RBM({self.dtype}, n={self.N}, α={self.M / self.N}, f={self.f})"
+
+
+class NDM:
+    FIELDS = ("b_mu", "h_mu", "w_mu", "u_mu", "b_la", "h_la", "d_la", "w_la", "u_la")
+
+    def __init__(self, T, N, alpha_h, alpha_a, f=af_softplus):
+        self.dtype = np.dtype(T)
+        if self.dtype.kind == "c":          # NDM.jl:46-47: complex T becomes real
+            self.dtype = np.dtype(self.dtype.type(0).real.dtype)
+        self.N = int(N)
+        self.Mh = int(round(alpha_h * N))
+        self.Ma = int(round(alpha_a * N))
+        self.f = f
+        N, Mh, Ma = self.N, self.Mh, self.Ma
+        self.shapes = {"b_mu": (N,), "h_mu": (Mh,), "w_mu": (Mh, N), "u_mu": (Ma, N),
+                       "b_la": (N,), "h_la": (Mh,), "d_la": (Ma,), "w_la": (Mh, N),
+                       "u_la": (Ma, N)}
+        for k in self.FIELDS:
+            setattr(self, k, np.zeros(self.shapes[k], self.dtype))
+
+    @property
+    def n_params(self):
+        return sum(int(np.prod(s)) for s in self.shapes.values())
+
+    def flat(self):
+        return np.concatenate([getattr(self, k).reshape(-1, order="F") for k in self.FIELDS])
+
+    def set_flat(self, v):
+        v = np.real(np.asarray(v))
+        o = 0
+        for k in self.FIELDS:
+            n = int(np.prod(self.shapes[k]))
+            setattr(self, k, v[o:o + n].reshape(self.shapes[k], order="F").astype(self.dtype))
+            o += n
+
+
+def init_random_pars_(net, sigma=0.01, rng=None):
+    """``init_random_pars!`` (src/utils/rng.jl:27-38): every weight is drawn
+    from randn * sqrt(sigma); complex draws have variance 1/2 per part."""
+    rng = np.random.default_rng() if rng is None else rng
+    p = net.flat()
+    if np.iscomplexobj(p):
+        v = (rng.standard_normal(p.size) + 1j * rng.standard_normal(p.size)) / np.sqrt(2.0)
+    else:
+        v = rng.standard_normal(p.size)
+    net.set_flat(v * np.sqrt(sigma))
+    return net

@@ -1,0 +1,199 @@
+"""RBM and NDM networks in FP64 (test infrastructure, see ``oracle/__init__``).
+
+Flat parameter order = functor field order, each array column-major
+(src/tuple_logic.jl:31-72):
+
+* RBM  (src/Networks/ClosedSystems/RBM.jl:3-12):  a (N), b (M), W (M x N)
+* NDM  (src/Networks/MixedDensityMatrix/NDM.jl:3-19): b_mu (N), h_mu (aN),
+  w_mu (aN x N), u_mu (bN x N), b_la (N), h_la (aN), d_la (bN), w_la (aN x N),
+  u_la (bN x N)
+
+Activations follow src/Networks/activation.jl:5-45; the derivative used by the
+networks is ``fwd_der(f, x)`` (tanh for logcosh, sigmoid for softplus).
+"""
+import numpy as np
+
+LOGCOSH = "logcosh"
+SOFTPLUS = "softplus"
+
+
+def logcosh(x):
+    """``logℒ2`` (activation.jl:9-13)."""
+    x = np.asarray(x)
+    if np.iscomplexobj(x):
+        re, im = x.real, x.imag
+        return _logcosh_real(re) + np.log(np.cos(im) + 1j * np.tanh(re) * np.sin(im))
+    return _logcosh_real(x)
+
+
+def _logcosh_real(x):
+    ax = np.abs(x)
+    with np.errstate(over="ignore"):
+        small = np.log(np.cosh(np.where(ax <= 12.0, x, 0.0)))
+    return np.where(ax <= 12.0, small, ax - np.log(2.0))
+
+
+def softplus(x):
+    """``logℒ(x) = log1p(exp(x))`` (activation.jl:20)."""
+    return np.log1p(np.exp(x))
+
+
+def act(name, x):
+    return logcosh(x) if name == LOGCOSH else softplus(x)
+
+
+def dact(name, x):
+    """``fwd_der(f, x)`` (activation.jl:22-27)."""
+    if name == LOGCOSH:
+        return np.tanh(x)
+    return 1.0 / (1.0 + np.exp(-x))
+
+
+# ---------------------------------------------------------------------------
+# RBM
+# ---------------------------------------------------------------------------
+
+class RBM:
+    def __init__(self, n, m, activation=LOGCOSH, dtype=np.complex128):
+        self.N, self.M = int(n), int(m)
+        self.activation = activation
+        self.a = np.zeros(self.N, dtype)
+        self.b = np.zeros(self.M, dtype)
+        self.W = np.zeros((self.M, self.N), dtype)
+
+    @property
+    def n_params(self):
+        return self.N + self.M + self.M * self.N
+
+    def flat(self):
+        return np.concatenate([self.a, self.b, self.W.reshape(-1, order="F")])
+
+    def set_flat(self, v):
+        v = np.asarray(v)
+        N, M = self.N, self.M
+        self.a = v[:N].astype(self.a.dtype).copy()
+        self.b = v[N:N + M].astype(self.b.dtype).copy()
+        self.W = v[N + M:].reshape((M, N), order="F").astype(self.W.dtype).copy()
+
+    def theta(self, sigma):
+        """θ = Wσ + b for a batch sigma (B, N) -> (B, M)."""
+        return sigma @ self.W.T + self.b[None, :]
+
+    def logpsi(self, sigma):
+        """RBMBatched.jl:37-56."""
+        sigma = np.atleast_2d(sigma)
+        th = self.theta(sigma)
+        return sigma @ self.a + act(self.activation, th).sum(axis=1)
+
+    def logpsi_and_grad(self, sigma):
+        """RBMBatched.jl:58-91; grad has shape (B, P)."""
+        sigma = np.atleast_2d(sigma)
+        th = self.theta(sigma)
+        out = sigma @ self.a + act(self.activation, th).sum(axis=1)
+        g = dact(self.activation, th)
+        B = sigma.shape[0]
+        dW = g[:, :, None] * np.conj(sigma)[:, None, :]            # (B, M, N)
+        grad = np.concatenate([sigma.astype(g.dtype), g,
+                               dW.transpose(0, 2, 1).reshape(B, -1)], axis=1)
+        return out, grad
+
+    def log_prob(self, sigma):
+        """``log_prob_ψ!`` for kets: 2 Re logψ (base_batched_networks.jl:255-258)."""
+        return 2.0 * np.real(self.logpsi(sigma))
+
+
+# ---------------------------------------------------------------------------
+# NDM
+# ---------------------------------------------------------------------------
+
+class NDM:
+    FIELDS = ("b_mu", "h_mu", "w_mu", "u_mu", "b_la", "h_la", "d_la", "w_la", "u_la")
+
+    def __init__(self, n, alpha_h, alpha_a, activation=SOFTPLUS):
+        self.N = int(n)
+        self.Mh = int(round(alpha_h * n))
+        self.Ma = int(round(alpha_a * n))
+        self.activation = activation
+        N, Mh, Ma = self.N, self.Mh, self.Ma
+        self.shapes = {"b_mu": (N,), "h_mu": (Mh,), "w_mu": (Mh, N), "u_mu": (Ma, N),
+                       "b_la": (N,), "h_la": (Mh,), "d_la": (Ma,), "w_la": (Mh, N),
+                       "u_la": (Ma, N)}
+        for f in self.FIELDS:
+            setattr(self, f, np.zeros(self.shapes[f]))
+
+    @property
+    def n_params(self):
+        return sum(int(np.prod(s)) for s in self.shapes.values())
+
+    def flat(self):
+        return np.concatenate([getattr(self, f).reshape(-1, order="F") for f in self.FIELDS])
+
+    def set_flat(self, v):
+        v = np.real(np.asarray(v)).astype(np.float64)
+        o = 0
+        for f in self.FIELDS:
+            n = int(np.prod(self.shapes[f]))
+            setattr(self, f, v[o:o + n].reshape(self.shapes[f], order="F").copy())
+            o += n
+
+    def _parts(self, sr, sc):
+        f = self.activation
+        tl_s = sr @ self.w_la.T + self.h_la
+        tm_s = sr @ self.w_mu.T + self.h_mu
+        tl_c = sc @ self.w_la.T + self.h_la
+        tm_c = sc @ self.w_mu.T + self.h_mu
+        ssum = sr + sc
+        sdif = sr - sc
+        pi = 0.5 * ssum @ self.u_la.T + 0.5j * sdif @ self.u_mu.T + self.d_la
+        gl = 0.5 * (act(f, tl_s).sum(1) + act(f, tl_c).sum(1) + ssum @ self.b_la)
+        gm = 0.5 * (act(f, tm_s).sum(1) - act(f, tm_c).sum(1) + sdif @ self.b_mu)
+        out = gl + 1j * gm + act(f, pi).sum(1)
+        return out, tl_s, tm_s, tl_c, tm_c, ssum, sdif, pi
+
+    def logpsi(self, sr, sc):
+        """NDM.jl:76-96 / NDMBatched.jl:94-175 for batches (B, N)."""
+        sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
+        return self._parts(sr, sc)[0]
+
+    def logpsi_and_grad(self, sr, sc):
+        """NDMBatched.jl:177-280; grad (B, P) complex in the flat order."""
+        sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
+        out, tl_s, tm_s, tl_c, tm_c, ssum, sdif, pi = self._parts(sr, sc)
+        f = self.activation
+        dl_s, dm_s = dact(f, tl_s), dact(f, tm_s)
+        dl_c, dm_c = dact(f, tl_c), dact(f, tm_c)
+        dpi = dact(f, pi)
+        B = sr.shape[0]
+
+        def outer(v, w):   # (B, M, N) -> column-major flattening
+            return (v[:, :, None] * np.conj(w)[:, None, :]).transpose(0, 2, 1).reshape(B, -1)
+
+        parts = {
+            "b_mu": 0.5j * sdif,
+            "h_mu": 0.5j * (dm_s - dm_c),
+            "w_mu": 0.5j * (outer(dm_s, sr) - outer(dm_c, sc)),
+            "u_mu": 0.5j * outer(dpi, sdif),
+            "b_la": 0.5 * ssum + 0j,
+            "h_la": 0.5 * (dl_s + dl_c) + 0j,
+            "d_la": dpi,
+            "w_la": 0.5 * (outer(dl_s, sr) + outer(dl_c, sc)) + 0j,
+            "u_la": 0.5 * outer(dpi, ssum),
+        }
+        grad = np.concatenate([parts[k] for k in self.FIELDS], axis=1)
+        return out, grad
+
+    def log_prob(self, sr, sc):
+        """2 Re log ρ(σ, η) on doubled states (base_batched_networks.jl:255-258)."""
+        return 2.0 * np.real(self.logpsi(sr, sc))
+
+
+def init_random_pars(net, rng, sigma=1e-4):
+    """``init_random_pars!`` (src/utils/rng.jl:27-38): randn * sqrt(sigma);
+    complex randn has variance 1/2 per part (Julia convention)."""
+    p = net.flat()
+    if np.iscomplexobj(p):
+        v = (rng.standard_normal(p.size) + 1j * rng.standard_normal(p.size)) / np.sqrt(2)
+    else:
+        v = rng.standard_normal(p.size)
+    net.set_flat(v * np.sqrt(sigma))
+    return net

@@ -1,0 +1,91 @@
+"""Metropolis local-flip sampler replay (test infrastructure, see
+``oracle/__init__``).
+
+Restates src/Samplers/Metropolis.jl:101-167 with src/Samplers/MCMCRules/
+LocalRule.jl:19-28 and the chain bookkeeping of
+src/IterativeInterface/Samplers/BaseIterativeSampler.jl:5-17, with the
+reference MersenneTwister stream replaced by the Philox schema of
+``oracle.philox``:
+
+* every ``sample!`` call re-initialises all chains uniformly at random
+  (``init_sampler!`` :101-115), then runs ``burn`` sweeps;
+* a sweep (``samplenext!``) is ``passes`` Metropolis steps; ``passes`` is made
+  odd by the constructor (:30-38);
+* a step flips one uniformly chosen site per chain (sites 0..2N-1 on doubled
+  states: >= N flips the column, DoubledHilbert.jl:19-27) and accepts iff
+  ``u < exp(lp' - lp)`` (:148-159) with lp = 2 Re log psi;
+* recorded slot k (1-based) holds the state after burn + k sweeps.  With
+  ``stale_last_slot`` the reference's bookkeeping is reproduced exactly: the
+  loop breaks before writing slot L, which keeps its previous contents
+  (BaseIterativeSampler.jl:11-16 with ``done`` Metropolis.jl:122).
+"""
+import numpy as np
+
+from . import philox
+
+
+def fix_passes(passes):
+    return passes + 1 if passes % 2 == 0 else passes
+
+
+def init_configs(hilb, seed, call, chains, n_sites_total):
+    w = philox.init_words(seed, call, chains, n_sites_total)
+    top = (w >> np.uint32(31)).astype(np.int64)          # floor(u*2), u = w/2^32
+    return hilb.value(top)
+
+
+def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
+        doubled=False, stale_last_slot=False, prev_samples=None,
+        gpu_accept_bits=None, tie_tol=1e-3, chain_offset=0):
+    """Replays one ``_sample_state!`` call.
+
+    ``log_prob(batch)`` maps (B, nsites_total) configurations to 2 Re log psi.
+    ``gpu_accept_bits`` (optional, (steps, B) bool) resolves near-tie
+    decisions (|log u - Δ| < tie_tol) the way the GPU took them; all other
+    decisions must agree.  Returns (samples (L, B, nsites_total), info)."""
+    N = hilb.n_sites
+    nt = 2 * N if doubled else N
+    chains = np.arange(n_chains) + chain_offset
+    sigma = init_configs(hilb, seed, call, chains, nt)
+    lp = log_prob(sigma)
+    passes = fix_passes(passes)
+    L = chain_length
+    samples = np.empty((L, n_chains, nt))
+    if prev_samples is not None:
+        samples[:] = prev_samples
+    else:
+        samples[:] = hilb.fill_value()
+    n_record = L - 1 if (stale_last_slot and L > 1) else L
+    n_sweeps = burn + n_record
+    if stale_last_slot and L == 1:
+        n_sweeps = burn
+    info = {"ambiguous": 0, "mismatch": 0, "accepted": 0, "steps": 0}
+    t = 0
+    for sweep in range(n_sweeps):
+        for _ in range(passes):
+            site, u = philox.mh_draws(seed, call, chains, t, nt)
+            new = sigma.copy()
+            rows = np.arange(n_chains)
+            new[rows, site] = hilb.flip(sigma[rows, site])
+            lpn = log_prob(new)
+            delta = lpn - lp
+            with np.errstate(over="ignore", divide="ignore"):
+                acc = u < np.exp(delta)
+                logu = np.log(np.maximum(u, 1e-300))
+            if gpu_accept_bits is not None:
+                g = np.asarray(gpu_accept_bits[t], dtype=bool)
+                amb = np.abs(logu - delta) < tie_tol
+                info["ambiguous"] += int(np.sum(amb & (g != acc)))
+                info["mismatch"] += int(np.sum(~amb & (g != acc)))
+                acc = np.where(amb, g, acc)
+            sigma = np.where(acc[:, None], new, sigma)
+            lp = np.where(acc, lpn, lp)
+            info["accepted"] += int(acc.sum())
+            info["steps"] += n_chains
+            t += 1
+        k = sweep - burn
+        if k >= 0:
+            samples[k] = sigma
+    if stale_last_slot and L == 1:
+        samples[0] = sigma          # init_sampler! writes the first slot
+    return samples, info

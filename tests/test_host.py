@@ -1,0 +1,126 @@
+"""Host-side logic (CPU only): the C-ABI library exports, operator
+flattening against the oracle, golden fixtures, and API validation that
+needs no GPU."""
+import ctypes
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import nqcuda as nq
+from nqcuda import _lib
+from oracle import operators as oops, exact as oex, networks as onw, estimators as oest
+from oracle.hilbert import Hilbert, SPIN, FOCK
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def declared_symbols():
+    src = open(os.path.join(REPO, "include", "nqcuda.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(nq_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_loads_and_exports_every_declared_symbol():
+    nq.build()
+    L = ctypes.CDLL(_lib.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 18
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) <= set(_lib.EXPORTS), set(syms) - set(_lib.EXPORTS)
+    lib = nq.lib()
+    assert lib.nq_abi_version() == 1
+    assert b"sm_103a" in lib.nq_version()
+
+
+def test_create_rejects_bad_config_without_touching_the_gpu():
+    lib = nq.lib()
+    cfg = _lib.NqConfig()
+    cfg.network = 7
+    h = ctypes.c_void_p()
+    assert lib.nq_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.NQ_ERR_ARG
+    assert not h.value
+    assert lib.nq_create(None, ctypes.byref(h)) == _lib.NQ_ERR_ARG
+
+
+def _random_configs(n, N, kind, rng):
+    vals = [-1, 1] if kind == "spin" else [0, 1]
+    return rng.choice(vals, size=(n, N))
+
+
+@pytest.mark.parametrize("kind", ["spin", "fock"])
+def test_ket_op_table_matches_oracle_connections(kind):
+    N, h_, J = 7, 0.8, 1.3
+    hilb = nq.HomogeneousSpin(N) if kind == "spin" else nq.HomogeneousFock(N)
+    H = nq.LocalOperator(hilb)
+    for i in range(1, N + 1):
+        H -= h_ * nq.sigmax(hilb, i)
+        H += J * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i % N + 1)
+    tab = nq.op_table(H)
+    ohilb = Hilbert(N, SPIN if kind == "spin" else FOCK)
+    oH = oex.tfim_1d(ohilb, h_, J)
+    rng = np.random.default_rng(0)
+    for cfg in _random_configs(50, N, kind, rng):
+        a = tab.connections(cfg)
+        b = oops.connections_ket(oH, cfg.astype(float))
+        assert len(a) == len(b)
+        for (ma, ca), (mb, cb) in zip(a, b):
+            assert abs(ma - mb) < 1e-14
+            assert sorted(ca) == sorted((s, int(v)) for s, v in cb)
+
+
+def test_liouvillian_op_table_matches_oracle_connections():
+    N, g, V = 5, 1.0, 2.0
+    hilb = nq.HomogeneousFock(N)
+    H = nq.LocalOperator(hilb)
+    Ls = []
+    for i in range(1, N + 1):
+        H += g / 2 * nq.sigmax(hilb, i)
+        Ls.append(nq.sigmam(hilb, i))
+    for i in range(1, N):
+        H += V / 4 * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i + 1)
+    lv = nq.liouvillian(H, Ls)
+    tab = nq.op_table(lv)
+    ohilb = Hilbert(N, FOCK)
+    oH, oL = oex.dissipative_ising(ohilb, g, V)
+    olv = oops.liouvillian(oH, oL)
+    rng = np.random.default_rng(1)
+    for _ in range(40):
+        s = rng.integers(0, 2, N)
+        e = rng.integers(0, 2, N)
+        a = tab.connections(np.concatenate([s, e]))
+        b = oops.connections_doubled(olv, s.astype(float), e.astype(float))
+        assert len(a) == len(b)
+        for (ma, ca), (mb, cl, cr) in zip(a, b):
+            assert abs(ma - mb) < 1e-14
+            ref = [(s_, int(v)) for s_, v in cl] + [(s_ + N, int(v)) for s_, v in cr]
+            assert sorted(ca) == sorted(ref)
+
+
+def test_golden_rbm_fixture_pins_the_oracle():
+    fx = json.load(open(os.path.join(GOLDEN, "rbm_logpsi.json")))
+    r = onw.RBM(fx["N"], fx["M"], onw.LOGCOSH)
+    r.set_flat(np.array(fx["params_re"]) + 1j * np.array(fx["params_im"]))
+    st = np.array(fx["states"], dtype=float)
+    lp = r.logpsi(st)
+    assert np.allclose(lp.real, fx["logpsi_re"], atol=1e-12)
+    assert np.allclose(lp.imag, fx["logpsi_im"], atol=1e-12)
+    H = oex.tfim_1d(Hilbert(fx["N"], SPIN), 1.0, 1.0)
+    E = oest.local_energy(r, H, st)
+    assert np.allclose(E.real, fx["eloc_re"], atol=1e-12)
+
+
+def test_host_api_mirrors_reference_names():
+    for name in ("BatchedSampler", "MetropolisSampler", "LocalRule", "RBM", "NDM", "SR",
+                 "Descent", "sample_", "precondition_", "update_", "sigmax", "sigmaz", "sigmam",
+                 "liouvillian", "LocalOperator", "init_random_pars_", "HomogeneousSpin",
+                 "HomogeneousFock"):
+        assert hasattr(nq, name), name
+    s = nq.MetropolisSampler(nq.LocalRule(), 20, 20, burn=50)
+    assert s.passes == 21        # Metropolis.jl:30-38
+    with pytest.raises(ValueError):
+        nq.sigmax(nq.HomogeneousSpin(4), 5)

@@ -1,0 +1,171 @@
+"""Pins the FP64 oracle to the reference's known answers and test properties
+(CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import philox, operators as ops, networks as nw, exact, sampler as osm, stats as ost, \
+    estimators as oest, sr as osr
+from oracle.hilbert import Hilbert, SPIN, FOCK
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_philox_known_answers():
+    """Random123 known-answer vectors of Philox4x32-10."""
+    kat = json.load(open(os.path.join(GOLDEN, "philox_kat.json")))
+    for case in kat:
+        r = philox.philox4x32_10(*case["ctr"], *case["key"])
+        assert [int(x) for x in r] == case["out"]
+
+
+@pytest.mark.parametrize("kind", [SPIN, FOCK])
+def test_operator_and_liouvillian_matrices(kind):
+    """test/Operators/ising.jl:5-42: H and the Liouvillian from the row
+    tables equal independently built dense operators (N=4, g=0.7, V=2)."""
+    N, g, V = 4, 0.7, 2.0
+    h = Hilbert(N, kind)
+    H = ops.OpSum(h)
+    Ls = []
+    for i in range(N):
+        H = H + ops.sigmax(h, i).scale(g / 2)
+        Ls.append(ops.sigmam(h, i))
+    for i in range(N):
+        H = H + ops.prod(ops.sigmaz(h, i), ops.sigmaz(h, (i + 1) % N)).scale(V / 4)
+    sx = np.array([[0, 1], [1, 0]]); sz = np.diag([1.0, -1.0]); sm = np.array([[0, 0], [1, 0.0]])
+    Hq = sum(g / 2 * ops.embed(h, i, sx) for i in range(N)) + \
+        sum(V / 4 * ops.embed(h, i, sz) @ ops.embed(h, (i + 1) % N, sz) for i in range(N))
+    assert np.abs(ops.to_matrix(H) - Hq).max() < 1e-12
+    Lq = [ops.embed(h, i, sm) for i in range(N)]
+    assert np.abs(ops.liouvillian_to_matrix(ops.liouvillian(H, [])) - ops.dense_liouvillian(Hq, [])).max() < 1e-12
+    assert np.abs(ops.liouvillian_to_matrix(ops.liouvillian(ops.OpSum(h), Ls)) -
+                  ops.dense_liouvillian(0 * Hq, Lq)).max() < 1e-12
+    assert np.abs(ops.liouvillian_to_matrix(ops.liouvillian(H, Ls)) - ops.dense_liouvillian(Hq, Lq)).max() < 1e-12
+
+
+def test_row_table_conventions():
+    """Diagonal always stored (KLocalOperator.jl:76-80), σz = diag(+1,-1) on
+    local index (0,1) (SimpleOperators.jl:55-65), σ⁻ maps index 0 -> 1."""
+    h = Hilbert(2, SPIN)
+    sx = ops.sigmax(h, 0)
+    assert sx.conns[0][0][0] == 0 and sx.conns[0][0][1] == []
+    assert sx.conns[0][1][1] == [(0, 1.0)]
+    sz = ops.sigmaz(h, 1)
+    assert sz.conns[0][0][0] == 1 and sz.conns[1][0][0] == -1
+    sm = ops.sigmam(h, 0)
+    assert sm.conns[0] == [[0j, []]] and sm.conns[1][1][1] == [(0, -1.0)]
+
+
+def test_known_ground_energy_1d():
+    """examples/ising1d.jl:46-47: E0 = -1.274549484318 * 20 for
+    H = -Σσx + Σσzσz, N=20, periodic."""
+    kat = json.load(open(os.path.join(GOLDEN, "known_answers.json")))
+    e = exact.tfim_ground_energy_1d(20, 1.0, 1.0)
+    assert abs(e / 20 - kat["tfim1d_N20_h1_J1_energy_per_site"]) < 1e-9
+
+
+def test_oracle_hamiltonian_matches_lanczos_convention():
+    N = 8
+    h = Hilbert(N, SPIN)
+    H = exact.tfim_1d(h, 1.0, 1.0)
+    e_dense = np.linalg.eigvalsh(ops.to_matrix(H).real)[0]
+    assert abs(e_dense - exact.tfim_ground_energy_1d(N, 1.0, 1.0)) < 1e-9
+
+
+@pytest.mark.parametrize("act", [nw.LOGCOSH, nw.SOFTPLUS])
+def test_gradients_vs_finite_differences(act):
+    """test/Machines/test_grad.jl:108-138 (hand-written gradient == AD)."""
+    rng = np.random.default_rng(0)
+    N = 4
+    r = nw.RBM(N, 2 * N, act)
+    nw.init_random_pars(r, rng, sigma=0.2 ** 2)
+    n = nw.NDM(N, 1, 2, act)
+    nw.init_random_pars(n, rng, sigma=0.2 ** 2)
+    s = rng.choice([-1.0, 1.0], size=(3, N))
+    sr = rng.choice([0.0, 1.0], size=(3, N)); sc = rng.choice([0.0, 1.0], size=(3, N))
+    for net, f, args in ((r, r.logpsi, (s,)), (n, n.logpsi, (sr, sc))):
+        _, g = net.logpsi_and_grad(*args)
+        p = net.flat()
+        eps = 1e-6
+        for k in range(p.size):
+            q = p.copy(); q[k] += eps; net.set_flat(q); lp = f(*args)
+            q[k] -= 2 * eps; net.set_flat(q); lm = f(*args)
+            assert np.max(np.abs((lp - lm) / (2 * eps) - g[:, k])) < 1e-7
+        net.set_flat(p)
+
+
+def test_ndm_parameter_count():
+    n = nw.NDM(6, 1, 1)
+    assert n.n_params == 2 * 6 + 2 * 6 + 6 + 2 * 36 + 2 * 36
+
+
+def test_stats_matches_formula():
+    rng = np.random.default_rng(1)
+    v = rng.standard_normal((16, 10)) + 1j * rng.standard_normal((16, 10))
+    st = ost.stat_analysis(v)
+    assert abs(st["mean"] - v.mean()) < 1e-12
+    mc = v.mean(1)
+    assert abs(st["error"] - np.sqrt(np.var(mc, ddof=1) / 16)) < 1e-12
+
+
+def test_sampler_replay_is_deterministic_and_detailed_balance():
+    """χ² of the replayed local-flip chain against exact |ψ|² (N=4)."""
+    from scipy.stats import chisquare
+    rng = np.random.default_rng(5)
+    h = Hilbert(4, SPIN)
+    r = nw.RBM(4, 4, nw.LOGCOSH)
+    nw.init_random_pars(r, rng, sigma=0.2 ** 2)
+    s1, _ = osm.run(r.log_prob, h, 4096, 1, 20, 5, seed=9)
+    s2, _ = osm.run(r.log_prob, h, 4096, 1, 20, 5, seed=9)
+    np.testing.assert_array_equal(s1, s2)
+    idx = h.index_of_state(s1.reshape(-1, 4))
+    counts = np.bincount(idx, minlength=16)
+    p = exact.ket_distribution(r, h)
+    assert chisquare(counts, p * counts.sum())[1] >= 0.01
+
+
+def test_local_energy_sums_to_exact_expectation():
+    """<E_loc>_{|ψ|²} over all states equals <ψ|H|ψ>/<ψ|ψ>."""
+    rng = np.random.default_rng(2)
+    h = Hilbert(5, SPIN)
+    r = nw.RBM(5, 5, nw.LOGCOSH)
+    nw.init_random_pars(r, rng, sigma=0.3 ** 2)
+    H = exact.tfim_1d(h, 1.0, 1.0)
+    st = h.all_states()
+    E = oest.local_energy(r, H, st)
+    p = exact.ket_distribution(r, h)
+    assert abs(np.sum(p * E) - exact.exact_local_energy_expectation(r, H)) < 1e-10
+
+
+def test_liouvillian_local_values_exact():
+    """L_loc(σ,η) = (L ρ)(σ,η)/ρ(σ,η) against the dense super-operator
+    (idea of test/Problems/problem_algs.jl:23-30)."""
+    rng = np.random.default_rng(4)
+    N = 3
+    h = Hilbert(N, FOCK)
+    n = nw.NDM(N, 1, 1, nw.SOFTPLUS)
+    nw.init_random_pars(n, rng, sigma=0.3 ** 2)
+    H, Ls = exact.dissipative_ising(h, 1.0, 2.0)
+    lv = ops.liouvillian(H, Ls)
+    st = h.all_states()
+    D = h.dim
+    sr = np.repeat(st[None], D, axis=0).reshape(-1, N)
+    sc = np.repeat(st, D, axis=0)
+    rho = np.exp(n.logpsi(sr, sc))
+    Lm = ops.liouvillian_to_matrix(lv)
+    Lrho = Lm @ rho
+    L, _ = oest.local_liouvillian(n, lv, sr, sc, with_grad=False)
+    assert np.max(np.abs(L - Lrho / rho)) < 1e-9
+
+
+def test_sr_solve_matches_direct():
+    rng = np.random.default_rng(3)
+    O = rng.standard_normal((200, 12)) + 1j * rng.standard_normal((200, 12))
+    E = rng.standard_normal(200) + 0j
+    Oc, _ = oest.center(O)
+    S = osr.build_S(Oc, False)
+    F = oest.force_ket(E, O)
+    dw = osr.precondition(S, F, 0.01)
+    assert np.allclose((S + 0.01 * np.eye(12)) @ dw, F)
