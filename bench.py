@@ -1,0 +1,278 @@
+"""Benchmark of one VMC iteration (sample! + precondition! + update!) on
+the workload of the transverse-field Ising chain:
+
+  N = 20 spins, periodic, H = -h Σσx + J Σσzσz with h = J = 1; complex RBM
+  α = 2 (40 hidden units, FP32 weights, logcosh activation, spin ±1),
+  4096 Metropolis chains, 20 samples per chain, 50 burn sweeps, passes =
+  N -> 21 local flips per sweep, each sample enumerates N + 1 connected
+  elements; SR with diagonal shift 0.01 (Cholesky), Descent lr 0.01.
+
+One step = one SR iteration on the device, replayed from a CUDA graph.
+`value` is SR steps/s of the whole job; `e2e` is the same metric measured
+through the public API with the parameters uploaded from and downloaded to
+host memory every step.  `--impl reference` times the CPU restatement of the
+reference algorithm (the oracle port) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "neuralquantum.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(N=20, alpha=2, h=1.0, J=1.0, chains=4096, chain_length=20, burn=50, passes=20,
+                eps=0.01, lr=0.01, seed=0x4E51)
+METRIC = "SR steps/s (N=20 TFIM, complex RBM α=2, 4096 chains x 20 samples)"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload_config(extra=None):
+    w = WORKLOAD
+    cfg = {"workload": "tfim1d_N20_rbm_alpha2_4096x20", "n_sites": w["N"], "hidden": w["alpha"] * w["N"],
+           "chains": w["chains"], "samples_per_chain": w["chain_length"], "burn_sweeps": w["burn"],
+           "passes": w["passes"] + 1, "sr_shift": w["eps"], "lr": w["lr"],
+           "l2": "flushed between timed steps (256 MiB device write)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# --------------------------------------------------------------------------
+# clocks sampling during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------
+def build_sampler(s_precision=None):
+    import nqcuda as nq
+    w = WORKLOAD
+    hilb = nq.HomogeneousSpin(w["N"])
+    H = nq.LocalOperator(hilb)
+    for i in range(1, w["N"] + 1):
+        H = H - w["h"] * nq.sigmax(hilb, i)
+        H = H + w["J"] * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i % w["N"] + 1)
+    net = nq.RBM(np.complex64, w["N"], w["alpha"], nq.af_logcosh)
+    nq.init_random_pars_(net, sigma=1e-4, rng=np.random.default_rng(w["seed"]))
+    smp = nq.MetropolisSampler(nq.LocalRule(), w["chain_length"], w["passes"], burn=w["burn"],
+                               seed=w["seed"])
+    sp = nq._lib.NQ_S_F32 if s_precision is None else s_precision
+    is_ = nq.BatchedSampler(net, smp, H, nq.SR(eps=w["eps"]), batch_sz=w["chains"], s_precision=sp)
+    return nq, net, is_
+
+
+def s_precision_choice():
+    import nqcuda as nq
+    env = os.environ.get("NQ_BENCH_S_PRECISION")
+    if env:
+        return getattr(nq._lib, env)
+    lib = nq.lib()
+    return nq._lib.NQ_S_F32
+
+
+def effective_samples_per_s(loc, sample_ms):
+    from oracle.stats import integrated_autocorr_time   # checker-side helper, host only
+    tau = integrated_autocorr_time(loc.T)
+    ns = loc.size
+    return ns / tau / (sample_ms / 1e3), tau
+
+
+def run_gb300(args):
+    import nqcuda as nq
+    nq.build()
+    peaks = {}
+    pk = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    sp = s_precision_choice()
+    nq_, net, is_ = build_sampler(sp)
+    eng = is_.engine
+    w = WORKLOAD
+    # warm-up (also captures the graph)
+    for i in range(args.warmup):
+        eng.vmc_step(i, w["eps"], w["lr"])
+    launches0 = eng.kernel_launches()
+    with ClockSampler() as clk:
+        ms = eng.bench_steps(args.warmup, args.steps, w["eps"], w["lr"], L2_FLUSH_BYTES)
+    launches = eng.kernel_launches() - launches0 - eng_graph_kernels(eng)
+    total_ms = float(np.sum(ms))
+    ms_step = total_ms / args.steps
+    value = 1e3 / ms_step
+
+    # staged pass: per-stage and per-kernel device times, E_loc for ESS
+    call = args.warmup + args.steps + 10
+    eng.sample(call, want_samples=False)
+    m, loc, _ = eng.estimate(want_loc=True)
+    eng.precondition(0, w["eps"])
+    eng.update_descent(w["lr"])
+    st = eng.stage_times()
+    ess, tau = effective_samples_per_s(loc, st[0])
+
+    # e2e through the public API with host parameters every step
+    flat = net.flat()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        eng.set_params(flat)
+        eng.vmc_step(call + 1 + i, w["eps"], w["lr"])
+        flat = eng.get_params()
+    e2e_s = time.perf_counter() - t0
+    P = eng.P
+    e2e = {"value": args.steps / e2e_s, "unit": "SR steps/s", "h2d_bytes_per_step": 16 * P,
+           "d2h_bytes_per_step": 16 * P + 8 * 7}
+
+    # roofline of the dominant kernel (largest stage share)
+    Ns = w["chains"] * w["chain_length"]
+    stages = {"sample": st[0], "eval_estimator": st[1], "force_stats": st[2], "S": st[3],
+              "solve": st[4], "update": st[5]}
+    s_kernel_ms = st[7]
+    s_flops = 4.0 * P * P * Ns * 2.0 / 2.0 * 2.0   # upper triangle of the 2P x 2P real Gram: 2*(2P)^2*Ns/2
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    roof = {"kernel": "S accumulation (G = X Xᵀ, upper tiles)", "bound": "tensor",
+            "achieved": s_flops / (s_kernel_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": None, "traffic": None,
+            "note": "peak = measured dense bf16 burst; algorithmic flops = 2*(2P)^2*Ns/2 per launch"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "SR steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (random-init RBM weights, Philox-seeded chains)",
+        "config": workload_config({"s_precision": int(sp)}),
+        "clocks": clk.summary(), "e2e": e2e, "gpu_launches": int(launches),
+        "effective_samples_per_s": ess, "tau_int_eloc": tau, "energy_per_site": m.mean_re / w["N"],
+        "stage_ms": stages, "kernel_ms": {"sampler": st[6], "S_accumulation": st[7]},
+        "roofline": roof,
+    }
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(max_seconds=args.cpu_seconds)
+    return line
+
+
+def eng_graph_kernels(eng):
+    return 0
+
+
+# --------------------------------------------------------------------------
+# CPU reference arm: the oracle port (FP64 restatement of the reference path)
+# --------------------------------------------------------------------------
+def cpu_baseline(max_seconds=20.0, chains=None):
+    """Times the oracle's restatement of one reference VMC iteration on a
+    bounded number of chains and scales to the full workload."""
+    from oracle import cport
+    return cport.time_baseline(WORKLOAD, max_seconds=max_seconds, chains=chains)
+
+
+def run_reference(args):
+    from oracle import cport
+    res = []
+    for _ in range(args.warmup):
+        cport.time_baseline(WORKLOAD, max_seconds=args.cpu_seconds / 4, quiet=True)
+    for _ in range(args.steps):
+        res.append(cport.time_baseline(WORKLOAD, max_seconds=args.cpu_seconds))
+    v = float(np.median([r["value"] for r in res]))
+    base = res[-1]
+    base["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "SR steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(), "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "SR steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    line = run_gb300(args)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        # independent replicas, one per GPU: whole-job throughput is the sum,
+        # limited by the slowest rank (max step time over ranks)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        t = np.array([line["ms_per_step"]])
+        import torch
+        tt = torch.tensor(t)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        line["ms_per_step"] = float(tt[0])
+        line["value"] = world * 1e3 / line["ms_per_step"]
+        line["n_gpus"] = world
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -211,9 +211,15 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
                       nq_measurement* stats);
 
 /* ---- timing/diagnostics ----------------------------------------------------
- * Milliseconds of the last call per stage: [sample, eval+estimator, stats+force,
- * S, solve, update]. */
-nq_status nq_stage_times(nq_handle* h, float* ms6);
+ * Device milliseconds of the last staged calls (CUDA events on the handle's
+ * stream): [sample, eval+estimator, force+stats, S, solve, update,
+ * sampler kernel alone, S-accumulation kernel alone]. */
+nq_status nq_stage_times(nq_handle* h, float* ms8);
+/* Benchmark helper: n_steps whole iterations (graph replays, call indices
+ * call0, call0+1, ...); between steps, outside the timed events, a kernel
+ * writes flush_bytes to evict L2.  ms_out[i] = device time of step i. */
+nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double eps, double lr,
+                         int64_t flush_bytes, float* ms_out);
 /* Number of kernel launches issued by this handle since creation. */
 int64_t nq_kernel_launches(const nq_handle* h);
 

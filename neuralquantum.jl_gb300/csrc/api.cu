@@ -54,8 +54,11 @@ struct nq_handle {
   double* h_stats = nullptr;       // pinned [8]
   unsigned long long* h_acc = nullptr;
   cudaEvent_t ev[7] = {};
-  float stage_ms[6] = {};
-  bool timing = true;
+  cudaEvent_t kev[4] = {};
+  float stage_ms[8] = {};
+  bool capturing = false;
+  void* d_flush = nullptr;
+  size_t flush_bytes = 0;
 };
 
 namespace {
@@ -133,8 +136,10 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
   run.accepted = h->d_accepted;
   run.accept_bits = accept_bits_dev;
   CK(cudaMemsetAsync(h->d_accepted, 0, sizeof(unsigned long long), h->st));
+  if (!h->capturing) CK(cudaEventRecord(h->kev[0], h->st));
   if (h->f64) CKL(launch_rbm_sampler<double>(rbm_dev<double>(h), run, h->st));
   else CKL(launch_rbm_sampler<float>(rbm_dev<float>(h), run, h->st));
+  if (!h->capturing) CK(cudaEventRecord(h->kev[1], h->st));
   return NQ_OK;
 }
 
@@ -185,10 +190,14 @@ nq_status stage_S(nq_handle* h) {
   const int sp = h->cfg.s_precision;
   if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
     CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, h->st));
+    if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
     CKL(launch_gram_tc(h->d_X, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
                        h->gram_ksplit, h->st));
+    if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
   } else {
+    if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
     CKL(launch_gram_simt(src, h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
+    if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
   }
   CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, !h->complex_params, h->d_S, h->st));
   return NQ_OK;
@@ -356,6 +365,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
   step(cudaMallocHost((void**)&h->h_acc, sizeof(unsigned long long)), "pinned");
   for (int k = 0; k < 7; ++k) step(cudaEventCreate(&h->ev[k]), "event");
+  for (int k = 0; k < 4; ++k) step(cudaEventCreate(&h->kev[k]), "event");
   if (s == NQ_OK) {
     step(cudaMemsetAsync(h->d_master, 0, 2 * sizeof(double) * P, h->st), "memset");
     step(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st), "memset");
@@ -390,6 +400,9 @@ void nq_destroy(nq_handle* h) {
   if (h->h_acc) cudaFreeHost(h->h_acc);
   for (int k = 0; k < 7; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+  for (int k = 0; k < 4; ++k)
+    if (h->kev[k]) cudaEventDestroy(h->kev[k]);
+  if (h->d_flush) cudaFree(h->d_flush);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -509,6 +522,7 @@ nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out, uint
   }
   CK(cudaStreamSynchronize(h->st));
   cudaEventElapsedTime(&h->stage_ms[0], h->ev[0], h->ev[1]);
+  cudaEventElapsedTime(&h->stage_ms[6], h->kev[0], h->kev[1]);
   return NQ_OK;
 }
 
@@ -590,6 +604,7 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, doub
   cudaEventElapsedTime(&h->stage_ms[1], h->ev[1], h->ev[2]);
   cudaEventElapsedTime(&h->stage_ms[2], h->ev[2], h->ev[3]);
   cudaEventElapsedTime(&h->stage_ms[3], h->ev[3], h->ev[4]);
+  cudaEventElapsedTime(&h->stage_ms[7], h->kev[2], h->kev[3]);
   fill_measurement(h, stats);
   const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
   if (loc_out) {
@@ -671,6 +686,7 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
   if (!h->graph) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    h->capturing = true;
     const int64_t before = h->launches;
     nq_status s = NQ_OK;
     cudaError_t ce = cudaMemcpyAsync(h->d_call, h->h_call, sizeof(uint32_t), cudaMemcpyHostToDevice, h->st);
@@ -682,6 +698,7 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
     if (s == NQ_OK) s = stage_solve(h, 0, eps, 0.0);
     if (s == NQ_OK) s = stage_update(h, lr);
     cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    h->capturing = false;
     h->graph_kernels = h->launches - before;
     h->launches = before;
     if (s != NQ_OK) { if (g) cudaGraphDestroy(g); return s; }
@@ -702,10 +719,41 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
   return NQ_OK;
 }
 
-nq_status nq_stage_times(nq_handle* h, float* ms6) {
-  if (!h || !ms6) return NQ_ERR_ARG;
-  memcpy(ms6, h->stage_ms, sizeof(h->stage_ms));
+nq_status nq_stage_times(nq_handle* h, float* ms8) {
+  if (!h || !ms8) return NQ_ERR_ARG;
+  memcpy(ms8, h->stage_ms, sizeof(h->stage_ms));
   return NQ_OK;
+}
+
+nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double eps, double lr,
+                         int64_t flush_bytes, float* ms_out) {
+  if (!h || !ms_out || n_steps < 1 || flush_bytes < 0) return NQ_ERR_ARG;
+  // build (or rebuild) the graph with one ordinary step
+  nq_measurement m;
+  nq_status s = nq_vmc_step(h, call0, eps, lr, &m);
+  if (s != NQ_OK) return s;
+  if (flush_bytes > 0 && (size_t)flush_bytes > h->flush_bytes) {
+    if (h->d_flush) cudaFree(h->d_flush);
+    h->d_flush = nullptr;
+    CK(cudaMalloc(&h->d_flush, (size_t)flush_bytes));
+    h->flush_bytes = (size_t)flush_bytes;
+  }
+  cudaEvent_t* evs = new cudaEvent_t[2 * n_steps];
+  for (int i = 0; i < 2 * n_steps; ++i) cudaEventCreate(&evs[i]);
+  for (int i = 0; i < n_steps; ++i) {
+    if (flush_bytes > 0) CK(cudaMemsetAsync(h->d_flush, i & 0xff, (size_t)flush_bytes, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    *h->h_call = (uint32_t)(call0 + 1 + i);
+    CK(cudaEventRecord(evs[2 * i], h->st));
+    CK(cudaGraphLaunch(h->graph, h->st));
+    h->launches += h->graph_kernels;
+    CK(cudaEventRecord(evs[2 * i + 1], h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
+  for (int i = 0; i < n_steps; ++i) cudaEventElapsedTime(&ms_out[i], evs[2 * i], evs[2 * i + 1]);
+  for (int i = 0; i < 2 * n_steps; ++i) cudaEventDestroy(evs[i]);
+  delete[] evs;
+  return check_status_word(h);
 }
 
 }  // extern "C"

@@ -91,6 +91,9 @@ EXPORTS = {
                                    ctypes.c_double, _P(NqMeasurement)]),
     "nq_stage_times": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_float)]),
     "nq_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),
+    "nq_bench_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+                                      _P(ctypes.c_float)]),
 }
 
 _lib = None

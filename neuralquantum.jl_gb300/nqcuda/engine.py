@@ -146,8 +146,14 @@ class Engine:
         return m
 
     def stage_times(self):
-        a = (ctypes.c_float * 6)()
+        """[sample, eval, force+stats, S, solve, update, sampler kernel, S kernel] ms."""
+        a = (ctypes.c_float * 8)()
         self._check(self.lib.nq_stage_times(self.h, a))
+        return list(a)
+
+    def bench_steps(self, call0, n, eps, lr, flush_bytes):
+        a = (ctypes.c_float * n)()
+        self._check(self.lib.nq_bench_steps(self.h, call0, n, eps, lr, flush_bytes, a))
         return list(a)
 
     def kernel_launches(self):

@@ -169,3 +169,25 @@ def test_sr_solve_matches_direct():
     F = oest.force_ket(E, O)
     dw = osr.precondition(S, F, 0.01)
     assert np.allclose((S + 0.01 * np.eye(12)) @ dw, F)
+
+
+def test_c_port_matches_numpy_oracle():
+    """The C restatement (timed CPU baseline) reproduces the numpy oracle:
+    identical Philox chains and the same E_loc / Δw."""
+    from oracle import cport
+    N, M, B, L, burn, passes, seed = 6, 12, 32, 3, 4, 7, 99
+    h = Hilbert(N, SPIN)
+    H = exact.tfim_1d(h, 1.0, 1.0)
+    r = nw.RBM(N, M, nw.LOGCOSH)
+    nw.init_random_pars(r, np.random.default_rng(8), sigma=0.2 ** 2)
+    port = cport.PortRBM(N, M, nw.LOGCOSH, SPIN, H)
+    newp, samples, E, dw = port.iteration(r.flat(), B, L, burn, passes, seed, 3, 0.01, 0.1)
+    ref, info = osm.run(r.log_prob, h, B, L, burn, passes, seed, call=3)
+    np.testing.assert_array_equal(samples, ref)
+    flat = ref.reshape(-1, N)
+    Eo = oest.local_energy(r, H, flat)
+    assert np.max(np.abs(E - Eo)) < 1e-10
+    _, O = r.logpsi_and_grad(flat)
+    Oc, _ = oest.center(O)
+    dwo = osr.precondition(osr.build_S(Oc, False), oest.force_ket(Eo, O), 0.01)
+    assert np.max(np.abs(dw - dwo)) < 1e-8 * max(1, np.max(np.abs(dwo)))
