@@ -39,6 +39,7 @@ struct nq_handle {
   float* d_Gpart = nullptr;
   int gram_ksplit = 1;
   float* d_X = nullptr;
+  float* d_Xlo = nullptr;
   int Ns_pad = 0;
   double* d_S = nullptr;
   SolveBufs sb;
@@ -189,10 +190,10 @@ nq_status stage_S(nq_handle* h) {
   src.meanO = h->fb.meanO;
   const int sp = h->cfg.s_precision;
   if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
-    CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, h->st));
+    CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, sp == NQ_S_TF32X3 ? h->d_Xlo : nullptr, h->st));
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
-    CKL(launch_gram_tc(h->d_X, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
-                       h->gram_ksplit, h->st));
+    CKL(launch_gram_tc(h->d_X, h->d_Xlo, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
+                       h->gram_ksplit, h->sb.status, h->st));
     if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
   } else {
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
@@ -221,6 +222,8 @@ nq_status check_status_word(nq_handle* h) {
   CK(cudaStreamSynchronize(h->st));
   if (st != 0) {
     CK(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (st & 0x10) return fail(h, NQ_ERR_TIMEOUT, "a bounded device-side wait gave up (status 0x%x)", st);
     return fail(h, NQ_ERR_NOT_PD, "SR matrix is not positive definite after the diagonal shift");
   }
   return NQ_OK;
@@ -352,7 +355,12 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
   if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
+    h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad);
+    cudaFree(h->d_Gpart);
+    h->d_Gpart = nullptr;
+    step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
+    if (c.s_precision == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
   }
   step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
   step(dalloc(&h->sb.Lf, (size_t)P * P), "Lf");
@@ -391,7 +399,7 @@ void nq_destroy(nq_handle* h) {
   void* bufs[] = {h->d_master, h->d_p32, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
                   h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE,
-                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_S, h->sb.Lf, h->sb.x, h->sb.r,
+                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.Lf, h->sb.x, h->sb.r,
                   h->sb.rf, h->sb.status, h->d_dw};
   for (void* p : bufs)
     if (p) cudaFree(p);

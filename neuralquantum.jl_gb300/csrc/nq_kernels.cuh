@@ -82,12 +82,19 @@ struct RbmOSource {
 // upper tiles only, FP32 CUDA cores.  G is 2P x 2P row-major.
 cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* partial, int ksplit,
                              cudaStream_t st);
-// materialise X (2P x Ns_pad, row-major, zero padded) in FP32 for tcgen05
-cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, cudaStream_t st);
-// tcgen05 kind::tf32 SYRK: G = X X^T (upper tiles), split-K partials reduced.
-cudaError_t launch_gram_tc(const float* X, int rows, int Ns_pad, int split3, float* G,
-                           float* partial, int ksplit, cudaStream_t st);
+// materialise X (2P x Ns_pad, row-major, zero padded) rounded to TF32 for
+// tcgen05; if Xlo is given it receives the TF32 remainder x - tf32(x).
+cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo,
+                           cudaStream_t st);
+// tcgen05 kind::tf32 SYRK: G = X X^T (upper 128x128 tiles), split-K partials
+// [ksplit][rp][rp] (rp = rows rounded up to 128) reduced into G.  split3 adds
+// the hi*lo + lo*hi products (3xTF32).  err receives timeout status bits.
+cudaError_t launch_gram_tc(const float* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
+                           float* partial, int ksplit, int* err, cudaStream_t st);
 int gram_tc_supported();
+int gram_tc_ksplit(int rows, int Ns_pad);
+cudaError_t launch_gram_reduce(const float* partial, int rows, int rp, int tile, int ksplit, float* G,
+                               cudaStream_t st);
 // S (P x P complex double, full Hermitian) = combine(G)/Ns
 cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_params, double* S,
                               cudaStream_t st);

@@ -333,12 +333,12 @@ rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ sa
   const int P = N + M + M * N;
   const int s0 = blockIdx.x * CH;
   const int n = min(CH, Ns - s0);
-  cpx<R>* s_g = reinterpret_cast<cpx<R>*>(smem_raw);   // [M][CH]
+  cpx<R>* s_g = reinterpret_cast<cpx<R>*>(smem_raw);   // [CH][M]: consecutive h conflict-free
   cpx<R>* s_e = s_g + (size_t)M * CH;                  // [CH]
   R* s_v = reinterpret_cast<R*>(s_e + CH);             // [N][CH]
   for (int k = threadIdx.x; k < M * CH; k += blockDim.x) {
     int h = k / CH, t = k % CH;
-    s_g[k] = t < n ? g[(size_t)h * Ns + s0 + t] : mk(R(0), R(0));
+    s_g[t * M + h] = t < n ? g[(size_t)h * Ns + s0 + t] : mk(R(0), R(0));
   }
   for (int t = threadIdx.x; t < CH; t += blockDim.x) {
     uint64_t bits = t < n ? samples[s0 + t] : 0;
@@ -356,8 +356,8 @@ rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ sa
     for (int t = 0; t < n; ++t) {
       cpx<R> o;
       if (kind == 0) o = mk(s_v[j * CH + t], R(0));
-      else if (kind == 1) o = s_g[h * CH + t];
-      else o = s_v[j * CH + t] * s_g[h * CH + t];
+      else if (kind == 1) o = s_g[t * M + h];
+      else o = s_v[j * CH + t] * s_g[t * M + h];
       // Kahan
       cpx<R> y = o - co;
       cpx<R> tt = so + y;

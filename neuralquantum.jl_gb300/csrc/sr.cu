@@ -49,7 +49,10 @@ gram_simt_kernel(RbmOSource src, int rows, int nt, int ksplit, float* __restrict
   const int per = (src.Ns + ksplit - 1) / ksplit;
   const int kb = kz * per, ke = min(src.Ns, kb + per);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  float acc[4][4] = {};
+  // two-level accumulation: acc over <= 512 samples, folded into tot, keeps
+  // the FP32 rounding error independent of Ns
+  float acc[4][4] = {}, tot[4][4] = {};
+  int nk = 0;
   for (int k0 = kb; k0 < ke; k0 += GK) {
     // generate: thread -> (sample t = tid % 16, rows tid/16 + 16 q)
     {
@@ -77,7 +80,18 @@ gram_simt_kernel(RbmOSource src, int rows, int nt, int ksplit, float* __restrict
         for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
+    if (++nk == 32) {
+      nk = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { tot[i][j] += acc[i][j]; acc[i][j] = 0.f; }
+    }
   }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tot[i][j] += acc[i][j];
   // partial layout: [ksplit][rows_pad][rows_pad] with rows_pad = nt*64
   const int rp = nt * GT;
   float* dst = partial + (size_t)kz * rp * rp;
@@ -85,7 +99,7 @@ gram_simt_kernel(RbmOSource src, int rows, int nt, int ksplit, float* __restrict
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      dst[(size_t)(ti * GT + ty * 4 + i) * rp + tj * GT + tx * 4 + j] = acc[i][j];
+      dst[(size_t)(ti * GT + ty * 4 + i) * rp + tj * GT + tx * 4 + j] = tot[i][j];
 }
 
 // sum split-K partials of the upper tiles into G (rows x rows, row-major)
@@ -100,13 +114,22 @@ __global__ void gram_reduce_kernel(const float* __restrict__ partial, int rows, 
   G[idx] = s;
 }
 
-__global__ void build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X) {
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__global__ void build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X,
+                               float* __restrict__ Xlo) {
   long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (idx >= (long)rows * Ns_pad) return;
   int row = (int)(idx / Ns_pad), s = (int)(idx % Ns_pad);
   float v = 0.f;
   if (s < src.Ns) v = x_value(src, row, s, src.samples[s]);
-  X[idx] = v;
+  const float hi = to_tf32(v);
+  X[idx] = hi;
+  if (Xlo) Xlo[idx] = to_tf32(v - hi);
 }
 
 __device__ __forceinline__ float gsym(const float* G, int rows, int a, int b) {
@@ -457,9 +480,17 @@ cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* part
   return cudaGetLastError();
 }
 
-cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, cudaStream_t st) {
+cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo,
+                           cudaStream_t st) {
   long tot = 2L * P * Ns_pad;
-  build_X_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(src, 2 * P, Ns_pad, X);
+  build_X_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(src, 2 * P, Ns_pad, X, Xlo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gram_reduce(const float* partial, int rows, int rp, int tile, int ksplit, float* G,
+                               cudaStream_t st) {
+  long tot = (long)rows * rows;
+  gram_reduce_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(partial, rows, rp, tile, ksplit, G);
   return cudaGetLastError();
 }
 
