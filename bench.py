@@ -114,7 +114,7 @@ def build_sampler(s_precision=None):
     nq.init_random_pars_(net, sigma=1e-4, rng=np.random.default_rng(w["seed"]))
     smp = nq.MetropolisSampler(nq.LocalRule(), w["chain_length"], w["passes"], burn=w["burn"],
                                seed=w["seed"])
-    sp = nq._lib.NQ_S_F32 if s_precision is None else s_precision
+    sp = nq._lib.NQ_S_TF32 if s_precision is None else s_precision
     is_ = nq.BatchedSampler(net, smp, H, nq.SR(eps=w["eps"]), batch_sz=w["chains"], s_precision=sp)
     return nq, net, is_
 
@@ -124,8 +124,7 @@ def s_precision_choice():
     env = os.environ.get("NQ_BENCH_S_PRECISION")
     if env:
         return getattr(nq._lib, env)
-    lib = nq.lib()
-    return nq._lib.NQ_S_F32
+    return nq._lib.NQ_S_TF32
 
 
 def effective_samples_per_s(loc, sample_ms):
@@ -200,6 +199,7 @@ def run_gb300(args):
         "clocks": clk.summary(), "e2e": e2e, "gpu_launches": int(launches),
         "effective_samples_per_s": ess, "tau_int_eloc": tau, "energy_per_site": m.mean_re / w["N"],
         "stage_ms": stages, "kernel_ms": {"sampler": st[6], "S_accumulation": st[7]},
+        "tuning": eng.tuning(),
         "roofline": roof,
     }
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:

@@ -103,7 +103,8 @@ typedef struct {
   int32_t eval_precision;  /* nq_eval_precision */
   int32_t s_precision;     /* nq_s_precision */
   uint32_t quirks;         /* NQ_QUIRK_* bits */
-  int32_t reserved[7];
+  int32_t sampler_lanes;   /* lanes per Metropolis chain (4, 8, 16, 32); 0 = autotune */
+  int32_t reserved[6];
 } nq_config;
 
 /* Statistics of the local estimator (src/utils/stats.jl:1-50). */
@@ -212,14 +213,18 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
 
 /* ---- timing/diagnostics ----------------------------------------------------
  * Device milliseconds of the last staged calls (CUDA events on the handle's
- * stream): [sample, eval+estimator, force+stats, S, solve, update,
- * sampler kernel alone, S-accumulation kernel alone]. */
-nq_status nq_stage_times(nq_handle* h, float* ms8);
+ * stream), 12 floats: [sample, eval+estimator, force+stats, S, solve, update,
+ * sampler kernel alone, S-accumulation kernel alone, factorisation,
+ * transpose+rhs, first triangular solve, refinement]. */
+nq_status nq_stage_times(nq_handle* h, float* ms12);
 /* Benchmark helper: n_steps whole iterations (graph replays, call indices
  * call0, call0+1, ...); between steps, outside the timed events, a kernel
  * writes flush_bytes to evict L2.  ms_out[i] = device time of step i. */
 nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double eps, double lr,
                          int64_t flush_bytes, float* ms_out);
+/* Autotuned launch choices of this handle: [lanes per Metropolis chain,
+ * split-K of the S accumulation, reserved].  Tunes on first use. */
+nq_status nq_tuning(nq_handle* h, int32_t* out, int32_t n);
 /* Number of kernel launches issued by this handle since creation. */
 int64_t nq_kernel_launches(const nq_handle* h);
 

@@ -2,6 +2,9 @@
 // one VMC iteration and its CUDA-graph replay.  See include/nqcuda.h for the
 // mapping of every entry point onto the reference interface it replaces.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -35,6 +38,7 @@ struct nq_handle {
   ForceBufs fb;
   int force_nblk = 0;
   double* d_stats = nullptr;       // 6 doubles
+  double* d_chainstats = nullptr;  // [B][3] chain mean (re, im) and variance
   float* d_G = nullptr;
   float* d_Gpart = nullptr;
   int gram_ksplit = 1;
@@ -56,8 +60,10 @@ struct nq_handle {
   unsigned long long* h_acc = nullptr;
   cudaEvent_t ev[7] = {};
   cudaEvent_t kev[4] = {};
-  float stage_ms[8] = {};
+  cudaEvent_t sev[6] = {};
+  float stage_ms[12] = {};
   bool capturing = false;
+  int sampler_lanes = 0;           // lanes per chain chosen by the autotuner (0 = not tuned)
   void* d_flush = nullptr;
   size_t flush_bytes = 0;
 };
@@ -124,6 +130,55 @@ nq_status refresh_params(nq_handle* h) {
   return NQ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: picks the lanes-per-chain of the Metropolis kernel by timing
+// every instantiated candidate on a shortened schedule (a few sweeps into a
+// scratch buffer) with the handle's current parameters.  Results are cached
+// per (N, M, B, activation, Hilbert space, precision) for the process.
+// ---------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int, int, int>, int> g_tune_cache;
+
+nq_status ensure_tuned(nq_handle* h) {
+  if (h->sampler_lanes) return NQ_OK;
+  const auto key = std::make_tuple(h->N, h->M, h->B, h->act, h->hilb, h->f64 ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) { h->sampler_lanes = it->second; return NQ_OK; }
+  }
+  int cand[4];
+  const int nc = rbm_sampler_valid_lanes(h->M, cand, 4);
+  if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", h->M);
+  uint64_t* scratch = nullptr;
+  CK(cudaMalloc(&scratch, sizeof(uint64_t) * (size_t)h->B * 2));
+  SamplerRun run;
+  run.B = h->B; run.L = 1; run.burn = std::min(6, h->cfg.burn + h->L); run.passes = h->passes;
+  run.n_record = 1; run.k0 = 0x1234u; run.k1 = 0x5678u; run.call = 0xFFFFFFFFu;
+  run.samples = scratch; run.accepted = h->d_accepted;
+  int best = cand[0];
+  float best_ms = 1e30f;
+  for (int c = 0; c < nc; ++c) {
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {      // first launch warms up
+      CK(cudaEventRecord(h->kev[0], h->st));
+      cudaError_t e = h->f64 ? launch_rbm_sampler<double>(rbm_dev<double>(h), run, cand[c], h->st)
+                             : launch_rbm_sampler<float>(rbm_dev<float>(h), run, cand[c], h->st);
+      ++h->launches;
+      if (e != cudaSuccess) { cudaFree(scratch); return fail(h, NQ_ERR_CUDA, "autotune: %s", cudaGetErrorString(e)); }
+      CK(cudaEventRecord(h->kev[1], h->st));
+      CK(cudaEventSynchronize(h->kev[1]));
+      CK(cudaEventElapsedTime(&ms, h->kev[0], h->kev[1]));
+    }
+    if (ms < best_ms) { best_ms = ms; best = cand[c]; }
+  }
+  cudaFree(scratch);
+  h->sampler_lanes = best;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = best;
+  return NQ_OK;
+}
+
 nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_dev,
                        const uint32_t* call_ptr = nullptr) {
   SamplerRun run;
@@ -138,8 +193,8 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
   run.accept_bits = accept_bits_dev;
   CK(cudaMemsetAsync(h->d_accepted, 0, sizeof(unsigned long long), h->st));
   if (!h->capturing) CK(cudaEventRecord(h->kev[0], h->st));
-  if (h->f64) CKL(launch_rbm_sampler<double>(rbm_dev<double>(h), run, h->st));
-  else CKL(launch_rbm_sampler<float>(rbm_dev<float>(h), run, h->st));
+  if (h->f64) CKL(launch_rbm_sampler<double>(rbm_dev<double>(h), run, h->sampler_lanes, h->st));
+  else CKL(launch_rbm_sampler<float>(rbm_dev<float>(h), run, h->sampler_lanes, h->st));
   if (!h->capturing) CK(cudaEventRecord(h->kev[1], h->st));
   return NQ_OK;
 }
@@ -165,11 +220,11 @@ nq_status stage_force(nq_handle* h) {
   if (h->f64) {
     CKL(launch_rbm_force<double>(rbm_dev<double>(h), h->d_samples, h->Ns, (cpx<double>*)h->d_g,
                                  (cpx<double>*)h->d_eloc, h->fb, h->st));
-    CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_stats, h->st));
+    CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
   } else {
     CKL(launch_rbm_force<float>(rbm_dev<float>(h), h->d_samples, h->Ns, (cpx<float>*)h->d_g,
                                 (cpx<float>*)h->d_eloc, h->fb, h->st));
-    CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 0, h->d_stats, h->st));
+    CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
   }
   return NQ_OK;
 }
@@ -205,8 +260,10 @@ nq_status stage_S(nq_handle* h) {
 }
 
 nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
-  CKL(launch_sr_solve(h->sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, 2, h->st));
-  h->launches += 4L * ((h->P + 31) / 32) + 12;
+  SolveBufs sb = h->sb;
+  sb.ev = h->capturing ? nullptr : h->sev;
+  CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, 1, h->st));
+  h->launches += 8;
   return NQ_OK;
 }
 
@@ -312,6 +369,14 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->act = c.activation;
   h->f64 = c.eval_precision == NQ_EVAL_F64;
   h->complex_params = true;
+  if (c.sampler_lanes != 0) {
+    int cand[4];
+    const int nc = rbm_sampler_valid_lanes(c.n_hidden, cand, 4);
+    bool ok = false;
+    for (int i = 0; i < nc; ++i) ok = ok || cand[i] == c.sampler_lanes;
+    if (!ok) return bad("sampler_lanes not available for this number of hidden units");
+    h->sampler_lanes = c.sampler_lanes;
+  }
   if ((long)h->Ns * h->M > (1L << 31)) return bad("B*L*M too large");
 
   nq_status s = NQ_OK;
@@ -341,6 +406,8 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->fb.force, 2 * (size_t)P), "force");
   step(dalloc(&h->fb.meanE, 2), "meanE");
   step(dalloc(&h->d_stats, 8), "stats");
+  step(dalloc(&h->d_chainstats, 3 * (size_t)h->B), "chain stats");
+  step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
   const int rows = 2 * P;
   const int rp = ((rows + 127) / 128) * 128;
   // split-K so that the S stage fills the GPU with ~2 waves of tiles
@@ -364,16 +431,20 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   }
   step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
   step(dalloc(&h->sb.Lf, (size_t)P * P), "Lf");
+  step(dalloc(&h->sb.LT, (size_t)P * P), "LT");
   step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
   step(dalloc(&h->sb.r, 2 * (size_t)P), "r");
   step(dalloc(&h->sb.rf, (size_t)P), "rf");
   step(dalloc(&h->sb.status, 1), "status");
+  step(cudaMalloc(&h->sb.ctl, chol_ctl_bytes()), "chol ctl");
+  step(dalloc(&h->sb.Dinv, (size_t)((P + 31) / 32) * 32 * 32), "Dinv");
   h->sb.S = h->d_S;
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
   step(cudaMallocHost((void**)&h->h_acc, sizeof(unsigned long long)), "pinned");
   for (int k = 0; k < 7; ++k) step(cudaEventCreate(&h->ev[k]), "event");
   for (int k = 0; k < 4; ++k) step(cudaEventCreate(&h->kev[k]), "event");
+  for (int k = 0; k < 6; ++k) step(cudaEventCreate(&h->sev[k]), "event");
   if (s == NQ_OK) {
     step(cudaMemsetAsync(h->d_master, 0, 2 * sizeof(double) * P, h->st), "memset");
     step(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st), "memset");
@@ -398,9 +469,10 @@ void nq_destroy(nq_handle* h) {
   free_op(h);
   void* bufs[] = {h->d_master, h->d_p32, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
                   h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
-                  h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE,
-                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.Lf, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.status, h->d_dw};
+                  h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
+                  h->d_chainstats,
+                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.Lf, h->sb.LT, h->sb.x, h->sb.r,
+                  h->sb.rf, h->sb.status, h->sb.ctl, h->sb.Dinv, h->d_dw};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->h_call) cudaFreeHost(h->h_call);
@@ -410,6 +482,8 @@ void nq_destroy(nq_handle* h) {
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);
   for (int k = 0; k < 4; ++k)
     if (h->kev[k]) cudaEventDestroy(h->kev[k]);
+  for (int k = 0; k < 6; ++k)
+    if (h->sev[k]) cudaEventDestroy(h->sev[k]);
   if (h->d_flush) cudaFree(h->d_flush);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -506,6 +580,7 @@ nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
 
 nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out, uint8_t* accept_bits) {
   if (!h) return NQ_ERR_ARG;
+  if (nq_status ts = ensure_tuned(h)) return ts;
   unsigned char* d_bits = nullptr;
   size_t nbits = (size_t)h->B * h->passes * (h->cfg.burn + h->n_record);
   if (accept_bits) CK(cudaMalloc(&d_bits, nbits));
@@ -657,6 +732,7 @@ nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0, d
   CK(cudaEventRecord(h->ev[5], h->st));
   if ((s = check_status_word(h)) != NQ_OK) return s;
   cudaEventElapsedTime(&h->stage_ms[4], h->ev[4], h->ev[5]);
+  for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&h->stage_ms[8 + k], h->sev[k + 1], h->sev[k + 2]);
   if (dw_out) {
     std::vector<double> x(2 * (size_t)h->P);
     CK(cudaMemcpy(x.data(), h->sb.x, x.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -690,6 +766,7 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
     h->graph = nullptr;
   }
   CK(cudaStreamSynchronize(h->st));
+  if (nq_status ts = ensure_tuned(h)) return ts;
   *h->h_call = (uint32_t)call_index;
   if (!h->graph) {
     cudaGraph_t g = nullptr;
@@ -727,9 +804,17 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
   return NQ_OK;
 }
 
-nq_status nq_stage_times(nq_handle* h, float* ms8) {
-  if (!h || !ms8) return NQ_ERR_ARG;
-  memcpy(ms8, h->stage_ms, sizeof(h->stage_ms));
+nq_status nq_tuning(nq_handle* h, int32_t* out, int32_t n) {
+  if (!h || !out || n < 1) return NQ_ERR_ARG;
+  if (nq_status ts = ensure_tuned(h)) return ts;
+  const int32_t v[3] = {h->sampler_lanes, h->gram_ksplit, 0};
+  for (int i = 0; i < n && i < 3; ++i) out[i] = v[i];
+  return NQ_OK;
+}
+
+nq_status nq_stage_times(nq_handle* h, float* ms12) {
+  if (!h || !ms12) return NQ_ERR_ARG;
+  memcpy(ms12, h->stage_ms, sizeof(h->stage_ms));
   return NQ_OK;
 }
 

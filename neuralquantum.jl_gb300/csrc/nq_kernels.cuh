@@ -46,8 +46,11 @@ struct SamplerRun {
   unsigned long long* accepted = nullptr;      // scalar counter
   unsigned char* accept_bits = nullptr;        // nullable [steps][B]
 };
+// G = lanes per chain (4, 8, 16 or 32); rbm_sampler_valid_lanes lists the
+// values instantiated for M hidden units (used by the autotuner).
 template <typename R>
-cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st);
+cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
+int rbm_sampler_valid_lanes(int M, int* out, int max_out);
 
 // logψ, g = f'(θ) (hidden-major [M][Ns]) and the local estimator on Ns samples.
 template <typename R>
@@ -63,6 +66,7 @@ struct ForceBufs {
   double* meanO = nullptr;     // [P] complex
   double* force = nullptr;     // [P] complex
   double* meanE = nullptr;     // complex scalar
+  double* sums = nullptr;      // [4P+2] reduction scratch
 };
 int rbm_force_nblocks(int Ns, int N, int M, int csize);
 template <typename R>
@@ -103,11 +107,23 @@ cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_pa
 struct SolveBufs {
   double* S = nullptr;        // [P*P] complex (input, untouched)
   float2* Lf = nullptr;       // [P*P] complex float factor workspace
+  float2* LT = nullptr;       // [P*P] conjugate transpose of the factor
   double* x = nullptr;        // [P] complex solution
   double* r = nullptr;        // [P] complex residual
   float2* rf = nullptr;       // [P] complex float rhs workspace
   int* status = nullptr;      // device status word
+  void* ctl = nullptr;        // grid-barrier control block of the cooperative factorisation
+  float2* Dinv = nullptr;     // [ceil(P/32)][32][32] inverses of the diagonal blocks
+  cudaEvent_t* ev = nullptr;  // optional [6] events: copy, factor, transpose, solve, residual, end
 };
+size_t chol_ctl_bytes();
+// blocked Cholesky of the lower triangle of A (P x P complex float,
+// column-major) in one cooperative launch; pivots <= 0 set bit 0 of status.
+// Dinv receives the row-major inverse of every 32x32 diagonal block.
+cudaError_t launch_chol_coop(float2* A, int P, void* ctl, int* status, float2* Dinv, cudaStream_t st);
+// L y = b, Lᴴ x = y in place on rhs (P <= 6000: rhs staged in shared memory)
+cudaError_t launch_chol_solve(const float2* L, const float2* LT, const float2* Dinv, int P, float2* rhs,
+                              cudaStream_t st);
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st);
 
@@ -119,8 +135,8 @@ cudaError_t launch_descent(double* master, const double* dw, long n_doubles, dou
 // sample-major (value index s = chain + B*slot); mode 0: complex values,
 // mode 1: |value|^2 (the Liouvillian cost).
 template <typename R>
-cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* out6,
-                         cudaStream_t st);
+cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* chain_scratch,
+                         double* out6, cudaStream_t st);
 
 // bit-packed configurations <-> int8 site values (N x n column-major)
 cudaError_t launch_pack_int8(const signed char* v, int nsites, long n, int hilb, uint64_t* bits,

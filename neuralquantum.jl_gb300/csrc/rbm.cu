@@ -46,139 +46,6 @@ __global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>*
 }
 
 // ---------------------------------------------------------------------------
-// Persistent Metropolis sampler.  G lanes advance one chain; lane l owns the
-// hidden units h = l + G*k (k < HPL) and keeps θ_h and g_h = f'(θ_h) in
-// registers.  A proposal flipping site i costs HPL complex FMAs per lane
-// (ratio t0 + g*t1 per unit) plus a log2(G)-step shuffle reduction; an
-// accepted flip updates θ additively and g by the Möbius map of the
-// single-flip tables.  g is recomputed from θ at the end of every sweep, so
-// rounding drift is bounded by one sweep.
-// ---------------------------------------------------------------------------
-template <typename R, int G, int HPL, int ACT>
-__global__ void __launch_bounds__(256)
-rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = net.N, M = net.M;
-  cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
-  cpx<R>* s_t1 = s_t0 + N * M;
-  cpx<R>* s_t2 = s_t1 + N * M;
-  R* s_are = reinterpret_cast<R*>(s_t2 + N * M);      // Re a_i
-  for (int k = threadIdx.x; k < N * M; k += blockDim.x) {
-    s_t0[k] = net.t0[k];
-    s_t1[k] = net.t1[k];
-    if (ACT == ACT_LOGCOSH) s_t2[k] = net.t2[k];
-  }
-  for (int k = threadIdx.x; k < N; k += blockDim.x) s_are[k] = net.a[k].x;
-  __syncthreads();
-
-  const int lane = threadIdx.x % G;
-  const int chain_raw = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const bool active = chain_raw < run.B;
-  const int chain = active ? chain_raw : run.B - 1;
-  const int hilb = net.hilb;
-  if (run.call_ptr) run.call = *run.call_ptr;
-
-  // random initial configuration (rand!, HomogeneousSpin.jl:130-135)
-  uint64_t bits = 0;
-  for (int q = 0; q < N; q += 4) {
-    u32x4 w = philox4x32_10((uint32_t)(q >> 2), run.call, (uint32_t)chain, TAG_INIT, run.k0, run.k1);
-    uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (q + k < N && (ws[k] >> 31)) bits |= 1ull << (q + k);
-  }
-
-  cpx<R> th[HPL], g[HPL];
-  // θ = b + W v
-#pragma unroll
-  for (int k = 0; k < HPL; ++k) {
-    int h = lane + G * k;
-    th[k] = mk(R(0), R(0));
-    g[k] = mk(R(0), R(0));
-    if (h < M) {
-      cpx<R> t = net.b[h];
-      for (int j = 0; j < N; ++j) {
-        R v = site_value<R>(bits, j, hilb);
-        cpx<R> w = net.W[h + M * j];
-        t.x += w.x * v;
-        t.y += w.y * v;
-      }
-      th[k] = t;
-      g[k] = act_df<ACT>(t);
-    }
-  }
-
-  unsigned long long naccept = 0;
-  const int nsweeps = run.burn + run.n_record;
-  uint32_t t = 0;
-  for (int sweep = 0; sweep < nsweeps; ++sweep) {
-    for (int pass = 0; pass < run.passes; ++pass, ++t) {
-      u32x4 r = philox4x32_10(t, run.call, (uint32_t)chain, TAG_MH, run.k0, run.k1);
-      const int i = (int)uniform_site(r.x, (uint32_t)N);
-      const R u = (R)uniform24(r.y);
-      const int bit = (int)((bits >> i) & 1ull);
-      R dv;
-      if (hilb == HILB_SPIN) dv = bit ? R(-2) : R(2);
-      else dv = bit ? R(-1) : R(1);
-      const bool pos = dv > 0;
-      R prod = R(1);
-#pragma unroll
-      for (int k = 0; k < HPL; ++k) {
-        int h = lane + G * k;
-        if (h < M) {
-          cpx<R> rr;
-          if (ACT == ACT_LOGCOSH) {
-            cpx<R> c1 = s_t1[i * M + h];
-            if (!pos) c1 = mk(-c1.x, -c1.y);
-            rr = cfma(g[k], c1, s_t0[i * M + h]);
-          } else {
-            cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
-            rr = cfma(g[k], bb, mk(R(1), R(0)));
-          }
-          prod *= abs2c(rr);
-        }
-      }
-      R lsum = r_log(prod);
-#pragma unroll
-      for (int off = G / 2; off > 0; off >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
-      const R logA = R(2) * s_are[i] * dv + lsum;
-      const bool acc = (logA >= R(0)) || (u < r_exp(logA));
-      if (acc) {
-#pragma unroll
-        for (int k = 0; k < HPL; ++k) {
-          int h = lane + G * k;
-          if (h < M) {
-            cpx<R> w = net.W[h + M * i];
-            th[k].x += w.x * dv;
-            th[k].y += w.y * dv;
-            if (ACT == ACT_LOGCOSH) {
-              cpx<R> tau = s_t2[i * M + h];
-              if (!pos) tau = mk(-tau.x, -tau.y);
-              g[k] = divc(g[k] + tau, cfma(g[k], tau, mk(R(1), R(0))));
-            } else {
-              cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
-              cpx<R> num = g[k] * mk(R(1) + bb.x, bb.y);
-              g[k] = divc(num, cfma(g[k], bb, mk(R(1), R(0))));
-            }
-          }
-        }
-        bits ^= 1ull << i;
-        ++naccept;
-      }
-      if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = acc ? 1 : 0;
-    }
-    // end of sweep: record and resynchronise g with θ
-    const int slot = sweep - run.burn;
-    if (slot >= 0 && active && lane == 0) run.samples[(size_t)slot * run.B + chain] = bits;
-#pragma unroll
-    for (int k = 0; k < HPL; ++k)
-      if (lane + G * k < M) g[k] = act_df<ACT>(th[k]);
-  }
-  if (run.write_last_at_end && active && lane == 0) run.samples[chain] = bits;
-  if (active && lane == 0) atomicAdd(run.accepted, naccept);
-}
-
-// ---------------------------------------------------------------------------
 // Batched evaluation, one thread per sample: θ = Wσ + b, logψ = aᵀσ + Σ f(θ),
 // g = f'(θ) and, if an operator is given, the local estimator
 //   E_loc(σ) = Σ_diag mel + Σ_{σ'≠σ} mel ψ(σ')/ψ(σ)
@@ -379,31 +246,51 @@ rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ sa
   }
 }
 
-// F = ΣE conj(O)/Ns - <E> conj(<O>),  <O> = ΣO/Ns   (FP64, fixed order)
-__global__ void force_reduce_kernel(int P, int nblk, int Ns, const double* __restrict__ partial,
-                                    const double* __restrict__ partialE, double* meanO,
-                                    double* force, double* meanE) {
-  __shared__ double sE[2];
-  if (threadIdx.x == 0) {
-    double ex = 0, ey = 0;
-    for (int b = 0; b < nblk; ++b) { ex += partialE[2 * b]; ey += partialE[2 * b + 1]; }
-    sE[0] = ex / Ns; sE[1] = ey / Ns;
-    if (blockIdx.x == 0) { meanE[0] = sE[0]; meanE[1] = sE[1]; }
+// Deterministic FP64 reduction of the per-chunk partials: one warp per
+// parameter (index P carries ΣE), lanes stride over chunks, fixed-order
+// shuffle tree.  sums[0..2P) = ΣO, [2P..4P) = ΣE conj(O), [4P..4P+2) = ΣE.
+__global__ void force_sums_kernel(int P, int nblk, const double* __restrict__ partial,
+                                  const double* __restrict__ partialE, double* __restrict__ sums) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w > P) return;
+  double a = 0, b = 0, c = 0, d = 0;
+  if (w < P) {
+    for (int k = lane; k < nblk; k += 32) {
+      const double* src = partial + (size_t)k * 4 * P;
+      a += src[2 * w]; b += src[2 * w + 1];
+      c += src[2 * P + 2 * w]; d += src[2 * P + 2 * w + 1];
+    }
+  } else {
+    for (int k = lane; k < nblk; k += 32) { a += partialE[2 * k]; b += partialE[2 * k + 1]; }
   }
-  __syncthreads();
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    b += __shfl_xor_sync(0xffffffffu, b, off);
+    c += __shfl_xor_sync(0xffffffffu, c, off);
+    d += __shfl_xor_sync(0xffffffffu, d, off);
+  }
+  if (lane == 0) {
+    if (w < P) {
+      sums[2 * w] = a; sums[2 * w + 1] = b;
+      sums[2 * P + 2 * w] = c; sums[2 * P + 2 * w + 1] = d;
+    } else {
+      sums[4 * P] = a; sums[4 * P + 1] = b;
+    }
+  }
+}
+
+// <O> = ΣO/Ns, <E> = ΣE/Ns, F = ΣE conj(O)/Ns - <E> conj(<O>)
+__global__ void force_finalize_kernel(int P, int Ns, const double* __restrict__ sums, double* meanO,
+                                      double* force, double* meanE) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const double ex = sums[4 * P] / Ns, ey = sums[4 * P + 1] / Ns;
+  if (p == 0) { meanE[0] = ex; meanE[1] = ey; }
   if (p >= P) return;
-  double ox = 0, oy = 0, fx = 0, fy = 0;
-  for (int b = 0; b < nblk; ++b) {
-    const double* src = partial + (size_t)b * 4 * P;
-    ox += src[2 * p]; oy += src[2 * p + 1];
-    fx += src[2 * P + 2 * p]; fy += src[2 * P + 2 * p + 1];
-  }
-  ox /= Ns; oy /= Ns; fx /= Ns; fy /= Ns;
+  const double ox = sums[2 * p] / Ns, oy = sums[2 * p + 1] / Ns;
+  double fx = sums[2 * P + 2 * p] / Ns, fy = sums[2 * P + 2 * p + 1] / Ns;
   meanO[2 * p] = ox; meanO[2 * p + 1] = oy;
-  // - <E> conj(<O>)
-  fx -= sE[0] * ox + sE[1] * oy;
-  fy -= sE[1] * ox - sE[0] * oy;
+  fx -= ex * ox + ey * oy;
+  fy -= ey * ox - ex * oy;
   force[2 * p] = fx; force[2 * p + 1] = fy;
 }
 
@@ -464,46 +351,6 @@ cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<
   int n = net.N * net.M;
   rbm_tables_kernel<R><<<(n + 127) / 128, 128, 0, st>>>(net, t0, t1, t2);
   return cudaGetLastError();
-}
-
-template <typename R, int G, int HPL, int ACT>
-static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
-  const int threads = 256;
-  const int chains_per_block = threads / G;
-  const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
-  size_t smem = (size_t)3 * net.N * net.M * sizeof(cpx<R>) + net.N * sizeof(R);
-  auto kern = rbm_sampler_kernel<R, G, HPL, ACT>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  kern<<<blocks, threads, smem, st>>>(net, run);
-  return cudaGetLastError();
-}
-
-template <typename R, int G, int ACT>
-static cudaError_t sampler_hpl(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
-  const int hpl = (net.M + G - 1) / G;
-  switch (hpl) {
-    case 1: return sampler_inst<R, G, 1, ACT>(net, run, st);
-    case 2: return sampler_inst<R, G, 2, ACT>(net, run, st);
-    case 3: return sampler_inst<R, G, 3, ACT>(net, run, st);
-    case 4: return sampler_inst<R, G, 4, ACT>(net, run, st);
-    case 5: return sampler_inst<R, G, 5, ACT>(net, run, st);
-    case 6: return sampler_inst<R, G, 6, ACT>(net, run, st);
-    case 7: return sampler_inst<R, G, 7, ACT>(net, run, st);
-    case 8: return sampler_inst<R, G, 8, ACT>(net, run, st);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-template <typename R>
-cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
-  if (net.N > 64 || net.M > 256) return cudaErrorInvalidValue;
-  const bool small = net.M <= 64;
-  if (net.act == ACT_LOGCOSH)
-    return small ? sampler_hpl<R, 8, ACT_LOGCOSH>(net, run, st) : sampler_hpl<R, 32, ACT_LOGCOSH>(net, run, st);
-  return small ? sampler_hpl<R, 8, ACT_SOFTPLUS>(net, run, st) : sampler_hpl<R, 32, ACT_SOFTPLUS>(net, run, st);
 }
 
 static int eval_threads(int M, size_t csize) {
@@ -567,8 +414,8 @@ cudaError_t launch_rbm_force(const RbmDev<R>& net, const uint64_t* samples, int 
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int P = net.N + net.M + net.M * net.N;
-  force_reduce_kernel<<<(P + 127) / 128, 128, 0, st>>>(P, nblk, Ns, fb.partial, fb.partialE,
-                                                        fb.meanO, fb.force, fb.meanE);
+  force_sums_kernel<<<(32 * (P + 1) + 255) / 256, 256, 0, st>>>(P, nblk, fb.partial, fb.partialE, fb.sums);
+  force_finalize_kernel<<<(P + 255) / 256, 256, 0, st>>>(P, Ns, fb.sums, fb.meanO, fb.force, fb.meanE);
   return cudaGetLastError();
 }
 
@@ -596,8 +443,6 @@ cudaError_t launch_unpack_int8(const uint64_t* bits, int nsites, long n, int hil
 // explicit instantiations
 template cudaError_t launch_rbm_tables<float>(const RbmDev<float>&, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
 template cudaError_t launch_rbm_tables<double>(const RbmDev<double>&, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
-template cudaError_t launch_rbm_sampler<float>(const RbmDev<float>&, const SamplerRun&, cudaStream_t);
-template cudaError_t launch_rbm_sampler<double>(const RbmDev<double>&, const SamplerRun&, cudaStream_t);
 template cudaError_t launch_rbm_eval<float>(const RbmDev<float>&, const uint64_t*, int, const DevOp*, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
 template cudaError_t launch_rbm_eval<double>(const RbmDev<double>&, const uint64_t*, int, const DevOp*, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
 template cudaError_t launch_rbm_force<float>(const RbmDev<float>&, const uint64_t*, int, const cpx<float>*, const cpx<float>*, const ForceBufs&, cudaStream_t);

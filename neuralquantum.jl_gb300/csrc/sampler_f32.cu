@@ -1,0 +1,14 @@
+// FP32 instantiations of the Metropolis sampler (see sampler_impl.cuh).
+#include "sampler_impl.cuh"
+
+int rbm_sampler_valid_lanes(int M, int* out, int max_out) {
+  const int cand[4] = {4, 8, 16, 32};
+  int n = 0;
+  for (int c : cand) {
+    const int hpl = (M + c - 1) / c;
+    if (hpl_ok(hpl) && n < max_out) out[n++] = c;
+  }
+  return n;
+}
+
+template cudaError_t launch_rbm_sampler<float>(const RbmDev<float>&, const SamplerRun&, int, cudaStream_t);

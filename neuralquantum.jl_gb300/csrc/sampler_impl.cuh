@@ -1,0 +1,219 @@
+// Persistent Metropolis sampler for the RBM (local-flip rule) with an
+// incremental θ-cache.  Reference: src/Samplers/Metropolis.jl:101-167,
+// src/Samplers/MCMCRules/LocalRule.jl:19-28, flipat! of
+// src/Hilbert/HomogeneousSpin.jl:95-104 and HomogeneousFock.jl:72-81.
+#pragma once
+#include "nq_kernels.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Persistent Metropolis sampler.  G lanes advance one chain; lane l owns the
+// hidden units h = l + G*k (k < HPL) and keeps θ_h and g_h = f'(θ_h) in
+// registers.  A proposal flipping site i costs HPL complex FMAs per lane
+// (ratio t0 + g*t1 per unit, tables in shared memory) plus a log2(G)-step
+// shuffle reduction of log2|ratio|^2; an accepted flip updates θ additively
+// and g by the Möbius map of the single-flip tables.  g is recomputed from θ
+// at the end of every sweep, so rounding drift is bounded by one sweep.
+// Random draws are software-pipelined: every G steps each lane evaluates the
+// Philox block of one upcoming step and the chain's lanes broadcast (site, u)
+// by shuffle when the step is reached.
+// ---------------------------------------------------------------------------
+template <typename R> NQ_D R fast_log2(R x) { return log2(x); }
+template <> NQ_D float fast_log2<float>(float x) { return __log2f(x); }
+template <typename R> NQ_D R fast_rcp(R x) { return R(1) / x; }
+template <> NQ_D float fast_rcp<float>(float x) { return __frcp_rn(x); }
+
+template <typename R, int G, int HPL, int ACT>
+__global__ void __launch_bounds__(256)
+rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = net.N, M = net.M;
+  cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* s_t1 = s_t0 + N * M;
+  cpx<R>* s_t2 = s_t1 + N * M;
+  cpx<R>* s_w = s_t2 + N * M;                          // W[h, i] at i*M + h
+  R* s_are = reinterpret_cast<R*>(s_w + N * M);      // 2 Re a_i log2(e)
+  for (int k = threadIdx.x; k < N * M; k += blockDim.x) {
+    s_t0[k] = net.t0[k];
+    s_t1[k] = net.t1[k];
+    if (ACT == ACT_LOGCOSH) s_t2[k] = net.t2[k];
+    const int i = k / M, h = k % M;
+    s_w[k] = net.W[h + M * i];
+  }
+  for (int k = threadIdx.x; k < N; k += blockDim.x) s_are[k] = R(2.8853900817779268) * net.a[k].x;
+  __syncthreads();
+
+  const int lane = threadIdx.x % G;
+  const int chain_raw = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const bool active = chain_raw < run.B;
+  const int chain = active ? chain_raw : run.B - 1;
+  const int hilb = net.hilb;
+  if (run.call_ptr) run.call = *run.call_ptr;
+
+  // random initial configuration (rand!, HomogeneousSpin.jl:130-135)
+  uint64_t bits = 0;
+  for (int q = 0; q < N; q += 4) {
+    u32x4 w = philox4x32_10((uint32_t)(q >> 2), run.call, (uint32_t)chain, TAG_INIT, run.k0, run.k1);
+    uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (q + k < N && (ws[k] >> 31)) bits |= 1ull << (q + k);
+  }
+
+  cpx<R> th[HPL], g[HPL];
+#pragma unroll
+  for (int k = 0; k < HPL; ++k) {
+    const int h = lane + G * k;
+    th[k] = mk(R(0), R(0));
+    g[k] = mk(R(0), R(0));
+    if (h < M) {
+      cpx<R> t = net.b[h];
+      for (int j = 0; j < N; ++j) {
+        const R v = site_value<R>(bits, j, hilb);
+        const cpx<R> w = s_w[j * M + h];
+        t.x += w.x * v;
+        t.y += w.y * v;
+      }
+      th[k] = t;
+      g[k] = act_df<ACT>(t);
+    }
+  }
+
+  unsigned long long naccept = 0;
+  const int nsweeps = run.burn + run.n_record;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
+  uint32_t t = 0;
+  int my_site = 0;
+  R my_lu = 0;
+  for (int sweep = 0; sweep < nsweeps; ++sweep) {
+    for (int pass = 0; pass < run.passes; ++pass, ++t) {
+      const int slot = (int)(t & (G - 1));
+      if (slot == 0) {
+        const u32x4 r = philox4x32_10(t + (uint32_t)lane, run.call, (uint32_t)chain, TAG_MH, run.k0, run.k1);
+        my_site = (int)uniform_site(r.x, (uint32_t)N);
+        my_lu = fast_log2((R)uniform24(r.y));       // log2 u; u = 0 -> -inf (always accept)
+      }
+      const int i = __shfl_sync(gmask, my_site, slot, G);
+      const R lu = __shfl_sync(gmask, my_lu, slot, G);
+      const int bit = (int)((bits >> i) & 1ull);
+      R dv;
+      if (hilb == HILB_SPIN) dv = bit ? R(-2) : R(2);
+      else dv = bit ? R(-1) : R(1);
+      const bool pos = dv > 0;
+      R prod = R(1);
+#pragma unroll
+      for (int k = 0; k < HPL; ++k) {
+        const int h = lane + G * k;
+        if (h < M) {
+          cpx<R> rr;
+          if (ACT == ACT_LOGCOSH) {
+            cpx<R> c1 = s_t1[i * M + h];
+            if (!pos) c1 = mk(-c1.x, -c1.y);
+            rr = cfma(g[k], c1, s_t0[i * M + h]);
+          } else {
+            const cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
+            rr = cfma(g[k], bb, mk(R(1), R(0)));
+          }
+          prod *= abs2c(rr);
+        }
+      }
+      R lsum = fast_log2(prod);
+#pragma unroll
+      for (int off = G / 2; off > 0; off >>= 1) lsum += __shfl_xor_sync(gmask, lsum, off, G);
+      const R logA = s_are[i] * dv + lsum;                  // log2 of the acceptance ratio
+      const bool acc = lu < logA;
+      if (acc) {
+#pragma unroll
+        for (int k = 0; k < HPL; ++k) {
+          const int h = lane + G * k;
+          if (h < M) {
+            const cpx<R> w = s_w[i * M + h];
+            th[k].x += w.x * dv;
+            th[k].y += w.y * dv;
+            cpx<R> num, den;
+            if (ACT == ACT_LOGCOSH) {
+              cpx<R> tau = s_t2[i * M + h];
+              if (!pos) tau = mk(-tau.x, -tau.y);
+              num = g[k] + tau;
+              den = cfma(g[k], tau, mk(R(1), R(0)));
+            } else {
+              const cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
+              num = g[k] * mk(R(1) + bb.x, bb.y);
+              den = cfma(g[k], bb, mk(R(1), R(0)));
+            }
+            const R inv = fast_rcp(abs2c(den));
+            g[k] = inv * (num * conjc(den));
+          }
+        }
+        bits ^= 1ull << i;
+        ++naccept;
+      }
+      if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = acc ? 1 : 0;
+    }
+    // end of sweep: record and resynchronise g with θ
+    const int slot = sweep - run.burn;
+    if (slot >= 0 && active && lane == 0) run.samples[(size_t)slot * run.B + chain] = bits;
+#pragma unroll
+    for (int k = 0; k < HPL; ++k)
+      if (lane + G * k < M) g[k] = act_df<ACT>(th[k]);
+  }
+  if (run.write_last_at_end && active && lane == 0) run.samples[chain] = bits;
+  if (active && lane == 0) atomicAdd(run.accepted, naccept);
+}
+
+}  // namespace
+
+template <typename R, int G, int HPL, int ACT>
+static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
+  const int threads = 256;
+  const int chains_per_block = threads / G;
+  const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
+  size_t smem = (size_t)4 * net.N * net.M * sizeof(cpx<R>) + net.N * sizeof(R);
+  auto kern = rbm_sampler_kernel<R, G, HPL, ACT>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<blocks, threads, smem, st>>>(net, run);
+  return cudaGetLastError();
+}
+
+template <typename R, int G, int ACT>
+static cudaError_t sampler_hpl(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
+  const int hpl = (net.M + G - 1) / G;
+  switch (hpl) {
+    case 1: return sampler_inst<R, G, 1, ACT>(net, run, st);
+    case 2: return sampler_inst<R, G, 2, ACT>(net, run, st);
+    case 3: return sampler_inst<R, G, 3, ACT>(net, run, st);
+    case 4: return sampler_inst<R, G, 4, ACT>(net, run, st);
+    case 5: return sampler_inst<R, G, 5, ACT>(net, run, st);
+    case 6: return sampler_inst<R, G, 6, ACT>(net, run, st);
+    case 8: return sampler_inst<R, G, 8, ACT>(net, run, st);
+    case 10: return sampler_inst<R, G, 10, ACT>(net, run, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R, int ACT>
+static cudaError_t sampler_g(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st) {
+  switch (G) {
+    case 4: return sampler_hpl<R, 4, ACT>(net, run, st);
+    case 8: return sampler_hpl<R, 8, ACT>(net, run, st);
+    case 16: return sampler_hpl<R, 16, ACT>(net, run, st);
+    case 32: return sampler_hpl<R, 32, ACT>(net, run, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// hidden units per lane supported by the instantiations above
+static inline bool hpl_ok(int hpl) { return hpl <= 6 || hpl == 8 || hpl == 10; }
+
+template <typename R>
+cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st) {
+  if (net.N > 64 || net.M > 320) return cudaErrorInvalidValue;
+  if (!hpl_ok((net.M + G - 1) / G)) return cudaErrorInvalidValue;
+  if (net.act == ACT_LOGCOSH) return sampler_g<R, ACT_LOGCOSH>(net, run, G, st);
+  return sampler_g<R, ACT_SOFTPLUS>(net, run, G, st);
+}
+

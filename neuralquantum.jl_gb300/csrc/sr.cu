@@ -173,7 +173,6 @@ __global__ void shift_copy_kernel(const double* __restrict__ S, int P, int kind,
   Lf[idx] = make_float2((float)re, (float)im);
 }
 
-constexpr int CB = 32;   // Cholesky block size
 
 __device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -182,153 +181,21 @@ __device__ __forceinline__ float2 f2mulconj(float2 a, float2 b) {  // a * conj(b
   return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 
-// factor the nb x nb diagonal block at k0 in shared memory
-__global__ void __launch_bounds__(1024) potrf_diag_kernel(float2* A, int P, int k0, int nb, int* status) {
-  __shared__ float2 D[CB][CB + 1];
-  const int tid = threadIdx.x;
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    int i = e % nb, j = e / nb;
-    D[i][j] = A[(size_t)(k0 + i) + (size_t)P * (k0 + j)];
+// LT = Lᴴ (column-major) for coalesced backward substitution
+__global__ void conj_transpose_kernel(const float2* __restrict__ L, int P, float2* __restrict__ LT) {
+  __shared__ float2 t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    int row = by + r, col = bx + threadIdx.x;       // read L[col + P*row] coalesced over col
+    if (row < P && col < P) t[r][threadIdx.x] = L[(size_t)col + (size_t)P * row];
   }
   __syncthreads();
-  for (int j = 0; j < nb; ++j) {
-    __shared__ float piv;
-    if (tid == 0) {
-      float d = D[j][j].x;
-      if (!(d > 0.f)) { atomicExch(status, 1); d = 1.0f; }
-      piv = sqrtf(d);
-      D[j][j] = make_float2(piv, 0.f);
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    int row = bx + r, col = by + threadIdx.x;        // LT[col + P*row] = conj(L[row + P*col])
+    if (row < P && col < P) {
+      float2 v = t[threadIdx.x][r];
+      LT[(size_t)col + (size_t)P * row] = make_float2(v.x, -v.y);
     }
-    __syncthreads();
-    const float inv = 1.0f / piv;
-    for (int i = j + 1 + tid; i < nb; i += blockDim.x) D[i][j] = make_float2(D[i][j].x * inv, D[i][j].y * inv);
-    __syncthreads();
-    // trailing update of the lower part: D[i][c] -= D[i][j] conj(D[c][j]), i >= c > j
-    const int m = nb - j - 1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      int i = j + 1 + e % m, c = j + 1 + e / m;
-      if (i >= c) {
-        float2 p = f2mulconj(D[i][j], D[c][j]);
-        D[i][c].x -= p.x;
-        D[i][c].y -= p.y;
-      }
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    int i = e % nb, j = e / nb;
-    if (i >= j) A[(size_t)(k0 + i) + (size_t)P * (k0 + j)] = D[i][j];
-  }
-}
-
-// rows i >= k0+nb of the panel: X L_kkᴴ = A_ik  (forward substitution per row)
-__global__ void __launch_bounds__(128) trsm_panel_kernel(float2* A, int P, int k0, int nb) {
-  __shared__ float2 Lk[CB][CB + 1];
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int i = e % nb, j = e / nb;
-    Lk[i][j] = A[(size_t)(k0 + i) + (size_t)P * (k0 + j)];
-  }
-  __syncthreads();
-  const int i = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P) return;
-  float2 x[CB];
-#pragma unroll
-  for (int j = 0; j < CB; ++j) {
-    if (j < nb) {
-      float2 a = A[(size_t)i + (size_t)P * (k0 + j)];
-      for (int p = 0; p < j; ++p) {
-        float2 q = f2mulconj(x[p], Lk[j][p]);
-        a.x -= q.x;
-        a.y -= q.y;
-      }
-      const float inv = 1.0f / Lk[j][j].x;
-      x[j] = make_float2(a.x * inv, a.y * inv);
-      A[(size_t)i + (size_t)P * (k0 + j)] = x[j];
-    }
-  }
-}
-
-// trailing update A[i][j] -= Σ_p L[i][k0+p] conj(L[j][k0+p]) on lower tiles of
-// the trailing matrix (rows/cols >= t0 = k0 + nb), 32x32 tiles, 256 threads
-__global__ void __launch_bounds__(256) herk_update_kernel(float2* A, int P, int k0, int nb, int t0, int ntt) {
-  __shared__ float2 Li[CB][CB + 1];
-  __shared__ float2 Lj[CB][CB + 1];
-  int ti, tj;
-  {
-    // lower tiles enumerated column by column: (0,0),(1,0),..,(ntt-1,0),(1,1),...
-    int c = 0, rem = blockIdx.x;
-    while (rem >= ntt - c) { rem -= ntt - c; ++c; }
-    tj = c; ti = c + rem;
-  }
-  const int r0 = t0 + ti * CB, c0 = t0 + tj * CB;
-  for (int e = threadIdx.x; e < CB * nb; e += blockDim.x) {
-    int r = e % CB, p = e / CB;
-    int gi = r0 + r, gj = c0 + r;
-    Li[r][p] = gi < P ? A[(size_t)gi + (size_t)P * (k0 + p)] : make_float2(0.f, 0.f);
-    Lj[r][p] = gj < P ? A[(size_t)gj + (size_t)P * (k0 + p)] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  const int tr = threadIdx.x % CB, tc4 = threadIdx.x / CB;   // 8 column groups of 4
-  for (int q = 0; q < 4; ++q) {
-    int c = tc4 * 4 + q;
-    int gi = r0 + tr, gj = c0 + c;
-    if (gi >= P || gj >= P || gi < gj) continue;
-    float2 s = make_float2(0.f, 0.f);
-    for (int p = 0; p < nb; ++p) {
-      float2 m = f2mulconj(Li[tr][p], Lj[c][p]);
-      s.x += m.x;
-      s.y += m.y;
-    }
-    float2* a = A + (size_t)gi + (size_t)P * gj;
-    a->x -= s.x;
-    a->y -= s.y;
-  }
-}
-
-// single-block triangular solves with the FP32 factor: L y = b, Lᴴ x = y
-__global__ void __launch_bounds__(1024) trsv_kernel(const float2* __restrict__ L, int P, float2* b) {
-  __shared__ float2 xj;
-  for (int j = 0; j < P; ++j) {
-    if (threadIdx.x == 0) {
-      float2 v = b[j];
-      float inv = 1.0f / L[(size_t)j + (size_t)P * j].x;
-      xj = make_float2(v.x * inv, v.y * inv);
-      b[j] = xj;
-    }
-    __syncthreads();
-    float2 x = xj;
-    for (int i = j + 1 + threadIdx.x; i < P; i += blockDim.x) {
-      float2 m = f2mul(L[(size_t)i + (size_t)P * j], x);
-      b[i].x -= m.x;
-      b[i].y -= m.y;
-    }
-    __syncthreads();
-  }
-  // backward: x_j = (y_j - Σ_{i>j} conj(L[i][j]) x_i) / L_jj
-  __shared__ float red[2][32];
-  for (int j = P - 1; j >= 0; --j) {
-    float sx = 0.f, sy = 0.f;
-    for (int i = j + 1 + threadIdx.x; i < P; i += blockDim.x) {
-      float2 l = L[(size_t)i + (size_t)P * j];
-      float2 x = b[i];
-      // conj(l) * x
-      sx += l.x * x.x + l.y * x.y;
-      sy += l.x * x.y - l.y * x.x;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, off);
-      sy += __shfl_xor_sync(0xffffffffu, sy, off);
-    }
-    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = sx; red[1][threadIdx.x >> 5] = sy; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float tx = 0.f, ty = 0.f;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { tx += red[0][w]; ty += red[1][w]; }
-      float2 y = b[j];
-      float inv = 1.0f / L[(size_t)j + (size_t)P * j].x;
-      b[j] = make_float2((y.x - tx) * inv, (y.y - ty) * inv);
-    }
-    __syncthreads();
   }
 }
 
@@ -415,44 +282,50 @@ __device__ void block_sum2(double& a, double& b, double* sh) {
   a = sh[64]; b = sh[65];
 }
 
+// pass 1 (one thread per chain): chain mean μ_c and unbiased variance var_c
 template <typename R>
-__global__ void __launch_bounds__(1024) stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
-                                                     double* __restrict__ out) {
+__global__ void chain_stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
+                                   double* __restrict__ cs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= B) return;
+  double mx = 0, my = 0;
+  for (int l = 0; l < L; ++l) { cpx<double> x = stat_val(v, c + (long)B * l, mode); mx += x.x; my += x.y; }
+  mx /= L; my /= L;
+  double vv = 0;
+  for (int l = 0; l < L; ++l) {
+    cpx<double> x = stat_val(v, c + (long)B * l, mode);
+    vv += (x.x - mx) * (x.x - mx) + (x.y - my) * (x.y - my);
+  }
+  cs[3 * c] = mx;
+  cs[3 * c + 1] = my;
+  cs[3 * c + 2] = L > 1 ? vv / (L - 1) : 0.0;
+}
+
+// pass 2 (one block): μ = mean μ_c; var_μ_ch = Σ|μ_c-μ|²/(B-1);
+// var_μ = Σ_c[(L-1) var_c + L|μ_c-μ|²]/(BL-1) (= var of all values about μ);
+// variance = mean var_c; t = var_μ_ch/var_μ (stats.jl:26-50)
+__global__ void __launch_bounds__(1024) stats_final_kernel(const double* __restrict__ cs, int B, int L,
+                                                           double* __restrict__ out) {
   __shared__ double sh[66];
-  // pass 1: μ = mean of chain means, mean of chain variances
   double smx = 0, smy = 0, svar = 0, dummy = 0;
   for (int c = threadIdx.x; c < B; c += blockDim.x) {
-    double mx = 0, my = 0;
-    for (int l = 0; l < L; ++l) { cpx<double> x = stat_val(v, c + (long)B * l, mode); mx += x.x; my += x.y; }
-    mx /= L; my /= L;
-    double vv = 0;
-    for (int l = 0; l < L; ++l) {
-      cpx<double> x = stat_val(v, c + (long)B * l, mode);
-      vv += (x.x - mx) * (x.x - mx) + (x.y - my) * (x.y - my);
-    }
-    svar += L > 1 ? vv / (L - 1) : 0.0;
-    smx += mx; smy += my;
+    smx += cs[3 * c]; smy += cs[3 * c + 1]; svar += cs[3 * c + 2];
   }
   block_sum2(smx, smy, sh);
   block_sum2(svar, dummy, sh);
   const double mux = smx / B, muy = smy / B;
-  // pass 2: variance of chain means and of all values around μ
   double vmc = 0, vall = 0;
   for (int c = threadIdx.x; c < B; c += blockDim.x) {
-    double mx = 0, my = 0;
-    for (int l = 0; l < L; ++l) {
-      cpx<double> x = stat_val(v, c + (long)B * l, mode);
-      mx += x.x; my += x.y;
-      vall += (x.x - mux) * (x.x - mux) + (x.y - muy) * (x.y - muy);
-    }
-    mx /= L; my /= L;
-    vmc += (mx - mux) * (mx - mux) + (my - muy) * (my - muy);
+    const double dx = cs[3 * c] - mux, dy = cs[3 * c + 1] - muy;
+    const double d2 = dx * dx + dy * dy;
+    vmc += d2;
+    vall += (L - 1) * cs[3 * c + 2] + L * d2;
   }
   block_sum2(vmc, vall, sh);
   if (threadIdx.x == 0) {
-    double var_mu_ch = vmc / (B - 1);
-    double var_mu = vall / ((double)B * L - 1);
-    double t = var_mu_ch / var_mu;
+    const double var_mu_ch = vmc / (B - 1);
+    const double var_mu = vall / ((double)B * L - 1);
+    const double t = var_mu_ch / var_mu;
     out[0] = mux;
     out[1] = muy;
     out[2] = sqrt(var_mu_ch / B);
@@ -503,30 +376,30 @@ cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_pa
 
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st) {
+  auto mark = [&](int k) { if (sb.ev) cudaEventRecord(sb.ev[k], st); };
   long tot = (long)P * P;
+  mark(0);
   shift_copy_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(sb.S, P, kind, eps, lam, sb.Lf);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  for (int k0 = 0; k0 < P; k0 += CB) {
-    const int nb = min(CB, P - k0);
-    potrf_diag_kernel<<<1, 1024, 0, st>>>(sb.Lf, P, k0, nb, sb.status);
-    const int rem = P - k0 - nb;
-    if (rem > 0) {
-      trsm_panel_kernel<<<(rem + 127) / 128, 128, 0, st>>>(sb.Lf, P, k0, nb);
-      const int ntt = (rem + CB - 1) / CB;
-      herk_update_kernel<<<ntt * (ntt + 1) / 2, 256, 0, st>>>(sb.Lf, P, k0, nb, k0 + nb, ntt);
-    }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
+  mark(1);
+  e = launch_chol_coop(sb.Lf, P, sb.ctl, sb.status, sb.Dinv, st);
+  if (e != cudaSuccess) return e;
+  mark(2);
+  dim3 tb(32, 8), tg((P + 31) / 32, (P + 31) / 32);
+  conj_transpose_kernel<<<tg, tb, 0, st>>>(sb.Lf, P, sb.LT);
   rhs_init_kernel<<<(P + 255) / 256, 256, 0, st>>>(F, P, real_params ? 1 : 0, sb.rf);
+  mark(3);
   for (int it = 0; it <= refine_iters; ++it) {
-    trsv_kernel<<<1, 1024, 0, st>>>(sb.Lf, P, sb.rf);
+    e = launch_chol_solve(sb.Lf, sb.LT, sb.Dinv, P, sb.rf, st);
+    if (e != cudaSuccess) return e;
+    if (it == 0) mark(4);
     refine_update_kernel<<<(P + 255) / 256, 256, 0, st>>>(sb.x, sb.rf, P, it == 0);
     residual_kernel<<<P, 128, 0, st>>>(sb.S, P, F, sb.x, kind, eps, lam, real_params ? 1 : 0, sb.r, sb.rf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
+  mark(5);
   return cudaSuccess;
 }
 
@@ -537,9 +410,11 @@ cudaError_t launch_descent(double* master, const double* dw, long n_doubles, dou
 }
 
 template <typename R>
-cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* out6, cudaStream_t st) {
-  stats_kernel<R><<<1, 1024, 0, st>>>(vals, B, L, mode, out6);
+cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* chain_scratch, double* out6,
+                         cudaStream_t st) {
+  chain_stats_kernel<R><<<(B + 255) / 256, 256, 0, st>>>(vals, B, L, mode, chain_scratch);
+  stats_final_kernel<<<1, 1024, 0, st>>>(chain_scratch, B, L, out6);
   return cudaGetLastError();
 }
-template cudaError_t launch_stats<float>(const cpx<float>*, int, int, int, double*, cudaStream_t);
-template cudaError_t launch_stats<double>(const cpx<double>*, int, int, int, double*, cudaStream_t);
+template cudaError_t launch_stats<float>(const cpx<float>*, int, int, int, double*, double*, cudaStream_t);
+template cudaError_t launch_stats<double>(const cpx<double>*, int, int, int, double*, double*, cudaStream_t);

@@ -17,7 +17,7 @@ CSRC = os.path.join(_ROOT, "csrc")
 INCLUDE = os.path.join(_REPO, "include")
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
-SOURCES = ["api.cu", "rbm.cu", "sr.cu", "tc.cu"]
+SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "chol.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -42,7 +42,7 @@ class NqConfig(ctypes.Structure):
                 ("burn", ctypes.c_int32), ("passes", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("eval_precision", ctypes.c_int32),
                 ("s_precision", ctypes.c_int32), ("quirks", ctypes.c_uint32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("sampler_lanes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
 
 
 class NqMeasurement(ctypes.Structure):
@@ -91,6 +91,7 @@ EXPORTS = {
                                    ctypes.c_double, _P(NqMeasurement)]),
     "nq_stage_times": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_float)]),
     "nq_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),
+    "nq_tuning": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int32), ctypes.c_int32]),
     "nq_bench_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                       _P(ctypes.c_float)]),

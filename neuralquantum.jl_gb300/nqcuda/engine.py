@@ -10,7 +10,8 @@ from .networks import RBM, NDM, af_logcosh
 
 class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
-                 eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0):
+                 eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
+                 sampler_lanes=0):
         L = _lib.lib()
         cfg = _lib.NqConfig()
         ph = physical(hilb)
@@ -37,6 +38,7 @@ class Engine:
         cfg.eval_precision = eval_precision
         cfg.s_precision = s_precision
         cfg.quirks = quirks
+        cfg.sampler_lanes = sampler_lanes
         self.cfg = cfg
         self.lib = L
         self.h = ctypes.c_void_p()
@@ -146,8 +148,9 @@ class Engine:
         return m
 
     def stage_times(self):
-        """[sample, eval, force+stats, S, solve, update, sampler kernel, S kernel] ms."""
-        a = (ctypes.c_float * 8)()
+        """[sample, eval, force+stats, S, solve, update, sampler kernel, S kernel,
+        factorisation, transpose+rhs, first solve, refinement] ms."""
+        a = (ctypes.c_float * 12)()
         self._check(self.lib.nq_stage_times(self.h, a))
         return list(a)
 
@@ -155,6 +158,12 @@ class Engine:
         a = (ctypes.c_float * n)()
         self._check(self.lib.nq_bench_steps(self.h, call0, n, eps, lr, flush_bytes, a))
         return list(a)
+
+    def tuning(self):
+        """Autotuned choices: {'sampler_lanes': G, 'gram_ksplit': k}."""
+        a = (ctypes.c_int32 * 3)()
+        self._check(self.lib.nq_tuning(self.h, a, 3))
+        return {"sampler_lanes": a[0], "gram_ksplit": a[1]}
 
     def kernel_launches(self):
         return int(self.lib.nq_kernel_launches(self.h))

@@ -152,3 +152,23 @@ def test_vmc_converges_small_tfim(nqlib):
         m = is_.step(lr=0.05, eps=0.01)
         E.append(m.mean.real)
     assert np.mean(E[-10:]) < e0 + 0.05 * abs(e0)
+
+
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+def test_sampler_every_lane_layout_replays_bitexact(nqlib, lanes):
+    """All instantiated lanes-per-chain layouts (the autotuner's candidates)
+    reproduce the Philox replay."""
+    N, B, L, burn, M = 10, 64, 3, 2, 20
+    hilb = nq.HomogeneousSpin(N)
+    net = nq.RBM(np.complex64, N, 2, nq.af_logcosh)
+    nq.init_random_pars_(net, sigma=0.3 ** 2, rng=np.random.default_rng(4))
+    eng = nq.Engine(net, hilb, B, L, burn, N, 31, sampler_lanes=lanes)
+    eng.set_params(net.flat())
+    samples, bits = eng.sample(1, want_accept_bits=True)
+    onet = onw.RBM(N, M, onw.LOGCOSH)
+    onet.set_flat(net.flat())
+    ref, info = osm.run(onet.log_prob, Hilbert(N, SPIN), B, L, burn, eng.passes, 31, call=1,
+                        gpu_accept_bits=bits)
+    assert info["mismatch"] == 0
+    np.testing.assert_array_equal(samples.astype(np.float64), ref)
+    assert eng.tuning()["sampler_lanes"] == lanes
