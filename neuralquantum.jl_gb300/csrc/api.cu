@@ -13,13 +13,20 @@
 #include <vector>
 
 #include "../../include/nqcuda.h"
-#include "nq_kernels.cuh"
+#include "ndm_kernels.cuh"
 
 struct nq_handle {
   nq_config cfg{};
-  int N = 0, M = 0, Ma = 0, nst = 0, P = 0, B = 0, L = 0, Ns = 0, passes = 1;
+  int N = 0, M = 0, nst = 0, P = 0, B = 0, L = 0, Ns = 0, passes = 1;
   int n_record = 0, write_last = 0;
-  bool doubled = false, complex_params = true, f64 = false;
+  bool doubled = false, complex_params = true, f64 = false, ndm = false;
+  int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
+  void* d_eff[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // C, b, a, Cs, bs (cpx<R>)
+  void* d_w = nullptr;             // NDM connection weights [Ns][maxc] cpx<R>
+  int* d_wconn = nullptr;          // connection ids [Ns][maxc]
+  int* d_nconn = nullptr;          // connections per sample [Ns]
+  int maxc = 0;
+  double* d_ndm_partial = nullptr; // [nblk][2P]
   int hilb = 0, act = 0;
   cudaStream_t st = nullptr;
   std::string err;
@@ -99,24 +106,60 @@ cudaError_t dalloc(T** p, size_t count) {
   return cudaMalloc((void**)p, count * sizeof(T) + 16);
 }
 
+// Sampler / table view of the network: the RBM itself, or for the NDM the
+// effective network of the units entering |ρ|^2 over the 2N doubled sites.
 template <typename R>
 RbmDev<R> rbm_dev(nq_handle* h) {
   RbmDev<R> d;
-  d.N = h->N; d.M = h->M; d.act = h->act; d.hilb = h->hilb;
-  const cpx<R>* base;
-  if (h->f64) base = reinterpret_cast<const cpx<R>*>(h->d_master);
-  else base = reinterpret_cast<const cpx<R>*>(h->d_p32);
-  d.a = base;
-  d.b = base + h->N;
-  d.W = base + h->N + h->M;
+  d.act = h->act; d.hilb = h->hilb;
+  if (h->ndm) {
+    d.N = h->N2; d.M = h->Ms; d.n_half = 2 * h->Mh;
+    d.a = reinterpret_cast<const cpx<R>*>(h->d_eff[2]);
+    d.b = reinterpret_cast<const cpx<R>*>(h->d_eff[4]);
+    d.W = reinterpret_cast<const cpx<R>*>(h->d_eff[3]);
+  } else {
+    d.N = h->N; d.M = h->M;
+    const cpx<R>* base;
+    if (h->f64) base = reinterpret_cast<const cpx<R>*>(h->d_master);
+    else base = reinterpret_cast<const cpx<R>*>(h->d_p32);
+    d.a = base;
+    d.b = base + h->N;
+    d.W = base + h->N + h->M;
+  }
   d.t0 = reinterpret_cast<const cpx<R>*>(h->d_tab[0]);
   d.t1 = reinterpret_cast<const cpx<R>*>(h->d_tab[1]);
   d.t2 = reinterpret_cast<const cpx<R>*>(h->d_tab[2]);
   return d;
 }
 
+template <typename R>
+NdmEff<R> ndm_eff(nq_handle* h) {
+  NdmEff<R> e;
+  e.N = h->N; e.N2 = h->N2; e.Mh = h->Mh; e.Ma = h->Ma; e.U = h->U; e.P = h->P;
+  e.C = reinterpret_cast<const cpx<R>*>(h->d_eff[0]);
+  e.b = reinterpret_cast<const cpx<R>*>(h->d_eff[1]);
+  e.a = reinterpret_cast<const cpx<R>*>(h->d_eff[2]);
+  return e;
+}
+
+template <typename R>
+nq_status ndm_refresh(nq_handle* h) {
+  const R* p = h->f64 ? reinterpret_cast<const R*>(h->d_master) : reinterpret_cast<const R*>(h->d_p32);
+  NdmEffBufs<R> b;
+  b.C = (cpx<R>*)h->d_eff[0]; b.b = (cpx<R>*)h->d_eff[1]; b.a = (cpx<R>*)h->d_eff[2];
+  b.Cs = (cpx<R>*)h->d_eff[3]; b.bs = (cpx<R>*)h->d_eff[4];
+  CKL(launch_ndm_effective<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), b, h->st));
+  RbmDev<R> d = rbm_dev<R>(h);
+  CKL(launch_rbm_tables<R>(d, (cpx<R>*)h->d_tab[0], (cpx<R>*)h->d_tab[1], (cpx<R>*)h->d_tab[2], h->st));
+  return NQ_OK;
+}
+
 // refresh FP32 copies and the per-flip tables after a parameter change
 nq_status refresh_params(nq_handle* h) {
+  if (h->ndm) {
+    if (!h->f64) CKL(launch_master_to_f32(h->d_master, h->P, h->d_p32, h->st));
+    return h->f64 ? ndm_refresh<double>(h) : ndm_refresh<float>(h);
+  }
   if (!h->f64) CKL(launch_rbm_params_from_master(h->d_master, h->N, h->M, h->d_p32, h->st));
   if (h->f64) {
     RbmDev<double> d = rbm_dev<double>(h);
@@ -141,15 +184,16 @@ static std::map<std::tuple<int, int, int, int, int, int>, int> g_tune_cache;
 
 nq_status ensure_tuned(nq_handle* h) {
   if (h->sampler_lanes) return NQ_OK;
-  const auto key = std::make_tuple(h->N, h->M, h->B, h->act, h->hilb, h->f64 ? 1 : 0);
+  const int sN = h->ndm ? h->N2 : h->N, sM = h->ndm ? h->Ms : h->M;
+  const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb, (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) { h->sampler_lanes = it->second; return NQ_OK; }
   }
   int cand[4];
-  const int nc = rbm_sampler_valid_lanes(h->M, cand, 4);
-  if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", h->M);
+  const int nc = rbm_sampler_valid_lanes(sM, cand, 4);
+  if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", sM);
   uint64_t* scratch = nullptr;
   CK(cudaMalloc(&scratch, sizeof(uint64_t) * (size_t)h->B * 2));
   SamplerRun run;
@@ -199,7 +243,22 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
   return NQ_OK;
 }
 
+template <typename R>
+nq_status ndm_stage_eval(nq_handle* h) {
+  const NdmEff<R> e = ndm_eff<R>(h);
+  const int sp = h->cfg.s_precision;
+  const bool tc = sp == NQ_S_TF32 || sp == NQ_S_TF32X3;
+  CKL(launch_ndm_eval<R>(e, h->act, h->d_samples, h->Ns, h->hilb, (cpx<R>*)h->d_logpsi, h->d_X, h->Ns_pad,
+                         nullptr, h->st));
+  CKL(launch_x_center(h->d_X, sp == NQ_S_TF32X3 ? h->d_Xlo : nullptr, 2 * h->P, h->Ns_pad, h->Ns, h->fb.meanO,
+                      tc ? 1 : 0, h->st));
+  CKL(launch_ndm_loc<R>(e, h->act, h->op, h->d_samples, h->Ns, h->hilb, h->maxc, (cpx<R>*)h->d_eloc,
+                        (cpx<R>*)h->d_w, h->d_wconn, h->d_nconn, h->st));
+  return NQ_OK;
+}
+
 nq_status stage_eval(nq_handle* h) {
+  if (h->ndm) return h->f64 ? ndm_stage_eval<double>(h) : ndm_stage_eval<float>(h);
   const DevOp* op = h->has_op ? &h->op : nullptr;
   if (h->f64) {
     CKL(launch_rbm_eval<double>(rbm_dev<double>(h), h->d_samples, h->Ns, op, (cpx<double>*)h->d_logpsi,
@@ -216,7 +275,18 @@ __global__ void g64_to_32_kernel(const double* g, long n, float2* out) {
   if (i < n) out[i] = make_float2((float)g[2 * i], (float)g[2 * i + 1]);
 }
 
+template <typename R>
+nq_status ndm_stage_force(nq_handle* h) {
+  // cost C = mean |L_loc|^2 with its statistics, then F
+  CKL(launch_stats<R>((cpx<R>*)h->d_eloc, h->B, h->L, 1, h->d_chainstats, h->d_stats, h->st));
+  CKL(launch_ndm_grad<R>(ndm_eff<R>(h), h->act, h->op, h->d_samples, h->Ns, h->hilb, h->maxc,
+                         (const cpx<R>*)h->d_eloc, (const cpx<R>*)h->d_w, h->d_wconn, h->d_nconn,
+                         h->d_ndm_partial, h->fb.meanO, h->d_stats, h->fb.force, h->st));
+  return NQ_OK;
+}
+
 nq_status stage_force(nq_handle* h) {
+  if (h->ndm) return h->f64 ? ndm_stage_force<double>(h) : ndm_stage_force<float>(h);
   if (h->f64) {
     CKL(launch_rbm_force<double>(rbm_dev<double>(h), h->d_samples, h->Ns, (cpx<double>*)h->d_g,
                                  (cpx<double>*)h->d_eloc, h->fb, h->st));
@@ -230,6 +300,19 @@ nq_status stage_force(nq_handle* h) {
 }
 
 nq_status stage_S(nq_handle* h) {
+  if (h->ndm) {
+    const int sp = h->cfg.s_precision;
+    if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
+    if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
+      CKL(launch_gram_tc(h->d_X, h->d_Xlo, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
+                         h->gram_ksplit, h->sb.status, h->st));
+    } else {
+      CKL(launch_gram_simt_x(h->d_X, h->Ns_pad, h->Ns, 2 * h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
+    }
+    if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
+    CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, true, h->d_S, h->st));
+    return NQ_OK;
+  }
   RbmOSource src;
   src.N = h->N; src.M = h->M; src.hilb = h->hilb; src.Ns = h->Ns;
   src.samples = h->d_samples;
@@ -268,8 +351,8 @@ nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
 }
 
 nq_status stage_update(nq_handle* h, double lr) {
-  long nd = h->complex_params ? 2L * h->P : h->P;
-  CKL(launch_descent(h->d_master, h->sb.x, nd, lr, h->st));
+  const long nd = h->complex_params ? 2L * h->P : h->P;
+  CKL(launch_descent(h->d_master, h->sb.x, nd, h->complex_params ? 1 : 2, lr, h->st));
   return refresh_params(h);
 }
 
@@ -336,10 +419,6 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     return NQ_ERR_ARG;
   };
   if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM) return bad("unknown network");
-  if (c.network == NQ_NET_NDM) {
-    delete h;
-    return NQ_ERR_UNSUPPORTED;
-  }
   if (c.activation != NQ_ACT_LOGCOSH && c.activation != NQ_ACT_SOFTPLUS) return bad("unknown activation");
   if (c.hilbert != NQ_HILB_SPIN && c.hilbert != NQ_HILB_FOCK) return bad("unknown hilbert space");
   if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
@@ -356,8 +435,23 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   }
   h->N = c.n_sites;
   h->M = c.n_hidden;
-  h->nst = h->N;
-  h->P = h->N + h->M + h->M * h->N;
+  if (c.network == NQ_NET_NDM) {
+    h->ndm = true;
+    h->Mh = c.n_hidden;
+    h->Ma = c.n_ancilla;
+    if (h->Ma < 1) return bad("the NDM needs n_ancilla >= 1");
+    h->N2 = 2 * h->N;
+    h->U = 4 * h->Mh + h->Ma;
+    h->Ms = 2 * h->Mh + h->Ma;
+    h->nst = h->N2;
+    h->P = ndm_n_params(h->N, h->Mh, h->Ma);
+    if (h->N2 > 64) return bad("the NDM supports n_sites <= 32 (2N doubled sites)");
+    if (h->Ms > 320) return bad("2*n_hidden + n_ancilla must be <= 320");
+    if (h->P > 256 * 24) return bad("too many NDM parameters (max 6144)");
+  } else {
+    h->nst = h->N;
+    h->P = h->N + h->M + h->M * h->N;
+  }
   h->B = c.n_chains;
   h->L = c.chain_length;
   h->Ns = h->B * h->L;
@@ -368,10 +462,11 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->hilb = c.hilbert;
   h->act = c.activation;
   h->f64 = c.eval_precision == NQ_EVAL_F64;
-  h->complex_params = true;
+  h->complex_params = !h->ndm;
+  const int sampler_M = h->ndm ? h->Ms : h->M, sampler_N = h->ndm ? h->N2 : h->N;
   if (c.sampler_lanes != 0) {
     int cand[4];
-    const int nc = rbm_sampler_valid_lanes(c.n_hidden, cand, 4);
+    const int nc = rbm_sampler_valid_lanes(sampler_M, cand, 4);
     bool ok = false;
     for (int i = 0; i < nc; ++i) ok = ok || cand[i] == c.sampler_lanes;
     if (!ok) return bad("sampler_lanes not available for this number of hidden units");
@@ -391,15 +486,20 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   const int P = h->P;
   step(dalloc(&h->d_master, 2 * (size_t)P), "params");
   step(dalloc(&h->d_p32, 2 * (size_t)P), "params32");
-  for (int k = 0; k < 3; ++k) step(cudaMalloc(&h->d_tab[k], (size_t)h->N * h->M * csz + 16), "tables");
+  for (int k = 0; k < 3; ++k) step(cudaMalloc(&h->d_tab[k], (size_t)sampler_N * sampler_M * csz + 16), "tables");
+  if (h->ndm) {
+    const size_t ne[5] = {(size_t)h->U * h->N2, (size_t)h->U, (size_t)h->N2, (size_t)h->Ms * h->N2, (size_t)h->Ms};
+    for (int k = 0; k < 5; ++k) step(cudaMalloc(&h->d_eff[k], ne[k] * csz + 16), "effective network");
+    step(dalloc(&h->d_ndm_partial, (size_t)ndm_grad_nblocks(h->Ns) * 2 * h->P), "ndm partial");
+  }
   step(dalloc(&h->d_samples, (size_t)h->Ns), "samples");
   step(dalloc(&h->d_accepted, 1), "accepted");
   step(dalloc(&h->d_call, 1), "call");
   step(cudaMalloc(&h->d_logpsi, (size_t)h->Ns * csz), "logpsi");
-  step(cudaMalloc(&h->d_g, (size_t)h->Ns * h->M * csz), "g");
+  if (!h->ndm) step(cudaMalloc(&h->d_g, (size_t)h->Ns * h->M * csz), "g");
   step(cudaMalloc(&h->d_eloc, (size_t)h->Ns * csz), "eloc");
-  if (h->f64) step(dalloc(&h->d_g32, (size_t)h->Ns * h->M), "g32");
-  h->force_nblk = rbm_force_nblocks(h->Ns, h->N, h->M, (int)csz);
+  if (h->f64 && !h->ndm) step(dalloc(&h->d_g32, (size_t)h->Ns * h->M), "g32");
+  h->force_nblk = h->ndm ? 1 : rbm_force_nblocks(h->Ns, h->N, h->M, (int)csz);
   step(dalloc(&h->fb.partial, (size_t)h->force_nblk * 4 * P), "force partial");
   step(dalloc(&h->fb.partialE, 2 * (size_t)h->force_nblk), "force partialE");
   step(dalloc(&h->fb.meanO, 2 * (size_t)P), "meanO");
@@ -428,6 +528,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
     if (c.s_precision == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
+  } else if (h->ndm) {
+    h->Ns_pad = ((h->Ns + 127) / 128) * 128;
+    step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
   }
   step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
   step(dalloc(&h->sb.Lf, (size_t)P * P), "Lf");
@@ -472,7 +575,8 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.Lf, h->sb.LT, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.status, h->sb.ctl, h->sb.Dinv, h->d_dw};
+                  h->sb.rf, h->sb.status, h->sb.ctl, h->sb.Dinv, h->d_dw, h->d_eff[0], h->d_eff[1],
+                  h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->h_call) cudaFreeHost(h->h_call);
@@ -501,12 +605,20 @@ int64_t nq_kernel_launches(const nq_handle* h) { return h ? h->launches : -1; }
 nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype) {
   if (!h || !flat) return NQ_ERR_ARG;
   if (n != h->P) return fail(h, NQ_ERR_ARG, "expected %d parameters, got %lld", h->P, (long long)n);
-  std::vector<double> buf(2 * (size_t)h->P, 0.0);
-  if (dtype == NQ_DTYPE_C128) memcpy(buf.data(), flat, buf.size() * sizeof(double));
-  else if (dtype == NQ_DTYPE_C64) {
-    const float* f = (const float*)flat;
-    for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
-  } else return fail(h, NQ_ERR_ARG, "RBM parameters are complex (dtype c64 or c128)");
+  std::vector<double> buf((h->complex_params ? 2 : 1) * (size_t)h->P, 0.0);
+  if (h->complex_params) {
+    if (dtype == NQ_DTYPE_C128) memcpy(buf.data(), flat, buf.size() * sizeof(double));
+    else if (dtype == NQ_DTYPE_C64) {
+      const float* f = (const float*)flat;
+      for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
+    } else return fail(h, NQ_ERR_ARG, "RBM parameters are complex (dtype c64 or c128)");
+  } else {
+    if (dtype == NQ_DTYPE_F64) memcpy(buf.data(), flat, buf.size() * sizeof(double));
+    else if (dtype == NQ_DTYPE_F32) {
+      const float* f = (const float*)flat;
+      for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
+    } else return fail(h, NQ_ERR_ARG, "NDM parameters are real (dtype f32 or f64)");
+  }
   for (double v : buf)
     if (!std::isfinite(v)) return fail(h, NQ_ERR_NAN, "non-finite parameter");
   CK(cudaMemcpyAsync(h->d_master, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
@@ -519,14 +631,18 @@ nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype
 nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
   if (!h || !flat) return NQ_ERR_ARG;
   if (n != h->P) return fail(h, NQ_ERR_ARG, "expected %d parameters, got %lld", h->P, (long long)n);
-  std::vector<double> buf(2 * (size_t)h->P);
+  std::vector<double> buf((h->complex_params ? 2 : 1) * (size_t)h->P);
   CK(cudaMemcpyAsync(buf.data(), h->d_master, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  if (dtype == NQ_DTYPE_C128) memcpy(flat, buf.data(), buf.size() * sizeof(double));
-  else if (dtype == NQ_DTYPE_C64) {
+  const bool want_c = dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_C64;
+  if (want_c != h->complex_params)
+    return fail(h, NQ_ERR_ARG, h->complex_params ? "RBM parameters are complex (dtype c64 or c128)"
+                                                 : "NDM parameters are real (dtype f32 or f64)");
+  if (dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_F64) memcpy(flat, buf.data(), buf.size() * sizeof(double));
+  else {
     float* f = (float*)flat;
     for (size_t i = 0; i < buf.size(); ++i) f[i] = (float)buf[i];
-  } else return fail(h, NQ_ERR_ARG, "RBM parameters are complex (dtype c64 or c128)");
+  }
   return NQ_OK;
 }
 
@@ -574,6 +690,30 @@ nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
     return s;
   h->op = d;
   h->has_op = true;
+  if (h->ndm) {
+    // the Liouvillian estimator keeps the weight of every connection: bound
+    // the connections per configuration by the longest row of each operator
+    int maxc = 0;
+    for (int o = 0; o < t->n_ops; ++o) {
+      int longest = 0;
+      const int nrows = 1 << t->op_n_sites[o];
+      for (int r = 0; r < nrows; ++r) {
+        const int row = t->op_row_offset[o] + r;
+        longest = std::max(longest, t->row_conn_offset[row + 1] - t->row_conn_offset[row]);
+      }
+      maxc += longest;
+    }
+    maxc = std::max(maxc, 1);
+    if (h->d_w) cudaFree(h->d_w);
+    if (h->d_wconn) cudaFree(h->d_wconn);
+    if (h->d_nconn) cudaFree(h->d_nconn);
+    h->d_w = nullptr; h->d_wconn = nullptr; h->d_nconn = nullptr;
+    const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
+    CK(cudaMalloc(&h->d_w, (size_t)h->Ns * maxc * csz));
+    CK(cudaMalloc((void**)&h->d_wconn, (size_t)h->Ns * maxc * sizeof(int)));
+    CK(cudaMalloc((void**)&h->d_nconn, (size_t)h->Ns * sizeof(int)));
+    h->maxc = maxc;
+  }
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
   return NQ_OK;
 }
@@ -636,11 +776,15 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
   CK(cudaMalloc(&d_v, (size_t)n * h->nst));
   CK(cudaMalloc(&d_bits, (size_t)n * sizeof(uint64_t)));
   CK(cudaMalloc(&d_lp, (size_t)n * csz));
-  CK(cudaMalloc(&d_g, (size_t)n * h->M * csz));
+  if (!h->ndm) CK(cudaMalloc(&d_g, (size_t)n * h->M * csz));
   CK(cudaMemcpyAsync(d_v, sigma, (size_t)n * h->nst, cudaMemcpyHostToDevice, h->st));
   ++h->launches;
   CK(launch_pack_int8(d_v, h->nst, n, h->hilb, d_bits, h->st));
-  if (h->f64) CKL(launch_rbm_eval<double>(rbm_dev<double>(h), d_bits, (int)n, nullptr, (cpx<double>*)d_lp, (cpx<double>*)d_g, nullptr, h->st));
+  if (h->ndm) {
+    if (grad) CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
+    if (h->f64) CKL(launch_ndm_eval<double>(ndm_eff<double>(h), h->act, d_bits, (int)n, h->hilb, (cpx<double>*)d_lp, nullptr, 0, d_out, h->st));
+    else CKL(launch_ndm_eval<float>(ndm_eff<float>(h), h->act, d_bits, (int)n, h->hilb, (cpx<float>*)d_lp, nullptr, 0, d_out, h->st));
+  } else if (h->f64) CKL(launch_rbm_eval<double>(rbm_dev<double>(h), d_bits, (int)n, nullptr, (cpx<double>*)d_lp, (cpx<double>*)d_g, nullptr, h->st));
   else CKL(launch_rbm_eval<float>(rbm_dev<float>(h), d_bits, (int)n, nullptr, (cpx<float>*)d_lp, (cpx<float>*)d_g, nullptr, h->st));
   std::vector<double> lp(2 * n);
   if (h->f64) CK(cudaMemcpyAsync(lp.data(), d_lp, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -650,12 +794,13 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
     CK(cudaStreamSynchronize(h->st));
     for (int64_t i = 0; i < 2 * n; ++i) lp[i] = f[i];
   }
-  if (grad) {
+  if (grad && !h->ndm) {
     CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
     if (h->f64) CKL(launch_rbm_grad_matrix<double>(d_bits, (int)n, h->N, h->M, h->hilb, (cpx<double>*)d_g, d_out, h->st));
     else CKL(launch_rbm_grad_matrix<float>(d_bits, (int)n, h->N, h->M, h->hilb, (cpx<float>*)d_g, d_out, h->st));
     CK(cudaMemcpyAsync(grad, d_out, (size_t)2 * h->P * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   }
+  if (grad && h->ndm) CK(cudaMemcpyAsync(grad, d_out, (size_t)2 * h->P * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   memcpy(out, lp.data(), 2 * n * sizeof(double));
   cudaFree(d_v); cudaFree(d_bits); cudaFree(d_lp); cudaFree(d_g);

@@ -1,0 +1,489 @@
+// NDM (purified neural density matrix) path: effective-network construction,
+// batched logρ / ∇logρ on doubled states (σ, η), the Liouvillian local
+// estimator L_loc and the cost gradient accumulation.
+//
+// Reference: src/Networks/MixedDensityMatrix/NDM.jl:76-96 and 241-337,
+// NDMBatched.jl:94-280 (network and gradient), AccumulatorObsGrad.jl:39-127
+// and BatchedGradSampler.jl:77-123 (estimator and gradient).
+//
+// With σ the row and η the column configuration, the NDM is written as a
+// generalised RBM over the 2N doubled sites v = (σ, η) with U = 4Mh + Ma
+// hidden units u of weight ω_u:
+//   logρ = Σ_i a_i v_i + Σ_u ω_u f(x_u),  x_u = b_u + Σ_i C[u, i] v_i
+//   units [λσ (Mh), λη (Mh), π (Ma), μσ (Mh), μη (Mh)] with
+//   ω = 1/2, 1/2, 1, i/2, -i/2;  a_i = b_la/2 ± i b_mu/2 (row/column).
+// The first Ms = 2Mh + Ma units are the ones that enter |ρ|^2, so the
+// Metropolis sampler of the RBM runs unchanged on them (λ units at weight
+// 1/2 through RbmDev::n_half).
+#include "ndm_kernels.cuh"
+
+namespace {
+
+template <typename R>
+__global__ void ndm_effective_kernel(NdmDev<R> n, cpx<R>* C, cpx<R>* bu, cpx<R>* a, cpx<R>* Cs, cpx<R>* bs) {
+  const int N = n.N, Mh = n.Mh, Ma = n.Ma, U = 4 * Mh + Ma, Ms = 2 * Mh + Ma, N2 = 2 * N;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < U * N2) {
+    const int u = idx % U, i = idx / U;
+    const bool row = i < N;
+    const int j = row ? i : i - N;
+    cpx<R> c = mk(R(0), R(0));
+    if (u < Mh) { if (row) c.x = n.w_la[u + Mh * j]; }
+    else if (u < 2 * Mh) { if (!row) c.x = n.w_la[(u - Mh) + Mh * j]; }
+    else if (u < 2 * Mh + Ma) {
+      const int q = u - 2 * Mh;
+      c.x = R(0.5) * n.u_la[q + Ma * j];
+      c.y = (row ? R(0.5) : R(-0.5)) * n.u_mu[q + Ma * j];
+    } else if (u < 3 * Mh + Ma) { if (row) c.x = n.w_mu[(u - 2 * Mh - Ma) + Mh * j]; }
+    else { if (!row) c.x = n.w_mu[(u - 3 * Mh - Ma) + Mh * j]; }
+    C[u + (size_t)U * i] = c;
+    if (u < Ms) Cs[u + (size_t)Ms * i] = c;
+  }
+  if (idx < U) {
+    const int u = idx;
+    cpx<R> b = mk(R(0), R(0));
+    if (u < 2 * Mh) b.x = n.h_la[u % Mh];
+    else if (u < 2 * Mh + Ma) b.x = n.d_la[u - 2 * Mh];
+    else b.x = n.h_mu[(u - 2 * Mh - Ma) % Mh];
+    bu[u] = b;
+    if (u < Ms) bs[u] = b;
+  }
+  if (idx < N2) {
+    const int j = idx < N ? idx : idx - N;
+    a[idx] = mk(R(0.5) * n.b_la[j], (idx < N ? R(0.5) : R(-0.5)) * n.b_mu[j]);
+  }
+}
+
+template <typename R> NQ_D cpx<R> unit_weight(int u, int Mh, int Ma) {
+  if (u < 2 * Mh) return mk(R(0.5), R(0));
+  if (u < 2 * Mh + Ma) return mk(R(1), R(0));
+  if (u < 3 * Mh + Ma) return mk(R(0), R(0.5));
+  return mk(R(0), R(-0.5));
+}
+
+// O_k at a doubled configuration with unit derivatives g (real parameter k of
+// the reference order b_mu, h_mu, w_mu, u_mu, b_la, h_la, d_la, w_la, u_la).
+template <typename R>
+NQ_D cpx<R> ndm_O(int k, int N, int Mh, int Ma, const cpx<R>* g, int gstride, uint64_t bits, int hilb) {
+  const cpx<R> half_i = mk(R(0), R(0.5));
+  // unit offsets: λσ 0, λη Mh, π 2Mh, μσ 2Mh+Ma, μη 3Mh+Ma
+  const int oLs = 0, oLe = Mh, oPi = 2 * Mh, oMs = 2 * Mh + Ma, oMe = 3 * Mh + Ma;
+#define G_(u) g[(size_t)(u) * gstride]
+  int o = 0;
+  if (k < o + N) { const int j = k - o; return half_i * mk(site_value<R>(bits, j, hilb) - site_value<R>(bits, N + j, hilb), R(0)); }
+  o += N;
+  if (k < o + Mh) { const int h = k - o; return half_i * (G_(oMs + h) - G_(oMe + h)); }
+  o += Mh;
+  if (k < o + Mh * N) {
+    const int q = k - o, h = q % Mh, j = q / Mh;
+    return half_i * (site_value<R>(bits, j, hilb) * G_(oMs + h) - site_value<R>(bits, N + j, hilb) * G_(oMe + h));
+  }
+  o += Mh * N;
+  if (k < o + Ma * N) {
+    const int q = k - o, a = q % Ma, j = q / Ma;
+    return (site_value<R>(bits, j, hilb) - site_value<R>(bits, N + j, hilb)) * (half_i * G_(oPi + a));
+  }
+  o += Ma * N;
+  if (k < o + N) { const int j = k - o; return mk(R(0.5) * (site_value<R>(bits, j, hilb) + site_value<R>(bits, N + j, hilb)), R(0)); }
+  o += N;
+  if (k < o + Mh) { const int h = k - o; return R(0.5) * (G_(oLs + h) + G_(oLe + h)); }
+  o += Mh;
+  if (k < o + Ma) { const int a = k - o; return G_(oPi + a); }
+  o += Ma;
+  if (k < o + Mh * N) {
+    const int q = k - o, h = q % Mh, j = q / Mh;
+    return R(0.5) * (site_value<R>(bits, j, hilb) * G_(oLs + h) + site_value<R>(bits, N + j, hilb) * G_(oLe + h));
+  }
+  o += Mh * N;
+  {
+    const int q = k - o, a = q % Ma, j = q / Ma;
+    return (R(0.5) * (site_value<R>(bits, j, hilb) + site_value<R>(bits, N + j, hilb))) * G_(oPi + a);
+  }
+#undef G_
+}
+
+// unit pre-activations x_u and derivatives g_u at configuration `bits`
+// into per-thread slices of shared memory (stride T)
+template <typename R, int ACT>
+NQ_D cpx<R> ndm_units(const NdmEff<R>& e, uint64_t bits, int hilb, cpx<R>* x, cpx<R>* g, int T) {
+  const int U = e.U, N2 = e.N2;
+  cpx<R> lp = mk(R(0), R(0));
+  for (int i = 0; i < N2; ++i) lp = lp + site_value<R>(bits, i, hilb) * e.a[i];
+  for (int u = 0; u < U; ++u) {
+    cpx<R> t = e.b[u];
+    for (int i = 0; i < N2; ++i) {
+      const R v = site_value<R>(bits, i, hilb);
+      if (v != R(0)) { const cpx<R> c = e.C[u + (size_t)U * i]; t.x += c.x * v; t.y += c.y * v; }
+    }
+    x[(size_t)u * T] = t;
+    g[(size_t)u * T] = act_df<ACT>(t);
+    lp = lp + unit_weight<R>(u, e.Mh, e.Ma) * act_f<ACT>(t);
+  }
+  return lp;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation: logρ and O (P entries) per sample.  O is written either to the
+// interleaved real rows of X (row 2k = Re O_k, 2k+1 = Im O_k, sample-major
+// columns, uncentred) or to a P x n complex double matrix.
+// ---------------------------------------------------------------------------
+template <typename R, int ACT>
+__global__ void __launch_bounds__(128)
+ndm_eval_kernel(NdmEff<R> e, const uint64_t* __restrict__ samples, int n, int hilb, cpx<R>* logrho,
+                float* X, int ldx, double* Oout) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = blockDim.x, U = e.U;
+  cpx<R>* sx = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* sg = sx + (size_t)U * T;
+  const int s = blockIdx.x * T + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t bits = samples[s];
+  const cpx<R> lp = ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
+  logrho[s] = lp;
+  for (int k = 0; k < e.P; ++k) {
+    const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sg + threadIdx.x, T, bits, hilb);
+    if (X) {
+      X[(size_t)(2 * k) * ldx + s] = (float)o.x;
+      X[(size_t)(2 * k + 1) * ldx + s] = (float)o.y;
+    }
+    if (Oout) {
+      Oout[2 * ((size_t)k + (size_t)e.P * s)] = (double)o.x;
+      Oout[2 * ((size_t)k + (size_t)e.P * s) + 1] = (double)o.y;
+    }
+  }
+}
+
+// Δlogρ of a connection: Σ_i a_i Δv_i + Σ_u ω_u [f(x_u + Δx_u) - f(x_u)]
+template <typename R, int ACT>
+NQ_D cpx<R> ndm_delta(const NdmEff<R>& e, const DevOp& op, int c, uint64_t bits, int hilb, const cpx<R>* x,
+                      int T, int nch) {
+  const int U = e.U;
+  cpx<R> d = mk(R(0), R(0));
+  int site[8];
+  R dv[8];
+  for (int q = 0; q < nch; ++q) {
+    site[q] = __ldg(op.conn_change_site + 8 * c + q);
+    dv[q] = (R)__ldg(op.conn_change_value + 8 * c + q) - site_value<R>(bits, site[q], hilb);
+    d = d + dv[q] * e.a[site[q]];
+  }
+  for (int u = 0; u < U; ++u) {
+    cpx<R> dx = mk(R(0), R(0));
+    for (int q = 0; q < nch; ++q) {
+      const cpx<R> cc = e.C[u + (size_t)U * site[q]];
+      dx.x += cc.x * dv[q];
+      dx.y += cc.y * dv[q];
+    }
+    if (dx.x == R(0) && dx.y == R(0)) continue;
+    const cpx<R> xu = x[(size_t)u * T];
+    d = d + unit_weight<R>(u, e.Mh, e.Ma) * (act_f<ACT>(xu + dx) - act_f<ACT>(xu));
+  }
+  return d;
+}
+
+// ---------------------------------------------------------------------------
+// Local Liouvillian L_loc(σ,η) = Σ_c mel_c ρ(σ'_c)/ρ(σ,η) over every
+// non-zero connection, including those without changes
+// (AccumulatorObsGrad.jl:62-75); the weights w_c are kept for the gradient.
+// ---------------------------------------------------------------------------
+template <typename R, int ACT>
+__global__ void __launch_bounds__(128)
+ndm_loc_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int n, int hilb, int maxc,
+               cpx<R>* __restrict__ L, cpx<R>* __restrict__ w, int* __restrict__ wconn,
+               int* __restrict__ nconn) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = blockDim.x, U = e.U;
+  cpx<R>* sx = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* sg = sx + (size_t)U * T;
+  const int s = blockIdx.x * T + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t bits = samples[s];
+  ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
+  cpx<R> acc = mk(R(0), R(0));
+  int cnt = 0;
+  for (int o = 0; o < op.n_ops; ++o) {
+    const int ns_o = __ldg(op.op_n_sites + o);
+    int r = 0;
+    for (int d = 0; d < ns_o; ++d) r |= (int)((bits >> __ldg(op.op_sites + 8 * o + d)) & 1ull) << d;
+    const int row = __ldg(op.op_row_offset + o) + r;
+    const int c0 = __ldg(op.row_conn_offset + row), c1 = __ldg(op.row_conn_offset + row + 1);
+    for (int c = c0; c < c1; ++c) {
+      const double mre = __ldg(op.conn_mel + 2 * c), mim = __ldg(op.conn_mel + 2 * c + 1);
+      if (mre == 0.0 && mim == 0.0) continue;
+      const int nch = __ldg(op.conn_n_changes + c);
+      const cpx<R> d = ndm_delta<R, ACT>(e, op, c, bits, hilb, sx + threadIdx.x, T, nch);
+      const cpx<R> wc = mk((R)mre, (R)mim) * cexpc(d);
+      acc = acc + wc;
+      if (cnt < maxc) {
+        w[(size_t)s * maxc + cnt] = wc;
+        wconn[(size_t)s * maxc + cnt] = c;
+      }
+      ++cnt;
+    }
+  }
+  L[s] = acc;
+  nconn[s] = min(cnt, maxc);
+}
+
+// ---------------------------------------------------------------------------
+// Gradient accumulation G_k = Σ_s conj(L_s) Σ_c w_c O_k(σ'_c) (the
+// conj(Σ L conj(∇L)) of BatchedGradSampler.jl:108-111).  One block per chunk
+// of samples; connections are expanded 32 at a time into shared memory (their
+// unit derivatives and configurations), then each thread accumulates its own
+// parameters over them.  Partial sums per block in FP64.
+// ---------------------------------------------------------------------------
+template <typename R, int ACT>
+__global__ void __launch_bounds__(256)
+ndm_grad_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int n, int hilb, int maxc,
+                const cpx<R>* __restrict__ L, const cpx<R>* __restrict__ w, const int* __restrict__ wconn,
+                const int* __restrict__ nconn, int chunk, double* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int CB = 32;
+  const int U = e.U, P = e.P;
+  cpx<R>* sgp = reinterpret_cast<cpx<R>*>(smem_raw);                 // [U][CB] derivatives at σ'
+  cpx<R>* sbeta = sgp + (size_t)U * CB;                               // [CB]
+  uint64_t* sbits = reinterpret_cast<uint64_t*>(sbeta + CB);          // [CB]
+  __shared__ int s_list_s[CB], s_list_c[CB];
+  const int s0 = blockIdx.x * chunk, s1 = min(n, s0 + chunk);
+  // own-parameter accumulators (P <= 256 * PPT)
+  constexpr int PPT = 24;
+  cpx<double> acc[PPT];
+#pragma unroll
+  for (int q = 0; q < PPT; ++q) acc[q] = mk(0.0, 0.0);
+  // enumerate (sample, connection) pairs of the chunk in batches of CB
+  int cur_s = s0, cur_c = 0;
+  while (true) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int m = 0;
+      while (m < CB && cur_s < s1) {
+        if (cur_c < nconn[cur_s]) { s_list_s[m] = cur_s; s_list_c[m] = cur_c; ++m; ++cur_c; }
+        else { ++cur_s; cur_c = 0; }
+      }
+      for (int q = m; q < CB; ++q) s_list_s[q] = -1;
+    }
+    __syncthreads();
+    if (s_list_s[0] < 0) break;
+    // expand: one thread per (pair, unit)
+    for (int t = threadIdx.x; t < CB * U; t += blockDim.x) {
+      const int m = t % CB, u = t / CB;
+      const int s = s_list_s[m];
+      if (s < 0) { sgp[(size_t)u * CB + m] = mk(R(0), R(0)); continue; }
+      const int cc = wconn[(size_t)s * maxc + s_list_c[m]];
+      const uint64_t bits = samples[s];
+      // x_u at σ, then add the connection's change
+      cpx<R> xu = e.b[u];
+      for (int i = 0; i < e.N2; ++i) {
+        const R v = site_value<R>(bits, i, hilb);
+        if (v != R(0)) { const cpx<R> c = e.C[u + (size_t)U * i]; xu.x += c.x * v; xu.y += c.y * v; }
+      }
+      uint64_t nb = bits;
+      const int nch = __ldg(op.conn_n_changes + cc);
+      for (int q = 0; q < nch; ++q) {
+        const int site = __ldg(op.conn_change_site + 8 * cc + q);
+        const R nv = (R)__ldg(op.conn_change_value + 8 * cc + q);
+        const R dv = nv - site_value<R>(bits, site, hilb);
+        const cpx<R> c = e.C[u + (size_t)U * site];
+        xu.x += c.x * dv;
+        xu.y += c.y * dv;
+        const uint64_t bit = (hilb == HILB_SPIN) ? (nv > 0 ? 1ull : 0ull) : (nv != R(0) ? 1ull : 0ull);
+        nb = (nb & ~(1ull << site)) | (bit << site);
+      }
+      sgp[(size_t)u * CB + m] = act_df<ACT>(xu);
+      if (u == 0) {
+        sbits[m] = nb;
+        sbeta[m] = conjc(L[s]) * w[(size_t)s * maxc + s_list_c[m]];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+      const int k = threadIdx.x + q * blockDim.x;
+      if (k < P) {
+        for (int m = 0; m < CB; ++m) {
+          if (s_list_s[m] < 0) break;
+          const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sgp + m, CB, sbits[m], hilb);
+          const cpx<R> b = sbeta[m];
+          acc[q].x += (double)(b.x * o.x - b.y * o.y);
+          acc[q].y += (double)(b.x * o.y + b.y * o.x);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < PPT; ++q) {
+    const int k = threadIdx.x + q * blockDim.x;
+    if (k < P) {
+      partial[(size_t)blockIdx.x * 2 * P + 2 * k] = acc[q].x;
+      partial[(size_t)blockIdx.x * 2 * P + 2 * k + 1] = acc[q].y;
+    }
+  }
+}
+
+// deterministic reduction of the gradient partials, then
+// F = G/Ns - C <O>  with C = mean |L|^2 (stats[0]); real parameters keep Re.
+__global__ void ndm_force_finalize_kernel(int P, int nblk, int Ns, const double* __restrict__ partial,
+                                          const double* __restrict__ meanO, const double* __restrict__ stats,
+                                          double* __restrict__ force) {
+  const int wp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (wp >= P) return;
+  double gx = 0, gy = 0;
+  for (int b = lane; b < nblk; b += 32) {
+    gx += partial[(size_t)b * 2 * P + 2 * wp];
+    gy += partial[(size_t)b * 2 * P + 2 * wp + 1];
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, off);
+    gy += __shfl_xor_sync(0xffffffffu, gy, off);
+  }
+  if (lane == 0) {
+    const double C = stats[0];
+    force[2 * wp] = gx / Ns - C * meanO[2 * wp];
+    force[2 * wp + 1] = gy / Ns - C * meanO[2 * wp + 1];
+  }
+}
+
+// row means of X (FP64, one warp per row) -> meanO (complex per parameter)
+__global__ void x_row_mean_kernel(const float* __restrict__ X, int rows, int ld, int ns, double* __restrict__ meanO) {
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (r >= rows) return;
+  double s = 0;
+  const float* row = X + (size_t)r * ld;
+  for (int i = lane; i < ns; i += 32) s += (double)row[i];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) meanO[r] = s / ns;        // row 2k -> Re <O_k>, 2k+1 -> Im <O_k>
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// centre X in place (padding columns stay 0); optionally round to TF32 and
+// emit the TF32 remainder
+__global__ void x_center_kernel(float* __restrict__ X, float* __restrict__ Xlo, int rows, int ld, int ns,
+                                const double* __restrict__ meanO, int tf32) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)rows * ld) return;
+  const int r = (int)(idx / ld), s = (int)(idx % ld);
+  float v = s < ns ? (float)((double)X[idx] - meanO[r]) : 0.f;
+  if (tf32) {
+    const float hi = tf32_round(v);
+    X[idx] = hi;
+    if (Xlo) Xlo[idx] = tf32_round(v - hi);
+  } else {
+    X[idx] = v;
+  }
+}
+
+template <typename R>
+__global__ void ndm_grad_to_host_layout(const double* Oout, int P, int n, double* out) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx < 2L * P * n) out[idx] = Oout[idx];
+}
+
+}  // namespace
+
+// ------------------------------- launchers ---------------------------------
+
+template <typename R>
+cudaError_t launch_ndm_effective(const NdmDev<R>& n, const NdmEffBufs<R>& b, cudaStream_t st) {
+  const int U = 4 * n.Mh + n.Ma, tot = U * 2 * n.N;
+  ndm_effective_kernel<R><<<(tot + 127) / 128, 128, 0, st>>>(n, b.C, b.b, b.a, b.Cs, b.bs);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static size_t unit_smem(int U, int T) { return (size_t)2 * U * T * sizeof(cpx<R>); }
+
+template <typename R>
+static int ndm_threads(int U) {
+  int T = 128;
+  while (T > 32 && unit_smem<R>(U, T) > 96 * 1024) T /= 2;
+  return T;
+}
+
+template <typename R, typename K>
+static cudaError_t set_smem(K kern, size_t smem) {
+  if (smem > 48 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_ndm_eval(const NdmEff<R>& e, int act, const uint64_t* samples, int n, int hilb,
+                            cpx<R>* logrho, float* X, int ldx, double* Oout, cudaStream_t st) {
+  const int T = ndm_threads<R>(e.U);
+  const size_t smem = unit_smem<R>(e.U, T);
+  cudaError_t err;
+  if (act == ACT_LOGCOSH) {
+    if ((err = set_smem<R>(ndm_eval_kernel<R, ACT_LOGCOSH>, smem)) != cudaSuccess) return err;
+    ndm_eval_kernel<R, ACT_LOGCOSH><<<(n + T - 1) / T, T, smem, st>>>(e, samples, n, hilb, logrho, X, ldx, Oout);
+  } else {
+    if ((err = set_smem<R>(ndm_eval_kernel<R, ACT_SOFTPLUS>, smem)) != cudaSuccess) return err;
+    ndm_eval_kernel<R, ACT_SOFTPLUS><<<(n + T - 1) / T, T, smem, st>>>(e, samples, n, hilb, logrho, X, ldx, Oout);
+  }
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_ndm_loc(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+                           int hilb, int maxc, cpx<R>* L, cpx<R>* w, int* wconn, int* nconn, cudaStream_t st) {
+  const int T = ndm_threads<R>(e.U);
+  const size_t smem = unit_smem<R>(e.U, T);
+  cudaError_t err;
+  if (act == ACT_LOGCOSH) {
+    if ((err = set_smem<R>(ndm_loc_kernel<R, ACT_LOGCOSH>, smem)) != cudaSuccess) return err;
+    ndm_loc_kernel<R, ACT_LOGCOSH><<<(n + T - 1) / T, T, smem, st>>>(e, op, samples, n, hilb, maxc, L, w, wconn, nconn);
+  } else {
+    if ((err = set_smem<R>(ndm_loc_kernel<R, ACT_SOFTPLUS>, smem)) != cudaSuccess) return err;
+    ndm_loc_kernel<R, ACT_SOFTPLUS><<<(n + T - 1) / T, T, smem, st>>>(e, op, samples, n, hilb, maxc, L, w, wconn, nconn);
+  }
+  return cudaGetLastError();
+}
+
+int ndm_grad_chunk() { return 16; }
+
+template <typename R>
+cudaError_t launch_ndm_grad(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+                            int hilb, int maxc, const cpx<R>* L, const cpx<R>* w, const int* wconn,
+                            const int* nconn, double* partial, const double* meanO, const double* stats,
+                            double* force, cudaStream_t st) {
+  if (e.P > 256 * 24) return cudaErrorInvalidValue;
+  const int chunk = ndm_grad_chunk();
+  const int nblk = (n + chunk - 1) / chunk;
+  const size_t smem = (size_t)e.U * 32 * sizeof(cpx<R>) + 32 * sizeof(cpx<R>) + 32 * sizeof(uint64_t);
+  cudaError_t err;
+  if (act == ACT_LOGCOSH) {
+    if ((err = set_smem<R>(ndm_grad_kernel<R, ACT_LOGCOSH>, smem)) != cudaSuccess) return err;
+    ndm_grad_kernel<R, ACT_LOGCOSH><<<nblk, 256, smem, st>>>(e, op, samples, n, hilb, maxc, L, w, wconn, nconn,
+                                                             chunk, partial);
+  } else {
+    if ((err = set_smem<R>(ndm_grad_kernel<R, ACT_SOFTPLUS>, smem)) != cudaSuccess) return err;
+    ndm_grad_kernel<R, ACT_SOFTPLUS><<<nblk, 256, smem, st>>>(e, op, samples, n, hilb, maxc, L, w, wconn, nconn,
+                                                              chunk, partial);
+  }
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  ndm_force_finalize_kernel<<<(32 * e.P + 255) / 256, 256, 0, st>>>(e.P, nblk, n, partial, meanO, stats, force);
+  return cudaGetLastError();
+}
+
+int ndm_grad_nblocks(int n) { return (n + ndm_grad_chunk() - 1) / ndm_grad_chunk(); }
+
+cudaError_t launch_x_center(float* X, float* Xlo, int rows, int ld, int ns, double* meanO, int tf32,
+                            cudaStream_t st) {
+  x_row_mean_kernel<<<(rows * 32 + 255) / 256, 256, 0, st>>>(X, rows, ld, ns, meanO);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const long tot = (long)rows * ld;
+  x_center_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(X, Xlo, rows, ld, ns, meanO, tf32);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_ndm_effective<float>(const NdmDev<float>&, const NdmEffBufs<float>&, cudaStream_t);
+template cudaError_t launch_ndm_effective<double>(const NdmDev<double>&, const NdmEffBufs<double>&, cudaStream_t);
+template cudaError_t launch_ndm_eval<float>(const NdmEff<float>&, int, const uint64_t*, int, int, cpx<float>*, float*, int, double*, cudaStream_t);
+template cudaError_t launch_ndm_eval<double>(const NdmEff<double>&, int, const uint64_t*, int, int, cpx<double>*, float*, int, double*, cudaStream_t);
+template cudaError_t launch_ndm_loc<float>(const NdmEff<float>&, int, const DevOp&, const uint64_t*, int, int, int, cpx<float>*, cpx<float>*, int*, int*, cudaStream_t);
+template cudaError_t launch_ndm_loc<double>(const NdmEff<double>&, int, const DevOp&, const uint64_t*, int, int, int, cpx<double>*, cpx<double>*, int*, int*, cudaStream_t);
+template cudaError_t launch_ndm_grad<float>(const NdmEff<float>&, int, const DevOp&, const uint64_t*, int, int, int, const cpx<float>*, const cpx<float>*, const int*, const int*, double*, const double*, const double*, double*, cudaStream_t);
+template cudaError_t launch_ndm_grad<double>(const NdmEff<double>&, int, const DevOp&, const uint64_t*, int, int, int, const cpx<double>*, const cpx<double>*, const int*, const int*, double*, const double*, const double*, double*, cudaStream_t);

@@ -1,0 +1,63 @@
+// Launch interfaces of the NDM (purified density matrix) path.
+#pragma once
+#include "nq_kernels.cuh"
+
+// Real NDM parameters (reference flat order), pointers into one array.
+template <typename R> struct NdmDev {
+  int N = 0, Mh = 0, Ma = 0;
+  const R *b_mu = nullptr, *h_mu = nullptr, *w_mu = nullptr, *u_mu = nullptr;
+  const R *b_la = nullptr, *h_la = nullptr, *d_la = nullptr, *w_la = nullptr, *u_la = nullptr;
+};
+
+template <typename R> NQ_HD NdmDev<R> ndm_view(const R* p, int N, int Mh, int Ma) {
+  NdmDev<R> d;
+  d.N = N; d.Mh = Mh; d.Ma = Ma;
+  const R* q = p;
+  d.b_mu = q; q += N;
+  d.h_mu = q; q += Mh;
+  d.w_mu = q; q += (size_t)Mh * N;
+  d.u_mu = q; q += (size_t)Ma * N;
+  d.b_la = q; q += N;
+  d.h_la = q; q += Mh;
+  d.d_la = q; q += Ma;
+  d.w_la = q; q += (size_t)Mh * N;
+  d.u_la = q;
+  return d;
+}
+
+NQ_HD int ndm_n_params(int N, int Mh, int Ma) { return 2 * N + 2 * Mh + Ma + 2 * Mh * N + 2 * Ma * N; }
+
+// Effective generalised-RBM form over the 2N doubled sites (see ndm.cu).
+template <typename R> struct NdmEff {
+  int N = 0, N2 = 0, Mh = 0, Ma = 0, U = 0, P = 0;
+  const cpx<R>* C = nullptr;   // [U x N2] column-major
+  const cpx<R>* b = nullptr;   // [U]
+  const cpx<R>* a = nullptr;   // [N2]
+};
+
+template <typename R> struct NdmEffBufs {
+  cpx<R>* C = nullptr;    // [U x N2]
+  cpx<R>* b = nullptr;    // [U]
+  cpx<R>* a = nullptr;    // [N2]
+  cpx<R>* Cs = nullptr;   // [Ms x N2] units entering |ρ|^2 (sampler)
+  cpx<R>* bs = nullptr;   // [Ms]
+};
+
+template <typename R>
+cudaError_t launch_ndm_effective(const NdmDev<R>& n, const NdmEffBufs<R>& b, cudaStream_t st);
+template <typename R>
+cudaError_t launch_ndm_eval(const NdmEff<R>& e, int act, const uint64_t* samples, int n, int hilb,
+                            cpx<R>* logrho, float* X, int ldx, double* Oout, cudaStream_t st);
+template <typename R>
+cudaError_t launch_ndm_loc(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+                           int hilb, int maxc, cpx<R>* L, cpx<R>* w, int* wconn, int* nconn, cudaStream_t st);
+template <typename R>
+cudaError_t launch_ndm_grad(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+                            int hilb, int maxc, const cpx<R>* L, const cpx<R>* w, const int* wconn,
+                            const int* nconn, double* partial, const double* meanO, const double* stats,
+                            double* force, cudaStream_t st);
+int ndm_grad_nblocks(int n);
+// centre the rows of X (rows x ld, first ns columns valid), meanO[r] = row mean;
+// tf32: round to TF32 and write the remainder to Xlo (if given)
+cudaError_t launch_x_center(float* X, float* Xlo, int rows, int ld, int ns, double* meanO, int tf32,
+                            cudaStream_t st);

@@ -24,6 +24,8 @@ struct DevOp {
 // of a single flip with Δ = W dv is t0 + g*sign(dv)*t1 (resp. 1 + g*t0|t1).
 template <typename R> struct RbmDev {
   int N = 0, M = 0, act = 0, hilb = 0;
+  int n_half = 0;              // hidden units h < n_half enter log|ψ|^2 with weight 1/2
+                               // (the λ units of the purified density matrix)
   const cpx<R>* a = nullptr;   // [N]
   const cpx<R>* b = nullptr;   // [M]
   const cpx<R>* W = nullptr;   // [M*N] column-major
@@ -34,6 +36,7 @@ template <typename R> struct RbmDev {
 
 cudaError_t launch_rbm_params_from_master(const double* master, int N, int M, float* f32_out,
                                           cudaStream_t st);
+cudaError_t launch_master_to_f32(const double* master, long n, float* f32_out, cudaStream_t st);
 template <typename R>
 cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2,
                               cudaStream_t st);
@@ -127,9 +130,14 @@ cudaError_t launch_chol_solve(const float2* L, const float2* LT, const float2* D
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st);
 
-// w -= lr * dw on the FP64 master vector (complex: 2P doubles, real: P)
-cudaError_t launch_descent(double* master, const double* dw, long n_doubles, double lr,
+// w[i] -= lr * dw[i*stride] on the FP64 master vector (complex parameters:
+// 2P doubles, stride 1; real parameters: P doubles, stride 2 over the complex
+// solution)
+cudaError_t launch_descent(double* master, const double* dw, long n_doubles, int stride, double lr,
                            cudaStream_t st);
+// G = X X^T from a materialised X (rows x ldx, first ns columns), FP32 CUDA cores
+cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float* G, float* partial, int ksplit,
+                               cudaStream_t st);
 
 // Measurement statistics (stats.jl:26-50) of a chains x samples matrix stored
 // sample-major (value index s = chain + B*slot); mode 0: complex values,

@@ -345,6 +345,11 @@ cudaError_t launch_rbm_params_from_master(const double* master, int N, int M, fl
   return cudaGetLastError();
 }
 
+cudaError_t launch_master_to_f32(const double* master, long n, float* f32_out, cudaStream_t st) {
+  master_to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(master, n, f32_out);
+  return cudaGetLastError();
+}
+
 template <typename R>
 cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2,
                               cudaStream_t st) {

@@ -28,7 +28,7 @@ template <typename R, int G, int HPL, int ACT>
 __global__ void __launch_bounds__(256)
 rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = net.N, M = net.M;
+  const int N = net.N, M = net.M, n_half = net.n_half;
   cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
   cpx<R>* s_t1 = s_t0 + N * M;
   cpx<R>* s_t2 = s_t1 + N * M;
@@ -101,7 +101,7 @@ rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
       if (hilb == HILB_SPIN) dv = bit ? R(-2) : R(2);
       else dv = bit ? R(-1) : R(1);
       const bool pos = dv > 0;
-      R prod = R(1);
+      R prod = R(1), prod_half = R(1);
 #pragma unroll
       for (int k = 0; k < HPL; ++k) {
         const int h = lane + G * k;
@@ -115,10 +115,12 @@ rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
             const cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
             rr = cfma(g[k], bb, mk(R(1), R(0)));
           }
-          prod *= abs2c(rr);
+          if (h < n_half) prod_half *= abs2c(rr);
+          else prod *= abs2c(rr);
         }
       }
       R lsum = fast_log2(prod);
+      if (n_half > 0) lsum += R(0.5) * fast_log2(prod_half);
 #pragma unroll
       for (int off = G / 2; off > 0; off >>= 1) lsum += __shfl_xor_sync(gmask, lsum, off, G);
       const R logA = s_are[i] * dv + lsum;                  // log2 of the acceptance ratio

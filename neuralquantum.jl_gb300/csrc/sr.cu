@@ -39,8 +39,10 @@ __device__ __forceinline__ void tile_of(int t, int nt, int* ti, int* tj) {
 // 64x64 output tile per block, 16x16 threads with 4x4 micro tiles, K chunks of
 // 16 samples generated on the fly from (σ, g, <O>).
 constexpr int GT = 64, GK = 16;
+template <bool FROM_X>
 __global__ void __launch_bounds__(256)
-gram_simt_kernel(RbmOSource src, int rows, int nt, int ksplit, float* __restrict__ partial) {
+gram_simt_kernel(RbmOSource src, const float* __restrict__ X, int ldx, int rows, int nt, int ksplit,
+                 float* __restrict__ partial) {
   __shared__ float As[GK][GT + 4];
   __shared__ float Bs[GK][GT + 4];
   int ti, tj;
@@ -59,13 +61,18 @@ gram_simt_kernel(RbmOSource src, int rows, int nt, int ksplit, float* __restrict
       const int t = threadIdx.x % GK;
       const int s = k0 + t;
       const bool ok = s < ke;
-      const uint64_t bits = ok ? src.samples[s] : 0;
+      const uint64_t bits = (ok && !FROM_X) ? src.samples[s] : 0;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         int r = threadIdx.x / GK + 16 * q;
         int ra = ti * GT + r, rb = tj * GT + r;
-        As[t][r] = (ok && ra < rows) ? x_value(src, ra, s, bits) : 0.f;
-        Bs[t][r] = (ok && rb < rows) ? x_value(src, rb, s, bits) : 0.f;
+        if (FROM_X) {
+          As[t][r] = (ok && ra < rows) ? X[(size_t)ra * ldx + s] : 0.f;
+          Bs[t][r] = (ok && rb < rows) ? X[(size_t)rb * ldx + s] : 0.f;
+        } else {
+          As[t][r] = (ok && ra < rows) ? x_value(src, ra, s, bits) : 0.f;
+          Bs[t][r] = (ok && rb < rows) ? x_value(src, rb, s, bits) : 0.f;
+        }
       }
     }
     __syncthreads();
@@ -249,9 +256,9 @@ __global__ void rhs_init_kernel(const double* F, int P, int real_params, float2*
   rf[i] = make_float2((float)F[2 * i], real_params ? 0.f : (float)F[2 * i + 1]);
 }
 
-__global__ void descent_kernel(double* w, const double* dw, long n, double lr) {
+__global__ void descent_kernel(double* w, const double* dw, long n, int stride, double lr) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < n) w[i] -= lr * dw[i];
+  if (i < n) w[i] -= lr * dw[i * stride];
 }
 
 // ---------------------------------------------------------------------------
@@ -345,7 +352,22 @@ cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* part
   const int nt = (rows + GT - 1) / GT;
   const int ntiles = nt * (nt + 1) / 2;
   dim3 grid(ntiles, ksplit);
-  gram_simt_kernel<<<grid, 256, 0, st>>>(src, rows, nt, ksplit, partial);
+  gram_simt_kernel<false><<<grid, 256, 0, st>>>(src, nullptr, 0, rows, nt, ksplit, partial);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  long tot = (long)rows * rows;
+  gram_reduce_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(partial, rows, nt * GT, GT, ksplit, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float* G, float* partial, int ksplit,
+                               cudaStream_t st) {
+  const int nt = (rows + GT - 1) / GT;
+  const int ntiles = nt * (nt + 1) / 2;
+  dim3 grid(ntiles, ksplit);
+  RbmOSource src;
+  src.Ns = ns;
+  gram_simt_kernel<true><<<grid, 256, 0, st>>>(src, X, ldx, rows, nt, ksplit, partial);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   long tot = (long)rows * rows;
@@ -403,9 +425,9 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   return cudaSuccess;
 }
 
-cudaError_t launch_descent(double* master, const double* dw, long n_doubles, double lr,
+cudaError_t launch_descent(double* master, const double* dw, long n_doubles, int stride, double lr,
                            cudaStream_t st) {
-  descent_kernel<<<(unsigned)((n_doubles + 255) / 256), 256, 0, st>>>(master, dw, n_doubles, lr);
+  descent_kernel<<<(unsigned)((n_doubles + 255) / 256), 256, 0, st>>>(master, dw, n_doubles, stride, lr);
   return cudaGetLastError();
 }
 
