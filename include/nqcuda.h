@@ -228,6 +228,38 @@ nq_status nq_tuning(nq_handle* h, int32_t* out, int32_t n);
 /* Number of kernel launches issued by this handle since creation. */
 int64_t nq_kernel_launches(const nq_handle* h);
 
+/* ---- learned autoregressive proposal (no counterpart in the reference) ------
+ * The reference samples with local rules only (src/Samplers/MCMCRules/
+ * LocalRule.jl:19-28 under Metropolis.jl:101-167).  These calls attach a MADE
+ * network q(x) = Π_i p(x_i | x_<i) (N -> hidden -> hidden -> N, ReLU,
+ * Bernoulli outputs; FP32 master, BF16 inference copy) to an RBM handle with
+ * N <= 64.  With a mixing probability p_ar > 0, nq_sample / nq_vmc_step run
+ * the mixture sampler: every step is an AR independence move with probability
+ * p_ar (accepted with |ψ(x')|² q(x) / (|ψ(x)|² q(x'))), else a local flip.
+ * Configurations are passed as uint64 bit strings: bit i = local index of site
+ * i (spin up / occupied = 1).  Parameter order: W1 [H][N], b1 [H], W2 [H][H],
+ * b2 [H], W3 [N][H], b3 [N]; autoregressive-masked entries are forced to 0. */
+nq_status nq_proposal_init(nq_handle* h, int32_t hidden, double p_ar, uint64_t seed);
+nq_status nq_proposal_set_mix(nq_handle* h, double p_ar);
+int64_t nq_proposal_n_params(const nq_handle* h);
+nq_status nq_proposal_set_params(nq_handle* h, const float* p, int64_t n);
+nq_status nq_proposal_get_params(nq_handle* h, float* p, int64_t n);
+/* out[k] = log q(x[k]) */
+nq_status nq_proposal_logq(nq_handle* h, const uint64_t* x, int64_t n, float* out);
+/* The proposals the mixture sampler would draw in sample call `call_index`:
+ * for chain c and AR slot s, x_out[c*slots + s] and lq_out[c*slots + s]. */
+nq_status nq_proposal_sample(nq_handle* h, uint64_t call_index, int32_t slots, uint64_t* x_out,
+                             float* lq_out);
+/* Masked gradient of the mean negative log-likelihood of x[0..n) (grad_out,
+ * nq_proposal_n_params floats, nullable) and that mean (nll_out, nullable). */
+nq_status nq_proposal_grad(nq_handle* h, const uint64_t* x, int64_t n, float* grad_out, double* nll_out);
+/* `steps` Adam steps (lr) on minibatches of `batch` configurations taken in
+ * order from the samples of the last sample call; nll_out (nullable) = mean
+ * NLL over all those samples after training. */
+nq_status nq_proposal_train(nq_handle* h, int32_t steps, int32_t batch, double lr, double* nll_out);
+/* AR moves proposed and accepted during the last sample call (2 values). */
+nq_status nq_proposal_stats(nq_handle* h, uint64_t* out2);
+
 #ifdef __cplusplus
 }
 #endif

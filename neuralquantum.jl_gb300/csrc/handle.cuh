@@ -1,0 +1,140 @@
+// Internal state of a libnqcuda handle and the helpers shared by the C-ABI
+// translation units (api.cu, proposal.cu).
+#pragma once
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/nqcuda.h"
+#include "ndm_kernels.cuh"
+#include "made_kernels.cuh"
+
+struct MadeState;   // learned proposal (proposal.cu)
+
+struct nq_handle {
+  nq_config cfg{};
+  int N = 0, M = 0, nst = 0, P = 0, B = 0, L = 0, Ns = 0, passes = 1;
+  int n_record = 0, write_last = 0;
+  bool doubled = false, complex_params = true, f64 = false, ndm = false;
+  int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
+  void* d_eff[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // C, b, a, Cs, bs (cpx<R>)
+  void* d_w = nullptr;             // NDM connection weights [Ns][maxc] cpx<R>
+  int* d_wconn = nullptr;          // connection ids [Ns][maxc]
+  int* d_nconn = nullptr;          // connections per sample [Ns]
+  int maxc = 0;
+  double* d_ndm_partial = nullptr; // [nblk][2P]
+  int hilb = 0, act = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int64_t launches = 0;
+
+  double* d_master = nullptr;      // FP64 master parameters (complex interleaved or real)
+  float* d_p32 = nullptr;          // FP32 working copy (RBM, complex)
+  void* d_tab[3] = {nullptr, nullptr, nullptr};
+  uint64_t* d_samples = nullptr;   // [L][B]
+  unsigned long long* d_accepted = nullptr;
+  uint32_t* d_call = nullptr;
+  void* d_logpsi = nullptr;        // cpx<R>[Ns]
+  void* d_g = nullptr;             // cpx<R>[M][Ns]
+  void* d_eloc = nullptr;          // cpx<R>[Ns]
+  float2* d_g32 = nullptr;         // FP32 view of g for the S stage
+  ForceBufs fb;
+  int force_nblk = 0;
+  double* d_stats = nullptr;       // 6 doubles
+  double* d_chainstats = nullptr;  // [B][3] chain mean (re, im) and variance
+  float* d_G = nullptr;
+  float* d_Gpart = nullptr;
+  int gram_ksplit = 1;
+  float* d_X = nullptr;
+  float* d_Xlo = nullptr;
+  int Ns_pad = 0;
+  double* d_S = nullptr;
+  SolveBufs sb;
+  double* d_dw = nullptr;          // Δw as stored for the update (complex or real)
+  DevOp op;
+  bool has_op = false;
+  std::vector<void*> op_allocs;
+
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_kernels = 0;
+  double graph_eps = -1, graph_lr = -1;
+  uint32_t* h_call = nullptr;      // pinned
+  double* h_stats = nullptr;       // pinned [8]
+  unsigned long long* h_acc = nullptr;
+  cudaEvent_t ev[7] = {};
+  cudaEvent_t kev[4] = {};
+  cudaEvent_t sev[6] = {};
+  float stage_ms[12] = {};
+  bool capturing = false;
+  int sampler_lanes = 0;           // lanes per chain chosen by the autotuner (0 = not tuned)
+  void* d_flush = nullptr;
+  size_t flush_bytes = 0;
+  MadeState* made = nullptr;       // learned proposal, null until nq_proposal_init
+};
+
+inline nq_status fail(nq_handle* h, nq_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  return code;
+}
+
+#define CK(expr)                                                                          \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess)                                                                \
+      return fail(h, NQ_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                  __FILE__, __LINE__);                                                    \
+  } while (0)
+
+#define CKL(expr)       \
+  do {                  \
+    ++h->launches;      \
+    CK(expr);           \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  return cudaMalloc((void**)p, count * sizeof(T) + 16);
+}
+
+// Sampler / table view of the network: the RBM itself, or for the NDM the
+// effective network of the units entering |ρ|^2 over the 2N doubled sites.
+template <typename R>
+RbmDev<R> rbm_dev(nq_handle* h) {
+  RbmDev<R> d;
+  d.act = h->act; d.hilb = h->hilb;
+  if (h->ndm) {
+    d.N = h->N2; d.M = h->Ms; d.n_half = 2 * h->Mh;
+    d.a = reinterpret_cast<const cpx<R>*>(h->d_eff[2]);
+    d.b = reinterpret_cast<const cpx<R>*>(h->d_eff[4]);
+    d.W = reinterpret_cast<const cpx<R>*>(h->d_eff[3]);
+  } else {
+    d.N = h->N; d.M = h->M;
+    const cpx<R>* base;
+    if (h->f64) base = reinterpret_cast<const cpx<R>*>(h->d_master);
+    else base = reinterpret_cast<const cpx<R>*>(h->d_p32);
+    d.a = base;
+    d.b = base + h->N;
+    d.W = base + h->N + h->M;
+  }
+  d.t0 = reinterpret_cast<const cpx<R>*>(h->d_tab[0]);
+  d.t1 = reinterpret_cast<const cpx<R>*>(h->d_tab[1]);
+  d.t2 = reinterpret_cast<const cpx<R>*>(h->d_tab[2]);
+  return d;
+}
+
+// learned-proposal hooks used by the stage sequence (proposal.cu)
+void proposal_destroy(nq_handle* h);
+// launches the mixture sampler when a proposal with p_ar > 0 is attached; *used = false otherwise
+nq_status proposal_sample_stage(nq_handle* h, const SamplerRun& run, bool* used);

@@ -17,7 +17,8 @@ CSRC = os.path.join(_ROOT, "csrc")
 INCLUDE = os.path.join(_REPO, "include")
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
-SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "chol.cu", "ndm.cu"]
+SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "chol.cu", "ndm.cu",
+           "made.cu", "mix_sampler.cu", "proposal.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -95,6 +96,19 @@ EXPORTS = {
     "nq_bench_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                       _P(ctypes.c_float)]),
+    "nq_proposal_init": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64]),
+    "nq_proposal_set_mix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "nq_proposal_n_params": (ctypes.c_int64, [ctypes.c_void_p]),
+    "nq_proposal_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "nq_proposal_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "nq_proposal_logq": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "nq_proposal_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "nq_proposal_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                        _P(ctypes.c_double)]),
+    "nq_proposal_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                         _P(ctypes.c_double)]),
+    "nq_proposal_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 _lib = None

@@ -167,3 +167,49 @@ class Engine:
 
     def kernel_launches(self):
         return int(self.lib.nq_kernel_launches(self.h))
+
+    # ---- learned autoregressive proposal (MADE), nq_proposal_* -------------
+    def proposal_init(self, hidden=128, p_ar=0.5, seed=0):
+        self._check(self.lib.nq_proposal_init(self.h, hidden, float(p_ar), seed))
+        self.proposal_P = int(self.lib.nq_proposal_n_params(self.h))
+
+    def proposal_set_mix(self, p_ar):
+        self._check(self.lib.nq_proposal_set_mix(self.h, float(p_ar)))
+
+    def proposal_set_params(self, flat):
+        v = np.ascontiguousarray(flat, dtype=np.float32)
+        self._check(self.lib.nq_proposal_set_params(self.h, v.ctypes.data, v.size))
+
+    def proposal_get_params(self):
+        v = np.empty(self.proposal_P, dtype=np.float32)
+        self._check(self.lib.nq_proposal_get_params(self.h, v.ctypes.data, v.size))
+        return v
+
+    def proposal_logq(self, x_bits):
+        x = np.ascontiguousarray(x_bits, dtype=np.uint64)
+        out = np.empty(x.size, dtype=np.float32)
+        self._check(self.lib.nq_proposal_logq(self.h, x.ctypes.data, x.size, out.ctypes.data))
+        return out
+
+    def proposal_sample(self, call_index, slots):
+        x = np.empty(self.B * slots, dtype=np.uint64)
+        lq = np.empty(self.B * slots, dtype=np.float32)
+        self._check(self.lib.nq_proposal_sample(self.h, call_index, slots, x.ctypes.data, lq.ctypes.data))
+        return x.reshape(self.B, slots), lq.reshape(self.B, slots)
+
+    def proposal_grad(self, x_bits):
+        x = np.ascontiguousarray(x_bits, dtype=np.uint64)
+        g = np.empty(self.proposal_P, dtype=np.float32)
+        nll = ctypes.c_double()
+        self._check(self.lib.nq_proposal_grad(self.h, x.ctypes.data, x.size, g.ctypes.data, ctypes.byref(nll)))
+        return g, nll.value
+
+    def proposal_train(self, steps, batch, lr):
+        nll = ctypes.c_double()
+        self._check(self.lib.nq_proposal_train(self.h, steps, batch, float(lr), ctypes.byref(nll)))
+        return nll.value
+
+    def proposal_stats(self):
+        v = np.zeros(2, dtype=np.uint64)
+        self._check(self.lib.nq_proposal_stats(self.h, v.ctypes.data))
+        return int(v[0]), int(v[1])

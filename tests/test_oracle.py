@@ -191,3 +191,68 @@ def test_c_port_matches_numpy_oracle():
     Oc, _ = oest.center(O)
     dwo = osr.precondition(osr.build_S(Oc, False), oest.force_ket(Eo, O), 0.01)
     assert np.max(np.abs(dw - dwo)) < 1e-8 * max(1, np.max(np.abs(dwo)))
+
+
+def test_made_oracle_gradient_mask_and_normalisation():
+    """MADE oracle: q sums to 1 over the space, the NLL gradient matches
+    central differences, and masked weights get a zero gradient."""
+    from oracle import made as om
+    N = 5
+    m = om.MADE(N, 128, rng=np.random.default_rng(1))
+    rng = np.random.default_rng(2)
+    m.b1, m.b2, m.b3 = rng.standard_normal(128) * 0.3, rng.standard_normal(128) * 0.3, rng.standard_normal(N)
+    allx = om.bits_to_x(np.arange(2 ** N, dtype=np.uint64), N)
+    assert abs(np.exp(m.logq(allx)).sum() - 1.0) < 1e-12
+    x = allx[rng.integers(0, 2 ** N, size=40)]
+    _, g = m.nll_grad(x)
+    p0 = m.flat()
+    for k in rng.choice(p0.size, 25, replace=False):
+        e = np.zeros_like(p0)
+        e[k] = 1e-6
+        m.set_flat(p0 + e)
+        fp = m.nll_grad(x)[0]
+        m.set_flat(p0 - e)
+        fm = m.nll_grad(x)[0]
+        m.set_flat(p0)
+        assert abs((fp - fm) / 2e-6 - g[k]) < 1e-6
+    M1, M2, M3 = om.masks(N, 128)
+    mask = np.concatenate([M1.ravel(), np.ones(128), M2.ravel(), np.ones(128), M3.ravel(), np.ones(N)])
+    assert np.all(g[mask == 0] == 0)
+
+
+def test_made_bf16_rounding_matches_torch():
+    """The inference copy rounds like a float32 -> bfloat16 conversion."""
+    torch = pytest.importorskip("torch")
+    from oracle import made as om
+    v = np.random.default_rng(0).standard_normal(10000).astype(np.float32) * 3
+    v[:4] = [1.00390625, 1.01171875, -1.00390625, 0.0]        # exact ties either way
+    ref = torch.tensor(v).to(torch.bfloat16).to(torch.float64).numpy()
+    np.testing.assert_array_equal(om.to_bf16(v), ref)
+
+
+def test_mixture_oracle_with_exact_proposal_always_accepts():
+    """With q equal to the normalised |ψ|² every AR move is accepted, so the
+    mixture replay's AR bookkeeping and acceptance ratio are consistent."""
+    from oracle import made as om
+    N, B = 4, 16
+    h = Hilbert(N, SPIN)
+    r = nw.RBM(N, 8, nw.LOGCOSH)
+    nw.init_random_pars(r, np.random.default_rng(5), sigma=0.3 ** 2)
+
+    class ExactQ:
+        def __init__(self):
+            allx = om.bits_to_x(np.arange(2 ** N, dtype=np.uint64), N)
+            lp = r.log_prob(2 * allx - 1)
+            self.lq = lp - np.log(np.sum(np.exp(lp)))
+
+        def logq(self, x):
+            return self.lq[om.x_to_bits(x).astype(np.int64)]
+
+        def sample_with_uniforms(self, u):
+            cdf = np.cumsum(np.exp(self.lq))
+            idx = np.minimum(np.searchsorted(cdf, u[:, 0]), 2 ** N - 1)
+            return om.bits_to_x(idx.astype(np.uint64), N)
+
+    _, info = om.run_mixture(r.log_prob, h, ExactQ(), 1.0, B, 3, 2, 3, 17, call=1)
+    assert info["ar"] == info["steps"]
+    assert info["ar_accepted"] == info["ar"]
