@@ -260,6 +260,39 @@ nq_status nq_proposal_train(nq_handle* h, int32_t steps, int32_t batch, double l
 /* AR moves proposed and accepted during the last sample call (2 values). */
 nq_status nq_proposal_stats(nq_handle* h, uint64_t* out2);
 
+/* ---- allocation-free chain statistics (no counterpart in the reference) -----
+ * The Measurement of nq_estimate (mean, error, variance, tau, R, following
+ * src/utils/stats.jl:26-50) computed from local values that already sit in
+ * the caller's device memory, without a handle and without allocating any
+ * device memory: no cudaMalloc, cudaFree or allocating library call.  It is
+ * meant for callers that cannot allocate at this point: a host program that
+ * hands all device memory to its own pool allocator (CUDA.jl's pool, PyTorch's
+ * caching allocator) and runs close to the memory limit, where an allocation
+ * from inside the library could fail or make the pool release its cache, and
+ * latency-critical loops where cudaMalloc / cudaFree would synchronise the
+ * device.
+ *   d_values : n_chains * chain_length complex values on the current device,
+ *              value of chain c at sweep l at index l * n_chains + c
+ *              (dtype NQ_DTYPE_C64 or NQ_DTYPE_C128).
+ *   kind     : 0 = statistics of the values, 1 = of their squared modulus.
+ *   d_out6   : 6 doubles on the current device, written with
+ *              [mean_re, mean_im, error, variance, tau, R].
+ *   stream   : cudaStream_t the two kernels are queued on (NULL = default);
+ *              the call returns without waiting for them.
+ *   err      : optional buffer for a message when the status is not NQ_OK.
+ * Limit: n_chains <= NQ_NOALLOC_MAX_CHAINS.  The per-chain scratch (3 doubles
+ * per chain, 1.5 MiB) is one fixed device array shared by every call on a
+ * device; nothing in it needs to start at zero.  Calls whose kernels can
+ * overlap in time (different streams, or several host threads) race on that
+ * array: order them on one stream or with events.  The first call on each
+ * device looks the array's address up once (cudaGetSymbolAddress), which may
+ * load the library's device code on that device; make that first call before
+ * any stream capture begins. */
+#define NQ_NOALLOC_MAX_CHAINS 65536
+nq_status nq_measurement_noalloc(const void* d_values, int32_t dtype, int32_t n_chains,
+                                 int32_t chain_length, int32_t kind, double* d_out6, void* stream,
+                                 char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ INCLUDE = os.path.join(_REPO, "include")
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "chol.cu", "ndm.cu",
-           "made.cu", "mix_sampler.cu", "proposal.cu"]
+           "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -109,6 +109,9 @@ EXPORTS = {
     "nq_proposal_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                          _P(ctypes.c_double)]),
     "nq_proposal_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "nq_measurement_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                              ctypes.c_size_t]),
 }
 
 _lib = None
