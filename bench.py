@@ -127,8 +127,13 @@ def s_precision_choice():
     return nq._lib.NQ_S_TF32
 
 
+# DRAM bytes (read + write) of one gram_tf32_kernel launch on this workload, from
+# the ncu capture summarised in profiles/gram_tf32_c1.txt
+GRAM_TRAFFIC_BYTES = 742.76e6
+
+
 def effective_samples_per_s(loc, sample_ms):
-    from oracle.stats import integrated_autocorr_time   # checker-side helper, host only
+    from nqcuda.stats import integrated_autocorr_time
     tau = integrated_autocorr_time(loc.T)
     ns = loc.size
     return ns / tau / (sample_ms / 1e3), tau
@@ -177,18 +182,24 @@ def run_gb300(args):
     e2e = {"value": args.steps / e2e_s, "unit": "SR steps/s", "h2d_bytes_per_step": 16 * P,
            "d2h_bytes_per_step": 16 * P + 8 * 7}
 
-    # roofline of the dominant kernel (largest stage share)
+    # roofline of the tensor-core kernel; shares of the three largest kernels
     Ns = w["chains"] * w["chain_length"]
+    kernels = {"sampler": st[6], "S_accumulation": st[7], "factorisation": st[8]}
+    ksum = sum(kernels.values())
     stages = {"sample": st[0], "eval_estimator": st[1], "force_stats": st[2], "S": st[3],
               "solve": st[4], "update": st[5]}
     s_kernel_ms = st[7]
-    s_flops = 4.0 * P * P * Ns * 2.0 / 2.0 * 2.0   # upper triangle of the 2P x 2P real Gram: 2*(2P)^2*Ns/2
+    s_flops = 2.0 * (2 * P) ** 2 * Ns / 2.0        # upper triangle of the 2P x 2P real Gram
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     roof = {"kernel": "S accumulation (G = X Xᵀ, upper tiles)", "bound": "tensor",
             "achieved": s_flops / (s_kernel_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
-            "frac": None, "traffic": None,
-            "note": "peak = measured dense bf16 burst; algorithmic flops = 2*(2P)^2*Ns/2 per launch"}
+            "frac": None, "traffic": GRAM_TRAFFIC_BYTES,
+            "note": "peak = measured dense bf16 burst (of measured); algorithmic flops = 2*(2P)^2*Ns/2 "
+                    "per launch; TF32 operands, so the bf16 peak is an upper bound twice the TF32 rate"}
     roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["kernel_ms"] = kernels
+    roof["dominant_kernel"] = max(kernels, key=kernels.get)
+    roof["share_of_three"] = {k: v / ksum for k, v in kernels.items()}
 
     line = {
         "metric": METRIC, "value": value, "unit": "SR steps/s", "n_gpus": args.gpus,
@@ -198,7 +209,7 @@ def run_gb300(args):
         "config": workload_config({"s_precision": int(sp)}),
         "clocks": clk.summary(), "e2e": e2e, "gpu_launches": int(launches),
         "effective_samples_per_s": ess, "tau_int_eloc": tau, "energy_per_site": m.mean_re / w["N"],
-        "stage_ms": stages, "kernel_ms": {"sampler": st[6], "S_accumulation": st[7]},
+        "stage_ms": stages, "kernel_ms": kernels,
         "tuning": eng.tuning(),
         "roofline": roof,
     }
@@ -241,7 +252,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

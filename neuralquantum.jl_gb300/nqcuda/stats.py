@@ -14,3 +14,33 @@ class Measurement:
             ms = f"{m:6.4f}"
         return (f"({ms}) ± {self.error:6.4f} [var={self.variance:6.4f}, tau={self.tau:6.4f}, "
                 f"R={self.R:6.4f}]")
+
+
+def integrated_autocorr_time(x, window=5.0):
+    """Integrated autocorrelation time of a (chains, samples) series, in
+    samples: the chain-averaged autocovariance (computed by FFT) summed up to
+    the first lag M with M >= window * tau (Sokal's self-consistent window).
+    The reference reports only its ``tau`` of ``Measurement``; this one backs
+    the effective-sample-size figures."""
+    import numpy as np
+    v = np.asarray(x, dtype=np.complex128)
+    v = v - v.mean(axis=1, keepdims=True)
+    n = v.shape[1]
+    spec = np.fft.fft(v, n=2 * n, axis=1)
+    acov = np.fft.ifft(np.abs(spec) ** 2, axis=1)[:, :n].real.mean(axis=0)
+    if not acov[0] > 0:
+        return 0.5
+    rho = acov / acov[0]
+    tau = 0.5
+    for lag in range(1, n):
+        tau += rho[lag]
+        if lag >= window * tau:
+            break
+    return max(tau, 0.5)
+
+
+def effective_sample_size(x, window=5.0):
+    """Number of samples divided by the integrated autocorrelation time."""
+    import numpy as np
+    v = np.asarray(x)
+    return v.size / integrated_autocorr_time(v, window)
