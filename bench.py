@@ -184,7 +184,7 @@ def run_gb300(args):
 
     # roofline of the tensor-core kernel; shares of the three largest kernels
     Ns = w["chains"] * w["chain_length"]
-    kernels = {"sampler": st[6], "S_accumulation": st[7], "factorisation": st[8]}
+    kernels = {"sampler": st[6], "S_accumulation": st[7], "inversion": st[8]}
     ksum = sum(kernels.values())
     stages = {"sample": st[0], "eval_estimator": st[1], "force_stats": st[2], "S": st[3],
               "solve": st[4], "update": st[5]}

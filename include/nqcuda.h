@@ -198,8 +198,10 @@ nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
 
 /* ---- precondition!(prec, SR, iter) ----------------------------------------
  * kind: 0 = sr_shift (S_ii += eps), 1 = sr_multiplicative
- * (S + max(lam0*b^iter, lam_min) diag S), 2 = sr_none.  Cholesky solve of
- * S Δw = F.  dw_out (nullable) receives Δw (complex128 or float64). */
+ * (S + max(lam0*b^iter, lam_min) diag S), 2 = sr_none.  The reference's
+ * Cholesky solve of S Δw = F becomes an FP32 inverse of the shifted S (block
+ * Gauss–Jordan) with FP64-residual refinement.  dw_out (nullable) receives Δw
+ * (complex128 or float64). */
 nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0,
                           double b, double lam_min, int32_t iter, double* dw_out);
 
@@ -214,8 +216,8 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
 /* ---- timing/diagnostics ----------------------------------------------------
  * Device milliseconds of the last staged calls (CUDA events on the handle's
  * stream), 12 floats: [sample, eval+estimator, force+stats, S, solve, update,
- * sampler kernel alone, S-accumulation kernel alone, factorisation,
- * transpose+rhs, first triangular solve, refinement]. */
+ * sampler kernel alone, S-accumulation kernel alone, inversion of the shifted
+ * S, right-hand side, first solve, FP64 refinement]. */
 nq_status nq_stage_times(nq_handle* h, float* ms12);
 /* Benchmark helper: n_steps whole iterations (graph replays, call indices
  * call0, call0+1, ...); between steps, outside the timed events, a kernel

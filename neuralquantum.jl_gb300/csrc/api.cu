@@ -5,6 +5,10 @@
 
 namespace {
 
+// FP64-residual corrections after the first solve with the FP32 inverse; each
+// gains about -log10(cond(S + shift) * 6e-8) digits
+constexpr int kSolveRefine = 3;
+
 
 template <typename R>
 NdmEff<R> ndm_eff(nq_handle* h) {
@@ -225,7 +229,7 @@ nq_status stage_S(nq_handle* h) {
 nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
   SolveBufs sb = h->sb;
   sb.ev = h->capturing ? nullptr : h->sev;
-  CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, 1, h->st));
+  CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, kSolveRefine, h->st));
   h->launches += 8;
   return NQ_OK;
 }
@@ -413,14 +417,14 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
   }
   step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
-  step(dalloc(&h->sb.Lf, (size_t)P * P), "Lf");
-  step(dalloc(&h->sb.LT, (size_t)P * P), "LT");
+  step(dalloc(&h->sb.W, (size_t)P * P), "W");
   step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
   step(dalloc(&h->sb.r, 2 * (size_t)P), "r");
   step(dalloc(&h->sb.rf, (size_t)P), "rf");
   step(dalloc(&h->sb.status, 1), "status");
-  step(cudaMalloc(&h->sb.ctl, chol_ctl_bytes()), "chol ctl");
-  step(dalloc(&h->sb.Dinv, (size_t)((P + 31) / 32) * 32 * 32), "Dinv");
+  step(cudaMalloc(&h->sb.ctl, sweep_ctl_bytes()), "sweep ctl");
+  step(dalloc(&h->sb.work, sweep_work_elems(P)), "sweep work");
+  step(dalloc(&h->sb.yf, (size_t)P), "yf");
   h->sb.S = h->d_S;
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
@@ -455,8 +459,8 @@ void nq_destroy(nq_handle* h) {
                   h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
-                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.Lf, h->sb.LT, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.status, h->sb.ctl, h->sb.Dinv, h->d_dw, h->d_eff[0], h->d_eff[1],
+                  h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
   for (void* p : bufs)
     if (p) cudaFree(p);

@@ -106,27 +106,29 @@ cudaError_t launch_gram_reduce(const float* partial, int rows, int rp, int tile,
 cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_params, double* S,
                               cudaStream_t st);
 
-// shifted FP32 factorisation + FP64 iterative refinement solve of S x = F.
+// block Gauss–Jordan inverse of the Hermitian positive-definite W in place (W <- -W^-1,
+// full Hermitian afterwards), one cooperative launch; ctl: sweep_ctl_bytes()
+size_t sweep_ctl_bytes();
+size_t sweep_work_elems(int P);
+cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st);
+// y = -W x for the full Hermitian W
+cudaError_t launch_herm_gemv_neg(const float2* W, int P, const float2* x, float2* y, cudaStream_t st);
+
 struct SolveBufs {
   double* S = nullptr;        // [P*P] complex (input, untouched)
-  float2* Lf = nullptr;       // [P*P] complex float factor workspace
-  float2* LT = nullptr;       // [P*P] conjugate transpose of the factor
+  float2* W = nullptr;        // [P*P] complex float: shifted S, then -(S + shift)^-1 (full Hermitian)
+  float2* work = nullptr;     // sweep workspace: sweep_work_elems(P) complex floats
   double* x = nullptr;        // [P] complex solution
   double* r = nullptr;        // [P] complex residual
-  float2* rf = nullptr;       // [P] complex float rhs workspace
+  float2* rf = nullptr;       // [P] complex float right-hand side of the next correction
+  float2* yf = nullptr;       // [P] complex float correction
   int* status = nullptr;      // device status word
-  void* ctl = nullptr;        // grid-barrier control block of the cooperative factorisation
-  float2* Dinv = nullptr;     // [ceil(P/32)][32][32] inverses of the diagonal blocks
-  cudaEvent_t* ev = nullptr;  // optional [6] events: copy, factor, transpose, solve, residual, end
+  void* ctl = nullptr;        // grid-barrier control block of the cooperative sweep
+  cudaEvent_t* ev = nullptr;  // optional [6] events: copy, inversion, fill+rhs, first solve, refinement, end
 };
-size_t chol_ctl_bytes();
-// blocked Cholesky of the lower triangle of A (P x P complex float,
-// column-major) in one cooperative launch; pivots <= 0 set bit 0 of status.
-// Dinv receives the row-major inverse of every 32x32 diagonal block.
-cudaError_t launch_chol_coop(float2* A, int P, void* ctl, int* status, float2* Dinv, cudaStream_t st);
-// L y = b, Lᴴ x = y in place on rhs (P <= 6000: rhs staged in shared memory)
-cudaError_t launch_chol_solve(const float2* L, const float2* LT, const float2* Dinv, int P, float2* rhs,
-                              cudaStream_t st);
+// shifted solve (S + shift) x = F: FP32 explicit inverse, then x_0 = A^-1 F and
+// refine_iters corrections x += A^-1 (F - A x) with the residual in FP64;
+// a pivot <= 0 sets bit 0 of status
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st);
 

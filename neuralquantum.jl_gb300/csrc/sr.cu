@@ -171,13 +171,13 @@ __device__ __forceinline__ double diag_shift(const double* S, int P, int i, int 
 }
 
 __global__ void shift_copy_kernel(const double* __restrict__ S, int P, int kind, double eps,
-                                  double lam, float2* __restrict__ Lf) {
+                                  double lam, float2* __restrict__ W) {
   long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (idx >= (long)P * P) return;
   int i = (int)(idx % P), j = (int)(idx / P);
   double re = S[2 * idx], im = S[2 * idx + 1];
   if (i == j) { re += diag_shift(S, P, i, kind, eps, lam); im = 0.0; }
-  Lf[idx] = make_float2((float)re, (float)im);
+  W[idx] = make_float2((float)re, (float)im);
 }
 
 
@@ -188,25 +188,6 @@ __device__ __forceinline__ float2 f2mulconj(float2 a, float2 b) {  // a * conj(b
   return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 
-// LT = Lᴴ (column-major) for coalesced backward substitution
-__global__ void conj_transpose_kernel(const float2* __restrict__ L, int P, float2* __restrict__ LT) {
-  __shared__ float2 t[32][33];
-  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    int row = by + r, col = bx + threadIdx.x;       // read L[col + P*row] coalesced over col
-    if (row < P && col < P) t[r][threadIdx.x] = L[(size_t)col + (size_t)P * row];
-  }
-  __syncthreads();
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    int row = bx + r, col = by + threadIdx.x;        // LT[col + P*row] = conj(L[row + P*col])
-    if (row < P && col < P) {
-      float2 v = t[threadIdx.x][r];
-      LT[(size_t)col + (size_t)P * row] = make_float2(v.x, -v.y);
-    }
-  }
-}
-
-// FP64 residual r = F - (S + D) x with x updated by the FP32 correction d
 __global__ void refine_update_kernel(double* x, const float2* __restrict__ d, int P, int first) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
@@ -401,22 +382,20 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   auto mark = [&](int k) { if (sb.ev) cudaEventRecord(sb.ev[k], st); };
   long tot = (long)P * P;
   mark(0);
-  shift_copy_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(sb.S, P, kind, eps, lam, sb.Lf);
+  shift_copy_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(sb.S, P, kind, eps, lam, sb.W);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   mark(1);
-  e = launch_chol_coop(sb.Lf, P, sb.ctl, sb.status, sb.Dinv, st);
+  e = launch_spd_inverse(sb.W, P, sb.ctl, sb.status, sb.work, st);
   if (e != cudaSuccess) return e;
   mark(2);
-  dim3 tb(32, 8), tg((P + 31) / 32, (P + 31) / 32);
-  conj_transpose_kernel<<<tg, tb, 0, st>>>(sb.Lf, P, sb.LT);
   rhs_init_kernel<<<(P + 255) / 256, 256, 0, st>>>(F, P, real_params ? 1 : 0, sb.rf);
   mark(3);
   for (int it = 0; it <= refine_iters; ++it) {
-    e = launch_chol_solve(sb.Lf, sb.LT, sb.Dinv, P, sb.rf, st);
+    e = launch_herm_gemv_neg(sb.W, P, sb.rf, sb.yf, st);
     if (e != cudaSuccess) return e;
     if (it == 0) mark(4);
-    refine_update_kernel<<<(P + 255) / 256, 256, 0, st>>>(sb.x, sb.rf, P, it == 0);
+    refine_update_kernel<<<(P + 255) / 256, 256, 0, st>>>(sb.x, sb.yf, P, it == 0);
     residual_kernel<<<P, 128, 0, st>>>(sb.S, P, F, sb.x, kind, eps, lam, real_params ? 1 : 0, sb.r, sb.rf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

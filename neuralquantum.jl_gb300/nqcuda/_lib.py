@@ -17,7 +17,7 @@ CSRC = os.path.join(_ROOT, "csrc")
 INCLUDE = os.path.join(_REPO, "include")
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
-SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "chol.cu", "ndm.cu",
+SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
            "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]

@@ -149,7 +149,7 @@ class Engine:
 
     def stage_times(self):
         """[sample, eval, force+stats, S, solve, update, sampler kernel, S kernel,
-        factorisation, transpose+rhs, first solve, refinement] ms."""
+        inversion, rhs, first solve, refinement] ms."""
         a = (ctypes.c_float * 12)()
         self._check(self.lib.nq_stage_times(self.h, a))
         return list(a)
