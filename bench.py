@@ -213,6 +213,10 @@ def run_gb300(args):
         "tuning": eng.tuning(),
         "roofline": roof,
     }
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_batch:
+        line["many_problems"] = batched_vs_sequential()
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_learned:
+        line["learned_proposal"] = learned_vs_local()
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(max_seconds=args.cpu_seconds)
     return line
@@ -220,6 +224,150 @@ def run_gb300(args):
 
 def eng_graph_kernels(eng):
     return 0
+
+
+# --------------------------------------------------------------------------
+# Learned proposal vs local Metropolis on the 6x6 transverse-field Ising model
+# --------------------------------------------------------------------------
+LEARNED = dict(L=6, h=3.04, J=1.0, alpha=4, chains=8192, chain_length=20, burn=50, eps=0.01, lr=0.02,
+               sr_steps=100, train_every=10, train_steps=50, train_batch=4096, train_lr=1e-3, p_ar=0.5,
+               ess_length=64, ess_burn=20, seed=0x4E51)
+
+
+def _tfim2d(nq, Lx, h, J):
+    N = Lx * Lx
+    hilb = nq.HomogeneousSpin(N)
+    H = nq.LocalOperator(hilb)
+    for x in range(Lx):
+        for y in range(Lx):
+            i = x + Lx * y + 1
+            H = H - h * nq.sigmax(hilb, i)
+            H = H + J * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, (x + 1) % Lx + Lx * y + 1)
+            H = H + J * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, x + Lx * ((y + 1) % Lx) + 1)
+    return hilb, H
+
+
+BATCH = dict(n_problems=64, sizes=(3, 4, 5), h_range=(2.0, 4.0), J=1.0, alpha=1, chains=1024, chain_length=20,
+             burn=50, eps=0.01, lr=0.01, seed=1, steps=10)
+
+
+def batched_vs_sequential():
+    """64 independent 2D TFIM ground-state problems (L in {3,4,5}, h in
+    U[2,4] from seed 1, J = 1, complex RBM alpha = 1, 1024 chains x 20
+    samples): one batched SR step (one sampler, one estimator and one
+    inversion launch for all problems, per-problem stages as parallel graph
+    branches) against the same 64 problems stepped one after the other, each
+    replaying its own single-problem graph."""
+    import nqcuda as nq
+    c = BATCH
+    rng = np.random.default_rng(c["seed"])
+    spec = [(int(rng.choice(c["sizes"])), float(rng.uniform(*c["h_range"]))) for _ in range(c["n_problems"])]
+    probs = []
+    for k, (L, h) in enumerate(spec):
+        hilb, H = _tfim2d(nq, L, h, c["J"])
+        net = nq.RBM(np.complex64, L * L, c["alpha"], nq.af_logcosh)
+        nq.init_random_pars_(net, sigma=0.01, rng=np.random.default_rng(100 + k))
+        probs.append((net, hilb, H))
+    batch = nq.ProblemBatch(probs, c["chains"], c["chain_length"], c["burn"])
+    for i in range(3):
+        batch.vmc_step(i, c["eps"], c["lr"])
+    l0 = batch.kernel_launches()
+    ms_b = batch.bench_steps(10, c["steps"], c["eps"], c["lr"])
+    launches_b = (batch.kernel_launches() - l0) / c["steps"]
+    tuning = batch.tuning()
+    del batch
+    engines = []
+    for k, (net, hilb, H) in enumerate(probs):
+        smp = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], hilb.n_sites, burn=c["burn"],
+                                   seed=0x4E51 + 7919 * k)
+        engines.append(nq.BatchedSampler(net, smp, H, nq.SR(eps=c["eps"]), batch_sz=c["chains"],
+                                         s_precision=nq._lib.NQ_S_TF32).engine)
+    for e in engines:
+        for i in range(3):
+            e.vmc_step(i, c["eps"], c["lr"])
+    dev_ms = sum(float(np.mean(e.bench_steps(10, 3, c["eps"], c["lr"], 0))) for e in engines)
+    t0 = time.perf_counter()
+    for it in range(c["steps"]):
+        for e in engines:
+            e.vmc_step(100 + it, c["eps"], c["lr"])
+    wall_seq = (time.perf_counter() - t0) / c["steps"] * 1e3
+    ms_bat = float(np.mean(ms_b))
+    return {"workload": "64 x tfim2d L in {3,4,5}, h~U[2,4], rbm alpha=1, 1024 chains x 20",
+            "sizes": [L for L, _ in spec], "batched_ms_per_step": ms_bat,
+            "batched_problem_steps_per_s": c["n_problems"] * 1e3 / ms_bat,
+            "batched_kernels_per_step": launches_b, "tuning": tuning,
+            "sequential_device_ms_per_step": dev_ms,
+            "sequential_wall_ms_per_step": wall_seq,
+            "sequential_problem_steps_per_s": c["n_problems"] * 1e3 / wall_seq,
+            "speedup_vs_sequential_wall": wall_seq / ms_bat,
+            "speedup_vs_sequential_device": dev_ms / ms_bat}
+
+
+def learned_vs_local():
+    """SR on the 6x6 TFIM (h = 3.04) with the MADE proposal trained online on
+    the chains' samples every 10 SR steps, then effective samples/s of local
+    Metropolis and of the 50/50 mixture at several sweep lengths (passes).
+    ESS = samples / tau_int with tau_int = 1 + 2 Σ ρ (Sokal window) of E_loc
+    and of |Σσz| per chain; the sampling time is the sampler stage's device
+    time.  Energies of both samplers are reported with their difference."""
+    import nqcuda as nq
+    from nqcuda.stats import integrated_autocorr_time
+    c = LEARNED
+    N = c["L"] * c["L"]
+    hilb, H = _tfim2d(nq, c["L"], c["h"], c["J"])
+    net = nq.RBM(np.complex64, N, c["alpha"], nq.af_logcosh)
+    nq.init_random_pars_(net, sigma=0.01, rng=np.random.default_rng(c["seed"]))
+    smp = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], N, burn=c["burn"], seed=c["seed"])
+    eng = nq.BatchedSampler(net, smp, H, nq.SR(eps=c["eps"]), batch_sz=c["chains"],
+                            s_precision=nq._lib.NQ_S_TF32).engine
+    eng.proposal_init(128, 0.0, c["seed"])
+    t0 = time.perf_counter()
+    nll = []
+    for it in range(c["sr_steps"]):
+        m = eng.vmc_step(it, c["eps"], c["lr"])
+        if it % c["train_every"] == c["train_every"] - 1:
+            nll.append(eng.proposal_train(c["train_steps"], c["train_batch"], c["train_lr"]))
+    wall = time.perf_counter() - t0
+    params = eng.get_params()
+    made = eng.proposal_get_params()
+    sr_ms = float(np.mean(eng.bench_steps(1000, 5, c["eps"], 0.0, L2_FLUSH_BYTES)))
+    del eng
+
+    def measure(p_ar, passes):
+        s2 = nq.MetropolisSampler(nq.LocalRule(), c["ess_length"], passes, burn=c["ess_burn"], seed=c["seed"] + 1)
+        e = nq.BatchedSampler(net, s2, H, nq.SR(eps=c["eps"]), batch_sz=c["chains"],
+                              s_precision=nq._lib.NQ_S_TF32).engine
+        e.set_params(params)
+        if p_ar > 0:
+            e.proposal_init(128, 0.0, c["seed"])
+            e.proposal_set_params(made)
+            e.proposal_set_mix(p_ar)
+        e.sample(5000, want_samples=False)          # warm-up (autotuner, first launch)
+        smp_, _ = e.sample(5001)
+        ms = float(e.stage_times()[0])
+        mm, loc, _ = e.estimate(want_loc=True)
+        mz = np.abs(smp_.sum(axis=2)).astype(np.float64)
+        tE = integrated_autocorr_time(loc.T)
+        tM = integrated_autocorr_time(mz.T)
+        r = {"passes": e.passes, "sample_ms": ms, "tau_E": tE, "tau_absM": tM,
+             "ess_per_s_E": loc.size / tE / (ms * 1e-3), "ess_per_s_absM": loc.size / tM / (ms * 1e-3),
+             "energy_per_site": mm.mean_re / N, "energy_err_per_site": mm.error / N}
+        if p_ar > 0:
+            a, b = e.proposal_stats()
+            r["ar_acceptance"] = b / max(a, 1)
+        del e
+        return r
+
+    local = [measure(0.0, p) for p in (1, 3, 9, N)]
+    mixed = [measure(c["p_ar"], p) for p in (1, 3)]
+    bl = max(local, key=lambda r: r["ess_per_s_E"])
+    bm = max(mixed, key=lambda r: r["ess_per_s_E"])
+    return {"workload": "tfim2d_6x6_h3.04_rbm_alpha4_8192_chains", "sr_ms_per_step": sr_ms,
+            "sr_steps_per_s": 1e3 / sr_ms, "training_wall_s": wall, "energy_per_site_after_sr": m.mean_re / N,
+            "made_nll_after_each_training": nll, "local": local, "learned_mixture": mixed,
+            "best_local_ess_per_s_E": bl["ess_per_s_E"], "best_learned_ess_per_s_E": bm["ess_per_s_E"],
+            "learned_over_local_ess_ratio": bm["ess_per_s_E"] / bl["ess_per_s_E"],
+            "abs_dE_per_site_learned_vs_local": abs(bm["energy_per_site"] - bl["energy_per_site"])}
 
 
 # --------------------------------------------------------------------------
@@ -257,6 +405,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 64-problem batched vs sequential comparison")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-proposal vs local Metropolis comparison (6x6 TFIM)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -74,7 +74,8 @@ typedef enum { NQ_DTYPE_C64 = 0, NQ_DTYPE_C128 = 1, NQ_DTYPE_F32 = 2, NQ_DTYPE_F
 typedef enum {
   NQ_EVAL_F32 = 0,         /* FP32 CUDA cores */
   NQ_EVAL_TC_BF16X2 = 1,   /* θ = Wσ+b on tcgen05, W split in bf16 hi+lo, FP32 accumulate */
-  NQ_EVAL_F64 = 2          /* FP64 (small reference-precision runs) */
+  NQ_EVAL_F64 = 2,         /* FP64 (small reference-precision runs) */
+  NQ_EVAL_TC_BF16X3 = 3    /* θ on tcgen05, W split in bf16 hi+mid+lo (FP32-like θ) */
 } nq_eval_precision;
 
 /* Precision of the S = O_c O_c† accumulation. */
@@ -193,6 +194,14 @@ nq_status nq_logpsi_grad(nq_handle* h, const int8_t* sigma, int64_t n, double* o
  * P complex128 (real parameters: P float64). */
 nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out,
                       double* force_out);
+
+/* ---- compute_observable(BatchedObsKetSampler, Ô)
+ * (src/IterativeInterface/Samplers/Obs/BatchedObsKetSampler.jl:42-60):
+ * O_loc(σ) = Σ_σ' O_σσ' ψ(σ')/ψ(σ) over the samples of the last nq_sample /
+ * nq_vmc_step (same estimator kernel as E_loc, another operator table) and
+ * their Measurement.  loc_out (nullable): Ns complex128, [L][B].  RBM only;
+ * the handle's own operator, S and F are left untouched. */
+nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* stats, double* loc_out);
 /* S (nullable out): P x P column-major complex128 (real parameters: float64). */
 nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
 
@@ -229,6 +238,33 @@ nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double e
 nq_status nq_tuning(nq_handle* h, int32_t* out, int32_t n);
 /* Number of kernel launches issued by this handle since creation. */
 int64_t nq_kernel_launches(const nq_handle* h);
+
+/* ---- many independent problems per step (no counterpart in the reference) --
+ * The reference runs one problem per BatchedSampler (build_Batched.jl:1-14);
+ * parallel problems are separate processes or threads
+ * (src/Parallel/Threads/threads_wrappers.jl:14-31).  A batch owns n problem
+ * handles (RBM, FP32 evaluation, one activation and Hilbert kind; sizes may
+ * differ) and runs one SR step of all of them as one CUDA graph: the
+ * Metropolis sampler, the estimator and the inversion of the shifted S of
+ * every problem are one launch each; the force, S, refinement and update of
+ * each problem are parallel branches of the graph.  The lanes per chain of the
+ * batched sampler are autotuned on the batch's own schedule.  Parameters and
+ * operators are set on the problem handles (nq_batch_handle), which stay
+ * usable with every single-problem call. */
+typedef struct nq_batch nq_batch;
+nq_status nq_batch_create(const nq_config* cfgs, int32_t n, nq_batch** out);
+void nq_batch_destroy(nq_batch* b);
+nq_status nq_batch_last_error(const nq_batch* b, char* buf, size_t len);
+int32_t nq_batch_size(const nq_batch* b);
+nq_handle* nq_batch_handle(nq_batch* b, int32_t i);
+/* one SR step (sr_shift eps, Descent lr) of every problem; stats (nullable) [n] */
+nq_status nq_batch_vmc_step(nq_batch* b, uint64_t call_index, double eps, double lr, nq_measurement* stats);
+/* n_steps graph replays timed with CUDA events, call indices call0+1, ... */
+nq_status nq_batch_bench_steps(nq_batch* b, uint64_t call0, int32_t n_steps, double eps, double lr,
+                               float* ms_out);
+/* [lanes per chain, estimator threads per block, inversion CTAs, kernels per step] */
+nq_status nq_batch_tuning(nq_batch* b, int32_t* out, int32_t n);
+int64_t nq_batch_kernel_launches(const nq_batch* b);
 
 /* ---- learned autoregressive proposal (no counterpart in the reference) ------
  * The reference samples with local rules only (src/Samplers/MCMCRules/

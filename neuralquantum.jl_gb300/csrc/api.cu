@@ -47,6 +47,7 @@ nq_status refresh_params(nq_handle* h) {
     RbmDev<float> d = rbm_dev<float>(h);
     CKL(launch_rbm_tables<float>(d, (cpx<float>*)h->d_tab[0], (cpx<float>*)h->d_tab[1],
                                  (cpx<float>*)h->d_tab[2], h->st));
+    if (h->tc_theta) CKL(launch_theta_pack(d.W, h->M, h->N, h->theta_terms, h->d_theta_img, h->st));
   }
   return NQ_OK;
 }
@@ -75,14 +76,15 @@ nq_status ensure_tuned(nq_handle* h) {
   uint64_t* scratch = nullptr;
   CK(cudaMalloc(&scratch, sizeof(uint64_t) * (size_t)h->B * 2));
   SamplerRun run;
-  run.B = h->B; run.L = 1; run.burn = std::min(6, h->cfg.burn + h->L); run.passes = h->passes;
+  run.B = h->B; run.L = 1; run.burn = std::min(24, h->cfg.burn + h->L); run.passes = h->passes;
   run.n_record = 1; run.k0 = 0x1234u; run.k1 = 0x5678u; run.call = 0xFFFFFFFFu;
   run.samples = scratch; run.accepted = h->d_accepted;
   int best = cand[0];
   float best_ms = 1e30f;
   for (int c = 0; c < nc; ++c) {
-    float ms = 0.f;
-    for (int rep = 0; rep < 2; ++rep) {      // first launch warms up
+    float best_c = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {      // first launch warms up; fastest of the other three
+      float ms = 0.f;
       CK(cudaEventRecord(h->kev[0], h->st));
       cudaError_t e = h->f64 ? launch_rbm_sampler<double>(rbm_dev<double>(h), run, cand[c], h->st)
                              : launch_rbm_sampler<float>(rbm_dev<float>(h), run, cand[c], h->st);
@@ -91,8 +93,9 @@ nq_status ensure_tuned(nq_handle* h) {
       CK(cudaEventRecord(h->kev[1], h->st));
       CK(cudaEventSynchronize(h->kev[1]));
       CK(cudaEventElapsedTime(&ms, h->kev[0], h->kev[1]));
+      if (rep > 0) best_c = std::min(best_c, ms);
     }
-    if (ms < best_ms) { best_ms = ms; best = cand[c]; }
+    if (best_c < best_ms) { best_ms = best_c; best = cand[c]; }
   }
   cudaFree(scratch);
   h->sampler_lanes = best;
@@ -147,6 +150,12 @@ nq_status stage_eval(nq_handle* h) {
   if (h->f64) {
     CKL(launch_rbm_eval<double>(rbm_dev<double>(h), h->d_samples, h->Ns, op, (cpx<double>*)h->d_logpsi,
                                 (cpx<double>*)h->d_g, (cpx<double>*)h->d_eloc, h->st));
+  } else if (h->tc_theta) {
+    const RbmDev<float> d = rbm_dev<float>(h);
+    CKL(launch_theta_bf16x2(h->d_theta_img, h->theta_terms, h->M, h->N, d.b, h->d_samples, h->Ns, h->hilb, (cpx<float>*)h->d_g,
+                            h->sb.status, h->st));
+    CKL(launch_rbm_eval<float>(d, h->d_samples, h->Ns, op, (cpx<float>*)h->d_logpsi, (cpx<float>*)h->d_g,
+                               (cpx<float>*)h->d_eloc, h->st, 1));
   } else {
     CKL(launch_rbm_eval<float>(rbm_dev<float>(h), h->d_samples, h->Ns, op, (cpx<float>*)h->d_logpsi,
                                (cpx<float>*)h->d_g, (cpx<float>*)h->d_eloc, h->st));
@@ -273,13 +282,61 @@ void free_op(nq_handle* h) {
 }
 
 template <typename T>
-nq_status upload(nq_handle* h, const T* src, size_t count, const T** dst) {
+nq_status upload(nq_handle* h, const T* src, size_t count, const T** dst, std::vector<void*>* allocs = nullptr) {
   if (count == 0) count = 1;
   T* d = nullptr;
   CK(cudaMalloc((void**)&d, count * sizeof(T)));
-  h->op_allocs.push_back(d);
+  (allocs ? allocs : &h->op_allocs)->push_back(d);
   if (src) CK(cudaMemcpy(d, src, count * sizeof(T), cudaMemcpyHostToDevice));
   *dst = d;
+  return NQ_OK;
+}
+
+// host-side validation of a flattened operator against the handle's sites
+nq_status validate_op(nq_handle* h, const nq_op_table* t) {
+  if (t->n_ops < 1 || t->n_rows < 1 || t->n_conns < 0) return fail(h, NQ_ERR_ARG, "empty operator");
+  for (int o = 0; o < t->n_ops; ++o) {
+    int k = t->op_n_sites[o];
+    if (k < 1 || k > 8) return fail(h, NQ_ERR_ARG, "operator %d: %d sites (1..8 supported)", o, k);
+    for (int d = 0; d < k; ++d)
+      if (t->op_sites[8 * o + d] < 0 || t->op_sites[8 * o + d] >= h->nst)
+        return fail(h, NQ_ERR_ARG, "operator %d: site out of range", o);
+    if (t->op_row_offset[o] < 0 || t->op_row_offset[o] + (1 << k) > t->n_rows)
+      return fail(h, NQ_ERR_ARG, "operator %d: row offset out of range", o);
+  }
+  for (int r = 0; r < t->n_rows; ++r)
+    if (t->row_conn_offset[r] > t->row_conn_offset[r + 1] || t->row_conn_offset[r] < 0)
+      return fail(h, NQ_ERR_ARG, "row offsets not monotone");
+  if (t->row_conn_offset[t->n_rows] != t->n_conns) return fail(h, NQ_ERR_ARG, "row offsets do not end at n_conns");
+  for (int c = 0; c < t->n_conns; ++c) {
+    int nc = t->conn_n_changes[c];
+    if (nc < 0 || nc > 8) return fail(h, NQ_ERR_ARG, "connection %d: bad change count", c);
+    for (int q = 0; q < nc; ++q) {
+      int s = t->conn_change_site[8 * c + q];
+      int v = t->conn_change_value[8 * c + q];
+      if (s < 0 || s >= h->nst) return fail(h, NQ_ERR_ARG, "connection %d: site out of range", c);
+      bool ok = h->hilb == NQ_HILB_SPIN ? (v == 1 || v == -1) : (v == 0 || v == 1);
+      if (!ok) return fail(h, NQ_ERR_ARG, "connection %d: invalid site value %d", c, v);
+    }
+  }
+  return NQ_OK;
+}
+
+nq_status upload_op(nq_handle* h, const nq_op_table* t, DevOp* out, std::vector<void*>* allocs) {
+  DevOp d;
+  d.n_ops = t->n_ops; d.n_rows = t->n_rows; d.n_conns = t->n_conns;
+  nq_status s;
+  if ((s = upload(h, t->op_n_sites, t->n_ops, &d.op_n_sites, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, t->op_sites, 8 * (size_t)t->n_ops, &d.op_sites, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, t->op_row_offset, t->n_ops, &d.op_row_offset, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, t->row_conn_offset, (size_t)t->n_rows + 1, &d.row_conn_offset, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, t->conn_mel, 2 * (size_t)t->n_conns, &d.conn_mel, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, t->conn_n_changes, (size_t)t->n_conns, &d.conn_n_changes, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, t->conn_change_site, 8 * (size_t)t->n_conns, &d.conn_change_site, allocs)) != NQ_OK) return s;
+  if ((s = upload(h, (const signed char*)t->conn_change_value, 8 * (size_t)t->n_conns, &d.conn_change_value,
+                  allocs)) != NQ_OK)
+    return s;
+  *out = d;
   return NQ_OK;
 }
 
@@ -308,7 +365,10 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
   if (c.n_hidden < 1 || c.n_hidden > 256) return bad("n_hidden must be in 1..256");
   if (c.n_chains < 2 || c.chain_length < 1 || c.burn < 0 || c.passes < 1) return bad("bad sampler sizes");
-  if (c.eval_precision != NQ_EVAL_F32 && c.eval_precision != NQ_EVAL_F64) {
+  if (c.eval_precision != NQ_EVAL_F32 && c.eval_precision != NQ_EVAL_F64 &&
+      !((c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3) &&
+        c.network == NQ_NET_RBM &&
+        theta_tc_supported(c.n_sites, c.n_hidden) && gram_tc_supported())) {
     delete h;
     return NQ_ERR_UNSUPPORTED;
   }
@@ -346,6 +406,8 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->hilb = c.hilbert;
   h->act = c.activation;
   h->f64 = c.eval_precision == NQ_EVAL_F64;
+  h->tc_theta = c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3;
+  h->theta_terms = c.eval_precision == NQ_EVAL_TC_BF16X3 ? 3 : 2;
   h->complex_params = !h->ndm;
   const int sampler_M = h->ndm ? h->Ms : h->M, sampler_N = h->ndm ? h->N2 : h->N;
   if (c.sampler_lanes != 0) {
@@ -425,6 +487,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(cudaMalloc(&h->sb.ctl, sweep_ctl_bytes()), "sweep ctl");
   step(dalloc(&h->sb.work, sweep_work_elems(P)), "sweep work");
   step(dalloc(&h->sb.yf, (size_t)P), "yf");
+  if (h->tc_theta) step(dalloc(&h->d_theta_img, theta_tc_image_elems(h->M, h->theta_terms)), "theta image");
   h->sb.S = h->d_S;
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
@@ -460,7 +523,7 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_dw, h->d_eff[0], h->d_eff[1],
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -533,46 +596,11 @@ nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
 
 nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
   if (!h || !t) return NQ_ERR_ARG;
-  if (t->n_ops < 1 || t->n_rows < 1 || t->n_conns < 0) return fail(h, NQ_ERR_ARG, "empty operator");
-  // validate on the host
-  for (int o = 0; o < t->n_ops; ++o) {
-    int k = t->op_n_sites[o];
-    if (k < 1 || k > 8) return fail(h, NQ_ERR_ARG, "operator %d: %d sites (1..8 supported)", o, k);
-    for (int d = 0; d < k; ++d)
-      if (t->op_sites[8 * o + d] < 0 || t->op_sites[8 * o + d] >= h->nst)
-        return fail(h, NQ_ERR_ARG, "operator %d: site out of range", o);
-    if (t->op_row_offset[o] < 0 || t->op_row_offset[o] + (1 << k) > t->n_rows)
-      return fail(h, NQ_ERR_ARG, "operator %d: row offset out of range", o);
-  }
-  for (int r = 0; r < t->n_rows; ++r)
-    if (t->row_conn_offset[r] > t->row_conn_offset[r + 1] || t->row_conn_offset[r] < 0)
-      return fail(h, NQ_ERR_ARG, "row offsets not monotone");
-  if (t->row_conn_offset[t->n_rows] != t->n_conns) return fail(h, NQ_ERR_ARG, "row offsets do not end at n_conns");
-  for (int c = 0; c < t->n_conns; ++c) {
-    int nc = t->conn_n_changes[c];
-    if (nc < 0 || nc > 8) return fail(h, NQ_ERR_ARG, "connection %d: bad change count", c);
-    for (int q = 0; q < nc; ++q) {
-      int s = t->conn_change_site[8 * c + q];
-      int v = t->conn_change_value[8 * c + q];
-      if (s < 0 || s >= h->nst) return fail(h, NQ_ERR_ARG, "connection %d: site out of range", c);
-      bool ok = h->hilb == NQ_HILB_SPIN ? (v == 1 || v == -1) : (v == 0 || v == 1);
-      if (!ok) return fail(h, NQ_ERR_ARG, "connection %d: invalid site value %d", c, v);
-    }
-  }
+  if (nq_status v = validate_op(h, t)) return v;
   CK(cudaStreamSynchronize(h->st));
   free_op(h);
   DevOp d;
-  d.n_ops = t->n_ops; d.n_rows = t->n_rows; d.n_conns = t->n_conns;
-  nq_status s;
-  if ((s = upload(h, t->op_n_sites, t->n_ops, &d.op_n_sites)) != NQ_OK) return s;
-  if ((s = upload(h, t->op_sites, 8 * (size_t)t->n_ops, &d.op_sites)) != NQ_OK) return s;
-  if ((s = upload(h, t->op_row_offset, t->n_ops, &d.op_row_offset)) != NQ_OK) return s;
-  if ((s = upload(h, t->row_conn_offset, (size_t)t->n_rows + 1, &d.row_conn_offset)) != NQ_OK) return s;
-  if ((s = upload(h, t->conn_mel, 2 * (size_t)t->n_conns, &d.conn_mel)) != NQ_OK) return s;
-  if ((s = upload(h, t->conn_n_changes, (size_t)t->n_conns, &d.conn_n_changes)) != NQ_OK) return s;
-  if ((s = upload(h, t->conn_change_site, 8 * (size_t)t->n_conns, &d.conn_change_site)) != NQ_OK) return s;
-  if ((s = upload(h, (const signed char*)t->conn_change_value, 8 * (size_t)t->n_conns, &d.conn_change_value)) != NQ_OK)
-    return s;
+  if (nq_status s = upload_op(h, t, &d, nullptr)) return s;
   h->op = d;
   h->has_op = true;
   if (h->ndm) {
@@ -601,6 +629,61 @@ nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
   }
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
   return NQ_OK;
+}
+
+nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* stats, double* loc_out) {
+  if (!h || !obs || !stats) return NQ_ERR_ARG;
+  if (h->ndm) return fail(h, NQ_ERR_UNSUPPORTED, "observables of density matrices are not provided");
+  if (nq_status v = validate_op(h, obs)) return v;
+  std::vector<void*> allocs;
+  DevOp d;
+  void* d_lp = nullptr;
+  void* d_loc = nullptr;
+  double* d_cs = nullptr;
+  double* d_st = nullptr;
+  const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
+  auto cleanup = [&](nq_status s) {
+    cudaStreamSynchronize(h->st);
+    for (void* p : allocs) cudaFree(p);
+    cudaFree(d_lp); cudaFree(d_loc); cudaFree(d_cs); cudaFree(d_st);
+    return s;
+  };
+  nq_status s = upload_op(h, obs, &d, &allocs);
+  if (s != NQ_OK) return cleanup(s);
+  if (cudaMalloc(&d_lp, (size_t)h->Ns * csz) != cudaSuccess || cudaMalloc(&d_loc, (size_t)h->Ns * csz) != cudaSuccess ||
+      cudaMalloc((void**)&d_cs, (size_t)h->B * 3 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&d_st, 8 * sizeof(double)) != cudaSuccess)
+    return cleanup(fail(h, NQ_ERR_CUDA, "observable buffers"));
+  cudaError_t e;
+  ++h->launches;
+  if (h->f64) {
+    e = launch_rbm_eval<double>(rbm_dev<double>(h), h->d_samples, h->Ns, &d, (cpx<double>*)d_lp, nullptr,
+                                (cpx<double>*)d_loc, h->st);
+    if (e == cudaSuccess) e = launch_stats<double>((cpx<double>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
+  } else {
+    e = launch_rbm_eval<float>(rbm_dev<float>(h), h->d_samples, h->Ns, &d, (cpx<float>*)d_lp, nullptr,
+                               (cpx<float>*)d_loc, h->st);
+    if (e == cudaSuccess) e = launch_stats<float>((cpx<float>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
+  }
+  h->launches += 2;
+  if (e != cudaSuccess) return cleanup(fail(h, NQ_ERR_CUDA, "observable: %s", cudaGetErrorString(e)));
+  double v[6];
+  if (cudaMemcpyAsync(v, d_st, 6 * sizeof(double), cudaMemcpyDeviceToHost, h->st) != cudaSuccess ||
+      cudaStreamSynchronize(h->st) != cudaSuccess)
+    return cleanup(fail(h, NQ_ERR_CUDA, "observable copy"));
+  stats->mean_re = v[0]; stats->mean_im = v[1]; stats->error = v[2]; stats->variance = v[3];
+  stats->tau = v[4]; stats->R = v[5]; stats->acceptance = 0.0;
+  if (loc_out) {
+    std::vector<char> buf((size_t)h->Ns * csz);
+    if (cudaMemcpy(buf.data(), d_loc, buf.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return cleanup(fail(h, NQ_ERR_CUDA, "observable copy"));
+    if (h->f64) memcpy(loc_out, buf.data(), buf.size());
+    else {
+      const float* f = (const float*)buf.data();
+      for (size_t i = 0; i < 2 * (size_t)h->Ns; ++i) loc_out[i] = f[i];
+    }
+  }
+  return cleanup(NQ_OK);
 }
 
 nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out, uint8_t* accept_bits) {
@@ -670,7 +753,12 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
     if (h->f64) CKL(launch_ndm_eval<double>(ndm_eff<double>(h), h->act, d_bits, (int)n, h->hilb, (cpx<double>*)d_lp, nullptr, 0, d_out, h->st));
     else CKL(launch_ndm_eval<float>(ndm_eff<float>(h), h->act, d_bits, (int)n, h->hilb, (cpx<float>*)d_lp, nullptr, 0, d_out, h->st));
   } else if (h->f64) CKL(launch_rbm_eval<double>(rbm_dev<double>(h), d_bits, (int)n, nullptr, (cpx<double>*)d_lp, (cpx<double>*)d_g, nullptr, h->st));
-  else CKL(launch_rbm_eval<float>(rbm_dev<float>(h), d_bits, (int)n, nullptr, (cpx<float>*)d_lp, (cpx<float>*)d_g, nullptr, h->st));
+  else if (h->tc_theta) {
+    const RbmDev<float> d = rbm_dev<float>(h);
+    CKL(launch_theta_bf16x2(h->d_theta_img, h->theta_terms, h->M, h->N, d.b, d_bits, (int)n, h->hilb, (cpx<float>*)d_g,
+                            h->sb.status, h->st));
+    CKL(launch_rbm_eval<float>(d, d_bits, (int)n, nullptr, (cpx<float>*)d_lp, (cpx<float>*)d_g, nullptr, h->st, 1));
+  } else CKL(launch_rbm_eval<float>(rbm_dev<float>(h), d_bits, (int)n, nullptr, (cpx<float>*)d_lp, (cpx<float>*)d_g, nullptr, h->st));
   std::vector<double> lp(2 * n);
   if (h->f64) CK(cudaMemcpyAsync(lp.data(), d_lp, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   else {
@@ -878,5 +966,431 @@ nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double e
   delete[] evs;
   return check_status_word(h);
 }
+
+}  // extern "C"
+
+// ===========================================================================
+// Many independent problems per step (nq_batch_*): the sampler, the
+// estimator and the SR inversion of all problems run as one launch each; the
+// per-problem force/S/solve-refinement/update stages run as parallel branches
+// of the same CUDA graph.
+// ===========================================================================
+struct nq_batch {
+  std::vector<nq_handle*> hs;
+  std::string err;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t graph = nullptr;
+  double geps = -1, glr = -1;
+  int64_t graph_kernels = 0;
+  uint32_t* h_call = nullptr;           // pinned
+  uint32_t* d_call = nullptr;
+  SamplerJob<float>* d_sjobs = nullptr;
+  EvalJob<float>* d_ejobs = nullptr;
+  SweepJob* d_wjobs = nullptr;
+  int* d_sblk = nullptr;                // [np+1] sampler block starts
+  int* d_eblk = nullptr;                // [np+1] estimator block starts
+  int* d_wcta = nullptr;                // [np+1] inversion CTA starts
+  int s_blocks = 0, e_blocks = 0, w_ctas = 0, M_max = 0, N_max = 0, act = 0;
+  int lanes = 0, eval_T = 0;
+  void* d_ctl = nullptr;                // per-problem barrier blocks, 64 B each
+  unsigned long long* d_acc = nullptr;  // [np] accepted-move counters
+  double** d_stat_src = nullptr;        // [np] -> each problem's d_stats
+  int** d_status_src = nullptr;         // [np] -> each problem's status word
+  double* d_gather = nullptr;           // [np][8]
+  double* h_gather = nullptr;           // pinned [np][8]
+  int64_t launches = 0;
+};
+
+namespace {
+
+nq_status bfail(nq_batch* b, nq_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return code;
+}
+
+#define BCK(expr)                                                                          \
+  do {                                                                                     \
+    cudaError_t _e = (expr);                                                               \
+    if (_e != cudaSuccess)                                                                 \
+      return bfail(b, NQ_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                   __FILE__, __LINE__);                                                    \
+  } while (0)
+
+__global__ void batch_gather_kernel(int np, double* const* __restrict__ stats, int* const* __restrict__ status,
+                                    const unsigned long long* __restrict__ acc, double* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  for (int k = 0; k < 6; ++k) out[8 * p + k] = stats[p][k];
+  out[8 * p + 6] = (double)acc[p];
+  out[8 * p + 7] = (double)*status[p];
+}
+
+// problem p gets CTAs in proportion to its inversion work (nblk^3), at least
+// one and at most its number of column blocks
+void split_ctas(const std::vector<int>& P, int total, std::vector<int>& start) {
+  const int np = (int)P.size();
+  std::vector<double> w(np);
+  double sum = 0;
+  for (int p = 0; p < np; ++p) {
+    const double nb = (P[p] + 31) / 32;
+    w[p] = nb * nb * nb;
+    sum += w[p];
+  }
+  const int spare = std::max(0, total - np);
+  start.assign(np + 1, 0);
+  for (int p = 0; p < np; ++p) {
+    const int nb = (P[p] + 31) / 32;
+    int extra = (int)std::floor(spare * w[p] / sum);
+    extra = std::min(extra, std::max(0, nb - 1));
+    start[p + 1] = start[p] + 1 + extra;
+  }
+}
+
+nq_status batch_build_tables(nq_batch* b) {
+  const int np = (int)b->hs.size();
+  std::vector<SamplerJob<float>> sj(np);
+  std::vector<EvalJob<float>> ej(np);
+  std::vector<SweepJob> wj(np);
+  std::vector<int> sblk(np + 1, 0), eblk(np + 1, 0), Ps(np);
+  std::vector<double*> sp(np);
+  std::vector<int*> stp(np);
+  b->M_max = 0;
+  b->N_max = 0;
+  for (nq_handle* h : b->hs) {
+    b->M_max = std::max(b->M_max, h->M);
+    b->N_max = std::max(b->N_max, h->N);
+  }
+  b->eval_T = rbm_eval_threads(b->M_max);
+  const int cpb = 256 / b->lanes;          // chains per sampler block
+  for (int p = 0; p < np; ++p) {
+    nq_handle* h = b->hs[p];
+    SamplerRun run;
+    run.B = h->B; run.L = h->L; run.burn = h->cfg.burn; run.passes = h->passes;
+    run.n_record = h->n_record; run.write_last_at_end = h->write_last;
+    run.k0 = (uint32_t)(h->cfg.seed & 0xffffffffu);
+    run.k1 = (uint32_t)(h->cfg.seed >> 32);
+    run.call_ptr = b->d_call;
+    run.samples = h->d_samples;
+    run.accepted = b->d_acc + p;
+    sj[p].net = rbm_dev<float>(h);
+    sj[p].run = run;
+    sblk[p + 1] = sblk[p] + (h->B + cpb - 1) / cpb;
+    ej[p].net = rbm_dev<float>(h);
+    ej[p].samples = h->d_samples;
+    ej[p].Ns = h->Ns;
+    ej[p].op = h->op;
+    ej[p].has_op = 1;
+    ej[p].logpsi = (cpx<float>*)h->d_logpsi;
+    ej[p].g = (cpx<float>*)h->d_g;
+    ej[p].eloc = (cpx<float>*)h->d_eloc;
+    eblk[p + 1] = eblk[p] + (h->Ns + b->eval_T - 1) / b->eval_T;
+    wj[p].W = h->sb.W;
+    wj[p].P = h->P;
+    wj[p].ctl = (char*)b->d_ctl + (size_t)p * 64;
+    wj[p].status = h->sb.status;
+    wj[p].work = h->sb.work;
+    Ps[p] = h->P;
+    sp[p] = h->d_stats;
+    stp[p] = h->sb.status;
+  }
+  int sms = 0, dev = 0;
+  BCK(cudaGetDevice(&dev));
+  BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  std::vector<int> wcta;
+  split_ctas(Ps, sms, wcta);
+  if (wcta[np] > sms)
+    return bfail(b, NQ_ERR_UNSUPPORTED, "%d problems exceed the %d SMs of the inversion launch", np, sms);
+  b->s_blocks = sblk[np];
+  b->e_blocks = eblk[np];
+  b->w_ctas = wcta[np];
+  BCK(cudaMemcpy(b->d_sjobs, sj.data(), np * sizeof(SamplerJob<float>), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_ejobs, ej.data(), np * sizeof(EvalJob<float>), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_wjobs, wj.data(), np * sizeof(SweepJob), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_sblk, sblk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_eblk, eblk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_wcta, wcta.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_stat_src, sp.data(), np * sizeof(double*), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_status_src, stp.data(), np * sizeof(int*), cudaMemcpyHostToDevice));
+  return NQ_OK;
+}
+
+// lanes per chain of the many-problem sampler: every candidate runs the
+// batch's real schedule twice (the first launch warms up) and the fastest wins
+nq_status batch_tune(nq_batch* b) {
+  if (b->lanes) return NQ_OK;
+  int cand[4];
+  int M_max = 0;
+  for (nq_handle* h : b->hs) M_max = std::max(M_max, h->M);
+  const int nc = rbm_sampler_valid_lanes(M_max, cand, 4);
+  if (nc == 0) return bfail(b, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", M_max);
+  cudaEvent_t e0, e1;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  *b->h_call = 0xFFFFFFFFu;
+  BCK(cudaMemcpy(b->d_call, b->h_call, sizeof(uint32_t), cudaMemcpyHostToDevice));
+  int best = cand[0];
+  float best_ms = 1e30f;
+  for (int c = 0; c < nc; ++c) {
+    b->lanes = cand[c];
+    if (nq_status s = batch_build_tables(b)) return s;
+    float best_c = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {      // first launch warms up; fastest of the other three
+      float ms = 0.f;
+      BCK(cudaEventRecord(e0, b->st));
+      BCK(launch_rbm_sampler_batch<float>(b->d_sjobs, b->d_sblk, (int)b->hs.size(), b->s_blocks, b->M_max,
+                                          b->N_max, b->act, b->lanes, b->st));
+      ++b->launches;
+      BCK(cudaEventRecord(e1, b->st));
+      BCK(cudaEventSynchronize(e1));
+      BCK(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) best_c = std::min(best_c, ms);
+    }
+    if (best_c < best_ms) {
+      best_ms = best_c;
+      best = cand[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->lanes = best;
+  return batch_build_tables(b);
+}
+
+nq_status batch_capture(nq_batch* b, double eps, double lr) {
+  const int np = (int)b->hs.size();
+  cudaGraph_t g = nullptr;
+  BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  for (nq_handle* h : b->hs) h->capturing = true;
+  const int64_t before = b->launches;
+  int64_t hbefore = 0;
+  for (nq_handle* h : b->hs) hbefore += h->launches;
+  nq_status s = NQ_OK;
+  auto ck = [&](cudaError_t e, const char* what) {
+    if (s == NQ_OK && e != cudaSuccess) s = bfail(b, NQ_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  };
+  ck(cudaMemcpyAsync(b->d_call, b->h_call, sizeof(uint32_t), cudaMemcpyHostToDevice, b->st), "call copy");
+  ck(cudaMemsetAsync(b->d_acc, 0, np * sizeof(unsigned long long), b->st), "acc reset");
+  ck(launch_rbm_sampler_batch<float>(b->d_sjobs, b->d_sblk, np, b->s_blocks, b->M_max, b->N_max, b->act, b->lanes,
+                                     b->st), "batched sampler");
+  ck(launch_rbm_eval_batch<float>(b->d_ejobs, b->d_eblk, np, b->e_blocks, b->M_max, b->N_max, b->act, b->eval_T,
+                                  b->st), "batched estimator");
+  b->launches += 2;
+  // branches: force + statistics, S, shifted copy
+  ck(cudaEventRecord(b->fork, b->st), "fork");
+  for (int p = 0; p < np && s == NQ_OK; ++p) {
+    nq_handle* h = b->hs[p];
+    ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch");
+    if (s == NQ_OK) s = stage_force(h);
+    if (s == NQ_OK) s = stage_S(h);
+    if (s == NQ_OK) {
+      ck(launch_sr_shift(h->sb, h->P, 0, eps, 0.0, h->st), "shift");
+      ++h->launches;
+    }
+    ck(cudaEventRecord(b->join[p], h->st), "join");
+    ck(cudaStreamWaitEvent(b->st, b->join[p], 0), "join wait");
+  }
+  // one cooperative launch inverts every problem's shifted S
+  ck(launch_spd_inverse_batch(b->d_wjobs, b->d_wcta, np, b->w_ctas, b->d_ctl, (size_t)np * 64, b->st),
+     "batched inversion");
+  ++b->launches;
+  ck(cudaEventRecord(b->fork, b->st), "fork 2");
+  for (int p = 0; p < np && s == NQ_OK; ++p) {
+    nq_handle* h = b->hs[p];
+    ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch 2");
+    if (s == NQ_OK) {
+      ck(launch_sr_finish(h->sb, h->P, h->fb.force, 0, eps, 0.0, !h->complex_params, kSolveRefine, h->st),
+         "solve");
+      h->launches += 2 + 3 * (kSolveRefine + 1);
+    }
+    if (s == NQ_OK) s = stage_update(h, lr);
+    ck(cudaEventRecord(b->join[p], h->st), "join 2");
+    ck(cudaStreamWaitEvent(b->st, b->join[p], 0), "join wait 2");
+  }
+  if (s == NQ_OK) {
+    batch_gather_kernel<<<(np + 63) / 64, 64, 0, b->st>>>(np, b->d_stat_src, b->d_status_src, b->d_acc,
+                                                         b->d_gather);
+    ck(cudaGetLastError(), "gather");
+    ++b->launches;
+  }
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  int64_t hafter = 0;
+  for (nq_handle* h : b->hs) {
+    h->capturing = false;
+    hafter += h->launches;
+  }
+  b->graph_kernels = (b->launches - before) + (hafter - hbefore);
+  b->launches = before;
+  if (s != NQ_OK) {
+    if (g) cudaGraphDestroy(g);
+    return s;
+  }
+  BCK(e);
+  BCK(cudaGraphInstantiate(&b->graph, g, 0));
+  cudaGraphDestroy(g);
+  b->geps = eps;
+  b->glr = lr;
+  return NQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nq_status nq_batch_create(const nq_config* cfgs, int32_t n, nq_batch** out) {
+  if (!cfgs || !out || n < 1 || n > 1024) return NQ_ERR_ARG;
+  *out = nullptr;
+  for (int p = 0; p < n; ++p) {
+    const nq_config& c = cfgs[p];
+    if (c.network != NQ_NET_RBM || c.eval_precision != NQ_EVAL_F32) return NQ_ERR_UNSUPPORTED;
+    if (c.activation != cfgs[0].activation || c.hilbert != cfgs[0].hilbert) return NQ_ERR_UNSUPPORTED;
+  }
+  nq_batch* b = new nq_batch();
+  auto cleanup = [&](nq_status s) {
+    nq_batch_destroy(b);
+    return s;
+  };
+  b->act = cfgs[0].activation;
+  for (int p = 0; p < n; ++p) {
+    nq_handle* h = nullptr;
+    nq_status s = nq_create(&cfgs[p], &h);
+    if (s != NQ_OK) return cleanup(s);
+    b->hs.push_back(h);
+  }
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) return cleanup(NQ_ERR_CUDA);
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) return cleanup(NQ_ERR_CUDA);
+  b->join.assign(n, nullptr);
+  for (int p = 0; p < n; ++p)
+    if (cudaEventCreateWithFlags(&b->join[p], cudaEventDisableTiming) != cudaSuccess) return cleanup(NQ_ERR_CUDA);
+  const bool ok = cudaMallocHost((void**)&b->h_call, sizeof(uint32_t)) == cudaSuccess &&
+                  cudaMallocHost((void**)&b->h_gather, (size_t)n * 8 * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_call, sizeof(uint32_t)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_sjobs, n * sizeof(SamplerJob<float>)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_ejobs, n * sizeof(EvalJob<float>)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_wjobs, n * sizeof(SweepJob)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_sblk, (n + 1) * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_eblk, (n + 1) * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_wcta, (n + 1) * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&b->d_ctl, (size_t)n * 64) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_acc, n * sizeof(unsigned long long)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_stat_src, n * sizeof(double*)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_status_src, n * sizeof(int*)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_gather, (size_t)n * 8 * sizeof(double)) == cudaSuccess;
+  if (!ok) return cleanup(NQ_ERR_CUDA);
+  *out = b;
+  return NQ_OK;
+}
+
+void nq_batch_destroy(nq_batch* b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (nq_handle* h : b->hs) nq_destroy(h);
+  void* bufs[] = {b->d_call, b->d_sjobs, b->d_ejobs, b->d_wjobs, b->d_sblk, b->d_eblk, b->d_wcta, b->d_ctl,
+                  b->d_acc, b->d_stat_src, b->d_status_src, b->d_gather};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (b->h_call) cudaFreeHost(b->h_call);
+  if (b->h_gather) cudaFreeHost(b->h_gather);
+  for (cudaEvent_t e : b->join)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+nq_status nq_batch_last_error(const nq_batch* b, char* buf, size_t len) {
+  if (!b || !buf || len == 0) return NQ_ERR_ARG;
+  snprintf(buf, len, "%s", b->err.c_str());
+  return NQ_OK;
+}
+
+int32_t nq_batch_size(const nq_batch* b) { return b ? (int32_t)b->hs.size() : -1; }
+
+nq_handle* nq_batch_handle(nq_batch* b, int32_t i) {
+  if (!b || i < 0 || i >= (int32_t)b->hs.size()) return nullptr;
+  return b->hs[i];
+}
+
+nq_status nq_batch_vmc_step(nq_batch* b, uint64_t call_index, double eps, double lr, nq_measurement* stats) {
+  if (!b) return NQ_ERR_ARG;
+  const int np = (int)b->hs.size();
+  for (int p = 0; p < np; ++p)
+    if (!b->hs[p]->has_op) return bfail(b, NQ_ERR_STATE, "problem %d has no operator (nq_set_operator)", p);
+  if (b->graph && (b->geps != eps || b->glr != lr)) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  for (nq_handle* h : b->hs) BCK(cudaStreamSynchronize(h->st));
+  BCK(cudaStreamSynchronize(b->st));
+  if (nq_status s = batch_tune(b)) return s;
+  *b->h_call = (uint32_t)call_index;
+  if (!b->graph)
+    if (nq_status s = batch_capture(b, eps, lr)) return s;
+  BCK(cudaGraphLaunch(b->graph, b->st));
+  b->launches += b->graph_kernels;
+  BCK(cudaMemcpyAsync(b->h_gather, b->d_gather, (size_t)np * 8 * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+  BCK(cudaStreamSynchronize(b->st));
+  nq_status worst = NQ_OK;
+  for (int p = 0; p < np; ++p) {
+    nq_handle* h = b->hs[p];
+    const double* v = b->h_gather + 8 * p;
+    const int st = (int)v[7];
+    if (st != 0) {
+      BCK(cudaMemsetAsync(h->sb.status, 0, sizeof(int), b->st));
+      worst = (st & 0x10) ? NQ_ERR_TIMEOUT : NQ_ERR_NOT_PD;
+      bfail(b, worst, "problem %d: status 0x%x after the step", p, st);
+    }
+    if (stats) {
+      nq_measurement& m = stats[p];
+      m.mean_re = v[0];
+      m.mean_im = v[1];
+      m.error = v[2];
+      m.variance = v[3];
+      m.tau = v[4];
+      m.R = v[5];
+      const double steps = (double)h->B * h->passes * (h->cfg.burn + h->n_record);
+      m.acceptance = steps > 0 ? v[6] / steps : 0.0;
+    }
+  }
+  if (worst != NQ_OK) BCK(cudaStreamSynchronize(b->st));
+  return worst;
+}
+
+nq_status nq_batch_bench_steps(nq_batch* b, uint64_t call0, int32_t n_steps, double eps, double lr,
+                               float* ms_out) {
+  if (!b || !ms_out || n_steps < 1) return NQ_ERR_ARG;
+  if (nq_status s = nq_batch_vmc_step(b, call0, eps, lr, nullptr)) return s;
+  std::vector<cudaEvent_t> ev(2 * n_steps);
+  for (auto& e : ev) BCK(cudaEventCreate(&e));
+  for (int i = 0; i < n_steps; ++i) {
+    BCK(cudaStreamSynchronize(b->st));
+    *b->h_call = (uint32_t)(call0 + 1 + i);
+    BCK(cudaEventRecord(ev[2 * i], b->st));
+    BCK(cudaGraphLaunch(b->graph, b->st));
+    b->launches += b->graph_kernels;
+    BCK(cudaEventRecord(ev[2 * i + 1], b->st));
+  }
+  BCK(cudaStreamSynchronize(b->st));
+  for (int i = 0; i < n_steps; ++i) cudaEventElapsedTime(&ms_out[i], ev[2 * i], ev[2 * i + 1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return NQ_OK;
+}
+
+nq_status nq_batch_tuning(nq_batch* b, int32_t* out, int32_t n) {
+  if (!b || !out || n < 1) return NQ_ERR_ARG;
+  if (nq_status s = batch_tune(b)) return s;
+  const int32_t v[4] = {b->lanes, b->eval_T, b->w_ctas, (int32_t)b->graph_kernels};
+  for (int i = 0; i < n && i < 4; ++i) out[i] = v[i];
+  return NQ_OK;
+}
+
+int64_t nq_batch_kernel_launches(const nq_batch* b) { return b ? b->launches : -1; }
 
 }  // extern "C"

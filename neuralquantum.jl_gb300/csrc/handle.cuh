@@ -77,6 +77,9 @@ struct nq_handle {
   void* d_flush = nullptr;
   size_t flush_bytes = 0;
   MadeState* made = nullptr;       // learned proposal, null until nq_proposal_init
+  bool tc_theta = false;           // NQ_EVAL_TC_BF16X2 / X3: θ = Wσ + b on tcgen05
+  int theta_terms = 2;             // BF16 terms of W (2 or 3)
+  __nv_bfloat16* d_theta_img = nullptr;   // packed BF16 hi/lo image of W
 };
 
 inline nq_status fail(nq_handle* h, nq_status code, const char* fmt, ...) {

@@ -1,6 +1,7 @@
 // Kernel launch interfaces shared between the translation units of
 // libnqcuda.  Every launcher returns a cudaError_t and enqueues on `st`.
 #pragma once
+#include <cuda_bf16.h>
 #include "nq_common.cuh"
 
 // Flattened operator on the device (see nq_op_table in include/nqcuda.h).
@@ -55,11 +56,53 @@ template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
 int rbm_sampler_valid_lanes(int M, int* out, int max_out);
 
+// Many independent problems in one sampler launch (FP32): problem p runs on
+// blocks [blk_start[p], blk_start[p+1]) of 256 threads (256/G chains each);
+// M_max / N_max size the shared tables, G is common to all problems.
+template <typename R> struct SamplerJob {
+  RbmDev<R> net;
+  SamplerRun run;
+};
+template <typename R>
+cudaError_t launch_rbm_sampler_batch(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
+                                     int M_max, int N_max, int act, int G, cudaStream_t st);
+
+// Many-problem evaluation: problem p on blocks [blk_start[p], blk_start[p+1])
+// of T threads (T = rbm_eval_threads(M_max)); the shared tables are sized for
+// M_max x N_max and every job has an operator (has_op = 1).
+template <typename R> struct EvalJob {
+  RbmDev<R> net;
+  const uint64_t* samples;
+  int Ns;
+  DevOp op;
+  int has_op;
+  cpx<R>* logpsi;
+  cpx<R>* g;
+  cpx<R>* eloc;
+};
+int rbm_eval_threads(int M_max);
+template <typename R>
+cudaError_t launch_rbm_eval_batch(const EvalJob<R>* jobs, const int* blk_start, int np, int total_blocks,
+                                  int M_max, int N_max, int act, int T, cudaStream_t st);
+
 // logψ, g = f'(θ) (hidden-major [M][Ns]) and the local estimator on Ns samples.
+// theta_in_g = 1: g holds θ = Wσ + b on entry (launch_theta_bf16x2).
 template <typename R>
 cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int Ns,
                             const DevOp* op, cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc,
-                            cudaStream_t st);
+                            cudaStream_t st, int theta_in_g = 0);
+
+// θ = Wσ + b on tcgen05 with W split into nterms BF16 terms (2: hi + lo,
+// 3: hi + mid + lo; FP32 accumulation): the packed W image
+// (theta_tc_image_elems(M, nterms) BF16) is rebuilt whenever W changes; θ is
+// written as complex FP32 [h][Ns].  N <= 64, 2M <= 512.
+int theta_tc_rows(int M);
+size_t theta_tc_image_elems(int M, int nterms);
+bool theta_tc_supported(int N, int M);
+cudaError_t launch_theta_pack(const cpx<float>* W, int M, int N, int nterms, __nv_bfloat16* img, cudaStream_t st);
+cudaError_t launch_theta_bf16x2(const __nv_bfloat16* img, int nterms, int M, int N, const cpx<float>* b,
+                                const uint64_t* samples, int Ns, int hilb, cpx<float>* theta, int* err,
+                                cudaStream_t st);
 
 // Per-block partial sums of O, E conj(O) and E over sample chunks, then a
 // deterministic FP64 reduction into <O> (meanO) and F.
@@ -106,11 +149,25 @@ cudaError_t launch_gram_reduce(const float* partial, int rows, int rp, int tile,
 cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_params, double* S,
                               cudaStream_t st);
 
-// block Gauss–Jordan inverse of the Hermitian positive-definite W in place (W <- -W^-1,
-// full Hermitian afterwards), one cooperative launch; ctl: sweep_ctl_bytes()
+// block Gauss–Jordan inverse of the Hermitian positive-definite W in place (lower
+// triangle: W <- -W^-1), one cooperative launch; ctl: sweep_ctl_bytes().
+// launch_herm_fill then mirrors the lower triangle into the upper one.
 size_t sweep_ctl_bytes();
 size_t sweep_work_elems(int P);
 cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st);
+// many matrices in one cooperative launch (one CTA group per matrix, groups
+// of total_ctas <= SMs); every job's ctl lies in ctl_base (zeroed here).
+// The Hermitian fill is left to launch_herm_fill per matrix.
+struct SweepJob {
+  float2* W;
+  int P;
+  void* ctl;
+  int* status;
+  float2* work;
+};
+cudaError_t launch_spd_inverse_batch(const SweepJob* jobs, const int* cta_start, int np, int total_ctas,
+                                     void* ctl_base, size_t ctl_bytes, cudaStream_t st);
+cudaError_t launch_herm_fill(float2* W, int P, cudaStream_t st);
 // y = -W x for the full Hermitian W
 cudaError_t launch_herm_gemv_neg(const float2* W, int P, const float2* x, float2* y, cudaStream_t st);
 
@@ -131,6 +188,11 @@ struct SolveBufs {
 // a pivot <= 0 sets bit 0 of status
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st);
+// the two halves around the inversion, for callers that invert several matrices in one launch:
+// W = S + shift; then (after the inversion) fill, x_0 and the refinement steps
+cudaError_t launch_sr_shift(const SolveBufs& sb, int P, int kind, double eps, double lam, cudaStream_t st);
+cudaError_t launch_sr_finish(const SolveBufs& sb, int P, const double* F, int kind, double eps, double lam,
+                             bool real_params, int refine_iters, cudaStream_t st);
 
 // w[i] -= lr * dw[i*stride] on the FP64 master vector (complex parameters:
 // 2P doubles, stride 1; real parameters: P doubles, stride 2 over the complex

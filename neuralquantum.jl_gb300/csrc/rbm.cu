@@ -54,11 +54,12 @@ __global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>*
 // multi-site changes.  Zero matrix elements are skipped
 // (AccumulatorObsScalar.jl:92).
 // ---------------------------------------------------------------------------
+// theta_in_g: gout already holds θ = Wσ + b ([h][Ns], from the tensor-core
+// contraction); it is read and overwritten with g = f'(θ) by the same thread.
 template <typename R, int ACT>
-__global__ void __launch_bounds__(128)
-rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, DevOp op,
-                int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
-                cpx<R>* __restrict__ eloc) {
+NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples, int Ns, const DevOp& op,
+                     int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
+                     cpx<R>* __restrict__ eloc, int blk, int theta_in_g = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = net.N, M = net.M, T = blockDim.x;
   cpx<R>* s_W = reinterpret_cast<cpx<R>*>(smem_raw);     // [M*N]
@@ -73,7 +74,7 @@ rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, Dev
   if (has_op)
     for (int k = threadIdx.x; k < N * M; k += T) { s_t0[k] = net.t0[k]; s_t1[k] = net.t1[k]; }
   __syncthreads();
-  const int s = blockIdx.x * T + threadIdx.x;
+  const int s = blk * T + threadIdx.x;
   if (s >= Ns) return;
   const int hilb = net.hilb;
   const uint64_t bits = samples[s];
@@ -85,11 +86,16 @@ rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, Dev
     lp.y += s_a[j].y * v;
   }
   for (int h = 0; h < M; ++h) {
-    cpx<R> th = s_b[h];
-    for (int j = 0; j < N; ++j) {
-      R v = site_value<R>(bits, j, hilb);
-      th.x += s_W[h + M * j].x * v;
-      th.y += s_W[h + M * j].y * v;
+    cpx<R> th;
+    if (theta_in_g) {
+      th = gout[(size_t)h * Ns + s];
+    } else {
+      th = s_b[h];
+      for (int j = 0; j < N; ++j) {
+        R v = site_value<R>(bits, j, hilb);
+        th.x += s_W[h + M * j].x * v;
+        th.y += s_W[h + M * j].y * v;
+      }
     }
     lp = lp + act_f<ACT>(th);
     cpx<R> gh = act_df<ACT>(th);
@@ -183,6 +189,30 @@ rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, Dev
     }
   }
   eloc[s] = E;
+}
+
+template <typename R, int ACT>
+__global__ void __launch_bounds__(128)
+rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, DevOp op,
+                int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
+                cpx<R>* __restrict__ eloc, int theta_in_g) {
+  eval_block<R, ACT>(net, samples, Ns, op, has_op, logpsi, gout, eloc, blockIdx.x, theta_in_g);
+}
+
+// Many independent problems in one launch: problem p owns blocks
+// [blk_start[p], blk_start[p+1]) of blockDim samples each.
+template <typename R, int ACT>
+__global__ void __launch_bounds__(128)
+rbm_eval_batch_kernel(const EvalJob<R>* __restrict__ jobs, const int* __restrict__ blk_start, int np) {
+  int lo = 0, hi = np - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(blk_start + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  const EvalJob<R>& job = jobs[lo];
+  eval_block<R, ACT>(job.net, job.samples, job.Ns, job.op, job.has_op, job.logpsi, job.g, job.eloc,
+                     b - __ldg(blk_start + lo));
 }
 
 // ---------------------------------------------------------------------------
@@ -366,7 +396,7 @@ static int eval_threads(int M, size_t csize) {
 
 template <typename R>
 cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int Ns, const DevOp* op,
-                            cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc, cudaStream_t st) {
+                            cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc, cudaStream_t st, int theta_in_g) {
   const int T = eval_threads(net.M, sizeof(cpx<R>));
   const int has_op = op != nullptr && eloc != nullptr;
   size_t smem = ((size_t)net.M * net.N + net.M + net.N + (size_t)net.M * T +
@@ -380,17 +410,44 @@ cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int N
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    kern<<<blocks, T, smem, st>>>(net, samples, Ns, dop, has_op, logpsi, g, eloc);
+    kern<<<blocks, T, smem, st>>>(net, samples, Ns, dop, has_op, logpsi, g, eloc, theta_in_g);
   } else {
     auto kern = rbm_eval_kernel<R, ACT_SOFTPLUS>;
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    kern<<<blocks, T, smem, st>>>(net, samples, Ns, dop, has_op, logpsi, g, eloc);
+    kern<<<blocks, T, smem, st>>>(net, samples, Ns, dop, has_op, logpsi, g, eloc, theta_in_g);
   }
   return cudaGetLastError();
 }
+
+int rbm_eval_threads(int M_max) { return eval_threads(M_max, sizeof(cpx<float>)); }
+
+template <typename R>
+cudaError_t launch_rbm_eval_batch(const EvalJob<R>* jobs, const int* blk_start, int np, int total_blocks,
+                                  int M_max, int N_max, int act, int T, cudaStream_t st) {
+  const size_t smem = ((size_t)M_max * N_max + M_max + N_max + (size_t)M_max * T + 2 * (size_t)N_max * M_max) *
+                      sizeof(cpx<R>);
+  if (act == ACT_LOGCOSH) {
+    auto kern = rbm_eval_batch_kernel<R, ACT_LOGCOSH>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<total_blocks, T, smem, st>>>(jobs, blk_start, np);
+  } else {
+    auto kern = rbm_eval_batch_kernel<R, ACT_SOFTPLUS>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<total_blocks, T, smem, st>>>(jobs, blk_start, np);
+  }
+  return cudaGetLastError();
+}
+template cudaError_t launch_rbm_eval_batch<float>(const EvalJob<float>*, const int*, int, int, int, int, int, int,
+                                                  cudaStream_t);
 
 static int force_chunk(int N, int M, int csize) {
   int CH = 256;
@@ -448,8 +505,8 @@ cudaError_t launch_unpack_int8(const uint64_t* bits, int nsites, long n, int hil
 // explicit instantiations
 template cudaError_t launch_rbm_tables<float>(const RbmDev<float>&, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
 template cudaError_t launch_rbm_tables<double>(const RbmDev<double>&, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
-template cudaError_t launch_rbm_eval<float>(const RbmDev<float>&, const uint64_t*, int, const DevOp*, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
-template cudaError_t launch_rbm_eval<double>(const RbmDev<double>&, const uint64_t*, int, const DevOp*, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
+template cudaError_t launch_rbm_eval<float>(const RbmDev<float>&, const uint64_t*, int, const DevOp*, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t, int);
+template cudaError_t launch_rbm_eval<double>(const RbmDev<double>&, const uint64_t*, int, const DevOp*, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t, int);
 template cudaError_t launch_rbm_force<float>(const RbmDev<float>&, const uint64_t*, int, const cpx<float>*, const cpx<float>*, const ForceBufs&, cudaStream_t);
 template cudaError_t launch_rbm_force<double>(const RbmDev<double>&, const uint64_t*, int, const cpx<double>*, const cpx<double>*, const ForceBufs&, cudaStream_t);
 template cudaError_t launch_rbm_grad_matrix<float>(const uint64_t*, int, int, int, int, const cpx<float>*, double*, cudaStream_t);

@@ -24,9 +24,11 @@ template <> NQ_D float fast_log2<float>(float x) { return __log2f(x); }
 template <typename R> NQ_D R fast_rcp(R x) { return R(1) / x; }
 template <> NQ_D float fast_rcp<float>(float x) { return __frcp_rn(x); }
 
+// One block of the sampler: chains (blk * blockDim + tid) / G of the problem
+// described by (net, run).  Shared by the single-problem kernel and the
+// many-problem kernel below.
 template <typename R, int G, int HPL, int ACT>
-__global__ void __launch_bounds__(256)
-rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
+NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = net.N, M = net.M, n_half = net.n_half;
   cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
@@ -45,7 +47,7 @@ rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
   __syncthreads();
 
   const int lane = threadIdx.x % G;
-  const int chain_raw = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int chain_raw = (blk * blockDim.x + threadIdx.x) / G;
   const bool active = chain_raw < run.B;
   const int chain = active ? chain_raw : run.B - 1;
   const int hilb = net.hilb;
@@ -164,6 +166,26 @@ rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
   if (active && lane == 0) atomicAdd(run.accepted, naccept);
 }
 
+template <typename R, int G, int HPL, int ACT>
+__global__ void __launch_bounds__(256) rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
+  sampler_block<R, G, HPL, ACT>(net, run, blockIdx.x);
+}
+
+// Many independent problems in one launch: problem p owns blocks
+// [blk_start[p], blk_start[p+1]); every block loads its own problem's tables.
+template <typename R, int G, int HPL, int ACT>
+__global__ void __launch_bounds__(256)
+rbm_sampler_batch_kernel(const SamplerJob<R>* __restrict__ jobs, const int* __restrict__ blk_start, int np) {
+  int lo = 0, hi = np - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {                       // last p with blk_start[p] <= b
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(blk_start + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  const SamplerJob<R> job = jobs[lo];
+  sampler_block<R, G, HPL, ACT>(job.net, job.run, b - __ldg(blk_start + lo));
+}
+
 }  // namespace
 
 template <typename R, int G, int HPL, int ACT>
@@ -219,3 +241,49 @@ cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int 
   return sampler_g<R, ACT_SOFTPLUS>(net, run, G, st);
 }
 
+
+template <typename R, int G, int HPL, int ACT>
+static cudaError_t sampler_batch_inst(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
+                                      size_t smem, cudaStream_t st) {
+  auto kern = rbm_sampler_batch_kernel<R, G, HPL, ACT>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<total_blocks, 256, smem, st>>>(jobs, blk_start, np);
+  return cudaGetLastError();
+}
+
+template <typename R, int G, int ACT>
+static cudaError_t sampler_batch_hpl(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
+                                     int M_max, size_t smem, cudaStream_t st) {
+  switch ((M_max + G - 1) / G) {
+    case 1: return sampler_batch_inst<R, G, 1, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 2: return sampler_batch_inst<R, G, 2, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 3: return sampler_batch_inst<R, G, 3, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 4: return sampler_batch_inst<R, G, 4, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 5: return sampler_batch_inst<R, G, 5, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 6: return sampler_batch_inst<R, G, 6, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 8: return sampler_batch_inst<R, G, 8, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 10: return sampler_batch_inst<R, G, 10, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+cudaError_t launch_rbm_sampler_batch(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
+                                     int M_max, int N_max, int act, int G, cudaStream_t st) {
+  if (N_max > 64 || !hpl_ok((M_max + G - 1) / G)) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)4 * N_max * M_max * sizeof(cpx<R>) + N_max * sizeof(R);
+  switch (G) {
+    case 4: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 4, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
+                                      : sampler_batch_hpl<R, 4, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
+    case 8: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 8, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
+                                      : sampler_batch_hpl<R, 8, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
+    case 16: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 16, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
+                                       : sampler_batch_hpl<R, 16, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
+    case 32: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 32, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
+                                       : sampler_batch_hpl<R, 32, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
+    default: return cudaErrorInvalidValue;
+  }
+}

@@ -32,7 +32,8 @@ struct SweepCtl {
   int pad;
 };
 
-__device__ bool grid_barrier(SweepCtl* ctl, int* err) {
+// Barrier over the `n` CTAs that share ctl (the whole grid, or one group).
+__device__ bool group_barrier(SweepCtl* ctl, unsigned n, int* err) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -40,7 +41,7 @@ __device__ bool grid_barrier(SweepCtl* ctl, int* err) {
     volatile unsigned* vgen = &ctl->gen;
     const unsigned g = *vgen;
     __threadfence();
-    if (atomicAdd(&ctl->count, 1u) == gridDim.x - 1) {
+    if (atomicAdd(&ctl->count, 1u) == n - 1) {
       atomicExch(&ctl->count, 0u);
       __threadfence();
       atomicAdd(&ctl->gen, 1u);
@@ -142,9 +143,9 @@ NQ_D void tile_mm(const float2 (*U)[CB + 1], const float2 (*V)[CB + 1], float2 o
   }
 }
 
-__global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W, int P, SweepCtl* ctl,
-                                                         int* status, float2* __restrict__ Cbuf,
-                                                         float2* __restrict__ Gbuf, float2* __restrict__ pivbuf) {
+// The sweep of one matrix by the CTAs rank = 0..nranks-1 of its group.
+NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status, float2* __restrict__ Cbuf,
+                      float2* __restrict__ Gbuf, float2* __restrict__ pivbuf, int rank, int nranks) {
   __shared__ float2 Dt[CB][CB + 1];
   __shared__ float2 Ut[CB][CB + 1];
   __shared__ float2 Vt[CB][CB + 1];
@@ -155,8 +156,8 @@ __global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W,
     const int k0 = kb * CB, nbk = min(CB, P - k0);
     // ---------------- phase A: pivot inverse, C_i and the old column ----------------
     const int ncol = nblk - 1;
-    const bool has_col = blockIdx.x < ncol;
-    if (has_col || blockIdx.x == 0) {
+    const bool has_col = rank < ncol;
+    if (has_col || rank == 0) {
       for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
         const int r = e & 31, c = e >> 5;
         float2 v;
@@ -172,11 +173,11 @@ __global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W,
       }
       __syncthreads();
       const bool ok = hpd_inverse_32(Dt, colbuf);
-      if (!ok && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, 1);
-      if (blockIdx.x == 0)
+      if (!ok && rank == 0 && threadIdx.x == 0) atomicOr(status, 1);
+      if (rank == 0)
         for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) pivbuf[e] = Dt[e & 31][e >> 5];
     }
-    for (int b = blockIdx.x; b < ncol; b += gridDim.x) {
+    for (int b = rank; b < ncol; b += nranks) {
       const int ib = b < kb ? b : b + 1;
       const int i0 = ib * CB;
       __syncthreads();
@@ -200,10 +201,10 @@ __global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W,
 #pragma unroll
       for (int q = 0; q < 4; ++q) Cbuf[(size_t)ib * CB * CB + (cg + q) * CB + tr] = o[q];
     }
-    if (!grid_barrier(ctl, status)) return;
+    if (!group_barrier(ctl, (unsigned)nranks, status)) return;
     // ---------------- phase B: lower tiles ----------------
     const int ntiles = nblk * (nblk + 1) / 2;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (int t = rank; t < ntiles; t += nranks) {
       int ti, tj;
       {
         int c = 0, r = t;
@@ -254,8 +255,31 @@ __global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W,
         }
       }
     }
-    if (!grid_barrier(ctl, status)) return;
+    if (!group_barrier(ctl, (unsigned)nranks, status)) return;
   }
+}
+
+__global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W, int P, SweepCtl* ctl,
+                                                         int* status, float2* __restrict__ Cbuf,
+                                                         float2* __restrict__ Gbuf, float2* __restrict__ pivbuf) {
+  sweep_group(W, P, ctl, status, Cbuf, Gbuf, pivbuf, blockIdx.x, gridDim.x);
+}
+
+// Many matrices in one cooperative launch: matrix p is swept by CTAs
+// [cta_start[p], cta_start[p+1]) with its own barrier block.
+__global__ void __launch_bounds__(256) sweep_batch_kernel(const SweepJob* __restrict__ jobs,
+                                                          const int* __restrict__ cta_start, int np) {
+  int lo = 0, hi = np - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(cta_start + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  const SweepJob& j = jobs[lo];
+  const int r0 = __ldg(cta_start + lo), n = __ldg(cta_start + lo + 1) - r0;
+  sweep_group(j.W, j.P, reinterpret_cast<SweepCtl*>(j.ctl), j.status, j.work,
+              j.work + (size_t)((j.P + CB - 1) / CB) * CB * CB, j.work + (size_t)2 * ((j.P + CB - 1) / CB) * CB * CB,
+              b - r0, n);
 }
 
 // W upper = conj(W lower) so that column i holds row i of the Hermitian matrix
@@ -335,14 +359,34 @@ cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2*
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   SweepCtl* c = reinterpret_cast<SweepCtl*>(ctl);
-  e = cudaLaunchKernelEx(&cfg, sweep_coop_kernel, W, P, c, status, Cbuf, Gbuf, pivbuf);
-  if (e != cudaSuccess) return e;
-  const dim3 tb(32, 8), tg((unsigned)nblk, (unsigned)nblk);
-  herm_fill_kernel<<<tg, tb, 0, st>>>(W, P);
-  return cudaGetLastError();
+  return cudaLaunchKernelEx(&cfg, sweep_coop_kernel, W, P, c, status, Cbuf, Gbuf, pivbuf);
 }
 
 cudaError_t launch_herm_gemv_neg(const float2* W, int P, const float2* x, float2* y, cudaStream_t st) {
   herm_gemv_neg_kernel<<<(P + 7) / 8, 256, 0, st>>>(W, P, x, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spd_inverse_batch(const SweepJob* jobs, const int* cta_start, int np, int total_ctas,
+                                     void* ctl_base, size_t ctl_bytes, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(ctl_base, 0, ctl_bytes, st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(total_ctas);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, sweep_batch_kernel, jobs, cta_start, np);
+}
+
+cudaError_t launch_herm_fill(float2* W, int P, cudaStream_t st) {
+  const int nblk = (P + CB - 1) / CB;
+  const dim3 tb(32, 8), tg((unsigned)nblk, (unsigned)nblk);
+  herm_fill_kernel<<<tg, tb, 0, st>>>(W, P);
   return cudaGetLastError();
 }

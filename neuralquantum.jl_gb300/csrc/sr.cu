@@ -1,12 +1,13 @@
 // Stochastic reconfiguration: the S = O_c O_c† accumulation (FP32 CUDA-core
 // variant and the X materialisation for the tcgen05 variant), assembly of the
-// Hermitian S, the diagonally shifted solve (FP32 blocked Cholesky with FP64
-// iterative refinement, so the returned Δw solves the FP64 system), the
+// Hermitian S, the diagonally shifted solve (FP32 inverse of the shifted S
+// with FP64 iterative refinement, so the returned Δw solves the FP64 system), the
 // Descent update and the Measurement statistics.
 //
 // Reference: src/Algorithms/SR/SRDirect.jl:26-90 (S, F, shift, Cholesky),
 // src/Optimisers/apply.jl:25-32 + rules.jl:15-17 (Descent),
 // src/utils/stats.jl:26-50 (Measurement).
+#include <algorithm>
 #include "nq_kernels.cuh"
 
 namespace {
@@ -127,16 +128,50 @@ __device__ __forceinline__ float to_tf32(float x) {
   return __uint_as_float(r);
 }
 
-__global__ void build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X,
-                               float* __restrict__ Xlo) {
-  long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (idx >= (long)rows * Ns_pad) return;
-  int row = (int)(idx / Ns_pad), s = (int)(idx % Ns_pad);
-  float v = 0.f;
-  if (s < src.Ns) v = x_value(src, row, s, src.samples[s]);
-  const float hi = to_tf32(v);
-  X[idx] = hi;
-  if (Xlo) Xlo[idx] = to_tf32(v - hi);
+// One row of X per blockIdx.y (the row's kind, hidden unit, site and mean are
+// block-uniform), four consecutive samples per thread with 16-byte stores.
+// HBM-bound: writes 4·rows·Ns_pad bytes (twice with Xlo); g rows and σ are
+// re-read by the 2(N+1) rows that share them, from L2.
+__global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X,
+                                                      float* __restrict__ Xlo) {
+  const int row = blockIdx.y;
+  const int N = src.N, M = src.M, Ns = src.Ns, hilb = src.hilb;
+  const int k = row >> 1, part = row & 1;
+  int kind, h = 0, j = 0;          // 0: visible unit j, 1: hidden unit h, 2: weight (h, j)
+  if (k < N) { kind = 0; j = k; }
+  else if (k < N + M) { kind = 1; h = k - N; }
+  else { kind = 2; const int q = k - N - M; h = q % M; j = q / M; }
+  const float mean = (float)src.meanO[2 * k + part];
+  const float2* __restrict__ grow = src.g + (size_t)h * Ns;
+  float* xrow = X + (size_t)row * Ns_pad;
+  float* lrow = Xlo ? Xlo + (size_t)row * Ns_pad : nullptr;
+  for (int s0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4; s0 < Ns_pad; s0 += gridDim.x * blockDim.x * 4) {
+    float v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int s = s0 + e;
+      float val = 0.f;
+      if (s < Ns) {
+        float ox, oy;
+        if (kind == 0) {
+          ox = site_valuef(src.samples[s], j, hilb);
+          oy = 0.f;
+        } else {
+          const float2 g = grow[s];
+          const float w = kind == 2 ? site_valuef(src.samples[s], j, hilb) : 1.f;
+          ox = g.x * w;
+          oy = g.y * w;
+        }
+        val = (part ? oy : ox) - mean;
+      }
+      v[e] = val;
+    }
+    const float4 hi = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+    *reinterpret_cast<float4*>(xrow + s0) = hi;
+    if (lrow)
+      *reinterpret_cast<float4*>(lrow + s0) =
+          make_float4(to_tf32(v[0] - hi.x), to_tf32(v[1] - hi.y), to_tf32(v[2] - hi.z), to_tf32(v[3] - hi.w));
+  }
 }
 
 __device__ __forceinline__ float gsym(const float* G, int rows, int a, int b) {
@@ -358,8 +393,10 @@ cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float*
 
 cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo,
                            cudaStream_t st) {
-  long tot = 2L * P * Ns_pad;
-  build_X_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(src, 2 * P, Ns_pad, X, Xlo);
+  if (Ns_pad % 4 != 0 || 2 * P > 65535) return cudaErrorInvalidValue;
+  const int per_block = 256 * 4;
+  const int bx = std::min((Ns_pad + per_block - 1) / per_block, 64);
+  build_X_kernel<<<dim3((unsigned)bx, (unsigned)(2 * P)), 256, 0, st>>>(src, 2 * P, Ns_pad, X, Xlo);
   return cudaGetLastError();
 }
 
@@ -377,16 +414,16 @@ cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_pa
   return cudaGetLastError();
 }
 
-cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
-                            double lam, bool real_params, int refine_iters, cudaStream_t st) {
-  auto mark = [&](int k) { if (sb.ev) cudaEventRecord(sb.ev[k], st); };
-  long tot = (long)P * P;
-  mark(0);
+cudaError_t launch_sr_shift(const SolveBufs& sb, int P, int kind, double eps, double lam, cudaStream_t st) {
+  const long tot = (long)P * P;
   shift_copy_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(sb.S, P, kind, eps, lam, sb.W);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  mark(1);
-  e = launch_spd_inverse(sb.W, P, sb.ctl, sb.status, sb.work, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sr_finish(const SolveBufs& sb, int P, const double* F, int kind, double eps, double lam,
+                             bool real_params, int refine_iters, cudaStream_t st) {
+  auto mark = [&](int k) { if (sb.ev) cudaEventRecord(sb.ev[k], st); };
+  cudaError_t e = launch_herm_fill(sb.W, P, st);
   if (e != cudaSuccess) return e;
   mark(2);
   rhs_init_kernel<<<(P + 255) / 256, 256, 0, st>>>(F, P, real_params ? 1 : 0, sb.rf);
@@ -402,6 +439,18 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   }
   mark(5);
   return cudaSuccess;
+}
+
+cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
+                            double lam, bool real_params, int refine_iters, cudaStream_t st) {
+  auto mark = [&](int k) { if (sb.ev) cudaEventRecord(sb.ev[k], st); };
+  mark(0);
+  cudaError_t e = launch_sr_shift(sb, P, kind, eps, lam, st);
+  if (e != cudaSuccess) return e;
+  mark(1);
+  e = launch_spd_inverse(sb.W, P, sb.ctl, sb.status, sb.work, st);
+  if (e != cudaSuccess) return e;
+  return launch_sr_finish(sb, P, F, kind, eps, lam, real_params, refine_iters, st);
 }
 
 cudaError_t launch_descent(double* master, const double* dw, long n_doubles, int stride, double lr,

@@ -13,6 +13,7 @@ from .operators import (LocalOperator, KLocalOperator, KLocalOperatorSum, KLocal
 from .networks import RBM, NDM, af_logcosh, af_softplus, init_random_pars_  # noqa: F401
 from .samplers import MetropolisSampler, LocalRule  # noqa: F401
 from .stats import Measurement  # noqa: F401
-from .iterative import (BatchedSampler, SR, Descent, sample_, precondition_, update_,  # noqa: F401
+from .iterative import (BatchedSampler, BatchedObsKetSampler, add_observable_, SR, Descent, sample_,  # noqa: F401
+                        precondition_, update_,  # noqa: F401
                         sr_shift, sr_multiplicative, sr_none, sr_cholesky)
-from .engine import Engine  # noqa: F401
+from .engine import Engine, ProblemBatch  # noqa: F401

@@ -18,7 +18,7 @@ INCLUDE = os.path.join(_REPO, "include")
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
-           "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu"]
+           "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -30,7 +30,7 @@ NQ_NET_RBM, NQ_NET_NDM = 0, 1
 NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS = 0, 1
 NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3
-NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64 = 0, 1, 2
+NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64, NQ_EVAL_TC_BF16X3 = 0, 1, 2, 3
 NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64 = 0, 1, 2, 3
 NQ_QUIRK_STALE_LAST_SLOT = 0x1
 
@@ -83,6 +83,7 @@ EXPORTS = {
                                       ctypes.c_void_p, ctypes.c_void_p]),
     "nq_estimate": (ctypes.c_int, [ctypes.c_void_p, _P(NqMeasurement), ctypes.c_void_p,
                                    ctypes.c_void_p]),
+    "nq_observable": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable), _P(NqMeasurement), ctypes.c_void_p]),
     "nq_get_sr_matrix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_precondition": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -109,6 +110,17 @@ EXPORTS = {
     "nq_proposal_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                          _P(ctypes.c_double)]),
     "nq_proposal_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "nq_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_void_p)]),
+    "nq_batch_destroy": (None, [ctypes.c_void_p]),
+    "nq_batch_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "nq_batch_size": (ctypes.c_int32, [ctypes.c_void_p]),
+    "nq_batch_handle": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_int32]),
+    "nq_batch_vmc_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_void_p]),
+    "nq_batch_bench_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_double,
+                                            ctypes.c_double, _P(ctypes.c_float)]),
+    "nq_batch_tuning": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int32), ctypes.c_int32]),
+    "nq_batch_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),
     "nq_measurement_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                               ctypes.c_size_t]),

@@ -8,43 +8,56 @@ from .hilbert import SuperOpSpace, physical
 from .networks import RBM, NDM, af_logcosh
 
 
+def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
+                s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0):
+    """nq_config of one problem (include/nqcuda.h)."""
+    cfg = _lib.NqConfig()
+    ph = physical(hilb)
+    if isinstance(net, RBM):
+        cfg.network = _lib.NQ_NET_RBM
+        cfg.n_hidden = net.M
+        cfg.n_ancilla = 0
+    elif isinstance(net, NDM):
+        cfg.network = _lib.NQ_NET_NDM
+        cfg.n_hidden = net.Mh
+        cfg.n_ancilla = net.Ma
+    else:
+        raise TypeError(f"unsupported network {type(net)}")
+    cfg.activation = _lib.NQ_ACT_LOGCOSH if net.f == af_logcosh else _lib.NQ_ACT_SOFTPLUS
+    cfg.hilbert = _lib.NQ_HILB_SPIN if ph.kind == "spin" else _lib.NQ_HILB_FOCK
+    cfg.n_sites = ph.n_sites
+    cfg.n_chains = n_chains
+    cfg.chain_length = chain_length
+    cfg.burn = burn
+    cfg.passes = passes
+    cfg.seed = seed
+    cfg.eval_precision = eval_precision
+    cfg.s_precision = s_precision
+    cfg.quirks = quirks
+    cfg.sampler_lanes = sampler_lanes
+    return cfg
+
+
 class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
                  eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
-                 sampler_lanes=0):
+                 sampler_lanes=0, _handle=None, _owner=None):
         L = _lib.lib()
-        cfg = _lib.NqConfig()
-        ph = physical(hilb)
-        if isinstance(net, RBM):
-            cfg.network = _lib.NQ_NET_RBM
-            cfg.n_hidden = net.M
-            cfg.n_ancilla = 0
-            self.complex_params = True
-        elif isinstance(net, NDM):
-            cfg.network = _lib.NQ_NET_NDM
-            cfg.n_hidden = net.Mh
-            cfg.n_ancilla = net.Ma
-            self.complex_params = False
-        else:
-            raise TypeError(f"unsupported network {type(net)}")
-        cfg.activation = _lib.NQ_ACT_LOGCOSH if net.f == af_logcosh else _lib.NQ_ACT_SOFTPLUS
-        cfg.hilbert = _lib.NQ_HILB_SPIN if ph.kind == "spin" else _lib.NQ_HILB_FOCK
-        cfg.n_sites = ph.n_sites
-        cfg.n_chains = n_chains
-        cfg.chain_length = chain_length
-        cfg.burn = burn
-        cfg.passes = passes
-        cfg.seed = seed
-        cfg.eval_precision = eval_precision
-        cfg.s_precision = s_precision
-        cfg.quirks = quirks
-        cfg.sampler_lanes = sampler_lanes
+        cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
+                          s_precision, quirks, sampler_lanes)
+        self.complex_params = isinstance(net, RBM)
         self.cfg = cfg
         self.lib = L
-        self.h = ctypes.c_void_p()
-        st = L.nq_create(ctypes.byref(cfg), ctypes.byref(self.h))
-        if st != _lib.NQ_OK:
-            raise _lib.NqError(st, "nq_create failed (see stderr)")
+        self._owned = _handle is None
+        self._owner = _owner                  # keeps a batch alive while its problem handles are used
+        if _handle is None:
+            self.h = ctypes.c_void_p()
+            st = L.nq_create(ctypes.byref(cfg), ctypes.byref(self.h))
+            if st != _lib.NQ_OK:
+                raise _lib.NqError(st, "nq_create failed (see stderr)")
+        else:
+            self.h = ctypes.c_void_p(_handle)
+        ph = physical(hilb)
         self.P = int(L.nq_n_params(self.h))
         self.N = ph.n_sites
         self.nsites = 2 * ph.n_sites if isinstance(hilb, SuperOpSpace) else ph.n_sites
@@ -54,7 +67,7 @@ class Engine:
 
     def __del__(self):
         try:
-            if self.h:
+            if self.h and self._owned:
                 self.lib.nq_destroy(self.h)
                 self.h = ctypes.c_void_p()
         except Exception:
@@ -128,6 +141,15 @@ class Engine:
                                          loc.ctypes.data if loc is not None else None,
                                          force.ctypes.data if force is not None else None))
         return m, loc, force
+
+    def observable(self, table, want_loc=False):
+        """Measurement of the local values of another operator on the current samples."""
+        m = _lib.NqMeasurement()
+        loc = np.empty((self.L, self.B), np.complex128) if want_loc else None
+        st = table.struct()
+        self._check(self.lib.nq_observable(self.h, ctypes.byref(st), ctypes.byref(m),
+                                           loc.ctypes.data if loc is not None else None))
+        return m, loc
 
     def sr_matrix(self):
         S = np.empty((self.P, self.P), np.complex128 if self.complex_params else np.float64, order="F")
@@ -213,3 +235,73 @@ class Engine:
         v = np.zeros(2, dtype=np.uint64)
         self._check(self.lib.nq_proposal_stats(self.h, v.ctypes.data))
         return int(v[0]), int(v[1])
+
+
+class ProblemBatch:
+    """Many independent RBM problems stepped together (nq_batch_*): one
+    sampler launch, one estimator launch and one inversion launch for all of
+    them per SR step, inside one CUDA graph.  ``problems`` is a list of
+    (net, hilb, operator) with RBM networks of one activation; every problem
+    gets n_chains chains of chain_length samples."""
+
+    def __init__(self, problems, n_chains, chain_length, burn, passes=None, seed=0x4E51,
+                 s_precision=_lib.NQ_S_TF32):
+        from .operators import op_table
+        L = _lib.lib()
+        self.lib = L
+        n = len(problems)
+        cfgs = (_lib.NqConfig * n)()
+        for i, (net, hilb, _) in enumerate(problems):
+            ps = passes if passes is not None else physical(hilb).n_sites
+            cfgs[i] = make_config(net, hilb, n_chains, chain_length, burn, ps, seed + 7919 * i,
+                                  _lib.NQ_EVAL_F32, s_precision)
+        self.b = ctypes.c_void_p()
+        st = L.nq_batch_create(ctypes.cast(cfgs, ctypes.c_void_p), n, ctypes.byref(self.b))
+        if st != _lib.NQ_OK:
+            raise _lib.NqError(st, "nq_batch_create failed")
+        self.engines = []
+        for i, (net, hilb, op) in enumerate(problems):
+            ps = passes if passes is not None else physical(hilb).n_sites
+            h = L.nq_batch_handle(self.b, i)
+            e = Engine(net, hilb, n_chains, chain_length, burn, ps, seed + 7919 * i, _lib.NQ_EVAL_F32,
+                       s_precision, _handle=h, _owner=self)
+            e.set_params(net.flat())
+            e.set_operator(op_table(op))
+            self.engines.append(e)
+        self.n = n
+
+    def _check(self, st):
+        if st != _lib.NQ_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.nq_batch_last_error(self.b, buf, 512)
+            raise _lib.NqError(st, buf.value.decode(errors="replace"))
+
+    def vmc_step(self, call_index, eps, lr):
+        ms = (_lib.NqMeasurement * self.n)()
+        self._check(self.lib.nq_batch_vmc_step(self.b, call_index, eps, lr, ctypes.cast(ms, ctypes.c_void_p)))
+        return list(ms)
+
+    def bench_steps(self, call0, n, eps, lr):
+        out = np.zeros(n, np.float32)
+        self._check(self.lib.nq_batch_bench_steps(self.b, call0, n, eps, lr,
+                                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def tuning(self):
+        v = (ctypes.c_int32 * 4)()
+        self._check(self.lib.nq_batch_tuning(self.b, v, 4))
+        return {"sampler_lanes": v[0], "estimator_threads": v[1], "inversion_ctas": v[2],
+                "kernels_per_step": v[3]}
+
+    def kernel_launches(self):
+        return int(self.lib.nq_batch_kernel_launches(self.b))
+
+    def __del__(self):
+        try:
+            for e in getattr(self, "engines", []):
+                e.h = ctypes.c_void_p()
+            if getattr(self, "b", None):
+                self.lib.nq_batch_destroy(self.b)
+                self.b = ctypes.c_void_p()
+        except Exception:
+            pass

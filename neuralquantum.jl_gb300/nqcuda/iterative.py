@@ -115,3 +115,30 @@ def update_(opt, net, grad):
     s.engine.update_descent(opt.eta)
     s.sync_net()
     return net
+
+
+class BatchedObsKetSampler:
+    """``BatchedObsKetSampler`` (Obs/BatchedObsKetSampler.jl:1-60): local
+    values of named observables on the samples of the last sample call of a
+    ``BatchedSampler``, with their ``Measurement``."""
+
+    def __init__(self, sampler):
+        self.sampler = sampler
+        self.observables = {}
+        self.results = {}
+
+    def add_observable_(self, name, op):
+        self.observables[name] = op_table(op)
+
+    def compute_observable(self, table):
+        m, _ = self.sampler.engine.observable(table)
+        return Measurement(complex(m.mean_re, m.mean_im), m.error, m.variance, m.tau, m.R)
+
+    def compute_observables(self):
+        for name, table in self.observables.items():
+            self.results[name] = self.compute_observable(table)
+        return self.results
+
+
+def add_observable_(obs, name, op):
+    obs.add_observable_(name, op)

@@ -18,10 +18,12 @@ class Measurement:
 
 def integrated_autocorr_time(x, window=5.0):
     """Integrated autocorrelation time of a (chains, samples) series, in
-    samples: the chain-averaged autocovariance (computed by FFT) summed up to
-    the first lag M with M >= window * tau (Sokal's self-consistent window).
-    The reference reports only its ``tau`` of ``Measurement``; this one backs
-    the effective-sample-size figures."""
+    samples, in the convention tau = 1 + 2 Σ_{t>=1} ρ(t) (tau = 1 for
+    independent samples, so the effective sample size is n / tau).  ρ is the
+    chain-averaged autocovariance (computed by FFT) normalised at lag 0; the
+    sum stops at the first lag M with M >= window * tau (Sokal's
+    self-consistent window).  The reference reports only the ``tau`` of
+    ``Measurement``; this one backs the effective-sample-size figures."""
     import numpy as np
     v = np.asarray(x, dtype=np.complex128)
     v = v - v.mean(axis=1, keepdims=True)
@@ -29,14 +31,14 @@ def integrated_autocorr_time(x, window=5.0):
     spec = np.fft.fft(v, n=2 * n, axis=1)
     acov = np.fft.ifft(np.abs(spec) ** 2, axis=1)[:, :n].real.mean(axis=0)
     if not acov[0] > 0:
-        return 0.5
+        return 1.0
     rho = acov / acov[0]
-    tau = 0.5
+    tau = 1.0
     for lag in range(1, n):
-        tau += rho[lag]
+        tau += 2.0 * rho[lag]
         if lag >= window * tau:
             break
-    return max(tau, 0.5)
+    return max(tau, 1.0)
 
 
 def effective_sample_size(x, window=5.0):

@@ -172,3 +172,39 @@ def test_sampler_every_lane_layout_replays_bitexact(nqlib, lanes):
     assert info["mismatch"] == 0
     np.testing.assert_array_equal(samples.astype(np.float64), ref)
     assert eng.tuning()["sampler_lanes"] == lanes
+
+
+def test_observables_match_oracle(nqlib):
+    """BatchedObsKetSampler: local values of Σσx, σyσy and a σz correlator on the
+    current samples (estimator kernel with another operator table) against the
+    FP64 oracle; an observable equal to H reproduces the energy estimate."""
+    from oracle import operators as oops, estimators as oest2
+    N, B, L = 6, 128, 5
+    is_, net, onet, oH, ohilb = make(N=N, B=B, L=L, sigma=0.2 ** 2)
+    hilb = nq.HomogeneousSpin(N)
+    samples, _ = is_.engine.sample(4)
+    mE, locE, _ = is_.engine.estimate(want_loc=True)
+    flat = samples.reshape(-1, N).astype(np.float64)
+    cases = []
+    X = nq.LocalOperator(hilb)
+    oX = oops.OpSum(ohilb)
+    for i in range(1, N + 1):
+        X = X + nq.sigmax(hilb, i)
+        oX = oX + oops.sigmax(ohilb, i - 1)
+    cases.append((X, oX))
+    cases.append((nq.sigmay(hilb, 2) * nq.sigmay(hilb, 3),
+                  oops.OpSum(ohilb) + oops.prod(oops.sigmay(ohilb, 1), oops.sigmay(ohilb, 2))))
+    cases.append((nq.sigmaz(hilb, 1) * nq.sigmaz(hilb, 4),
+                  oops.OpSum(ohilb) + oops.prod(oops.sigmaz(ohilb, 0), oops.sigmaz(ohilb, 3))))
+    obs = nq.BatchedObsKetSampler(is_)
+    for k, (op, oop) in enumerate(cases):
+        m, loc = is_.engine.observable(nq.op_table(op), want_loc=True)
+        ref = oest2.local_energy(onet, oop, flat)
+        assert rel(loc.reshape(-1), ref) < 2e-5
+        assert abs(m.mean_re - ref.real.mean()) < 2e-5 * max(1.0, np.max(np.abs(ref)))
+        nq.add_observable_(obs, f"o{k}", op)
+    res = obs.compute_observables()
+    assert set(res) == {"o0", "o1", "o2"}
+    mH, locH = is_.engine.observable(nq.op_table(is_.prob), want_loc=True)
+    np.testing.assert_allclose(locH, locE, rtol=0, atol=1e-12)
+    assert mH.mean_re == mE.mean_re

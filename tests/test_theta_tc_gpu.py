@@ -1,0 +1,86 @@
+"""θ = Wσ + b on tcgen05 (NQ_EVAL_TC_BF16X2) against the FP64 oracle and
+the FP32 CUDA-core evaluation.
+
+W is split into BF16 terms and accumulated in FP32.  With three terms
+(hi + mid + lo, about 24 significant bits) θ is as accurate as the FP32
+CUDA-core path: the errors of logψ and ∇logψ against the FP64 oracle stay
+within twice the FP32 path's errors on the same inputs (which grow with N
+and near the poles of tanh for complex θ).  With two terms (about 16 bits)
+logψ stays within 1e-4 relative and g = tanh θ within 2e-3.  Sizes cover one K step (N = 7),
+two column chunks of the MMA (2M = 288 > 256) and partial tiles.
+"""
+import numpy as np
+import pytest
+
+import nqcuda as nq
+from oracle import networks as onw
+
+pytestmark = pytest.mark.gpu
+
+
+def engine(N, alpha, prec, B=96, L=3, sigma=0.2 ** 2, seed=5):
+    hilb = nq.HomogeneousSpin(N)
+    net = nq.RBM(np.complex64, N, alpha, nq.af_logcosh)
+    nq.init_random_pars_(net, sigma=sigma, rng=np.random.default_rng(seed))
+    H = nq.LocalOperator(hilb)
+    for i in range(1, N + 1):
+        H = H - 1.3 * nq.sigmax(hilb, i)
+        H = H + nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i % N + 1)
+    s = nq.MetropolisSampler(nq.LocalRule(), L, N, burn=4, seed=seed)
+    is_ = nq.BatchedSampler(net, s, H, nq.SR(eps=0.01), batch_sz=B, eval_precision=prec)
+    onet = onw.RBM(N, net.M, onw.LOGCOSH)
+    onet.set_flat(net.flat())
+    return is_.engine, onet
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(1e-30, np.max(np.abs(b))))
+
+
+X2, X3 = nq._lib.NQ_EVAL_TC_BF16X2, nq._lib.NQ_EVAL_TC_BF16X3
+
+
+def _errors(N, alpha, prec):
+    eng, onet = engine(N, alpha, prec)
+    rng = np.random.default_rng(N)
+    sig = rng.choice([-1, 1], size=(301, N)).astype(np.int8)
+    lp, g = eng.logpsi(sig, with_grad=True)
+    olp, og = onet.logpsi_and_grad(sig.astype(np.float64))
+    d = lp - olp
+    d = d.real + 1j * ((d.imag + np.pi) % (2 * np.pi) - np.pi)
+    return np.max(np.abs(d)) / np.max(np.abs(olp)), rel(g, og)
+
+
+@pytest.mark.parametrize("N,alpha", [(7, 2), (20, 2), (36, 4), (33, 3)])
+def test_theta_tc_logpsi_and_grad(nqlib, N, alpha):
+    """Three BF16 terms are as accurate as FP32 CUDA cores (within 2x of the
+    FP32 path's own error on the same inputs); two terms keep logψ within
+    1e-4 and g within 2e-3."""
+    lp32, g32 = _errors(N, alpha, nq._lib.NQ_EVAL_F32)
+    lp3, g3 = _errors(N, alpha, X3)
+    lp2, g2 = _errors(N, alpha, X2)
+    assert lp3 <= max(2 * lp32, 1e-6) and g3 <= max(2 * g32, 1e-6)
+    assert lp2 < 1e-4 and g2 < 2e-3
+
+
+@pytest.mark.parametrize("N,alpha", [(20, 2), (36, 4)])
+def test_theta_tc_estimator_matches_cuda_cores(nqlib, N, alpha):
+    tc, _ = engine(N, alpha, X3, B=256, L=4)
+    f32, _ = engine(N, alpha, nq._lib.NQ_EVAL_F32, B=256, L=4)
+    samples, _ = f32.sample(3)
+    tc.set_samples(samples)
+    m1, loc1, f1 = f32.estimate(want_loc=True, want_force=True)
+    m2, loc2, f2 = tc.estimate(want_loc=True, want_force=True)
+    assert rel(loc2, loc1) < 1e-4
+    assert rel(f2, f1) < 1e-3
+    assert abs(m2.mean_re - m1.mean_re) < 1e-4 * abs(m1.mean_re)
+
+
+def test_theta_tc_vmc_step(nqlib):
+    tc, _ = engine(20, 2, X2, B=512, L=8)
+    f32, _ = engine(20, 2, nq._lib.NQ_EVAL_F32, B=512, L=8)
+    for it in range(3):
+        a = tc.vmc_step(it, 0.01, 0.02)
+        b = f32.vmc_step(it, 0.01, 0.02)
+    assert abs(a.mean_re - b.mean_re) < 5e-3 * abs(b.mean_re)
+    assert rel(tc.get_params(), f32.get_params()) < 1e-2
