@@ -332,6 +332,14 @@ def learned_vs_local():
     made = eng.proposal_get_params()
     sr_ms = float(np.mean(eng.bench_steps(1000, 5, c["eps"], 0.0, L2_FLUSH_BYTES)))
     del eng
+    # the same SR step with the matrix-free conjugate-gradient solve (no S)
+    smp_cg = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], N, burn=c["burn"], seed=c["seed"])
+    cg = nq.BatchedSampler(net, smp_cg, H, nq.SR(eps=c["eps"], algorithm=nq.sr_cg, precision=1e-4),
+                           batch_sz=c["chains"]).engine
+    cg.set_params(params)
+    cg_ms = float(np.mean(cg.bench_steps(1000, 5, c["eps"], 0.0, L2_FLUSH_BYTES)))
+    cg_iters, cg_res = cg.sr_info()
+    del cg
 
     def measure(p_ar, passes):
         s2 = nq.MetropolisSampler(nq.LocalRule(), c["ess_length"], passes, burn=c["ess_burn"], seed=c["seed"] + 1)
@@ -363,7 +371,10 @@ def learned_vs_local():
     bl = max(local, key=lambda r: r["ess_per_s_E"])
     bm = max(mixed, key=lambda r: r["ess_per_s_E"])
     return {"workload": "tfim2d_6x6_h3.04_rbm_alpha4_8192_chains", "sr_ms_per_step": sr_ms,
-            "sr_steps_per_s": 1e3 / sr_ms, "training_wall_s": wall, "energy_per_site_after_sr": m.mean_re / N,
+            "sr_steps_per_s": 1e3 / sr_ms,
+            "matrix_free_cg": {"sr_ms_per_step": cg_ms, "sr_steps_per_s": 1e3 / cg_ms, "iterations": cg_iters,
+                               "relative_residual": cg_res, "tolerance": 1e-4},
+            "training_wall_s": wall, "energy_per_site_after_sr": m.mean_re / N,
             "made_nll_after_each_training": nll, "local": local, "learned_mixture": mixed,
             "best_local_ess_per_s_E": bl["ess_per_s_E"], "best_learned_ess_per_s_E": bm["ess_per_s_E"],
             "learned_over_local_ess_ratio": bm["ess_per_s_E"] / bl["ess_per_s_E"],

@@ -105,8 +105,17 @@ typedef struct {
   int32_t s_precision;     /* nq_s_precision */
   uint32_t quirks;         /* NQ_QUIRK_* bits */
   int32_t sampler_lanes;   /* lanes per Metropolis chain (4, 8, 16, 32); 0 = autotune */
-  int32_t reserved[6];
+  int32_t sr_algorithm;    /* nq_sr_algorithm */
+  int32_t reserved[5];
 } nq_config;
+
+/* SR solver (SR.jl:5-6 SRAlgorithm).  NQ_SR_DIRECT forms S and solves the
+ * shifted system exactly (sr_cholesky); NQ_SR_CG never forms S: conjugate
+ * gradients on the operator v -> conj(O_c) O_cᵀ v / Ns + shift v
+ * (SRIterative.jl with SR_notfull.jl's SrMatrixC), for the reference's
+ * iterative algorithms (sr_cg; sr_minres / sr_qlp / sr_lsq solve the same
+ * system to the same tolerance).  RBM, FP32 evaluation; no P x P storage. */
+typedef enum { NQ_SR_DIRECT = 0, NQ_SR_CG = 1 } nq_sr_algorithm;
 
 /* Statistics of the local estimator (src/utils/stats.jl:1-50). */
 typedef struct {
@@ -204,6 +213,12 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out,
 nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* stats, double* loc_out);
 /* S (nullable out): P x P column-major complex128 (real parameters: float64). */
 nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
+/* Iterative SR settings (NQ_SR_CG): relative residual tolerance |r|/|F|
+ * (SR(precision=...), default 1e-4) and the iteration cap (default 10 P as
+ * SRIterative.jl:99).  nq_sr_info returns [iterations, |r|/|F|] of the last
+ * iterative solve. */
+nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter);
+nq_status nq_sr_info(nq_handle* h, double* out2);
 
 /* ---- precondition!(prec, SR, iter) ----------------------------------------
  * kind: 0 = sr_shift (S_ii += eps), 1 = sr_multiplicative

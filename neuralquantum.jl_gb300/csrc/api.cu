@@ -193,6 +193,7 @@ nq_status stage_force(nq_handle* h) {
 }
 
 nq_status stage_S(nq_handle* h) {
+  if (h->cg) return NQ_OK;          // matrix-free SR: S is never formed
   if (h->ndm) {
     const int sp = h->cfg.s_precision;
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
@@ -236,6 +237,20 @@ nq_status stage_S(nq_handle* h) {
 }
 
 nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
+  if (h->cg) {
+    SrCgArgs a = h->cga;
+    a.eps = eps;
+    a.tol = h->cg_tol;
+    a.maxiter = h->cg_maxiter;
+    a.real_params = h->complex_params ? 0 : 1;
+    if (!h->capturing) CK(cudaEventRecord(h->sev[0], h->st));
+    CKL(launch_sr_cg(a, kind, lam, h->st));
+    ++h->launches;
+    if (!h->capturing) {
+      for (int k = 1; k < 6; ++k) CK(cudaEventRecord(h->sev[k], h->st));
+    }
+    return NQ_OK;
+  }
   SolveBufs sb = h->sb;
   sb.ev = h->capturing ? nullptr : h->sev;
   CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, kSolveRefine, h->st));
@@ -373,6 +388,13 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     return NQ_ERR_UNSUPPORTED;
   }
   if (c.s_precision == NQ_S_F64) { delete h; return NQ_ERR_UNSUPPORTED; }
+  if (c.sr_algorithm != NQ_SR_DIRECT && c.sr_algorithm != NQ_SR_CG) return bad("unknown sr_algorithm");
+  if (c.sr_algorithm == NQ_SR_CG &&
+      (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64 ||
+       !sr_cg_supported(c.n_sites + c.n_hidden + c.n_sites * c.n_hidden))) {
+    delete h;
+    return NQ_ERR_UNSUPPORTED;
+  }
   if ((c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) && !gram_tc_supported()) {
     delete h;
     return NQ_ERR_UNSUPPORTED;
@@ -454,8 +476,33 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->d_stats, 8), "stats");
   step(dalloc(&h->d_chainstats, 3 * (size_t)h->B), "chain stats");
   step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
+  h->cg = c.sr_algorithm == NQ_SR_CG;
   const int rows = 2 * P;
   const int rp = ((rows + 127) / 128) * 128;
+  if (h->cg) {
+    // matrix-free SR: O(P) vectors and per-CTA partials only
+    const int G = sr_cg_grid();
+    SrCgArgs& a = h->cga;
+    a.N = h->N; a.M = h->M; a.P = P; a.Ns = h->Ns; a.hilb = h->hilb;
+    a.samples = h->d_samples; a.g = reinterpret_cast<const float2*>(h->d_g); a.meanO = h->fb.meanO;
+    a.F = h->fb.force;
+    step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
+    step(dalloc(&a.r, 2 * (size_t)P), "cg r");
+    step(dalloc(&a.pv, 2 * (size_t)P), "cg p");
+    step(dalloc(&a.w, 2 * (size_t)P), "cg w");
+    step(dalloc(&a.part, 2 * (size_t)G * P), "cg partials");
+    step(dalloc(&a.tsum, 2 * (size_t)G), "cg tsum");
+    step(dalloc(&a.dots, 4 * (size_t)G), "cg dots");
+    step(dalloc(&a.t, (size_t)h->Ns), "cg t");
+    step(dalloc(&a.shift, (size_t)P), "cg shift");
+    step(cudaMalloc(&a.ctl, sr_cg_ctl_bytes()), "cg ctl");
+    step(dalloc(&a.info, 2), "cg info");
+    step(dalloc(&h->sb.status, 1), "status");
+    step(cudaMallocHost((void**)&h->h_cginfo, 2 * sizeof(double)), "pinned");
+    a.x = h->sb.x;
+    a.status = h->sb.status;
+    h->cg_maxiter = 10 * P;
+  }
   // split-K so that the S stage fills the GPU with ~2 waves of tiles
   {
     const int nt = (rows + 63) / 64;
@@ -464,9 +511,10 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     while (tiles * ks < 2 * 152 && ks < 16 && h->Ns / (ks * 2) >= 256) ks *= 2;
     h->gram_ksplit = ks;
   }
-  step(dalloc(&h->d_G, (size_t)rows * rows), "G");
-  step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
-  if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) {
+  if (!h->cg) step(dalloc(&h->d_G, (size_t)rows * rows), "G");
+  if (!h->cg) step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
+  if (h->cg) {
+  } else if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad);
     cudaFree(h->d_Gpart);
@@ -478,15 +526,17 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
   }
-  step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
-  step(dalloc(&h->sb.W, (size_t)P * P), "W");
-  step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
-  step(dalloc(&h->sb.r, 2 * (size_t)P), "r");
-  step(dalloc(&h->sb.rf, (size_t)P), "rf");
-  step(dalloc(&h->sb.status, 1), "status");
-  step(cudaMalloc(&h->sb.ctl, sweep_ctl_bytes()), "sweep ctl");
-  step(dalloc(&h->sb.work, sweep_work_elems(P)), "sweep work");
-  step(dalloc(&h->sb.yf, (size_t)P), "yf");
+  if (!h->cg) {
+    step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
+    step(dalloc(&h->sb.W, (size_t)P * P), "W");
+    step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
+    step(dalloc(&h->sb.r, 2 * (size_t)P), "r");
+    step(dalloc(&h->sb.rf, (size_t)P), "rf");
+    step(dalloc(&h->sb.status, 1), "status");
+    step(cudaMalloc(&h->sb.ctl, sweep_ctl_bytes()), "sweep ctl");
+    step(dalloc(&h->sb.work, sweep_work_elems(P)), "sweep work");
+    step(dalloc(&h->sb.yf, (size_t)P), "yf");
+  }
   if (h->tc_theta) step(dalloc(&h->d_theta_img, theta_tc_image_elems(h->M, h->theta_terms)), "theta image");
   h->sb.S = h->d_S;
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
@@ -500,7 +550,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     step(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st), "memset");
     // sample buffer starts as the state() fill: all sites at local index 0
     step(cudaMemsetAsync(h->d_samples, 0, sizeof(uint64_t) * h->Ns, h->st), "memset");
-    step(cudaMemsetAsync(h->d_S, 0, 2 * sizeof(double) * P * P, h->st), "memset");
+    if (!h->cg) step(cudaMemsetAsync(h->d_S, 0, 2 * sizeof(double) * P * P, h->st), "memset");
     if (refresh_params(h) != NQ_OK) s = NQ_ERR_CUDA;
     step(cudaStreamSynchronize(h->st), "sync");
   }
@@ -527,6 +577,13 @@ void nq_destroy(nq_handle* h) {
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
   for (void* p : bufs)
     if (p) cudaFree(p);
+  {
+    void* cgb[] = {h->cga.r, h->cga.pv, h->cga.w, h->cga.part, h->cga.tsum, h->cga.dots, h->cga.t, h->cga.shift,
+                   h->cga.ctl, h->cga.info};
+    for (void* p : cgb)
+      if (p) cudaFree(p);
+    if (h->h_cginfo) cudaFreeHost(h->h_cginfo);
+  }
   if (h->h_call) cudaFreeHost(h->h_call);
   if (h->h_stats) cudaFreeHost(h->h_stats);
   if (h->h_acc) cudaFreeHost(h->h_acc);
@@ -712,8 +769,8 @@ nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out, uint
     cudaFree(d_bits);
   }
   CK(cudaStreamSynchronize(h->st));
-  cudaEventElapsedTime(&h->stage_ms[0], h->ev[0], h->ev[1]);
-  cudaEventElapsedTime(&h->stage_ms[6], h->kev[0], h->kev[1]);
+  h->stage_ms[0] = elapsed_ms(h->ev[0], h->ev[1]);
+  h->stage_ms[6] = elapsed_ms(h->kev[0], h->kev[1]);
   return NQ_OK;
 }
 
@@ -802,10 +859,10 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, doub
   CK(cudaEventRecord(h->ev[4], h->st));
   CK(cudaMemcpyAsync(h->h_stats, h->d_stats, 6 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  cudaEventElapsedTime(&h->stage_ms[1], h->ev[1], h->ev[2]);
-  cudaEventElapsedTime(&h->stage_ms[2], h->ev[2], h->ev[3]);
-  cudaEventElapsedTime(&h->stage_ms[3], h->ev[3], h->ev[4]);
-  cudaEventElapsedTime(&h->stage_ms[7], h->kev[2], h->kev[3]);
+  h->stage_ms[1] = elapsed_ms(h->ev[1], h->ev[2]);
+  h->stage_ms[2] = elapsed_ms(h->ev[2], h->ev[3]);
+  h->stage_ms[3] = elapsed_ms(h->ev[3], h->ev[4]);
+  h->stage_ms[7] = elapsed_ms(h->kev[2], h->kev[3]);
   fill_measurement(h, stats);
   const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
   if (loc_out) {
@@ -827,7 +884,26 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, doub
   return NQ_OK;
 }
 
+nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter) {
+  if (!h || !(tol > 0.0) || maxiter < 1) return NQ_ERR_ARG;
+  h->cg_tol = tol;
+  h->cg_maxiter = maxiter;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NQ_OK;
+}
+
+nq_status nq_sr_info(nq_handle* h, double* out2) {
+  if (!h || !out2) return NQ_ERR_ARG;
+  if (!h->cg) return fail(h, NQ_ERR_STATE, "the handle uses the direct SR solve");
+  CK(cudaMemcpyAsync(h->h_cginfo, h->cga.info, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  out2[0] = h->h_cginfo[0];
+  out2[1] = h->h_cginfo[1];
+  return NQ_OK;
+}
+
 nq_status nq_get_sr_matrix(nq_handle* h, double* s_out) {
+  if (h && h->cg) return fail(h, NQ_ERR_STATE, "S is not formed by the matrix-free SR solve (NQ_SR_CG)");
   if (!h || !s_out) return NQ_ERR_ARG;
   std::vector<double> S(2 * (size_t)h->P * h->P);
   CK(cudaMemcpyAsync(S.data(), h->d_S, S.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -849,8 +925,8 @@ nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0, d
   if (s != NQ_OK) return s;
   CK(cudaEventRecord(h->ev[5], h->st));
   if ((s = check_status_word(h)) != NQ_OK) return s;
-  cudaEventElapsedTime(&h->stage_ms[4], h->ev[4], h->ev[5]);
-  for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&h->stage_ms[8 + k], h->sev[k + 1], h->sev[k + 2]);
+  h->stage_ms[4] = elapsed_ms(h->ev[4], h->ev[5]);
+  for (int k = 0; k < 4; ++k) h->stage_ms[8 + k] = elapsed_ms(h->sev[k + 1], h->sev[k + 2]);
   if (dw_out) {
     std::vector<double> x(2 * (size_t)h->P);
     CK(cudaMemcpy(x.data(), h->sb.x, x.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -868,7 +944,7 @@ nq_status nq_update_descent(nq_handle* h, double lr) {
   if (s != NQ_OK) return s;
   CK(cudaEventRecord(h->ev[6], h->st));
   CK(cudaStreamSynchronize(h->st));
-  cudaEventElapsedTime(&h->stage_ms[5], h->ev[5], h->ev[6]);
+  h->stage_ms[5] = elapsed_ms(h->ev[5], h->ev[6]);
   if (h->graph) { /* parameters live on the device; the graph stays valid */ }
   return NQ_OK;
 }
@@ -961,7 +1037,7 @@ nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double e
     CK(cudaEventRecord(evs[2 * i + 1], h->st));
   }
   CK(cudaStreamSynchronize(h->st));
-  for (int i = 0; i < n_steps; ++i) cudaEventElapsedTime(&ms_out[i], evs[2 * i], evs[2 * i + 1]);
+  for (int i = 0; i < n_steps; ++i) ms_out[i] = elapsed_ms(evs[2 * i], evs[2 * i + 1]);
   for (int i = 0; i < 2 * n_steps; ++i) cudaEventDestroy(evs[i]);
   delete[] evs;
   return check_status_word(h);
@@ -1248,7 +1324,8 @@ nq_status nq_batch_create(const nq_config* cfgs, int32_t n, nq_batch** out) {
   *out = nullptr;
   for (int p = 0; p < n; ++p) {
     const nq_config& c = cfgs[p];
-    if (c.network != NQ_NET_RBM || c.eval_precision != NQ_EVAL_F32) return NQ_ERR_UNSUPPORTED;
+    if (c.network != NQ_NET_RBM || c.eval_precision != NQ_EVAL_F32 || c.sr_algorithm != NQ_SR_DIRECT)
+      return NQ_ERR_UNSUPPORTED;
     if (c.activation != cfgs[0].activation || c.hilbert != cfgs[0].hilbert) return NQ_ERR_UNSUPPORTED;
   }
   nq_batch* b = new nq_batch();
@@ -1378,7 +1455,7 @@ nq_status nq_batch_bench_steps(nq_batch* b, uint64_t call0, int32_t n_steps, dou
     BCK(cudaEventRecord(ev[2 * i + 1], b->st));
   }
   BCK(cudaStreamSynchronize(b->st));
-  for (int i = 0; i < n_steps; ++i) cudaEventElapsedTime(&ms_out[i], ev[2 * i], ev[2 * i + 1]);
+  for (int i = 0; i < n_steps; ++i) ms_out[i] = elapsed_ms(ev[2 * i], ev[2 * i + 1]);
   for (auto& e : ev) cudaEventDestroy(e);
   return NQ_OK;
 }

@@ -77,10 +77,27 @@ struct nq_handle {
   void* d_flush = nullptr;
   size_t flush_bytes = 0;
   MadeState* made = nullptr;       // learned proposal, null until nq_proposal_init
+  bool cg = false;                 // NQ_SR_CG: matrix-free iterative SR, no S
+  SrCgArgs cga;                    // device work of the iterative solve
+  double cg_tol = 1e-4;
+  int cg_maxiter = 0;
+  double* h_cginfo = nullptr;      // pinned [2]
   bool tc_theta = false;           // NQ_EVAL_TC_BF16X2 / X3: θ = Wσ + b on tcgen05
   int theta_terms = 2;             // BF16 terms of W (2 or 3)
   __nv_bfloat16* d_theta_img = nullptr;   // packed BF16 hi/lo image of W
 };
+
+// Device time between two events; 0 when one of them was not recorded in the
+// last call (a stage that did not run), without leaving the error behind for
+// the next cudaGetLastError.
+inline float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.f;
+  }
+  return ms;
+}
 
 inline nq_status fail(nq_handle* h, nq_status code, const char* fmt, ...) {
   char buf[512];

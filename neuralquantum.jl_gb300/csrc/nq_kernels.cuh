@@ -168,6 +168,36 @@ struct SweepJob {
 cudaError_t launch_spd_inverse_batch(const SweepJob* jobs, const int* cta_start, int np, int total_ctas,
                                      void* ctl_base, size_t ctl_bytes, cudaStream_t st);
 cudaError_t launch_herm_fill(float2* W, int P, cudaStream_t st);
+// Matrix-free conjugate-gradient solve of (S + shift) x = F for the RBM,
+// S = conj(O_c) O_cᵀ / Ns applied from (σ, g, ⟨O⟩) without forming S; one
+// cooperative launch (sr_cg_grid() CTAs).  shift_p = eps (kind 0),
+// lam * S_pp (kind 1) or 0 (kind 2).  info = [iterations, |r| / |F|].
+struct SrCgArgs {
+  int N = 0, M = 0, P = 0, Ns = 0, hilb = 0, real_params = 0;
+  const uint64_t* samples = nullptr;
+  const float2* g = nullptr;       // [M][Ns] f'(θ)
+  const double* meanO = nullptr;   // [P] complex
+  const double* F = nullptr;       // [P] complex right-hand side
+  double eps = 0.0, tol = 1e-4;
+  int maxiter = 1000;
+  double* x = nullptr;             // [P] complex solution
+  double* r = nullptr;             // [P] complex work vectors
+  double* pv = nullptr;
+  double* w = nullptr;
+  double* part = nullptr;          // [grid][P] complex adjoint partials
+  double* tsum = nullptr;          // [grid] complex
+  double* dots = nullptr;          // [grid][4]
+  float2* t = nullptr;             // [Ns]
+  double* shift = nullptr;         // [P]
+  void* ctl = nullptr;             // sr_cg_ctl_bytes()
+  int* status = nullptr;
+  double* info = nullptr;          // [2]
+};
+int sr_cg_grid();
+size_t sr_cg_ctl_bytes();
+bool sr_cg_supported(int P);
+cudaError_t launch_sr_cg(const SrCgArgs& args, int kind, double lam, cudaStream_t st);
+
 // y = -W x for the full Hermitian W
 cudaError_t launch_herm_gemv_neg(const float2* W, int P, const float2* x, float2* y, cudaStream_t st);
 

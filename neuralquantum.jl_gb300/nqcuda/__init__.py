@@ -15,5 +15,5 @@ from .samplers import MetropolisSampler, LocalRule  # noqa: F401
 from .stats import Measurement  # noqa: F401
 from .iterative import (BatchedSampler, BatchedObsKetSampler, add_observable_, SR, Descent, sample_,  # noqa: F401
                         precondition_, update_,  # noqa: F401
-                        sr_shift, sr_multiplicative, sr_none, sr_cholesky)
+                        sr_shift, sr_multiplicative, sr_none, sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq)
 from .engine import Engine, ProblemBatch  # noqa: F401

@@ -18,7 +18,8 @@ INCLUDE = os.path.join(_REPO, "include")
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
-           "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu"]
+           "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu",
+           "srcg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -32,6 +33,7 @@ NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3
 NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64, NQ_EVAL_TC_BF16X3 = 0, 1, 2, 3
 NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64 = 0, 1, 2, 3
+NQ_SR_DIRECT, NQ_SR_CG = 0, 1
 NQ_QUIRK_STALE_LAST_SLOT = 0x1
 
 
@@ -43,7 +45,8 @@ class NqConfig(ctypes.Structure):
                 ("burn", ctypes.c_int32), ("passes", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("eval_precision", ctypes.c_int32),
                 ("s_precision", ctypes.c_int32), ("quirks", ctypes.c_uint32),
-                ("sampler_lanes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("sampler_lanes", ctypes.c_int32), ("sr_algorithm", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 class NqMeasurement(ctypes.Structure):
@@ -84,6 +87,8 @@ EXPORTS = {
     "nq_estimate": (ctypes.c_int, [ctypes.c_void_p, _P(NqMeasurement), ctypes.c_void_p,
                                    ctypes.c_void_p]),
     "nq_observable": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable), _P(NqMeasurement), ctypes.c_void_p]),
+    "nq_set_sr_tolerance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32]),
+    "nq_sr_info": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double)]),
     "nq_get_sr_matrix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_precondition": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,

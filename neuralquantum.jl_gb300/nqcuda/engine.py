@@ -9,7 +9,7 @@ from .networks import RBM, NDM, af_logcosh
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
-                s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0):
+                s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT):
     """nq_config of one problem (include/nqcuda.h)."""
     cfg = _lib.NqConfig()
     ph = physical(hilb)
@@ -35,16 +35,17 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
     cfg.s_precision = s_precision
     cfg.quirks = quirks
     cfg.sampler_lanes = sampler_lanes
+    cfg.sr_algorithm = sr_algorithm
     return cfg
 
 
 class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
                  eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
-                 sampler_lanes=0, _handle=None, _owner=None):
+                 sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT, _handle=None, _owner=None):
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
-                          s_precision, quirks, sampler_lanes)
+                          s_precision, quirks, sampler_lanes, sr_algorithm)
         self.complex_params = isinstance(net, RBM)
         self.cfg = cfg
         self.lib = L
@@ -150,6 +151,15 @@ class Engine:
         self._check(self.lib.nq_observable(self.h, ctypes.byref(st), ctypes.byref(m),
                                            loc.ctypes.data if loc is not None else None))
         return m, loc
+
+    def set_sr_tolerance(self, tol, maxiter):
+        self._check(self.lib.nq_set_sr_tolerance(self.h, float(tol), int(maxiter)))
+
+    def sr_info(self):
+        """[iterations, |r|/|F|] of the last matrix-free SR solve."""
+        v = (ctypes.c_double * 2)()
+        self._check(self.lib.nq_sr_info(self.h, v))
+        return int(v[0]), float(v[1])
 
     def sr_matrix(self):
         S = np.empty((self.P, self.P), np.complex128 if self.complex_params else np.float64, order="F")

@@ -21,20 +21,28 @@ from .hilbert import SuperOpSpace
 from .stats import Measurement
 
 sr_shift, sr_multiplicative, sr_none = 0, 1, 2
-sr_cholesky = "sr_cholesky"
+sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq = "sr_cholesky", "sr_cg", "sr_minres", "sr_qlp", "sr_lsq"
+_ITERATIVE = (sr_cg, sr_minres, sr_qlp, sr_lsq)
 
 
 class SR:
-    """``SR(T; ϵ=0.001, precondition_type=sr_shift, algorithm=sr_cholesky,
-    λ0=100, b=0.95, λmin=1e-4)``.  Only the direct Cholesky algorithm is
-    provided by the engine."""
+    """``SR(T; ϵ=0.001, precision=1e-4, precondition_type=sr_shift,
+    algorithm=sr_cholesky, λ0=100, b=0.95, λmin=1e-4)`` (SR.jl:41-50).
+    sr_cholesky forms S and solves directly; the iterative algorithms run the
+    engine's matrix-free conjugate-gradient solve of the same shifted system
+    to the relative residual ``precision``."""
 
     def __init__(self, eps=0.001, precondition_type=sr_shift, algorithm=sr_cholesky,
-                 lam0=100.0, b=0.95, lam_min=1e-4):
-        if algorithm != sr_cholesky:
-            raise NotImplementedError("the engine implements the sr_cholesky algorithm")
+                 lam0=100.0, b=0.95, lam_min=1e-4, precision=1e-4):
+        if algorithm != sr_cholesky and algorithm not in _ITERATIVE:
+            raise NotImplementedError(f"unknown SR algorithm {algorithm}")
         self.eps, self.precondition_type = float(eps), precondition_type
         self.lam0, self.b, self.lam_min = float(lam0), float(b), float(lam_min)
+        self.algorithm, self.precision = algorithm, float(precision)
+
+    @property
+    def iterative(self):
+        return self.algorithm in _ITERATIVE
 
 
 class Descent:
@@ -68,8 +76,12 @@ class BatchedSampler:
         self.liouvillian = isinstance(prob, KLocalLiouvillian)
         hilb = prob.hilb if not self.liouvillian else prob.hilb
         quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
+        sr_alg = _lib.NQ_SR_CG if self.algo.iterative else _lib.NQ_SR_DIRECT
         self.engine = Engine(net, hilb, batch_sz, sampler.chain_length, sampler.burn_length,
-                             sampler.passes, sampler.seed, eval_precision, s_precision, quirks)
+                             sampler.passes, sampler.seed, eval_precision, s_precision, quirks,
+                             sr_algorithm=sr_alg)
+        if self.algo.iterative:
+            self.engine.set_sr_tolerance(self.algo.precision, 10 * self.engine.P)
         self.engine.set_params(net.flat())
         self.engine.set_operator(op_table(prob))
         self.calls = 0
