@@ -139,7 +139,7 @@ def effective_samples_per_s(loc, sample_ms):
     return ns / tau / (sample_ms / 1e3), tau
 
 
-def run_gb300(args):
+def run_gb300(args, barrier=None):
     import nqcuda as nq
     nq.build()
     peaks = {}
@@ -154,8 +154,12 @@ def run_gb300(args):
     for i in range(args.warmup):
         eng.vmc_step(i, w["eps"], w["lr"])
     launches0 = eng.kernel_launches()
-    with ClockSampler() as clk:
-        ms = eng.bench_steps(args.warmup, args.steps, w["eps"], w["lr"], L2_FLUSH_BYTES)
+    if barrier:
+        barrier()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms = eng.bench_steps(args.warmup, args.steps, w["eps"], w["lr"], L2_FLUSH_BYTES)   # synchronises
+    if barrier:
+        barrier()
     launches = eng.kernel_launches() - launches0 - eng_graph_kernels(eng)
     total_ms = float(np.sum(ms))
     ms_step = total_ms / args.steps
@@ -408,6 +412,21 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "SR steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def aggregate_replicas(line, world):
+    """N independent replicas (one per GPU, "scaling": "weak"): the whole-job
+    throughput is N steps per slowest rank's step time, for the device-timed
+    value and for e2e.  Collective over the default process group."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([line["ms_per_step"], -line["e2e"]["value"]], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    line["ms_per_step"] = float(t[0])
+    line["value"] = world * 1e3 / line["ms_per_step"]
+    line["e2e"]["value"] = world * float(-t[1])
+    line["n_gpus"] = world
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,25 +443,25 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         if rank != 0:
             return
         print(json.dumps(run_reference(args)))
         return
-    line = run_gb300(args)
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    barrier = None
     if world > 1:
-        # independent replicas, one per GPU: whole-job throughput is the sum,
-        # limited by the slowest rank (max step time over ranks)
+        # one replica per GPU: the library sees only this rank's device
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", str(rank))
         import torch.distributed as dist
         dist.init_process_group("gloo")
-        t = np.array([line["ms_per_step"]])
-        import torch
-        tt = torch.tensor(t)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        line["ms_per_step"] = float(tt[0])
-        line["value"] = world * 1e3 / line["ms_per_step"]
-        line["n_gpus"] = world
+        barrier = dist.barrier
+        if rank != 0:
+            args.no_cpu_baseline = args.no_learned = args.no_batch = True
+    line = run_gb300(args, barrier)
+    if world > 1:
+        import torch.distributed as dist
+        aggregate_replicas(line, world)
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line))

@@ -249,7 +249,8 @@ nq_status nq_stage_times(nq_handle* h, float* ms12);
 nq_status nq_bench_steps(nq_handle* h, uint64_t call0, int32_t n_steps, double eps, double lr,
                          int64_t flush_bytes, float* ms_out);
 /* Autotuned launch choices of this handle: [lanes per Metropolis chain,
- * split-K of the S accumulation, reserved].  Tunes on first use. */
+ * split-K of the S accumulation, threads per sampler block].  Tunes on first
+ * use. */
 nq_status nq_tuning(nq_handle* h, int32_t* out, int32_t n);
 /* Number of kernel launches issued by this handle since creation. */
 int64_t nq_kernel_launches(const nq_handle* h);

@@ -59,48 +59,63 @@ nq_status refresh_params(nq_handle* h) {
 // per (N, M, B, activation, Hilbert space, precision) for the process.
 // ---------------------------------------------------------------------------
 static std::mutex g_tune_mu;
-static std::map<std::tuple<int, int, int, int, int, int>, int> g_tune_cache;
+static std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
 
+// Lanes per chain and threads per block of the Metropolis sampler: every
+// candidate runs a shortened schedule (up to 24 sweeps, one record) four
+// times and the fastest of the last three counts.  Smaller blocks spread the
+// chains more evenly over the SMs when there are few of them.
 nq_status ensure_tuned(nq_handle* h) {
-  if (h->sampler_lanes) return NQ_OK;
+  if (h->sampler_lanes && h->sampler_block) return NQ_OK;
   const int sN = h->ndm ? h->N2 : h->N, sM = h->ndm ? h->Ms : h->M;
   const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb, (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
-    if (it != g_tune_cache.end()) { h->sampler_lanes = it->second; return NQ_OK; }
+    if (it != g_tune_cache.end()) {
+      if (!h->sampler_lanes) h->sampler_lanes = it->second.first;
+      h->sampler_block = it->second.second;
+      return NQ_OK;
+    }
   }
   int cand[4];
-  const int nc = rbm_sampler_valid_lanes(sM, cand, 4);
+  int nc = rbm_sampler_valid_lanes(sM, cand, 4);
   if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", sM);
+  if (h->sampler_lanes) { cand[0] = h->sampler_lanes; nc = 1; }     // fixed by the caller
+  const int blocks[3] = {64, 128, 256};
   uint64_t* scratch = nullptr;
   CK(cudaMalloc(&scratch, sizeof(uint64_t) * (size_t)h->B * 2));
   SamplerRun run;
   run.B = h->B; run.L = 1; run.burn = std::min(24, h->cfg.burn + h->L); run.passes = h->passes;
   run.n_record = 1; run.k0 = 0x1234u; run.k1 = 0x5678u; run.call = 0xFFFFFFFFu;
   run.samples = scratch; run.accepted = h->d_accepted;
-  int best = cand[0];
+  int best = cand[0], best_block = 256;
   float best_ms = 1e30f;
   for (int c = 0; c < nc; ++c) {
-    float best_c = 1e30f;
-    for (int rep = 0; rep < 4; ++rep) {      // first launch warms up; fastest of the other three
-      float ms = 0.f;
-      CK(cudaEventRecord(h->kev[0], h->st));
-      cudaError_t e = h->f64 ? launch_rbm_sampler<double>(rbm_dev<double>(h), run, cand[c], h->st)
-                             : launch_rbm_sampler<float>(rbm_dev<float>(h), run, cand[c], h->st);
-      ++h->launches;
-      if (e != cudaSuccess) { cudaFree(scratch); return fail(h, NQ_ERR_CUDA, "autotune: %s", cudaGetErrorString(e)); }
-      CK(cudaEventRecord(h->kev[1], h->st));
-      CK(cudaEventSynchronize(h->kev[1]));
-      CK(cudaEventElapsedTime(&ms, h->kev[0], h->kev[1]));
-      if (rep > 0) best_c = std::min(best_c, ms);
+    for (int bb = 0; bb < 3; ++bb) {
+      if (blocks[bb] < cand[c]) continue;
+      run.block = blocks[bb];
+      float best_c = 1e30f;
+      for (int rep = 0; rep < 4; ++rep) {
+        float ms = 0.f;
+        CK(cudaEventRecord(h->kev[0], h->st));
+        cudaError_t e = h->f64 ? launch_rbm_sampler<double>(rbm_dev<double>(h), run, cand[c], h->st)
+                               : launch_rbm_sampler<float>(rbm_dev<float>(h), run, cand[c], h->st);
+        ++h->launches;
+        if (e != cudaSuccess) { cudaFree(scratch); return fail(h, NQ_ERR_CUDA, "autotune: %s", cudaGetErrorString(e)); }
+        CK(cudaEventRecord(h->kev[1], h->st));
+        CK(cudaEventSynchronize(h->kev[1]));
+        CK(cudaEventElapsedTime(&ms, h->kev[0], h->kev[1]));
+        if (rep > 0) best_c = std::min(best_c, ms);
+      }
+      if (best_c < best_ms) { best_ms = best_c; best = cand[c]; best_block = blocks[bb]; }
     }
-    if (best_c < best_ms) { best_ms = best_c; best = cand[c]; }
   }
   cudaFree(scratch);
   h->sampler_lanes = best;
+  h->sampler_block = best_block;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune_cache[key] = best;
+  g_tune_cache[key] = std::make_pair(best, best_block);
   return NQ_OK;
 }
 
@@ -116,6 +131,7 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
   run.samples = h->d_samples;
   run.accepted = h->d_accepted;
   run.accept_bits = accept_bits_dev;
+  run.block = h->sampler_block ? h->sampler_block : 256;
   CK(cudaMemsetAsync(h->d_accepted, 0, sizeof(unsigned long long), h->st));
   if (!h->capturing) CK(cudaEventRecord(h->kev[0], h->st));
   bool mixed = false;
@@ -1001,7 +1017,7 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
 nq_status nq_tuning(nq_handle* h, int32_t* out, int32_t n) {
   if (!h || !out || n < 1) return NQ_ERR_ARG;
   if (nq_status ts = ensure_tuned(h)) return ts;
-  const int32_t v[3] = {h->sampler_lanes, h->gram_ksplit, 0};
+  const int32_t v[3] = {h->sampler_lanes, h->gram_ksplit, h->sampler_block};
   for (int i = 0; i < n && i < 3; ++i) out[i] = v[i];
   return NQ_OK;
 }

@@ -74,6 +74,7 @@ struct nq_handle {
   float stage_ms[12] = {};
   bool capturing = false;
   int sampler_lanes = 0;           // lanes per chain chosen by the autotuner (0 = not tuned)
+  int sampler_block = 0;           // threads per sampler block chosen by the autotuner
   void* d_flush = nullptr;
   size_t flush_bytes = 0;
   MadeState* made = nullptr;       // learned proposal, null until nq_proposal_init

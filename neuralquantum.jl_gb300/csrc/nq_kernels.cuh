@@ -49,6 +49,7 @@ struct SamplerRun {
   uint64_t* samples = nullptr;                 // [L][B]
   unsigned long long* accepted = nullptr;      // scalar counter
   unsigned char* accept_bits = nullptr;        // nullable [steps][B]
+  int block = 256;                             // threads per block (64, 128 or 256)
 };
 // G = lanes per chain (4, 8, 16 or 32); rbm_sampler_valid_lanes lists the
 // values instantiated for M hidden units (used by the autotuner).

@@ -22,7 +22,13 @@ namespace {
 template <typename R> NQ_D R fast_log2(R x) { return log2(x); }
 template <> NQ_D float fast_log2<float>(float x) { return __log2f(x); }
 template <typename R> NQ_D R fast_rcp(R x) { return R(1) / x; }
-template <> NQ_D float fast_rcp<float>(float x) { return __frcp_rn(x); }
+template <> NQ_D float fast_rcp<float>(float x) { return __fdividef(1.0f, x); }
+
+// two complex table entries of one (site, hidden unit) loaded together:
+// {t0, t1} for the ratio, {t2, W} for an accepted flip
+template <typename R> struct alignas(4 * sizeof(R)) cpx_pair {
+  cpx<R> a, b;
+};
 
 // One block of the sampler: chains (blk * blockDim + tid) / G of the problem
 // described by (net, run).  Shared by the single-problem kernel and the
@@ -31,17 +37,18 @@ template <typename R, int G, int HPL, int ACT>
 NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = net.N, M = net.M, n_half = net.n_half;
-  cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
-  cpx<R>* s_t1 = s_t0 + N * M;
-  cpx<R>* s_t2 = s_t1 + N * M;
-  cpx<R>* s_w = s_t2 + N * M;                          // W[h, i] at i*M + h
-  R* s_are = reinterpret_cast<R*>(s_w + N * M);      // 2 Re a_i log2(e)
+  cpx_pair<R>* s_t01 = reinterpret_cast<cpx_pair<R>*>(smem_raw);   // {t0, t1} at i*M + h
+  cpx_pair<R>* s_t2w = s_t01 + N * M;                             // {t2, W[h, i]} at i*M + h
+  R* s_are = reinterpret_cast<R*>(s_t2w + N * M);                 // 2 Re a_i log2(e)
   for (int k = threadIdx.x; k < N * M; k += blockDim.x) {
-    s_t0[k] = net.t0[k];
-    s_t1[k] = net.t1[k];
-    if (ACT == ACT_LOGCOSH) s_t2[k] = net.t2[k];
     const int i = k / M, h = k % M;
-    s_w[k] = net.W[h + M * i];
+    cpx_pair<R> p01, p2w;
+    p01.a = net.t0[k];
+    p01.b = net.t1[k];
+    p2w.a = ACT == ACT_LOGCOSH ? net.t2[k] : mk(R(0), R(0));
+    p2w.b = net.W[h + M * i];
+    s_t01[k] = p01;
+    s_t2w[k] = p2w;
   }
   for (int k = threadIdx.x; k < N; k += blockDim.x) s_are[k] = R(2.8853900817779268) * net.a[k].x;
   __syncthreads();
@@ -73,7 +80,7 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
       cpx<R> t = net.b[h];
       for (int j = 0; j < N; ++j) {
         const R v = site_value<R>(bits, j, hilb);
-        const cpx<R> w = s_w[j * M + h];
+        const cpx<R> w = s_t2w[j * M + h].b;
         t.x += w.x * v;
         t.y += w.y * v;
       }
@@ -108,13 +115,14 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
       for (int k = 0; k < HPL; ++k) {
         const int h = lane + G * k;
         if (h < M) {
+          const cpx_pair<R> tt = s_t01[i * M + h];
           cpx<R> rr;
           if (ACT == ACT_LOGCOSH) {
-            cpx<R> c1 = s_t1[i * M + h];
+            cpx<R> c1 = tt.b;
             if (!pos) c1 = mk(-c1.x, -c1.y);
-            rr = cfma(g[k], c1, s_t0[i * M + h]);
+            rr = cfma(g[k], c1, tt.a);
           } else {
-            const cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
+            const cpx<R> bb = pos ? tt.a : tt.b;
             rr = cfma(g[k], bb, mk(R(1), R(0)));
           }
           if (h < n_half) prod_half *= abs2c(rr);
@@ -132,17 +140,19 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
         for (int k = 0; k < HPL; ++k) {
           const int h = lane + G * k;
           if (h < M) {
-            const cpx<R> w = s_w[i * M + h];
+            const cpx_pair<R> tw = s_t2w[i * M + h];
+            const cpx<R> w = tw.b;
             th[k].x += w.x * dv;
             th[k].y += w.y * dv;
             cpx<R> num, den;
             if (ACT == ACT_LOGCOSH) {
-              cpx<R> tau = s_t2[i * M + h];
+              cpx<R> tau = tw.a;
               if (!pos) tau = mk(-tau.x, -tau.y);
               num = g[k] + tau;
               den = cfma(g[k], tau, mk(R(1), R(0)));
             } else {
-              const cpx<R> bb = pos ? s_t0[i * M + h] : s_t1[i * M + h];
+              const cpx_pair<R> tt = s_t01[i * M + h];
+              const cpx<R> bb = pos ? tt.a : tt.b;
               num = g[k] * mk(R(1) + bb.x, bb.y);
               den = cfma(g[k], bb, mk(R(1), R(0)));
             }
@@ -190,7 +200,7 @@ rbm_sampler_batch_kernel(const SamplerJob<R>* __restrict__ jobs, const int* __re
 
 template <typename R, int G, int HPL, int ACT>
 static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
-  const int threads = 256;
+  const int threads = run.block;
   const int chains_per_block = threads / G;
   const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
   size_t smem = (size_t)4 * net.N * net.M * sizeof(cpx<R>) + net.N * sizeof(R);

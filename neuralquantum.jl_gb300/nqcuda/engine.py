@@ -192,10 +192,11 @@ class Engine:
         return list(a)
 
     def tuning(self):
-        """Autotuned choices: {'sampler_lanes': G, 'gram_ksplit': k}."""
+        """Autotuned choices: lanes per chain and threads per block of the
+        sampler, split-K of the S accumulation."""
         a = (ctypes.c_int32 * 3)()
         self._check(self.lib.nq_tuning(self.h, a, 3))
-        return {"sampler_lanes": a[0], "gram_ksplit": a[1]}
+        return {"sampler_lanes": a[0], "gram_ksplit": a[1], "sampler_block": a[2]}
 
     def kernel_launches(self):
         return int(self.lib.nq_kernel_launches(self.h))
