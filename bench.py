@@ -219,6 +219,8 @@ def run_gb300(args, barrier=None):
     }
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_batch:
         line["many_problems"] = batched_vs_sequential()
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_precision:
+        line["precision_modes"] = precision_modes()
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_learned:
         line["learned_proposal"] = learned_vs_local()
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
@@ -249,6 +251,67 @@ def _tfim2d(nq, Lx, h, J):
             H = H + J * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, (x + 1) % Lx + Lx * y + 1)
             H = H + J * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, x + Lx * ((y + 1) % Lx) + 1)
     return hilb, H
+
+
+PRECISION = dict(N=12, alpha=2, beta=2, g=1.0, V=2.0, gamma=1.0, chains=16384, chain_length=8, burn=100,
+                 eps=0.01, lr=0.01, sr_steps=20, seed=0x4E51)
+
+
+def _dissipative(nq, hilb, N, g, V, gamma):
+    H = nq.LocalOperator(hilb)
+    Ls = []
+    for i in range(1, N + 1):
+        H = H + (g / 2) * nq.sigmax(hilb, i)
+        Ls.append(float(np.sqrt(gamma)) * nq.sigmam(hilb, i))
+    for i in range(1, N):
+        H = H + (V / 4) * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i + 1)
+    return nq.liouvillian(H, Ls)
+
+
+def precision_modes():
+    """Dissipative Ising chain N = 12 (open; g = 1, V = 2, γ = 1), NDM α = β = 2
+    (P = 1248 real parameters), 16384 chains x 8 samples: on the same samples,
+    the relative error of L_loc, F, S and Δw of the precision mode (FP32
+    evaluation, TF32 S on tcgen05, FP32 inverse with FP64 refinement) against
+    FP64 evaluation with FP32 S; then 20 SR steps of TF32 S vs FP32 S from the
+    same start, comparing the cost ⟨|Lρ|²⟩/⟨ρ²⟩."""
+    import nqcuda as nq
+    c = PRECISION
+    N = c["N"]
+    hilb = nq.HomogeneousSpin(N)
+    lv = _dissipative(nq, hilb, N, c["g"], c["V"], c["gamma"])
+
+    def engine(prec, sp):
+        net = nq.NDM(np.float64, N, c["alpha"], c["beta"], nq.af_softplus)
+        nq.init_random_pars_(net, sigma=1e-4, rng=np.random.default_rng(c["seed"]))
+        smp = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], 2 * N, burn=c["burn"], seed=c["seed"])
+        return nq.BatchedSampler(net, smp, lv, nq.SR(eps=c["eps"]), batch_sz=c["chains"], eval_precision=prec,
+                                 s_precision=sp).engine
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(1e-300, np.max(np.abs(b))))
+
+    ref = engine(nq._lib.NQ_EVAL_F64, nq._lib.NQ_S_F32)
+    fast = engine(nq._lib.NQ_EVAL_F32, nq._lib.NQ_S_TF32)
+    samples, _ = ref.sample(3)
+    fast.set_samples(samples)
+    out = {"workload": "ndm_dissipative_ising_N12_alpha2_beta2_16384x8", "n_params": ref.P}
+    m0, l0, f0 = ref.estimate(want_loc=True, want_force=True)
+    m1, l1, f1 = fast.estimate(want_loc=True, want_force=True)
+    s0, s1 = ref.sr_matrix(), fast.sr_matrix()
+    d0, d1 = ref.precondition(0, c["eps"]), fast.precondition(0, c["eps"])
+    out["relative_error_vs_fp64_eval"] = {"L_loc": rel(l1, l0), "cost": abs(m1.mean_re - m0.mean_re) / abs(m0.mean_re),
+                                          "F": rel(f1, f0), "S": rel(s1, s0), "dw": rel(d1, d0)}
+    del ref, fast
+    curves = {}
+    for name, sp in (("tf32", nq._lib.NQ_S_TF32), ("fp32", nq._lib.NQ_S_F32)):
+        e = engine(nq._lib.NQ_EVAL_F32, sp)
+        curves[name] = [e.vmc_step(it, c["eps"], c["lr"]).mean_re for it in range(c["sr_steps"])]
+        del e
+    out["cost_curve_tf32"] = curves["tf32"]
+    out["cost_curve_fp32"] = curves["fp32"]
+    out["final_cost_relative_difference"] = abs(curves["tf32"][-1] - curves["fp32"][-1]) / abs(curves["fp32"][-1])
+    return out
 
 
 BATCH = dict(n_problems=64, sizes=(3, 4, 5), h_range=(2.0, 4.0), J=1.0, alpha=1, chains=1024, chain_length=20,
@@ -437,6 +500,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-problem batched vs sequential comparison")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the precision-mode comparison (NDM N=12)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-proposal vs local Metropolis comparison (6x6 TFIM)")
     args = ap.parse_args()
@@ -457,7 +522,7 @@ def main():
         dist.init_process_group("gloo")
         barrier = dist.barrier
         if rank != 0:
-            args.no_cpu_baseline = args.no_learned = args.no_batch = True
+            args.no_cpu_baseline = args.no_learned = args.no_batch = args.no_precision = True
     line = run_gb300(args, barrier)
     if world > 1:
         import torch.distributed as dist

@@ -340,7 +340,10 @@ cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2*
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_coop_kernel, 256, 0);
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorCooperativeLaunchTooLarge;
-    grid = sms;     // one CTA per SM (co-residency guaranteed by the cooperative launch)
+    // two CTAs per SM where they fit: phase B has ~nblk^2/2 tiles per step, and
+    // a second resident CTA halves the tiles per CTA (co-residency of every
+    // CTA is guaranteed by the cooperative launch)
+    grid = sms * (per >= 2 ? 2 : 1);
   }
   cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(SweepCtl), st);
   if (e != cudaSuccess) return e;
