@@ -67,10 +67,11 @@ __global__ void __launch_bounds__(256) made_logq_kernel(MadeDev m, const uint64_
 // one warp per proposal (chain, slot), chain-major: index chain*slots + slot
 template <int UPL>
 __global__ void __launch_bounds__(256)
-made_sample_kernel(MadeDev m, int n_chains, int slots, uint32_t call, uint32_t k0, uint32_t k1,
-                   uint64_t* __restrict__ xout, float* __restrict__ lqout) {
+made_sample_kernel(MadeDev m, int n_chains, int slots, uint32_t call, const uint32_t* call_ptr, uint32_t k0,
+                   uint32_t k1, uint64_t* __restrict__ xout, float* __restrict__ lqout) {
   const long gid = (long)blockIdx.x * 8 + (threadIdx.x >> 5);
   if (gid >= (long)n_chains * slots) return;
+  if (call_ptr) call = *call_ptr;
   const uint32_t chain = (uint32_t)(gid / slots), slot = (uint32_t)(gid % slots);
   uint64_t x = 0;
   const float lq = made::walk<UPL, true>(m, x, slot, chain, call, k0, k1);
@@ -249,11 +250,12 @@ cudaError_t launch_made_logq(const MadeDev& m, const uint64_t* x, int n, float* 
 }
 
 cudaError_t launch_made_sample(const MadeDev& m, int n_chains, int slots, uint32_t call, uint32_t k0, uint32_t k1,
-                               uint64_t* xout, float* lqout, cudaStream_t st) {
+                               uint64_t* xout, float* lqout, cudaStream_t st, const uint32_t* call_ptr) {
   if (m.H != 128 || m.N < 2 || m.N > 64) return cudaErrorInvalidValue;
   const long n = (long)n_chains * slots;
   if (n <= 0) return cudaSuccess;
-  made_sample_kernel<4><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(m, n_chains, slots, call, k0, k1, xout, lqout);
+  made_sample_kernel<4><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(m, n_chains, slots, call, call_ptr, k0, k1, xout,
+                                                                  lqout);
   return cudaGetLastError();
 }
 

@@ -35,9 +35,10 @@ cudaError_t launch_made_mask(int N, int H, float* mask, cudaStream_t st);
 cudaError_t launch_made_apply_mask(int n_params, const float* mask, float* master, cudaStream_t st);
 cudaError_t launch_made_pack(const MadeDev& m, const float* master, cudaStream_t st);
 cudaError_t launch_made_logq(const MadeDev& m, const uint64_t* x, int n, float* out, cudaStream_t st);
-// proposals for `slots` AR steps of every chain, Philox stream TAG_AR
+// proposals for `slots` AR steps of every chain, Philox stream TAG_AR; the
+// call index is read from call_ptr when it is given (graph replays)
 cudaError_t launch_made_sample(const MadeDev& m, int n_chains, int slots, uint32_t call, uint32_t k0, uint32_t k1,
-                               uint64_t* xout, float* lqout, cudaStream_t st);
+                               uint64_t* xout, float* lqout, cudaStream_t st, const uint32_t* call_ptr = nullptr);
 // samples per block of the gradient kernel; partial needs ceil(n/chunk)*n_params floats
 int made_grad_chunk();
 // masked gradient of the mean NLL of x[0..n) into grad (n_params floats)
@@ -51,6 +52,12 @@ struct MixParams {
   MadeDev made;
   unsigned long long thr = 0;              // AR move iff TAG_MIX word < thr (= ceil(p_ar 2^32))
   unsigned long long* ar_stats = nullptr;  // [2]: AR proposals, accepted AR proposals (added to)
+  // proposals drawn ahead of the chain kernel (launch_made_sample with the same
+  // call and key): slot k of chain c at c * pre_slots + k; slots past
+  // pre_slots are drawn inside the chain kernel
+  const uint64_t* pre_x = nullptr;
+  const float* pre_lq = nullptr;
+  int pre_slots = 0;
 };
 bool mix_sampler_supported(int N, int M, int n_half, int H);
 cudaError_t launch_rbm_mix_sampler(const RbmDev<float>& net, const SamplerRun& run, const MixParams& mix,

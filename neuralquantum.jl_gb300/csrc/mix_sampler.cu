@@ -6,7 +6,9 @@
 //   local: accept iff u < |ψ(x')/ψ(x)|²               (symmetric proposal)
 //   AR   : accept iff u < |ψ(x')|² q(x) / (|ψ(x)|² q(x'))
 // u is the TAG_MH uniform of the step in both cases.  The chain's k-th AR step
-// uses proposal slot k (uniforms TAG_AR word k*N + i).  log q(x) of the current
+// uses proposal slot k (uniforms TAG_AR word k*N + i); the first pre_slots
+// slots of every chain are drawn ahead by the proposal kernel (they do not
+// depend on the chain), later ones inline.  log q(x) of the current
 // state is cached and recomputed only after a local move was accepted; θ(x')
 // is rebuilt from scratch for an AR proposal and replaces the θ-cache when it
 // is accepted.  One warp per chain (lane l owns hidden units l + 32 k).
@@ -24,7 +26,8 @@ template <typename R> NQ_D R warp_sum_r(R s) {
 template <typename R, int HPL, int ACT>
 __global__ void __launch_bounds__(256, 1)
 rbm_mix_sampler_kernel(RbmDev<R> net, SamplerRun run, MadeDev made, unsigned long long thr,
-                       unsigned long long* __restrict__ ar_stats) {
+                       unsigned long long* __restrict__ ar_stats, const uint64_t* __restrict__ pre_x,
+                       const float* __restrict__ pre_lq, int pre_slots) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = net.N, M = net.M;
   cpx<R>* s_t0 = reinterpret_cast<cpx<R>*>(smem_raw);
@@ -150,7 +153,15 @@ rbm_mix_sampler_kernel(RbmDev<R> net, SamplerRun run, MadeDev made, unsigned lon
         }
       } else {
         uint64_t xp = 0;
-        const float lqp = made::walk<4, true>(made, xp, ar_slot++, (uint32_t)chain, run.call, run.k0, run.k1);
+        float lqp;
+        if ((int)ar_slot < pre_slots) {          // drawn ahead by the proposal kernel
+          const size_t q = (size_t)chain * pre_slots + ar_slot;
+          xp = pre_x[q];
+          lqp = pre_lq[q];
+        } else {
+          lqp = made::walk<4, true>(made, xp, ar_slot, (uint32_t)chain, run.call, run.k0, run.k1);
+        }
+        ++ar_slot;
         if (!lq_ok) {
           uint64_t xc = bits;
           lq_x = made::walk<4, false>(made, xc, 0, 0, 0, 0, 0);
@@ -219,7 +230,8 @@ cudaError_t mix_inst(const RbmDev<float>& net, const SamplerRun& run, const MixP
   auto kern = rbm_mix_sampler_kernel<float, HPL, ACT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<blocks, threads, smem, st>>>(net, run, mix.made, mix.thr, mix.ar_stats);
+  kern<<<blocks, threads, smem, st>>>(net, run, mix.made, mix.thr, mix.ar_stats, mix.pre_x, mix.pre_lq,
+                                      mix.pre_x ? mix.pre_slots : 0);
   return cudaGetLastError();
 }
 

@@ -1,5 +1,7 @@
 // C-ABI of the learned autoregressive proposal: parameter storage, the
 // mixture-sampler stage hook and training on the samples of the last call.
+#include <cmath>
+
 #include <cuda_bf16.h>
 
 #include "handle.cuh"
@@ -21,6 +23,9 @@ struct MadeState {
   uint64_t* x = nullptr;          // staging for host configurations
   float* lq = nullptr;
   size_t x_cap = 0;
+  uint64_t* pre_x = nullptr;      // proposals drawn ahead of the chain kernel [B][pre_slots]
+  float* pre_lq = nullptr;
+  int pre_slots = 0;
   int adam_step = 0;
 };
 
@@ -119,7 +124,8 @@ struct HostNormal {
 void proposal_destroy(nq_handle* h) {
   if (!h || !h->made) return;
   MadeState* s = h->made;
-  void* bufs[] = {s->master, s->m, s->v, s->mask, s->grad, s->partial, s->wbf, s->bias, s->stats, s->x, s->lq};
+  void* bufs[] = {s->master, s->m, s->v, s->mask, s->grad, s->partial, s->wbf, s->bias, s->stats, s->x, s->lq,
+                  s->pre_x, s->pre_lq};
   for (void* p : bufs)
     if (p) cudaFree(p);
   delete s;
@@ -131,10 +137,27 @@ nq_status proposal_sample_stage(nq_handle* h, const SamplerRun& run, bool* used)
   MadeState* s = h->made;
   if (!s || s->p_ar <= 0.0) return NQ_OK;
   CK(cudaMemsetAsync(s->stats, 0, 2 * sizeof(unsigned long long), h->st));
+  // AR moves of one chain in this call: Binomial(T, p_ar); draw the slots up to
+  // its mean + 6 standard deviations ahead (the rare rest is drawn inline)
+  const double T = (double)run.passes * (run.burn + run.n_record);
+  const int slots = (int)std::min(T, std::ceil(T * s->p_ar + 6.0 * std::sqrt(T * s->p_ar * (1.0 - s->p_ar))) + 8.0);
+  if (slots > s->pre_slots) {
+    if (s->pre_x) cudaFree(s->pre_x);
+    if (s->pre_lq) cudaFree(s->pre_lq);
+    s->pre_x = nullptr; s->pre_lq = nullptr; s->pre_slots = 0;
+    CK(cudaMalloc((void**)&s->pre_x, (size_t)h->B * slots * sizeof(uint64_t)));
+    CK(cudaMalloc((void**)&s->pre_lq, (size_t)h->B * slots * sizeof(float)));
+    s->pre_slots = slots;
+  }
+  CKL(launch_made_sample(made_dev(s), h->B, slots, run.call, run.k0, run.k1, s->pre_x, s->pre_lq, h->st,
+                         run.call_ptr));
   MixParams mp;
   mp.made = made_dev(s);
   mp.thr = s->thr;
   mp.ar_stats = s->stats;
+  mp.pre_x = s->pre_x;
+  mp.pre_lq = s->pre_lq;
+  mp.pre_slots = slots;
   CKL(launch_rbm_mix_sampler(rbm_dev<float>(h), run, mp, h->st));
   *used = true;
   return NQ_OK;
