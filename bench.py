@@ -165,6 +165,23 @@ def run_gb300(args, barrier=None):
     ms_step = total_ms / args.steps
     value = 1e3 / ms_step
 
+    # the same step with S accumulated from BF16 O (tcgen05 kind::f16)
+    modes = {}
+    if sp != nq._lib.NQ_S_BF16:
+        _, _, is_bf = build_sampler(nq._lib.NQ_S_BF16)
+        e_bf = is_bf.engine
+        for i in range(args.warmup):
+            e_bf.vmc_step(i, w["eps"], w["lr"])
+        ms_bf = float(np.mean(e_bf.bench_steps(args.warmup, max(10, args.steps // 4), w["eps"], w["lr"],
+                                               L2_FLUSH_BYTES)))
+        modes["bf16_S"] = {"ms_per_step": ms_bf, "sr_steps_per_s": 1e3 / ms_bf,
+                           "S_accumulation_ms": None, "note": "S from BF16 O, FP32 accumulation; S within 1e-2 "
+                                                             "relative of the FP64 oracle (tests/test_tc_gpu.py)"}
+        e_bf.sample(10 ** 6, want_samples=False)
+        e_bf.estimate()
+        modes["bf16_S"]["S_accumulation_ms"] = float(e_bf.stage_times()[7])
+        del e_bf, is_bf
+
     # staged pass: per-stage and per-kernel device times, E_loc for ESS
     call = args.warmup + args.steps + 10
     eng.sample(call, want_samples=False)
@@ -215,6 +232,7 @@ def run_gb300(args, barrier=None):
         "effective_samples_per_s": ess, "tau_int_eloc": tau, "energy_per_site": m.mean_re / w["N"],
         "stage_ms": stages, "kernel_ms": kernels,
         "tuning": eng.tuning(),
+        "s_precision_modes": modes,
         "roofline": roof,
     }
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_batch:

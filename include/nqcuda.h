@@ -83,7 +83,8 @@ typedef enum {
   NQ_S_F32 = 0,            /* FP32 CUDA cores */
   NQ_S_TF32 = 1,           /* tcgen05 kind::tf32, FP32 accumulate */
   NQ_S_TF32X3 = 2,         /* tcgen05 kind::tf32 with hi/lo split (3 products) */
-  NQ_S_F64 = 3             /* FP64 CUDA cores */
+  NQ_S_F64 = 3,            /* FP64 CUDA cores (not provided) */
+  NQ_S_BF16 = 4            /* tcgen05 kind::f16 on BF16 O (RBM): half the bytes of TF32 */
 } nq_s_precision;
 
 /* Reference quirks that can be reproduced exactly (off by default). */

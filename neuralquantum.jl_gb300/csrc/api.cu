@@ -237,11 +237,12 @@ nq_status stage_S(nq_handle* h) {
   }
   src.meanO = h->fb.meanO;
   const int sp = h->cfg.s_precision;
-  if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
-    CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, sp == NQ_S_TF32X3 ? h->d_Xlo : nullptr, h->st));
+  if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3 || sp == NQ_S_BF16) {
+    const int bf16 = sp == NQ_S_BF16 ? 1 : 0;
+    CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, sp == NQ_S_TF32X3 ? h->d_Xlo : nullptr, h->st, bf16));
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
     CKL(launch_gram_tc(h->d_X, h->d_Xlo, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
-                       h->gram_ksplit, h->sb.status, h->st));
+                       h->gram_ksplit, h->sb.status, h->st, bf16));
     if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
   } else {
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
@@ -411,10 +412,13 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     delete h;
     return NQ_ERR_UNSUPPORTED;
   }
-  if ((c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) && !gram_tc_supported()) {
+  if ((c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3 || c.s_precision == NQ_S_BF16) &&
+      !gram_tc_supported()) {
     delete h;
     return NQ_ERR_UNSUPPORTED;
   }
+  if (c.s_precision == NQ_S_BF16 && c.network != NQ_NET_RBM) { delete h; return NQ_ERR_UNSUPPORTED; }
+  if (c.s_precision < NQ_S_F32 || c.s_precision > NQ_S_BF16) return bad("unknown s_precision");
   h->N = c.n_sites;
   h->M = c.n_hidden;
   if (c.network == NQ_NET_NDM) {
@@ -530,13 +534,14 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (!h->cg) step(dalloc(&h->d_G, (size_t)rows * rows), "G");
   if (!h->cg) step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
   if (h->cg) {
-  } else if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3) {
+  } else if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3 || c.s_precision == NQ_S_BF16) {
+    const int bf16 = c.s_precision == NQ_S_BF16 ? 1 : 0;
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
-    h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad);
+    h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad, bf16);
     cudaFree(h->d_Gpart);
     h->d_Gpart = nullptr;
     step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
-    step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
+    step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad / (bf16 ? 2 : 1)), "X");     // BF16 X: half the bytes
     if (c.s_precision == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
   } else if (h->ndm) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;

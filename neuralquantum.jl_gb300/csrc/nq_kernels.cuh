@@ -135,15 +135,16 @@ cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* part
                              cudaStream_t st);
 // materialise X (2P x Ns_pad, row-major, zero padded) rounded to TF32 for
 // tcgen05; if Xlo is given it receives the TF32 remainder x - tf32(x).
-cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo,
-                           cudaStream_t st);
+// bf16 = 1: X is written as BF16 (round to nearest) for the BF16 S mode; Xlo unused
+cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo, cudaStream_t st,
+                           int bf16 = 0);
 // tcgen05 kind::tf32 SYRK: G = X X^T (upper 128x128 tiles), split-K partials
 // [ksplit][rp][rp] (rp = rows rounded up to 128) reduced into G.  split3 adds
 // the hi*lo + lo*hi products (3xTF32).  err receives timeout status bits.
-cudaError_t launch_gram_tc(const float* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
-                           float* partial, int ksplit, int* err, cudaStream_t st);
+cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
+                           float* partial, int ksplit, int* err, cudaStream_t st, int bf16 = 0);
 int gram_tc_supported();
-int gram_tc_ksplit(int rows, int Ns_pad);
+int gram_tc_ksplit(int rows, int Ns_pad, int bf16 = 0);
 cudaError_t launch_gram_reduce(const float* partial, int rows, int rp, int tile, int ksplit, float* G,
                                cudaStream_t st);
 // S (P x P complex double, full Hermitian) = combine(G)/Ns

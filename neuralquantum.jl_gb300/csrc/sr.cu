@@ -132,6 +132,7 @@ __device__ __forceinline__ float to_tf32(float x) {
 // block-uniform), four consecutive samples per thread with 16-byte stores.
 // HBM-bound: writes 4·rows·Ns_pad bytes (twice with Xlo); g rows and σ are
 // re-read by the 2(N+1) rows that share them, from L2.
+template <bool BF16>
 __global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X,
                                                       float* __restrict__ Xlo) {
   const int row = blockIdx.y;
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int rows, 
   const float mean = (float)src.meanO[2 * k + part];
   const float2* __restrict__ grow = src.g + (size_t)h * Ns;
   float* xrow = X + (size_t)row * Ns_pad;
+  __nv_bfloat16* brow = reinterpret_cast<__nv_bfloat16*>(X) + (size_t)row * Ns_pad;
   float* lrow = Xlo ? Xlo + (size_t)row * Ns_pad : nullptr;
   for (int s0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4; s0 < Ns_pad; s0 += gridDim.x * blockDim.x * 4) {
     float v[4];
@@ -166,11 +168,18 @@ __global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int rows, 
       }
       v[e] = val;
     }
-    const float4 hi = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
-    *reinterpret_cast<float4*>(xrow + s0) = hi;
-    if (lrow)
-      *reinterpret_cast<float4*>(lrow + s0) =
-          make_float4(to_tf32(v[0] - hi.x), to_tf32(v[1] - hi.y), to_tf32(v[2] - hi.z), to_tf32(v[3] - hi.w));
+    if (BF16) {
+      __align__(8) __nv_bfloat16 b[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) b[e] = __float2bfloat16_rn(v[e]);
+      *reinterpret_cast<uint2*>(brow + s0) = *reinterpret_cast<const uint2*>(b);
+    } else {
+      const float4 hi = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+      *reinterpret_cast<float4*>(xrow + s0) = hi;
+      if (lrow)
+        *reinterpret_cast<float4*>(lrow + s0) =
+            make_float4(to_tf32(v[0] - hi.x), to_tf32(v[1] - hi.y), to_tf32(v[2] - hi.z), to_tf32(v[3] - hi.w));
+    }
   }
 }
 
@@ -392,11 +401,13 @@ cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float*
 }
 
 cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo,
-                           cudaStream_t st) {
+                           cudaStream_t st, int bf16) {
   if (Ns_pad % 4 != 0 || 2 * P > 65535) return cudaErrorInvalidValue;
   const int per_block = 256 * 4;
   const int bx = std::min((Ns_pad + per_block - 1) / per_block, 64);
-  build_X_kernel<<<dim3((unsigned)bx, (unsigned)(2 * P)), 256, 0, st>>>(src, 2 * P, Ns_pad, X, Xlo);
+  const dim3 grid((unsigned)bx, (unsigned)(2 * P));
+  if (bf16) build_X_kernel<true><<<grid, 256, 0, st>>>(src, 2 * P, Ns_pad, X, nullptr);
+  else build_X_kernel<false><<<grid, 256, 0, st>>>(src, 2 * P, Ns_pad, X, Xlo);
   return cudaGetLastError();
 }
 

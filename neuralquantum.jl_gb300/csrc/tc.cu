@@ -1,6 +1,9 @@
 // tcgen05 (5th-generation tensor core) kernels for sm_103a.
 //
 // gram_tf32_kernel: the SR matrix accumulation G = X Xᵀ over the real rows
+// (TF32 operands, optionally 3xTF32 hi/lo, or BF16 operands with
+// tcgen05.mma.kind::f16 — the same 128-byte swizzled row layout holds 32 fp32
+// or 64 bf16 samples per stage)
 // X = [Re O_c; Im O_c] (2P x Ns, sample index contiguous), i.e. the
 // O_c O_c† of SRDirect.jl:32 written as one real symmetric rank-Ns update.
 // One CTA owns a 128 x 128 upper tile of G and a contiguous range of the
@@ -35,7 +38,7 @@ __device__ __forceinline__ void upper_tile(int t, int nt, int* ti, int* tj) {
 
 __global__ void __launch_bounds__(192, 1)
 gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap xlomap,
-                 int split3, int stages, int nt, int nchunks_total, int ksplit, int rp,
+                 int split3, int bf16, int stages, int nt, int nchunks_total, int ksplit, int rp,
                  float* __restrict__ partial, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -86,7 +89,7 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
         const uint32_t round = (uint32_t)(c / stages);
         if (c >= stages && !mbar_wait_bounded(&empty[s], (round - 1) & 1u, err)) { s_abort = 1; break; }
         uint8_t* buf = ring + (size_t)s * nops * TILE_BYTES;
-        const int kx = (c_begin + c) * KC;
+        const int kx = (c_begin + c) * (bf16 ? 2 * KC : KC);     // elements of 128-byte rows
         const uint32_t per_op = (uint32_t)TILE_BYTES * (diag ? 1u : 2u);
         mbar_arrive_expect_tx(&full[s], per_op * (split3 ? 2u : 1u));
         tma_load_2d(buf, &xmap, kx, ti * TM, &full[s]);
@@ -105,7 +108,7 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
   } else if (warp == 5) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      const uint32_t idesc = idesc_f32acc(2u, 128u, 128u);
+      const uint32_t idesc = idesc_f32acc(bf16 ? 1u : 2u, 128u, 128u);
       for (int c = 0; c < nch; ++c) {
         const int seg = c / SEG, b = seg & 1;
         const bool first = (c % SEG) == 0;
@@ -123,13 +126,21 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
         const uint32_t a_lo = smem_u32(buf + 2 * TILE_BYTES);
         const uint32_t b_lo = smem_u32(buf + (diag ? 2 : 3) * TILE_BYTES);
         const uint32_t d = tmem + (uint32_t)(b * TM);
+        if (bf16) {
 #pragma unroll
-        for (int kk = 0; kk < KC / 8; ++kk) {      // K = 8 tf32 (32 bytes) per instruction
-          const uint32_t off = kk * 32;
-          mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc, (first && kk == 0) ? 0u : 1u);
-          if (split3) {
-            mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_lo + off), idesc, 1u);
-            mma_tf32(d, sdesc_k_sw128(a_lo + off), sdesc_k_sw128(b_hi + off), idesc, 1u);
+          for (int kk = 0; kk < 4; ++kk) {         // K = 16 bf16 (32 bytes) per instruction
+            const uint32_t off = kk * 32;
+            mma_f16(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc, (first && kk == 0) ? 0u : 1u);
+          }
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < KC / 8; ++kk) {    // K = 8 tf32 (32 bytes) per instruction
+            const uint32_t off = kk * 32;
+            mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc, (first && kk == 0) ? 0u : 1u);
+            if (split3) {
+              mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_lo + off), idesc, 1u);
+              mma_tf32(d, sdesc_k_sw128(a_lo + off), sdesc_k_sw128(b_hi + off), idesc, 1u);
+            }
           }
         }
         mma_commit(&empty[s]);
@@ -184,17 +195,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// row-major fp32 [rows][cols] matrix, box = 32 cols (128 B) x 128 rows, SW128
-bool encode_rowmajor_f32(CUtensorMap* map, const float* ptr, int rows, int cols) {
+// row-major [rows][cols] matrix of fp32 (bf16 = 0) or bf16 elements, box = one
+// 128-byte row segment (32 fp32 / 64 bf16) x 128 rows, SW128
+bool encode_rowmajor(CUtensorMap* map, const void* ptr, int rows, int cols, int bf16) {
   auto fn = encode_fn();
   if (!fn) return false;
+  const size_t esz = bf16 ? 2 : 4;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
-  cuuint32_t box[2] = {(cuuint32_t)KC, (cuuint32_t)TM};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * esz};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)TM};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                  const_cast<void*>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
@@ -209,23 +222,25 @@ int gram_tc_supported() {
   return (major == 10 && minor == 3 && encode_fn() != nullptr) ? 1 : 0;
 }
 
-int gram_tc_ksplit(int rows, int Ns_pad) {
+int gram_tc_ksplit(int rows, int Ns_pad, int bf16) {
   const int nt = (rows + TM - 1) / TM;
   const int tiles = nt * (nt + 1) / 2;
-  const int nchunks = Ns_pad / KC;
+  const int nchunks = Ns_pad / (bf16 ? 2 * KC : KC);
   // fill >= 2 waves of 152 SMs, keep >= 8 chunks per CTA
   int ks = 1;
   while (tiles * ks < 2 * 152 && nchunks / (ks * 2) >= 8) ks *= 2;
   return ks;
 }
 
-cudaError_t launch_gram_tc(const float* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
-                           float* partial, int ksplit, int* err, cudaStream_t st) {
-  if (Ns_pad % KC != 0 || ((uintptr_t)X & 15u) != 0) return cudaErrorInvalidValue;
+cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
+                           float* partial, int ksplit, int* err, cudaStream_t st, int bf16) {
+  const int kc = bf16 ? 2 * KC : KC;
+  if (Ns_pad % kc != 0 || ((uintptr_t)X & 15u) != 0) return cudaErrorInvalidValue;
+  if (bf16 && split3) return cudaErrorInvalidValue;
   if (split3 && (!Xlo || ((uintptr_t)Xlo & 15u) != 0)) return cudaErrorInvalidValue;
   CUtensorMap xmap, xlomap;
-  if (!encode_rowmajor_f32(&xmap, X, rows, Ns_pad)) return cudaErrorInvalidValue;
-  if (!encode_rowmajor_f32(&xlomap, split3 ? Xlo : X, rows, Ns_pad)) return cudaErrorInvalidValue;
+  if (!encode_rowmajor(&xmap, X, rows, Ns_pad, bf16)) return cudaErrorInvalidValue;
+  if (!encode_rowmajor(&xlomap, split3 ? (const void*)Xlo : X, rows, Ns_pad, bf16)) return cudaErrorInvalidValue;
   const int nt = (rows + TM - 1) / TM;
   const int tiles = nt * (nt + 1) / 2;
   const int stages = split3 ? 2 : 4;
@@ -234,7 +249,8 @@ cudaError_t launch_gram_tc(const float* X, const float* Xlo, int rows, int Ns_pa
   if (e != cudaSuccess) return e;
   dim3 grid(tiles, ksplit);
   const int rp = nt * TM;
-  gram_tf32_kernel<<<grid, 192, smem, st>>>(xmap, xlomap, split3, stages, nt, Ns_pad / KC, ksplit, rp, partial, err);
+  gram_tf32_kernel<<<grid, 192, smem, st>>>(xmap, xlomap, split3, bf16, stages, nt, Ns_pad / kc, ksplit, rp,
+                                            partial, err);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return launch_gram_reduce(partial, rows, rp, TM, ksplit, G, st);

@@ -32,7 +32,7 @@ NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS = 0, 1
 NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3
 NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64, NQ_EVAL_TC_BF16X3 = 0, 1, 2, 3
-NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64 = 0, 1, 2, 3
+NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64, NQ_S_BF16 = 0, 1, 2, 3, 4
 NQ_SR_DIRECT, NQ_SR_CG = 0, 1
 NQ_QUIRK_STALE_LAST_SLOT = 0x1
 
