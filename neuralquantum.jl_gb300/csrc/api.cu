@@ -215,7 +215,7 @@ nq_status stage_S(nq_handle* h) {
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
     if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
       CKL(launch_gram_tc(h->d_X, h->d_Xlo, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
-                         h->gram_ksplit, h->sb.status, h->st));
+                         h->sb.status, h->st));
     } else {
       CKL(launch_gram_simt_x(h->d_X, h->Ns_pad, h->Ns, 2 * h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
     }
@@ -242,7 +242,7 @@ nq_status stage_S(nq_handle* h) {
     CKL(launch_build_X(src, h->P, h->Ns_pad, h->d_X, sp == NQ_S_TF32X3 ? h->d_Xlo : nullptr, h->st, bf16));
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
     CKL(launch_gram_tc(h->d_X, h->d_Xlo, 2 * h->P, h->Ns_pad, sp == NQ_S_TF32X3 ? 1 : 0, h->d_G, h->d_Gpart,
-                       h->gram_ksplit, h->sb.status, h->st, bf16));
+                       h->sb.status, h->st, bf16));
     if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
   } else {
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
@@ -540,7 +540,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad, bf16);
     cudaFree(h->d_Gpart);
     h->d_Gpart = nullptr;
-    step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
+    step(dalloc(&h->d_Gpart, gram_tc_partial_elems(rows, h->Ns_pad, bf16)), "G partial");
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad / (bf16 ? 2 : 1)), "X");     // BF16 X: half the bytes
     if (c.s_precision == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
   } else if (h->ndm) {

@@ -138,13 +138,16 @@ cudaError_t launch_gram_simt(const RbmOSource& src, int P, float* G, float* part
 // bf16 = 1: X is written as BF16 (round to nearest) for the BF16 S mode; Xlo unused
 cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo, cudaStream_t st,
                            int bf16 = 0);
-// tcgen05 kind::tf32 SYRK: G = X X^T (upper 128x128 tiles), split-K partials
-// [ksplit][rp][rp] (rp = rows rounded up to 128) reduced into G.  split3 adds
-// the hi*lo + lo*hi products (3xTF32).  err receives timeout status bits.
+// tcgen05 SYRK: G = X X^T (upper 128x128 tiles of the rows x rows row-major G).
+// Persistent CTAs over (k-split, tile) items; each item writes a column-major
+// 128x128 partial tile into `partial` (gram_tc_partial_elems floats), and a
+// second kernel sums the k-splits into G.  split3 adds the hi*lo + lo*hi
+// products (3xTF32); bf16 = 1 reads X as BF16.  err receives timeout bits.
 cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
-                           float* partial, int ksplit, int* err, cudaStream_t st, int bf16 = 0);
+                           float* partial, int* err, cudaStream_t st, int bf16 = 0);
 int gram_tc_supported();
 int gram_tc_ksplit(int rows, int Ns_pad, int bf16 = 0);
+size_t gram_tc_partial_elems(int rows, int Ns_pad, int bf16 = 0);
 cudaError_t launch_gram_reduce(const float* partial, int rows, int rp, int tile, int ksplit, float* G,
                                cudaStream_t st);
 // S (P x P complex double, full Hermitian) = combine(G)/Ns

@@ -6,16 +6,27 @@
 // or 64 bf16 samples per stage)
 // X = [Re O_c; Im O_c] (2P x Ns, sample index contiguous), i.e. the
 // O_c O_c† of SRDirect.jl:32 written as one real symmetric rank-Ns update.
-// One CTA owns a 128 x 128 upper tile of G and a contiguous range of the
-// sample (K) dimension.  Warp 4 issues TMA into a shared-memory ring
-// (128-byte swizzle, one 128 x 32 fp32 box per operand), warp 5 issues
-// tcgen05.mma.kind::tf32 into one of two TMEM accumulators.  The tensor core
-// accumulates in FP32 without round-to-nearest, so long K chains drift low;
-// every SEG chunks (1024 samples) the accumulator is handed to warps 0-3,
-// which drain it into a round-to-nearest FP32 tile in shared memory while the
-// MMAs continue in the other TMEM buffer.  Every mbarrier wait is bounded
-// (1 s); a timeout sets a status bit, drains outstanding copies, frees TMEM
-// and exits.
+//
+// A work item is (k-split y, block (ti, J)): rows [128 ti, +128) x columns
+// [256 J, +256) of G for every J whose block reaches the upper triangle.
+// One tcgen05.mma of M = 128, N = 256 covers the whole block: the MMA issue
+// rate, not the operand bytes, bounds this kernel, and an N = 256 instruction
+// costs about as much as an N = 128 one.  Items are ordered y-major so that
+// the CTAs running at the same time read the same sample range of X and share
+// it through L2.  One persistent CTA per SM walks items q = blockIdx.x +
+// j * gridDim.x; its TMA ring runs on across item boundaries.
+// Warp 8 issues TMA into the ring (128-byte swizzle, 128 x 128-byte boxes:
+// B = X rows [256 J, +256) as two boxes, then A = X rows [128 ti, +128); when
+// the A rows lie inside B the A box is not loaded and the MMA reads them from
+// B), warp 9 issues tcgen05.mma into one of two TMEM accumulators.  The tensor
+// core accumulates in FP32 without round-to-nearest, so long K chains drift
+// low: every SEG chunks the accumulator is handed to warps 0-7, which add it
+// into round-to-nearest FP32 sums held in registers (warp w: TMEM lanes
+// 32 (w mod 4).., columns 128 (w div 4)..) while the MMAs continue in the other
+// accumulator.  At the end of an item the sums go to the item's partial block,
+// column-major, one 128-byte store per warp and column.  Every mbarrier wait
+// is bounded (1 s); a timeout sets a status bit, drains outstanding copies,
+// frees TMEM and exits.
 #include <cudaTypedefs.h>
 
 #include "nq_kernels.cuh"
@@ -23,42 +34,49 @@
 
 namespace {
 
-constexpr int TM = 128;                      // tile rows = tile cols
+constexpr int TM = 128;                      // block rows; TMA box rows
+constexpr int NW = 256;                      // block columns (MMA N)
 constexpr int KC = 32;                       // fp32 K elements per stage (128 B rows)
-constexpr int TILE_BYTES = TM * KC * 4;      // 16 KiB per operand per stage
+constexpr int TILE_BYTES = TM * KC * 4;      // 16 KiB per 128-row box
 constexpr int SEG = 32;                      // chunks per TMEM accumulation segment
-constexpr int ACC_LD = TM + 1;               // padded leading dimension of the smem tile
-constexpr int ACC_BYTES = TM * ACC_LD * 4;
+constexpr int BLOCK_ELEMS = TM * NW;
+constexpr int NDRAIN = 8;                    // drain warps
+constexpr int THREADS = (NDRAIN + 2) * 32;
 
-__device__ __forceinline__ void upper_tile(int t, int nt, int* ti, int* tj) {
-  int i = 0, rem = t;
-  while (rem >= nt - i) { rem -= nt - i; ++i; }
-  *ti = i; *tj = i + rem;
+__host__ __device__ __forceinline__ int first_block(int ti) { return (ti * TM) / NW; }
+
+// number of (ti, J) blocks in rows < ti, with nj = ceil(rows / NW) column blocks
+__host__ __device__ __forceinline__ int blocks_before(int ti, int nj) {
+  int s = 0;
+  for (int i = 0; i < ti; ++i) s += nj - first_block(i);
+  return s;
 }
 
-__global__ void __launch_bounds__(192, 1)
+__device__ __forceinline__ void block_coords(int p, int nj, int* ti, int* J) {
+  int i = 0, rem = p;
+  while (rem >= nj - first_block(i)) { rem -= nj - first_block(i); ++i; }
+  *ti = i; *J = first_block(i) + rem;
+}
+
+// chunk range of k-split y: [y * per, min(nch, (y + 1) * per))
+__device__ __forceinline__ int item_chunks(int y, int per, int nch) { return min(nch, (y + 1) * per) - y * per; }
+
+__global__ void __launch_bounds__(THREADS, 1)
 gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap xlomap,
-                 int split3, int bf16, int stages, int nt, int nchunks_total, int ksplit, int rp,
-                 float* __restrict__ partial, int* __restrict__ err) {
+                 int split3, int bf16, int stages, int nj, int nblocks, int nch, int per, int items,
+                 float* __restrict__ slots, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int nops = split3 ? 4 : 2;
+  const int nbox = split3 ? 6 : 3;          // [B0 B1 A] (+ [B0lo B1lo Alo])
+  const size_t stage_bytes = (size_t)nbox * TILE_BYTES;
   uint8_t* ring = base;
-  float* acc = reinterpret_cast<float*>(base + (size_t)stages * nops * TILE_BYTES);   // [col][ACC_LD]
-  uint64_t* full = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(acc) + ACC_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)stages * stage_bytes);
   uint64_t* empty = full + stages;
   uint64_t* seg_full = empty + stages;     // [2]
   uint64_t* seg_empty = seg_full + 2;      // [2]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(seg_empty + 2);
   __shared__ int s_abort;
 
-  int ti, tj;
-  upper_tile(blockIdx.x, nt, &ti, &tj);
-  const bool diag = ti == tj;
-  const int per = (nchunks_total + ksplit - 1) / ksplit;
-  const int c_begin = blockIdx.y * per;
-  const int nch = max(0, min(nchunks_total, c_begin + per) - c_begin);
-  const int nseg = (nch + SEG - 1) / SEG;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -68,118 +86,189 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&seg_full[b], 1);
-      mbar_init(&seg_empty[b], 4);
+      mbar_init(&seg_empty[b], NDRAIN);
     }
     s_abort = 0;
     fence_mbar_init();
   }
-  for (int i = threadIdx.x; i < TM * ACC_LD; i += blockDim.x) acc[i] = 0.f;
-  if (warp == 5) tmem_alloc(tmem_slot, 256);
+  if (warp == NDRAIN + 1) tmem_alloc(tmem_slot, 2 * NW);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 4) {
+  if (warp == NDRAIN) {
     if (lane == 0) {
       // ---- TMA producer ----
-      int issued = 0;
-      for (int c = 0; c < nch && !*(volatile int*)&s_abort; ++c) {
-        const int s = c % stages;
-        const uint32_t round = (uint32_t)(c / stages);
-        if (c >= stages && !mbar_wait_bounded(&empty[s], (round - 1) & 1u, err)) { s_abort = 1; break; }
-        uint8_t* buf = ring + (size_t)s * nops * TILE_BYTES;
-        const int kx = (c_begin + c) * (bf16 ? 2 * KC : KC);     // elements of 128-byte rows
-        const uint32_t per_op = (uint32_t)TILE_BYTES * (diag ? 1u : 2u);
-        mbar_arrive_expect_tx(&full[s], per_op * (split3 ? 2u : 1u));
-        tma_load_2d(buf, &xmap, kx, ti * TM, &full[s]);
-        if (!diag) tma_load_2d(buf + TILE_BYTES, &xmap, kx, tj * TM, &full[s]);
-        if (split3) {
-          tma_load_2d(buf + 2 * TILE_BYTES, &xlomap, kx, ti * TM, &full[s]);
-          if (!diag) tma_load_2d(buf + 3 * TILE_BYTES, &xlomap, kx, tj * TM, &full[s]);
+      int k = 0;                      // stage counter across items
+      bool stop = false;
+      for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
+        const int y = q / nblocks;
+        int ti, J;
+        block_coords(q - y * nblocks, nj, &ti, &J);
+        const bool a_in_b = first_block(ti) == J;
+        const int n = item_chunks(y, per, nch);
+        const uint32_t bytes = (uint32_t)TILE_BYTES * (a_in_b ? 2u : 3u) * (split3 ? 2u : 1u);
+        for (int c = 0; c < n; ++c, ++k) {
+          if (*(volatile int*)&s_abort) { stop = true; break; }
+          const int s = k % stages;
+          const uint32_t round = (uint32_t)(k / stages);
+          if (k >= stages && !mbar_wait_bounded(&empty[s], (round - 1) & 1u, err)) {
+            s_abort = 1;
+            stop = true;
+            break;
+          }
+          uint8_t* buf = ring + (size_t)s * stage_bytes;
+          const int kx = (y * per + c) * (bf16 ? 2 * KC : KC);     // elements of 128-byte rows
+          mbar_arrive_expect_tx(&full[s], bytes);
+          tma_load_2d(buf, &xmap, kx, J * NW, &full[s]);
+          tma_load_2d(buf + TILE_BYTES, &xmap, kx, J * NW + TM, &full[s]);
+          if (!a_in_b) tma_load_2d(buf + 2 * TILE_BYTES, &xmap, kx, ti * TM, &full[s]);
+          if (split3) {
+            uint8_t* lb = buf + 3 * TILE_BYTES;
+            tma_load_2d(lb, &xlomap, kx, J * NW, &full[s]);
+            tma_load_2d(lb + TILE_BYTES, &xlomap, kx, J * NW + TM, &full[s]);
+            if (!a_in_b) tma_load_2d(lb + 2 * TILE_BYTES, &xlomap, kx, ti * TM, &full[s]);
+          }
         }
-        issued = c + 1;
       }
       // drain: every issued copy has landed before the CTA may exit
-      for (int c = max(0, issued - stages); c < issued; ++c)
+      for (int c = max(0, k - stages); c < k; ++c)
         mbar_wait_bounded(&full[c % stages], (uint32_t)(c / stages) & 1u, err);
     }
     __syncwarp();
-  } else if (warp == 5) {
+  } else if (warp == NDRAIN + 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      const uint32_t idesc = idesc_f32acc(bf16 ? 1u : 2u, 128u, 128u);
-      for (int c = 0; c < nch; ++c) {
-        const int seg = c / SEG, b = seg & 1;
-        const bool first = (c % SEG) == 0;
-        const bool last = (c % SEG) == SEG - 1 || c == nch - 1;
-        if (first && seg >= 2 && !mbar_wait_bounded(&seg_empty[b], (uint32_t)(seg / 2 - 1) & 1u, err)) {
-          s_abort = 1;
-          break;
-        }
-        const int s = c % stages;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)(c / stages) & 1u, err)) { s_abort = 1; break; }
-        tc_fence_after();
-        uint8_t* buf = ring + (size_t)s * nops * TILE_BYTES;
-        const uint32_t a_hi = smem_u32(buf);
-        const uint32_t b_hi = smem_u32(buf + (diag ? 0 : TILE_BYTES));
-        const uint32_t a_lo = smem_u32(buf + 2 * TILE_BYTES);
-        const uint32_t b_lo = smem_u32(buf + (diag ? 2 : 3) * TILE_BYTES);
-        const uint32_t d = tmem + (uint32_t)(b * TM);
-        if (bf16) {
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {         // K = 16 bf16 (32 bytes) per instruction
-            const uint32_t off = kk * 32;
-            mma_f16(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc, (first && kk == 0) ? 0u : 1u);
+      const uint32_t idesc = idesc_f32acc(bf16 ? 1u : 2u, (uint32_t)TM, (uint32_t)NW);
+      int k = 0, seg = 0;
+      bool stop = false;
+      for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
+        const int y = q / nblocks;
+        int ti, J;
+        block_coords(q - y * nblocks, nj, &ti, &J);
+        const bool a_in_b = first_block(ti) == J;
+        const uint32_t a_off = a_in_b ? (uint32_t)((ti * TM - J * NW) / TM) * TILE_BYTES : 2u * TILE_BYTES;
+        const int n = item_chunks(y, per, nch);
+        for (int c = 0; c < n; ++c, ++k) {
+          const int b = seg & 1;
+          const bool first = (c % SEG) == 0;
+          const bool last = (c % SEG) == SEG - 1 || c == n - 1;
+          if (first && seg >= 2 && !mbar_wait_bounded(&seg_empty[b], (uint32_t)(seg / 2 - 1) & 1u, err)) {
+            s_abort = 1;
+            stop = true;
+            break;
           }
-        } else {
+          const int s = k % stages;
+          if (!mbar_wait_bounded(&full[s], (uint32_t)(k / stages) & 1u, err)) {
+            s_abort = 1;
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t b_hi = smem_u32(ring + (size_t)s * stage_bytes);
+          const uint32_t a_hi = b_hi + a_off;
+          const uint32_t b_lo = b_hi + 3u * TILE_BYTES;
+          const uint32_t a_lo = a_hi + 3u * TILE_BYTES;
+          const uint32_t d = tmem + (uint32_t)(b * NW);
+          if (bf16) {
 #pragma unroll
-          for (int kk = 0; kk < KC / 8; ++kk) {    // K = 8 tf32 (32 bytes) per instruction
-            const uint32_t off = kk * 32;
-            mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc, (first && kk == 0) ? 0u : 1u);
-            if (split3) {
-              mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_lo + off), idesc, 1u);
-              mma_tf32(d, sdesc_k_sw128(a_lo + off), sdesc_k_sw128(b_hi + off), idesc, 1u);
+            for (int kk = 0; kk < 4; ++kk) {         // K = 16 bf16 (32 bytes) per instruction
+              const uint32_t off = kk * 32;
+              mma_f16(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc,
+                      (first && kk == 0) ? 0u : 1u);
+            }
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < KC / 8; ++kk) {    // K = 8 tf32 (32 bytes) per instruction
+              const uint32_t off = kk * 32;
+              mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc,
+                       (first && kk == 0) ? 0u : 1u);
+              if (split3) {
+                mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_lo + off), idesc, 1u);
+                mma_tf32(d, sdesc_k_sw128(a_lo + off), sdesc_k_sw128(b_hi + off), idesc, 1u);
+              }
             }
           }
+          mma_commit(&empty[s]);
+          if (last) {
+            mma_commit(&seg_full[b]);
+            ++seg;
+          }
         }
-        mma_commit(&empty[s]);
-        if (last) mma_commit(&seg_full[b]);
       }
     }
     __syncwarp();
   } else {
-    // ---- warps 0-3: drain TMEM segments into the round-to-nearest smem tile ----
-    const int row = warp * 32 + lane;
-    for (int seg = 0; seg < nseg; ++seg) {
-      const int b = seg & 1;
-      if (!mbar_wait_bounded(&seg_full[b], (uint32_t)(seg / 2) & 1u, err)) { s_abort = 1; break; }
-      tc_fence_after();
-#pragma unroll 1
-      for (int cc = 0; cc < TM; cc += 32) {
-        uint32_t r[32];
-        tmem_ld_32x32b_x32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * TM + cc), r);
-        tmem_ld_wait();
+    // ---- warps 0-7: drain TMEM segments into round-to-nearest sums in registers ----
+    const int lq = warp & 3, hc = warp >> 2;
+    const int row = lq * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(hc * TM);
+    int seg = 0;
+    bool stop = false;
+    for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
+      const int y = q / nblocks;
+      const int nseg = (item_chunks(y, per, nch) + SEG - 1) / SEG;
+      float acc[TM];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) acc[(cc + q) * ACC_LD + row] += __uint_as_float(r[q]);
+      for (int c = 0; c < TM; ++c) acc[c] = 0.f;
+      for (int j = 0; j < nseg; ++j, ++seg) {
+        const int b = seg & 1;
+        if (!mbar_wait_bounded(&seg_full[b], (uint32_t)(seg / 2) & 1u, err)) {
+          s_abort = 1;
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int cc = 0; cc < TM; cc += 16) {
+          uint32_t r[16];
+          tmem_ld_32x32b_x16(lane_base + (uint32_t)(b * NW + cc), r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int e = 0; e < 16; ++e) acc[cc + e] += __uint_as_float(r[e]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&seg_empty[b]);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&seg_empty[b]);
-    }
-  }
-  __syncthreads();
-  // ---- write the tile (zeros for an empty K range) ----
-  if (!s_abort) {
-    float* dst = partial + (size_t)blockIdx.y * rp * rp + (size_t)(ti * TM) * rp + tj * TM;
-    for (int i = threadIdx.x; i < TM * TM; i += blockDim.x) {
-      const int r = i / TM, c = i % TM;
-      dst[(size_t)r * rp + c] = acc[c * ACC_LD + r];
+      if (stop || *(volatile int*)&s_abort) break;
+      // item's partial block, column-major: element (r, c) at c * TM + r
+      float* dst = slots + (size_t)q * BLOCK_ELEMS + (size_t)(hc * TM) * TM + row;
+#pragma unroll
+      for (int c = 0; c < TM; ++c) dst[(size_t)c * TM] = acc[c];
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 5) tmem_dealloc(tmem, 256);
+  if (warp == NDRAIN + 1) tmem_dealloc(tmem, 2 * NW);
+}
+
+// G (rows x rows, row-major, upper 128 x 128 tiles) = sum over k-splits of the
+// column-major partial blocks; 32 x 32 sub-blocks transposed through shared
+// memory so that both the partial reads and the G writes are coalesced.
+// blockIdx.x: upper tile t = (ti, tj) in row-major order, blockIdx.y: sub-block.
+__global__ void __launch_bounds__(256) gram_slot_reduce_kernel(const float* __restrict__ slots, int rows, int nt,
+                                                               int nj, int nblocks, int ks, float* __restrict__ G) {
+  __shared__ float buf[32][33];
+  const int sr = (blockIdx.y >> 2) * 32, sc = (blockIdx.y & 3) * 32;
+  int ti = 0, rem = blockIdx.x;
+  while (rem >= nt - ti) { rem -= nt - ti; ++ti; }
+  const int tj = ti + rem;
+  const int J = (tj * TM) / NW;
+  const int p = blocks_before(ti, nj) + (J - first_block(ti));
+  const size_t col0 = (size_t)(tj * TM - J * NW);
+  for (int cl = threadIdx.y; cl < 32; cl += 8) {
+    const size_t off = (col0 + sc + cl) * TM + sr + threadIdx.x;
+    float s = 0.f;
+    for (int z = 0; z < ks; ++z) s += slots[((size_t)z * nblocks + p) * BLOCK_ELEMS + off];
+    buf[cl][threadIdx.x] = s;
+  }
+  __syncthreads();
+  for (int rl = threadIdx.y; rl < 32; rl += 8) {
+    const int gr = ti * TM + sr + rl, gc = tj * TM + sc + threadIdx.x;
+    if (gr < rows && gc < rows) G[(size_t)gr * rows + gc] = buf[threadIdx.x][rl];
+  }
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -222,18 +311,62 @@ int gram_tc_supported() {
   return (major == 10 && minor == 3 && encode_fn() != nullptr) ? 1 : 0;
 }
 
-int gram_tc_ksplit(int rows, int Ns_pad, int bf16) {
-  const int nt = (rows + TM - 1) / TM;
-  const int tiles = nt * (nt + 1) / 2;
-  const int nchunks = Ns_pad / (bf16 ? 2 * KC : KC);
-  // fill >= 2 waves of 152 SMs, keep >= 8 chunks per CTA
-  int ks = 1;
-  while (tiles * ks < 2 * 152 && nchunks / (ks * 2) >= 8) ks *= 2;
-  return ks;
+namespace {
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+  }
+  return n;
 }
 
+// Split of the sample dimension and grid of the persistent Gram kernel.  Each
+// CTA takes ceil(items / ncta) items in turn; the cost counts the stages of
+// the busiest CTA plus, per k-split, the write and read of one more set of
+// partial blocks (about nblocks / 6 stage times).
+struct GramPlan {
+  int nt, nj, nblocks, nch, ks, per, items, ncta;
+};
+
+GramPlan gram_plan(int rows, int Ns_pad, int bf16) {
+  GramPlan p;
+  p.nt = (rows + TM - 1) / TM;
+  p.nj = (rows + NW - 1) / NW;
+  p.nblocks = blocks_before(p.nt, p.nj);
+  p.nch = Ns_pad / (bf16 ? 2 * KC : KC);
+  const int nsm = sm_count();
+  long best = -1;
+  p.ks = 1;
+  for (int ks = 1; ks <= 32 && ks <= p.nch; ++ks) {
+    const int per = (p.nch + ks - 1) / ks;
+    if ((p.nch + per - 1) / per != ks) continue;       // same split as a smaller ks
+    if (ks > 1 && per < 16) break;
+    const long items = (long)p.nblocks * ks;
+    const long rounds = (items + nsm - 1) / nsm;
+    const long cost = 6L * rounds * per + (long)ks * p.nblocks;
+    if (best < 0 || cost < best) { best = cost; p.ks = ks; }
+  }
+  p.per = (p.nch + p.ks - 1) / p.ks;
+  p.items = p.nblocks * p.ks;
+  p.ncta = std::min(nsm, p.items);
+  return p;
+}
+
+}  // namespace
+
+size_t gram_tc_partial_elems(int rows, int Ns_pad, int bf16) {
+  const GramPlan p = gram_plan(rows, Ns_pad, bf16);
+  return (size_t)p.items * BLOCK_ELEMS;
+}
+
+int gram_tc_ksplit(int rows, int Ns_pad, int bf16) { return gram_plan(rows, Ns_pad, bf16).ks; }
+
 cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad, int split3, float* G,
-                           float* partial, int ksplit, int* err, cudaStream_t st, int bf16) {
+                           float* partial, int* err, cudaStream_t st, int bf16) {
   const int kc = bf16 ? 2 * KC : KC;
   if (Ns_pad % kc != 0 || ((uintptr_t)X & 15u) != 0) return cudaErrorInvalidValue;
   if (bf16 && split3) return cudaErrorInvalidValue;
@@ -241,17 +374,17 @@ cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad
   CUtensorMap xmap, xlomap;
   if (!encode_rowmajor(&xmap, X, rows, Ns_pad, bf16)) return cudaErrorInvalidValue;
   if (!encode_rowmajor(&xlomap, split3 ? (const void*)Xlo : X, rows, Ns_pad, bf16)) return cudaErrorInvalidValue;
-  const int nt = (rows + TM - 1) / TM;
-  const int tiles = nt * (nt + 1) / 2;
+  const GramPlan p = gram_plan(rows, Ns_pad, bf16);
   const int stages = split3 ? 2 : 4;
-  const size_t smem = (size_t)stages * (split3 ? 4 : 2) * TILE_BYTES + ACC_BYTES + 1024 + 256;
+  const size_t smem = (size_t)stages * (split3 ? 6 : 3) * TILE_BYTES + 1024 + 256;
   cudaError_t e = cudaFuncSetAttribute(gram_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid(tiles, ksplit);
-  const int rp = nt * TM;
-  gram_tf32_kernel<<<grid, 192, smem, st>>>(xmap, xlomap, split3, bf16, stages, nt, Ns_pad / kc, ksplit, rp,
-                                            partial, err);
+  gram_tf32_kernel<<<p.ncta, THREADS, smem, st>>>(xmap, xlomap, split3, bf16, stages, p.nj, p.nblocks, p.nch,
+                                                   p.per, p.items, partial, err);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return launch_gram_reduce(partial, rows, rp, TM, ksplit, G, st);
+  const int tiles = p.nt * (p.nt + 1) / 2;
+  gram_slot_reduce_kernel<<<dim3((unsigned)tiles, 16), dim3(32, 8), 0, st>>>(partial, rows, p.nt, p.nj, p.nblocks,
+                                                                              p.ks, G);
+  return cudaGetLastError();
 }
