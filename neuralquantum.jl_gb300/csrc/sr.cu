@@ -128,58 +128,85 @@ __device__ __forceinline__ float to_tf32(float x) {
   return __uint_as_float(r);
 }
 
-// One row of X per blockIdx.y (the row's kind, hidden unit, site and mean are
-// block-uniform), four consecutive samples per thread with 16-byte stores.
-// HBM-bound: writes 4·rows·Ns_pad bytes (twice with Xlo); g rows and σ are
-// re-read by the 2(N+1) rows that share them, from L2.
 template <bool BF16>
-__global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int rows, int Ns_pad, float* __restrict__ X,
+__device__ __forceinline__ void put_x_row(float* X, float* Xlo, int row, int Ns_pad, int s0, const float (&v)[4]) {
+  if (BF16) {
+    __align__(8) __nv_bfloat16 b[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) b[e] = __float2bfloat16_rn(v[e]);
+    *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(X) + (size_t)row * Ns_pad + s0) =
+        *reinterpret_cast<const uint2*>(b);
+  } else {
+    const float4 hi = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+    *reinterpret_cast<float4*>(X + (size_t)row * Ns_pad + s0) = hi;
+    if (Xlo)
+      *reinterpret_cast<float4*>(Xlo + (size_t)row * Ns_pad + s0) =
+          make_float4(to_tf32(v[0] - hi.x), to_tf32(v[1] - hi.y), to_tf32(v[2] - hi.z), to_tf32(v[3] - hi.w));
+  }
+}
+
+// X row 2k + part holds Re (part 0) or Im (part 1) of O_k - <O_k> over the
+// samples, zero in the padding.  One block per (sample range, source unit u):
+// u < M is hidden unit h = u and writes the rows of b_h (k = N + h) and of
+// every weight W_hj (k = N + M + j M + h); u = M writes the rows of the
+// visible units a_j (k = j).  Each thread loads σ and g_h of four consecutive
+// samples once and writes all 2(N + 1) rows that depend on them, 16-byte
+// stores coalesced across the warp: the kernel is bound by the X writes
+// (4 rows Ns_pad bytes, twice with Xlo, half with BF16), not by re-reads.
+template <bool BF16>
+__global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int Ns_pad, float* __restrict__ X,
                                                       float* __restrict__ Xlo) {
-  const int row = blockIdx.y;
+  const int u = blockIdx.y;
   const int N = src.N, M = src.M, Ns = src.Ns, hilb = src.hilb;
-  const int k = row >> 1, part = row & 1;
-  int kind, h = 0, j = 0;          // 0: visible unit j, 1: hidden unit h, 2: weight (h, j)
-  if (k < N) { kind = 0; j = k; }
-  else if (k < N + M) { kind = 1; h = k - N; }
-  else { kind = 2; const int q = k - N - M; h = q % M; j = q / M; }
-  const float mean = (float)src.meanO[2 * k + part];
-  const float2* __restrict__ grow = src.g + (size_t)h * Ns;
-  float* xrow = X + (size_t)row * Ns_pad;
-  __nv_bfloat16* brow = reinterpret_cast<__nv_bfloat16*>(X) + (size_t)row * Ns_pad;
-  float* lrow = Xlo ? Xlo + (size_t)row * Ns_pad : nullptr;
-  for (int s0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4; s0 < Ns_pad; s0 += gridDim.x * blockDim.x * 4) {
-    float v[4];
+  const int s0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (s0 >= Ns_pad) return;
+  uint64_t bits[4];
+  float2 g[4];
+  bool valid[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int s = s0 + e;
+    valid[e] = s < Ns;
+    bits[e] = valid[e] ? src.samples[s] : 0ull;
+    g[e] = (valid[e] && u < M) ? src.g[(size_t)u * Ns + s] : make_float2(0.f, 0.f);
+  }
+  float vr[4], vi[4];
+  if (u == M) {
+    for (int j = 0; j < N; ++j) {
+      const float mr = (float)src.meanO[2 * j], mi = (float)src.meanO[2 * j + 1];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        vr[e] = valid[e] ? site_valuef(bits[e], j, hilb) - mr : 0.f;
+        vi[e] = valid[e] ? 0.f - mi : 0.f;
+      }
+      put_x_row<BF16>(X, Xlo, 2 * j, Ns_pad, s0, vr);
+      put_x_row<BF16>(X, Xlo, 2 * j + 1, Ns_pad, s0, vi);
+    }
+    return;
+  }
+  const int h = u;
+  {
+    const int k = N + h;
+    const float mr = (float)src.meanO[2 * k], mi = (float)src.meanO[2 * k + 1];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int s = s0 + e;
-      float val = 0.f;
-      if (s < Ns) {
-        float ox, oy;
-        if (kind == 0) {
-          ox = site_valuef(src.samples[s], j, hilb);
-          oy = 0.f;
-        } else {
-          const float2 g = grow[s];
-          const float w = kind == 2 ? site_valuef(src.samples[s], j, hilb) : 1.f;
-          ox = g.x * w;
-          oy = g.y * w;
-        }
-        val = (part ? oy : ox) - mean;
-      }
-      v[e] = val;
+      vr[e] = valid[e] ? g[e].x - mr : 0.f;
+      vi[e] = valid[e] ? g[e].y - mi : 0.f;
     }
-    if (BF16) {
-      __align__(8) __nv_bfloat16 b[4];
+    put_x_row<BF16>(X, Xlo, 2 * k, Ns_pad, s0, vr);
+    put_x_row<BF16>(X, Xlo, 2 * k + 1, Ns_pad, s0, vi);
+  }
+  for (int j = 0; j < N; ++j) {
+    const int k = N + M + j * M + h;
+    const float mr = (float)src.meanO[2 * k], mi = (float)src.meanO[2 * k + 1];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) b[e] = __float2bfloat16_rn(v[e]);
-      *reinterpret_cast<uint2*>(brow + s0) = *reinterpret_cast<const uint2*>(b);
-    } else {
-      const float4 hi = make_float4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
-      *reinterpret_cast<float4*>(xrow + s0) = hi;
-      if (lrow)
-        *reinterpret_cast<float4*>(lrow + s0) =
-            make_float4(to_tf32(v[0] - hi.x), to_tf32(v[1] - hi.y), to_tf32(v[2] - hi.z), to_tf32(v[3] - hi.w));
+    for (int e = 0; e < 4; ++e) {
+      const float w = site_valuef(bits[e], j, hilb);
+      vr[e] = valid[e] ? g[e].x * w - mr : 0.f;
+      vi[e] = valid[e] ? g[e].y * w - mi : 0.f;
     }
+    put_x_row<BF16>(X, Xlo, 2 * k, Ns_pad, s0, vr);
+    put_x_row<BF16>(X, Xlo, 2 * k + 1, Ns_pad, s0, vi);
   }
 }
 
@@ -402,12 +429,11 @@ cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float*
 
 cudaError_t launch_build_X(const RbmOSource& src, int P, int Ns_pad, float* X, float* Xlo,
                            cudaStream_t st, int bf16) {
-  if (Ns_pad % 4 != 0 || 2 * P > 65535) return cudaErrorInvalidValue;
+  if (Ns_pad % 4 != 0 || src.M + 1 > 65535 || P != src.N + src.M + src.N * src.M) return cudaErrorInvalidValue;
   const int per_block = 256 * 4;
-  const int bx = std::min((Ns_pad + per_block - 1) / per_block, 64);
-  const dim3 grid((unsigned)bx, (unsigned)(2 * P));
-  if (bf16) build_X_kernel<true><<<grid, 256, 0, st>>>(src, 2 * P, Ns_pad, X, nullptr);
-  else build_X_kernel<false><<<grid, 256, 0, st>>>(src, 2 * P, Ns_pad, X, Xlo);
+  const dim3 grid((unsigned)((Ns_pad + per_block - 1) / per_block), (unsigned)(src.M + 1));
+  if (bf16) build_X_kernel<true><<<grid, 256, 0, st>>>(src, Ns_pad, X, nullptr);
+  else build_X_kernel<false><<<grid, 256, 0, st>>>(src, Ns_pad, X, Xlo);
   return cudaGetLastError();
 }
 

@@ -61,14 +61,24 @@ __device__ __forceinline__ void block_coords(int p, int nj, int* ti, int* J) {
 // chunk range of k-split y: [y * per, min(nch, (y + 1) * per))
 __device__ __forceinline__ int item_chunks(int y, int per, int nch) { return min(nch, (y + 1) * per) - y * per; }
 
+// Operand kinds of the Gram kernel; everything that depends on the kind (ring
+// depth, boxes per stage, MMA kind and count) is a compile-time constant, as
+// are the stage indices: a runtime kind branch and a runtime modulo in the
+// issuing thread's loop measurably slowed the MMA issue on GB300.
+enum GramKind { GRAM_TF32 = 0, GRAM_TF32X3 = 1, GRAM_BF16 = 2 };
+
+template <int KIND>
 __global__ void __launch_bounds__(THREADS, 1)
 gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap xlomap,
-                 int split3, int bf16, int stages, int nj, int nblocks, int nch, int per, int items,
-                 float* __restrict__ slots, int* __restrict__ err) {
+                 int nj, int nblocks, int nch, int per, int items, float* __restrict__ slots,
+                 int* __restrict__ err) {
+  constexpr bool split3 = KIND == GRAM_TF32X3;
+  constexpr bool bf16 = KIND == GRAM_BF16;
+  constexpr int stages = split3 ? 2 : 4;
   extern __shared__ unsigned char smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int nbox = split3 ? 6 : 3;          // [B0 B1 A] (+ [B0lo B1lo Alo])
-  const size_t stage_bytes = (size_t)nbox * TILE_BYTES;
+  constexpr int nbox = split3 ? 6 : 3;      // [B0 B1 A] (+ [B0lo B1lo Alo])
+  constexpr uint32_t stage_bytes = (uint32_t)nbox * TILE_BYTES;
   uint8_t* ring = base;
   uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)stages * stage_bytes);
   uint64_t* empty = full + stages;
@@ -140,7 +150,10 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
   } else if (warp == NDRAIN + 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      const uint32_t idesc = idesc_f32acc(bf16 ? 1u : 2u, (uint32_t)TM, (uint32_t)NW);
+      constexpr uint32_t idesc = idesc_f32acc(bf16 ? 1u : 2u, (uint32_t)TM, (uint32_t)NW);
+      // descriptors of the stage buffers: the start-address field counts 16 bytes
+      const uint64_t desc0 = sdesc_k_sw128(smem_u32(ring));
+      constexpr uint64_t desc_stage = stage_bytes >> 4, desc_box = TILE_BYTES >> 4, desc_k = 32 >> 4;
       int k = 0, seg = 0;
       bool stop = false;
       for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
@@ -148,7 +161,7 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
         int ti, J;
         block_coords(q - y * nblocks, nj, &ti, &J);
         const bool a_in_b = first_block(ti) == J;
-        const uint32_t a_off = a_in_b ? (uint32_t)((ti * TM - J * NW) / TM) * TILE_BYTES : 2u * TILE_BYTES;
+        const uint64_t a_off = a_in_b ? (uint64_t)((ti * TM - J * NW) / TM) * desc_box : 2u * desc_box;
         const int n = item_chunks(y, per, nch);
         for (int c = 0; c < n; ++c, ++k) {
           const int b = seg & 1;
@@ -166,27 +179,19 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
             break;
           }
           tc_fence_after();
-          const uint32_t b_hi = smem_u32(ring + (size_t)s * stage_bytes);
-          const uint32_t a_hi = b_hi + a_off;
-          const uint32_t b_lo = b_hi + 3u * TILE_BYTES;
-          const uint32_t a_lo = a_hi + 3u * TILE_BYTES;
+          const uint64_t db = desc0 + (uint64_t)s * desc_stage;
+          const uint64_t da = db + a_off;
           const uint32_t d = tmem + (uint32_t)(b * NW);
-          if (bf16) {
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {         // K = 16 bf16 (32 bytes) per instruction
-              const uint32_t off = kk * 32;
-              mma_f16(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc,
-                      (first && kk == 0) ? 0u : 1u);
-            }
-          } else {
-#pragma unroll
-            for (int kk = 0; kk < KC / 8; ++kk) {    // K = 8 tf32 (32 bytes) per instruction
-              const uint32_t off = kk * 32;
-              mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_hi + off), idesc,
-                       (first && kk == 0) ? 0u : 1u);
+          for (int kk = 0; kk < 4; ++kk) {           // K = 32 bytes per instruction (16 bf16 / 8 tf32)
+            const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+            if (bf16) {
+              mma_f16(d, da + kk * desc_k, db + kk * desc_k, idesc, acc);
+            } else {
+              mma_tf32(d, da + kk * desc_k, db + kk * desc_k, idesc, acc);
               if (split3) {
-                mma_tf32(d, sdesc_k_sw128(a_hi + off), sdesc_k_sw128(b_lo + off), idesc, 1u);
-                mma_tf32(d, sdesc_k_sw128(a_lo + off), sdesc_k_sw128(b_hi + off), idesc, 1u);
+                mma_tf32(d, da + kk * desc_k, db + 3 * desc_box + kk * desc_k, idesc, 1u);
+                mma_tf32(d, da + 3 * desc_box + kk * desc_k, db + kk * desc_k, idesc, 1u);
               }
             }
           }
@@ -377,10 +382,10 @@ cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad
   const GramPlan p = gram_plan(rows, Ns_pad, bf16);
   const int stages = split3 ? 2 : 4;
   const size_t smem = (size_t)stages * (split3 ? 6 : 3) * TILE_BYTES + 1024 + 256;
-  cudaError_t e = cudaFuncSetAttribute(gram_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kernel = split3 ? gram_tf32_kernel<GRAM_TF32X3> : bf16 ? gram_tf32_kernel<GRAM_BF16> : gram_tf32_kernel<GRAM_TF32>;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  gram_tf32_kernel<<<p.ncta, THREADS, smem, st>>>(xmap, xlomap, split3, bf16, stages, p.nj, p.nblocks, p.nch,
-                                                   p.per, p.items, partial, err);
+  kernel<<<p.ncta, THREADS, smem, st>>>(xmap, xlomap, p.nj, p.nblocks, p.nch, p.per, p.items, partial, err);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int tiles = p.nt * (p.nt + 1) / 2;
