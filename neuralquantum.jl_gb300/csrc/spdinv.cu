@@ -12,12 +12,12 @@
 //   W_ik  = C_i (i > k);  W_ki = C_iᴴ (i < k);  W_kk = -piv
 // (Goodnight's sweep operator; every pivot is a Schur complement of A, so it
 // is positive definite and no pivoting is needed).  After all blocks
-// W = -A^-1.  Each step has two phases separated by grid barriers:
-//   A. the CTAs owning a block i != k invert W_kk (32x32 Gauss–Jordan held in
-//      registers, one column group per warp) and store C_i and the old W_ik;
-//   B. every lower tile is either updated or, on row/column k, overwritten.
-// The grid barrier is a generation counter with a bounded spin (1 s, sticky
-// abort flag): a stalled barrier ends the kernel with a status bit.
+// W = -A^-1.  Each step is one phase between grid barriers: the rank-32
+// update of step k runs beside the preparation of step k+1 (its pivot
+// inverse, a 32x32 Gauss–Jordan held in registers, and its C and G), see
+// sweep_group.  The grid barrier is a generation counter with a bounded spin
+// (1 s, sticky abort flag): a stalled barrier ends the kernel with a status
+// bit.
 #include "nq_kernels.cuh"
 #include "tc_common.cuh"
 
@@ -66,59 +66,6 @@ __device__ bool group_barrier(SweepCtl* ctl, unsigned n, int* err) {
 
 NQ_D float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
-// In-place inverse of the Hermitian positive-definite 32x32 block T (shared
-// memory, all 32x32 entries) by Gauss–Jordan without pivoting, 256 threads:
-// lane = row, warp w owns columns 4w..4w+3 in registers.  Per pivot p the
-// owner warp publishes the old column p (double-buffered), row p is taken by
-// shuffles from lane p.  Returns false if a pivot was not positive.
-__device__ bool hpd_inverse_32(float2 (*T)[CB + 1], float2 (*colbuf)[CB]) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float2 a[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) a[q] = T[lane][4 * w + q];
-  bool ok = true;
-#pragma unroll 1
-  for (int p = 0; p < CB; ++p) {
-    if (w == (p >> 2)) {
-      const int oq = p & 3;
-      float2 v = a[0];
-#pragma unroll
-      for (int q = 1; q < 4; ++q)
-        if (q == oq) v = a[q];
-      colbuf[p & 1][lane] = v;
-    }
-    __syncthreads();
-    const float2 f = colbuf[p & 1][lane];
-    float d = colbuf[p & 1][p].x;
-    if (!(d > 0.f)) { ok = false; d = 1.f; }
-    const float inv = 1.0f / d;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int j = 4 * w + q;
-      float2 rp;
-      rp.x = __shfl_sync(0xffffffffu, a[q].x, p);
-      rp.y = __shfl_sync(0xffffffffu, a[q].y, p);
-      if (j == p) {
-        a[q] = lane == p ? make_float2(inv, 0.f) : make_float2(-f.x * inv, -f.y * inv);
-      } else {
-        const float2 np = make_float2(rp.x * inv, rp.y * inv);
-        if (lane == p) {
-          a[q] = np;
-        } else {
-          const float2 t = cmul(f, np);
-          a[q].x -= t.x;
-          a[q].y -= t.y;
-        }
-      }
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < 4; ++q) T[lane][4 * w + q] = a[q];
-  __syncthreads();
-  return ok;
-}
-
 // X[r][c] = Σ_p U[r][p] V[p][c] (mode 0)  or  Σ_p U[r][p] conj(V[c][p]) (mode 1),
 // element (tid & 31, 4 (tid >> 5) + q) per thread
 template <int MODE>
@@ -143,89 +90,263 @@ NQ_D void tile_mm(const float2 (*U)[CB + 1], const float2 (*V)[CB + 1], float2 o
   }
 }
 
+NQ_D void bar_sync_128(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+// In-place inverse of the Hermitian positive-definite 32x32 block T by
+// Gauss–Jordan without pivoting, run by warps 0-3 only (128 threads, named
+// barrier 1): lane = row, warp w holds columns 8w..8w+7 in registers.  Per
+// pivot p the owner warp publishes the old column p (double-buffered), row p
+// is taken by shuffles from lane p; the pivot loop is unrolled so every
+// register index is static.  Same arithmetic per element as a plain
+// Gauss–Jordan sweep; 1/d is the correctly rounded reciprocal.  Returns false
+// if a pivot was not positive.
+NQ_D bool hpd_inverse_32_w4(float2 (*T)[CB + 1], float2 (*colbuf)[CB]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float2 a[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) a[q] = T[lane][8 * w + q];
+  bool ok = true;
+#pragma unroll
+  for (int p = 0; p < CB; ++p) {
+    if (w == (p >> 3)) colbuf[p & 1][lane] = a[p & 7];
+    bar_sync_128(1);
+    const float2 f = colbuf[p & 1][lane];
+    float d = colbuf[p & 1][p].x;
+    if (!(d > 0.f)) { ok = false; d = 1.f; }
+    const float inv = __frcp_rn(d);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int j = 8 * w + q;
+      float2 rp;
+      rp.x = __shfl_sync(0xffffffffu, a[q].x, p);
+      rp.y = __shfl_sync(0xffffffffu, a[q].y, p);
+      if (j == p) {
+        a[q] = lane == p ? make_float2(inv, 0.f) : make_float2(-f.x * inv, -f.y * inv);
+      } else {
+        const float2 np = make_float2(rp.x * inv, rp.y * inv);
+        if (lane == p) {
+          a[q] = np;
+        } else {
+          const float2 t = cmul(f, np);
+          a[q].x -= t.x;
+          a[q].y -= t.y;
+        }
+      }
+    }
+  }
+  bar_sync_128(1);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) T[lane][8 * w + q] = a[q];
+  bar_sync_128(1);
+  return ok;
+}
+
+// tile_mm<MODE> for 128 threads t = 0..127: element (t & 31, 8 (t >> 5) + q)
+template <int MODE>
+NQ_D void tile_mm128(const float2 (*U)[CB + 1], const float2 (*V)[CB + 1], int t, float2 out[8]) {
+  const int r = t & 31, cg = (t >> 5) * 8;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = make_float2(0.f, 0.f);
+#pragma unroll 4
+  for (int p = 0; p < CB; ++p) {
+    const float2 u = U[r][p];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float2 v = MODE == 0 ? V[p][cg + q] : V[cg + q][p];
+      if (MODE == 0) {
+        out[q].x += u.x * v.x - u.y * v.y;
+        out[q].y += u.x * v.y + u.y * v.x;
+      } else {
+        out[q].x += u.x * v.x + u.y * v.y;
+        out[q].y += u.y * v.x - u.x * v.y;
+      }
+    }
+  }
+}
+
+// Element (r, c) of block (bi, bj) of the Hermitian matrix held as its stored
+// lower triangle; diagonal entries of a diagonal block are made real, padding
+// outside P is the identity on a diagonal block and zero elsewhere.
+NQ_D float2 herm_block_elem(const float2* __restrict__ W, int P, int bi, int bj, int r, int c) {
+  const int gi = bi * CB + r, gj = bj * CB + c;
+  if (gi >= P || gj >= P) return make_float2(bi == bj && r == c ? 1.f : 0.f, 0.f);
+  float2 v = gi >= gj ? __ldcg(W + (size_t)gi + (size_t)P * gj) : __ldcg(W + (size_t)gj + (size_t)P * gi);
+  if (gi < gj) v.y = -v.y;
+  if (gi == gj) v.y = 0.f;
+  return v;
+}
+
 // The sweep of one matrix by the CTAs rank = 0..nranks-1 of its group.
-NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status, float2* __restrict__ Cbuf,
-                      float2* __restrict__ Gbuf, float2* __restrict__ pivbuf, int rank, int nranks) {
+//
+// Each step k is one phase between grid barriers.  Besides the rank-32
+// update of the tiles off rows/columns k and k+1 and the store of
+// W_kk = -piv_k, the phase prepares step k+1 ("column units", one per block
+// i != k+1): each of them forms the updated pivot tile
+// W_{k+1,k+1} - C_{k+1} G_{k+1}ᴴ and inverts it (redundantly, identically),
+// forms the updated stored tile of (i, k+1) the way the rank-32 update would,
+// and from it G_i and C_i of step k+1, and writes the step-(k+1) value C_i
+// (or C_iᴴ) into W.  C, G and the pivot are double-buffered by step parity.
+// A bootstrap phase does the same for step 0 from the unmodified matrix.  The
+// arithmetic of every stored value is that of the two-phase sweep; one grid
+// barrier per step instead of two, and the serial 32-step pivot inverse runs
+// beside the rank-32 update instead of before it.
+NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status, float2* __restrict__ work,
+                      int rank, int nranks) {
   __shared__ float2 Dt[CB][CB + 1];
   __shared__ float2 Ut[CB][CB + 1];
   __shared__ float2 Vt[CB][CB + 1];
+  __shared__ float2 Xt[CB][CB + 1];
+  __shared__ float2 Yt[CB][CB + 1];
   __shared__ float2 colbuf[2][CB];
   const int nblk = (P + CB - 1) / CB;
+  const size_t tile = (size_t)CB * CB;
+  // [C even | C odd | G even | G odd | piv even | piv odd]
+  auto Cb = [&](int par) { return work + (size_t)par * nblk * tile; };
+  auto Gb = [&](int par) { return work + (size_t)(2 + par) * nblk * tile; };
+  auto Pb = [&](int par) { return work + (size_t)4 * nblk * tile + (size_t)par * tile; };
   const int tr = threadIdx.x & 31, cg = (threadIdx.x >> 5) * 4;
-  for (int kb = 0; kb < nblk; ++kb) {
-    const int k0 = kb * CB, nbk = min(CB, P - k0);
-    // ---------------- phase A: pivot inverse, C_i and the old column ----------------
-    const int ncol = nblk - 1;
-    const bool has_col = rank < ncol;
-    if (has_col || rank == 0) {
-      for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
-        const int r = e & 31, c = e >> 5;
-        float2 v;
-        if (r < nbk && c < nbk) {
-          v = r >= c ? __ldcg(W + (size_t)(k0 + r) + (size_t)P * (k0 + c))
-                     : __ldcg(W + (size_t)(k0 + c) + (size_t)P * (k0 + r));
-          if (r < c) v.y = -v.y;
-          if (r == c) v.y = 0.f;
-        } else {
-          v = make_float2(r == c ? 1.f : 0.f, 0.f);
-        }
-        Dt[r][c] = v;
-      }
+
+  for (int k = -1; k < nblk; ++k) {
+    const int kn = k + 1;                               // pivot block prepared in this phase
+    const bool prep = kn < nblk;
+    const int ncol = prep ? max(nblk - 1, 1) : 0;       // column units (a bare pivot unit if nblk == 1)
+    const int m = nblk - (prep ? 2 : 1);                // blocks left for the rank-32 update
+    const int nreg = k >= 0 ? m * (m + 1) / 2 : 0;
+    const int nlight = k >= 0 ? 1 + nreg : 0;           // pivot store of step k + rank-32 tiles
+    const float2* Cc = k >= 0 ? Cb(k & 1) : nullptr;
+    const float2* Gc = k >= 0 ? Gb(k & 1) : nullptr;
+    const float2* pc = k >= 0 ? Pb(k & 1) : nullptr;
+    float2* Cn = Cb(kn & 1);
+    float2* Gn = Gb(kn & 1);
+    float2* pn = Pb(kn & 1);
+    // heavy units on ranks [0, ncol), light units on the other ranks; with too
+    // few ranks everything is dealt round-robin
+    const bool split = nranks > ncol;
+    const int nunits = ncol + nlight;
+    for (int u0 = split ? (rank < ncol ? rank : ncol + (rank - ncol)) : rank; u0 < nunits;
+         u0 += split ? (rank < ncol ? nunits : nranks - ncol) : nranks) {
+      const int u = u0;
       __syncthreads();
-      const bool ok = hpd_inverse_32(Dt, colbuf);
-      if (!ok && rank == 0 && threadIdx.x == 0) atomicOr(status, 1);
-      if (rank == 0)
-        for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) pivbuf[e] = Dt[e & 31][e >> 5];
-    }
-    for (int b = rank; b < ncol; b += nranks) {
-      const int ib = b < kb ? b : b + 1;
-      const int i0 = ib * CB;
-      __syncthreads();
-      for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
-        const int r = e & 31, c = e >> 5;
-        float2 v = make_float2(0.f, 0.f);
-        if (i0 + r < P && c < nbk) {
-          if (ib > kb) {
-            v = __ldcg(W + (size_t)(i0 + r) + (size_t)P * (k0 + c));
-          } else {
-            v = __ldcg(W + (size_t)(k0 + c) + (size_t)P * (i0 + r));
-            v.y = -v.y;
-          }
-        }
-        Ut[r][c] = v;
-        Gbuf[(size_t)ib * CB * CB + e] = v;
-      }
-      __syncthreads();
-      float2 o[4];
-      tile_mm<0>(Ut, Dt, o);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) Cbuf[(size_t)ib * CB * CB + (cg + q) * CB + tr] = o[q];
-    }
-    if (!group_barrier(ctl, (unsigned)nranks, status)) return;
-    // ---------------- phase B: lower tiles ----------------
-    const int ntiles = nblk * (nblk + 1) / 2;
-    for (int t = rank; t < ntiles; t += nranks) {
-      int ti, tj;
-      {
-        int c = 0, r = t;
-        while (r >= nblk - c) { r -= nblk - c; ++c; }
-        tj = c; ti = c + r;
-      }
-      const int r0 = ti * CB, c0 = tj * CB;
-      __syncthreads();
-      if (ti != kb && tj != kb) {
-        // W_ij -= C_i G_jᴴ
+      if (u < ncol) {
+        // ---------------- column unit: pivot of step kn, then block i ----------------
+        // Warps 0-3 form and invert the pivot of step kn while warps 4-7 form
+        // V = block (i, kn) after step k from the stored tile of (sa, sb).
+        // The tile both need is loaded once: G_kn (Vt) when i > kn, C_kn (Ut)
+        // when i < kn; the other operand of V's product goes to Yt.
+        const int i = nblk == 1 ? 0 : (u < kn ? u : u + 1);
+        const int sa = max(i, kn), sb = min(i, kn);
+        const bool v_from_c = k >= 0 && i == k;          // stored (kn, k) after step k is C_kn
+        const bool v_update = k >= 0 && nblk > 1 && !v_from_c;
         for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
           const int r = e & 31, c = e >> 5;
-          Ut[r][c] = __ldcg(Cbuf + (size_t)ti * CB * CB + e);
-          Vt[r][c] = __ldcg(Gbuf + (size_t)tj * CB * CB + e);
+          Dt[r][c] = herm_block_elem(W, P, kn, kn, r, c);
+          if (k >= 0) {
+            Ut[r][c] = __ldcg(Cc + (size_t)kn * tile + e);
+            Vt[r][c] = __ldcg(Gc + (size_t)kn * tile + e);
+          }
+          if (nblk > 1) {
+            const int gi = sa * CB + r, gj = sb * CB + c;
+            Xt[r][c] = v_from_c ? __ldcg(Cc + (size_t)kn * tile + e)
+                                : (gi < P && gj < P) ? __ldcg(W + (size_t)gi + (size_t)P * gj) : make_float2(0.f, 0.f);
+            if (v_update) Yt[r][c] = __ldcg(i > kn ? Cc + (size_t)sa * tile + e : Gc + (size_t)sb * tile + e);
+          }
+        }
+        __syncthreads();
+        bool ok = true;
+        if (threadIdx.x < 128) {
+          if (k >= 0) {
+            // updated pivot tile (stored lower) W_kn,kn - C_kn G_knᴴ, mirrored
+            float2 o[8];
+            tile_mm128<1>(Ut, Vt, threadIdx.x, o);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int r = threadIdx.x & 31, c = (threadIdx.x >> 5) * 8 + q, gi = kn * CB + r, gj = kn * CB + c;
+              if (gi < P && gj < P && r >= c) {
+                const float2 w = __ldcg(W + (size_t)gi + (size_t)P * gj);
+                Dt[r][c] = make_float2(w.x - o[q].x, r == c ? 0.f : w.y - o[q].y);
+              }
+            }
+            bar_sync_128(1);
+            for (int e = threadIdx.x; e < CB * CB; e += 128) {
+              const int r = e & 31, c = e >> 5;
+              if (r < c && kn * CB + c < P) Dt[r][c] = make_float2(Dt[c][r].x, -Dt[c][r].y);
+            }
+            bar_sync_128(1);
+          }
+          ok = hpd_inverse_32_w4(Dt, colbuf);
+        } else if (v_update) {
+          // V = stored (sa, sb) - C_sa G_sbᴴ (the rank-32 update of that tile)
+          float2 o[8];
+          tile_mm128<1>(i > kn ? Yt : Ut, i > kn ? Vt : Yt, threadIdx.x - 128, o);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int r = threadIdx.x & 31, c = ((threadIdx.x - 128) >> 5) * 8 + q;
+            if (sa * CB + r < P && sb * CB + c < P) {
+              Xt[r][c].x -= o[q].x;
+              Xt[r][c].y -= o[q].y;
+            }
+          }
+        }
+        __syncthreads();
+        if (u == 0) {
+          if (!ok && threadIdx.x == 0) atomicOr(status, 1);
+          for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) pn[e] = Dt[e & 31][e >> 5];
+        }
+        if (nblk == 1) continue;
+        // G_i = V (column-major), V into Ut for the product
+        for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+          const int r = e & 31, c = e >> 5;
+          float2 v = make_float2(0.f, 0.f);
+          if (i * CB + r < P && kn * CB + c < P) {
+            if (i > kn) v = Xt[r][c];
+            else v = make_float2(Xt[c][r].x, -Xt[c][r].y);
+          }
+          Ut[r][c] = v;
+          Gn[(size_t)i * tile + e] = v;
+        }
+        __syncthreads();
+        float2 o[4];
+        tile_mm<0>(Ut, Dt, o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int c = cg + q;
+          Cn[(size_t)i * tile + c * CB + tr] = o[q];
+          // step-kn value of W on row/column kn: W_{i,kn} = C_i (i > kn), W_{kn,i} = C_iᴴ (i < kn)
+          if (i > kn) {
+            const int gi = i * CB + tr, gj = kn * CB + c;
+            if (gi < P && gj < P) W[(size_t)gi + (size_t)P * gj] = o[q];
+          } else {
+            const int gi = kn * CB + c, gj = i * CB + tr;
+            if (gi < P && gj < P) W[(size_t)gi + (size_t)P * gj] = make_float2(o[q].x, -o[q].y);
+          }
+        }
+      } else if (u == ncol) {
+        // ---------------- W_kk = -piv_k ----------------
+        for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+          const int r = e & 31, c = e >> 5, gi = k * CB + r, gj = k * CB + c;
+          if (gi < P && gj < P && gi >= gj) {
+            const float2 v = __ldcg(pc + e);
+            W[(size_t)gi + (size_t)P * gj] = make_float2(-v.x, -v.y);
+          }
+        }
+      } else {
+        // ---------------- rank-32 update of a tile off rows/columns k, kn ----------------
+        int c0 = 0, rr = u - ncol - 1;
+        while (rr >= m - c0) { rr -= m - c0; ++c0; }
+        int ti = c0 + rr, tj = c0;
+        ti += ti >= k ? (prep ? 2 : 1) : 0;
+        tj += tj >= k ? (prep ? 2 : 1) : 0;
+        for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+          const int r = e & 31, c = e >> 5;
+          Ut[r][c] = __ldcg(Cc + (size_t)ti * tile + e);
+          Vt[r][c] = __ldcg(Gc + (size_t)tj * tile + e);
         }
         __syncthreads();
         float2 o[4];
         tile_mm<1>(Ut, Vt, o);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const int gi = r0 + tr, gj = c0 + cg + q;
+          const int gi = ti * CB + tr, gj = tj * CB + cg + q;
           if (gi < P && gj < P && gi >= gj) {
             float2* a = W + (size_t)gi + (size_t)P * gj;
             float2 cur = __ldcg(a);
@@ -234,40 +355,20 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
             *a = cur;
           }
         }
-      } else {
-        // row/column k: W_ik = C_i (i > k), W_kj = C_jᴴ (j < k), W_kk = -piv
-        for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
-          const int r = e & 31, c = e >> 5;
-          const int gi = r0 + r, gj = c0 + c;
-          if (gi >= P || gj >= P || gi < gj) continue;
-          float2 v;
-          if (ti == kb && tj == kb) {
-            v = __ldcg(pivbuf + e);
-            v.x = -v.x;
-            v.y = -v.y;
-          } else if (tj == kb) {
-            v = __ldcg(Cbuf + (size_t)ti * CB * CB + e);
-          } else {
-            v = __ldcg(Cbuf + (size_t)tj * CB * CB + r * CB + c);   // (C_j)ᴴ[r][c] = conj(C_j[c][r])
-            v.y = -v.y;
-          }
-          W[(size_t)gi + (size_t)P * gj] = v;
-        }
       }
     }
-    if (!group_barrier(ctl, (unsigned)nranks, status)) return;
+    if (k + 1 < nblk && !group_barrier(ctl, (unsigned)nranks, status)) return;
   }
 }
 
-__global__ void __launch_bounds__(256) sweep_coop_kernel(float2* __restrict__ W, int P, SweepCtl* ctl,
-                                                         int* status, float2* __restrict__ Cbuf,
-                                                         float2* __restrict__ Gbuf, float2* __restrict__ pivbuf) {
-  sweep_group(W, P, ctl, status, Cbuf, Gbuf, pivbuf, blockIdx.x, gridDim.x);
+__global__ void __launch_bounds__(256, 2) sweep_coop_kernel(float2* __restrict__ W, int P, SweepCtl* ctl,
+                                                         int* status, float2* __restrict__ work) {
+  sweep_group(W, P, ctl, status, work, blockIdx.x, gridDim.x);
 }
 
 // Many matrices in one cooperative launch: matrix p is swept by CTAs
 // [cta_start[p], cta_start[p+1]) with its own barrier block.
-__global__ void __launch_bounds__(256) sweep_batch_kernel(const SweepJob* __restrict__ jobs,
+__global__ void __launch_bounds__(256, 2) sweep_batch_kernel(const SweepJob* __restrict__ jobs,
                                                           const int* __restrict__ cta_start, int np) {
   int lo = 0, hi = np - 1;
   const int b = blockIdx.x;
@@ -277,9 +378,7 @@ __global__ void __launch_bounds__(256) sweep_batch_kernel(const SweepJob* __rest
   }
   const SweepJob& j = jobs[lo];
   const int r0 = __ldg(cta_start + lo), n = __ldg(cta_start + lo + 1) - r0;
-  sweep_group(j.W, j.P, reinterpret_cast<SweepCtl*>(j.ctl), j.status, j.work,
-              j.work + (size_t)((j.P + CB - 1) / CB) * CB * CB, j.work + (size_t)2 * ((j.P + CB - 1) / CB) * CB * CB,
-              b - r0, n);
+  sweep_group(j.W, j.P, reinterpret_cast<SweepCtl*>(j.ctl), j.status, j.work, b - r0, n);
 }
 
 // W upper = conj(W lower) so that column i holds row i of the Hermitian matrix
@@ -327,7 +426,8 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
 }  // namespace
 
 size_t sweep_ctl_bytes() { return sizeof(SweepCtl); }
-size_t sweep_work_elems(int P) { return (size_t)(2 * ((P + CB - 1) / CB) + 1) * CB * CB; }
+// C and G of every block and the pivot inverse, each twice (step parity)
+size_t sweep_work_elems(int P) { return (size_t)(4 * ((P + CB - 1) / CB) + 2) * CB * CB; }
 
 cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st) {
   static int grid = 0;
@@ -347,10 +447,6 @@ cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2*
   }
   cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(SweepCtl), st);
   if (e != cudaSuccess) return e;
-  const size_t tile = (size_t)CB * CB, nblk = (size_t)(P + CB - 1) / CB;
-  float2* Cbuf = work;
-  float2* Gbuf = work + nblk * tile;
-  float2* pivbuf = work + 2 * nblk * tile;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(256);
@@ -362,7 +458,7 @@ cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2*
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   SweepCtl* c = reinterpret_cast<SweepCtl*>(ctl);
-  return cudaLaunchKernelEx(&cfg, sweep_coop_kernel, W, P, c, status, Cbuf, Gbuf, pivbuf);
+  return cudaLaunchKernelEx(&cfg, sweep_coop_kernel, W, P, c, status, work);
 }
 
 cudaError_t launch_herm_gemv_neg(const float2* W, int P, const float2* x, float2* y, cudaStream_t st) {
