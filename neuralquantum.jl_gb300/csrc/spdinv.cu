@@ -237,8 +237,9 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
         const int sa = max(i, kn), sb = min(i, kn);
         const bool v_from_c = k >= 0 && i == k;          // stored (kn, k) after step k is C_kn
         const bool v_update = k >= 0 && nblk > 1 && !v_from_c;
-        for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
-          const int r = e & 31, c = e >> 5;
+#pragma unroll
+        for (int e0 = 0; e0 < CB * CB; e0 += 256) {
+          const int e = e0 + threadIdx.x, r = e & 31, c = e >> 5;
           Dt[r][c] = herm_block_elem(W, P, kn, kn, r, c);
           if (k >= 0) {
             Ut[r][c] = __ldcg(Cc + (size_t)kn * tile + e);
@@ -252,27 +253,27 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
           }
         }
         __syncthreads();
+        if (k >= 0) {
+          // updated pivot tile W_kn,kn - C_kn G_knᴴ on the stored lower triangle
+          // (the lower part of Dt holds the stored values; the diagonal is
+          // real), then mirrored
+          float2 o[4];
+          tile_mm<1>(Ut, Vt, o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int c = cg + q;
+            if (kn * CB + tr < P && kn * CB + c < P && tr >= c)
+              Dt[tr][c] = make_float2(Dt[tr][c].x - o[q].x, tr == c ? 0.f : Dt[tr][c].y - o[q].y);
+          }
+          __syncthreads();
+          for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) {
+            const int r = e & 31, c = e >> 5;
+            if (r < c && kn * CB + c < P) Dt[r][c] = make_float2(Dt[c][r].x, -Dt[c][r].y);
+          }
+          __syncthreads();
+        }
         bool ok = true;
         if (threadIdx.x < 128) {
-          if (k >= 0) {
-            // updated pivot tile (stored lower) W_kn,kn - C_kn G_knᴴ, mirrored
-            float2 o[8];
-            tile_mm128<1>(Ut, Vt, threadIdx.x, o);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const int r = threadIdx.x & 31, c = (threadIdx.x >> 5) * 8 + q, gi = kn * CB + r, gj = kn * CB + c;
-              if (gi < P && gj < P && r >= c) {
-                const float2 w = __ldcg(W + (size_t)gi + (size_t)P * gj);
-                Dt[r][c] = make_float2(w.x - o[q].x, r == c ? 0.f : w.y - o[q].y);
-              }
-            }
-            bar_sync_128(1);
-            for (int e = threadIdx.x; e < CB * CB; e += 128) {
-              const int r = e & 31, c = e >> 5;
-              if (r < c && kn * CB + c < P) Dt[r][c] = make_float2(Dt[c][r].x, -Dt[c][r].y);
-            }
-            bar_sync_128(1);
-          }
           ok = hpd_inverse_32_w4(Dt, colbuf);
         } else if (v_update) {
           // V = stored (sa, sb) - C_sa G_sbᴴ (the rank-32 update of that tile)
