@@ -103,6 +103,27 @@ template <int ACT, typename R> NQ_D cpx<R> act_f(cpx<R> z) {
   }
 }
 
+// logcosh(z) and tanh(z) together, from e = exp(-2|x|) and sincos(y), z = x + iy:
+//   log cosh z = |x| - log 2 + log1p(e) + log(cos y + i tanh(x) sin y)
+//   tanh x     = sgn(x) (1 - e) / (1 + e)
+//   tanh z     = (sgn(x) (1 - e)(1 + e) + 4i e sin y cos y) / ((1 - e)^2 + 4 e cos^2 y)
+// The last is (sinh 2x + i sin 2y) / (cosh 2x + cos 2y) multiplied by 2e; its
+// denominator is a sum of non-negative terms.  The first is the logℒ2 form of
+// activation.jl:9-13 with log cosh x written without overflow.
+template <typename R> NQ_D void logcosh_tanh(cpx<R> z, cpx<R>* f, cpx<R>* df) {
+  const R ax = r_abs(z.x);
+  const R e = r_exp(R(-2) * ax);
+  R s, c;
+  r_sincos(z.y, &s, &c);
+  const R sg = z.x < R(0) ? R(-1) : R(1);
+  const R ope = R(1) + e, ome = R(1) - e;
+  const R thx = sg * ome / ope;
+  const cpx<R> lw = clogc(mk(c, thx * s));
+  *f = mk(ax - R(0.6931471805599453) + r_log1p(e) + lw.x, lw.y);
+  const R inv = R(1) / (ome * ome + R(4) * e * c * c);
+  *df = mk(sg * ome * ope * inv, R(4) * e * s * c * inv);
+}
+
 // f'(z): tanh or sigmoid of complex z
 template <int ACT, typename R> NQ_D cpx<R> act_df(cpx<R> z) {
   if (ACT == ACT_LOGCOSH) {

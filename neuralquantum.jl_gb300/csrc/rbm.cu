@@ -56,23 +56,42 @@ __global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>*
 // ---------------------------------------------------------------------------
 // theta_in_g: gout already holds θ = Wσ + b ([h][Ns], from the tensor-core
 // contraction); it is read and overwritten with g = f'(θ) by the same thread.
+// p /= |p| into logscale when |p| leaves [1e-10, 1e10]
+template <typename R> NQ_D void rescale(cpx<R>& p, R& logscale) {
+  const R m2 = abs2c(p);
+  if (m2 > R(1e20) || m2 < R(1e-20)) {
+    const R m = sqrt(m2);
+    logscale += r_log(m);
+    p = (R(1) / m) * p;
+  }
+}
+
+// {t0, t1} of one (site, hidden unit), one 16-byte (FP32) shared-memory load
+template <typename R> struct alignas(16) cpx_t01 {
+  cpx<R> t0, t1;
+};
+
 template <typename R, int ACT>
 NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples, int Ns, const DevOp& op,
                      int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
                      cpx<R>* __restrict__ eloc, int blk, int theta_in_g = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = net.N, M = net.M, T = blockDim.x;
-  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(smem_raw);     // [M*N]
+  cpx_t01<R>* s_t01 = reinterpret_cast<cpx_t01<R>*>(smem_raw);  // [N*M] (if has_op)
+  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(s_t01 + (has_op ? N * M : 0));  // [M*N]
   cpx<R>* s_b = s_W + M * N;                              // [M]
   cpx<R>* s_a = s_b + M;                                  // [N]
   cpx<R>* s_g = s_a + N;                                  // [M][T]
-  cpx<R>* s_t0 = s_g + (size_t)M * T;                     // [N*M] (if has_op)
-  cpx<R>* s_t1 = s_t0 + (has_op ? N * M : 0);
   for (int k = threadIdx.x; k < M * N; k += T) s_W[k] = net.W[k];
   for (int k = threadIdx.x; k < M; k += T) s_b[k] = net.b[k];
   for (int k = threadIdx.x; k < N; k += T) s_a[k] = net.a[k];
   if (has_op)
-    for (int k = threadIdx.x; k < N * M; k += T) { s_t0[k] = net.t0[k]; s_t1[k] = net.t1[k]; }
+    for (int k = threadIdx.x; k < N * M; k += T) {
+      cpx_t01<R> t;
+      t.t0 = net.t0[k];
+      t.t1 = net.t1[k];
+      s_t01[k] = t;
+    }
   __syncthreads();
   const int s = blk * T + threadIdx.x;
   if (s >= Ns) return;
@@ -85,22 +104,42 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
     lp.x += s_a[j].x * v;
     lp.y += s_a[j].y * v;
   }
-  for (int h = 0; h < M; ++h) {
-    cpx<R> th;
-    if (theta_in_g) {
-      th = gout[(size_t)h * Ns + s];
-    } else {
-      th = s_b[h];
+  // θ of four hidden units per pass over the sites (one site value per j)
+  for (int h0 = 0; h0 < M; h0 += 4) {
+    cpx<R> th[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int h = h0 + u;
+      th[u] = h < M ? (theta_in_g ? gout[(size_t)h * Ns + s] : s_b[h]) : mk(R(0), R(0));
+    }
+    if (!theta_in_g) {
       for (int j = 0; j < N; ++j) {
-        R v = site_value<R>(bits, j, hilb);
-        th.x += s_W[h + M * j].x * v;
-        th.y += s_W[h + M * j].y * v;
+        const R v = site_value<R>(bits, j, hilb);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (h0 + u < M) {
+            const cpx<R> w = s_W[h0 + u + M * j];
+            th[u].x += w.x * v;
+            th[u].y += w.y * v;
+          }
       }
     }
-    lp = lp + act_f<ACT>(th);
-    cpx<R> gh = act_df<ACT>(th);
-    s_g[h * T + threadIdx.x] = gh;
-    if (gout) gout[(size_t)h * Ns + s] = gh;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int h = h0 + u;
+      if (h < M) {
+        cpx<R> f, gh;
+        if (ACT == ACT_LOGCOSH) {
+          logcosh_tanh(th[u], &f, &gh);
+        } else {
+          f = act_f<ACT>(th[u]);
+          gh = act_df<ACT>(th[u]);
+        }
+        lp = lp + f;
+        s_g[h * T + threadIdx.x] = gh;
+        if (gout) gout[(size_t)h * Ns + s] = gh;
+      }
+    }
   }
   logpsi[s] = lp;
   if (!has_op) return;
@@ -136,26 +175,34 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
       cpx<R> prod = mk(R(1), R(0));
       R logscale = R(0);
       if (nch == 1) {
+        // Π_h (t0 + g t1) over two independent chains (even / odd h),
+        // rescaled every eight units
         const bool pos = dv1 > 0;
-        for (int h = 0; h < M; ++h) {
-          cpx<R> gh = s_g[h * T + threadIdx.x];
-          cpx<R> rr;
-          if (ACT == ACT_LOGCOSH) {
-            cpx<R> t1 = s_t1[i1 * M + h];
-            if (!pos) t1 = mk(-t1.x, -t1.y);
-            rr = cfma(gh, t1, s_t0[i1 * M + h]);
-          } else {
-            cpx<R> bb = pos ? s_t0[i1 * M + h] : s_t1[i1 * M + h];
-            rr = cfma(gh, bb, mk(R(1), R(0)));
+        const cpx_t01<R>* tt = s_t01 + i1 * M;
+        cpx<R> pa = mk(R(1), R(0)), pb = mk(R(1), R(0));
+        for (int h0 = 0; h0 < M; h0 += 8) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int h = h0 + u;
+            if (h < M) {
+              const cpx_t01<R> t = tt[h];
+              const cpx<R> gh = s_g[h * T + threadIdx.x];
+              cpx<R> rr;
+              if (ACT == ACT_LOGCOSH) {
+                cpx<R> c1 = t.t1;
+                if (!pos) c1 = mk(-c1.x, -c1.y);
+                rr = cfma(gh, c1, t.t0);
+              } else {
+                rr = cfma(gh, pos ? t.t0 : t.t1, mk(R(1), R(0)));
+              }
+              if (u & 1) pb = pb * rr;
+              else pa = pa * rr;
+            }
           }
-          prod = prod * rr;
-          R m2 = abs2c(prod);
-          if (m2 > R(1e20) || m2 < R(1e-20)) {
-            R m = sqrt(m2);
-            logscale += r_log(m);
-            prod = (R(1) / m) * prod;
-          }
+          rescale(pa, logscale);
+          rescale(pb, logscale);
         }
+        prod = pa * pb;
       } else {
         for (int h = 0; h < M; ++h) {
           cpx<R> dth = mk(R(0), R(0));
