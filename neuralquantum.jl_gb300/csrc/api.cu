@@ -494,7 +494,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->fb.force, 2 * (size_t)P), "force");
   step(dalloc(&h->fb.meanE, 2), "meanE");
   step(dalloc(&h->d_stats, 8), "stats");
-  step(dalloc(&h->d_chainstats, 3 * (size_t)h->B), "chain stats");
+  step(dalloc(&h->d_chainstats, 3 * (size_t)h->B + 4), "chain stats");
   step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
   h->cg = c.sr_algorithm == NQ_SR_CG;
   const int rows = 2 * P;
@@ -729,7 +729,7 @@ nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* st
   nq_status s = upload_op(h, obs, &d, &allocs);
   if (s != NQ_OK) return cleanup(s);
   if (cudaMalloc(&d_lp, (size_t)h->Ns * csz) != cudaSuccess || cudaMalloc(&d_loc, (size_t)h->Ns * csz) != cudaSuccess ||
-      cudaMalloc((void**)&d_cs, (size_t)h->B * 3 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&d_cs, ((size_t)h->B * 3 + 4) * sizeof(double)) != cudaSuccess ||
       cudaMalloc((void**)&d_st, 8 * sizeof(double)) != cudaSuccess)
     return cleanup(fail(h, NQ_ERR_CUDA, "observable buffers"));
   cudaError_t e;

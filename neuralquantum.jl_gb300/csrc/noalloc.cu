@@ -14,9 +14,10 @@ namespace {
 constexpr int kMaxChains = NQ_NOALLOC_MAX_CHAINS;
 constexpr int kMaxDevices = 64;
 
-// 3 doubles per chain (mean re, mean im, variance); 1.5 MiB per device.
-// Every word a call reads is written earlier in the same call, so nothing has
-// to start at zero.
+// Scratch of the statistics kernels (4 doubles per 64 chains; sized by the
+// 3B + 4 bound that launch_stats documents, 1.5 MiB per device).  Every word
+// a call reads is written earlier in the same call, so nothing has to start
+// at zero.
 static __device__ __align__(256) double g_chain_scratch[3 * kMaxChains];
 
 std::mutex g_mu;

@@ -127,12 +127,15 @@ template <typename R> NQ_D void logcosh_tanh(cpx<R> z, cpx<R>* f, cpx<R>* df) {
 // f'(z): tanh or sigmoid of complex z
 template <int ACT, typename R> NQ_D cpx<R> act_df(cpx<R> z) {
   if (ACT == ACT_LOGCOSH) {
-    // tanh(x+iy) = (sinh 2x + i sin 2y) / (cosh 2x + cos 2y)
-    if (r_abs(z.x) > R(20)) return mk(z.x > 0 ? R(1) : R(-1), R(0));
-    R s2, c2;
-    r_sincos(R(2) * z.y, &s2, &c2);
-    R den = r_cosh(R(2) * z.x) + c2;
-    return mk(r_sinh(R(2) * z.x) / den, s2 / den);
+    // tanh z = (sgn(x) (1 - e)(1 + e) + 4i e sin y cos y) / ((1 - e)^2 + 4 e cos^2 y),
+    // e = exp(-2|x|): (sinh 2x + i sin 2y) / (cosh 2x + cos 2y) multiplied by 2e
+    const R e = r_exp(R(-2) * r_abs(z.x));
+    R s, c;
+    r_sincos(z.y, &s, &c);
+    const R sg = z.x < R(0) ? R(-1) : R(1);
+    const R ope = R(1) + e, ome = R(1) - e;
+    const R inv = R(1) / (ome * ome + R(4) * e * c * c);
+    return mk(sg * ome * ope * inv, R(4) * e * s * c * inv);
   } else {
     // 1 / (1 + exp(-z))
     if (z.x < R(-30)) return cexpc(z);

@@ -240,7 +240,8 @@ cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float*
 
 // Measurement statistics (stats.jl:26-50) of a chains x samples matrix stored
 // sample-major (value index s = chain + B*slot); mode 0: complex values,
-// mode 1: |value|^2 (the Liouvillian cost).
+// mode 1: |value|^2 (the Liouvillian cost).  chain_scratch: 4 ceil(B/64)
+// doubles (at most 3B + 4).
 template <typename R>
 cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* chain_scratch,
                          double* out6, cudaStream_t st);

@@ -441,10 +441,11 @@ cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2*
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_coop_kernel, 256, 0);
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorCooperativeLaunchTooLarge;
-    // two CTAs per SM where they fit: phase B has ~nblk^2/2 tiles per step, and
-    // a second resident CTA halves the tiles per CTA (co-residency of every
-    // CTA is guaranteed by the cooperative launch)
-    grid = sms * (per >= 2 ? 2 : 1);
+    // one CTA per SM: the step time is the column units' (pivot inverse and
+    // tile products), which run 20-25% faster without a second CTA on the SM
+    // than the rank-32 update gains from one (measured: 0.46 vs 0.57 ms for
+    // P = 860)
+    grid = sms;
   }
   cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(SweepCtl), st);
   if (e != cudaSuccess) return e;

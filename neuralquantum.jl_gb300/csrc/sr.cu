@@ -323,72 +323,59 @@ __device__ __forceinline__ cpx<double> stat_val(const cpx<R>* v, long i, int mod
   return mk((double)a.x, (double)a.y);
 }
 
-__device__ void block_sum2(double& a, double& b, double* sh) {
-  for (int off = 16; off > 0; off >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, off);
-    b += __shfl_xor_sync(0xffffffffu, b, off);
-  }
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) { sh[2 * w] = a; sh[2 * w + 1] = b; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double x = 0, y = 0;
-    for (int i = 0; i < nw; ++i) { x += sh[2 * i]; y += sh[2 * i + 1]; }
-    sh[64] = x; sh[65] = y;
-  }
-  __syncthreads();
-  a = sh[64]; b = sh[65];
-}
 
 // pass 1 (one thread per chain): chain mean μ_c and unbiased variance var_c
 template <typename R>
-__global__ void chain_stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
-                                   double* __restrict__ cs) {
+__global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
+                                                         double* __restrict__ part) {
+  // per chain (one thread): μ_c and var_c (two passes over its L values);
+  // per block (64 chains, fixed shuffle/smem order): Σ Re μ_c, Σ Im μ_c,
+  // Σ var_c, Σ |μ_c|² into part[4 blockIdx.x ..]
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= B) return;
-  double mx = 0, my = 0;
-  for (int l = 0; l < L; ++l) { cpx<double> x = stat_val(v, c + (long)B * l, mode); mx += x.x; my += x.y; }
-  mx /= L; my /= L;
-  double vv = 0;
-  for (int l = 0; l < L; ++l) {
-    cpx<double> x = stat_val(v, c + (long)B * l, mode);
-    vv += (x.x - mx) * (x.x - mx) + (x.y - my) * (x.y - my);
+  double mx = 0, my = 0, var = 0;
+  if (c < B) {
+    for (int l = 0; l < L; ++l) { cpx<double> x = stat_val(v, c + (long)B * l, mode); mx += x.x; my += x.y; }
+    mx /= L; my /= L;
+    double vv = 0;
+    for (int l = 0; l < L; ++l) {
+      cpx<double> x = stat_val(v, c + (long)B * l, mode);
+      vv += (x.x - mx) * (x.x - mx) + (x.y - my) * (x.y - my);
+    }
+    var = L > 1 ? vv / (L - 1) : 0.0;
   }
-  cs[3 * c] = mx;
-  cs[3 * c + 1] = my;
-  cs[3 * c + 2] = L > 1 ? vv / (L - 1) : 0.0;
+  double q[4] = {mx, my, var, mx * mx + my * my};
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    for (int off = 16; off > 0; off >>= 1) q[k] += __shfl_xor_sync(0xffffffffu, q[k], off);
+  __shared__ double sh[2][4];
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 4; ++k) sh[threadIdx.x >> 5][k] = q[k];
+  __syncthreads();
+  if (threadIdx.x < 4) part[4 * blockIdx.x + threadIdx.x] = sh[0][threadIdx.x] + sh[1][threadIdx.x];
 }
 
-// pass 2 (one block): μ = mean μ_c; var_μ_ch = Σ|μ_c-μ|²/(B-1);
-// var_μ = Σ_c[(L-1) var_c + L|μ_c-μ|²]/(BL-1) (= var of all values about μ);
+// pass 2 (one warp, fixed order): μ = Σμ_c / B;
+// Σ|μ_c-μ|² = Σ|μ_c|² - B|μ|²; var_μ_ch = Σ|μ_c-μ|²/(B-1);
+// var_μ = [(L-1) Σ var_c + L Σ|μ_c-μ|²]/(BL-1) (= var of all values about μ);
 // variance = mean var_c; t = var_μ_ch/var_μ (stats.jl:26-50)
-__global__ void __launch_bounds__(1024) stats_final_kernel(const double* __restrict__ cs, int B, int L,
-                                                           double* __restrict__ out) {
-  __shared__ double sh[66];
-  double smx = 0, smy = 0, svar = 0, dummy = 0;
-  for (int c = threadIdx.x; c < B; c += blockDim.x) {
-    smx += cs[3 * c]; smy += cs[3 * c + 1]; svar += cs[3 * c + 2];
-  }
-  block_sum2(smx, smy, sh);
-  block_sum2(svar, dummy, sh);
-  const double mux = smx / B, muy = smy / B;
-  double vmc = 0, vall = 0;
-  for (int c = threadIdx.x; c < B; c += blockDim.x) {
-    const double dx = cs[3 * c] - mux, dy = cs[3 * c + 1] - muy;
-    const double d2 = dx * dx + dy * dy;
-    vmc += d2;
-    vall += (L - 1) * cs[3 * c + 2] + L * d2;
-  }
-  block_sum2(vmc, vall, sh);
+__global__ void __launch_bounds__(32) stats_final_kernel(const double* __restrict__ part, int nblk, int B, int L,
+                                                         double* __restrict__ out) {
+  double q[4] = {0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblk; b += 32)
+    for (int k = 0; k < 4; ++k) q[k] += part[4 * b + k];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    for (int off = 16; off > 0; off >>= 1) q[k] += __shfl_xor_sync(0xffffffffu, q[k], off);
   if (threadIdx.x == 0) {
-    const double var_mu_ch = vmc / (B - 1);
-    const double var_mu = vall / ((double)B * L - 1);
+    const double mux = q[0] / B, muy = q[1] / B;
+    const double dev = fmax(0.0, q[3] - B * (mux * mux + muy * muy));   // Σ|μ_c - μ|²
+    const double var_mu_ch = dev / (B - 1);
+    const double var_mu = ((L - 1) * q[2] + L * dev) / ((double)B * L - 1);
     const double t = var_mu_ch / var_mu;
     out[0] = mux;
     out[1] = muy;
     out[2] = sqrt(var_mu_ch / B);
-    out[3] = svar / B;
+    out[3] = q[2] / B;
     out[4] = fmax(0.0, 0.5 * (t * L - 1.0));
     out[5] = sqrt((double)(L - 1) / L + t);
   }
@@ -499,8 +486,9 @@ cudaError_t launch_descent(double* master, const double* dw, long n_doubles, int
 template <typename R>
 cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* chain_scratch, double* out6,
                          cudaStream_t st) {
-  chain_stats_kernel<R><<<(B + 255) / 256, 256, 0, st>>>(vals, B, L, mode, chain_scratch);
-  stats_final_kernel<<<1, 1024, 0, st>>>(chain_scratch, B, L, out6);
+  const int nblk = (B + 63) / 64;
+  chain_stats_kernel<R><<<nblk, 64, 0, st>>>(vals, B, L, mode, chain_scratch);
+  stats_final_kernel<<<1, 32, 0, st>>>(chain_scratch, nblk, B, L, out6);
   return cudaGetLastError();
 }
 template cudaError_t launch_stats<float>(const cpx<float>*, int, int, int, double*, double*, cudaStream_t);
