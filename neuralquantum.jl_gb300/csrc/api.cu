@@ -79,7 +79,7 @@ nq_status ensure_tuned(nq_handle* h) {
     }
   }
   int cand[4];
-  int nc = rbm_sampler_valid_lanes(sM, cand, 4);
+  int nc = rbm_sampler_valid_lanes(h->ndm ? h->N2 : h->N, sM, h->f64 ? 16 : 8, cand, 4);
   if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", sM);
   if (h->sampler_lanes) { cand[0] = h->sampler_lanes; nc = 1; }     // fixed by the caller
   const int blocks[3] = {64, 128, 256};
@@ -454,7 +454,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   const int sampler_M = h->ndm ? h->Ms : h->M, sampler_N = h->ndm ? h->N2 : h->N;
   if (c.sampler_lanes != 0) {
     int cand[4];
-    const int nc = rbm_sampler_valid_lanes(sampler_M, cand, 4);
+    const int nc = rbm_sampler_valid_lanes(sampler_N, sampler_M, h->f64 ? 16 : 8, cand, 4);
     bool ok = false;
     for (int i = 0; i < nc; ++i) ok = ok || cand[i] == c.sampler_lanes;
     if (!ok) return bad("sampler_lanes not available for this number of hidden units");
@@ -1223,9 +1223,12 @@ nq_status batch_build_tables(nq_batch* b) {
 nq_status batch_tune(nq_batch* b) {
   if (b->lanes) return NQ_OK;
   int cand[4];
-  int M_max = 0;
-  for (nq_handle* h : b->hs) M_max = std::max(M_max, h->M);
-  const int nc = rbm_sampler_valid_lanes(M_max, cand, 4);
+  int M_max = 0, N_max = 0;
+  for (nq_handle* h : b->hs) {
+    M_max = std::max(M_max, h->M);
+    N_max = std::max(N_max, h->N);
+  }
+  const int nc = rbm_sampler_valid_lanes(N_max, M_max, 8, cand, 4);
   if (nc == 0) return bfail(b, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", M_max);
   cudaEvent_t e0, e1;
   BCK(cudaEventCreate(&e0));

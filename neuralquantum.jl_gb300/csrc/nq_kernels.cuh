@@ -55,7 +55,7 @@ struct SamplerRun {
 // values instantiated for M hidden units (used by the autotuner).
 template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
-int rbm_sampler_valid_lanes(int M, int* out, int max_out);
+int rbm_sampler_valid_lanes(int N, int M, int csize, int* out, int max_out);
 
 // Many independent problems in one sampler launch (FP32): problem p runs on
 // blocks [blk_start[p], blk_start[p+1]) of 256 threads (256/G chains each);

@@ -33,20 +33,32 @@ template <typename R> struct alignas(4 * sizeof(R)) cpx_pair {
 // One block of the sampler: chains (blk * blockDim + tid) / G of the problem
 // described by (net, run).  Shared by the single-problem kernel and the
 // many-problem kernel below.
+// Hidden units are padded to MP = G*HPL with neutral table entries (ratio
+// factor 1, no θ change), so the proposal and accept loops have no unit-range
+// branches.
 template <typename R, int G, int HPL, int ACT>
 NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int MP = G * HPL;
   const int N = net.N, M = net.M, n_half = net.n_half;
-  cpx_pair<R>* s_t01 = reinterpret_cast<cpx_pair<R>*>(smem_raw);   // {t0, t1} at i*M + h
-  cpx_pair<R>* s_t2w = s_t01 + N * M;                             // {t2, W[h, i]} at i*M + h
-  R* s_are = reinterpret_cast<R*>(s_t2w + N * M);                 // 2 Re a_i log2(e)
-  for (int k = threadIdx.x; k < N * M; k += blockDim.x) {
-    const int i = k / M, h = k % M;
+  cpx_pair<R>* s_t01 = reinterpret_cast<cpx_pair<R>*>(smem_raw);   // {t0, t1} at i*MP + h
+  cpx_pair<R>* s_t2w = s_t01 + N * MP;                            // {t2, W[h, i]} at i*MP + h
+  R* s_are = reinterpret_cast<R*>(s_t2w + N * MP);                // 2 Re a_i log2(e)
+  for (int k = threadIdx.x; k < N * MP; k += blockDim.x) {
+    const int i = k / MP, h = k % MP;
     cpx_pair<R> p01, p2w;
-    p01.a = net.t0[k];
-    p01.b = net.t1[k];
-    p2w.a = ACT == ACT_LOGCOSH ? net.t2[k] : mk(R(0), R(0));
-    p2w.b = net.W[h + M * i];
+    if (h < M) {
+      p01.a = net.t0[i * M + h];
+      p01.b = net.t1[i * M + h];
+      p2w.a = ACT == ACT_LOGCOSH ? net.t2[i * M + h] : mk(R(0), R(0));
+      p2w.b = net.W[h + M * i];
+    } else {
+      // logcosh: t0 + g t1 = 1; softplus: 1 + g t0 = 1; accepted flip: θ, g unchanged
+      p01.a = ACT == ACT_LOGCOSH ? mk(R(1), R(0)) : mk(R(0), R(0));
+      p01.b = mk(R(0), R(0));
+      p2w.a = mk(R(0), R(0));
+      p2w.b = mk(R(0), R(0));
+    }
     s_t01[k] = p01;
     s_t2w[k] = p2w;
   }
@@ -71,23 +83,22 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   }
 
   cpx<R> th[HPL], g[HPL];
+  bool half[HPL];
 #pragma unroll
   for (int k = 0; k < HPL; ++k) {
     const int h = lane + G * k;
-    th[k] = mk(R(0), R(0));
-    g[k] = mk(R(0), R(0));
-    if (h < M) {
-      cpx<R> t = net.b[h];
-      for (int j = 0; j < N; ++j) {
-        const R v = site_value<R>(bits, j, hilb);
-        const cpx<R> w = s_t2w[j * M + h].b;
-        t.x += w.x * v;
-        t.y += w.y * v;
-      }
-      th[k] = t;
-      g[k] = act_df<ACT>(t);
+    half[k] = h < n_half;
+    cpx<R> t = h < M ? net.b[h] : mk(R(0), R(0));
+    for (int j = 0; j < N; ++j) {
+      const R v = site_value<R>(bits, j, hilb);
+      const cpx<R> w = s_t2w[j * MP + h].b;
+      t.x += w.x * v;
+      t.y += w.y * v;
     }
+    th[k] = t;
+    g[k] = act_df<ACT>(t);
   }
+  const R dmag = hilb == HILB_SPIN ? R(2) : R(1);
 
   unsigned long long naccept = 0;
   const int nsweeps = run.burn + run.n_record;
@@ -105,29 +116,24 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
       }
       const int i = __shfl_sync(gmask, my_site, slot, G);
       const R lu = __shfl_sync(gmask, my_lu, slot, G);
-      const int bit = (int)((bits >> i) & 1ull);
-      R dv;
-      if (hilb == HILB_SPIN) dv = bit ? R(-2) : R(2);
-      else dv = bit ? R(-1) : R(1);
-      const bool pos = dv > 0;
+      const bool pos = !((bits >> i) & 1ull);
+      const R dv = pos ? dmag : -dmag;
+      const cpx_pair<R>* trow = s_t01 + i * MP + lane;
       R prod = R(1), prod_half = R(1);
 #pragma unroll
       for (int k = 0; k < HPL; ++k) {
-        const int h = lane + G * k;
-        if (h < M) {
-          const cpx_pair<R> tt = s_t01[i * M + h];
-          cpx<R> rr;
-          if (ACT == ACT_LOGCOSH) {
-            cpx<R> c1 = tt.b;
-            if (!pos) c1 = mk(-c1.x, -c1.y);
-            rr = cfma(g[k], c1, tt.a);
-          } else {
-            const cpx<R> bb = pos ? tt.a : tt.b;
-            rr = cfma(g[k], bb, mk(R(1), R(0)));
-          }
-          if (h < n_half) prod_half *= abs2c(rr);
-          else prod *= abs2c(rr);
+        const cpx_pair<R> tt = trow[G * k];
+        cpx<R> rr;
+        if (ACT == ACT_LOGCOSH) {
+          cpx<R> c1 = tt.b;
+          if (!pos) c1 = mk(-c1.x, -c1.y);
+          rr = cfma(g[k], c1, tt.a);
+        } else {
+          const cpx<R> bb = pos ? tt.a : tt.b;
+          rr = cfma(g[k], bb, mk(R(1), R(0)));
         }
+        if (half[k]) prod_half *= abs2c(rr);
+        else prod *= abs2c(rr);
       }
       R lsum = fast_log2(prod);
       if (n_half > 0) lsum += R(0.5) * fast_log2(prod_half);
@@ -138,27 +144,24 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
       if (acc) {
 #pragma unroll
         for (int k = 0; k < HPL; ++k) {
-          const int h = lane + G * k;
-          if (h < M) {
-            const cpx_pair<R> tw = s_t2w[i * M + h];
-            const cpx<R> w = tw.b;
-            th[k].x += w.x * dv;
-            th[k].y += w.y * dv;
-            cpx<R> num, den;
-            if (ACT == ACT_LOGCOSH) {
-              cpx<R> tau = tw.a;
-              if (!pos) tau = mk(-tau.x, -tau.y);
-              num = g[k] + tau;
-              den = cfma(g[k], tau, mk(R(1), R(0)));
-            } else {
-              const cpx_pair<R> tt = s_t01[i * M + h];
-              const cpx<R> bb = pos ? tt.a : tt.b;
-              num = g[k] * mk(R(1) + bb.x, bb.y);
-              den = cfma(g[k], bb, mk(R(1), R(0)));
-            }
-            const R inv = fast_rcp(abs2c(den));
-            g[k] = inv * (num * conjc(den));
+          const cpx_pair<R> tw = s_t2w[i * MP + lane + G * k];
+          const cpx<R> w = tw.b;
+          th[k].x += w.x * dv;
+          th[k].y += w.y * dv;
+          cpx<R> num, den;
+          if (ACT == ACT_LOGCOSH) {
+            cpx<R> tau = tw.a;
+            if (!pos) tau = mk(-tau.x, -tau.y);
+            num = g[k] + tau;
+            den = cfma(g[k], tau, mk(R(1), R(0)));
+          } else {
+            const cpx_pair<R> tt = trow[G * k];
+            const cpx<R> bb = pos ? tt.a : tt.b;
+            num = g[k] * mk(R(1) + bb.x, bb.y);
+            den = cfma(g[k], bb, mk(R(1), R(0)));
           }
+          const R inv = fast_rcp(abs2c(den));
+          g[k] = inv * (num * conjc(den));
         }
         bits ^= 1ull << i;
         ++naccept;
@@ -169,8 +172,7 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
     const int slot = sweep - run.burn;
     if (slot >= 0 && active && lane == 0) run.samples[(size_t)slot * run.B + chain] = bits;
 #pragma unroll
-    for (int k = 0; k < HPL; ++k)
-      if (lane + G * k < M) g[k] = act_df<ACT>(th[k]);
+    for (int k = 0; k < HPL; ++k) g[k] = act_df<ACT>(th[k]);
   }
   if (run.write_last_at_end && active && lane == 0) run.samples[chain] = bits;
   if (active && lane == 0) atomicAdd(run.accepted, naccept);
@@ -203,7 +205,7 @@ static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cud
   const int threads = run.block;
   const int chains_per_block = threads / G;
   const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
-  size_t smem = (size_t)4 * net.N * net.M * sizeof(cpx<R>) + net.N * sizeof(R);
+  size_t smem = (size_t)4 * net.N * (G * HPL) * sizeof(cpx<R>) + net.N * sizeof(R);
   auto kern = rbm_sampler_kernel<R, G, HPL, ACT>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -254,7 +256,8 @@ cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int 
 
 template <typename R, int G, int HPL, int ACT>
 static cudaError_t sampler_batch_inst(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
-                                      size_t smem, cudaStream_t st) {
+                                      int N_max, cudaStream_t st) {
+  const size_t smem = (size_t)4 * N_max * (G * HPL) * sizeof(cpx<R>) + N_max * sizeof(R);
   auto kern = rbm_sampler_batch_kernel<R, G, HPL, ACT>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -266,16 +269,16 @@ static cudaError_t sampler_batch_inst(const SamplerJob<R>* jobs, const int* blk_
 
 template <typename R, int G, int ACT>
 static cudaError_t sampler_batch_hpl(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
-                                     int M_max, size_t smem, cudaStream_t st) {
+                                     int M_max, int N_max, cudaStream_t st) {
   switch ((M_max + G - 1) / G) {
-    case 1: return sampler_batch_inst<R, G, 1, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 2: return sampler_batch_inst<R, G, 2, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 3: return sampler_batch_inst<R, G, 3, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 4: return sampler_batch_inst<R, G, 4, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 5: return sampler_batch_inst<R, G, 5, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 6: return sampler_batch_inst<R, G, 6, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 8: return sampler_batch_inst<R, G, 8, ACT>(jobs, blk_start, np, total_blocks, smem, st);
-    case 10: return sampler_batch_inst<R, G, 10, ACT>(jobs, blk_start, np, total_blocks, smem, st);
+    case 1: return sampler_batch_inst<R, G, 1, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 2: return sampler_batch_inst<R, G, 2, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 3: return sampler_batch_inst<R, G, 3, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 4: return sampler_batch_inst<R, G, 4, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 5: return sampler_batch_inst<R, G, 5, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 6: return sampler_batch_inst<R, G, 6, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 8: return sampler_batch_inst<R, G, 8, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
+    case 10: return sampler_batch_inst<R, G, 10, ACT>(jobs, blk_start, np, total_blocks, N_max, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -284,16 +287,15 @@ template <typename R>
 cudaError_t launch_rbm_sampler_batch(const SamplerJob<R>* jobs, const int* blk_start, int np, int total_blocks,
                                      int M_max, int N_max, int act, int G, cudaStream_t st) {
   if (N_max > 64 || !hpl_ok((M_max + G - 1) / G)) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)4 * N_max * M_max * sizeof(cpx<R>) + N_max * sizeof(R);
   switch (G) {
-    case 4: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 4, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
-                                      : sampler_batch_hpl<R, 4, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
-    case 8: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 8, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
-                                      : sampler_batch_hpl<R, 8, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
-    case 16: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 16, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
-                                       : sampler_batch_hpl<R, 16, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
-    case 32: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 32, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, smem, st)
-                                       : sampler_batch_hpl<R, 32, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, smem, st);
+    case 4: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 4, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, N_max, st)
+                                      : sampler_batch_hpl<R, 4, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, N_max, st);
+    case 8: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 8, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, N_max, st)
+                                      : sampler_batch_hpl<R, 8, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, N_max, st);
+    case 16: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 16, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, N_max, st)
+                                       : sampler_batch_hpl<R, 16, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, N_max, st);
+    case 32: return act == ACT_LOGCOSH ? sampler_batch_hpl<R, 32, ACT_LOGCOSH>(jobs, blk_start, np, total_blocks, M_max, N_max, st)
+                                       : sampler_batch_hpl<R, 32, ACT_SOFTPLUS>(jobs, blk_start, np, total_blocks, M_max, N_max, st);
     default: return cudaErrorInvalidValue;
   }
 }
