@@ -77,19 +77,23 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
                      cpx<R>* __restrict__ eloc, int blk, int theta_in_g = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = net.N, M = net.M, T = blockDim.x;
-  cpx_t01<R>* s_t01 = reinterpret_cast<cpx_t01<R>*>(smem_raw);  // [N*M] (if has_op)
-  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(s_t01 + (has_op ? N * M : 0));  // [M*N]
+  const int M8 = (M + 7) & ~7;                           // hidden units padded to a multiple of 8
+  cpx_t01<R>* s_t01 = reinterpret_cast<cpx_t01<R>*>(smem_raw);  // [N*M8] (if has_op)
+  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(s_t01 + (has_op ? N * M8 : 0));  // [M*N]
   cpx<R>* s_b = s_W + M * N;                              // [M]
   cpx<R>* s_a = s_b + M;                                  // [N]
-  cpx<R>* s_g = s_a + N;                                  // [M][T]
+  cpx<R>* s_g = s_a + N;                                  // [M8][T], g = 0 on the padding
   for (int k = threadIdx.x; k < M * N; k += T) s_W[k] = net.W[k];
   for (int k = threadIdx.x; k < M; k += T) s_b[k] = net.b[k];
   for (int k = threadIdx.x; k < N; k += T) s_a[k] = net.a[k];
+  for (int k = threadIdx.x; k < (M8 - M) * T; k += T) s_g[M * T + k] = mk(R(0), R(0));
   if (has_op)
-    for (int k = threadIdx.x; k < N * M; k += T) {
+    for (int k = threadIdx.x; k < N * M8; k += T) {
+      const int i = k / M8, h = k % M8;
       cpx_t01<R> t;
-      t.t0 = net.t0[k];
-      t.t1 = net.t1[k];
+      // padding: single-flip factor t0 + g t1 = 1 (logcosh) or 1 + g t0 = 1 (softplus)
+      t.t0 = h < M ? net.t0[i * M + h] : (ACT == ACT_LOGCOSH ? mk(R(1), R(0)) : mk(R(0), R(0)));
+      t.t1 = h < M ? net.t1[i * M + h] : mk(R(0), R(0));
       s_t01[k] = t;
     }
   __syncthreads();
@@ -178,26 +182,24 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
         // Π_h (t0 + g t1) over two independent chains (even / odd h),
         // rescaled every eight units
         const bool pos = dv1 > 0;
-        const cpx_t01<R>* tt = s_t01 + i1 * M;
+        const cpx_t01<R>* tt = s_t01 + i1 * M8;
         cpx<R> pa = mk(R(1), R(0)), pb = mk(R(1), R(0));
-        for (int h0 = 0; h0 < M; h0 += 8) {
+        for (int h0 = 0; h0 < M8; h0 += 8) {
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const int h = h0 + u;
-            if (h < M) {
-              const cpx_t01<R> t = tt[h];
-              const cpx<R> gh = s_g[h * T + threadIdx.x];
-              cpx<R> rr;
-              if (ACT == ACT_LOGCOSH) {
-                cpx<R> c1 = t.t1;
-                if (!pos) c1 = mk(-c1.x, -c1.y);
-                rr = cfma(gh, c1, t.t0);
-              } else {
-                rr = cfma(gh, pos ? t.t0 : t.t1, mk(R(1), R(0)));
-              }
-              if (u & 1) pb = pb * rr;
-              else pa = pa * rr;
+            const cpx_t01<R> t = tt[h];
+            const cpx<R> gh = s_g[h * T + threadIdx.x];
+            cpx<R> rr;
+            if (ACT == ACT_LOGCOSH) {
+              cpx<R> c1 = t.t1;
+              if (!pos) c1 = mk(-c1.x, -c1.y);
+              rr = cfma(gh, c1, t.t0);
+            } else {
+              rr = cfma(gh, pos ? t.t0 : t.t1, mk(R(1), R(0)));
             }
+            if (u & 1) pb = pb * rr;
+            else pa = pa * rr;
           }
           rescale(pa, logscale);
           rescale(pb, logscale);
@@ -436,8 +438,9 @@ cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<
 }
 
 static int eval_threads(int M, size_t csize) {
+  const size_t M8 = (size_t)(M + 7) & ~(size_t)7;
   int T = 128;
-  while (T > 32 && (size_t)M * T * csize > 96 * 1024) T /= 2;
+  while (T > 32 && M8 * T * csize > 96 * 1024) T /= 2;
   return T;
 }
 
@@ -446,8 +449,9 @@ cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int N
                             cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc, cudaStream_t st, int theta_in_g) {
   const int T = eval_threads(net.M, sizeof(cpx<R>));
   const int has_op = op != nullptr && eloc != nullptr;
-  size_t smem = ((size_t)net.M * net.N + net.M + net.N + (size_t)net.M * T +
-                 (has_op ? 2 * (size_t)net.N * net.M : 0)) * sizeof(cpx<R>);
+  const size_t M8 = (size_t)(net.M + 7) & ~(size_t)7;
+  size_t smem = ((size_t)net.M * net.N + net.M + net.N + M8 * T + (has_op ? 2 * (size_t)net.N * M8 : 0)) *
+                sizeof(cpx<R>);
   DevOp dop;
   if (has_op) dop = *op;
   const int blocks = (Ns + T - 1) / T;
@@ -474,8 +478,8 @@ int rbm_eval_threads(int M_max) { return eval_threads(M_max, sizeof(cpx<float>))
 template <typename R>
 cudaError_t launch_rbm_eval_batch(const EvalJob<R>* jobs, const int* blk_start, int np, int total_blocks,
                                   int M_max, int N_max, int act, int T, cudaStream_t st) {
-  const size_t smem = ((size_t)M_max * N_max + M_max + N_max + (size_t)M_max * T + 2 * (size_t)N_max * M_max) *
-                      sizeof(cpx<R>);
+  const size_t M8 = (size_t)(M_max + 7) & ~(size_t)7;
+  const size_t smem = ((size_t)M_max * N_max + M_max + N_max + M8 * T + 2 * (size_t)N_max * M8) * sizeof(cpx<R>);
   if (act == ACT_LOGCOSH) {
     auto kern = rbm_eval_batch_kernel<R, ACT_LOGCOSH>;
     if (smem > 48 * 1024) {
