@@ -129,7 +129,7 @@ def s_precision_choice():
 
 # DRAM bytes (read + write) of one gram_tf32_kernel launch on this workload, from
 # the ncu capture summarised in profiles/gram_tf32_c1.txt
-GRAM_TRAFFIC_BYTES = 742.76e6
+GRAM_TRAFFIC_BYTES = 701.59e6
 
 
 def effective_samples_per_s(loc, sample_ms):

@@ -242,7 +242,9 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
  * Device milliseconds of the last staged calls (CUDA events on the handle's
  * stream), 12 floats: [sample, eval+estimator, force+stats, S, solve, update,
  * sampler kernel alone, S-accumulation kernel alone, inversion of the shifted
- * S, right-hand side, first solve, FP64 refinement]. */
+ * S, right-hand side, first solve, FP64 refinement].  With the direct solve
+ * the right-hand side, the first solve and the refinement run as one
+ * cooperative launch, reported in the last entry (the two before are 0). */
 nq_status nq_stage_times(nq_handle* h, float* ms12);
 /* Benchmark helper: n_steps whole iterations (graph replays, call indices
  * call0, call0+1, ...); between steps, outside the timed events, a kernel

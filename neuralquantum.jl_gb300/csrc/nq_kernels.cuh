@@ -158,6 +158,17 @@ cudaError_t launch_assemble_S(const float* G, int P, double inv_ns, bool real_pa
 // triangle: W <- -W^-1), one cooperative launch; ctl: sweep_ctl_bytes().
 // launch_herm_fill then mirrors the lower triangle into the upper one.
 size_t sweep_ctl_bytes();
+// diagonal shift of the SR matrix: kind 0 eps, kind 1 lam * S_ii (sr_multiplicative)
+NQ_D double sr_diag_shift(const double* S, int P, int i, int kind, double eps, double lam) {
+  if (kind == 0) return eps;
+  if (kind == 1) return lam * S[2 * ((size_t)i + (size_t)P * i)];
+  return 0.0;
+}
+// the FP64-residual refinement of launch_sr_finish (x0 = A⁻¹F, then `iters`
+// corrections, last residual in r) as one cooperative launch; ctl: sweep_ctl_bytes()
+cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const double* F, int kind, double eps,
+                               double lam, bool real_params, int iters, double* x, double* r, float2* rf, void* ctl,
+                               int* status, cudaStream_t st);
 size_t sweep_work_elems(int P);
 cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st);
 // many matrices in one cooperative launch (one CTA group per matrix, groups

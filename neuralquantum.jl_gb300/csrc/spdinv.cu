@@ -411,6 +411,7 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
   if (i >= P) return;
   const float2* col = W + (size_t)P * i;
   float sx = 0.f, sy = 0.f;
+#pragma unroll 8
   for (int j = lane; j < P; j += 32) {
     const float2 w = col[j], v = x[j];
     sx += w.x * v.x + w.y * v.y;
@@ -422,6 +423,79 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
     sy += __shfl_xor_sync(0xffffffffu, sy, off);
   }
   if (lane == 0) y[i] = make_float2(-sx, -sy);
+}
+
+// FP64-residual refinement of the shifted solve in one cooperative launch
+// (one CTA per SM): rf = F, then for it = 0..iters: x (+)= A⁻¹ rf (Hermitian
+// GEMV with W = -A⁻¹, one warp per row, the same warp adds its row into x),
+// grid barrier, r = F - A x in FP64 from the FP64 S and the shift (one warp
+// per row; rf = FP32 copy of r), grid barrier.  The last residual stays in r.
+// Same arithmetic per element as herm_gemv_neg_kernel + refine_update_kernel +
+// residual_kernel; 2 grid barriers per pass instead of three launches.
+__global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restrict__ W, const double* __restrict__ S,
+                                                          int P, const double* __restrict__ F, int kind, double eps,
+                                                          double lam, int real_params, int iters, double* x, double* r,
+                                                          float2* rf, SweepCtl* ctl, int* status) {
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x)
+    rf[i] = make_float2((float)F[2 * i], real_params ? 0.f : (float)F[2 * i + 1]);
+  if (!group_barrier(ctl, gridDim.x, status)) return;
+  for (int it = 0; it <= iters; ++it) {
+    for (int i = gw; i < P; i += nw) {
+      const float2* col = W + (size_t)P * i;
+      float sx = 0.f, sy = 0.f;
+#pragma unroll 8
+      for (int j = lane; j < P; j += 32) {
+        const float2 w = __ldcg(col + j), v = __ldcg(rf + j);
+        sx += w.x * v.x + w.y * v.y;
+        sy += w.x * v.y - w.y * v.x;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, off);
+        sy += __shfl_xor_sync(0xffffffffu, sy, off);
+      }
+      if (lane == 0) {
+        const float yx = -sx, yy = -sy;
+        if (it == 0) {
+          x[2 * i] = (double)yx;
+          x[2 * i + 1] = (double)yy;
+        } else {
+          x[2 * i] += (double)yx;
+          x[2 * i + 1] += (double)yy;
+        }
+      }
+    }
+    if (!group_barrier(ctl, gridDim.x, status)) return;
+    for (int k = gw; k < P; k += nw) {
+      // (S x)_k = Σ_l conj(S[l][k]) x_l (Hermitian; column k contiguous)
+      const double* col = S + 2 * (size_t)P * k;
+      double sx = 0.0, sy = 0.0;
+#pragma unroll 8
+      for (int l = lane; l < P; l += 32) {
+        const double ar = col[2 * l], ai = l == k ? 0.0 : -col[2 * l + 1];
+        const double xr = __ldcg(x + 2 * l), xi = __ldcg(x + 2 * l + 1);
+        sx += ar * xr - ai * xi;
+        sy += ar * xi + ai * xr;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, off);
+        sy += __shfl_xor_sync(0xffffffffu, sy, off);
+      }
+      if (lane == 0) {
+        const double dsh = sr_diag_shift(S, P, k, kind, eps, lam);
+        sx += dsh * __ldcg(x + 2 * k);
+        sy += dsh * __ldcg(x + 2 * k + 1);
+        const double rx = F[2 * k] - sx, ry = (real_params ? 0.0 : F[2 * k + 1]) - sy;
+        r[2 * k] = rx;
+        r[2 * k + 1] = ry;
+        rf[k] = make_float2((float)rx, (float)ry);
+      }
+    }
+    if (it < iters && !group_barrier(ctl, gridDim.x, status)) return;
+  }
 }
 
 }  // namespace
@@ -490,4 +564,35 @@ cudaError_t launch_herm_fill(float2* W, int P, cudaStream_t st) {
   const dim3 tb(32, 8), tg((unsigned)nblk, (unsigned)nblk);
   herm_fill_kernel<<<tg, tb, 0, st>>>(W, P);
   return cudaGetLastError();
+}
+
+cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const double* F, int kind, double eps,
+                               double lam, bool real_params, int iters, double* x, double* r, float2* rf, void* ctl,
+                               int* status, cudaStream_t st) {
+  static int grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, refine_coop_kernel, 256, 0);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorCooperativeLaunchTooLarge;
+    grid = sms;
+  }
+  cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(SweepCtl), st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, refine_coop_kernel, W, S, P, F, kind, eps, lam, real_params ? 1 : 0, iters, x, r,
+                            rf, reinterpret_cast<SweepCtl*>(ctl), status);
 }

@@ -236,9 +236,7 @@ __global__ void assemble_S_kernel(const float* __restrict__ G, int P, double inv
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double diag_shift(const double* S, int P, int i, int kind, double eps,
                                              double lam) {
-  if (kind == 0) return eps;
-  if (kind == 1) return lam * S[2 * ((size_t)i + (size_t)P * i)];
-  return 0.0;
+  return sr_diag_shift(S, P, i, kind, eps, lam);
 }
 
 __global__ void shift_copy_kernel(const double* __restrict__ S, int P, int kind, double eps,
@@ -252,12 +250,6 @@ __global__ void shift_copy_kernel(const double* __restrict__ S, int P, int kind,
 }
 
 
-__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 f2mulconj(float2 a, float2 b) {  // a * conj(b)
-  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
-}
 
 __global__ void refine_update_kernel(double* x, const float2* __restrict__ d, int P, int first) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -274,6 +266,7 @@ residual_kernel(const double* __restrict__ S, int P, const double* __restrict__ 
   const int k = blockIdx.x;
   // (S x)_k = Σ_l S[k][l] x_l = Σ_l conj(S[l][k]) x_l (Hermitian; column k contiguous)
   double sx = 0.0, sy = 0.0;
+#pragma unroll 4
   for (int l = threadIdx.x; l < P; l += blockDim.x) {
     double ar = S[2 * ((size_t)l + (size_t)P * k)], ai = -S[2 * ((size_t)l + (size_t)P * k) + 1];
     if (l == k) ai = 0.0;
@@ -474,7 +467,19 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   mark(1);
   e = launch_spd_inverse(sb.W, P, sb.ctl, sb.status, sb.work, st);
   if (e != cudaSuccess) return e;
-  return launch_sr_finish(sb, P, F, kind, eps, lam, real_params, refine_iters, st);
+  // one problem on the GPU: the refinement as one cooperative launch (the
+  // many-problem step keeps launch_sr_finish, whose small kernels run side by
+  // side in the graph branches)
+  e = launch_herm_fill(sb.W, P, st);
+  if (e != cudaSuccess) return e;
+  mark(2);
+  mark(3);
+  mark(4);
+  e = launch_refine_coop(sb.W, sb.S, P, F, kind, eps, lam, real_params, refine_iters, sb.x, sb.r, sb.rf, sb.ctl,
+                         sb.status, st);
+  if (e != cudaSuccess) return e;
+  mark(5);
+  return cudaSuccess;
 }
 
 cudaError_t launch_descent(double* master, const double* dw, long n_doubles, int stride, double lr,
