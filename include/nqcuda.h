@@ -107,8 +107,18 @@ typedef struct {
   uint32_t quirks;         /* NQ_QUIRK_* bits */
   int32_t sampler_lanes;   /* lanes per Metropolis chain (4, 8, 16, 32); 0 = autotune */
   int32_t sr_algorithm;    /* nq_sr_algorithm */
-  int32_t reserved[5];
+  int32_t sampler_kind;    /* nq_sampler_kind */
+  int32_t reserved[4];
 } nq_config;
+
+/* Sampler (src/Samplers/).  NQ_SAMPLER_METROPOLIS: the local-flip chains of
+ * MetropolisSampler + LocalRule (Metropolis.jl:101-167).  NQ_SAMPLER_EXACT:
+ * ExactSampler (Exact.jl:52-82, batched :133-176): the full distribution
+ * over the 2^N configurations of the sampler's space (N <= 26; 2N for the
+ * NDM's doubled space), its cumulative sum and inverse-CDF draws, recomputed
+ * at every nq_sample; each of the n_chains x chain_length slots holds an
+ * independent draw (burn and passes are not used). */
+typedef enum { NQ_SAMPLER_METROPOLIS = 0, NQ_SAMPLER_EXACT = 1 } nq_sampler_kind;
 
 /* SR solver (SR.jl:5-6 SRAlgorithm).  NQ_SR_DIRECT forms S and solves the
  * shifted system exactly (sr_cholesky); NQ_SR_CG never forms S: conjugate

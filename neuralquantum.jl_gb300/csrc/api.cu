@@ -66,7 +66,7 @@ static std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g
 // times and the fastest of the last three counts.  Smaller blocks spread the
 // chains more evenly over the SMs when there are few of them.
 nq_status ensure_tuned(nq_handle* h) {
-  if (h->sampler_lanes && h->sampler_block) return NQ_OK;
+  if (h->exact || (h->sampler_lanes && h->sampler_block)) return NQ_OK;
   const int sN = h->ndm ? h->N2 : h->N, sM = h->ndm ? h->Ms : h->M;
   const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb, (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0));
   {
@@ -140,6 +140,9 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
     if (ms != NQ_OK) return ms;
   }
   if (mixed) {
+  } else if (h->exact) {
+    if (h->f64) CKL(launch_exact_sampler<double>(rbm_dev<double>(h), run, h->d_exact, h->st));
+    else CKL(launch_exact_sampler<float>(rbm_dev<float>(h), run, h->d_exact, h->st));
   } else if (h->f64) CKL(launch_rbm_sampler<double>(rbm_dev<double>(h), run, h->sampler_lanes, h->st));
   else CKL(launch_rbm_sampler<float>(rbm_dev<float>(h), run, h->sampler_lanes, h->st));
   if (!h->capturing) CK(cudaEventRecord(h->kev[1], h->st));
@@ -406,6 +409,10 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   }
   if (c.s_precision == NQ_S_F64) { delete h; return NQ_ERR_UNSUPPORTED; }
   if (c.sr_algorithm != NQ_SR_DIRECT && c.sr_algorithm != NQ_SR_CG) return bad("unknown sr_algorithm");
+  if (c.sampler_kind != NQ_SAMPLER_METROPOLIS && c.sampler_kind != NQ_SAMPLER_EXACT) return bad("unknown sampler_kind");
+  if (c.sampler_kind == NQ_SAMPLER_EXACT &&
+      (c.network == NQ_NET_NDM ? 2 * c.n_sites : c.n_sites) > 26)
+    return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM) <= 26");
   if (c.sr_algorithm == NQ_SR_CG &&
       (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64 ||
        !sr_cg_supported(c.n_sites + c.n_hidden + c.n_sites * c.n_hidden))) {
@@ -497,6 +504,8 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->d_chainstats, 3 * (size_t)h->B + 4), "chain stats");
   step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
   h->cg = c.sr_algorithm == NQ_SR_CG;
+  h->exact = c.sampler_kind == NQ_SAMPLER_EXACT;
+  if (h->exact) step(dalloc(&h->d_exact, exact_sampler_work_doubles(h->ndm ? h->N2 : h->N)), "exact sampler");
   const int rows = 2 * P;
   const int rp = ((rows + 127) / 128) * 128;
   if (h->cg) {
@@ -594,7 +603,7 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_dw, h->d_eff[0], h->d_eff[1],
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_exact, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -1348,7 +1357,8 @@ nq_status nq_batch_create(const nq_config* cfgs, int32_t n, nq_batch** out) {
   *out = nullptr;
   for (int p = 0; p < n; ++p) {
     const nq_config& c = cfgs[p];
-    if (c.network != NQ_NET_RBM || c.eval_precision != NQ_EVAL_F32 || c.sr_algorithm != NQ_SR_DIRECT)
+    if (c.network != NQ_NET_RBM || c.eval_precision != NQ_EVAL_F32 || c.sr_algorithm != NQ_SR_DIRECT ||
+        c.sampler_kind != NQ_SAMPLER_METROPOLIS)
       return NQ_ERR_UNSUPPORTED;
     if (c.activation != cfgs[0].activation || c.hilbert != cfgs[0].hilbert) return NQ_ERR_UNSUPPORTED;
   }

@@ -79,6 +79,8 @@ struct nq_handle {
   size_t flush_bytes = 0;
   MadeState* made = nullptr;       // learned proposal, null until nq_proposal_init
   bool cg = false;                 // NQ_SR_CG: matrix-free iterative SR, no S
+  bool exact = false;              // NQ_SAMPLER_EXACT
+  double* d_exact = nullptr;       // exact sampler: CDF and block sums
   SrCgArgs cga;                    // device work of the iterative solve
   double cg_tol = 1e-4;
   int cg_maxiter = 0;

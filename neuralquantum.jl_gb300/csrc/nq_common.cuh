@@ -158,9 +158,9 @@ template <int ACT, typename R> NQ_D R act_df_real(R x) {
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11).  Counter schema shared with the
 // oracle: key = (seed lo, seed hi); init words (q/4, call, chain, 0);
-// Metropolis step t (t, call, chain, 1).
+// Metropolis step t (t, call, chain, 1); exact-sampler draw t (t, call, chain, 4).
 // ---------------------------------------------------------------------------
-enum { TAG_INIT = 0, TAG_MH = 1, TAG_AR = 2, TAG_MIX = 3 };
+enum { TAG_INIT = 0, TAG_MH = 1, TAG_AR = 2, TAG_MIX = 3, TAG_EXACT = 4 };
 
 struct u32x4 { uint32_t x, y, z, w; };
 
@@ -192,6 +192,10 @@ NQ_HD uint32_t uniform_site(uint32_t w, uint32_t nsites) {
 }
 // u in [0,1) with 24 random bits: exact in float
 NQ_HD float uniform24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+// u in [0,1) with 53 random bits (27 from a, 26 from b): exact in double
+NQ_HD double uniform53(uint32_t a, uint32_t b) {
+  return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
 
 // ---------------------------------------------------------------------------
 // Site encodings.  A configuration of up to 64 two-level sites is a bit mask;

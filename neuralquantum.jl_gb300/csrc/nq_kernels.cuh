@@ -57,6 +57,14 @@ template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
 int rbm_sampler_valid_lanes(int N, int M, int csize, int* out, int max_out);
 
+// Exact sampler (Exact.jl): all 2^N configurations of the sampler's space
+// (N <= 26), FP64 CDF, inverse-CDF draws into run.samples (n_record draws per
+// chain, plus one into slot 0 with write_last_at_end).  work:
+// exact_sampler_work_doubles(N) doubles.
+size_t exact_sampler_work_doubles(int nsites);
+template <typename R>
+cudaError_t launch_exact_sampler(const RbmDev<R>& net, const SamplerRun& run, double* work, cudaStream_t st);
+
 // Many independent problems in one sampler launch (FP32): problem p runs on
 // blocks [blk_start[p], blk_start[p+1]) of 256 threads (256/G chains each);
 // M_max / N_max size the shared tables, G is common to all problems.

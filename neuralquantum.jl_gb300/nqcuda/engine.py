@@ -9,7 +9,8 @@ from .networks import RBM, NDM, af_logcosh
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
-                s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT):
+                s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT,
+                sampler_kind=_lib.NQ_SAMPLER_METROPOLIS):
     """nq_config of one problem (include/nqcuda.h)."""
     cfg = _lib.NqConfig()
     ph = physical(hilb)
@@ -36,16 +37,18 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
     cfg.quirks = quirks
     cfg.sampler_lanes = sampler_lanes
     cfg.sr_algorithm = sr_algorithm
+    cfg.sampler_kind = sampler_kind
     return cfg
 
 
 class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
                  eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
-                 sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT, _handle=None, _owner=None):
+                 sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT, sampler_kind=_lib.NQ_SAMPLER_METROPOLIS,
+                 _handle=None, _owner=None):
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
-                          s_precision, quirks, sampler_lanes, sr_algorithm)
+                          s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind)
         self.complex_params = isinstance(net, RBM)
         self.cfg = cfg
         self.lib = L

@@ -79,7 +79,7 @@ class BatchedSampler:
         sr_alg = _lib.NQ_SR_CG if self.algo.iterative else _lib.NQ_SR_DIRECT
         self.engine = Engine(net, hilb, batch_sz, sampler.chain_length, sampler.burn_length,
                              sampler.passes, sampler.seed, eval_precision, s_precision, quirks,
-                             sr_algorithm=sr_alg)
+                             sr_algorithm=sr_alg, sampler_kind=getattr(sampler, "kind", 0))
         if self.algo.iterative:
             self.engine.set_sr_tolerance(self.algo.precision, 10 * self.engine.P)
         self.engine.set_params(net.flat())

@@ -16,6 +16,7 @@ class MetropolisSampler:
         if passes % 2 == 0:
             passes += 1
         self.rule = rule
+        self.kind = 0     # NQ_SAMPLER_METROPOLIS
         self.chain_length = int(chain_length)
         self.passes = int(passes)
         self.burn_length = int(burn)
@@ -24,3 +25,25 @@ class MetropolisSampler:
     def __repr__(self):
         return (f"MetropolisSampler(chain_length={self.chain_length}, burn={self.burn_length}, "
                 f"passes={self.passes}, seed={self.seed})")
+
+
+class ExactSampler:
+    """``ExactSampler(n_samples; seed)`` (src/Samplers/Exact.jl:16-27): every
+    sample call enumerates the 2^N configurations, builds the cumulative
+    distribution of |ψ|² and draws each of the ``batch_sz`` x ``n_samples``
+    slots independently by inverse CDF.  ``chain_length`` = n_samples draws
+    per batch entry, as the batched reference sampler takes one draw per
+    entry per step; burn and passes do not apply."""
+
+    kind = 1          # NQ_SAMPLER_EXACT
+
+    def __init__(self, n_samples, seed=None):
+        if n_samples < 1:
+            raise ValueError("n_samples must be positive")
+        self.chain_length = int(n_samples)
+        self.passes = 1
+        self.burn_length = 0
+        self.seed = 0x4E51 if seed is None else int(seed)
+
+    def __repr__(self):
+        return f"ExactSampler(n_samples={self.chain_length}, seed={self.seed})"

@@ -12,6 +12,8 @@ Counter schema (identical in ``csrc/philox.cuh``):
 * init  : word q of chain c in call n  -> philox((q // 4, n, c, TAG_INIT))[q % 4]
 * MH    : step t of chain c in call n  -> r = philox((t, n, c, TAG_MH));
           site = (r0 * nsites) >> 32,  u = (r1 >> 8) * 2**-24
+* exact : draw t of chain c in call n  -> r = philox((t, n, c, TAG_EXACT));
+          u = ((r0 >> 5) * 2**26 + (r1 >> 6)) * 2**-53
 """
 import numpy as np
 
@@ -25,6 +27,7 @@ TAG_INIT = 0
 TAG_MH = 1
 TAG_AR = 2      # learned autoregressive proposal draws
 TAG_MIX = 3     # proposal-type selection of the mixture kernel
+TAG_EXACT = 4   # exact-sampler draws
 
 
 def philox4x32_10(c0, c1, c2, c3, k0, k1):
@@ -81,3 +84,13 @@ def mh_draws(seed, call, chains, step, nsites):
     site = ((r0.astype(np.uint64) * np.uint64(nsites)) >> np.uint64(32)).astype(np.int64)
     u = (r1 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24
     return site, u
+
+
+def exact_uniforms(seed, call, chains, t):
+    """53-bit uniforms in [0, 1) of exact-sampler draw ``t`` for ``chains``."""
+    k0, k1 = split_seed(seed)
+    chains = np.asarray(chains, dtype=np.uint64)
+    r0, r1, _, _ = philox4x32_10(np.uint64(t), np.uint64(call), chains, TAG_EXACT, k0, k1)
+    a = (r0.astype(np.uint64) >> np.uint64(5)).astype(np.float64)
+    b = (r1.astype(np.uint64) >> np.uint64(6)).astype(np.float64)
+    return (a * 67108864.0 + b) / 9007199254740992.0

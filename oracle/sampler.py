@@ -89,3 +89,41 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
     if stale_last_slot and L == 1:
         samples[0] = sigma          # init_sampler! writes the first slot
     return samples, info
+
+
+def exact_run(p, n_chains, chain_length, seed, call=0, stale_last_slot=False, prev_samples=None,
+              gpu_samples=None, tie_tol=1e-6):
+    """Replays the exact sampler (src/Samplers/Exact.jl:52-82; batched
+    variant :133-176): cdf = cumsum(p) / sum(p) over configuration indices,
+    draw = searchsortedfirst(cdf, u) with the Philox 53-bit uniform of
+    ``philox.exact_uniforms``.  Slot k of chain c holds draw k; with
+    ``stale_last_slot`` slots 0..L-2 are drawn and slot L-1 keeps
+    ``prev_samples`` (L = 1: one draw into slot 0), as for the Metropolis
+    bookkeeping of BaseIterativeSampler.jl:11-16.
+
+    Returns (indices [L, B], number of near-ties).  With ``gpu_samples`` a
+    draw whose u lies within ``tie_tol`` of a CDF boundary takes the GPU's
+    index when it is one of the two neighbours (the GPU's CDF carries FP32
+    log-probabilities), and is counted."""
+    cdf = np.cumsum(np.asarray(p, dtype=np.float64))
+    cdf /= cdf[-1]
+    L = chain_length
+    n_rec = (L - 1 if L > 1 else 0) if stale_last_slot else L
+    draws = n_rec + (1 if stale_last_slot and L == 1 else 0)
+    out = np.zeros((L, n_chains), dtype=np.int64) if prev_samples is None else np.array(prev_samples)
+    chains = np.arange(n_chains)
+    ties = 0
+    for t in range(draws):
+        u = philox.exact_uniforms(seed, call, chains, t)
+        idx = np.searchsorted(cdf, u, side="left")
+        idx = np.minimum(idx, len(cdf) - 1)
+        slot = t if t < n_rec else 0
+        if gpu_samples is not None:
+            g = np.asarray(gpu_samples)[slot]
+            lo = np.where(idx > 0, cdf[np.maximum(idx - 1, 0)], 0.0)
+            near = (np.abs(u - cdf[idx]) < tie_tol) | (np.abs(u - lo) < tie_tol)
+            ok = near & (np.abs(g - idx) == 1)
+            ties += int(ok.sum())
+            idx = np.where(ok, g, idx)
+        out[slot] = idx
+    return out, ties

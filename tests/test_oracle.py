@@ -256,3 +256,22 @@ def test_mixture_oracle_with_exact_proposal_always_accepts():
     _, info = om.run_mixture(r.log_prob, h, ExactQ(), 1.0, B, 3, 2, 3, 17, call=1)
     assert info["ar"] == info["steps"]
     assert info["ar_accepted"] == info["ar"]
+
+
+def test_exact_sampler_oracle_chi_square():
+    """Inverse-CDF draws of the exact-sampler replay follow |ψ|² (N=4)."""
+    from scipy.stats import chisquare
+    from oracle import exact as oex, networks as onw, sampler as osm
+    from oracle.hilbert import Hilbert, SPIN
+    hilb = Hilbert(4, SPIN)
+    net = onw.RBM(4, 8, onw.LOGCOSH)
+    onw.init_random_pars(net, np.random.default_rng(2), sigma=0.3 ** 2)
+    p = oex.ket_distribution(net, hilb)
+    idx, ties = osm.exact_run(p, 256, 40, seed=9, call=3)
+    counts = np.bincount(idx.ravel(), minlength=hilb.dim)
+    stat, pval = chisquare(counts, p * counts.sum())
+    assert pval > 1e-3 and ties == 0
+    # stale-last-slot bookkeeping: slot L-1 keeps the previous contents
+    prev = np.full((5, 8), -7)
+    idx2, _ = osm.exact_run(p, 8, 5, seed=9, call=3, stale_last_slot=True, prev_samples=prev)
+    assert np.all(idx2[4] == -7) and np.array_equal(idx2[:4], osm.exact_run(p, 8, 5, seed=9, call=3)[0][:4])
