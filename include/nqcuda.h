@@ -108,8 +108,16 @@ typedef struct {
   int32_t sampler_lanes;   /* lanes per Metropolis chain (4, 8, 16, 32); 0 = autotune */
   int32_t sr_algorithm;    /* nq_sr_algorithm */
   int32_t sampler_kind;    /* nq_sampler_kind */
-  int32_t reserved[4];
+  int32_t rule;            /* nq_mcmc_rule (Metropolis sampler) */
+  int32_t reserved[3];
 } nq_config;
+
+/* Metropolis transition rule (src/Samplers/MCMCRules/).  NQ_RULE_LOCAL:
+ * LocalRule, one uniformly drawn site flips (LocalRule.jl:19-28).
+ * NQ_RULE_EXCHANGE: ExchangeRule(H), a uniformly drawn coupling (i, j) of the
+ * couplings given by nq_set_exchange swaps its two values (ExchangeRule.jl:
+ * 38-68); the total magnetisation of a chain is conserved.  RBM (ket), FP32. */
+typedef enum { NQ_RULE_LOCAL = 0, NQ_RULE_EXCHANGE = 1 } nq_mcmc_rule;
 
 /* Sampler (src/Samplers/).  NQ_SAMPLER_METROPOLIS: the local-flip chains of
  * MetropolisSampler + LocalRule (Metropolis.jl:101-167).  NQ_SAMPLER_EXACT:
@@ -247,6 +255,13 @@ nq_status nq_update_descent(nq_handle* h, double lr);
  * Replays a captured CUDA graph after the first call. */
 nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
                       nq_measurement* stats);
+
+/* Couplings of the exchange rule: n pairs (i, j) of 0-based sites, i != j,
+ * in the order ExchangeRule(H) collects them from the 2-site terms of H
+ * (ExchangeRule.jl:16-35; a pair listed twice is drawn twice as often).
+ * Required before sampling with rule = NQ_RULE_EXCHANGE; replaces earlier
+ * couplings. */
+nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs);
 
 /* ---- timing/diagnostics ----------------------------------------------------
  * Device milliseconds of the last staged calls (CUDA events on the handle's

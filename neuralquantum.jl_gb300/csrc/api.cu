@@ -47,6 +47,10 @@ nq_status refresh_params(nq_handle* h) {
     RbmDev<float> d = rbm_dev<float>(h);
     CKL(launch_rbm_tables<float>(d, (cpx<float>*)h->d_tab[0], (cpx<float>*)h->d_tab[1],
                                  (cpx<float>*)h->d_tab[2], h->st));
+    if (h->rule == NQ_RULE_EXCHANGE && h->n_exch > 0)
+      CKL(launch_rbm_exchange_tables<float>(d, h->n_exch, h->d_pairs, (cpx<float>*)h->d_xtab[0],
+                                            (cpx<float>*)h->d_xtab[1], (cpx<float>*)h->d_xtab[2],
+                                            (cpx<float>*)h->d_xW, h->d_xare, h->st));
     if (h->tc_theta) CKL(launch_theta_pack(d.W, h->M, h->N, h->theta_terms, h->d_theta_img, h->st));
   }
   return NQ_OK;
@@ -67,8 +71,11 @@ static std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g
 // chains more evenly over the SMs when there are few of them.
 nq_status ensure_tuned(nq_handle* h) {
   if (h->exact || (h->sampler_lanes && h->sampler_block)) return NQ_OK;
+  if (h->rule == NQ_RULE_EXCHANGE && h->n_exch == 0)
+    return fail(h, NQ_ERR_STATE, "exchange rule: no couplings (nq_set_exchange)");
   const int sN = h->ndm ? h->N2 : h->N, sM = h->ndm ? h->Ms : h->M;
-  const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb, (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0));
+  const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb,
+                                   (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0) + (h->rule ? 4 * (h->n_exch + 1) : 0));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -79,7 +86,8 @@ nq_status ensure_tuned(nq_handle* h) {
     }
   }
   int cand[4];
-  int nc = rbm_sampler_valid_lanes(h->ndm ? h->N2 : h->N, sM, h->f64 ? 16 : 8, cand, 4);
+  const int rows = h->rule == NQ_RULE_EXCHANGE ? h->n_exch : (h->ndm ? h->N2 : h->N);
+  int nc = rbm_sampler_valid_lanes(rows, sM, h->f64 ? 16 : 8, cand, 4);
   if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", sM);
   if (h->sampler_lanes) { cand[0] = h->sampler_lanes; nc = 1; }     // fixed by the caller
   const int blocks[3] = {64, 128, 256};
@@ -99,8 +107,8 @@ nq_status ensure_tuned(nq_handle* h) {
       for (int rep = 0; rep < 4; ++rep) {
         float ms = 0.f;
         CK(cudaEventRecord(h->kev[0], h->st));
-        cudaError_t e = h->f64 ? launch_rbm_sampler<double>(rbm_dev<double>(h), run, cand[c], h->st)
-                               : launch_rbm_sampler<float>(rbm_dev<float>(h), run, cand[c], h->st);
+        cudaError_t e = h->f64 ? launch_rbm_sampler<double>(rbm_sampler_dev<double>(h), run, cand[c], h->st)
+                               : launch_rbm_sampler<float>(rbm_sampler_dev<float>(h), run, cand[c], h->st);
         ++h->launches;
         if (e != cudaSuccess) { cudaFree(scratch); return fail(h, NQ_ERR_CUDA, "autotune: %s", cudaGetErrorString(e)); }
         CK(cudaEventRecord(h->kev[1], h->st));
@@ -143,8 +151,12 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
   } else if (h->exact) {
     if (h->f64) CKL(launch_exact_sampler<double>(rbm_dev<double>(h), run, h->d_exact, h->st));
     else CKL(launch_exact_sampler<float>(rbm_dev<float>(h), run, h->d_exact, h->st));
-  } else if (h->f64) CKL(launch_rbm_sampler<double>(rbm_dev<double>(h), run, h->sampler_lanes, h->st));
-  else CKL(launch_rbm_sampler<float>(rbm_dev<float>(h), run, h->sampler_lanes, h->st));
+  } else if (h->f64) CKL(launch_rbm_sampler<double>(rbm_sampler_dev<double>(h), run, h->sampler_lanes, h->st));
+  else {
+    if (h->rule == NQ_RULE_EXCHANGE && h->n_exch == 0)
+      return fail(h, NQ_ERR_STATE, "exchange rule: no couplings (nq_set_exchange)");
+    CKL(launch_rbm_sampler<float>(rbm_sampler_dev<float>(h), run, h->sampler_lanes, h->st));
+  }
   if (!h->capturing) CK(cudaEventRecord(h->kev[1], h->st));
   return NQ_OK;
 }
@@ -410,6 +422,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (c.s_precision == NQ_S_F64) { delete h; return NQ_ERR_UNSUPPORTED; }
   if (c.sr_algorithm != NQ_SR_DIRECT && c.sr_algorithm != NQ_SR_CG) return bad("unknown sr_algorithm");
   if (c.sampler_kind != NQ_SAMPLER_METROPOLIS && c.sampler_kind != NQ_SAMPLER_EXACT) return bad("unknown sampler_kind");
+  if (c.rule != NQ_RULE_LOCAL && c.rule != NQ_RULE_EXCHANGE) return bad("unknown rule");
+  if (c.rule == NQ_RULE_EXCHANGE && (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64))
+    return bad("the exchange rule is available for FP32 RBM handles");
   if (c.sampler_kind == NQ_SAMPLER_EXACT &&
       (c.network == NQ_NET_NDM ? 2 * c.n_sites : c.n_sites) > 26)
     return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM) <= 26");
@@ -505,6 +520,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
   h->cg = c.sr_algorithm == NQ_SR_CG;
   h->exact = c.sampler_kind == NQ_SAMPLER_EXACT;
+  h->rule = c.rule;
   if (h->exact) step(dalloc(&h->d_exact, exact_sampler_work_doubles(h->ndm ? h->N2 : h->N)), "exact sampler");
   const int rows = 2 * P;
   const int rp = ((rows + 127) / 128) * 128;
@@ -603,7 +619,8 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_exact, h->d_dw, h->d_eff[0], h->d_eff[1],
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_exact, h->d_pairs, h->d_xtab[0],
+                  h->d_xtab[1], h->d_xtab[2], h->d_xW, h->d_xare, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -678,6 +695,33 @@ nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
     float* f = (float*)flat;
     for (size_t i = 0; i < buf.size(); ++i) f[i] = (float)buf[i];
   }
+  return NQ_OK;
+}
+
+nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs) {
+  if (!h || n < 1 || !pairs) return NQ_ERR_ARG;
+  if (h->rule != NQ_RULE_EXCHANGE) return fail(h, NQ_ERR_STATE, "the handle was created with another rule");
+  for (int k = 0; k < n; ++k) {
+    const int i = pairs[2 * k], j = pairs[2 * k + 1];
+    if (i < 0 || j < 0 || i >= h->N || j >= h->N || i == j)
+      return fail(h, NQ_ERR_ARG, "coupling %d: sites (%d, %d) out of range or equal", k, i, j);
+  }
+  CK(cudaStreamSynchronize(h->st));
+  cudaFree(h->d_pairs); cudaFree(h->d_xW); cudaFree(h->d_xare);
+  for (void*& p : h->d_xtab) { cudaFree(p); p = nullptr; }
+  h->d_pairs = nullptr; h->d_xW = nullptr; h->d_xare = nullptr; h->n_exch = 0;
+  const size_t tab = (size_t)n * h->M * sizeof(cpx<float>);
+  CK(cudaMalloc((void**)&h->d_pairs, (size_t)n * sizeof(int2)));
+  for (void*& p : h->d_xtab) CK(cudaMalloc(&p, tab));
+  CK(cudaMalloc(&h->d_xW, tab));
+  CK(cudaMalloc((void**)&h->d_xare, (size_t)n * sizeof(float)));
+  CK(cudaMemcpy(h->d_pairs, pairs, (size_t)n * sizeof(int2), cudaMemcpyHostToDevice));
+  h->n_exch = n;
+  h->sampler_lanes = h->cfg.sampler_lanes;      // re-tune: the tables changed size
+  h->sampler_block = 0;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  if (nq_status s = refresh_params(h)) return s;
+  CK(cudaStreamSynchronize(h->st));
   return NQ_OK;
 }
 

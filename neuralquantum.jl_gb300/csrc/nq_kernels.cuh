@@ -30,9 +30,17 @@ template <typename R> struct RbmDev {
   const cpx<R>* a = nullptr;   // [N]
   const cpx<R>* b = nullptr;   // [M]
   const cpx<R>* W = nullptr;   // [M*N] column-major
-  const cpx<R>* t0 = nullptr;  // [N*M]
+  const cpx<R>* t0 = nullptr;  // [N*M] (exchange rule: [n_rows*M], per coupling)
   const cpx<R>* t1 = nullptr;
   const cpx<R>* t2 = nullptr;
+  // Exchange rule (ExchangeRule.jl): the move of row r swaps the values of
+  // sites pairs[r] = (i, j); with σ_i != σ_j it changes θ by Δv_i (W_hi - W_hj),
+  // so the single-flip tables are taken of rW = W_hi - W_hj.  n_rows = 0:
+  // local flips, row = site.
+  int n_rows = 0;
+  const int2* pairs = nullptr;   // [n_rows]
+  const cpx<R>* rW = nullptr;    // [M*n_rows] at h + M*r
+  const R* rare = nullptr;       // [n_rows] 2 log2(e) Re(a_i - a_j)
 };
 
 cudaError_t launch_rbm_params_from_master(const double* master, int N, int M, float* f32_out,
@@ -41,6 +49,11 @@ cudaError_t launch_master_to_f32(const double* master, long n, float* f32_out, c
 template <typename R>
 cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2,
                               cudaStream_t st);
+// exchange-rule tables of the couplings (i, j) = pairs[r]: t0..t2 of Δ = d (W_hi - W_hj)
+// at r*M + h, rW = W_hi - W_hj at h + M*r, rare[r] = 2 log2(e) Re(a_i - a_j)
+template <typename R>
+cudaError_t launch_rbm_exchange_tables(const RbmDev<R>& net, int n_rows, const int2* pairs, cpx<R>* t0,
+                                       cpx<R>* t1, cpx<R>* t2, cpx<R>* rW, R* rare, cudaStream_t st);
 
 struct SamplerRun {
   int B = 0, L = 0, burn = 0, passes = 1, n_record = 0, write_last_at_end = 0;
@@ -56,6 +69,8 @@ struct SamplerRun {
 template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
 int rbm_sampler_valid_lanes(int N, int M, int csize, int* out, int max_out);
+// the exchange-rule instantiations of the FP32 sampler (net.pairs set)
+cudaError_t launch_rbm_sampler_exchange(const RbmDev<float>& net, const SamplerRun& run, int G, cudaStream_t st);
 
 // Exact sampler (Exact.jl): all 2^N configurations of the sampler's space
 // (N <= 26), FP64 CDF, inverse-CDF draws into run.samples (n_record draws per

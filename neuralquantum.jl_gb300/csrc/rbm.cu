@@ -45,6 +45,38 @@ __global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>*
   t2[idx] = mk((R)c2.x, (R)c2.y);
 }
 
+template <typename R>
+__global__ void rbm_exchange_tables_kernel(RbmDev<R> net, int n_rows, const int2* __restrict__ pairs,
+                                           cpx<R>* t0, cpx<R>* t1, cpx<R>* t2, cpx<R>* rW, R* rare) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;   // idx = r*M + h
+  if (idx < n_rows) {
+    const int2 pr = pairs[idx];
+    rare[idx] = (R)(2.8853900817779268 * ((double)net.a[pr.x].x - (double)net.a[pr.y].x));
+  }
+  if (idx >= n_rows * net.M) return;
+  const int r = idx / net.M, h = idx % net.M;
+  const int2 pr = pairs[r];
+  const cpx<R> wi = net.W[h + net.M * pr.x], wj = net.W[h + net.M * pr.y];
+  const cpx<double> w = mk((double)wi.x - (double)wj.x, (double)wi.y - (double)wj.y);
+  rW[h + net.M * r] = mk((R)w.x, (R)w.y);
+  const double d = net.hilb == HILB_SPIN ? 2.0 : 1.0;
+  const cpx<double> z = mk(w.x * d, w.y * d);
+  cpx<double> c0, c1, c2;
+  if (net.act == ACT_LOGCOSH) {
+    c0 = ccoshc(z);
+    c1 = csinhc(z);
+    c2 = act_df<ACT_LOGCOSH>(z);
+  } else {
+    const cpx<double> ep = cexpc(z), em = cexpc(mk(-z.x, -z.y));
+    c0 = mk(ep.x - 1.0, ep.y);
+    c1 = mk(em.x - 1.0, em.y);
+    c2 = mk(0.0, 0.0);
+  }
+  t0[idx] = mk((R)c0.x, (R)c0.y);
+  t1[idx] = mk((R)c1.x, (R)c1.y);
+  t2[idx] = mk((R)c2.x, (R)c2.y);
+}
+
 // ---------------------------------------------------------------------------
 // Batched evaluation, one thread per sample: θ = Wσ + b, logψ = aᵀσ + Σ f(θ),
 // g = f'(θ) and, if an operator is given, the local estimator
@@ -428,6 +460,16 @@ cudaError_t launch_master_to_f32(const double* master, long n, float* f32_out, c
   master_to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(master, n, f32_out);
   return cudaGetLastError();
 }
+
+template <typename R>
+cudaError_t launch_rbm_exchange_tables(const RbmDev<R>& net, int n_rows, const int2* pairs, cpx<R>* t0,
+                                       cpx<R>* t1, cpx<R>* t2, cpx<R>* rW, R* rare, cudaStream_t st) {
+  const int n = n_rows * net.M > n_rows ? n_rows * net.M : n_rows;
+  rbm_exchange_tables_kernel<R><<<(n + 255) / 256, 256, 0, st>>>(net, n_rows, pairs, t0, t1, t2, rW, rare);
+  return cudaGetLastError();
+}
+template cudaError_t launch_rbm_exchange_tables<float>(const RbmDev<float>&, int, const int2*, cpx<float>*,
+                                                       cpx<float>*, cpx<float>*, cpx<float>*, float*, cudaStream_t);
 
 template <typename R>
 cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2,

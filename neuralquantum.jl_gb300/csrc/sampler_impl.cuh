@@ -3,6 +3,8 @@
 // src/Samplers/MCMCRules/LocalRule.jl:19-28, flipat! of
 // src/Hilbert/HomogeneousSpin.jl:95-104 and HomogeneousFock.jl:72-81.
 #pragma once
+#include <type_traits>
+
 #include "nq_kernels.cuh"
 
 namespace {
@@ -36,22 +38,27 @@ template <typename R> struct alignas(4 * sizeof(R)) cpx_pair {
 // Hidden units are padded to MP = G*HPL with neutral table entries (ratio
 // factor 1, no θ change), so the proposal and accept loops have no unit-range
 // branches.
-template <typename R, int G, int HPL, int ACT>
+// EXCH: the exchange rule (ExchangeRule.jl:38-68): a move draws a coupling
+// (i, j) and swaps the two values; equal values leave the state unchanged
+// (ratio 1, accepted).  The move tables are then per coupling.
+template <typename R, int G, int HPL, int ACT, bool EXCH = false>
 NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int MP = G * HPL;
   const int N = net.N, M = net.M, n_half = net.n_half;
-  cpx_pair<R>* s_t01 = reinterpret_cast<cpx_pair<R>*>(smem_raw);   // {t0, t1} at i*MP + h
-  cpx_pair<R>* s_t2w = s_t01 + N * MP;                            // {t2, W[h, i]} at i*MP + h
-  R* s_are = reinterpret_cast<R*>(s_t2w + N * MP);                // 2 Re a_i log2(e)
-  for (int k = threadIdx.x; k < N * MP; k += blockDim.x) {
+  const int NR = EXCH ? net.n_rows : N;                          // rows of the move tables
+  cpx_pair<R>* s_t01 = reinterpret_cast<cpx_pair<R>*>(smem_raw);   // {t0, t1} at r*MP + h
+  cpx_pair<R>* s_t2w = s_t01 + NR * MP;                           // {t2, W[h, i] or W_hi - W_hj} at r*MP + h
+  int2* s_pairs = reinterpret_cast<int2*>(s_t2w + NR * MP);       // EXCH: sites of coupling r
+  R* s_are = reinterpret_cast<R*>(s_pairs + (EXCH ? NR : 0));     // 2 Re a_i log2(e) (EXCH: of a_i - a_j)
+  for (int k = threadIdx.x; k < NR * MP; k += blockDim.x) {
     const int i = k / MP, h = k % MP;
     cpx_pair<R> p01, p2w;
     if (h < M) {
       p01.a = net.t0[i * M + h];
       p01.b = net.t1[i * M + h];
       p2w.a = ACT == ACT_LOGCOSH ? net.t2[i * M + h] : mk(R(0), R(0));
-      p2w.b = net.W[h + M * i];
+      p2w.b = EXCH ? net.rW[h + M * i] : net.W[h + M * i];
     } else {
       // logcosh: t0 + g t1 = 1; softplus: 1 + g t0 = 1; accepted flip: θ, g unchanged
       p01.a = ACT == ACT_LOGCOSH ? mk(R(1), R(0)) : mk(R(0), R(0));
@@ -62,7 +69,14 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
     s_t01[k] = p01;
     s_t2w[k] = p2w;
   }
-  for (int k = threadIdx.x; k < N; k += blockDim.x) s_are[k] = R(2.8853900817779268) * net.a[k].x;
+  for (int k = threadIdx.x; k < NR; k += blockDim.x) {
+    if (EXCH) {
+      s_pairs[k] = net.pairs[k];
+      s_are[k] = net.rare[k];
+    } else {
+      s_are[k] = R(2.8853900817779268) * net.a[k].x;
+    }
+  }
   __syncthreads();
 
   const int lane = threadIdx.x % G;
@@ -89,12 +103,13 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
     const int h = lane + G * k;
     half[k] = h < n_half;
     cpx<R> t = h < M ? net.b[h] : mk(R(0), R(0));
-    for (int j = 0; j < N; ++j) {
-      const R v = site_value<R>(bits, j, hilb);
-      const cpx<R> w = s_t2w[j * MP + h].b;
-      t.x += w.x * v;
-      t.y += w.y * v;
-    }
+    if (h < M)
+      for (int j = 0; j < N; ++j) {
+        const R v = site_value<R>(bits, j, hilb);
+        const cpx<R> w = EXCH ? net.W[h + M * j] : s_t2w[j * MP + h].b;
+        t.x += w.x * v;
+        t.y += w.y * v;
+      }
     th[k] = t;
     g[k] = act_df<ACT>(t);
   }
@@ -111,12 +126,25 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
       const int slot = (int)(t & (G - 1));
       if (slot == 0) {
         const u32x4 r = philox4x32_10(t + (uint32_t)lane, run.call, (uint32_t)chain, TAG_MH, run.k0, run.k1);
-        my_site = (int)uniform_site(r.x, (uint32_t)N);
+        my_site = (int)uniform_site(r.x, (uint32_t)NR);
         my_lu = fast_log2((R)uniform24(r.y));       // log2 u; u = 0 -> -inf (always accept)
       }
       const int i = __shfl_sync(gmask, my_site, slot, G);
       const R lu = __shfl_sync(gmask, my_lu, slot, G);
-      const bool pos = !((bits >> i) & 1ull);
+      uint64_t fmask = 1ull << i;
+      int site_i = i;
+      if (EXCH) {
+        const int2 pr = s_pairs[i];
+        site_i = pr.x;
+        fmask = (1ull << pr.x) | (1ull << pr.y);
+        if (((bits >> pr.x) & 1ull) == ((bits >> pr.y) & 1ull)) {
+          // swap of equal values: the same state, ratio 1 (u < 1 always accepts)
+          ++naccept;
+          if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = 1;
+          continue;
+        }
+      }
+      const bool pos = !((bits >> site_i) & 1ull);
       const R dv = pos ? dmag : -dmag;
       const cpx_pair<R>* trow = s_t01 + i * MP + lane;
       R prod = R(1), prod_half = R(1);
@@ -163,7 +191,7 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
           const R inv = fast_rcp(abs2c(den));
           g[k] = inv * (num * conjc(den));
         }
-        bits ^= 1ull << i;
+        bits ^= fmask;
         ++naccept;
       }
       if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = acc ? 1 : 0;
@@ -178,9 +206,9 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   if (active && lane == 0) atomicAdd(run.accepted, naccept);
 }
 
-template <typename R, int G, int HPL, int ACT>
+template <typename R, int G, int HPL, int ACT, bool EXCH>
 __global__ void __launch_bounds__(256) rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
-  sampler_block<R, G, HPL, ACT>(net, run, blockIdx.x);
+  sampler_block<R, G, HPL, ACT, EXCH>(net, run, blockIdx.x);
 }
 
 // Many independent problems in one launch: problem p owns blocks
@@ -200,13 +228,14 @@ rbm_sampler_batch_kernel(const SamplerJob<R>* __restrict__ jobs, const int* __re
 
 }  // namespace
 
-template <typename R, int G, int HPL, int ACT>
+template <typename R, int G, int HPL, int ACT, bool EXCH>
 static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
   const int threads = run.block;
   const int chains_per_block = threads / G;
   const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
-  size_t smem = (size_t)4 * net.N * (G * HPL) * sizeof(cpx<R>) + net.N * sizeof(R);
-  auto kern = rbm_sampler_kernel<R, G, HPL, ACT>;
+  const int NR = EXCH ? net.n_rows : net.N;
+  size_t smem = (size_t)4 * NR * (G * HPL) * sizeof(cpx<R>) + (EXCH ? NR * sizeof(int2) : 0) + NR * sizeof(R);
+  auto kern = rbm_sampler_kernel<R, G, HPL, ACT, EXCH>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -215,29 +244,29 @@ static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cud
   return cudaGetLastError();
 }
 
-template <typename R, int G, int ACT>
+template <typename R, int G, int ACT, bool EXCH>
 static cudaError_t sampler_hpl(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
   const int hpl = (net.M + G - 1) / G;
   switch (hpl) {
-    case 1: return sampler_inst<R, G, 1, ACT>(net, run, st);
-    case 2: return sampler_inst<R, G, 2, ACT>(net, run, st);
-    case 3: return sampler_inst<R, G, 3, ACT>(net, run, st);
-    case 4: return sampler_inst<R, G, 4, ACT>(net, run, st);
-    case 5: return sampler_inst<R, G, 5, ACT>(net, run, st);
-    case 6: return sampler_inst<R, G, 6, ACT>(net, run, st);
-    case 8: return sampler_inst<R, G, 8, ACT>(net, run, st);
-    case 10: return sampler_inst<R, G, 10, ACT>(net, run, st);
+    case 1: return sampler_inst<R, G, 1, ACT, EXCH>(net, run, st);
+    case 2: return sampler_inst<R, G, 2, ACT, EXCH>(net, run, st);
+    case 3: return sampler_inst<R, G, 3, ACT, EXCH>(net, run, st);
+    case 4: return sampler_inst<R, G, 4, ACT, EXCH>(net, run, st);
+    case 5: return sampler_inst<R, G, 5, ACT, EXCH>(net, run, st);
+    case 6: return sampler_inst<R, G, 6, ACT, EXCH>(net, run, st);
+    case 8: return sampler_inst<R, G, 8, ACT, EXCH>(net, run, st);
+    case 10: return sampler_inst<R, G, 10, ACT, EXCH>(net, run, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
-template <typename R, int ACT>
+template <typename R, int ACT, bool EXCH>
 static cudaError_t sampler_g(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st) {
   switch (G) {
-    case 4: return sampler_hpl<R, 4, ACT>(net, run, st);
-    case 8: return sampler_hpl<R, 8, ACT>(net, run, st);
-    case 16: return sampler_hpl<R, 16, ACT>(net, run, st);
-    case 32: return sampler_hpl<R, 32, ACT>(net, run, st);
+    case 4: return sampler_hpl<R, 4, ACT, EXCH>(net, run, st);
+    case 8: return sampler_hpl<R, 8, ACT, EXCH>(net, run, st);
+    case 16: return sampler_hpl<R, 16, ACT, EXCH>(net, run, st);
+    case 32: return sampler_hpl<R, 32, ACT, EXCH>(net, run, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -249,8 +278,13 @@ template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st) {
   if (net.N > 64 || net.M > 320) return cudaErrorInvalidValue;
   if (!hpl_ok((net.M + G - 1) / G)) return cudaErrorInvalidValue;
-  if (net.act == ACT_LOGCOSH) return sampler_g<R, ACT_LOGCOSH>(net, run, G, st);
-  return sampler_g<R, ACT_SOFTPLUS>(net, run, G, st);
+  if (net.pairs) {
+    // exchange rule: FP32 ket (RBM) handles only, instantiated in sampler_exch.cu
+    if constexpr (std::is_same<R, float>::value) return launch_rbm_sampler_exchange(net, run, G, st);
+    else return cudaErrorInvalidValue;
+  }
+  if (net.act == ACT_LOGCOSH) return sampler_g<R, ACT_LOGCOSH, false>(net, run, G, st);
+  return sampler_g<R, ACT_SOFTPLUS, false>(net, run, G, st);
 }
 
 

@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
            "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu",
-           "srcg.cu", "exact.cu"]
+           "srcg.cu", "exact.cu", "sampler_exch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -35,6 +35,7 @@ NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64, NQ_EVAL_TC_BF16X3 = 0, 1, 2, 3
 NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64, NQ_S_BF16 = 0, 1, 2, 3, 4
 NQ_SR_DIRECT, NQ_SR_CG = 0, 1
 NQ_SAMPLER_METROPOLIS, NQ_SAMPLER_EXACT = 0, 1
+NQ_RULE_LOCAL, NQ_RULE_EXCHANGE = 0, 1
 NQ_QUIRK_STALE_LAST_SLOT = 0x1
 
 
@@ -47,7 +48,7 @@ class NqConfig(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("eval_precision", ctypes.c_int32),
                 ("s_precision", ctypes.c_int32), ("quirks", ctypes.c_uint32),
                 ("sampler_lanes", ctypes.c_int32), ("sr_algorithm", ctypes.c_int32),
-                ("sampler_kind", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+                ("sampler_kind", ctypes.c_int32), ("rule", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class NqMeasurement(ctypes.Structure):
@@ -80,6 +81,7 @@ EXPORTS = {
     "nq_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]),
     "nq_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]),
     "nq_set_operator": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable)]),
+    "nq_set_exchange": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_int32)]),
     "nq_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]),
     "nq_set_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_logpsi": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),

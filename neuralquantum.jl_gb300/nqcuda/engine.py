@@ -10,7 +10,7 @@ from .networks import RBM, NDM, af_logcosh
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
                 s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT,
-                sampler_kind=_lib.NQ_SAMPLER_METROPOLIS):
+                sampler_kind=_lib.NQ_SAMPLER_METROPOLIS, rule=_lib.NQ_RULE_LOCAL):
     """nq_config of one problem (include/nqcuda.h)."""
     cfg = _lib.NqConfig()
     ph = physical(hilb)
@@ -38,6 +38,7 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
     cfg.sampler_lanes = sampler_lanes
     cfg.sr_algorithm = sr_algorithm
     cfg.sampler_kind = sampler_kind
+    cfg.rule = rule
     return cfg
 
 
@@ -45,10 +46,10 @@ class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
                  eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
                  sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT, sampler_kind=_lib.NQ_SAMPLER_METROPOLIS,
-                 _handle=None, _owner=None):
+                 rule=_lib.NQ_RULE_LOCAL, _handle=None, _owner=None):
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
-                          s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind)
+                          s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind, rule)
         self.complex_params = isinstance(net, RBM)
         self.cfg = cfg
         self.lib = L
@@ -105,6 +106,12 @@ class Engine:
         self._op = table           # keep the arrays alive
         st = table.struct()
         self._check(self.lib.nq_set_operator(self.h, ctypes.byref(st)))
+
+    def set_exchange(self, pairs):
+        """Couplings of the exchange rule: (i, j) pairs of 0-based sites."""
+        arr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        self._check(self.lib.nq_set_exchange(self.h, arr.shape[0],
+                                             arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
 
     # ---- stages -------------------------------------------------------------
     def sample(self, call_index, want_samples=True, want_accept_bits=False):

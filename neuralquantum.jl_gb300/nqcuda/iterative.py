@@ -77,9 +77,13 @@ class BatchedSampler:
         hilb = prob.hilb if not self.liouvillian else prob.hilb
         quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
         sr_alg = _lib.NQ_SR_CG if self.algo.iterative else _lib.NQ_SR_DIRECT
+        exch = getattr(getattr(sampler, "rule", None), "couplings", None)
         self.engine = Engine(net, hilb, batch_sz, sampler.chain_length, sampler.burn_length,
                              sampler.passes, sampler.seed, eval_precision, s_precision, quirks,
-                             sr_algorithm=sr_alg, sampler_kind=getattr(sampler, "kind", 0))
+                             sr_algorithm=sr_alg, sampler_kind=getattr(sampler, "kind", 0),
+                             rule=_lib.NQ_RULE_EXCHANGE if exch is not None else _lib.NQ_RULE_LOCAL)
+        if exch is not None:
+            self.engine.set_exchange(exch)
         if self.algo.iterative:
             self.engine.set_sr_tolerance(self.algo.precision, 10 * self.engine.P)
         self.engine.set_params(net.flat())

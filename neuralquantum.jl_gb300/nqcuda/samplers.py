@@ -5,6 +5,33 @@ class LocalRule:
     """Single-site flip proposals (src/Samplers/MCMCRules/LocalRule.jl:12-28)."""
 
 
+class ExchangeRule:
+    """``ExchangeRule(H)`` (src/Samplers/MCMCRules/ExchangeRule.jl:16-35):
+    the couplings (i, j) are the sites of the 2-site terms of the operator,
+    in its term order; 1-site terms are skipped and terms on more than two
+    sites are ignored with a warning, as in the reference.  A move draws one
+    coupling uniformly and swaps the two values (:38-68)."""
+
+    def __init__(self, op):
+        import warnings
+        ops = op.ops if hasattr(op, "ops") else [op]
+        pairs = []
+        for o in ops:
+            sites = list(o.sites)
+            if len(sites) == 1:
+                continue
+            if len(sites) > 2:
+                warnings.warn("Can't exchange between 3-site couplings. This coupling is ignored")
+                continue
+            pairs.append((int(sites[0]), int(sites[1])))
+        if not pairs:
+            raise ValueError("the operator has no 2-site terms")
+        self.couplings = pairs           # 0-based sites
+
+    def __repr__(self):
+        return f"ExchangeRule({len(self.couplings)} couplings)"
+
+
 class MetropolisSampler:
     """``MetropolisSampler(rule, chain_length, passes; burn=0, seed)``
     (src/Samplers/Metropolis.jl:26-40).  An even number of passes is raised

@@ -36,8 +36,13 @@ def init_configs(hilb, seed, call, chains, n_sites_total):
 
 def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
         doubled=False, stale_last_slot=False, prev_samples=None,
-        gpu_accept_bits=None, tie_tol=1e-3, chain_offset=0):
+        gpu_accept_bits=None, tie_tol=1e-3, chain_offset=0, couplings=None):
     """Replays one ``_sample_state!`` call.
+
+    ``couplings`` (list of 0-based site pairs) selects ExchangeRule
+    (src/Samplers/MCMCRules/ExchangeRule.jl:38-68): the step's draw picks
+    coupling ``(r0 * len(couplings)) >> 32`` and swaps its two values (a swap
+    of equal values proposes the same state, which ``u < exp(0)`` accepts).
 
     ``log_prob(batch)`` maps (B, nsites_total) configurations to 2 Re log psi.
     ``gpu_accept_bits`` (optional, (steps, B) bool) resolves near-tie
@@ -63,10 +68,16 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
     t = 0
     for sweep in range(n_sweeps):
         for _ in range(passes):
-            site, u = philox.mh_draws(seed, call, chains, t, nt)
-            new = sigma.copy()
             rows = np.arange(n_chains)
-            new[rows, site] = hilb.flip(sigma[rows, site])
+            new = sigma.copy()
+            if couplings is None:
+                site, u = philox.mh_draws(seed, call, chains, t, nt)
+                new[rows, site] = hilb.flip(sigma[rows, site])
+            else:
+                cidx, u = philox.mh_draws(seed, call, chains, t, len(couplings))
+                pr = np.asarray(couplings, dtype=np.int64)[cidx]
+                new[rows, pr[:, 0]] = sigma[rows, pr[:, 1]]
+                new[rows, pr[:, 1]] = sigma[rows, pr[:, 0]]
             lpn = log_prob(new)
             delta = lpn - lp
             with np.errstate(over="ignore", divide="ignore"):
