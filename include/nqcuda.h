@@ -109,8 +109,21 @@ typedef struct {
   int32_t sr_algorithm;    /* nq_sr_algorithm */
   int32_t sampler_kind;    /* nq_sampler_kind */
   int32_t rule;            /* nq_mcmc_rule (Metropolis sampler) */
-  int32_t reserved[3];
+  int32_t sampler_space;   /* nq_sampler_space */
+  int32_t reserved[2];
 } nq_config;
+
+/* Space the sampler draws from.  NQ_SPACE_NETWORK: the network's own space
+ * (the ket's N sites; the NDM's doubled (σ, η) space, p ∝ |ρ(σ,η)|²).
+ * NQ_SPACE_DIAGONAL (NDM only): the physical space with p(σ) ∝ ρ(σ,σ), the
+ * chains of BatchedObsDMSampler(net, sampler, hilb_doubled)
+ * (src/IterativeInterface/Samplers/Obs/BatchedObsDMSampler.jl:24-53, log
+ * probability real(logρ(σ,σ)) of src/base_networks.jl:157).  Such a handle
+ * samples N-site configurations and serves nq_sample, nq_set_samples,
+ * nq_logpsi / nq_logpsi_grad (logρ(σ,σ) of N-site σ) and nq_observable;
+ * the cost-function entry points (nq_set_operator, nq_estimate, SR,
+ * updates, nq_vmc_step) return NQ_ERR_UNSUPPORTED. */
+typedef enum { NQ_SPACE_NETWORK = 0, NQ_SPACE_DIAGONAL = 1 } nq_sampler_space;
 
 /* Metropolis transition rule (src/Samplers/MCMCRules/).  NQ_RULE_LOCAL:
  * LocalRule, one uniformly drawn site flips (LocalRule.jl:19-28).
@@ -227,8 +240,13 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out,
  * (src/IterativeInterface/Samplers/Obs/BatchedObsKetSampler.jl:42-60):
  * O_loc(σ) = Σ_σ' O_σσ' ψ(σ')/ψ(σ) over the samples of the last nq_sample /
  * nq_vmc_step (same estimator kernel as E_loc, another operator table) and
- * their Measurement.  loc_out (nullable): Ns complex128, [L][B].  RBM only;
- * the handle's own operator, S and F are left untouched. */
+ * their Measurement.  loc_out (nullable): Ns complex128, [L][B].  The
+ * handle's own operator, S and F are left untouched.
+ * ---- compute_observable(BatchedObsDMSampler, Ô) (BatchedObsDMSampler.jl:
+ * 80-105) on an NQ_SPACE_DIAGONAL NDM handle: Ô acts on the N physical
+ * sites, O_loc(σ) = Σ_σ' O_σσ' ρ(σ',σ)/ρ(σ,σ) (the connection changes the
+ * row, ApplyStateChanges.jl:18-21), so that the mean is Tr(ρÔ)/Tr(ρ).  An NDM
+ * handle sampling the doubled space returns NQ_ERR_UNSUPPORTED. */
 nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* stats, double* loc_out);
 /* S (nullable out): P x P column-major complex128 (real parameters: float64). */
 nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);

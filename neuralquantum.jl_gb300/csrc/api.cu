@@ -27,6 +27,9 @@ nq_status ndm_refresh(nq_handle* h) {
   b.C = (cpx<R>*)h->d_eff[0]; b.b = (cpx<R>*)h->d_eff[1]; b.a = (cpx<R>*)h->d_eff[2];
   b.Cs = (cpx<R>*)h->d_eff[3]; b.bs = (cpx<R>*)h->d_eff[4];
   CKL(launch_ndm_effective<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), b, h->st));
+  if (h->diag)
+    CKL(launch_ndm_diagonal<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), (cpx<R>*)h->d_diag[0], (cpx<R>*)h->d_diag[1],
+                               (cpx<R>*)h->d_diag[2], h->st));
   RbmDev<R> d = rbm_dev<R>(h);
   CKL(launch_rbm_tables<R>(d, (cpx<R>*)h->d_tab[0], (cpx<R>*)h->d_tab[1], (cpx<R>*)h->d_tab[2], h->st));
   return NQ_OK;
@@ -73,9 +76,10 @@ nq_status ensure_tuned(nq_handle* h) {
   if (h->exact || (h->sampler_lanes && h->sampler_block)) return NQ_OK;
   if (h->rule == NQ_RULE_EXCHANGE && h->n_exch == 0)
     return fail(h, NQ_ERR_STATE, "exchange rule: no couplings (nq_set_exchange)");
-  const int sN = h->ndm ? h->N2 : h->N, sM = h->ndm ? h->Ms : h->M;
+  const int sN = h->nst, sM = h->diag ? h->Md : (h->ndm ? h->Ms : h->M);
   const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb,
-                                   (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0) + (h->rule ? 4 * (h->n_exch + 1) : 0));
+                                   (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0) + (h->diag ? 8 : 0) +
+                                       (h->rule ? 4 * (h->n_exch + 1) : 0));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -86,7 +90,7 @@ nq_status ensure_tuned(nq_handle* h) {
     }
   }
   int cand[4];
-  const int rows = h->rule == NQ_RULE_EXCHANGE ? h->n_exch : (h->ndm ? h->N2 : h->N);
+  const int rows = h->rule == NQ_RULE_EXCHANGE ? h->n_exch : h->nst;
   int nc = rbm_sampler_valid_lanes(rows, sM, h->f64 ? 16 : 8, cand, 4);
   if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", sM);
   if (h->sampler_lanes) { cand[0] = h->sampler_lanes; nc = 1; }     // fixed by the caller
@@ -389,6 +393,15 @@ nq_status upload_op(nq_handle* h, const nq_op_table* t, DevOp* out, std::vector<
 
 }  // namespace
 
+// entry points of the cost function and the optimiser are not defined on a
+// handle that samples the diagonal of the density matrix
+#define NQ_REJECT_DIAG(h, what)                                                                           \
+  do {                                                                                                    \
+    if ((h)->diag)                                                                                        \
+      return fail((h), NQ_ERR_UNSUPPORTED, "%s: the handle samples the diagonal space (observables only)", \
+                  what);                                                                                  \
+  } while (0)
+
 // =============================== C ABI ======================================
 extern "C" {
 
@@ -425,9 +438,12 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (c.rule != NQ_RULE_LOCAL && c.rule != NQ_RULE_EXCHANGE) return bad("unknown rule");
   if (c.rule == NQ_RULE_EXCHANGE && (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64))
     return bad("the exchange rule is available for FP32 RBM handles");
+  if (c.sampler_space != NQ_SPACE_NETWORK && c.sampler_space != NQ_SPACE_DIAGONAL) return bad("unknown sampler_space");
+  if (c.sampler_space == NQ_SPACE_DIAGONAL && c.network != NQ_NET_NDM)
+    return bad("the diagonal sampler space is defined for the NDM");
   if (c.sampler_kind == NQ_SAMPLER_EXACT &&
-      (c.network == NQ_NET_NDM ? 2 * c.n_sites : c.n_sites) > 26)
-    return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM) <= 26");
+      (c.network == NQ_NET_NDM && c.sampler_space == NQ_SPACE_NETWORK ? 2 * c.n_sites : c.n_sites) > 26)
+    return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM's doubled space) <= 26");
   if (c.sr_algorithm == NQ_SR_CG &&
       (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64 ||
        !sr_cg_supported(c.n_sites + c.n_hidden + c.n_sites * c.n_hidden))) {
@@ -451,7 +467,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     h->N2 = 2 * h->N;
     h->U = 4 * h->Mh + h->Ma;
     h->Ms = 2 * h->Mh + h->Ma;
-    h->nst = h->N2;
+    h->diag = c.sampler_space == NQ_SPACE_DIAGONAL;
+    h->Md = h->Mh + h->Ma;
+    h->nst = h->diag ? h->N : h->N2;
     h->P = ndm_n_params(h->N, h->Mh, h->Ma);
     if (h->N2 > 64) return bad("the NDM supports n_sites <= 32 (2N doubled sites)");
     if (h->Ms > 320) return bad("2*n_hidden + n_ancilla must be <= 320");
@@ -473,7 +491,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->tc_theta = c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3;
   h->theta_terms = c.eval_precision == NQ_EVAL_TC_BF16X3 ? 3 : 2;
   h->complex_params = !h->ndm;
-  const int sampler_M = h->ndm ? h->Ms : h->M, sampler_N = h->ndm ? h->N2 : h->N;
+  const int sampler_M = h->diag ? h->Md : (h->ndm ? h->Ms : h->M), sampler_N = h->nst;
   if (c.sampler_lanes != 0) {
     int cand[4];
     const int nc = rbm_sampler_valid_lanes(sampler_N, sampler_M, h->f64 ? 16 : 8, cand, 4);
@@ -500,7 +518,12 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (h->ndm) {
     const size_t ne[5] = {(size_t)h->U * h->N2, (size_t)h->U, (size_t)h->N2, (size_t)h->Ms * h->N2, (size_t)h->Ms};
     for (int k = 0; k < 5; ++k) step(cudaMalloc(&h->d_eff[k], ne[k] * csz + 16), "effective network");
-    step(dalloc(&h->d_ndm_partial, (size_t)ndm_grad_nblocks(h->Ns) * 2 * h->P), "ndm partial");
+    if (h->diag) {
+      const size_t nd[3] = {(size_t)h->N, (size_t)h->Md, (size_t)h->Md * h->N};
+      for (int k = 0; k < 3; ++k) step(cudaMalloc(&h->d_diag[k], nd[k] * csz + 16), "diagonal network");
+    } else {
+      step(dalloc(&h->d_ndm_partial, (size_t)ndm_grad_nblocks(h->Ns) * 2 * h->P), "ndm partial");
+    }
   }
   step(dalloc(&h->d_samples, (size_t)h->Ns), "samples");
   step(dalloc(&h->d_accepted, 1), "accepted");
@@ -521,7 +544,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->cg = c.sr_algorithm == NQ_SR_CG;
   h->exact = c.sampler_kind == NQ_SAMPLER_EXACT;
   h->rule = c.rule;
-  if (h->exact) step(dalloc(&h->d_exact, exact_sampler_work_doubles(h->ndm ? h->N2 : h->N)), "exact sampler");
+  if (h->exact) step(dalloc(&h->d_exact, exact_sampler_work_doubles(h->nst)), "exact sampler");
+  // the diagonal-space handle estimates observables only: no S, X or solve buffers
+  const bool sr_bufs = !h->cg && !h->diag;
   const int rows = 2 * P;
   const int rp = ((rows + 127) / 128) * 128;
   if (h->cg) {
@@ -556,9 +581,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     while (tiles * ks < 2 * 152 && ks < 16 && h->Ns / (ks * 2) >= 256) ks *= 2;
     h->gram_ksplit = ks;
   }
-  if (!h->cg) step(dalloc(&h->d_G, (size_t)rows * rows), "G");
-  if (!h->cg) step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
-  if (h->cg) {
+  if (sr_bufs) step(dalloc(&h->d_G, (size_t)rows * rows), "G");
+  if (sr_bufs) step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
+  if (!sr_bufs) {
   } else if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3 || c.s_precision == NQ_S_BF16) {
     const int bf16 = c.s_precision == NQ_S_BF16 ? 1 : 0;
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
@@ -572,7 +597,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
   }
-  if (!h->cg) {
+  if (sr_bufs) {
     step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");
     step(dalloc(&h->sb.W, (size_t)P * P), "W");
     step(dalloc(&h->sb.x, 2 * (size_t)P), "x");
@@ -583,6 +608,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     step(dalloc(&h->sb.work, sweep_work_elems(P)), "sweep work");
     step(dalloc(&h->sb.yf, (size_t)P), "yf");
   }
+  if (h->diag) step(dalloc(&h->sb.status, 1), "status");
   if (h->tc_theta) step(dalloc(&h->d_theta_img, theta_tc_image_elems(h->M, h->theta_terms)), "theta image");
   h->sb.S = h->d_S;
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
@@ -596,7 +622,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     step(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st), "memset");
     // sample buffer starts as the state() fill: all sites at local index 0
     step(cudaMemsetAsync(h->d_samples, 0, sizeof(uint64_t) * h->Ns, h->st), "memset");
-    if (!h->cg) step(cudaMemsetAsync(h->d_S, 0, 2 * sizeof(double) * P * P, h->st), "memset");
+    if (sr_bufs) step(cudaMemsetAsync(h->d_S, 0, 2 * sizeof(double) * P * P, h->st), "memset");
     if (refresh_params(h) != NQ_OK) s = NQ_ERR_CUDA;
     step(cudaStreamSynchronize(h->st), "sync");
   }
@@ -621,7 +647,8 @@ void nq_destroy(nq_handle* h) {
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
                   h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_exact, h->d_pairs, h->d_xtab[0],
                   h->d_xtab[1], h->d_xtab[2], h->d_xW, h->d_xare, h->d_dw, h->d_eff[0], h->d_eff[1],
-                  h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial};
+                  h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial,
+                  h->d_diag[0], h->d_diag[1], h->d_diag[2]};
   for (void* p : bufs)
     if (p) cudaFree(p);
   {
@@ -727,6 +754,7 @@ nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs) {
 
 nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
   if (!h || !t) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_set_operator");
   if (nq_status v = validate_op(h, t)) return v;
   CK(cudaStreamSynchronize(h->st));
   free_op(h);
@@ -764,7 +792,9 @@ nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
 
 nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* stats, double* loc_out) {
   if (!h || !obs || !stats) return NQ_ERR_ARG;
-  if (h->ndm) return fail(h, NQ_ERR_UNSUPPORTED, "observables of density matrices are not provided");
+  if (h->ndm && !h->diag)
+    return fail(h, NQ_ERR_UNSUPPORTED,
+                "observables of a density matrix are estimated on its diagonal (NQ_SPACE_DIAGONAL handle)");
   if (nq_status v = validate_op(h, obs)) return v;
   std::vector<void*> allocs;
   DevOp d;
@@ -787,7 +817,17 @@ nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* st
     return cleanup(fail(h, NQ_ERR_CUDA, "observable buffers"));
   cudaError_t e;
   ++h->launches;
-  if (h->f64) {
+  if (h->diag) {
+    if (h->f64) {
+      e = launch_ndm_diag_obs<double>(ndm_eff<double>(h), h->act, d, h->d_samples, h->Ns, h->hilb,
+                                      (cpx<double>*)d_lp, (cpx<double>*)d_loc, h->st);
+      if (e == cudaSuccess) e = launch_stats<double>((cpx<double>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
+    } else {
+      e = launch_ndm_diag_obs<float>(ndm_eff<float>(h), h->act, d, h->d_samples, h->Ns, h->hilb,
+                                     (cpx<float>*)d_lp, (cpx<float>*)d_loc, h->st);
+      if (e == cudaSuccess) e = launch_stats<float>((cpx<float>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
+    }
+  } else if (h->f64) {
     e = launch_rbm_eval<double>(rbm_dev<double>(h), h->d_samples, h->Ns, &d, (cpx<double>*)d_lp, nullptr,
                                 (cpx<double>*)d_loc, h->st);
     if (e == cudaSuccess) e = launch_stats<double>((cpx<double>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
@@ -879,6 +919,7 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
   CK(cudaMemcpyAsync(d_v, sigma, (size_t)n * h->nst, cudaMemcpyHostToDevice, h->st));
   ++h->launches;
   CK(launch_pack_int8(d_v, h->nst, n, h->hilb, d_bits, h->st));
+  if (h->diag) CKL(launch_ndm_diag_expand(d_bits, (int)n, h->N, d_bits, h->st));   // logρ(σ,σ)
   if (h->ndm) {
     if (grad) CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
     if (h->f64) CKL(launch_ndm_eval<double>(ndm_eff<double>(h), h->act, d_bits, (int)n, h->hilb, (cpx<double>*)d_lp, nullptr, 0, d_out, h->st));
@@ -922,6 +963,7 @@ nq_status nq_logpsi_grad(nq_handle* h, const int8_t* sigma, int64_t n, double* o
 
 nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, double* force_out) {
   if (!h) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_estimate");
   if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
   nq_status s;
   CK(cudaEventRecord(h->ev[1], h->st));
@@ -979,6 +1021,7 @@ nq_status nq_sr_info(nq_handle* h, double* out2) {
 nq_status nq_get_sr_matrix(nq_handle* h, double* s_out) {
   if (h && h->cg) return fail(h, NQ_ERR_STATE, "S is not formed by the matrix-free SR solve (NQ_SR_CG)");
   if (!h || !s_out) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_get_sr_matrix");
   std::vector<double> S(2 * (size_t)h->P * h->P);
   CK(cudaMemcpyAsync(S.data(), h->d_S, S.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -991,6 +1034,7 @@ nq_status nq_get_sr_matrix(nq_handle* h, double* s_out) {
 nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0, double b,
                           double lam_min, int32_t iter, double* dw_out) {
   if (!h) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_precondition");
   if (kind < 0 || kind > 2) return fail(h, NQ_ERR_ARG, "unknown precondition kind %d", kind);
   double lam = 0.0;
   if (kind == 1) lam = std::max(lam0 * std::pow(b, (double)iter), lam_min);
@@ -1013,6 +1057,7 @@ nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0, d
 
 nq_status nq_update_descent(nq_handle* h, double lr) {
   if (!h) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_update_descent");
   CK(cudaEventRecord(h->ev[5], h->st));
   nq_status s = stage_update(h, lr);
   if (s != NQ_OK) return s;
@@ -1028,6 +1073,7 @@ nq_status nq_update_descent(nq_handle* h, double lr) {
 // node, so one graph serves every iteration.
 nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, nq_measurement* stats) {
   if (!h) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_vmc_step");
   if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
   if (h->graph && (h->graph_eps != eps || h->graph_lr != lr)) {
     cudaGraphExecDestroy(h->graph);

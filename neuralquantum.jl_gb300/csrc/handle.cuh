@@ -24,6 +24,9 @@ struct nq_handle {
   int n_record = 0, write_last = 0;
   bool doubled = false, complex_params = true, f64 = false, ndm = false;
   int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
+  bool diag = false;               // NQ_SPACE_DIAGONAL: NDM chains on the physical space, p ∝ ρ(σ,σ)
+  int Md = 0;                      // diagonal sampler units (Mh + Ma)
+  void* d_diag[3] = {};            // diagonal sampler network a [N], b [Md], W [Md x N] (cpx<R>)
   void* d_eff[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // C, b, a, Cs, bs (cpx<R>)
   void* d_w = nullptr;             // NDM connection weights [Ns][maxc] cpx<R>
   int* d_wconn = nullptr;          // connection ids [Ns][maxc]
@@ -137,13 +140,19 @@ cudaError_t dalloc(T** p, size_t count) {
   return cudaMalloc((void**)p, count * sizeof(T) + 16);
 }
 
-// Sampler / table view of the network: the RBM itself, or for the NDM the
-// effective network of the units entering |ρ|^2 over the 2N doubled sites.
+// Sampler / table view of the network: the RBM itself, for the NDM the
+// effective network of the units entering |ρ|^2 over the 2N doubled sites,
+// or on the diagonal space the N-site network of ρ(σ,σ).
 template <typename R>
 RbmDev<R> rbm_dev(nq_handle* h) {
   RbmDev<R> d;
   d.act = h->act; d.hilb = h->hilb;
-  if (h->ndm) {
+  if (h->diag) {
+    d.N = h->N; d.M = h->Md; d.n_half = h->Md;
+    d.a = reinterpret_cast<const cpx<R>*>(h->d_diag[0]);
+    d.b = reinterpret_cast<const cpx<R>*>(h->d_diag[1]);
+    d.W = reinterpret_cast<const cpx<R>*>(h->d_diag[2]);
+  } else if (h->ndm) {
     d.N = h->N2; d.M = h->Ms; d.n_half = 2 * h->Mh;
     d.a = reinterpret_cast<const cpx<R>*>(h->d_eff[2]);
     d.b = reinterpret_cast<const cpx<R>*>(h->d_eff[4]);

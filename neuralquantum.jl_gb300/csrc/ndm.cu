@@ -225,6 +225,75 @@ ndm_loc_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int 
 }
 
 // ---------------------------------------------------------------------------
+// Diagonal observables (BatchedObsDMSampler.jl:90-105 with
+// AccumulatorObsScalar.jl:52-137 over a doubled buffer): at the doubled
+// configuration (σ, σ) of a physical sample, O_loc(σ) = Σ_c mel_c
+// ρ(σ'_c, σ)/ρ(σ, σ), the connection's changes applied to the row sites
+// (ApplyStateChanges.jl:18-21), which are the doubled sites 0..N-1.  Zero
+// elements are skipped and elements without changes add mel (:90-107).
+// ---------------------------------------------------------------------------
+template <typename R, int ACT>
+__global__ void __launch_bounds__(128)
+ndm_diag_obs_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int n, int hilb,
+                    cpx<R>* __restrict__ logrho, cpx<R>* __restrict__ O) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = blockDim.x, U = e.U;
+  cpx<R>* sx = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* sg = sx + (size_t)U * T;
+  const int s = blockIdx.x * T + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t phys = samples[s];
+  const uint64_t bits = phys | (phys << e.N);
+  const cpx<R> lp = ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
+  if (logrho) logrho[s] = lp;
+  cpx<R> acc = mk(R(0), R(0));
+  for (int o = 0; o < op.n_ops; ++o) {
+    const int ns_o = __ldg(op.op_n_sites + o);
+    int r = 0;
+    for (int d = 0; d < ns_o; ++d) r |= (int)((phys >> __ldg(op.op_sites + 8 * o + d)) & 1ull) << d;
+    const int row = __ldg(op.op_row_offset + o) + r;
+    const int c0 = __ldg(op.row_conn_offset + row), c1 = __ldg(op.row_conn_offset + row + 1);
+    for (int c = c0; c < c1; ++c) {
+      const double mre = __ldg(op.conn_mel + 2 * c), mim = __ldg(op.conn_mel + 2 * c + 1);
+      if (mre == 0.0 && mim == 0.0) continue;
+      const int nch = __ldg(op.conn_n_changes + c);
+      if (nch == 0) {
+        acc.x += (R)mre;
+        acc.y += (R)mim;
+        continue;
+      }
+      const cpx<R> d = ndm_delta<R, ACT>(e, op, c, bits, hilb, sx + threadIdx.x, T, nch);
+      acc = acc + mk((R)mre, (R)mim) * cexpc(d);
+    }
+  }
+  O[s] = acc;
+}
+
+// N-site tables of the diagonal logρ(σ,σ) = b_la·σ + Σ_h f(h_la + w_la σ) +
+// Σ_k f(d_la + u_la σ) (NDM.jl:76-96 at η = σ: the μ units cancel and the
+// ancilla unit has no phase), in the sampler's convention log p =
+// 2 Re aᵀσ + Σ_u c_u 2 Re f(θ_u) with every unit at c_u = 1/2:
+// a = b_la / 2, units [λ (Mh), ancilla (Ma)].
+template <typename R>
+__global__ void ndm_diagonal_kernel(NdmDev<R> n, cpx<R>* __restrict__ a, cpx<R>* __restrict__ b,
+                                    cpx<R>* __restrict__ W) {
+  const int N = n.N, Mh = n.Mh, Ma = n.Ma, Md = Mh + Ma;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < Md * N) {
+    const int u = idx % Md, j = idx / Md;
+    W[idx] = mk(u < Mh ? n.w_la[u + Mh * j] : n.u_la[(u - Mh) + Ma * j], R(0));
+  }
+  if (idx < Md) b[idx] = mk(idx < Mh ? n.h_la[idx] : n.d_la[idx - Mh], R(0));
+  if (idx < N) a[idx] = mk(R(0.5) * n.b_la[idx], R(0));
+}
+
+// doubled configuration (σ, σ) of each physical configuration σ
+__global__ void ndm_diag_expand_kernel(const uint64_t* in, int n, int N, uint64_t* out) {   // in == out allowed
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[s] = in[s] | (in[s] << N);
+}
+
+// ---------------------------------------------------------------------------
 // Gradient accumulation G_k = Σ_s conj(L_s) Σ_c w_c O_k(σ'_c) (the
 // conj(Σ L conj(∇L)) of BatchedGradSampler.jl:108-111).  One block per chunk
 // of samples; connections are expanded 32 at a time into shared memory (their
@@ -441,6 +510,37 @@ cudaError_t launch_ndm_loc(const NdmEff<R>& e, int act, const DevOp& op, const u
   return cudaGetLastError();
 }
 
+template <typename R>
+cudaError_t launch_ndm_diag_obs(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+                                int hilb, cpx<R>* logrho, cpx<R>* O, cudaStream_t st) {
+  if (n < 1) return cudaSuccess;
+  const int T = ndm_threads<R>(e.U);
+  const size_t smem = unit_smem<R>(e.U, T);
+  cudaError_t err;
+  if (act == ACT_LOGCOSH) {
+    if ((err = set_smem<R>(ndm_diag_obs_kernel<R, ACT_LOGCOSH>, smem)) != cudaSuccess) return err;
+    ndm_diag_obs_kernel<R, ACT_LOGCOSH><<<(n + T - 1) / T, T, smem, st>>>(e, op, samples, n, hilb, logrho, O);
+  } else {
+    if ((err = set_smem<R>(ndm_diag_obs_kernel<R, ACT_SOFTPLUS>, smem)) != cudaSuccess) return err;
+    ndm_diag_obs_kernel<R, ACT_SOFTPLUS><<<(n + T - 1) / T, T, smem, st>>>(e, op, samples, n, hilb, logrho, O);
+  }
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_ndm_diagonal(const NdmDev<R>& n, cpx<R>* a, cpx<R>* b, cpx<R>* W, cudaStream_t st) {
+  const int md = n.Mh + n.Ma;
+  const int tot = md * n.N > n.N ? md * n.N : n.N;
+  ndm_diagonal_kernel<R><<<(tot + 127) / 128, 128, 0, st>>>(n, a, b, W);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ndm_diag_expand(const uint64_t* in, int n, int N, uint64_t* out, cudaStream_t st) {
+  if (n < 1) return cudaSuccess;
+  ndm_diag_expand_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, N, out);
+  return cudaGetLastError();
+}
+
 int ndm_grad_chunk() { return 16; }
 
 template <typename R>
@@ -487,3 +587,7 @@ template cudaError_t launch_ndm_loc<float>(const NdmEff<float>&, int, const DevO
 template cudaError_t launch_ndm_loc<double>(const NdmEff<double>&, int, const DevOp&, const uint64_t*, int, int, int, cpx<double>*, cpx<double>*, int*, int*, cudaStream_t);
 template cudaError_t launch_ndm_grad<float>(const NdmEff<float>&, int, const DevOp&, const uint64_t*, int, int, int, const cpx<float>*, const cpx<float>*, const int*, const int*, double*, const double*, const double*, double*, cudaStream_t);
 template cudaError_t launch_ndm_grad<double>(const NdmEff<double>&, int, const DevOp&, const uint64_t*, int, int, int, const cpx<double>*, const cpx<double>*, const int*, const int*, double*, const double*, const double*, double*, cudaStream_t);
+template cudaError_t launch_ndm_diag_obs<float>(const NdmEff<float>&, int, const DevOp&, const uint64_t*, int, int, cpx<float>*, cpx<float>*, cudaStream_t);
+template cudaError_t launch_ndm_diag_obs<double>(const NdmEff<double>&, int, const DevOp&, const uint64_t*, int, int, cpx<double>*, cpx<double>*, cudaStream_t);
+template cudaError_t launch_ndm_diagonal<float>(const NdmDev<float>&, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
+template cudaError_t launch_ndm_diagonal<double>(const NdmDev<double>&, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);

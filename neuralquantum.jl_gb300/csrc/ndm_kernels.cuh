@@ -57,6 +57,17 @@ cudaError_t launch_ndm_grad(const NdmEff<R>& e, int act, const DevOp& op, const 
                             const int* nconn, double* partial, const double* meanO, const double* stats,
                             double* force, cudaStream_t st);
 int ndm_grad_nblocks(int n);
+// BatchedObsDMSampler: O_loc(σ) = Σ_σ' O_σσ' ρ(σ',σ)/ρ(σ,σ) of physical samples
+// (N-site bits) and logρ(σ,σ) (nullable)
+template <typename R>
+cudaError_t launch_ndm_diag_obs(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+                                int hilb, cpx<R>* logrho, cpx<R>* O, cudaStream_t st);
+// N-site sampler tables of p(σ) ∝ ρ(σ,σ): a [N], b [Mh+Ma], W [(Mh+Ma) x N]
+template <typename R>
+cudaError_t launch_ndm_diagonal(const NdmDev<R>& n, cpx<R>* a, cpx<R>* b, cpx<R>* W, cudaStream_t st);
+// out[s] = (σ, σ) as 2N-site bits
+cudaError_t launch_ndm_diag_expand(const uint64_t* in, int n, int N, uint64_t* out, cudaStream_t st);
+
 // centre the rows of X (rows x ld, first ns columns valid), meanO[r] = row mean;
 // tf32: round to TF32 and write the remainder to Xlo (if given)
 cudaError_t launch_x_center(float* X, float* Xlo, int rows, int ld, int ns, double* meanO, int tf32,

@@ -13,7 +13,8 @@ from .operators import (LocalOperator, KLocalOperator, KLocalOperatorSum, KLocal
 from .networks import RBM, NDM, af_logcosh, af_softplus, init_random_pars_  # noqa: F401
 from .samplers import MetropolisSampler, ExactSampler, LocalRule, ExchangeRule  # noqa: F401
 from .stats import Measurement  # noqa: F401
-from .iterative import (BatchedSampler, BatchedObsKetSampler, add_observable_, SR, Descent, sample_,  # noqa: F401
+from .iterative import (BatchedSampler, BatchedObsKetSampler, BatchedObsDMSampler, add_observable_,  # noqa: F401
+                        compute_observables, SR, Descent, sample_,  # noqa: F401
                         precondition_, update_,  # noqa: F401
                         sr_shift, sr_multiplicative, sr_none, sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq)
 from .engine import Engine, ProblemBatch  # noqa: F401

@@ -36,6 +36,7 @@ NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64, NQ_S_BF16 = 0, 1, 2, 3, 4
 NQ_SR_DIRECT, NQ_SR_CG = 0, 1
 NQ_SAMPLER_METROPOLIS, NQ_SAMPLER_EXACT = 0, 1
 NQ_RULE_LOCAL, NQ_RULE_EXCHANGE = 0, 1
+NQ_SPACE_NETWORK, NQ_SPACE_DIAGONAL = 0, 1
 NQ_QUIRK_STALE_LAST_SLOT = 0x1
 
 
@@ -48,7 +49,8 @@ class NqConfig(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("eval_precision", ctypes.c_int32),
                 ("s_precision", ctypes.c_int32), ("quirks", ctypes.c_uint32),
                 ("sampler_lanes", ctypes.c_int32), ("sr_algorithm", ctypes.c_int32),
-                ("sampler_kind", ctypes.c_int32), ("rule", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("sampler_kind", ctypes.c_int32), ("rule", ctypes.c_int32), ("sampler_space", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class NqMeasurement(ctypes.Structure):

@@ -10,7 +10,8 @@ from .networks import RBM, NDM, af_logcosh
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
                 s_precision=_lib.NQ_S_F32, quirks=0, sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT,
-                sampler_kind=_lib.NQ_SAMPLER_METROPOLIS, rule=_lib.NQ_RULE_LOCAL):
+                sampler_kind=_lib.NQ_SAMPLER_METROPOLIS, rule=_lib.NQ_RULE_LOCAL,
+                sampler_space=_lib.NQ_SPACE_NETWORK):
     """nq_config of one problem (include/nqcuda.h)."""
     cfg = _lib.NqConfig()
     ph = physical(hilb)
@@ -39,6 +40,7 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
     cfg.sr_algorithm = sr_algorithm
     cfg.sampler_kind = sampler_kind
     cfg.rule = rule
+    cfg.sampler_space = sampler_space
     return cfg
 
 
@@ -46,10 +48,10 @@ class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
                  eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
                  sampler_lanes=0, sr_algorithm=_lib.NQ_SR_DIRECT, sampler_kind=_lib.NQ_SAMPLER_METROPOLIS,
-                 rule=_lib.NQ_RULE_LOCAL, _handle=None, _owner=None):
+                 rule=_lib.NQ_RULE_LOCAL, sampler_space=_lib.NQ_SPACE_NETWORK, _handle=None, _owner=None):
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
-                          s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind, rule)
+                          s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind, rule, sampler_space)
         self.complex_params = isinstance(net, RBM)
         self.cfg = cfg
         self.lib = L
@@ -65,7 +67,8 @@ class Engine:
         ph = physical(hilb)
         self.P = int(L.nq_n_params(self.h))
         self.N = ph.n_sites
-        self.nsites = 2 * ph.n_sites if isinstance(hilb, SuperOpSpace) else ph.n_sites
+        doubled = isinstance(hilb, SuperOpSpace) and sampler_space == _lib.NQ_SPACE_NETWORK
+        self.nsites = 2 * ph.n_sites if doubled else ph.n_sites
         self.B, self.L = n_chains, chain_length
         self.passes = passes + 1 if passes % 2 == 0 else passes
         self._op = None

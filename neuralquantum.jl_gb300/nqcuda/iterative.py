@@ -156,5 +156,61 @@ class BatchedObsKetSampler:
         return self.results
 
 
+class BatchedObsDMSampler:
+    """``BatchedObsDMSampler(net, sampler, hilb_doubled; batch_sz)``
+    (Obs/BatchedObsDMSampler.jl:24-105): its own chains on the physical
+    space with p(σ) ∝ ρ(σ,σ), and for each observable Ô the local values
+    O_loc(σ) = Σ_σ' O_σσ' ρ(σ',σ)/ρ(σ,σ), whose mean is Tr(ρÔ)/Tr(ρ).  Every
+    compute call draws a new set of samples (sample call index 0, 1, ...);
+    the network's current parameters are uploaded first."""
+
+    def __init__(self, net, sampler, hilb_doubled, batch_sz=16, eval_precision=_lib.NQ_EVAL_F32,
+                 reference_quirks=False):
+        from .networks import NDM
+        if not isinstance(net, NDM):
+            raise TypeError("BatchedObsDMSampler needs a density-matrix network (NDM)")
+        self.net = net
+        self.sampler = sampler
+        self.hilb = hilb_doubled
+        quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
+        if getattr(getattr(sampler, "rule", None), "couplings", None) is not None:
+            raise NotImplementedError("the diagonal sampler uses LocalRule")
+        self.engine = Engine(net, hilb_doubled, batch_sz, sampler.chain_length, sampler.burn_length,
+                             sampler.passes, sampler.seed, eval_precision, _lib.NQ_S_F32, quirks,
+                             sampler_kind=getattr(sampler, "kind", 0), sampler_space=_lib.NQ_SPACE_DIAGONAL)
+        self.engine.set_params(net.flat())
+        self.observables = {}
+        self.results = {}
+        self.calls = 0
+
+    def add_observable_(self, name, op):
+        self.observables[name] = op_table(op)
+
+    def _sample(self):
+        self.engine.set_params(self.net.flat())
+        self.engine.sample(self.calls, want_samples=False)
+        self.calls += 1
+
+    def _eval(self, table):
+        m, _ = self.engine.observable(table)
+        return Measurement(complex(m.mean_re, m.mean_im), m.error, m.variance, m.tau, m.R)
+
+    def compute_observable(self, op):
+        self._sample()
+        return self._eval(op if hasattr(op, "struct") else op_table(op))
+
+    def compute_observables(self):
+        if not self.observables:
+            return None
+        self._sample()
+        for name, table in self.observables.items():
+            self.results[name] = self._eval(table)
+        return self.results
+
+
+def compute_observables(obs):
+    return obs.compute_observables()
+
+
 def add_observable_(obs, name, op):
     obs.add_observable_(name, op)

@@ -10,6 +10,11 @@
   ``mel ρ'/ρ`` to L_loc and ``mel ρ'/ρ O(σ')`` to ∇L_loc (no -O(σ) term,
   :113); BatchedGradSampler.jl:77-123 then forms C = mean|L_loc|^2 and
   F = conj(Σ L_s conj(∇L_s)/Ns - C conj(<O>)).
+* density-matrix observables: BatchedObsDMSampler.jl:90-105 evaluates
+  AccumulatorObsScalar over a doubled buffer filled with (σ, σ)
+  (States.jl:131-132); a connection's changes go to the row
+  (ApplyStateChanges.jl:18-21), so O_loc(σ) = Σ mel ρ(σ', σ)/ρ(σ, σ), with
+  the same zero-skip and no-change rules as the ket estimator.
 """
 import numpy as np
 
@@ -38,6 +43,32 @@ def local_energy(net, H, samples):
         owner = np.array(owner)
         lp = net.logpsi(prime)
         np.add.at(res, owner, np.array(mels) * np.exp(lp - lpsi[owner]))
+    return res
+
+
+def local_observable_dm(net, O, samples):
+    """O_loc for physical samples (Ns, N) of the diagonal chain of an NDM;
+    returns complex (Ns,)."""
+    samples = np.atleast_2d(samples)
+    ns = samples.shape[0]
+    lrho = net.logpsi(samples, samples)
+    res = np.zeros(ns, dtype=np.complex128)
+    prime, owner, mels = [], [], []
+    for s in range(ns):
+        for mel, ch in connections_ket(O, samples[s]):
+            if mel == 0:
+                continue
+            if len(ch) == 0:
+                res[s] += mel
+            else:
+                prime.append(apply_changes(samples[s], ch))
+                owner.append(s)
+                mels.append(mel)
+    if prime:
+        prime = np.array(prime)
+        owner = np.array(owner)
+        lp = net.logpsi(prime, samples[owner])
+        np.add.at(res, owner, np.array(mels) * np.exp(lp - lrho[owner]))
     return res
 
 

@@ -5,7 +5,7 @@
   conventions pinned by test/Operators/ising.jl:5-42),
 * a matrix-free Lanczos ground state for the 1D TFIM of examples/ising1d.jl
   (known answer -1.274549484318 * 20, examples/ising1d.jl:46-47),
-* exact |ψ|^2 / |ρ|^2 distributions for chi-square sampler tests
+* exact |ψ|^2 / |ρ|^2 / ρ(σ,σ) distributions for chi-square sampler tests
   (test/Samplers/test_samplers.jl:7-31).
 """
 import numpy as np
@@ -92,6 +92,29 @@ def doubled_distribution(net, hilb):
     lp = np.real(net.logpsi(sr, sc)) * 2
     p = np.exp(lp - lp.max())
     return p / p.sum()      # index = col*D + row
+
+
+def diagonal_distribution(net, hilb):
+    """p(σ) ∝ ρ(σ, σ) = exp(Re logρ(σ, σ)) (base_networks.jl:157), index = σ."""
+    st = hilb.all_states()
+    lp = np.real(net.logpsi(st, st))
+    p = np.exp(lp - lp.max())
+    return p / p.sum()
+
+
+def density_matrix(net, hilb):
+    """ρ[σ, η] = exp(logρ(σ, η)) over all states (row index σ)."""
+    st = hilb.all_states()
+    D = hilb.dim
+    sr = np.repeat(st, D, axis=0)                                    # row slow
+    sc = np.repeat(st[None], D, axis=0).reshape(-1, hilb.n_sites)    # column fast
+    return np.exp(net.logpsi(sr, sc)).reshape(D, D)
+
+
+def dm_expectation(net, O):
+    """Tr(ρ O) / Tr(ρ) by dense enumeration."""
+    rho = density_matrix(net, O.hilb)
+    return np.trace(rho @ ops.to_matrix(O)) / np.trace(rho)
 
 
 def exact_local_energy_expectation(net, H):

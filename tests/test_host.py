@@ -45,6 +45,21 @@ def test_create_rejects_bad_config_without_touching_the_gpu():
     assert lib.nq_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.NQ_ERR_ARG
     assert not h.value
     assert lib.nq_create(None, ctypes.byref(h)) == _lib.NQ_ERR_ARG
+    # the diagonal sampler space is defined for the NDM only; unknown spaces are refused
+    for net, space in ((_lib.NQ_NET_RBM, _lib.NQ_SPACE_DIAGONAL), (_lib.NQ_NET_NDM, 5)):
+        cfg = _lib.NqConfig()
+        cfg.network, cfg.activation, cfg.hilbert = net, _lib.NQ_ACT_SOFTPLUS, _lib.NQ_HILB_FOCK
+        cfg.n_sites, cfg.n_hidden, cfg.n_ancilla, cfg.n_chains, cfg.chain_length, cfg.passes = 4, 4, 4, 16, 2, 1
+        cfg.sampler_space = space
+        assert lib.nq_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.NQ_ERR_ARG
+        assert not h.value
+
+
+def test_config_layout_matches_header():
+    """nq_config keeps the C layout of include/nqcuda.h: sampler_space takes
+    the first reserved word, the size is unchanged."""
+    assert ctypes.sizeof(_lib.NqConfig) == 88
+    assert _lib.NqConfig.sampler_space.offset == 76
 
 
 def _random_configs(n, N, kind, rng):
@@ -118,7 +133,8 @@ def test_host_api_mirrors_reference_names():
     for name in ("BatchedSampler", "MetropolisSampler", "LocalRule", "RBM", "NDM", "SR",
                  "Descent", "sample_", "precondition_", "update_", "sigmax", "sigmaz", "sigmam",
                  "liouvillian", "LocalOperator", "init_random_pars_", "HomogeneousSpin",
-                 "HomogeneousFock"):
+                 "HomogeneousFock", "BatchedObsKetSampler", "BatchedObsDMSampler", "ExactSampler",
+                 "ExchangeRule", "add_observable_", "compute_observables"):
         assert hasattr(nq, name), name
     s = nq.MetropolisSampler(nq.LocalRule(), 20, 20, burn=50)
     assert s.passes == 21        # Metropolis.jl:30-38

@@ -160,6 +160,31 @@ def test_liouvillian_local_values_exact():
     assert np.max(np.abs(L - Lrho / rho)) < 1e-9
 
 
+@pytest.mark.parametrize("kind", [SPIN, FOCK])
+def test_dm_local_observables_sum_to_trace(kind):
+    """Σ_σ ρ(σ,σ) O_loc(σ) / Tr ρ equals the dense Tr(ρ Ô)/Tr(ρ) for the
+    diagonal-chain estimator of BatchedObsDMSampler.jl:90-105, and ρ is
+    Hermitian with a real, positive diagonal."""
+    rng = np.random.default_rng(6)
+    N = 3
+    h = Hilbert(N, kind)
+    n = nw.NDM(N, 1, 2, nw.SOFTPLUS)
+    nw.init_random_pars(n, rng, sigma=0.4 ** 2)
+    rho = exact.density_matrix(n, h)
+    assert np.max(np.abs(rho - rho.conj().T)) < 1e-12
+    assert np.all(np.diag(rho).real > 0) and np.max(np.abs(np.diag(rho).imag)) < 1e-12
+    p = exact.diagonal_distribution(n, h)
+    np.testing.assert_allclose(p, np.diag(rho).real / np.trace(rho).real, rtol=1e-12)
+    st = h.all_states()
+    cases = [ops.OpSum(h) + ops.sigmax(h, 0) + ops.sigmax(h, 2),
+             ops.OpSum(h) + ops.prod(ops.sigmay(h, 0), ops.sigmay(h, 1)),
+             ops.OpSum(h) + ops.prod(ops.sigmaz(h, 1), ops.sigmam(h, 2)),
+             ops.OpSum(h) + ops.sigmaz(h, 1)]
+    for O in cases:
+        loc = oest.local_observable_dm(n, O, st)
+        assert abs(np.sum(p * loc) - exact.dm_expectation(n, O)) < 1e-10
+
+
 def test_sr_solve_matches_direct():
     rng = np.random.default_rng(3)
     O = rng.standard_normal((200, 12)) + 1j * rng.standard_normal((200, 12))
