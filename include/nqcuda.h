@@ -129,8 +129,12 @@ typedef enum { NQ_SPACE_NETWORK = 0, NQ_SPACE_DIAGONAL = 1 } nq_sampler_space;
  * LocalRule, one uniformly drawn site flips (LocalRule.jl:19-28).
  * NQ_RULE_EXCHANGE: ExchangeRule(H), a uniformly drawn coupling (i, j) of the
  * couplings given by nq_set_exchange swaps its two values (ExchangeRule.jl:
- * 38-68); the total magnetisation of a chain is conserved.  RBM (ket), FP32. */
-typedef enum { NQ_RULE_LOCAL = 0, NQ_RULE_EXCHANGE = 1 } nq_mcmc_rule;
+ * 38-68); the total magnetisation of a chain is conserved.
+ * NQ_RULE_OPERATOR: OperatorRule(Ô) (OperatorRule.jl:23-58), a uniformly drawn
+ * connection of the configuration's rows in the tables of the operator given
+ * by nq_set_rule_operator, accepted with the Hastings factor n(σ)/n(σ') of
+ * the row lengths.  The exchange and operator rules: RBM (ket), FP32. */
+typedef enum { NQ_RULE_LOCAL = 0, NQ_RULE_EXCHANGE = 1, NQ_RULE_OPERATOR = 2 } nq_mcmc_rule;
 
 /* Sampler (src/Samplers/).  NQ_SAMPLER_METROPOLIS: the local-flip chains of
  * MetropolisSampler + LocalRule (Metropolis.jl:101-167).  NQ_SAMPLER_EXACT:
@@ -280,6 +284,11 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr,
  * Required before sampling with rule = NQ_RULE_EXCHANGE; replaces earlier
  * couplings. */
 nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs);
+/* OperatorRule(Ô): the move operator of an NQ_RULE_OPERATOR handle, flattened
+ * like nq_set_operator's table (ket sites).  It needs at least one connection
+ * that changes the configuration; its move classes and tables must fit the
+ * sampler's shared memory (NQ_ERR_UNSUPPORTED otherwise). */
+nq_status nq_set_rule_operator(nq_handle* h, const nq_op_table* op);
 
 /* ---- timing/diagnostics ----------------------------------------------------
  * Device milliseconds of the last staged calls (CUDA events on the handle's

@@ -54,6 +54,9 @@ nq_status refresh_params(nq_handle* h) {
       CKL(launch_rbm_exchange_tables<float>(d, h->n_exch, h->d_pairs, (cpx<float>*)h->d_xtab[0],
                                             (cpx<float>*)h->d_xtab[1], (cpx<float>*)h->d_xtab[2],
                                             (cpx<float>*)h->d_xW, h->d_xare, h->st));
+    if (h->rule == NQ_RULE_OPERATOR && h->n_exch > 0)
+      CKL(launch_rbm_class_tables(d, h->opm, (cpx<float>*)h->d_xtab[0], (cpx<float>*)h->d_xtab[1],
+                                  (cpx<float>*)h->d_xtab[2], (cpx<float>*)h->d_xW, h->d_xare, h->st));
     if (h->tc_theta) CKL(launch_theta_pack(d.W, h->M, h->N, h->theta_terms, h->d_theta_img, h->st));
   }
   return NQ_OK;
@@ -76,10 +79,12 @@ nq_status ensure_tuned(nq_handle* h) {
   if (h->exact || (h->sampler_lanes && h->sampler_block)) return NQ_OK;
   if (h->rule == NQ_RULE_EXCHANGE && h->n_exch == 0)
     return fail(h, NQ_ERR_STATE, "exchange rule: no couplings (nq_set_exchange)");
+  if (h->rule == NQ_RULE_OPERATOR && h->n_exch == 0)
+    return fail(h, NQ_ERR_STATE, "operator rule: no move operator (nq_set_rule_operator)");
   const int sN = h->nst, sM = h->diag ? h->Md : (h->ndm ? h->Ms : h->M);
   const auto key = std::make_tuple(sN, sM, h->B, h->act, h->hilb,
                                    (h->f64 ? 1 : 0) + (h->ndm ? 2 : 0) + (h->diag ? 8 : 0) +
-                                       (h->rule ? 4 * (h->n_exch + 1) : 0));
+                                       (h->rule ? 16 * (h->rule + 4 * (h->n_exch + 4 * h->opm.n_ops)) : 0));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -90,8 +95,14 @@ nq_status ensure_tuned(nq_handle* h) {
     }
   }
   int cand[4];
-  const int rows = h->rule == NQ_RULE_EXCHANGE ? h->n_exch : h->nst;
+  const int rows = h->rule != NQ_RULE_LOCAL ? h->n_exch : h->nst;
   int nc = rbm_sampler_valid_lanes(rows, sM, h->f64 ? 16 : 8, cand, 4);
+  if (h->rule == NQ_RULE_OPERATOR) {      // the move set shares the shared memory with the tables
+    int k = 0;
+    for (int c = 0; c < nc; ++c)
+      if (oprule_sampler_smem(h->opm, sM, cand[c]) > 0) cand[k++] = cand[c];
+    nc = k;
+  }
   if (nc == 0) return fail(h, NQ_ERR_UNSUPPORTED, "no sampler instantiation for %d hidden units", sM);
   if (h->sampler_lanes) { cand[0] = h->sampler_lanes; nc = 1; }     // fixed by the caller
   const int blocks[3] = {64, 128, 256};
@@ -157,8 +168,8 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
     else CKL(launch_exact_sampler<float>(rbm_dev<float>(h), run, h->d_exact, h->st));
   } else if (h->f64) CKL(launch_rbm_sampler<double>(rbm_sampler_dev<double>(h), run, h->sampler_lanes, h->st));
   else {
-    if (h->rule == NQ_RULE_EXCHANGE && h->n_exch == 0)
-      return fail(h, NQ_ERR_STATE, "exchange rule: no couplings (nq_set_exchange)");
+    if (h->rule != NQ_RULE_LOCAL && h->n_exch == 0)
+      return fail(h, NQ_ERR_STATE, "rule without moves (nq_set_exchange / nq_set_rule_operator)");
     CKL(launch_rbm_sampler<float>(rbm_sampler_dev<float>(h), run, h->sampler_lanes, h->st));
   }
   if (!h->capturing) CK(cudaEventRecord(h->kev[1], h->st));
@@ -325,6 +336,12 @@ void fill_measurement(nq_handle* h, nq_measurement* m) {
   m->acceptance = steps > 0 ? (double)(*h->h_acc) / steps : 0.0;
 }
 
+void free_rule_operator(nq_handle* h) {
+  for (void* p : h->opm_allocs) cudaFree(p);
+  h->opm_allocs.clear();
+  h->opm = OpMovesDev();
+}
+
 void free_op(nq_handle* h) {
   for (void* p : h->op_allocs) cudaFree(p);
   h->op_allocs.clear();
@@ -435,9 +452,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (c.s_precision == NQ_S_F64) { delete h; return NQ_ERR_UNSUPPORTED; }
   if (c.sr_algorithm != NQ_SR_DIRECT && c.sr_algorithm != NQ_SR_CG) return bad("unknown sr_algorithm");
   if (c.sampler_kind != NQ_SAMPLER_METROPOLIS && c.sampler_kind != NQ_SAMPLER_EXACT) return bad("unknown sampler_kind");
-  if (c.rule != NQ_RULE_LOCAL && c.rule != NQ_RULE_EXCHANGE) return bad("unknown rule");
-  if (c.rule == NQ_RULE_EXCHANGE && (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64))
-    return bad("the exchange rule is available for FP32 RBM handles");
+  if (c.rule != NQ_RULE_LOCAL && c.rule != NQ_RULE_EXCHANGE && c.rule != NQ_RULE_OPERATOR) return bad("unknown rule");
+  if (c.rule != NQ_RULE_LOCAL && (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64))
+    return bad("the exchange and operator rules are available for FP32 RBM handles");
   if (c.sampler_space != NQ_SPACE_NETWORK && c.sampler_space != NQ_SPACE_DIAGONAL) return bad("unknown sampler_space");
   if (c.sampler_space == NQ_SPACE_DIAGONAL && c.network != NQ_NET_NDM)
     return bad("the diagonal sampler space is defined for the NDM");
@@ -640,6 +657,7 @@ void nq_destroy(nq_handle* h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
   proposal_destroy(h);
   free_op(h);
+  free_rule_operator(h);
   void* bufs[] = {h->d_master, h->d_p32, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
                   h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
@@ -748,6 +766,113 @@ nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs) {
   h->sampler_block = 0;
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
   if (nq_status s = refresh_params(h)) return s;
+  CK(cudaStreamSynchronize(h->st));
+  return NQ_OK;
+}
+
+// OperatorRule move set from the operator's row tables: the operators' sites
+// and rows as in the estimator, one code per connection (-1 without changes,
+// else its move class and orientation), and the classes' changed sites with
+// their canonical new local indices (first site at index 1).
+nq_status nq_set_rule_operator(nq_handle* h, const nq_op_table* t) {
+  if (!h || !t) return NQ_ERR_ARG;
+  if (h->rule != NQ_RULE_OPERATOR) return fail(h, NQ_ERR_STATE, "the handle was created with another rule");
+  if (nq_status v = validate_op(h, t)) return v;
+  const int no = t->n_ops, nr = t->n_rows, nconn = t->n_conns;
+  std::vector<unsigned long long> osites(no), omask(no);
+  std::vector<int> prefix(no + 1, 0);
+  bool const_counts = true;
+  for (int o = 0; o < no; ++o) {
+    unsigned long long packed = 0, mask = 0;
+    for (int d = 0; d < t->op_n_sites[o]; ++d) {
+      const int site = t->op_sites[8 * o + d];
+      packed |= (unsigned long long)site << (8 * d);
+      mask |= 1ull << site;
+    }
+    osites[o] = packed;
+    omask[o] = mask;
+    const int r0 = t->op_row_offset[o];
+    const int len0 = t->row_conn_offset[r0 + 1] - t->row_conn_offset[r0];
+    for (int r = 1; r < (1 << t->op_n_sites[o]); ++r)
+      if (t->row_conn_offset[r0 + r + 1] - t->row_conn_offset[r0 + r] != len0) const_counts = false;
+    prefix[o + 1] = prefix[o] + len0;
+  }
+  // move classes: key = (sites in connection order, new local indices normalised so that the
+  // first changed site goes to index 1)
+  std::map<std::pair<std::vector<int>, int>, int> classes;
+  std::vector<int> code(nconn, -1), csites, cbits;
+  std::vector<unsigned long long> cmask;
+  for (int c = 0; c < nconn; ++c) {
+    const int nch = t->conn_n_changes[c];
+    if (nch == 0) continue;
+    std::vector<int> sites(nch);
+    int bitsv = 0;
+    unsigned long long m = 0;
+    for (int q = 0; q < nch; ++q) {
+      sites[q] = t->conn_change_site[8 * c + q];
+      const int v = t->conn_change_value[8 * c + q];
+      const int b = h->hilb == NQ_HILB_SPIN ? (v > 0 ? 1 : 0) : v;
+      bitsv |= b << q;
+      m |= 1ull << sites[q];
+    }
+    const bool comp = (bitsv & 1) == 0;
+    if (comp) bitsv ^= (1 << nch) - 1;
+    auto key = std::make_pair(sites, bitsv);
+    auto it = classes.find(key);
+    int k;
+    if (it == classes.end()) {
+      k = (int)classes.size();
+      classes.emplace(key, k);
+      for (int q = 0; q < 8; ++q) csites.push_back(q < nch ? sites[q] : -1);
+      cbits.push_back(bitsv);
+      cmask.push_back(m);
+    } else {
+      k = it->second;
+    }
+    code[c] = 2 * k + (comp ? 1 : 0);
+  }
+  const int nclass = (int)classes.size();
+  if (nclass == 0) return fail(h, NQ_ERR_ARG, "the move operator has no connection that changes a configuration");
+  CK(cudaStreamSynchronize(h->st));
+  free_rule_operator(h);
+  cudaFree(h->d_xW); cudaFree(h->d_xare);
+  for (void*& p : h->d_xtab) { cudaFree(p); p = nullptr; }
+  h->d_xW = nullptr; h->d_xare = nullptr; h->n_exch = 0;
+  OpMovesDev m;
+  m.n_ops = no; m.n_rows = nr; m.n_conns = nconn; m.n_classes = nclass;
+  m.const_counts = const_counts ? 1 : 0;
+  m.n_total = prefix[no];
+  nq_status s;
+  if ((s = upload(h, osites.data(), osites.size(), &m.op_sites, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, omask.data(), omask.size(), &m.op_mask, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, t->op_n_sites, (size_t)no, &m.op_n_sites, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, t->op_row_offset, (size_t)no, &m.op_row_offset, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, (const int*)prefix.data(), prefix.size(), &m.op_prefix, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, t->row_conn_offset, (size_t)nr + 1, &m.row_conn_offset, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, (const int*)code.data(), code.size(), &m.conn_code, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, cmask.data(), cmask.size(), &m.class_mask, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, (const int*)csites.data(), csites.size(), &m.class_sites, &h->opm_allocs)) != NQ_OK ||
+      (s = upload(h, (const int*)cbits.data(), cbits.size(), &m.class_bits, &h->opm_allocs)) != NQ_OK) {
+    free_rule_operator(h);
+    return s;
+  }
+  h->opm = m;
+  bool fits = false;
+  for (int G : {4, 8, 16, 32}) fits = fits || oprule_sampler_smem(m, h->M, G) > 0;
+  if (!fits) {
+    free_rule_operator(h);
+    return fail(h, NQ_ERR_UNSUPPORTED, "operator rule: %d move classes x %d hidden units exceed the shared memory",
+                nclass, h->M);
+  }
+  const size_t tab = (size_t)nclass * h->M * sizeof(cpx<float>);
+  for (void*& p : h->d_xtab) CK(cudaMalloc(&p, tab));
+  CK(cudaMalloc(&h->d_xW, tab));
+  CK(cudaMalloc((void**)&h->d_xare, (size_t)nclass * sizeof(float)));
+  h->n_exch = nclass;
+  h->sampler_lanes = h->cfg.sampler_lanes;      // re-tune: the move set changed
+  h->sampler_block = 0;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  if (nq_status r = refresh_params(h)) return r;
   CK(cudaStreamSynchronize(h->st));
   return NQ_OK;
 }

@@ -84,11 +84,13 @@ struct nq_handle {
   bool cg = false;                 // NQ_SR_CG: matrix-free iterative SR, no S
   bool exact = false;              // NQ_SAMPLER_EXACT
   int rule = 0;                    // nq_mcmc_rule
-  int n_exch = 0;                  // exchange couplings
+  int n_exch = 0;                  // exchange couplings / OperatorRule move classes
   int2* d_pairs = nullptr;         // [n_exch]
   void* d_xtab[3] = {};            // exchange move tables t0..t2 [n_exch*M]
   void* d_xW = nullptr;            // W_hi - W_hj [M*n_exch]
   float* d_xare = nullptr;         // [n_exch]
+  OpMovesDev opm;                  // OperatorRule move set (device pointers in opm_allocs)
+  std::vector<void*> opm_allocs;
   double* d_exact = nullptr;       // exact sampler: CDF and block sums
   SrCgArgs cga;                    // device work of the iterative solve
   double cg_tol = 1e-4;
@@ -173,13 +175,15 @@ RbmDev<R> rbm_dev(nq_handle* h) {
 }
 
 // the network as the Metropolis sampler sees it: with the exchange rule the
-// move tables are the couplings' (the estimators keep rbm_dev's per-site tables)
+// move tables are the couplings', with the OperatorRule the move classes'
+// (the estimators keep rbm_dev's per-site tables)
 template <typename R>
 RbmDev<R> rbm_sampler_dev(nq_handle* h) {
   RbmDev<R> d = rbm_dev<R>(h);
-  if (h->rule == NQ_RULE_EXCHANGE && h->n_exch > 0) {
+  if (h->rule != NQ_RULE_LOCAL && h->n_exch > 0) {
     d.n_rows = h->n_exch;
-    d.pairs = h->d_pairs;
+    if (h->rule == NQ_RULE_EXCHANGE) d.pairs = h->d_pairs;
+    else d.opm = &h->opm;
     d.t0 = reinterpret_cast<const cpx<R>*>(h->d_xtab[0]);
     d.t1 = reinterpret_cast<const cpx<R>*>(h->d_xtab[1]);
     d.t2 = reinterpret_cast<const cpx<R>*>(h->d_xtab[2]);

@@ -23,6 +23,8 @@ struct DevOp {
 //   softplus: t0 = exp(W d) - 1, t1 = exp(-W d) - 1, t2 = 0
 // With g = f'(θ), the ratio cosh(θ+Δ)/cosh(θ) (resp. (1+e^{θ+Δ})/(1+e^θ))
 // of a single flip with Δ = W dv is t0 + g*sign(dv)*t1 (resp. 1 + g*t0|t1).
+struct OpMovesDev;
+
 template <typename R> struct RbmDev {
   int N = 0, M = 0, act = 0, hilb = 0;
   int n_half = 0;              // hidden units h < n_half enter log|ψ|^2 with weight 1/2
@@ -41,6 +43,32 @@ template <typename R> struct RbmDev {
   const int2* pairs = nullptr;   // [n_rows]
   const cpx<R>* rW = nullptr;    // [M*n_rows] at h + M*r
   const R* rare = nullptr;       // [n_rows] 2 log2(e) Re(a_i - a_j)
+  // OperatorRule: the rows are the move classes of the operator's
+  // connections (host pointer, read by the launcher only)
+  const OpMovesDev* opm = nullptr;
+};
+
+// OperatorRule (src/Samplers/MCMCRules/OperatorRule.jl:23-58): the moves of a
+// configuration σ are the connections of its rows in the operator's tables
+// (row_valdiff, KLocalOperator.jl:151-158, KLocalOperatorSum.jl:40-46),
+// drawn uniformly, with the Hastings factor n(σ)/n(σ') of the row lengths.
+// Connections that change sites are grouped into move classes (changed sites
+// and their new local indices, up to complement); a class's θ-tables are
+// those of Δθ = Σ_q W[h, s_q] dv_q, like the single-flip tables.
+struct OpMovesDev {
+  int n_ops = 0, n_rows = 0, n_conns = 0, n_classes = 0;
+  int const_counts = 0;                           // every row of an operator has the same length
+  int n_total = 0;                                // const_counts: connections of every configuration
+  const unsigned long long* op_sites = nullptr;   // [n_ops] site d in byte d
+  const unsigned long long* op_mask = nullptr;    // [n_ops] sites of the operator
+  const int* op_n_sites = nullptr;                // [n_ops]
+  const int* op_row_offset = nullptr;             // [n_ops]
+  const int* op_prefix = nullptr;                 // [n_ops + 1] const_counts: first move of each operator
+  const int* row_conn_offset = nullptr;           // [n_rows + 1]
+  const int* conn_code = nullptr;                 // [n_conns] -1: no change; 2 class + (complement ? 1 : 0)
+  const unsigned long long* class_mask = nullptr; // [n_classes] changed sites
+  const int* class_sites = nullptr;               // [8 n_classes] sites of the class (-1: unused)
+  const int* class_bits = nullptr;                // [n_classes] canonical new local index of site q in bit q
 };
 
 cudaError_t launch_rbm_params_from_master(const double* master, int N, int M, float* f32_out,
@@ -71,6 +99,14 @@ cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int 
 int rbm_sampler_valid_lanes(int N, int M, int csize, int* out, int max_out);
 // the exchange-rule instantiations of the FP32 sampler (net.pairs set)
 cudaError_t launch_rbm_sampler_exchange(const RbmDev<float>& net, const SamplerRun& run, int G, cudaStream_t st);
+// OperatorRule sampler (FP32 ket), net.opm set
+cudaError_t launch_rbm_sampler_oprule(const RbmDev<float>& net, const SamplerRun& run, int G, cudaStream_t st);
+// move-class tables of the OperatorRule: rW[h + M k] = Σ_q W[h, s_q] (2 b_q - 1),
+// rare[k] = 2 log2(e) Σ_q Re a_{s_q} (2 b_q - 1), t0..t2 of Δθ = d rW at k*M + h
+cudaError_t launch_rbm_class_tables(const RbmDev<float>& net, const OpMovesDev& m, cpx<float>* t0, cpx<float>* t1,
+                                    cpx<float>* t2, cpx<float>* rW, float* rare, cudaStream_t st);
+// shared memory of the OperatorRule sampler with G lanes per chain (0 if it does not fit)
+size_t oprule_sampler_smem(const OpMovesDev& m, int M, int G);
 
 // Exact sampler (Exact.jl): all 2^N configurations of the sampler's space
 // (N <= 26), FP64 CDF, inverse-CDF draws into run.samples (n_record draws per

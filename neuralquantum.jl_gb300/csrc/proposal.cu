@@ -169,6 +169,7 @@ nq_status nq_proposal_init(nq_handle* h, int32_t hidden, double p_ar, uint64_t s
   if (!h) return NQ_ERR_ARG;
   if (h->ndm || h->f64) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: FP32 RBM handles only");
   if (h->exact) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: the handle samples exactly (no chains)");
+  if (h->rule != NQ_RULE_LOCAL) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: mixes with LocalRule moves only");
   if (hidden != 128) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: hidden must be 128 (got %d)", hidden);
   if (!(p_ar >= 0.0 && p_ar <= 1.0)) return fail(h, NQ_ERR_ARG, "p_ar must lie in [0, 1]");
   if (!mix_sampler_supported(h->N, h->M, 0, hidden))

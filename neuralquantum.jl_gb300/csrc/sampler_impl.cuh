@@ -278,9 +278,11 @@ template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st) {
   if (net.N > 64 || net.M > 320) return cudaErrorInvalidValue;
   if (!hpl_ok((net.M + G - 1) / G)) return cudaErrorInvalidValue;
-  if (net.pairs) {
-    // exchange rule: FP32 ket (RBM) handles only, instantiated in sampler_exch.cu
-    if constexpr (std::is_same<R, float>::value) return launch_rbm_sampler_exchange(net, run, G, st);
+  if (net.pairs || net.opm) {
+    // exchange rule and OperatorRule: FP32 ket (RBM) handles only, instantiated
+    // in sampler_exch.cu and sampler_oprule.cu
+    if constexpr (std::is_same<R, float>::value)
+      return net.opm ? launch_rbm_sampler_oprule(net, run, G, st) : launch_rbm_sampler_exchange(net, run, G, st);
     else return cudaErrorInvalidValue;
   }
   if (net.act == ACT_LOGCOSH) return sampler_g<R, ACT_LOGCOSH, false>(net, run, G, st);

@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
            "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu",
-           "srcg.cu", "exact.cu", "sampler_exch.cu"]
+           "srcg.cu", "exact.cu", "sampler_exch.cu", "sampler_oprule.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -35,7 +35,7 @@ NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64, NQ_EVAL_TC_BF16X3 = 0, 1, 2, 3
 NQ_S_F32, NQ_S_TF32, NQ_S_TF32X3, NQ_S_F64, NQ_S_BF16 = 0, 1, 2, 3, 4
 NQ_SR_DIRECT, NQ_SR_CG = 0, 1
 NQ_SAMPLER_METROPOLIS, NQ_SAMPLER_EXACT = 0, 1
-NQ_RULE_LOCAL, NQ_RULE_EXCHANGE = 0, 1
+NQ_RULE_LOCAL, NQ_RULE_EXCHANGE, NQ_RULE_OPERATOR = 0, 1, 2
 NQ_SPACE_NETWORK, NQ_SPACE_DIAGONAL = 0, 1
 NQ_QUIRK_STALE_LAST_SLOT = 0x1
 
@@ -84,6 +84,7 @@ EXPORTS = {
     "nq_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]),
     "nq_set_operator": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable)]),
     "nq_set_exchange": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_int32)]),
+    "nq_set_rule_operator": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable)]),
     "nq_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]),
     "nq_set_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_logpsi": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),

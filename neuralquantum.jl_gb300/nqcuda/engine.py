@@ -116,6 +116,12 @@ class Engine:
         self._check(self.lib.nq_set_exchange(self.h, arr.shape[0],
                                              arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
 
+    def set_rule_operator(self, table):
+        """Move operator of the OperatorRule (an OpTable of ket sites)."""
+        self._rule_op = table
+        st = table.struct()
+        self._check(self.lib.nq_set_rule_operator(self.h, ctypes.byref(st)))
+
     # ---- stages -------------------------------------------------------------
     def sample(self, call_index, want_samples=True, want_accept_bits=False):
         out = np.empty((self.L, self.B, self.nsites), np.int8) if want_samples else None

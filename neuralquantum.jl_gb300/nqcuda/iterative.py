@@ -78,12 +78,19 @@ class BatchedSampler:
         quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
         sr_alg = _lib.NQ_SR_CG if self.algo.iterative else _lib.NQ_SR_DIRECT
         exch = getattr(getattr(sampler, "rule", None), "couplings", None)
+        move_op = getattr(getattr(sampler, "rule", None), "operator", None)
+        rule = _lib.NQ_RULE_LOCAL
+        if exch is not None:
+            rule = _lib.NQ_RULE_EXCHANGE
+        elif move_op is not None:
+            rule = _lib.NQ_RULE_OPERATOR
         self.engine = Engine(net, hilb, batch_sz, sampler.chain_length, sampler.burn_length,
                              sampler.passes, sampler.seed, eval_precision, s_precision, quirks,
-                             sr_algorithm=sr_alg, sampler_kind=getattr(sampler, "kind", 0),
-                             rule=_lib.NQ_RULE_EXCHANGE if exch is not None else _lib.NQ_RULE_LOCAL)
+                             sr_algorithm=sr_alg, sampler_kind=getattr(sampler, "kind", 0), rule=rule)
         if exch is not None:
             self.engine.set_exchange(exch)
+        if move_op is not None:
+            self.engine.set_rule_operator(op_table(move_op))
         if self.algo.iterative:
             self.engine.set_sr_tolerance(self.algo.precision, 10 * self.engine.P)
         self.engine.set_params(net.flat())
@@ -173,7 +180,8 @@ class BatchedObsDMSampler:
         self.sampler = sampler
         self.hilb = hilb_doubled
         quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
-        if getattr(getattr(sampler, "rule", None), "couplings", None) is not None:
+        rule = getattr(sampler, "rule", None)
+        if getattr(rule, "couplings", None) is not None or getattr(rule, "operator", None) is not None:
             raise NotImplementedError("the diagonal sampler uses LocalRule")
         self.engine = Engine(net, hilb_doubled, batch_sz, sampler.chain_length, sampler.burn_length,
                              sampler.passes, sampler.seed, eval_precision, _lib.NQ_S_F32, quirks,

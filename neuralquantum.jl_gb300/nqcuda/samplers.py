@@ -32,6 +32,20 @@ class ExchangeRule:
         return f"ExchangeRule({len(self.couplings)} couplings)"
 
 
+class OperatorRule:
+    """``OperatorRule(Ô)`` (src/Samplers/MCMCRules/OperatorRule.jl:9-58): a
+    move draws one connection of the configuration's rows in Ô's tables
+    uniformly (the diagonal entries included, which propose the same state)
+    and applies its changes; the acceptance carries the factor n(σ)/n(σ') of
+    the numbers of connections."""
+
+    def __init__(self, op):
+        self.operator = op
+
+    def __repr__(self):
+        return "OperatorRule()"
+
+
 class MetropolisSampler:
     """``MetropolisSampler(rule, chain_length, passes; burn=0, seed)``
     (src/Samplers/Metropolis.jl:26-40).  An even number of passes is raised

@@ -86,6 +86,16 @@ def mh_draws(seed, call, chains, step, nsites):
     return site, u
 
 
+def mh_raw(seed, call, chains, step):
+    """(r0, u) of Metropolis step ``step``: the raw 32-bit word that picks the
+    move (index floor(r0 n / 2^32) among n candidates) and the uniform."""
+    k0, k1 = split_seed(seed)
+    chains = np.asarray(chains, dtype=np.uint64)
+    r0, r1, _, _ = philox4x32_10(np.uint64(step), np.uint64(call), chains, TAG_MH, k0, k1)
+    u = (r1 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24
+    return r0.astype(np.uint64), u
+
+
 def exact_uniforms(seed, call, chains, t):
     """53-bit uniforms in [0, 1) of exact-sampler draw ``t`` for ``chains``."""
     k0, k1 = split_seed(seed)

@@ -2,7 +2,8 @@
 ``oracle/__init__``).
 
 Restates src/Samplers/Metropolis.jl:101-167 with src/Samplers/MCMCRules/
-LocalRule.jl:19-28 and the chain bookkeeping of
+LocalRule.jl:19-28 (ExchangeRule.jl:38-68 and OperatorRule.jl:42-58 as
+options) and the chain bookkeeping of
 src/IterativeInterface/Samplers/BaseIterativeSampler.jl:5-17, with the
 reference MersenneTwister stream replaced by the Philox schema of
 ``oracle.philox``:
@@ -22,6 +23,7 @@ reference MersenneTwister stream replaced by the Philox schema of
 import numpy as np
 
 from . import philox
+from .operators import connections_ket, apply_changes
 
 
 def fix_passes(passes):
@@ -36,13 +38,19 @@ def init_configs(hilb, seed, call, chains, n_sites_total):
 
 def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
         doubled=False, stale_last_slot=False, prev_samples=None,
-        gpu_accept_bits=None, tie_tol=1e-3, chain_offset=0, couplings=None):
+        gpu_accept_bits=None, tie_tol=1e-3, chain_offset=0, couplings=None, move_op=None):
     """Replays one ``_sample_state!`` call.
 
     ``couplings`` (list of 0-based site pairs) selects ExchangeRule
     (src/Samplers/MCMCRules/ExchangeRule.jl:38-68): the step's draw picks
     coupling ``(r0 * len(couplings)) >> 32`` and swaps its two values (a swap
     of equal values proposes the same state, which ``u < exp(0)`` accepts).
+
+    ``move_op`` (an ``OpSum``) selects OperatorRule
+    (src/Samplers/MCMCRules/OperatorRule.jl:42-58): the step's draw picks
+    connection ``(r0 * n_f) >> 32`` of the n_f connections of the chain's
+    rows (``connections_ket`` order), applies its changes, and adds
+    ``log(n_f / n_b)`` with n_b counted at the new configuration.
 
     ``log_prob(batch)`` maps (B, nsites_total) configurations to 2 Re log psi.
     ``gpu_accept_bits`` (optional, (steps, B) bool) resolves near-tie
@@ -70,7 +78,18 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
         for _ in range(passes):
             rows = np.arange(n_chains)
             new = sigma.copy()
-            if couplings is None:
+            bias = 0.0
+            if move_op is not None:
+                r0, u = philox.mh_raw(seed, call, chains, t)
+                bias = np.zeros(n_chains)
+                for b in range(n_chains):
+                    conns = connections_ket(move_op, sigma[b])
+                    nf = len(conns)
+                    ch = conns[(int(r0[b]) * nf) >> 32][1]
+                    if len(ch):
+                        new[b] = apply_changes(sigma[b], ch)
+                        bias[b] = np.log(nf / len(connections_ket(move_op, new[b])))
+            elif couplings is None:
                 site, u = philox.mh_draws(seed, call, chains, t, nt)
                 new[rows, site] = hilb.flip(sigma[rows, site])
             else:
@@ -79,7 +98,7 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
                 new[rows, pr[:, 0]] = sigma[rows, pr[:, 1]]
                 new[rows, pr[:, 1]] = sigma[rows, pr[:, 0]]
             lpn = log_prob(new)
-            delta = lpn - lp
+            delta = lpn - lp + bias
             with np.errstate(over="ignore", divide="ignore"):
                 acc = u < np.exp(delta)
                 logu = np.log(np.maximum(u, 1e-300))

@@ -126,6 +126,40 @@ def test_sampler_replay_is_deterministic_and_detailed_balance():
     assert chisquare(counts, p * counts.sum())[1] >= 0.01
 
 
+def hopping_field(h, N, t=1.0, g=0.4):
+    """Σ_i t(σ⁺_i σ⁻_{i+1} + σ⁻_i σ⁺_{i+1}) + g Σ_i σx_i on an open chain:
+    rows of the hopping terms have 1 or 2 connections, so the OperatorRule's
+    factor n(σ)/n(σ') is not 1; the field makes the moves ergodic."""
+    H = ops.OpSum(h)
+    for i in range(N - 1):
+        H = H + ops.prod(ops.sigmap(h, i), ops.sigmam(h, i + 1)).scale(t)
+        H = H + ops.prod(ops.sigmam(h, i), ops.sigmap(h, i + 1)).scale(t)
+    for i in range(N):
+        H = H + ops.sigmax(h, i).scale(g)
+    return H
+
+
+def test_operator_rule_replay_detailed_balance():
+    """χ² of the OperatorRule replay (OperatorRule.jl:42-58, with the factor
+    n(σ)/n(σ')) against exact |ψ|², on an operator with rows of unequal
+    length; without the factor the chain is biased."""
+    from scipy.stats import chisquare
+    rng = np.random.default_rng(8)
+    N = 4
+    h = Hilbert(N, SPIN)
+    r = nw.RBM(N, 4, nw.LOGCOSH)
+    nw.init_random_pars(r, rng, sigma=0.3 ** 2)
+    H = hopping_field(h, N)
+    lens = {len(ops.connections_ket(H, s)) for s in h.all_states()}
+    assert len(lens) > 1
+    s1, info = osm.run(r.log_prob, h, 3000, 1, 40, 5, seed=3, move_op=H)
+    idx = h.index_of_state(s1.reshape(-1, N))
+    counts = np.bincount(idx, minlength=h.dim)
+    p = exact.ket_distribution(r, h)
+    assert chisquare(counts, p * counts.sum())[1] >= 0.01
+    assert 0 < info["accepted"] < info["steps"]
+
+
 def test_local_energy_sums_to_exact_expectation():
     """<E_loc>_{|ψ|²} over all states equals <ψ|H|ψ>/<ψ|ψ>."""
     rng = np.random.default_rng(2)
