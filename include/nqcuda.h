@@ -65,7 +65,13 @@ typedef enum {
   NQ_ERR_UNSUPPORTED = 7   /* configuration outside the supported envelope */
 } nq_status;
 
-typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1 } nq_network;
+/* Networks.  NQ_NET_RBM: RBM ket (ClosedSystems/RBM.jl), complex parameters.
+ * NQ_NET_NDM: purified density matrix (MixedDensityMatrix/NDM.jl), real
+ * parameters, n_hidden = αN, n_ancilla = βN.  NQ_NET_RBM_SPLIT: RBMSplit
+ * density matrix (MixedDensityMatrix/RBMSplit.jl), complex parameters
+ * (ar, ac, b, Wr, Wc), n_hidden = αN.  The density matrices sample the
+ * doubled space (σ, η) and take the Liouvillian cost function. */
+typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2 } nq_network;
 typedef enum { NQ_ACT_LOGCOSH = 0, NQ_ACT_SOFTPLUS = 1 } nq_activation;
 typedef enum { NQ_HILB_SPIN = 0, NQ_HILB_FOCK = 1 } nq_hilbert;
 typedef enum { NQ_DTYPE_C64 = 0, NQ_DTYPE_C128 = 1, NQ_DTYPE_F32 = 2, NQ_DTYPE_F64 = 3 } nq_dtype;
@@ -115,7 +121,7 @@ typedef struct {
 
 /* Space the sampler draws from.  NQ_SPACE_NETWORK: the network's own space
  * (the ket's N sites; the NDM's doubled (σ, η) space, p ∝ |ρ(σ,η)|²).
- * NQ_SPACE_DIAGONAL (NDM only): the physical space with p(σ) ∝ ρ(σ,σ), the
+ * NQ_SPACE_DIAGONAL (NDM, RBMSplit): the physical space with p(σ) ∝ ρ(σ,σ), the
  * chains of BatchedObsDMSampler(net, sampler, hilb_doubled)
  * (src/IterativeInterface/Samplers/Obs/BatchedObsDMSampler.jl:24-53, log
  * probability real(logρ(σ,σ)) of src/base_networks.jl:157).  Such a handle

@@ -14,6 +14,7 @@ template <typename R>
 NdmEff<R> ndm_eff(nq_handle* h) {
   NdmEff<R> e;
   e.N = h->N; e.N2 = h->N2; e.Mh = h->Mh; e.Ma = h->Ma; e.U = h->U; e.P = h->P;
+  e.split = h->split ? 1 : 0;
   e.C = reinterpret_cast<const cpx<R>*>(h->d_eff[0]);
   e.b = reinterpret_cast<const cpx<R>*>(h->d_eff[1]);
   e.a = reinterpret_cast<const cpx<R>*>(h->d_eff[2]);
@@ -26,10 +27,18 @@ nq_status ndm_refresh(nq_handle* h) {
   NdmEffBufs<R> b;
   b.C = (cpx<R>*)h->d_eff[0]; b.b = (cpx<R>*)h->d_eff[1]; b.a = (cpx<R>*)h->d_eff[2];
   b.Cs = (cpx<R>*)h->d_eff[3]; b.bs = (cpx<R>*)h->d_eff[4];
-  CKL(launch_ndm_effective<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), b, h->st));
-  if (h->diag)
-    CKL(launch_ndm_diagonal<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), (cpx<R>*)h->d_diag[0], (cpx<R>*)h->d_diag[1],
-                               (cpx<R>*)h->d_diag[2], h->st));
+  if (h->split) {
+    const cpx<R>* pc = reinterpret_cast<const cpx<R>*>(p);
+    CKL(launch_split_effective<R>(pc, h->N, h->Ma, b, h->st));
+    if (h->diag)
+      CKL(launch_split_diagonal<R>(pc, h->N, h->Ma, (cpx<R>*)h->d_diag[0], (cpx<R>*)h->d_diag[1],
+                                   (cpx<R>*)h->d_diag[2], h->st));
+  } else {
+    CKL(launch_ndm_effective<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), b, h->st));
+    if (h->diag)
+      CKL(launch_ndm_diagonal<R>(ndm_view<R>(p, h->N, h->Mh, h->Ma), (cpx<R>*)h->d_diag[0],
+                                 (cpx<R>*)h->d_diag[1], (cpx<R>*)h->d_diag[2], h->st));
+  }
   RbmDev<R> d = rbm_dev<R>(h);
   CKL(launch_rbm_tables<R>(d, (cpx<R>*)h->d_tab[0], (cpx<R>*)h->d_tab[1], (cpx<R>*)h->d_tab[2], h->st));
   return NQ_OK;
@@ -38,7 +47,7 @@ nq_status ndm_refresh(nq_handle* h) {
 // refresh FP32 copies and the per-flip tables after a parameter change
 nq_status refresh_params(nq_handle* h) {
   if (h->ndm) {
-    if (!h->f64) CKL(launch_master_to_f32(h->d_master, h->P, h->d_p32, h->st));
+    if (!h->f64) CKL(launch_master_to_f32(h->d_master, (h->complex_params ? 2L : 1L) * h->P, h->d_p32, h->st));
     return h->f64 ? ndm_refresh<double>(h) : ndm_refresh<float>(h);
   }
   if (!h->f64) CKL(launch_rbm_params_from_master(h->d_master, h->N, h->M, h->d_p32, h->st));
@@ -250,7 +259,7 @@ nq_status stage_S(nq_handle* h) {
       CKL(launch_gram_simt_x(h->d_X, h->Ns_pad, h->Ns, 2 * h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
     }
     if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
-    CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, true, h->d_S, h->st));
+    CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, !h->complex_params, h->d_S, h->st));
     return NQ_OK;
   }
   RbmOSource src;
@@ -436,7 +445,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     delete h;
     return NQ_ERR_ARG;
   };
-  if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM) return bad("unknown network");
+  if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM && c.network != NQ_NET_RBM_SPLIT)
+    return bad("unknown network");
+  const bool matrix_net = c.network == NQ_NET_NDM || c.network == NQ_NET_RBM_SPLIT;
   if (c.activation != NQ_ACT_LOGCOSH && c.activation != NQ_ACT_SOFTPLUS) return bad("unknown activation");
   if (c.hilbert != NQ_HILB_SPIN && c.hilbert != NQ_HILB_FOCK) return bad("unknown hilbert space");
   if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
@@ -456,10 +467,10 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (c.rule != NQ_RULE_LOCAL && (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64))
     return bad("the exchange and operator rules are available for FP32 RBM handles");
   if (c.sampler_space != NQ_SPACE_NETWORK && c.sampler_space != NQ_SPACE_DIAGONAL) return bad("unknown sampler_space");
-  if (c.sampler_space == NQ_SPACE_DIAGONAL && c.network != NQ_NET_NDM)
-    return bad("the diagonal sampler space is defined for the NDM");
+  if (c.sampler_space == NQ_SPACE_DIAGONAL && !matrix_net)
+    return bad("the diagonal sampler space is defined for density-matrix networks (NDM, RBMSplit)");
   if (c.sampler_kind == NQ_SAMPLER_EXACT &&
-      (c.network == NQ_NET_NDM && c.sampler_space == NQ_SPACE_NETWORK ? 2 * c.n_sites : c.n_sites) > 26)
+      (matrix_net && c.sampler_space == NQ_SPACE_NETWORK ? 2 * c.n_sites : c.n_sites) > 26)
     return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM's doubled space) <= 26");
   if (c.sr_algorithm == NQ_SR_CG &&
       (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64 ||
@@ -476,21 +487,24 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (c.s_precision < NQ_S_F32 || c.s_precision > NQ_S_BF16) return bad("unknown s_precision");
   h->N = c.n_sites;
   h->M = c.n_hidden;
-  if (c.network == NQ_NET_NDM) {
+  if (matrix_net) {
+    // density-matrix networks share the doubled-space path; RBMSplit is its
+    // effective form with M units of weight 1 (Mh = 0, Ma = M)
     h->ndm = true;
-    h->Mh = c.n_hidden;
-    h->Ma = c.n_ancilla;
-    if (h->Ma < 1) return bad("the NDM needs n_ancilla >= 1");
+    h->split = c.network == NQ_NET_RBM_SPLIT;
+    h->Mh = h->split ? 0 : c.n_hidden;
+    h->Ma = h->split ? c.n_hidden : c.n_ancilla;
+    if (!h->split && h->Ma < 1) return bad("the NDM needs n_ancilla >= 1");
     h->N2 = 2 * h->N;
     h->U = 4 * h->Mh + h->Ma;
     h->Ms = 2 * h->Mh + h->Ma;
     h->diag = c.sampler_space == NQ_SPACE_DIAGONAL;
     h->Md = h->Mh + h->Ma;
     h->nst = h->diag ? h->N : h->N2;
-    h->P = ndm_n_params(h->N, h->Mh, h->Ma);
+    h->P = h->split ? 2 * h->N + h->Ma + 2 * h->N * h->Ma : ndm_n_params(h->N, h->Mh, h->Ma);
     if (h->N2 > 64) return bad("the NDM supports n_sites <= 32 (2N doubled sites)");
     if (h->Ms > 320) return bad("2*n_hidden + n_ancilla must be <= 320");
-    if (h->P > 256 * 24) return bad("too many NDM parameters (max 6144)");
+    if (h->P > 256 * 24) return bad("too many density-matrix parameters (max 6144)");
   } else {
     h->nst = h->N;
     h->P = h->N + h->M + h->M * h->N;
@@ -507,7 +521,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->f64 = c.eval_precision == NQ_EVAL_F64;
   h->tc_theta = c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3;
   h->theta_terms = c.eval_precision == NQ_EVAL_TC_BF16X3 ? 3 : 2;
-  h->complex_params = !h->ndm;
+  h->complex_params = !h->ndm || h->split;
   const int sampler_M = h->diag ? h->Md : (h->ndm ? h->Ms : h->M), sampler_N = h->nst;
   if (c.sampler_lanes != 0) {
     int cand[4];
@@ -708,7 +722,7 @@ nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype
     else if (dtype == NQ_DTYPE_C64) {
       const float* f = (const float*)flat;
       for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
-    } else return fail(h, NQ_ERR_ARG, "RBM parameters are complex (dtype c64 or c128)");
+    } else return fail(h, NQ_ERR_ARG, "RBM / RBMSplit parameters are complex (dtype c64 or c128)");
   } else {
     if (dtype == NQ_DTYPE_F64) memcpy(buf.data(), flat, buf.size() * sizeof(double));
     else if (dtype == NQ_DTYPE_F32) {
@@ -733,7 +747,7 @@ nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
   CK(cudaStreamSynchronize(h->st));
   const bool want_c = dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_C64;
   if (want_c != h->complex_params)
-    return fail(h, NQ_ERR_ARG, h->complex_params ? "RBM parameters are complex (dtype c64 or c128)"
+    return fail(h, NQ_ERR_ARG, h->complex_params ? "RBM / RBMSplit parameters are complex (dtype c64 or c128)"
                                                  : "NDM parameters are real (dtype f32 or f64)");
   if (dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_F64) memcpy(flat, buf.data(), buf.size() * sizeof(double));
   else {

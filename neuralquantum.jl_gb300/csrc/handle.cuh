@@ -24,6 +24,7 @@ struct nq_handle {
   int n_record = 0, write_last = 0;
   bool doubled = false, complex_params = true, f64 = false, ndm = false;
   int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
+  bool split = false;              // RBMSplit on the doubled-space path (complex parameters)
   bool diag = false;               // NQ_SPACE_DIAGONAL: NDM chains on the physical space, p ∝ ρ(σ,σ)
   int Md = 0;                      // diagonal sampler units (Mh + Ma)
   void* d_diag[3] = {};            // diagonal sampler network a [N], b [Md], W [Md x N] (cpx<R>)

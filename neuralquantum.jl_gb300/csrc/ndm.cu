@@ -15,6 +15,13 @@
 // The first Ms = 2Mh + Ma units are the ones that enter |ρ|^2, so the
 // Metropolis sampler of the RBM runs unchanged on them (λ units at weight
 // 1/2 through RbmDev::n_half).
+//
+// RBMSplit (src/Networks/MixedDensityMatrix/RBMSplit.jl:36-50, 111-129),
+// logρ = ar·σ + ac·η + Σ_h f(b_h + Wr_h·σ + Wc_h·η) with complex parameters,
+// is the same form with Mh = 0, U = Ma = M units of weight 1, a = (ar, ac)
+// and C = (Wr | Wc): its parameter vector (ar, ac, b, Wr, Wc) is exactly the
+// RBM layout over the 2N doubled sites, so the effective network is a copy of
+// it and O_k is the RBM's (v_i, f'(x_h), f'(x_h) v_i).
 #include "ndm_kernels.cuh"
 
 namespace {
@@ -64,7 +71,17 @@ template <typename R> NQ_D cpx<R> unit_weight(int u, int Mh, int Ma) {
 // O_k at a doubled configuration with unit derivatives g (real parameter k of
 // the reference order b_mu, h_mu, w_mu, u_mu, b_la, h_la, d_la, w_la, u_la).
 template <typename R>
-NQ_D cpx<R> ndm_O(int k, int N, int Mh, int Ma, const cpx<R>* g, int gstride, uint64_t bits, int hilb) {
+NQ_D cpx<R> ndm_O(int k, int N, int Mh, int Ma, const cpx<R>* g, int gstride, uint64_t bits, int hilb,
+                  int split) {
+  if (split) {
+    // RBMSplit: parameters (a over the 2N doubled sites, b, W column-major M x 2N)
+    const int N2 = 2 * N, M = Ma;
+    if (k < N2) return mk(site_value<R>(bits, k, hilb), R(0));
+    k -= N2;
+    if (k < M) return g[(size_t)k * gstride];
+    k -= M;
+    return site_value<R>(bits, k / M, hilb) * g[(size_t)(k % M) * gstride];
+  }
   const cpx<R> half_i = mk(R(0), R(0.5));
   // unit offsets: λσ 0, λη Mh, π 2Mh, μσ 2Mh+Ma, μη 3Mh+Ma
   const int oLs = 0, oLe = Mh, oPi = 2 * Mh, oMs = 2 * Mh + Ma, oMe = 3 * Mh + Ma;
@@ -141,7 +158,7 @@ ndm_eval_kernel(NdmEff<R> e, const uint64_t* __restrict__ samples, int n, int hi
   const cpx<R> lp = ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
   logrho[s] = lp;
   for (int k = 0; k < e.P; ++k) {
-    const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sg + threadIdx.x, T, bits, hilb);
+    const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sg + threadIdx.x, T, bits, hilb, e.split);
     if (X) {
       X[(size_t)(2 * k) * ldx + s] = (float)o.x;
       X[(size_t)(2 * k + 1) * ldx + s] = (float)o.y;
@@ -287,6 +304,41 @@ __global__ void ndm_diagonal_kernel(NdmDev<R> n, cpx<R>* __restrict__ a, cpx<R>*
   if (idx < N) a[idx] = mk(R(0.5) * n.b_la[idx], R(0));
 }
 
+// RBMSplit effective network: C = Cs = (Wr | Wc), b = bs = b, a = (ar, ac),
+// copied from the parameter vector p (complex, RBM layout over 2N sites)
+template <typename R>
+__global__ void split_effective_kernel(const cpx<R>* __restrict__ p, int N2, int M, cpx<R>* C, cpx<R>* bu,
+                                       cpx<R>* a, cpx<R>* Cs, cpx<R>* bs) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < M * N2) {
+    const cpx<R> w = p[N2 + M + idx];
+    C[idx] = w;
+    Cs[idx] = w;
+  }
+  if (idx < M) {
+    bu[idx] = p[N2 + idx];
+    bs[idx] = p[N2 + idx];
+  }
+  if (idx < N2) a[idx] = p[idx];
+}
+
+// RBMSplit diagonal: logρ(σ,σ) = (ar + ac)·σ + Σ_h f(b_h + (Wr + Wc)_h·σ), in
+// the sampler's convention with every unit at weight 1/2 (log p = Re logρ):
+// a = (ar + ac)/2, W = Wr + Wc
+template <typename R>
+__global__ void split_diagonal_kernel(const cpx<R>* __restrict__ p, int N, int M, cpx<R>* __restrict__ a,
+                                      cpx<R>* __restrict__ b, cpx<R>* __restrict__ W) {
+  const int N2 = 2 * N;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < M * N) {
+    const int h = idx % M, j = idx / M;
+    const cpx<R> wr = p[N2 + M + h + M * j], wc = p[N2 + M + h + M * (N + j)];
+    W[idx] = mk(wr.x + wc.x, wr.y + wc.y);
+  }
+  if (idx < M) b[idx] = p[N2 + idx];
+  if (idx < N) a[idx] = mk(R(0.5) * (p[idx].x + p[N + idx].x), R(0.5) * (p[idx].y + p[N + idx].y));
+}
+
 // doubled configuration (σ, σ) of each physical configuration σ
 __global__ void ndm_diag_expand_kernel(const uint64_t* in, int n, int N, uint64_t* out) {   // in == out allowed
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -370,7 +422,7 @@ ndm_grad_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int
       if (k < P) {
         for (int m = 0; m < CB; ++m) {
           if (s_list_s[m] < 0) break;
-          const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sgp + m, CB, sbits[m], hilb);
+          const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sgp + m, CB, sbits[m], hilb, e.split);
           const cpx<R> b = sbeta[m];
           acc[q].x += (double)(b.x * o.x - b.y * o.y);
           acc[q].y += (double)(b.x * o.y + b.y * o.x);
@@ -535,6 +587,20 @@ cudaError_t launch_ndm_diagonal(const NdmDev<R>& n, cpx<R>* a, cpx<R>* b, cpx<R>
   return cudaGetLastError();
 }
 
+template <typename R>
+cudaError_t launch_split_effective(const cpx<R>* p, int N, int M, const NdmEffBufs<R>& b, cudaStream_t st) {
+  const int N2 = 2 * N, tot = M * N2;
+  split_effective_kernel<R><<<(tot + 127) / 128, 128, 0, st>>>(p, N2, M, b.C, b.b, b.a, b.Cs, b.bs);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_split_diagonal(const cpx<R>* p, int N, int M, cpx<R>* a, cpx<R>* b, cpx<R>* W, cudaStream_t st) {
+  const int tot = M * N > N ? M * N : N;
+  split_diagonal_kernel<R><<<(tot + 127) / 128, 128, 0, st>>>(p, N, M, a, b, W);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ndm_diag_expand(const uint64_t* in, int n, int N, uint64_t* out, cudaStream_t st) {
   if (n < 1) return cudaSuccess;
   ndm_diag_expand_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, N, out);
@@ -591,3 +657,7 @@ template cudaError_t launch_ndm_diag_obs<float>(const NdmEff<float>&, int, const
 template cudaError_t launch_ndm_diag_obs<double>(const NdmEff<double>&, int, const DevOp&, const uint64_t*, int, int, cpx<double>*, cpx<double>*, cudaStream_t);
 template cudaError_t launch_ndm_diagonal<float>(const NdmDev<float>&, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
 template cudaError_t launch_ndm_diagonal<double>(const NdmDev<double>&, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
+template cudaError_t launch_split_effective<float>(const cpx<float>*, int, int, const NdmEffBufs<float>&, cudaStream_t);
+template cudaError_t launch_split_effective<double>(const cpx<double>*, int, int, const NdmEffBufs<double>&, cudaStream_t);
+template cudaError_t launch_split_diagonal<float>(const cpx<float>*, int, int, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
+template cudaError_t launch_split_diagonal<double>(const cpx<double>*, int, int, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);

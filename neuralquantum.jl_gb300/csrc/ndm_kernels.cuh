@@ -30,6 +30,7 @@ NQ_HD int ndm_n_params(int N, int Mh, int Ma) { return 2 * N + 2 * Mh + Ma + 2 *
 // Effective generalised-RBM form over the 2N doubled sites (see ndm.cu).
 template <typename R> struct NdmEff {
   int N = 0, N2 = 0, Mh = 0, Ma = 0, U = 0, P = 0;
+  int split = 0;               // RBMSplit: Mh = 0, Ma = U = M units of weight 1, RBM parameter layout
   const cpx<R>* C = nullptr;   // [U x N2] column-major
   const cpx<R>* b = nullptr;   // [U]
   const cpx<R>* a = nullptr;   // [N2]
@@ -65,6 +66,12 @@ cudaError_t launch_ndm_diag_obs(const NdmEff<R>& e, int act, const DevOp& op, co
 // N-site sampler tables of p(σ) ∝ ρ(σ,σ): a [N], b [Mh+Ma], W [(Mh+Ma) x N]
 template <typename R>
 cudaError_t launch_ndm_diagonal(const NdmDev<R>& n, cpx<R>* a, cpx<R>* b, cpx<R>* W, cudaStream_t st);
+// RBMSplit: effective network copied from the complex parameters p (RBM layout over 2N sites)
+template <typename R>
+cudaError_t launch_split_effective(const cpx<R>* p, int N, int M, const NdmEffBufs<R>& b, cudaStream_t st);
+// RBMSplit diagonal sampler tables: a [N], b [M], W [M x N]
+template <typename R>
+cudaError_t launch_split_diagonal(const cpx<R>* p, int N, int M, cpx<R>* a, cpx<R>* b, cpx<R>* W, cudaStream_t st);
 // out[s] = (σ, σ) as 2N-site bits
 cudaError_t launch_ndm_diag_expand(const uint64_t* in, int n, int N, uint64_t* out, cudaStream_t st);
 

@@ -27,7 +27,7 @@ NQ_OK, NQ_ERR_ARG, NQ_ERR_CUDA, NQ_ERR_NOT_PD, NQ_ERR_TIMEOUT, NQ_ERR_NAN, NQ_ER
     NQ_ERR_UNSUPPORTED = range(8)
 STATUS_NAMES = ["NQ_OK", "NQ_ERR_ARG", "NQ_ERR_CUDA", "NQ_ERR_NOT_PD", "NQ_ERR_TIMEOUT",
                 "NQ_ERR_NAN", "NQ_ERR_STATE", "NQ_ERR_UNSUPPORTED"]
-NQ_NET_RBM, NQ_NET_NDM = 0, 1
+NQ_NET_RBM, NQ_NET_NDM, NQ_NET_RBM_SPLIT = 0, 1, 2
 NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS = 0, 1
 NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3

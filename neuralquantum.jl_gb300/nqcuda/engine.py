@@ -5,7 +5,7 @@ import numpy as np
 
 from . import _lib
 from .hilbert import SuperOpSpace, physical
-from .networks import RBM, NDM, af_logcosh
+from .networks import RBM, NDM, RBMSplit, af_logcosh
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
@@ -23,6 +23,10 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
         cfg.network = _lib.NQ_NET_NDM
         cfg.n_hidden = net.Mh
         cfg.n_ancilla = net.Ma
+    elif isinstance(net, RBMSplit):
+        cfg.network = _lib.NQ_NET_RBM_SPLIT
+        cfg.n_hidden = net.M
+        cfg.n_ancilla = 0
     else:
         raise TypeError(f"unsupported network {type(net)}")
     cfg.activation = _lib.NQ_ACT_LOGCOSH if net.f == af_logcosh else _lib.NQ_ACT_SOFTPLUS
@@ -52,7 +56,7 @@ class Engine:
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
                           s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind, rule, sampler_space)
-        self.complex_params = isinstance(net, RBM)
+        self.complex_params = isinstance(net, (RBM, RBMSplit))
         self.cfg = cfg
         self.lib = L
         self._owned = _handle is None

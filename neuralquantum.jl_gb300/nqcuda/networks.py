@@ -1,8 +1,9 @@
 """Network parameter containers of the reference API (host side).
 
-``RBM(T, N, α, f)`` (src/Networks/ClosedSystems/RBM.jl:40-48) and
-``NDM(T, N, αh, αa, f)`` (src/Networks/MixedDensityMatrix/NDM.jl:50-63) hold
-their arrays on the host in the reference layout; the engine keeps the
+``RBM(T, N, α, f)`` (src/Networks/ClosedSystems/RBM.jl:40-48),
+``NDM(T, N, αh, αa, f)`` (src/Networks/MixedDensityMatrix/NDM.jl:50-63) and
+``RBMSplit(T, N, α)`` (src/Networks/MixedDensityMatrix/RBMSplit.jl:33-42)
+hold their arrays on the host in the reference layout; the engine keeps the
 authoritative FP64 copy on the device while a ``BatchedSampler`` is bound and
 writes it back after every ``update_``.  The flat parameter vector is the
 functor field order with column-major arrays (src/tuple_logic.jl:31-72).
@@ -75,6 +76,44 @@ class NDM:
             n = int(np.prod(self.shapes[k]))
             setattr(self, k, v[o:o + n].reshape(self.shapes[k], order="F").astype(self.dtype))
             o += n
+
+
+class RBMSplit:
+    """Density-matrix RBM over (σ, η) with complex weights: fields ar, ac (N),
+    b (αN), Wr, Wc (αN x N); the activation is logcosh (logℒ), as in the
+    reference, unless given."""
+
+    FIELDS = ("ar", "ac", "b", "Wr", "Wc")
+
+    def __init__(self, T, N, alpha, f=af_logcosh):
+        self.dtype = np.dtype(T)
+        if self.dtype.kind != "c":
+            raise ValueError("RBMSplit takes complex weights (ComplexF32 / ComplexF64)")
+        self.N = int(N)
+        self.M = int(round(alpha * N))
+        self.f = f
+        N, M = self.N, self.M
+        self.shapes = {"ar": (N,), "ac": (N,), "b": (M,), "Wr": (M, N), "Wc": (M, N)}
+        for k in self.FIELDS:
+            setattr(self, k, np.zeros(self.shapes[k], self.dtype))
+
+    @property
+    def n_params(self):
+        return 2 * self.N + self.M + 2 * self.M * self.N
+
+    def flat(self):
+        return np.concatenate([getattr(self, k).reshape(-1, order="F") for k in self.FIELDS]).astype(np.complex128)
+
+    def set_flat(self, v):
+        v = np.asarray(v)
+        o = 0
+        for k in self.FIELDS:
+            n = int(np.prod(self.shapes[k]))
+            setattr(self, k, v[o:o + n].reshape(self.shapes[k], order="F").astype(self.dtype))
+            o += n
+
+    def __repr__(self):
+        return f"RBMSplit({self.dtype}, n={self.N}, α={self.M / self.N})"
 
 
 def init_random_pars_(net, sigma=0.01, rng=None):

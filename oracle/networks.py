@@ -7,6 +7,8 @@ Flat parameter order = functor field order, each array column-major
 * NDM  (src/Networks/MixedDensityMatrix/NDM.jl:3-19): b_mu (N), h_mu (aN),
   w_mu (aN x N), u_mu (bN x N), b_la (N), h_la (aN), d_la (bN), w_la (aN x N),
   u_la (bN x N)
+* RBMSplit (src/Networks/MixedDensityMatrix/RBMSplit.jl:3-10): ar (N),
+  ac (N), b (aN), Wr (aN x N), Wc (aN x N)
 
 Activations follow src/Networks/activation.jl:5-45; the derivative used by the
 networks is ``fwd_der(f, x)`` (tanh for logcosh, sigmoid for softplus).
@@ -184,6 +186,59 @@ class NDM:
 
     def log_prob(self, sr, sc):
         """2 Re log ρ(σ, η) on doubled states (base_batched_networks.jl:255-258)."""
+        return 2.0 * np.real(self.logpsi(sr, sc))
+
+
+class RBMSplit:
+    """logρ(σ, η) = ar·σ + ac·η + Σ_h f(b_h + Wr_h·σ + Wc_h·η), complex
+    parameters (RBMSplit.jl:48-50 for the value, :111-129 for ∇: ar → σ,
+    ac → η, b → f'(θ), Wr → f'(θ) σᵀ, Wc → f'(θ) ηᵀ)."""
+
+    FIELDS = ("ar", "ac", "b", "Wr", "Wc")
+
+    def __init__(self, n, m, activation=LOGCOSH):
+        self.N, self.M = int(n), int(m)
+        self.activation = activation
+        N, M = self.N, self.M
+        self.shapes = {"ar": (N,), "ac": (N,), "b": (M,), "Wr": (M, N), "Wc": (M, N)}
+        for f in self.FIELDS:
+            setattr(self, f, np.zeros(self.shapes[f], np.complex128))
+
+    @property
+    def n_params(self):
+        return 2 * self.N + self.M + 2 * self.M * self.N
+
+    def flat(self):
+        return np.concatenate([getattr(self, f).reshape(-1, order="F") for f in self.FIELDS])
+
+    def set_flat(self, v):
+        v = np.asarray(v).astype(np.complex128)
+        o = 0
+        for f in self.FIELDS:
+            n = int(np.prod(self.shapes[f]))
+            setattr(self, f, v[o:o + n].reshape(self.shapes[f], order="F").copy())
+            o += n
+
+    def _theta(self, sr, sc):
+        return sr @ self.Wr.T + sc @ self.Wc.T + self.b[None, :]
+
+    def logpsi(self, sr, sc):
+        sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
+        return sr @ self.ar + sc @ self.ac + act(self.activation, self._theta(sr, sc)).sum(axis=1)
+
+    def logpsi_and_grad(self, sr, sc):
+        sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
+        th = self._theta(sr, sc)
+        out = sr @ self.ar + sc @ self.ac + act(self.activation, th).sum(axis=1)
+        g = dact(self.activation, th)
+        B = sr.shape[0]
+        dWr = (g[:, :, None] * sr[:, None, :]).transpose(0, 2, 1).reshape(B, -1)
+        dWc = (g[:, :, None] * sc[:, None, :]).transpose(0, 2, 1).reshape(B, -1)
+        grad = np.concatenate([sr.astype(np.complex128), sc.astype(np.complex128), g, dWr, dWc], axis=1)
+        return out, grad
+
+    def log_prob(self, sr, sc):
+        """2 Re logρ on doubled states (base_batched_networks.jl:255-258)."""
         return 2.0 * np.real(self.logpsi(sr, sc))
 
 

@@ -83,9 +83,11 @@ def test_gradients_vs_finite_differences(act):
     nw.init_random_pars(r, rng, sigma=0.2 ** 2)
     n = nw.NDM(N, 1, 2, act)
     nw.init_random_pars(n, rng, sigma=0.2 ** 2)
+    sp = nw.RBMSplit(N, 2 * N, act)
+    nw.init_random_pars(sp, rng, sigma=0.2 ** 2)
     s = rng.choice([-1.0, 1.0], size=(3, N))
     sr = rng.choice([0.0, 1.0], size=(3, N)); sc = rng.choice([0.0, 1.0], size=(3, N))
-    for net, f, args in ((r, r.logpsi, (s,)), (n, n.logpsi, (sr, sc))):
+    for net, f, args in ((r, r.logpsi, (s,)), (n, n.logpsi, (sr, sc)), (sp, sp.logpsi, (sr, sc))):
         _, g = net.logpsi_and_grad(*args)
         p = net.flat()
         eps = 1e-6
@@ -94,6 +96,24 @@ def test_gradients_vs_finite_differences(act):
             q[k] -= 2 * eps; net.set_flat(q); lm = f(*args)
             assert np.max(np.abs((lp - lm) / (2 * eps) - g[:, k])) < 1e-7
         net.set_flat(p)
+
+
+def test_rbmsplit_is_the_rbm_of_the_doubled_sites():
+    """RBMSplit.jl:48-50: logρ(σ, η) equals an RBM over the 2N sites (σ, η)
+    with a = (ar, ac) and W = (Wr | Wc); the flat vectors coincide
+    (ar, ac, b, Wr, Wc column-major = a, b, W column-major)."""
+    rng = np.random.default_rng(12)
+    N, M = 3, 5
+    sp = nw.RBMSplit(N, M, nw.LOGCOSH)
+    nw.init_random_pars(sp, rng, sigma=0.3 ** 2)
+    r = nw.RBM(2 * N, M, nw.LOGCOSH)
+    r.set_flat(sp.flat())
+    np.testing.assert_array_equal(r.a, np.concatenate([sp.ar, sp.ac]))
+    np.testing.assert_array_equal(r.W, np.concatenate([sp.Wr, sp.Wc], axis=1))
+    sr = rng.choice([-1.0, 1.0], size=(7, N)); sc = rng.choice([-1.0, 1.0], size=(7, N))
+    v = np.concatenate([sr, sc], axis=1)
+    np.testing.assert_allclose(sp.logpsi(sr, sc), r.logpsi(v), rtol=0, atol=1e-13)
+    np.testing.assert_allclose(sp.logpsi_and_grad(sr, sc)[1], r.logpsi_and_grad(v)[1], rtol=0, atol=1e-13)
 
 
 def test_ndm_parameter_count():
