@@ -69,9 +69,14 @@ typedef enum {
  * NQ_NET_NDM: purified density matrix (MixedDensityMatrix/NDM.jl), real
  * parameters, n_hidden = αN, n_ancilla = βN.  NQ_NET_RBM_SPLIT: RBMSplit
  * density matrix (MixedDensityMatrix/RBMSplit.jl), complex parameters
- * (ar, ac, b, Wr, Wc), n_hidden = αN.  The density matrices sample the
- * doubled space (σ, η) and take the Liouvillian cost function. */
-typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2 } nq_network;
+ * (ar, ac, b, Wr, Wc), n_hidden = αN.  NQ_NET_NDM_SYMM: NDMSymm
+ * (MixedDensityMatrix/NDMSymm.jl), an NDM whose n_symm x n_hidden hidden and
+ * n_symm x n_ancilla ancilla units are the permutations (nq_set_symmetry) of
+ * n_hidden / n_ancilla symmetric features; the trainable parameters are the
+ * symmetric NDM's (real, NDM order, sizes n_hidden and n_ancilla).  The
+ * density matrices sample the doubled space (σ, η) and take the Liouvillian
+ * cost function. */
+typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_SYMM = 3 } nq_network;
 typedef enum { NQ_ACT_LOGCOSH = 0, NQ_ACT_SOFTPLUS = 1 } nq_activation;
 typedef enum { NQ_HILB_SPIN = 0, NQ_HILB_FOCK = 1 } nq_hilbert;
 typedef enum { NQ_DTYPE_C64 = 0, NQ_DTYPE_C128 = 1, NQ_DTYPE_F32 = 2, NQ_DTYPE_F64 = 3 } nq_dtype;
@@ -116,7 +121,8 @@ typedef struct {
   int32_t sampler_kind;    /* nq_sampler_kind */
   int32_t rule;            /* nq_mcmc_rule (Metropolis sampler) */
   int32_t sampler_space;   /* nq_sampler_space */
-  int32_t reserved[2];
+  int32_t n_symm;          /* NQ_NET_NDM_SYMM: number of permutations */
+  int32_t reserved[1];
 } nq_config;
 
 /* Space the sampler draws from.  NQ_SPACE_NETWORK: the network's own space
@@ -295,6 +301,11 @@ nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs);
  * that changes the configuration; its move classes and tables must fit the
  * sampler's shared memory (NQ_ERR_UNSUPPORTED otherwise). */
 nq_status nq_set_rule_operator(nq_handle* h, const nq_op_table* op);
+/* NDMSymm permutations: n_perm (= n_symm) rows of n_sites 0-based sites,
+ * row j the image perm_j(i) of site i (NDMSymm.jl:114-120: bare unit
+ * j + f n_symm carries the symmetric weight (f, i) on site perm_j(i)).  Required
+ * before the parameters of an NQ_NET_NDM_SYMM handle take effect. */
+nq_status nq_set_symmetry(nq_handle* h, int32_t n_perm, const int32_t* perms);
 
 /* ---- timing/diagnostics ----------------------------------------------------
  * Device milliseconds of the last staged calls (CUDA events on the handle's

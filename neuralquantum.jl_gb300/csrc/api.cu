@@ -15,6 +15,7 @@ NdmEff<R> ndm_eff(nq_handle* h) {
   NdmEff<R> e;
   e.N = h->N; e.N2 = h->N2; e.Mh = h->Mh; e.Ma = h->Ma; e.U = h->U; e.P = h->P;
   e.split = h->split ? 1 : 0;
+  e.sym_off = h->d_sym_off; e.sym_idx = h->d_sym_idx; e.sym_coef = h->d_sym_coef;
   e.C = reinterpret_cast<const cpx<R>*>(h->d_eff[0]);
   e.b = reinterpret_cast<const cpx<R>*>(h->d_eff[1]);
   e.a = reinterpret_cast<const cpx<R>*>(h->d_eff[2]);
@@ -24,6 +25,12 @@ NdmEff<R> ndm_eff(nq_handle* h) {
 template <typename R>
 nq_status ndm_refresh(nq_handle* h) {
   const R* p = h->f64 ? reinterpret_cast<const R*>(h->d_master) : reinterpret_cast<const R*>(h->d_p32);
+  if (h->symm) {
+    // NDMSymm: evaluate the bare NDM built from the symmetric parameters
+    if (!h->sym_ready) return NQ_OK;
+    CKL(launch_ndm_symm_bare<R>(p, h->N, h->sym_h, h->sym_a, h->n_symm, h->d_perms, (R*)h->d_bare, h->st));
+    p = reinterpret_cast<const R*>(h->d_bare);
+  }
   NdmEffBufs<R> b;
   b.C = (cpx<R>*)h->d_eff[0]; b.b = (cpx<R>*)h->d_eff[1]; b.a = (cpx<R>*)h->d_eff[2];
   b.Cs = (cpx<R>*)h->d_eff[3]; b.bs = (cpx<R>*)h->d_eff[4];
@@ -47,6 +54,7 @@ nq_status ndm_refresh(nq_handle* h) {
 // refresh FP32 copies and the per-flip tables after a parameter change
 nq_status refresh_params(nq_handle* h) {
   if (h->ndm) {
+    if (h->symm) CKL(launch_ndm_symm_project(h->d_master, h->N, h->sym_h, h->sym_a, h->st));
     if (!h->f64) CKL(launch_master_to_f32(h->d_master, (h->complex_params ? 2L : 1L) * h->P, h->d_p32, h->st));
     return h->f64 ? ndm_refresh<double>(h) : ndm_refresh<float>(h);
   }
@@ -445,9 +453,11 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     delete h;
     return NQ_ERR_ARG;
   };
-  if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM && c.network != NQ_NET_RBM_SPLIT)
+  if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM && c.network != NQ_NET_RBM_SPLIT &&
+      c.network != NQ_NET_NDM_SYMM)
     return bad("unknown network");
-  const bool matrix_net = c.network == NQ_NET_NDM || c.network == NQ_NET_RBM_SPLIT;
+  const bool matrix_net = c.network == NQ_NET_NDM || c.network == NQ_NET_RBM_SPLIT || c.network == NQ_NET_NDM_SYMM;
+  if (c.network == NQ_NET_NDM_SYMM && (c.n_symm < 1 || c.n_symm > 64)) return bad("NDMSymm: n_symm must be in 1..64");
   if (c.activation != NQ_ACT_LOGCOSH && c.activation != NQ_ACT_SOFTPLUS) return bad("unknown activation");
   if (c.hilbert != NQ_HILB_SPIN && c.hilbert != NQ_HILB_FOCK) return bad("unknown hilbert space");
   if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
@@ -492,8 +502,12 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     // effective form with M units of weight 1 (Mh = 0, Ma = M)
     h->ndm = true;
     h->split = c.network == NQ_NET_RBM_SPLIT;
-    h->Mh = h->split ? 0 : c.n_hidden;
-    h->Ma = h->split ? c.n_hidden : c.n_ancilla;
+    h->symm = c.network == NQ_NET_NDM_SYMM;
+    h->n_symm = h->symm ? c.n_symm : 1;
+    h->sym_h = c.n_hidden;
+    h->sym_a = c.n_ancilla;
+    h->Mh = h->split ? 0 : c.n_hidden * h->n_symm;
+    h->Ma = h->split ? c.n_hidden : c.n_ancilla * h->n_symm;
     if (!h->split && h->Ma < 1) return bad("the NDM needs n_ancilla >= 1");
     h->N2 = 2 * h->N;
     h->U = 4 * h->Mh + h->Ma;
@@ -501,7 +515,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     h->diag = c.sampler_space == NQ_SPACE_DIAGONAL;
     h->Md = h->Mh + h->Ma;
     h->nst = h->diag ? h->N : h->N2;
-    h->P = h->split ? 2 * h->N + h->Ma + 2 * h->N * h->Ma : ndm_n_params(h->N, h->Mh, h->Ma);
+    h->P = h->split ? 2 * h->N + h->Ma + 2 * h->N * h->Ma
+                    : (h->symm ? ndm_n_params(h->N, h->sym_h, h->sym_a) : ndm_n_params(h->N, h->Mh, h->Ma));
+    h->P_bare = h->symm ? ndm_n_params(h->N, h->Mh, h->Ma) : h->P;
     if (h->N2 > 64) return bad("the NDM supports n_sites <= 32 (2N doubled sites)");
     if (h->Ms > 320) return bad("2*n_hidden + n_ancilla must be <= 320");
     if (h->P > 256 * 24) return bad("too many density-matrix parameters (max 6144)");
@@ -549,6 +565,8 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   if (h->ndm) {
     const size_t ne[5] = {(size_t)h->U * h->N2, (size_t)h->U, (size_t)h->N2, (size_t)h->Ms * h->N2, (size_t)h->Ms};
     for (int k = 0; k < 5; ++k) step(cudaMalloc(&h->d_eff[k], ne[k] * csz + 16), "effective network");
+    if (h->symm) step(cudaMalloc(&h->d_bare, (size_t)h->P_bare * (h->f64 ? sizeof(double) : sizeof(float)) + 16),
+                      "bare parameters");
     if (h->diag) {
       const size_t nd[3] = {(size_t)h->N, (size_t)h->Md, (size_t)h->Md * h->N};
       for (int k = 0; k < 3; ++k) step(cudaMalloc(&h->d_diag[k], nd[k] * csz + 16), "diagonal network");
@@ -680,7 +698,8 @@ void nq_destroy(nq_handle* h) {
                   h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_exact, h->d_pairs, h->d_xtab[0],
                   h->d_xtab[1], h->d_xtab[2], h->d_xW, h->d_xare, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial,
-                  h->d_diag[0], h->d_diag[1], h->d_diag[2]};
+                  h->d_diag[0], h->d_diag[1], h->d_diag[2], h->d_bare, h->d_perms};
+  for (void* p : h->sym_allocs) cudaFree(p);
   for (void* p : bufs)
     if (p) cudaFree(p);
   {
@@ -780,6 +799,72 @@ nq_status nq_set_exchange(nq_handle* h, int32_t n, const int32_t* pairs) {
   h->sampler_block = 0;
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
   if (nq_status s = refresh_params(h)) return s;
+  CK(cudaStreamSynchronize(h->st));
+  return NQ_OK;
+}
+
+// NDMSymm: permutations, and the map from the symmetric parameters to the bare
+// ones for the gradient (construct_∇matrices, NDMSymm.jl:135-180): b_mu / b_la
+// of every site average all bare sites' (coefficient 1/N), a hidden or
+// ancilla bias sums its n_symm copies, weight (f, i) sums the bare weights
+// (j + f n_symm, perm_j(i)).
+nq_status nq_set_symmetry(nq_handle* h, int32_t n_perm, const int32_t* perms) {
+  if (!h || !perms) return NQ_ERR_ARG;
+  if (!h->symm) return fail(h, NQ_ERR_STATE, "the handle is not an NDMSymm");
+  const int N = h->N, ns = h->n_symm, ah = h->sym_h, aa = h->sym_a, Mh = h->Mh, Ma = h->Ma;
+  if (n_perm != ns) return fail(h, NQ_ERR_ARG, "expected %d permutations, got %d", ns, n_perm);
+  for (int j = 0; j < ns; ++j) {
+    std::vector<int> seen(N, 0);
+    for (int i = 0; i < N; ++i) {
+      const int v = perms[j * N + i];
+      if (v < 0 || v >= N || seen[v]++) return fail(h, NQ_ERR_ARG, "permutation %d is not a permutation of 0..%d", j, N - 1);
+    }
+  }
+  // symmetric and bare field offsets (b_mu, h_mu, w_mu, u_mu, b_la, h_la, d_la, w_la, u_la)
+  auto offsets = [N](int mh, int ma, int* o) {
+    o[0] = 0; o[1] = o[0] + N; o[2] = o[1] + mh; o[3] = o[2] + mh * N; o[4] = o[3] + ma * N;
+    o[5] = o[4] + N; o[6] = o[5] + mh; o[7] = o[6] + ma; o[8] = o[7] + mh * N;
+  };
+  int so[9], bo[9];
+  offsets(ah, aa, so);
+  offsets(Mh, Ma, bo);
+  std::vector<int> off(1, 0), idx;
+  std::vector<double> coef;
+  auto put = [&](int bare, double c) { idx.push_back(bare); coef.push_back(c); };
+  for (int f9 = 0; f9 < 9; ++f9) {
+    const bool isb = f9 == 0 || f9 == 4, ish = f9 == 1 || f9 == 5, isd = f9 == 6;
+    const bool isw = f9 == 2 || f9 == 7, isu = f9 == 3 || f9 == 8;
+    const int n = isb ? N : (ish ? ah : (isd ? aa : (isw ? ah * N : aa * N)));
+    for (int k = 0; k < n; ++k) {
+      if (isb) {
+        for (int i = 0; i < N; ++i) put(bo[f9] + i, 1.0 / N);
+      } else if (ish || isd) {
+        for (int j = 0; j < ns; ++j) put(bo[f9] + k * ns + j, 1.0);
+      } else {
+        const int rows = isw ? ah : aa, brows = isw ? Mh : Ma;
+        const int f = k % rows, i = k / rows;
+        for (int j = 0; j < ns; ++j) put(bo[f9] + (j + f * ns) + brows * perms[j * N + i], 1.0);
+      }
+      off.push_back((int)idx.size());
+    }
+  }
+  if ((int)off.size() != h->P + 1) return fail(h, NQ_ERR_ARG, "internal: symmetric parameter count");
+  CK(cudaStreamSynchronize(h->st));
+  for (void* p : h->sym_allocs) cudaFree(p);
+  h->sym_allocs.clear();
+  cudaFree(h->d_perms);
+  h->d_perms = nullptr;
+  h->sym_ready = false;
+  nq_status s;
+  if ((s = upload(h, (const int*)off.data(), off.size(), &h->d_sym_off, &h->sym_allocs)) != NQ_OK ||
+      (s = upload(h, (const int*)idx.data(), idx.size(), &h->d_sym_idx, &h->sym_allocs)) != NQ_OK ||
+      (s = upload(h, (const double*)coef.data(), coef.size(), &h->d_sym_coef, &h->sym_allocs)) != NQ_OK)
+    return s;
+  CK(cudaMalloc((void**)&h->d_perms, (size_t)ns * N * sizeof(int)));
+  CK(cudaMemcpy(h->d_perms, perms, (size_t)ns * N * sizeof(int), cudaMemcpyHostToDevice));
+  h->sym_ready = true;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  if (nq_status r = refresh_params(h)) return r;
   CK(cudaStreamSynchronize(h->st));
   return NQ_OK;
 }
@@ -931,6 +1016,7 @@ nq_status nq_set_operator(nq_handle* h, const nq_op_table* t) {
 
 nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* stats, double* loc_out) {
   if (!h || !obs || !stats) return NQ_ERR_ARG;
+  if (h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
   if (h->ndm && !h->diag)
     return fail(h, NQ_ERR_UNSUPPORTED,
                 "observables of a density matrix are estimated on its diagonal (NQ_SPACE_DIAGONAL handle)");
@@ -997,6 +1083,7 @@ nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* st
 }
 
 nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out, uint8_t* accept_bits) {
+  if (h && h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
   if (!h) return NQ_ERR_ARG;
   if (nq_status ts = ensure_tuned(h)) return ts;
   unsigned char* d_bits = nullptr;
@@ -1041,6 +1128,7 @@ nq_status nq_set_samples(nq_handle* h, const int8_t* samples) {
 
 static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, double* out, double* grad) {
   if (!h || !sigma || !out || n < 1) return NQ_ERR_ARG;
+  if (h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
   for (int64_t i = 0; i < n * h->nst; ++i) {
     int v = sigma[i];
     bool ok = h->hilb == NQ_HILB_SPIN ? (v == 1 || v == -1) : (v == 0 || v == 1);
@@ -1103,6 +1191,7 @@ nq_status nq_logpsi_grad(nq_handle* h, const int8_t* sigma, int64_t n, double* o
 nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, double* force_out) {
   if (!h) return NQ_ERR_ARG;
   NQ_REJECT_DIAG(h, "nq_estimate");
+  if (h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
   if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
   nq_status s;
   CK(cudaEventRecord(h->ev[1], h->st));
@@ -1213,6 +1302,7 @@ nq_status nq_update_descent(nq_handle* h, double lr) {
 nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, nq_measurement* stats) {
   if (!h) return NQ_ERR_ARG;
   NQ_REJECT_DIAG(h, "nq_vmc_step");
+  if (h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
   if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
   if (h->graph && (h->graph_eps != eps || h->graph_lr != lr)) {
     cudaGraphExecDestroy(h->graph);

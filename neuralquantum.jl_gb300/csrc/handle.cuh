@@ -25,6 +25,15 @@ struct nq_handle {
   bool doubled = false, complex_params = true, f64 = false, ndm = false;
   int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
   bool split = false;              // RBMSplit on the doubled-space path (complex parameters)
+  bool symm = false;               // NDMSymm: trainable symmetric NDM, evaluated as its bare NDM
+  bool sym_ready = false;          // NDMSymm permutations set (nq_set_symmetry)
+  int n_symm = 0, sym_h = 0, sym_a = 0, P_bare = 0;   // permutations, symmetric features, bare parameters
+  void* d_bare = nullptr;          // bare NDM parameters (R)
+  int* d_perms = nullptr;          // [n_symm x N]
+  std::vector<void*> sym_allocs;   // symmetrisation map (offsets, bare indices, coefficients)
+  const int* d_sym_off = nullptr;
+  const int* d_sym_idx = nullptr;
+  const double* d_sym_coef = nullptr;
   bool diag = false;               // NQ_SPACE_DIAGONAL: NDM chains on the physical space, p ∝ ρ(σ,σ)
   int Md = 0;                      // diagonal sampler units (Mh + Ma)
   void* d_diag[3] = {};            // diagonal sampler network a [N], b [Md], W [Md x N] (cpx<R>)

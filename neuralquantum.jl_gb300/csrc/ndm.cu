@@ -119,6 +119,18 @@ NQ_D cpx<R> ndm_O(int k, int N, int Mh, int Ma, const cpx<R>* g, int gstride, ui
 #undef G_
 }
 
+// O of trainable parameter k: the network's own, or for NDMSymm the sum of
+// the bare parameters' O that the symmetric parameter k stands for
+// (symmetrize_∇logψ_NDM!, NDMSymm.jl:76-87)
+template <typename R>
+NQ_D cpx<R> ndm_O_train(const NdmEff<R>& e, int k, const cpx<R>* g, int gstride, uint64_t bits, int hilb) {
+  if (!e.sym_off) return ndm_O<R>(k, e.N, e.Mh, e.Ma, g, gstride, bits, hilb, e.split);
+  cpx<R> o = mk(R(0), R(0));
+  for (int q = e.sym_off[k]; q < e.sym_off[k + 1]; ++q)
+    o = o + (R)e.sym_coef[q] * ndm_O<R>(e.sym_idx[q], e.N, e.Mh, e.Ma, g, gstride, bits, hilb, 0);
+  return o;
+}
+
 // unit pre-activations x_u and derivatives g_u at configuration `bits`
 // into per-thread slices of shared memory (stride T)
 template <typename R, int ACT>
@@ -158,7 +170,7 @@ ndm_eval_kernel(NdmEff<R> e, const uint64_t* __restrict__ samples, int n, int hi
   const cpx<R> lp = ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
   logrho[s] = lp;
   for (int k = 0; k < e.P; ++k) {
-    const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sg + threadIdx.x, T, bits, hilb, e.split);
+    const cpx<R> o = ndm_O_train<R>(e, k, sg + threadIdx.x, T, bits, hilb);
     if (X) {
       X[(size_t)(2 * k) * ldx + s] = (float)o.x;
       X[(size_t)(2 * k + 1) * ldx + s] = (float)o.y;
@@ -339,6 +351,55 @@ __global__ void split_diagonal_kernel(const cpx<R>* __restrict__ p, int N, int M
   if (idx < N) a[idx] = mk(R(0.5) * (p[idx].x + p[N + idx].x), R(0.5) * (p[idx].y + p[N + idx].y));
 }
 
+// NDMSymm bare parameters (set_bare_params!, NDMSymm.jl:89-133): b = the
+// (already averaged) symmetric b; bare hidden unit j + f ns has bias h_f and
+// weights w[j + f ns, perm_j[i]] = w_symm[f, i]; ancilla units alike.
+template <typename R>
+__global__ void ndm_symm_bare_kernel(const R* __restrict__ symm, int N, int ah, int aa, int ns,
+                                     const int* __restrict__ perms, R* __restrict__ bare) {
+  const NdmDev<R> sv = ndm_view<R>(symm, N, ah, aa);
+  const int Mh = ah * ns, Ma = aa * ns;
+  const NdmDev<R> bv = ndm_view<R>(bare, N, Mh, Ma);
+  R* b_mu = const_cast<R*>(bv.b_mu); R* h_mu = const_cast<R*>(bv.h_mu); R* w_mu = const_cast<R*>(bv.w_mu);
+  R* u_mu = const_cast<R*>(bv.u_mu); R* b_la = const_cast<R*>(bv.b_la); R* h_la = const_cast<R*>(bv.h_la);
+  R* d_la = const_cast<R*>(bv.d_la); R* w_la = const_cast<R*>(bv.w_la); R* u_la = const_cast<R*>(bv.u_la);
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int i = tid; i < N; i += nth) {
+    b_mu[i] = sv.b_mu[i];
+    b_la[i] = sv.b_la[i];
+  }
+  for (int q = tid; q < Mh; q += nth) {
+    h_mu[q] = sv.h_mu[q / ns];
+    h_la[q] = sv.h_la[q / ns];
+  }
+  for (int q = tid; q < Ma; q += nth) d_la[q] = sv.d_la[q / ns];
+  for (int q = tid; q < ah * ns * N; q += nth) {     // (f, j, i): symm (f, i) -> bare (j + f ns, perm_j[i])
+    const int i = q % N, j = (q / N) % ns, f = q / (N * ns);
+    const int row = j + f * ns, col = perms[j * N + i];
+    w_mu[row + Mh * col] = sv.w_mu[f + ah * i];
+    w_la[row + Mh * col] = sv.w_la[f + ah * i];
+  }
+  for (int q = tid; q < aa * ns * N; q += nth) {
+    const int i = q % N, j = (q / N) % ns, f = q / (N * ns);
+    const int row = j + f * ns, col = perms[j * N + i];
+    u_mu[row + Ma * col] = sv.u_mu[f + aa * i];
+    u_la[row + Ma * col] = sv.u_la[f + aa * i];
+  }
+}
+
+// the symmetric b_mu and b_la become their means (NDMSymm.jl:97-98), in the FP64 master
+__global__ void ndm_symm_project_kernel(double* symm, int N, int ah, int aa) {
+  const NdmDev<double> v = ndm_view<double>(symm, N, ah, aa);
+  double* b[2] = {const_cast<double*>(v.b_mu), const_cast<double*>(v.b_la)};
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w > 1) return;
+  double s = 0.0;
+  for (int i = lane; i < N; i += 32) s += b[w][i];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  const double m = s / N;
+  for (int i = lane; i < N; i += 32) b[w][i] = m;
+}
+
 // doubled configuration (σ, σ) of each physical configuration σ
 __global__ void ndm_diag_expand_kernel(const uint64_t* in, int n, int N, uint64_t* out) {   // in == out allowed
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -422,7 +483,7 @@ ndm_grad_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int
       if (k < P) {
         for (int m = 0; m < CB; ++m) {
           if (s_list_s[m] < 0) break;
-          const cpx<R> o = ndm_O<R>(k, e.N, e.Mh, e.Ma, sgp + m, CB, sbits[m], hilb, e.split);
+          const cpx<R> o = ndm_O_train<R>(e, k, sgp + m, CB, sbits[m], hilb);
           const cpx<R> b = sbeta[m];
           acc[q].x += (double)(b.x * o.x - b.y * o.y);
           acc[q].y += (double)(b.x * o.y + b.y * o.x);
@@ -601,6 +662,19 @@ cudaError_t launch_split_diagonal(const cpx<R>* p, int N, int M, cpx<R>* a, cpx<
   return cudaGetLastError();
 }
 
+template <typename R>
+cudaError_t launch_ndm_symm_bare(const R* symm, int N, int ah, int aa, int ns, const int* perms, R* bare,
+                                 cudaStream_t st) {
+  const int work = (ah > aa ? ah : aa) * ns * N + N;
+  ndm_symm_bare_kernel<R><<<(work + 255) / 256, 256, 0, st>>>(symm, N, ah, aa, ns, perms, bare);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ndm_symm_project(double* symm, int N, int ah, int aa, cudaStream_t st) {
+  ndm_symm_project_kernel<<<1, 64, 0, st>>>(symm, N, ah, aa);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ndm_diag_expand(const uint64_t* in, int n, int N, uint64_t* out, cudaStream_t st) {
   if (n < 1) return cudaSuccess;
   ndm_diag_expand_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, N, out);
@@ -661,3 +735,5 @@ template cudaError_t launch_split_effective<float>(const cpx<float>*, int, int, 
 template cudaError_t launch_split_effective<double>(const cpx<double>*, int, int, const NdmEffBufs<double>&, cudaStream_t);
 template cudaError_t launch_split_diagonal<float>(const cpx<float>*, int, int, cpx<float>*, cpx<float>*, cpx<float>*, cudaStream_t);
 template cudaError_t launch_split_diagonal<double>(const cpx<double>*, int, int, cpx<double>*, cpx<double>*, cpx<double>*, cudaStream_t);
+template cudaError_t launch_ndm_symm_bare<float>(const float*, int, int, int, int, const int*, float*, cudaStream_t);
+template cudaError_t launch_ndm_symm_bare<double>(const double*, int, int, int, int, const int*, double*, cudaStream_t);

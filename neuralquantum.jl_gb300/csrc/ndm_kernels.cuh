@@ -31,6 +31,13 @@ NQ_HD int ndm_n_params(int N, int Mh, int Ma) { return 2 * N + 2 * Mh + Ma + 2 *
 template <typename R> struct NdmEff {
   int N = 0, N2 = 0, Mh = 0, Ma = 0, U = 0, P = 0;
   int split = 0;               // RBMSplit: Mh = 0, Ma = U = M units of weight 1, RBM parameter layout
+  // NDMSymm: the network is the bare NDM (Mh, Ma, C, b, a) and the trainable
+  // parameters are the symmetric NDM's; O of trainable k is
+  // Σ_q sym_coef[q] O_bare(sym_idx[q]) over q in [sym_off[k], sym_off[k+1]).  P
+  // counts the trainable parameters.
+  const int* sym_off = nullptr;
+  const int* sym_idx = nullptr;
+  const double* sym_coef = nullptr;
   const cpx<R>* C = nullptr;   // [U x N2] column-major
   const cpx<R>* b = nullptr;   // [U]
   const cpx<R>* a = nullptr;   // [N2]
@@ -72,6 +79,13 @@ cudaError_t launch_split_effective(const cpx<R>* p, int N, int M, const NdmEffBu
 // RBMSplit diagonal sampler tables: a [N], b [M], W [M x N]
 template <typename R>
 cudaError_t launch_split_diagonal(const cpx<R>* p, int N, int M, cpx<R>* a, cpx<R>* b, cpx<R>* W, cudaStream_t st);
+// NDMSymm (MixedDensityMatrix/NDMSymm.jl:89-133): bare NDM parameters
+// (hidden Mh = ah ns, ancilla Ma = aa ns) from the symmetric ones; perms [ns x N]
+template <typename R>
+cudaError_t launch_ndm_symm_bare(const R* symm, int N, int ah, int aa, int ns, const int* perms, R* bare,
+                                 cudaStream_t st);
+// NDMSymm: the symmetric visible biases b_mu, b_la replaced by their means (FP64 master, in place)
+cudaError_t launch_ndm_symm_project(double* symm, int N, int ah, int aa, cudaStream_t st);
 // out[s] = (σ, σ) as 2N-site bits
 cudaError_t launch_ndm_diag_expand(const uint64_t* in, int n, int N, uint64_t* out, cudaStream_t st);
 

@@ -10,7 +10,7 @@ from . import _lib  # noqa: F401
 from .hilbert import HomogeneousSpin, HomogeneousFock, SuperOpSpace, physical, nsites  # noqa: F401
 from .operators import (LocalOperator, KLocalOperator, KLocalOperatorSum, KLocalLiouvillian,  # noqa: F401
                         sigmax, sigmay, sigmaz, sigmam, sigmap, liouvillian, op_table)
-from .networks import RBM, NDM, RBMSplit, af_logcosh, af_softplus, init_random_pars_  # noqa: F401
+from .networks import RBM, NDM, NDMSymm, RBMSplit, af_logcosh, af_softplus, init_random_pars_  # noqa: F401
 from .samplers import MetropolisSampler, ExactSampler, LocalRule, ExchangeRule, OperatorRule  # noqa: F401
 from .stats import Measurement  # noqa: F401
 from .iterative import (BatchedSampler, BatchedObsKetSampler, BatchedObsDMSampler, add_observable_,  # noqa: F401

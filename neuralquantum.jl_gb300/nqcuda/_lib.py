@@ -27,7 +27,7 @@ NQ_OK, NQ_ERR_ARG, NQ_ERR_CUDA, NQ_ERR_NOT_PD, NQ_ERR_TIMEOUT, NQ_ERR_NAN, NQ_ER
     NQ_ERR_UNSUPPORTED = range(8)
 STATUS_NAMES = ["NQ_OK", "NQ_ERR_ARG", "NQ_ERR_CUDA", "NQ_ERR_NOT_PD", "NQ_ERR_TIMEOUT",
                 "NQ_ERR_NAN", "NQ_ERR_STATE", "NQ_ERR_UNSUPPORTED"]
-NQ_NET_RBM, NQ_NET_NDM, NQ_NET_RBM_SPLIT = 0, 1, 2
+NQ_NET_RBM, NQ_NET_NDM, NQ_NET_RBM_SPLIT, NQ_NET_NDM_SYMM = 0, 1, 2, 3
 NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS = 0, 1
 NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3
@@ -50,7 +50,7 @@ class NqConfig(ctypes.Structure):
                 ("s_precision", ctypes.c_int32), ("quirks", ctypes.c_uint32),
                 ("sampler_lanes", ctypes.c_int32), ("sr_algorithm", ctypes.c_int32),
                 ("sampler_kind", ctypes.c_int32), ("rule", ctypes.c_int32), ("sampler_space", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("n_symm", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
 
 class NqMeasurement(ctypes.Structure):
@@ -85,6 +85,7 @@ EXPORTS = {
     "nq_set_operator": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable)]),
     "nq_set_exchange": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_int32)]),
     "nq_set_rule_operator": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable)]),
+    "nq_set_symmetry": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_int32)]),
     "nq_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]),
     "nq_set_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_logpsi": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),

@@ -5,7 +5,7 @@ import numpy as np
 
 from . import _lib
 from .hilbert import SuperOpSpace, physical
-from .networks import RBM, NDM, RBMSplit, af_logcosh
+from .networks import RBM, NDM, NDMSymm, RBMSplit, af_logcosh
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
@@ -19,6 +19,11 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
         cfg.network = _lib.NQ_NET_RBM
         cfg.n_hidden = net.M
         cfg.n_ancilla = 0
+    elif isinstance(net, NDMSymm):
+        cfg.network = _lib.NQ_NET_NDM_SYMM
+        cfg.n_hidden = net.Mh
+        cfg.n_ancilla = net.Ma
+        cfg.n_symm = net.n_symm
     elif isinstance(net, NDM):
         cfg.network = _lib.NQ_NET_NDM
         cfg.n_hidden = net.Mh
@@ -66,6 +71,10 @@ class Engine:
             st = L.nq_create(ctypes.byref(cfg), ctypes.byref(self.h))
             if st != _lib.NQ_OK:
                 raise _lib.NqError(st, "nq_create failed (see stderr)")
+            if isinstance(net, NDMSymm):
+                perms = np.ascontiguousarray(net.permutations, dtype=np.int32)
+                self._check(L.nq_set_symmetry(self.h, perms.shape[0],
+                                              perms.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
         else:
             self.h = ctypes.c_void_p(_handle)
         ph = physical(hilb)

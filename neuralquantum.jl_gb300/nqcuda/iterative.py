@@ -174,7 +174,7 @@ class BatchedObsDMSampler:
     def __init__(self, net, sampler, hilb_doubled, batch_sz=16, eval_precision=_lib.NQ_EVAL_F32,
                  reference_quirks=False):
         from .networks import NDM, RBMSplit
-        if not isinstance(net, (NDM, RBMSplit)):
+        if not isinstance(net, (NDM, RBMSplit)):             # NDMSymm is an NDM
             raise TypeError("BatchedObsDMSampler needs a density-matrix network (NDM, RBMSplit)")
         self.net = net
         self.sampler = sampler

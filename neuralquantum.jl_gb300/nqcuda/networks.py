@@ -116,6 +116,31 @@ class RBMSplit:
         return f"RBMSplit({self.dtype}, n={self.N}, α={self.M / self.N})"
 
 
+class NDMSymm(NDM):
+    """``NDMSymm(T, N, αh, αa, permutations, f=logℒ)`` (NDMSymm.jl:17-30): the
+    trainable parameters are those of a symmetric NDM with αh hidden and αa
+    ancilla features (fields as NDM); the network evaluated is the bare NDM
+    whose units are those features under every permutation (0-based site
+    lists).  The symmetric visible biases are kept at their means."""
+
+    def __init__(self, T, N, alpha_h, alpha_a, permutations, f=af_logcosh):
+        super().__init__(T, N, alpha_h / N, alpha_a / N, f)
+        perms = np.asarray(permutations, dtype=np.int64)
+        if perms.ndim != 2 or perms.shape[1] != self.N:
+            raise ValueError("permutations must be a list of site lists of length N")
+        for p in perms:
+            if sorted(p.tolist()) != list(range(self.N)):
+                raise ValueError("every permutation must be a permutation of the sites 0..N-1")
+        self.permutations = perms
+
+    @property
+    def n_symm(self):
+        return len(self.permutations)
+
+    def __repr__(self):
+        return f"NDMSymm({self.dtype}, n={self.N}, αh={self.Mh}, αa={self.Ma}, n_symm={self.n_symm})"
+
+
 def init_random_pars_(net, sigma=0.01, rng=None):
     """``init_random_pars!`` (src/utils/rng.jl:27-38): every weight is drawn
     from randn * sqrt(sigma); complex draws have variance 1/2 per part."""

@@ -9,6 +9,8 @@ Flat parameter order = functor field order, each array column-major
   u_la (bN x N)
 * RBMSplit (src/Networks/MixedDensityMatrix/RBMSplit.jl:3-10): ar (N),
   ac (N), b (aN), Wr (aN x N), Wc (aN x N)
+* NDMSymm (src/Networks/MixedDensityMatrix/NDMSymm.jl:3-40): the trainable
+  vector is the symmetric NDM's (NDM order with ah hidden, aa ancilla)
 
 Activations follow src/Networks/activation.jl:5-45; the derivative used by the
 networks is ``fwd_der(f, x)`` (tanh for logcosh, sigmoid for softplus).
@@ -240,6 +242,90 @@ class RBMSplit:
     def log_prob(self, sr, sc):
         """2 Re logρ on doubled states (base_batched_networks.jl:255-258)."""
         return 2.0 * np.real(self.logpsi(sr, sc))
+
+
+class NDMSymm:
+    """NDMSymm.jl: a symmetric NDM ``sym`` (ah hidden, aa ancilla features)
+    and the bare NDM with ah n_symm / aa n_symm units built from it by
+    ``set_bare_params!`` (:89-133: visible biases replaced by their mean,
+    hidden and ancilla biases repeated, bare unit j + f n_symm carrying the
+    symmetric weights (f, i) on site perms[j][i]).  logρ is the bare NDM's;
+    ∇logρ is the bare gradient mapped by ``construct_∇matrices`` (:135-180).
+    ``perms`` are 0-based."""
+
+    def __init__(self, n, ah, aa, perms, activation=LOGCOSH):
+        self.N, self.ah, self.aa = int(n), int(ah), int(aa)
+        self.perms = np.asarray(perms, dtype=np.int64)
+        self.ns = len(self.perms)
+        self.activation = activation
+        self.sym = NDM(n, ah / n, aa / n, activation)
+        self.bare = NDM(n, ah * self.ns / n, aa * self.ns / n, activation)
+        self._set_bare()
+
+    @property
+    def n_params(self):
+        return self.sym.n_params
+
+    def flat(self):
+        return self.sym.flat()
+
+    def set_flat(self, v):
+        self.sym.set_flat(v)
+        self._set_bare()
+
+    def _set_bare(self):
+        s, b, ns = self.sym, self.bare, self.ns
+        s.b_mu = np.full_like(s.b_mu, s.b_mu.mean())
+        s.b_la = np.full_like(s.b_la, s.b_la.mean())
+        b.b_mu = s.b_mu.copy()
+        b.b_la = s.b_la.copy()
+        b.h_mu = np.repeat(s.h_mu, ns)
+        b.h_la = np.repeat(s.h_la, ns)
+        b.d_la = np.repeat(s.d_la, ns)
+        for f in range(self.ah):
+            for j, perm in enumerate(self.perms):
+                for i, ip in enumerate(perm):
+                    b.w_mu[j + f * ns, ip] = s.w_mu[f, i]
+                    b.w_la[j + f * ns, ip] = s.w_la[f, i]
+        for f in range(self.aa):
+            for j, perm in enumerate(self.perms):
+                for i, ip in enumerate(perm):
+                    b.u_mu[j + f * ns, ip] = s.u_mu[f, i]
+                    b.u_la[j + f * ns, ip] = s.u_la[f, i]
+
+    def grad_matrix(self):
+        """(P_sym, P_bare) matrix of construct_∇matrices in the flat orders."""
+        s, b, ns, N = self.sym, self.bare, self.ns, self.N
+        def offs(net):
+            o, out = 0, {}
+            for f in NDM.FIELDS:
+                out[f] = o
+                o += int(np.prod(net.shapes[f]))
+            return out
+        so, bo = offs(s), offs(b)
+        G = np.zeros((s.n_params, b.n_params))
+        for f in ("b_mu", "b_la"):
+            G[so[f]:so[f] + N, bo[f]:bo[f] + N] = 1.0 / N
+        for f, m in (("h_mu", self.ah), ("h_la", self.ah), ("d_la", self.aa)):
+            for k in range(m):
+                G[so[f] + k, bo[f] + k * ns:bo[f] + (k + 1) * ns] = 1.0
+        for f, m, mb in (("w_mu", self.ah, b.Mh), ("w_la", self.ah, b.Mh),
+                         ("u_mu", self.aa, b.Ma), ("u_la", self.aa, b.Ma)):
+            for fe in range(m):
+                for j, perm in enumerate(self.perms):
+                    for i, ip in enumerate(perm):
+                        G[so[f] + fe + m * i, bo[f] + (j + fe * ns) + mb * ip] = 1.0
+        return G
+
+    def logpsi(self, sr, sc):
+        return self.bare.logpsi(sr, sc)
+
+    def logpsi_and_grad(self, sr, sc):
+        out, g = self.bare.logpsi_and_grad(sr, sc)
+        return out, g @ self.grad_matrix().T
+
+    def log_prob(self, sr, sc):
+        return self.bare.log_prob(sr, sc)
 
 
 def init_random_pars(net, rng, sigma=1e-4):

@@ -116,6 +116,45 @@ def test_rbmsplit_is_the_rbm_of_the_doubled_sites():
     np.testing.assert_allclose(sp.logpsi_and_grad(sr, sc)[1], r.logpsi_and_grad(v)[1], rtol=0, atol=1e-13)
 
 
+def test_ndm_symm_restatement():
+    """NDMSymm (NDMSymm.jl): with the identity as the only permutation the
+    bare NDM is the symmetric one (up to the averaged visible biases); the
+    bare logρ is invariant under relabelling the sites by a permutation of
+    the group when the group is closed (translations of a ring), and the
+    symmetrised gradient equals finite differences of logρ in the symmetric
+    parameters along directions that keep the visible biases uniform."""
+    rng = np.random.default_rng(14)
+    N = 4
+    trans = [[(i + t) % N for i in range(N)] for t in range(N)]
+    ns = nw.NDMSymm(N, 2, 1, trans, nw.LOGCOSH)
+    v = rng.standard_normal(ns.n_params) * 0.3
+    ns.set_flat(v)
+    assert ns.bare.Mh == 2 * N and ns.bare.Ma == N
+    sr = rng.choice([0.0, 1.0], size=(5, N)); sc = rng.choice([0.0, 1.0], size=(5, N))
+    shift = [(i + 1) % N for i in range(N)]
+    np.testing.assert_allclose(ns.logpsi(sr, sc), ns.logpsi(sr[:, shift], sc[:, shift]), atol=1e-12)
+    one = nw.NDMSymm(N, 2, 1, [list(range(N))], nw.LOGCOSH)
+    one.set_flat(v)
+    np.testing.assert_allclose(one.bare.flat(), one.sym.flat(), atol=0)
+    _, g = ns.logpsi_and_grad(sr, sc)
+    p0 = ns.flat()
+    eps = 1e-6
+    for k in range(p0.size):
+        d = np.zeros_like(p0)
+        d[k] = 1.0
+        o = 0
+        for f in nw.NDM.FIELDS:
+            n = int(np.prod(ns.sym.shapes[f]))
+            if f in ("b_mu", "b_la") and o <= k < o + n:
+                d[o:o + n] = 1.0 / N          # a uniform visible-bias direction
+            o += n
+        ns.set_flat(p0 + eps * d); lp = ns.logpsi(sr, sc)
+        ns.set_flat(p0 - eps * d); lm = ns.logpsi(sr, sc)
+        fd = (lp - lm) / (2 * eps)
+        assert np.max(np.abs(fd - g @ d)) < 1e-7, k
+    ns.set_flat(p0)
+
+
 def test_ndm_parameter_count():
     n = nw.NDM(6, 1, 1)
     assert n.n_params == 2 * 6 + 2 * 6 + 6 + 2 * 36 + 2 * 36
