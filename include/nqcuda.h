@@ -76,8 +76,25 @@ typedef enum {
  * symmetric NDM's (real, NDM order, sizes n_hidden and n_ancilla).  The
  * density matrices sample the doubled space (σ, η) and take the Liouvillian
  * cost function. */
-typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_SYMM = 3 } nq_network;
-typedef enum { NQ_ACT_LOGCOSH = 0, NQ_ACT_SOFTPLUS = 1 } nq_activation;
+typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_SYMM = 3, NQ_NET_CHAIN = 4 } nq_network;
+
+/* Layers of a feed-forward ket, PureStateAnsatz(Chain(layers...), N)
+ * (src/Networks/Chains/Chain.jl, Layers/Dense.jl, Layers/WeightedSum.jl,
+ * Layers/sum.jl).  NQ_LAYER_DENSE: y = f(W x + b), W n_out x n_in, f an
+ * nq_activation; NQ_LAYER_WSUM: logψ = Σ_i c_i x_i (n_in weights);
+ * NQ_LAYER_SUM: logψ = Σ_i x_i (sum_autobatch).  A chain is 1..7 Dense
+ * layers (the first with n_in = n_sites, widths <= 256) closed by one WSUM or
+ * SUM.  Complex parameters in the functor order: per Dense layer W
+ * (column-major) then b, then c. */
+typedef enum { NQ_LAYER_DENSE = 0, NQ_LAYER_WSUM = 1, NQ_LAYER_SUM = 2 } nq_layer_kind;
+typedef struct {
+  int32_t kind;            /* nq_layer_kind */
+  int32_t n_in;
+  int32_t n_out;           /* Dense only */
+  int32_t activation;      /* Dense only: nq_activation */
+} nq_layer;
+/* NQ_ACT_IDENTITY: Dense layers of a chain only (fwd_der(identity) = 1). */
+typedef enum { NQ_ACT_LOGCOSH = 0, NQ_ACT_SOFTPLUS = 1, NQ_ACT_IDENTITY = 2 } nq_activation;
 typedef enum { NQ_HILB_SPIN = 0, NQ_HILB_FOCK = 1 } nq_hilbert;
 typedef enum { NQ_DTYPE_C64 = 0, NQ_DTYPE_C128 = 1, NQ_DTYPE_F32 = 2, NQ_DTYPE_F64 = 3 } nq_dtype;
 
@@ -214,6 +231,10 @@ typedef struct nq_handle nq_handle;
 const char* nq_version(void);
 int32_t nq_abi_version(void);
 nq_status nq_create(const nq_config* cfg, nq_handle** out);
+/* A handle for PureStateAnsatz(Chain(layers...)): cfg->network =
+ * NQ_NET_CHAIN (n_hidden, n_ancilla and activation are not used), local-flip
+ * Metropolis sampler, direct SR with NQ_S_F32 / NQ_S_TF32 / NQ_S_TF32X3. */
+nq_status nq_create_chain(const nq_config* cfg, int32_t n_layers, const nq_layer* layers, nq_handle** out);
 void nq_destroy(nq_handle* h);
 nq_status nq_last_error(const nq_handle* h, char* buf, size_t len);
 int64_t nq_n_params(const nq_handle* h);

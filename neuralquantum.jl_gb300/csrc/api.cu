@@ -53,6 +53,10 @@ nq_status ndm_refresh(nq_handle* h) {
 
 // refresh FP32 copies and the per-flip tables after a parameter change
 nq_status refresh_params(nq_handle* h) {
+  if (h->chain) {
+    if (!h->f64) CKL(launch_master_to_f32(h->d_master, 2L * h->P, h->d_p32, h->st));
+    return NQ_OK;
+  }
   if (h->ndm) {
     if (h->symm) CKL(launch_ndm_symm_project(h->d_master, h->N, h->sym_h, h->sym_a, h->st));
     if (!h->f64) CKL(launch_master_to_f32(h->d_master, (h->complex_params ? 2L : 1L) * h->P, h->d_p32, h->st));
@@ -93,7 +97,7 @@ static std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g
 // times and the fastest of the last three counts.  Smaller blocks spread the
 // chains more evenly over the SMs when there are few of them.
 nq_status ensure_tuned(nq_handle* h) {
-  if (h->exact || (h->sampler_lanes && h->sampler_block)) return NQ_OK;
+  if (h->exact || h->chain || (h->sampler_lanes && h->sampler_block)) return NQ_OK;
   if (h->rule == NQ_RULE_EXCHANGE && h->n_exch == 0)
     return fail(h, NQ_ERR_STATE, "exchange rule: no couplings (nq_set_exchange)");
   if (h->rule == NQ_RULE_OPERATOR && h->n_exch == 0)
@@ -180,6 +184,9 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
     if (ms != NQ_OK) return ms;
   }
   if (mixed) {
+  } else if (h->chain) {
+    if (h->f64) CKL(launch_chain_sampler<double>(chain_dev<double>(h), run, h->st));
+    else CKL(launch_chain_sampler<float>(chain_dev<float>(h), run, h->st));
   } else if (h->exact) {
     if (h->f64) CKL(launch_exact_sampler<double>(rbm_dev<double>(h), run, h->d_exact, h->st));
     else CKL(launch_exact_sampler<float>(rbm_dev<float>(h), run, h->d_exact, h->st));
@@ -209,6 +216,16 @@ nq_status ndm_stage_eval(nq_handle* h) {
 
 nq_status stage_eval(nq_handle* h) {
   if (h->ndm) return h->f64 ? ndm_stage_eval<double>(h) : ndm_stage_eval<float>(h);
+  if (h->chain) {
+    // logψ, E_loc and the uncentred O rows of X (centred after the force)
+    if (h->f64)
+      CKL(launch_chain_eval<double>(chain_dev<double>(h), h->d_samples, h->Ns, &h->op, (cpx<double>*)h->d_logpsi,
+                                    (cpx<double>*)h->d_eloc, h->d_X, h->Ns_pad, nullptr, h->st));
+    else
+      CKL(launch_chain_eval<float>(chain_dev<float>(h), h->d_samples, h->Ns, &h->op, (cpx<float>*)h->d_logpsi,
+                                   (cpx<float>*)h->d_eloc, h->d_X, h->Ns_pad, nullptr, h->st));
+    return NQ_OK;
+  }
   const DevOp* op = h->has_op ? &h->op : nullptr;
   if (h->f64) {
     CKL(launch_rbm_eval<double>(rbm_dev<double>(h), h->d_samples, h->Ns, op, (cpx<double>*)h->d_logpsi,
@@ -243,6 +260,22 @@ nq_status ndm_stage_force(nq_handle* h) {
 
 nq_status stage_force(nq_handle* h) {
   if (h->ndm) return h->f64 ? ndm_stage_force<double>(h) : ndm_stage_force<float>(h);
+  if (h->chain) {
+    const int sp = h->cfg.s_precision;
+    const bool tc = sp == NQ_S_TF32 || sp == NQ_S_TF32X3;
+    if (h->f64) {
+      CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
+      CKL(launch_chain_force<double>(h->d_X, h->Ns_pad, h->P, h->Ns, (const cpx<double>*)h->d_eloc, h->d_stats,
+                                     h->fb.force, h->st));
+    } else {
+      CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
+      CKL(launch_chain_force<float>(h->d_X, h->Ns_pad, h->P, h->Ns, (const cpx<float>*)h->d_eloc, h->d_stats,
+                                    h->fb.force, h->st));
+    }
+    CKL(launch_x_center(h->d_X, sp == NQ_S_TF32X3 ? h->d_Xlo : nullptr, 2 * h->P, h->Ns_pad, h->Ns, h->fb.meanO,
+                        tc ? 1 : 0, h->st));
+    return NQ_OK;
+  }
   if (h->f64) {
     CKL(launch_rbm_force<double>(rbm_dev<double>(h), h->d_samples, h->Ns, (cpx<double>*)h->d_g,
                                  (cpx<double>*)h->d_eloc, h->fb, h->st));
@@ -257,7 +290,7 @@ nq_status stage_force(nq_handle* h) {
 
 nq_status stage_S(nq_handle* h) {
   if (h->cg) return NQ_OK;          // matrix-free SR: S is never formed
-  if (h->ndm) {
+  if (h->ndm || h->chain) {
     const int sp = h->cfg.s_precision;
     if (!h->capturing) CK(cudaEventRecord(h->kev[2], h->st));
     if (sp == NQ_S_TF32 || sp == NQ_S_TF32X3) {
@@ -442,7 +475,47 @@ extern "C" {
 const char* nq_version(void) { return "libnqcuda 0.1.0 (sm_103a)"; }
 int32_t nq_abi_version(void) { return NQCUDA_ABI_VERSION; }
 
-nq_status nq_create(const nq_config* cfg, nq_handle** out) {
+}  // extern "C"
+
+namespace {
+
+// validated layer list of a chain into spec; "" or the reason it is refused
+const char* chain_layers(const nq_config& c, int n_layers, const nq_layer* layers, ChainDev<float>* spec) {
+  if (!layers || n_layers < 2 || n_layers > 8) return "a chain has 2..8 layers";
+  int off = 0, n_theta = 0, max_w = 0, prev = c.n_sites;
+  for (int l = 0; l < n_layers; ++l) {
+    const nq_layer& y = layers[l];
+    ChainLayerDev d;
+    d.kind = y.kind; d.in = y.n_in; d.out = y.n_out; d.act = y.activation;
+    if (y.n_in != prev) return "layer input width differs from the previous output";
+    const bool closing = l == n_layers - 1;
+    if (closing != (y.kind != NQ_LAYER_DENSE)) return "Dense layers, then exactly one closing WSum or sum";
+    if (y.kind == NQ_LAYER_DENSE) {
+      if (y.n_out < 1 || y.n_out > 256) return "Dense widths must be in 1..256";
+      if (y.activation != NQ_ACT_LOGCOSH && y.activation != NQ_ACT_SOFTPLUS && y.activation != NQ_ACT_IDENTITY)
+        return "unknown Dense activation";
+      d.w_off = off; off += y.n_out * y.n_in;
+      d.b_off = off; off += y.n_out;
+      n_theta += y.n_out;
+      max_w = std::max(max_w, y.n_out);
+      prev = y.n_out;
+    } else if (y.kind == NQ_LAYER_WSUM) {
+      d.w_off = off; off += y.n_in;
+      d.out = 1;
+    } else if (y.kind == NQ_LAYER_SUM) {
+      d.out = 1;
+    } else {
+      return "unknown layer kind";
+    }
+    spec->L[l] = d;
+  }
+  spec->N = c.n_sites; spec->hilb = c.hilbert; spec->n_layers = n_layers; spec->P = off;
+  spec->n_theta = n_theta; spec->max_w = max_w;
+  if (off > 256 * 24) return "too many chain parameters (max 6144)";
+  return "";
+}
+
+nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers, nq_handle** out) {
   if (!cfg || !out) return NQ_ERR_ARG;
   *out = nullptr;
   nq_handle* h = new nq_handle();
@@ -453,15 +526,24 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     delete h;
     return NQ_ERR_ARG;
   };
+  if (c.network == NQ_NET_CHAIN) {
+    if (!layers) return bad("chains are created with nq_create_chain");
+    if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
+    const char* why = chain_layers(c, n_layers, layers, &h->chain_spec);
+    if (*why) return bad(why);
+    if (c.sampler_kind != NQ_SAMPLER_METROPOLIS || c.rule != NQ_RULE_LOCAL || c.sampler_space != NQ_SPACE_NETWORK)
+      return bad("chains sample with the local-flip Metropolis rule");
+    h->chain = true;
+  }
   if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM && c.network != NQ_NET_RBM_SPLIT &&
-      c.network != NQ_NET_NDM_SYMM)
+      c.network != NQ_NET_NDM_SYMM && c.network != NQ_NET_CHAIN)
     return bad("unknown network");
   const bool matrix_net = c.network == NQ_NET_NDM || c.network == NQ_NET_RBM_SPLIT || c.network == NQ_NET_NDM_SYMM;
   if (c.network == NQ_NET_NDM_SYMM && (c.n_symm < 1 || c.n_symm > 64)) return bad("NDMSymm: n_symm must be in 1..64");
-  if (c.activation != NQ_ACT_LOGCOSH && c.activation != NQ_ACT_SOFTPLUS) return bad("unknown activation");
+  if (!h->chain && c.activation != NQ_ACT_LOGCOSH && c.activation != NQ_ACT_SOFTPLUS) return bad("unknown activation");
   if (c.hilbert != NQ_HILB_SPIN && c.hilbert != NQ_HILB_FOCK) return bad("unknown hilbert space");
   if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
-  if (c.n_hidden < 1 || c.n_hidden > 256) return bad("n_hidden must be in 1..256");
+  if (!h->chain && (c.n_hidden < 1 || c.n_hidden > 256)) return bad("n_hidden must be in 1..256");
   if (c.n_chains < 2 || c.chain_length < 1 || c.burn < 0 || c.passes < 1) return bad("bad sampler sizes");
   if (c.eval_precision != NQ_EVAL_F32 && c.eval_precision != NQ_EVAL_F64 &&
       !((c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3) &&
@@ -521,6 +603,10 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     if (h->N2 > 64) return bad("the NDM supports n_sites <= 32 (2N doubled sites)");
     if (h->Ms > 320) return bad("2*n_hidden + n_ancilla must be <= 320");
     if (h->P > 256 * 24) return bad("too many density-matrix parameters (max 6144)");
+  } else if (h->chain) {
+    h->nst = h->N;
+    h->M = h->chain_spec.L[0].out;
+    h->P = h->chain_spec.P;
   } else {
     h->nst = h->N;
     h->P = h->N + h->M + h->M * h->N;
@@ -537,9 +623,9 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   h->f64 = c.eval_precision == NQ_EVAL_F64;
   h->tc_theta = c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3;
   h->theta_terms = c.eval_precision == NQ_EVAL_TC_BF16X3 ? 3 : 2;
-  h->complex_params = !h->ndm || h->split;
+  h->complex_params = !h->ndm || h->split;      // RBM, RBMSplit and chains
   const int sampler_M = h->diag ? h->Md : (h->ndm ? h->Ms : h->M), sampler_N = h->nst;
-  if (c.sampler_lanes != 0) {
+  if (c.sampler_lanes != 0 && !h->chain) {
     int cand[4];
     const int nc = rbm_sampler_valid_lanes(sampler_N, sampler_M, h->f64 ? 16 : 8, cand, 4);
     bool ok = false;
@@ -578,10 +664,10 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   step(dalloc(&h->d_accepted, 1), "accepted");
   step(dalloc(&h->d_call, 1), "call");
   step(cudaMalloc(&h->d_logpsi, (size_t)h->Ns * csz), "logpsi");
-  if (!h->ndm) step(cudaMalloc(&h->d_g, (size_t)h->Ns * h->M * csz), "g");
+  if (!h->ndm && !h->chain) step(cudaMalloc(&h->d_g, (size_t)h->Ns * h->M * csz), "g");
   step(cudaMalloc(&h->d_eloc, (size_t)h->Ns * csz), "eloc");
-  if (h->f64 && !h->ndm) step(dalloc(&h->d_g32, (size_t)h->Ns * h->M), "g32");
-  h->force_nblk = h->ndm ? 1 : rbm_force_nblocks(h->Ns, h->N, h->M, (int)csz);
+  if (h->f64 && !h->ndm && !h->chain) step(dalloc(&h->d_g32, (size_t)h->Ns * h->M), "g32");
+  h->force_nblk = (h->ndm || h->chain) ? 1 : rbm_force_nblocks(h->Ns, h->N, h->M, (int)csz);
   step(dalloc(&h->fb.partial, (size_t)h->force_nblk * 4 * P), "force partial");
   step(dalloc(&h->fb.partialE, 2 * (size_t)h->force_nblk), "force partialE");
   step(dalloc(&h->fb.meanO, 2 * (size_t)P), "meanO");
@@ -642,7 +728,7 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
     step(dalloc(&h->d_Gpart, gram_tc_partial_elems(rows, h->Ns_pad, bf16)), "G partial");
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad / (bf16 ? 2 : 1)), "X");     // BF16 X: half the bytes
     if (c.s_precision == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
-  } else if (h->ndm) {
+  } else if (h->ndm || h->chain) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
   }
@@ -681,6 +767,17 @@ nq_status nq_create(const nq_config* cfg, nq_handle** out) {
   }
   *out = h;
   return NQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nq_status nq_create(const nq_config* cfg, nq_handle** out) { return create_impl(cfg, 0, nullptr, out); }
+
+nq_status nq_create_chain(const nq_config* cfg, int32_t n_layers, const nq_layer* layers, nq_handle** out) {
+  if (!cfg || cfg->network != NQ_NET_CHAIN) return NQ_ERR_ARG;
+  return create_impl(cfg, n_layers, layers, out);
 }
 
 void nq_destroy(nq_handle* h) {
@@ -1042,7 +1139,17 @@ nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* st
     return cleanup(fail(h, NQ_ERR_CUDA, "observable buffers"));
   cudaError_t e;
   ++h->launches;
-  if (h->diag) {
+  if (h->chain) {
+    if (h->f64) {
+      e = launch_chain_eval<double>(chain_dev<double>(h), h->d_samples, h->Ns, &d, (cpx<double>*)d_lp,
+                                    (cpx<double>*)d_loc, nullptr, 0, nullptr, h->st);
+      if (e == cudaSuccess) e = launch_stats<double>((cpx<double>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
+    } else {
+      e = launch_chain_eval<float>(chain_dev<float>(h), h->d_samples, h->Ns, &d, (cpx<float>*)d_lp,
+                                   (cpx<float>*)d_loc, nullptr, 0, nullptr, h->st);
+      if (e == cudaSuccess) e = launch_stats<float>((cpx<float>*)d_loc, h->B, h->L, 0, d_cs, d_st, h->st);
+    }
+  } else if (h->diag) {
     if (h->f64) {
       e = launch_ndm_diag_obs<double>(ndm_eff<double>(h), h->act, d, h->d_samples, h->Ns, h->hilb,
                                       (cpx<double>*)d_lp, (cpx<double>*)d_loc, h->st);
@@ -1142,12 +1249,18 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
   CK(cudaMalloc(&d_v, (size_t)n * h->nst));
   CK(cudaMalloc(&d_bits, (size_t)n * sizeof(uint64_t)));
   CK(cudaMalloc(&d_lp, (size_t)n * csz));
-  if (!h->ndm) CK(cudaMalloc(&d_g, (size_t)n * h->M * csz));
+  if (!h->ndm && !h->chain) CK(cudaMalloc(&d_g, (size_t)n * h->M * csz));
   CK(cudaMemcpyAsync(d_v, sigma, (size_t)n * h->nst, cudaMemcpyHostToDevice, h->st));
   ++h->launches;
   CK(launch_pack_int8(d_v, h->nst, n, h->hilb, d_bits, h->st));
   if (h->diag) CKL(launch_ndm_diag_expand(d_bits, (int)n, h->N, d_bits, h->st));   // logρ(σ,σ)
-  if (h->ndm) {
+  if (h->chain) {
+    if (grad) CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
+    if (h->f64) CKL(launch_chain_eval<double>(chain_dev<double>(h), d_bits, (int)n, nullptr, (cpx<double>*)d_lp,
+                                              nullptr, nullptr, 0, d_out, h->st));
+    else CKL(launch_chain_eval<float>(chain_dev<float>(h), d_bits, (int)n, nullptr, (cpx<float>*)d_lp, nullptr,
+                                      nullptr, 0, d_out, h->st));
+  } else if (h->ndm) {
     if (grad) CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
     if (h->f64) CKL(launch_ndm_eval<double>(ndm_eff<double>(h), h->act, d_bits, (int)n, h->hilb, (cpx<double>*)d_lp, nullptr, 0, d_out, h->st));
     else CKL(launch_ndm_eval<float>(ndm_eff<float>(h), h->act, d_bits, (int)n, h->hilb, (cpx<float>*)d_lp, nullptr, 0, d_out, h->st));
@@ -1166,13 +1279,13 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
     CK(cudaStreamSynchronize(h->st));
     for (int64_t i = 0; i < 2 * n; ++i) lp[i] = f[i];
   }
-  if (grad && !h->ndm) {
+  if (grad && !h->ndm && !h->chain) {
     CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
     if (h->f64) CKL(launch_rbm_grad_matrix<double>(d_bits, (int)n, h->N, h->M, h->hilb, (cpx<double>*)d_g, d_out, h->st));
     else CKL(launch_rbm_grad_matrix<float>(d_bits, (int)n, h->N, h->M, h->hilb, (cpx<float>*)d_g, d_out, h->st));
     CK(cudaMemcpyAsync(grad, d_out, (size_t)2 * h->P * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   }
-  if (grad && h->ndm) CK(cudaMemcpyAsync(grad, d_out, (size_t)2 * h->P * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (grad && (h->ndm || h->chain)) CK(cudaMemcpyAsync(grad, d_out, (size_t)2 * h->P * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   memcpy(out, lp.data(), 2 * n * sizeof(double));
   cudaFree(d_v); cudaFree(d_bits); cudaFree(d_lp); cudaFree(d_g);

@@ -24,6 +24,8 @@ struct nq_handle {
   int n_record = 0, write_last = 0;
   bool doubled = false, complex_params = true, f64 = false, ndm = false;
   int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
+  bool chain = false;              // feed-forward ket chain (chain_dev)
+  ChainDev<float> chain_spec;      // its layers (the parameter pointer is set per precision)
   bool split = false;              // RBMSplit on the doubled-space path (complex parameters)
   bool symm = false;               // NDMSymm: trainable symmetric NDM, evaluated as its bare NDM
   bool sym_ready = false;          // NDMSymm permutations set (nq_set_symmetry)
@@ -201,6 +203,17 @@ RbmDev<R> rbm_sampler_dev(nq_handle* h) {
     d.rare = reinterpret_cast<const R*>(h->d_xare);
   }
   return d;
+}
+
+// the chain's layers over the handle's current parameters (master or FP32 copy)
+template <typename R>
+ChainDev<R> chain_dev(nq_handle* h) {
+  ChainDev<R> c;
+  const ChainDev<float>& s = h->chain_spec;
+  c.N = s.N; c.hilb = s.hilb; c.n_layers = s.n_layers; c.P = s.P; c.n_theta = s.n_theta; c.max_w = s.max_w;
+  for (int l = 0; l < 8; ++l) c.L[l] = s.L[l];
+  c.p = h->f64 ? reinterpret_cast<const cpx<R>*>(h->d_master) : reinterpret_cast<const cpx<R>*>(h->d_p32);
+  return c;
 }
 
 // learned-proposal hooks used by the stage sequence (proposal.cu)

@@ -75,7 +75,7 @@ template <typename R> NQ_D cpx<R> csinhc(cpx<R> z) {
 // Activations.  logcosh = logℒ2 (activation.jl:9-13), derivative tanh;
 // softplus = logℒ = log1p(exp(x)) (activation.jl:20), derivative sigmoid.
 // ---------------------------------------------------------------------------
-enum { ACT_LOGCOSH = 0, ACT_SOFTPLUS = 1 };
+enum { ACT_LOGCOSH = 0, ACT_SOFTPLUS = 1, ACT_IDENTITY = 2 };   // identity: Dense layers of a chain only
 
 template <typename R> NQ_D R logcosh_real(R x) {
   R ax = r_abs(x);

@@ -108,6 +108,32 @@ cudaError_t launch_rbm_class_tables(const RbmDev<float>& net, const OpMovesDev& 
 // shared memory of the OperatorRule sampler with G lanes per chain (0 if it does not fit)
 size_t oprule_sampler_smem(const OpMovesDev& m, int M, int G);
 
+// Feed-forward ket chains (Chain.jl, Dense.jl, WeightedSum.jl, sum.jl): Dense
+// layers then one closing sum_autobatch or WSum; offsets into the complex
+// parameter vector p (functor order).
+enum { LAYER_DENSE = 0, LAYER_WSUM = 1, LAYER_SUM = 2 };
+struct ChainLayerDev {
+  int kind = 0, in = 0, out = 0, act = 0, w_off = 0, b_off = 0;
+};
+template <typename R> struct ChainDev {
+  int N = 0, hilb = 0, n_layers = 0, P = 0;
+  int n_theta = 0;             // Σ out over the Dense layers (stored pre-activations)
+  int max_w = 0;               // widest Dense output
+  ChainLayerDev L[8];
+  const cpx<R>* p = nullptr;
+};
+// logψ, E_loc (op nullable) and O into X (uncentred FP32 rows 2k, 2k+1) and/or
+// Oout (P x n complex FP64)
+template <typename R>
+cudaError_t launch_chain_eval(const ChainDev<R>& c, const uint64_t* samples, int n, const DevOp* op, cpx<R>* logpsi,
+                              cpx<R>* eloc, float* X, int ldx, double* Oout, cudaStream_t st);
+// F = E O_c† / Ns from the uncentred rows of X and the mean of E in stats[0..1]
+template <typename R>
+cudaError_t launch_chain_force(const float* X, int ldx, int P, int ns, const cpx<R>* E, const double* stats,
+                               double* force, cudaStream_t st);
+template <typename R>
+cudaError_t launch_chain_sampler(const ChainDev<R>& c, const SamplerRun& run, cudaStream_t st);
+
 // Exact sampler (Exact.jl): all 2^N configurations of the sampler's space
 // (N <= 26), FP64 CDF, inverse-CDF draws into run.samples (n_record draws per
 // chain, plus one into slot 0 with write_last_at_end).  work:

@@ -167,7 +167,7 @@ extern "C" {
 
 nq_status nq_proposal_init(nq_handle* h, int32_t hidden, double p_ar, uint64_t seed) {
   if (!h) return NQ_ERR_ARG;
-  if (h->ndm || h->f64) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: FP32 RBM handles only");
+  if (h->ndm || h->f64 || h->chain) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: FP32 RBM handles only");
   if (h->exact) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: the handle samples exactly (no chains)");
   if (h->rule != NQ_RULE_LOCAL) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: mixes with LocalRule moves only");
   if (hidden != 128) return fail(h, NQ_ERR_UNSUPPORTED, "learned proposal: hidden must be 128 (got %d)", hidden);

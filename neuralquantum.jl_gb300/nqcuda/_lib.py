@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
            "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu",
-           "srcg.cu", "exact.cu", "sampler_exch.cu", "sampler_oprule.cu"]
+           "srcg.cu", "exact.cu", "sampler_exch.cu", "sampler_oprule.cu", "chain.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -27,8 +27,9 @@ NQ_OK, NQ_ERR_ARG, NQ_ERR_CUDA, NQ_ERR_NOT_PD, NQ_ERR_TIMEOUT, NQ_ERR_NAN, NQ_ER
     NQ_ERR_UNSUPPORTED = range(8)
 STATUS_NAMES = ["NQ_OK", "NQ_ERR_ARG", "NQ_ERR_CUDA", "NQ_ERR_NOT_PD", "NQ_ERR_TIMEOUT",
                 "NQ_ERR_NAN", "NQ_ERR_STATE", "NQ_ERR_UNSUPPORTED"]
-NQ_NET_RBM, NQ_NET_NDM, NQ_NET_RBM_SPLIT, NQ_NET_NDM_SYMM = 0, 1, 2, 3
-NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS = 0, 1
+NQ_NET_RBM, NQ_NET_NDM, NQ_NET_RBM_SPLIT, NQ_NET_NDM_SYMM, NQ_NET_CHAIN = 0, 1, 2, 3, 4
+NQ_LAYER_DENSE, NQ_LAYER_WSUM, NQ_LAYER_SUM = 0, 1, 2
+NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS, NQ_ACT_IDENTITY = 0, 1, 2
 NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3
 NQ_EVAL_F32, NQ_EVAL_TC_BF16X2, NQ_EVAL_F64, NQ_EVAL_TC_BF16X3 = 0, 1, 2, 3
@@ -51,6 +52,11 @@ class NqConfig(ctypes.Structure):
                 ("sampler_lanes", ctypes.c_int32), ("sr_algorithm", ctypes.c_int32),
                 ("sampler_kind", ctypes.c_int32), ("rule", ctypes.c_int32), ("sampler_space", ctypes.c_int32),
                 ("n_symm", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+
+
+class NqLayer(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("n_in", ctypes.c_int32), ("n_out", ctypes.c_int32),
+                ("activation", ctypes.c_int32)]
 
 
 class NqMeasurement(ctypes.Structure):
@@ -86,6 +92,7 @@ EXPORTS = {
     "nq_set_exchange": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_int32)]),
     "nq_set_rule_operator": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable)]),
     "nq_set_symmetry": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _P(ctypes.c_int32)]),
+    "nq_create_chain": (ctypes.c_int, [_P(NqConfig), ctypes.c_int32, _P(NqLayer), _P(ctypes.c_void_p)]),
     "nq_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]),
     "nq_set_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_logpsi": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),

@@ -5,7 +5,7 @@ import numpy as np
 
 from . import _lib
 from .hilbert import SuperOpSpace, physical
-from .networks import RBM, NDM, NDMSymm, RBMSplit, af_logcosh
+from .networks import RBM, NDM, NDMSymm, RBMSplit, PureStateAnsatz, Dense, WSum, af_logcosh, af_softplus
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
@@ -28,13 +28,18 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
         cfg.network = _lib.NQ_NET_NDM
         cfg.n_hidden = net.Mh
         cfg.n_ancilla = net.Ma
+    elif isinstance(net, PureStateAnsatz):
+        cfg.network = _lib.NQ_NET_CHAIN
+        cfg.n_hidden = net.chain.layers[0].n_out
+        cfg.n_ancilla = 0
     elif isinstance(net, RBMSplit):
         cfg.network = _lib.NQ_NET_RBM_SPLIT
         cfg.n_hidden = net.M
         cfg.n_ancilla = 0
     else:
         raise TypeError(f"unsupported network {type(net)}")
-    cfg.activation = _lib.NQ_ACT_LOGCOSH if net.f == af_logcosh else _lib.NQ_ACT_SOFTPLUS
+    f = getattr(net, "f", af_logcosh)
+    cfg.activation = _lib.NQ_ACT_LOGCOSH if f == af_logcosh else _lib.NQ_ACT_SOFTPLUS
     cfg.hilbert = _lib.NQ_HILB_SPIN if ph.kind == "spin" else _lib.NQ_HILB_FOCK
     cfg.n_sites = ph.n_sites
     cfg.n_chains = n_chains
@@ -53,6 +58,23 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
     return cfg
 
 
+def chain_layers(net):
+    """nq_layer array of a PureStateAnsatz's chain."""
+    acts = {af_logcosh: _lib.NQ_ACT_LOGCOSH, af_softplus: _lib.NQ_ACT_SOFTPLUS, "identity": _lib.NQ_ACT_IDENTITY}
+    layers = net.chain.layers
+    arr = (_lib.NqLayer * len(layers))()
+    width = net.N
+    for k, l in enumerate(layers):
+        if isinstance(l, Dense):
+            arr[k] = _lib.NqLayer(_lib.NQ_LAYER_DENSE, l.n_in, l.n_out, acts[l.f])
+            width = l.n_out
+        elif isinstance(l, WSum):
+            arr[k] = _lib.NqLayer(_lib.NQ_LAYER_WSUM, l.n_in, 1, 0)
+        else:
+            arr[k] = _lib.NqLayer(_lib.NQ_LAYER_SUM, width, 1, 0)
+    return arr
+
+
 class Engine:
     def __init__(self, net, hilb, n_chains, chain_length, burn, passes, seed,
                  eval_precision=_lib.NQ_EVAL_F32, s_precision=_lib.NQ_S_F32, quirks=0,
@@ -61,14 +83,18 @@ class Engine:
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
                           s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind, rule, sampler_space)
-        self.complex_params = isinstance(net, (RBM, RBMSplit))
+        self.complex_params = isinstance(net, (RBM, RBMSplit, PureStateAnsatz))
         self.cfg = cfg
         self.lib = L
         self._owned = _handle is None
         self._owner = _owner                  # keeps a batch alive while its problem handles are used
         if _handle is None:
             self.h = ctypes.c_void_p()
-            st = L.nq_create(ctypes.byref(cfg), ctypes.byref(self.h))
+            if isinstance(net, PureStateAnsatz):
+                st = L.nq_create_chain(ctypes.byref(cfg), len(net.chain.layers), chain_layers(net),
+                                       ctypes.byref(self.h))
+            else:
+                st = L.nq_create(ctypes.byref(cfg), ctypes.byref(self.h))
             if st != _lib.NQ_OK:
                 raise _lib.NqError(st, "nq_create failed (see stderr)")
             if isinstance(net, NDMSymm):

@@ -12,6 +12,7 @@ import numpy as np
 
 af_logcosh = "logcosh"
 af_softplus = "softplus"
+identity = "identity"
 
 
 class RBM:
@@ -139,6 +140,122 @@ class NDMSymm(NDM):
 
     def __repr__(self):
         return f"NDMSymm({self.dtype}, n={self.N}, αh={self.Mh}, αa={self.Ma}, n_symm={self.n_symm})"
+
+
+def glorot_uniform(T, *dims, rng=None):
+    """``glorot_uniform`` (src/Networks/utils.jl:7): (rand(T, dims) .- 0.5) *
+    sqrt(24 / Σ dims); for a complex T Julia's rand draws both parts in [0, 1)
+    and the shift applies to the real part only."""
+    rng = np.random.default_rng() if rng is None else rng
+    T = np.dtype(T)
+    scale = np.sqrt(24.0 / sum(dims))
+    if T.kind == "c":
+        v = (rng.random(dims) - 0.5) + 1j * rng.random(dims)
+    else:
+        v = rng.random(dims) - 0.5
+    return (v * scale).astype(T)
+
+
+class Dense:
+    """``Dense(T, in, out, σ=identity)`` (Chains/Layers/Dense.jl:24-36):
+    y = σ.(W x .+ b), W out x in, glorot-uniform initialisation."""
+
+    def __init__(self, T, n_in, n_out, f=identity, rng=None):
+        self.dtype = np.dtype(T)
+        self.n_in, self.n_out, self.f = int(n_in), int(n_out), f
+        self.W = glorot_uniform(self.dtype, self.n_out, self.n_in, rng=rng)
+        self.b = glorot_uniform(self.dtype, self.n_out, rng=rng)
+
+    def arrays(self):
+        return [self.W, self.b]
+
+
+class WSum:
+    """``WSum(T, in)`` (Chains/Layers/WeightedSum.jl): logψ = Σ_i c_i x_i."""
+
+    def __init__(self, T, n_in, rng=None):
+        self.dtype = np.dtype(T)
+        self.n_in = int(n_in)
+        self.c = glorot_uniform(self.dtype, self.n_in, rng=rng)
+
+    def arrays(self):
+        return [self.c]
+
+
+class _SumAutobatch:
+    """``sum_autobatch`` (Chains/Layers/sum.jl): logψ = Σ_i x_i."""
+
+    def arrays(self):
+        return []
+
+    def __repr__(self):
+        return "sum_autobatch"
+
+
+sum_autobatch = _SumAutobatch()
+
+
+class Chain:
+    """``Chain(layers...)`` (Chains/Chain.jl:24-27)."""
+
+    def __init__(self, *layers):
+        self.layers = list(layers)
+
+
+class PureStateAnsatz:
+    """``PureStateAnsatz(chain, N)`` (ClosedSystems/PureChainWrapper.jl:23-41):
+    a ket whose logψ is the chain's output; the flat parameter vector is the
+    functor order of the layers (Dense: W column-major, then b; WSum: c)."""
+
+    def __init__(self, chain, n_sites):
+        if isinstance(n_sites, int):
+            self.N = n_sites
+        else:
+            self.N = n_sites.n_sites
+        self.chain = chain if isinstance(chain, Chain) else Chain(*chain)
+        layers = self.chain.layers
+        if not layers or not all(isinstance(l, Dense) for l in layers[:-1]) or \
+                not isinstance(layers[-1], (WSum, _SumAutobatch)) or len(layers) < 2:
+            raise ValueError("the chain is Dense layers closed by WSum or sum_autobatch")
+        width = self.N
+        for l in layers[:-1]:
+            if l.n_in != width:
+                raise ValueError("layer widths do not match")
+            width = l.n_out
+        if isinstance(layers[-1], WSum) and layers[-1].n_in != width:
+            raise ValueError("WSum width does not match the last Dense layer")
+        self.out_width = width
+        self.dtype = np.result_type(*[a.dtype for l in layers for a in l.arrays()])
+
+    @property
+    def n_params(self):
+        return sum(a.size for l in self.chain.layers for a in l.arrays())
+
+    def flat(self):
+        return np.concatenate([a.reshape(-1, order="F") for l in self.chain.layers for a in l.arrays()]).astype(
+            np.complex128)
+
+    def set_flat(self, v):
+        v = np.asarray(v)
+        o = 0
+        for l in self.chain.layers:
+            if isinstance(l, Dense):
+                n = l.W.size
+                l.W = v[o:o + n].reshape(l.W.shape, order="F").astype(l.dtype)
+                o += n
+                l.b = v[o:o + l.n_out].astype(l.dtype)
+                o += l.n_out
+            elif isinstance(l, WSum):
+                l.c = v[o:o + l.n_in].astype(l.dtype)
+                o += l.n_in
+
+    def __repr__(self):
+        return f"PureStateAnsatz(Chain of {len(self.chain.layers)} layers, N={self.N})"
+
+
+def PureChain(N, *layers):
+    """``PureChain(N, layers...)`` (PureChainWrapper.jl:57-60)."""
+    return PureStateAnsatz(Chain(*layers), N)
 
 
 def init_random_pars_(net, sigma=0.01, rng=None):

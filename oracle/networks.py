@@ -11,6 +11,8 @@ Flat parameter order = functor field order, each array column-major
   ac (N), b (aN), Wr (aN x N), Wc (aN x N)
 * NDMSymm (src/Networks/MixedDensityMatrix/NDMSymm.jl:3-40): the trainable
   vector is the symmetric NDM's (NDM order with ah hidden, aa ancilla)
+* Chain of Dense layers + WSum / sum_autobatch (src/Networks/Chains/): per
+  Dense layer W (out x in) then b, then the WSum weights c
 
 Activations follow src/Networks/activation.jl:5-45; the derivative used by the
 networks is ``fwd_der(f, x)`` (tanh for logcosh, sigmoid for softplus).
@@ -19,6 +21,7 @@ import numpy as np
 
 LOGCOSH = "logcosh"
 SOFTPLUS = "softplus"
+IDENTITY = "identity"
 
 
 def logcosh(x):
@@ -43,11 +46,15 @@ def softplus(x):
 
 
 def act(name, x):
+    if name == IDENTITY:
+        return np.asarray(x)
     return logcosh(x) if name == LOGCOSH else softplus(x)
 
 
 def dact(name, x):
-    """``fwd_der(f, x)`` (activation.jl:22-27)."""
+    """``fwd_der(f, x)`` (activation.jl:22-29)."""
+    if name == IDENTITY:
+        return np.ones_like(np.asarray(x))
     if name == LOGCOSH:
         return np.tanh(x)
     return 1.0 / (1.0 + np.exp(-x))
@@ -326,6 +333,84 @@ class NDMSymm:
 
     def log_prob(self, sr, sc):
         return self.bare.log_prob(sr, sc)
+
+
+class Chain:
+    """Feed-forward ket (Chain.jl:24-90): ``layers`` is a list of
+    ("dense", n_in, n_out, activation), then one ("wsum", n_in) or
+    ("sum", n_in).  Dense.jl:73-104: θ = W x + b, y = f(θ), ∇W = δθ xᵀ,
+    ∇b = δθ, δ_in = Wᵀ δθ with δθ = δ f'(θ); WeightedSum.jl: logψ = Σ c x,
+    ∇c = x, δ = c; sum.jl: logψ = Σ x, δ = 1.  Complex parameters."""
+
+    def __init__(self, n, layers):
+        self.N = int(n)
+        self.layers = [tuple(l) for l in layers]
+        self.params = []
+        for l in self.layers:
+            if l[0] == "dense":
+                self.params.append([np.zeros((l[2], l[1]), np.complex128), np.zeros(l[2], np.complex128)])
+            elif l[0] == "wsum":
+                self.params.append([np.zeros(l[1], np.complex128)])
+            else:
+                self.params.append([])
+
+    @property
+    def n_params(self):
+        return sum(a.size for ps in self.params for a in ps)
+
+    def flat(self):
+        return np.concatenate([a.reshape(-1, order="F") for ps in self.params for a in ps])
+
+    def set_flat(self, v):
+        v = np.asarray(v).astype(np.complex128)
+        o = 0
+        for ps in self.params:
+            for k, a in enumerate(ps):
+                ps[k] = v[o:o + a.size].reshape(a.shape, order="F").copy()
+                o += a.size
+
+    def _forward(self, sigma):
+        x = np.atleast_2d(sigma).astype(np.complex128)
+        xs, ths = [], []
+        for l, ps in zip(self.layers, self.params):
+            xs.append(x)
+            if l[0] == "dense":
+                th = x @ ps[0].T + ps[1][None, :]
+                ths.append(th)
+                x = act(l[3], th)
+            elif l[0] == "wsum":
+                ths.append(None)
+                return x @ ps[0], xs, ths
+            else:
+                ths.append(None)
+                return x.sum(axis=1), xs, ths
+        raise ValueError("the chain must end with wsum or sum")
+
+    def logpsi(self, sigma):
+        return self._forward(sigma)[0]
+
+    def logpsi_and_grad(self, sigma):
+        out, xs, ths = self._forward(sigma)
+        B = out.shape[0]
+        grads = [None] * len(self.layers)
+        last = len(self.layers) - 1
+        if self.layers[last][0] == "wsum":
+            grads[last] = [xs[last]]
+            d = np.repeat(self.params[last][0][None, :], B, axis=0)
+        else:
+            grads[last] = []
+            d = np.ones_like(xs[last])
+        for li in range(last - 1, -1, -1):
+            l, ps = self.layers[li], self.params[li]
+            dth = d * dact(l[3], ths[li])
+            gW = (dth[:, :, None] * xs[li][:, None, :]).transpose(0, 2, 1).reshape(B, -1)
+            grads[li] = [gW, dth]
+            d = dth @ ps[0]
+        grad = np.concatenate([g for gs in grads for g in gs], axis=1)
+        return out, grad
+
+    def log_prob(self, sigma):
+        return 2.0 * np.real(self.logpsi(sigma))
 
 
 def init_random_pars(net, rng, sigma=1e-4):

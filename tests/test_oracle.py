@@ -155,6 +155,34 @@ def test_ndm_symm_restatement():
     ns.set_flat(p0)
 
 
+@pytest.mark.parametrize("layers", [
+    [("dense", 4, 8, nw.LOGCOSH), ("sum", 8)],
+    [("dense", 4, 8, nw.IDENTITY), ("dense", 8, 12, nw.IDENTITY), ("wsum", 12)],
+    [("dense", 4, 3, nw.SOFTPLUS), ("dense", 3, 2, nw.SOFTPLUS), ("wsum", 2)],
+    [("dense", 4, 8, nw.LOGCOSH), ("dense", 8, 4, nw.LOGCOSH), ("sum", 4)]])
+def test_chain_gradients_vs_finite_differences(layers):
+    """The chains of test/Machines/test_grad.jl:29-44 and test_batched.jl:
+    32-46: backprop gradient == finite differences (holomorphic), and a
+    single Dense + sum is the RBM without visible bias."""
+    rng = np.random.default_rng(3)
+    N = 4
+    ch = nw.Chain(N, layers)
+    nw.init_random_pars(ch, rng, sigma=0.3 ** 2)
+    s = rng.choice([-1.0, 1.0], size=(5, N))
+    _, g = ch.logpsi_and_grad(s)
+    p = ch.flat()
+    eps = 1e-6
+    for k in range(p.size):
+        q = p.copy(); q[k] += eps; ch.set_flat(q); lp = ch.logpsi(s)
+        q[k] -= 2 * eps; ch.set_flat(q); lm = ch.logpsi(s)
+        assert np.max(np.abs((lp - lm) / (2 * eps) - g[:, k])) < 1e-7
+    ch.set_flat(p)
+    if layers[0][3] == nw.LOGCOSH and len(layers) == 2:
+        r = nw.RBM(N, 8, nw.LOGCOSH)
+        r.W, r.b = ch.params[0][0], ch.params[0][1]
+        np.testing.assert_allclose(ch.logpsi(s), r.logpsi(s), atol=1e-13)
+
+
 def test_ndm_parameter_count():
     n = nw.NDM(6, 1, 1)
     assert n.n_params == 2 * 6 + 2 * 6 + 6 + 2 * 36 + 2 * 36
