@@ -300,8 +300,20 @@ rbm_eval_batch_kernel(const EvalJob<R>* __restrict__ jobs, const int* __restrict
 // Force partial sums over chunks of CH samples (one block per chunk):
 //   O_s  = [v(s), g(s), g(s) v(s)ᵀ]          (P = N + M + M N entries)
 //   ΣO, Σ E conj(O), Σ E
-// accumulated in FP32 with Kahan compensation inside a chunk, emitted in FP64.
+// emitted in FP64 per chunk.  The W entries are register tiles of one hidden
+// unit h and four sites: per sample, E conj(g_h) and g_h are formed once and
+// multiplied by the four site values.  ΣO adds groups of 8 samples in FP32 and
+// the group sums with Kahan compensation; the visible-bias sums Σ v are exact
+// (integers).
 // ---------------------------------------------------------------------------
+template <typename R>
+NQ_D void kahan_add(cpx<R>& s, cpx<R>& c, cpx<R> x) {
+  const cpx<R> y = x - c;
+  const cpx<R> t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256)
 rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ samples, int Ns,
@@ -309,45 +321,92 @@ rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ sa
                          double* __restrict__ partial, double* __restrict__ partialE) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int P = N + M + M * N;
+  const int NJ = (N + 3) & ~3;                         // sites padded to groups of 4
   const int s0 = blockIdx.x * CH;
   const int n = min(CH, Ns - s0);
   cpx<R>* s_g = reinterpret_cast<cpx<R>*>(smem_raw);   // [CH][M]: consecutive h conflict-free
   cpx<R>* s_e = s_g + (size_t)M * CH;                  // [CH]
-  R* s_v = reinterpret_cast<R*>(s_e + CH);             // [N][CH]
+  R* s_v = reinterpret_cast<R*>(s_e + CH);             // [CH][NJ]
   for (int k = threadIdx.x; k < M * CH; k += blockDim.x) {
-    int h = k / CH, t = k % CH;
+    const int h = k / CH, t = k % CH;
     s_g[t * M + h] = t < n ? g[(size_t)h * Ns + s0 + t] : mk(R(0), R(0));
   }
   for (int t = threadIdx.x; t < CH; t += blockDim.x) {
-    uint64_t bits = t < n ? samples[s0 + t] : 0;
+    const uint64_t bits = t < n ? samples[s0 + t] : 0;
     s_e[t] = t < n ? eloc[s0 + t] : mk(R(0), R(0));
-    for (int j = 0; j < N; ++j) s_v[j * CH + t] = t < n ? site_value<R>(bits, j, hilb) : R(0);
+    for (int j = 0; j < NJ; ++j) s_v[t * NJ + j] = (t < n && j < N) ? site_value<R>(bits, j, hilb) : R(0);
   }
   __syncthreads();
-  for (int p = threadIdx.x; p < P; p += blockDim.x) {
-    cpx<R> so = mk(R(0), R(0)), co = mk(R(0), R(0));   // Kahan sum of O
-    cpx<R> se = mk(R(0), R(0));
-    int kind, h = 0, j = 0;
-    if (p < N) { kind = 0; j = p; }
-    else if (p < N + M) { kind = 1; h = p - N; }
-    else { kind = 2; h = (p - N - M) % M; j = (p - N - M) / M; }
-    for (int t = 0; t < n; ++t) {
-      cpx<R> o;
-      if (kind == 0) o = mk(s_v[j * CH + t], R(0));
-      else if (kind == 1) o = s_g[t * M + h];
-      else o = s_v[j * CH + t] * s_g[t * M + h];
-      // Kahan
-      cpx<R> y = o - co;
-      cpx<R> tt = so + y;
-      co = (tt - so) - y;
-      so = tt;
-      se = se + s_e[t] * conjc(o);
+  double* dst = partial + (size_t)blockIdx.x * 4 * P;
+  const int nW = M * (NJ / 4);
+  for (int item = threadIdx.x; item < nW + M + N; item += blockDim.x) {
+    if (item < nW) {
+      const int h = item % M, jq = item / M;
+      cpx<R> so[4], co[4], se[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { so[q] = mk(R(0), R(0)); co[q] = so[q]; se[q] = so[q]; }
+      for (int t0 = 0; t0 < n; t0 += 8) {
+        cpx<R> po[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) po[q] = mk(R(0), R(0));
+        const int t1 = min(n, t0 + 8);
+        for (int t = t0; t < t1; ++t) {
+          const cpx<R> gv = s_g[t * M + h];
+          const cpx<R> a = s_e[t] * conjc(gv);
+          const R* v = s_v + t * NJ + 4 * jq;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            po[q].x += gv.x * v[q];
+            po[q].y += gv.y * v[q];
+            se[q].x += a.x * v[q];
+            se[q].y += a.y * v[q];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) kahan_add(so[q], co[q], po[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = 4 * jq + q;
+        if (j >= N) break;
+        const int p = N + M + h + M * j;
+        dst[2 * p] = (double)so[q].x;
+        dst[2 * p + 1] = (double)so[q].y;
+        dst[2 * P + 2 * p] = (double)se[q].x;
+        dst[2 * P + 2 * p + 1] = (double)se[q].y;
+      }
+    } else if (item < nW + M) {
+      const int h = item - nW;
+      cpx<R> so = mk(R(0), R(0)), co = so, se = so;
+      for (int t0 = 0; t0 < n; t0 += 8) {
+        cpx<R> po = mk(R(0), R(0));
+        for (int t = t0; t < min(n, t0 + 8); ++t) {
+          const cpx<R> gv = s_g[t * M + h];
+          po = po + gv;
+          se = se + s_e[t] * conjc(gv);
+        }
+        kahan_add(so, co, po);
+      }
+      const int p = N + h;
+      dst[2 * p] = (double)so.x;
+      dst[2 * p + 1] = (double)so.y;
+      dst[2 * P + 2 * p] = (double)se.x;
+      dst[2 * P + 2 * p + 1] = (double)se.y;
+    } else {
+      const int j = item - nW - M;
+      R so = R(0);                                      // a sum of integers: exact
+      cpx<R> se = mk(R(0), R(0));
+      for (int t = 0; t < n; ++t) {
+        const R v = s_v[t * NJ + j];
+        so += v;
+        se.x += s_e[t].x * v;
+        se.y += s_e[t].y * v;
+      }
+      dst[2 * j] = (double)so;
+      dst[2 * j + 1] = 0.0;
+      dst[2 * P + 2 * j] = (double)se.x;
+      dst[2 * P + 2 * j + 1] = (double)se.y;
     }
-    double* dst = partial + (size_t)blockIdx.x * 4 * P;
-    dst[2 * p] = (double)so.x;
-    dst[2 * p + 1] = (double)so.y;
-    dst[2 * P + 2 * p] = (double)se.x;
-    dst[2 * P + 2 * p + 1] = (double)se.y;
   }
   if (threadIdx.x == 0) {
     double ex = 0, ey = 0;
@@ -542,9 +601,14 @@ cudaError_t launch_rbm_eval_batch(const EvalJob<R>* jobs, const int* blk_start, 
 template cudaError_t launch_rbm_eval_batch<float>(const EvalJob<float>*, const int*, int, int, int, int, int, int,
                                                   cudaStream_t);
 
+static size_t force_smem(int N, int M, int CH, int csize) {
+  const int NJ = (N + 3) & ~3;
+  return (size_t)(M + 1) * CH * csize + (size_t)NJ * CH * (csize / 2);
+}
+
 static int force_chunk(int N, int M, int csize) {
   int CH = 256;
-  while (CH > 32 && ((size_t)(M + 1) * CH * csize + (size_t)N * CH * (csize / 2)) > 64 * 1024) CH /= 2;
+  while (CH > 32 && force_smem(N, M, CH, csize) > 64 * 1024) CH /= 2;
   return CH;
 }
 
@@ -558,7 +622,7 @@ cudaError_t launch_rbm_force(const RbmDev<R>& net, const uint64_t* samples, int 
                              const cpx<R>* eloc, const ForceBufs& fb, cudaStream_t st) {
   const int CH = force_chunk(net.N, net.M, (int)sizeof(cpx<R>));
   const int nblk = (Ns + CH - 1) / CH;
-  size_t smem = ((size_t)net.M * CH + CH) * sizeof(cpx<R>) + (size_t)net.N * CH * sizeof(R);
+  const size_t smem = force_smem(net.N, net.M, CH, (int)sizeof(cpx<R>));
   auto kern = rbm_force_partial_kernel<R>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
