@@ -17,5 +17,6 @@ from .stats import Measurement  # noqa: F401
 from .iterative import (BatchedSampler, BatchedObsKetSampler, BatchedObsDMSampler, add_observable_,  # noqa: F401
                         compute_observables, SR, Descent, sample_,  # noqa: F401
                         precondition_, update_,  # noqa: F401
-                        sr_shift, sr_multiplicative, sr_none, sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq)
+                        sr_shift, sr_multiplicative, sr_none, sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq,
+                        sr_diag, sr_div)
 from .engine import Engine, ProblemBatch  # noqa: F401

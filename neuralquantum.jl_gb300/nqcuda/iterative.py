@@ -22,19 +22,25 @@ from .stats import Measurement
 
 sr_shift, sr_multiplicative, sr_none = 0, 1, 2
 sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq = "sr_cholesky", "sr_cg", "sr_minres", "sr_qlp", "sr_lsq"
+sr_diag, sr_div, sr_pivcholesky = "sr_diag", "sr_div", "sr_pivcholesky"
 _ITERATIVE = (sr_cg, sr_minres, sr_qlp, sr_lsq)
+_DIRECT = (sr_cholesky, sr_diag, sr_div)
 
 
 class SR:
     """``SR(T; ϵ=0.001, precision=1e-4, precondition_type=sr_shift,
     algorithm=sr_cholesky, λ0=100, b=0.95, λmin=1e-4)`` (SR.jl:41-50).
-    sr_cholesky forms S and solves directly; the iterative algorithms run the
-    engine's matrix-free conjugate-gradient solve of the same shifted system
-    to the relative residual ``precision``."""
+    sr_cholesky, sr_diag (pinv) and sr_div form S and solve the preconditioned
+    system directly (the shifted S is positive definite, where the three
+    agree; a singular S with sr_none is refused, not pseudo-inverted); the
+    iterative algorithms run the engine's matrix-free conjugate-gradient
+    solve of the same shifted system to the relative residual ``precision``.
+    sr_pivcholesky is not implemented by the reference's precondition!
+    either (SRDirect.jl:84-86)."""
 
     def __init__(self, eps=0.001, precondition_type=sr_shift, algorithm=sr_cholesky,
                  lam0=100.0, b=0.95, lam_min=1e-4, precision=1e-4):
-        if algorithm != sr_cholesky and algorithm not in _ITERATIVE:
+        if algorithm not in _DIRECT and algorithm not in _ITERATIVE:
             raise NotImplementedError(f"unknown SR algorithm {algorithm}")
         self.eps, self.precondition_type = float(eps), precondition_type
         self.lam0, self.b, self.lam_min = float(lam0), float(b), float(lam_min)
@@ -76,6 +82,7 @@ class BatchedSampler:
         self.liouvillian = isinstance(prob, KLocalLiouvillian)
         hilb = prob.hilb if not self.liouvillian else prob.hilb
         quirks = _lib.NQ_QUIRK_STALE_LAST_SLOT if reference_quirks else 0
+        self.reference_quirks = bool(reference_quirks)
         sr_alg = _lib.NQ_SR_CG if self.algo.iterative else _lib.NQ_SR_DIRECT
         exch = getattr(getattr(sampler, "rule", None), "couplings", None)
         move_op = getattr(getattr(sampler, "rule", None), "operator", None)
@@ -126,8 +133,16 @@ def sample_(is_):
 
 
 def precondition_(prec, algo, it):
+    """``precondition!(prec, SR, it)``.  With reference_quirks the reference's
+    handling of sr_multiplicative is reproduced: sr_cholesky and sr_div solve
+    with S itself and the multiplicative shift reaches only sr_diag
+    (SRDirect.jl:64-83)."""
     eng = prec.sampler.engine
-    dw = eng.precondition(algo.precondition_type, algo.eps, algo.lam0, algo.b, algo.lam_min, it)
+    kind = algo.precondition_type
+    if getattr(prec.sampler, "reference_quirks", False) and kind == sr_multiplicative and \
+            algo.algorithm in (sr_cholesky, sr_div):
+        kind = sr_none
+    dw = eng.precondition(kind, algo.eps, algo.lam0, algo.b, algo.lam_min, it)
     return Gradient(prec.sampler, dw)
 
 

@@ -306,6 +306,24 @@ def test_dm_local_observables_sum_to_trace(kind):
         assert abs(np.sum(p * loc) - exact.dm_expectation(n, O)) < 1e-10
 
 
+def test_sr_algorithms_and_the_multiplicative_quirk():
+    """SRDirect.jl:51-90: for a positive-definite shifted S, sr_diag (pinv),
+    sr_cholesky and sr_div agree; the reference's sr_cholesky / sr_div solve
+    with S itself under sr_multiplicative (the shift reaches sr_diag only)."""
+    rng = np.random.default_rng(9)
+    O = rng.standard_normal((300, 10)) + 1j * rng.standard_normal((300, 10))
+    S = osr.build_S(O - O.mean(0), real_params=False)
+    F = rng.standard_normal(10) + 1j * rng.standard_normal(10)
+    ref = osr.precondition(S, F, 0.01)
+    for alg in ("diag", "div"):
+        np.testing.assert_allclose(osr.precondition(S, F, 0.01, algorithm=alg), ref, rtol=1e-10, atol=1e-12)
+    q = osr.precondition(S, F, 0.01, kind="multiplicative", it=3, follow_reference=True)
+    np.testing.assert_allclose(q, osr.precondition(S, F, 0.01, kind="none"), rtol=1e-10, atol=1e-12)
+    d = osr.precondition(S, F, 0.01, kind="multiplicative", it=3, algorithm="diag", follow_reference=True)
+    np.testing.assert_allclose(d, osr.precondition(S, F, 0.01, kind="multiplicative", it=3), rtol=1e-10,
+                               atol=1e-12)
+
+
 def test_sr_solve_matches_direct():
     rng = np.random.default_rng(3)
     O = rng.standard_normal((200, 12)) + 1j * rng.standard_normal((200, 12))

@@ -208,3 +208,40 @@ def test_observables_match_oracle(nqlib):
     mH, locH = is_.engine.observable(nq.op_table(is_.prob), want_loc=True)
     np.testing.assert_allclose(locH, locE, rtol=0, atol=1e-12)
     assert mH.mean_re == mE.mean_re
+
+
+def test_sr_algorithms_and_reference_multiplicative_quirk(nqlib):
+    """precondition_ with SR(algorithm=sr_diag / sr_div / sr_cholesky) on the
+    engine's S and F agrees with the oracle; with reference_quirks,
+    sr_multiplicative + sr_cholesky / sr_div solve with S itself as the
+    reference's precondition! does (SRDirect.jl:64-83): the call is the
+    engine's unshifted solve (an ill-conditioned S makes that solve fragile,
+    in the reference too, so it is compared with the same engine call, not
+    with the oracle), while sr_diag keeps the shift."""
+    N, B, L = 6, 256, 8
+    for quirks in (False, True):
+        is_, net, onet, oH, ohilb = make(N=N, B=B, L=L, burn=10, sigma=0.2 ** 2, quirks=quirks)
+        is_.engine.sample(1)
+        prec = nq.iterative.SRCache(is_)
+        m, loc, force = is_.engine.estimate(want_loc=True, want_force=True)
+        S = is_.engine.sr_matrix()
+        for alg in (nq.sr_cholesky, nq.sr_diag, nq.sr_div):
+            for kind, okind in ((nq.sr_shift, "shift"), (nq.sr_multiplicative, "multiplicative")):
+                algo = nq.SR(eps=0.01, precondition_type=kind, algorithm=alg)
+                if quirks and kind == nq.sr_multiplicative and alg != nq.sr_diag:
+                    outs = []
+                    for call in (lambda: nq.precondition_(prec, algo, 3).values,
+                                 lambda: is_.engine.precondition(nq.sr_none, 0.01, it=3)):
+                        try:
+                            outs.append(call())
+                        except nq._lib.NqError as e:
+                            outs.append(e.status)
+                    if isinstance(outs[0], np.ndarray):
+                        np.testing.assert_array_equal(outs[0], outs[1])
+                    else:
+                        assert outs[0] == outs[1]
+                    continue
+                dw = nq.precondition_(prec, algo, 3).values
+                oalg = {nq.sr_cholesky: "cholesky", nq.sr_diag: "diag", nq.sr_div: "div"}[alg]
+                dwo = osr.precondition(S, force, 0.01, kind=okind, it=3, algorithm=oalg)
+                assert rel(dw, dwo) < 2e-3, (quirks, alg, okind)
