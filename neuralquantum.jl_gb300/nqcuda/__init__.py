@@ -20,3 +20,4 @@ from .iterative import (BatchedSampler, BatchedObsKetSampler, BatchedObsDMSample
                         sr_shift, sr_multiplicative, sr_none, sr_cholesky, sr_cg, sr_minres, sr_qlp, sr_lsq,
                         sr_diag, sr_div)
 from .engine import Engine, ProblemBatch  # noqa: F401
+from .lattice import HyperCube, translational_symm_table, quantum_ising_hamiltonian, lattice_average_operator  # noqa: F401,E501

@@ -121,14 +121,17 @@ class NDMSymm(NDM):
     """``NDMSymm(T, N, αh, αa, permutations, f=logℒ)`` (NDMSymm.jl:17-30): the
     trainable parameters are those of a symmetric NDM with αh hidden and αa
     ancilla features (fields as NDM); the network evaluated is the bare NDM
-    whose units are those features under every permutation (0-based site
-    lists).  The symmetric visible biases are kept at their means."""
+    whose units are those features under every permutation (site lists,
+    0-based or, as translational_symm_table gives them, 1-based).  The
+    symmetric visible biases are kept at their means."""
 
     def __init__(self, T, N, alpha_h, alpha_a, permutations, f=af_logcosh):
         super().__init__(T, N, alpha_h / N, alpha_a / N, f)
         perms = np.asarray(permutations, dtype=np.int64)
         if perms.ndim != 2 or perms.shape[1] != self.N:
             raise ValueError("permutations must be a list of site lists of length N")
+        if all(sorted(p.tolist()) == list(range(1, self.N + 1)) for p in perms):
+            perms = perms - 1            # 1-based site lists (translational_symm_table)
         for p in perms:
             if sorted(p.tolist()) != list(range(self.N)):
                 raise ValueError("every permutation must be a permutation of the sites 0..N-1")

@@ -140,3 +140,39 @@ def test_host_api_mirrors_reference_names():
     assert s.passes == 21        # Metropolis.jl:30-38
     with pytest.raises(ValueError):
         nq.sigmax(nq.HomogeneousSpin(4), 5)
+
+
+def test_hypercube_and_lattice_operators():
+    """HyperCube.jl:26-136 and SimpleOperators.jl:160-185: edges (u < v, in
+    the reference's SimpleGraph order), translations as circshift of the
+    column-major vertex grid, and the quantum Ising Hamiltonian of an open
+    chain equal to the oracle's g/2 Σσx + V/4 Σσzσz."""
+    from oracle import exact as oex, operators as oops
+    assert nq.HyperCube([4]).edges() == [(1, 2), (1, 4), (2, 3), (3, 4)]
+    assert nq.HyperCube([4], periodic=False).edges() == [(1, 2), (2, 3), (3, 4)]
+    sq = nq.HyperCube([3, 3])
+    assert sq.nv() == 9 and sq.ne() == 18 and sq.vert_coords[1] == [2, 1]
+    assert nq.HyperCube([2, 3], periodic=[False, True]).ne() == 3 + 6
+    assert nq.translational_symm_table(nq.HyperCube([4])) == [[1, 2, 3, 4], [4, 1, 2, 3], [3, 4, 1, 2],
+                                                               [2, 3, 4, 1]]
+    t2 = nq.translational_symm_table(sq)
+    assert len(t2) == 9 and t2[1] == [7, 8, 9, 1, 2, 3, 4, 5, 6] and t2[3] == [3, 1, 2, 6, 4, 5, 9, 7, 8]
+    N = 4
+    hilb = nq.HomogeneousFock(N)
+    H = nq.quantum_ising_hamiltonian(nq.HyperCube([N], periodic=False), hilb, g=1.0, V=2.0)
+    oh = Hilbert(N, FOCK)
+    oH, _ = oex.dissipative_ising(oh, 1.0, 2.0)
+    tab = nq.op_table(H)
+    dense = np.zeros((oh.dim, oh.dim), complex)
+    for i, st in enumerate(oh.all_states()):
+        for mel, ch in tab.connections(st):
+            s2 = st.copy()
+            for site, v in ch:
+                s2[site] = v
+            dense[i, oh.index_of_state(s2[None])[0]] += mel
+    np.testing.assert_allclose(dense, oops.to_matrix(oH), atol=1e-12)
+    avg = nq.lattice_average_operator(nq.HyperCube([N]), hilb, nq.sigmaz)
+    assert len(nq.op_table(avg).connections(oh.all_states()[0])) >= 1
+    perms = nq.translational_symm_table(nq.HyperCube([N]))
+    net = nq.NDMSymm(np.float64, N, 1, 1, perms)
+    assert net.permutations.min() == 0 and net.permutations.max() == N - 1
