@@ -97,6 +97,9 @@ struct SamplerRun {
 template <typename R>
 cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
 int rbm_sampler_valid_lanes(int N, int M, int csize, int* out, int max_out);
+// the instantiations with units at weight 1/2 (net.n_half > 0, density matrices)
+template <typename R>
+cudaError_t launch_rbm_sampler_half(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st);
 // the exchange-rule instantiations of the FP32 sampler (net.pairs set)
 cudaError_t launch_rbm_sampler_exchange(const RbmDev<float>& net, const SamplerRun& run, int G, cudaStream_t st);
 // OperatorRule sampler (FP32 ket), net.opm set

@@ -38,10 +38,13 @@ template <typename R> struct alignas(4 * sizeof(R)) cpx_pair {
 // Hidden units are padded to MP = G*HPL with neutral table entries (ratio
 // factor 1, no θ change), so the proposal and accept loops have no unit-range
 // branches.
+// HALF: the first net.n_half units enter log|ψ|^2 with weight 1/2 (the λ
+// units of a density matrix); without it no unit does, and the proposal loop
+// keeps a single product.
 // EXCH: the exchange rule (ExchangeRule.jl:38-68): a move draws a coupling
 // (i, j) and swaps the two values; equal values leave the state unchanged
 // (ratio 1, accepted).  The move tables are then per coupling.
-template <typename R, int G, int HPL, int ACT, bool EXCH = false>
+template <typename R, int G, int HPL, int ACT, bool EXCH = false, bool HALF = false>
 NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int MP = G * HPL;
@@ -101,7 +104,7 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
 #pragma unroll
   for (int k = 0; k < HPL; ++k) {
     const int h = lane + G * k;
-    half[k] = h < n_half;
+    half[k] = HALF && h < n_half;
     cpx<R> t = h < M ? net.b[h] : mk(R(0), R(0));
     if (h < M)
       for (int j = 0; j < N; ++j) {
@@ -160,11 +163,11 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
           const cpx<R> bb = pos ? tt.a : tt.b;
           rr = cfma(g[k], bb, mk(R(1), R(0)));
         }
-        if (half[k]) prod_half *= abs2c(rr);
+        if (HALF && half[k]) prod_half *= abs2c(rr);
         else prod *= abs2c(rr);
       }
       R lsum = fast_log2(prod);
-      if (n_half > 0) lsum += R(0.5) * fast_log2(prod_half);
+      if (HALF) lsum += R(0.5) * fast_log2(prod_half);
 #pragma unroll
       for (int off = G / 2; off > 0; off >>= 1) lsum += __shfl_xor_sync(gmask, lsum, off, G);
       const R logA = s_are[i] * dv + lsum;                  // log2 of the acceptance ratio
@@ -206,9 +209,9 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   if (active && lane == 0) atomicAdd(run.accepted, naccept);
 }
 
-template <typename R, int G, int HPL, int ACT, bool EXCH>
+template <typename R, int G, int HPL, int ACT, bool EXCH, bool HALF>
 __global__ void __launch_bounds__(256) rbm_sampler_kernel(RbmDev<R> net, SamplerRun run) {
-  sampler_block<R, G, HPL, ACT, EXCH>(net, run, blockIdx.x);
+  sampler_block<R, G, HPL, ACT, EXCH, HALF>(net, run, blockIdx.x);
 }
 
 // Many independent problems in one launch: problem p owns blocks
@@ -228,14 +231,14 @@ rbm_sampler_batch_kernel(const SamplerJob<R>* __restrict__ jobs, const int* __re
 
 }  // namespace
 
-template <typename R, int G, int HPL, int ACT, bool EXCH>
+template <typename R, int G, int HPL, int ACT, bool EXCH, bool HALF>
 static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
   const int threads = run.block;
   const int chains_per_block = threads / G;
   const int blocks = (run.B + chains_per_block - 1) / chains_per_block;
   const int NR = EXCH ? net.n_rows : net.N;
   size_t smem = (size_t)4 * NR * (G * HPL) * sizeof(cpx<R>) + (EXCH ? NR * sizeof(int2) : 0) + NR * sizeof(R);
-  auto kern = rbm_sampler_kernel<R, G, HPL, ACT, EXCH>;
+  auto kern = rbm_sampler_kernel<R, G, HPL, ACT, EXCH, HALF>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -244,29 +247,29 @@ static cudaError_t sampler_inst(const RbmDev<R>& net, const SamplerRun& run, cud
   return cudaGetLastError();
 }
 
-template <typename R, int G, int ACT, bool EXCH>
+template <typename R, int G, int ACT, bool EXCH, bool HALF>
 static cudaError_t sampler_hpl(const RbmDev<R>& net, const SamplerRun& run, cudaStream_t st) {
   const int hpl = (net.M + G - 1) / G;
   switch (hpl) {
-    case 1: return sampler_inst<R, G, 1, ACT, EXCH>(net, run, st);
-    case 2: return sampler_inst<R, G, 2, ACT, EXCH>(net, run, st);
-    case 3: return sampler_inst<R, G, 3, ACT, EXCH>(net, run, st);
-    case 4: return sampler_inst<R, G, 4, ACT, EXCH>(net, run, st);
-    case 5: return sampler_inst<R, G, 5, ACT, EXCH>(net, run, st);
-    case 6: return sampler_inst<R, G, 6, ACT, EXCH>(net, run, st);
-    case 8: return sampler_inst<R, G, 8, ACT, EXCH>(net, run, st);
-    case 10: return sampler_inst<R, G, 10, ACT, EXCH>(net, run, st);
+    case 1: return sampler_inst<R, G, 1, ACT, EXCH, HALF>(net, run, st);
+    case 2: return sampler_inst<R, G, 2, ACT, EXCH, HALF>(net, run, st);
+    case 3: return sampler_inst<R, G, 3, ACT, EXCH, HALF>(net, run, st);
+    case 4: return sampler_inst<R, G, 4, ACT, EXCH, HALF>(net, run, st);
+    case 5: return sampler_inst<R, G, 5, ACT, EXCH, HALF>(net, run, st);
+    case 6: return sampler_inst<R, G, 6, ACT, EXCH, HALF>(net, run, st);
+    case 8: return sampler_inst<R, G, 8, ACT, EXCH, HALF>(net, run, st);
+    case 10: return sampler_inst<R, G, 10, ACT, EXCH, HALF>(net, run, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
-template <typename R, int ACT, bool EXCH>
+template <typename R, int ACT, bool EXCH, bool HALF = false>
 static cudaError_t sampler_g(const RbmDev<R>& net, const SamplerRun& run, int G, cudaStream_t st) {
   switch (G) {
-    case 4: return sampler_hpl<R, 4, ACT, EXCH>(net, run, st);
-    case 8: return sampler_hpl<R, 8, ACT, EXCH>(net, run, st);
-    case 16: return sampler_hpl<R, 16, ACT, EXCH>(net, run, st);
-    case 32: return sampler_hpl<R, 32, ACT, EXCH>(net, run, st);
+    case 4: return sampler_hpl<R, 4, ACT, EXCH, HALF>(net, run, st);
+    case 8: return sampler_hpl<R, 8, ACT, EXCH, HALF>(net, run, st);
+    case 16: return sampler_hpl<R, 16, ACT, EXCH, HALF>(net, run, st);
+    case 32: return sampler_hpl<R, 32, ACT, EXCH, HALF>(net, run, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -285,6 +288,8 @@ cudaError_t launch_rbm_sampler(const RbmDev<R>& net, const SamplerRun& run, int 
       return net.opm ? launch_rbm_sampler_oprule(net, run, G, st) : launch_rbm_sampler_exchange(net, run, G, st);
     else return cudaErrorInvalidValue;
   }
+  // units at weight 1/2 (density matrices): instantiated in sampler_half32.cu / sampler_half64.cu
+  if (net.n_half > 0) return launch_rbm_sampler_half<R>(net, run, G, st);
   if (net.act == ACT_LOGCOSH) return sampler_g<R, ACT_LOGCOSH, false>(net, run, G, st);
   return sampler_g<R, ACT_SOFTPLUS, false>(net, run, G, st);
 }

@@ -19,7 +19,8 @@ BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libnqcuda.so")
 SOURCES = ["api.cu", "rbm.cu", "sampler_f32.cu", "sampler_f64.cu", "sr.cu", "tc.cu", "spdinv.cu", "ndm.cu",
            "made.cu", "mix_sampler.cu", "proposal.cu", "noalloc.cu", "sampler_batch.cu", "theta_tc.cu",
-           "srcg.cu", "exact.cu", "sampler_exch.cu", "sampler_oprule.cu", "chain.cu"]
+           "srcg.cu", "exact.cu", "sampler_exch.cu", "sampler_oprule.cu", "chain.cu",
+           "sampler_half32.cu", "sampler_half64.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
