@@ -111,12 +111,15 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
   const int N = net.N, M = net.M, T = blockDim.x;
   const int M8 = (M + 7) & ~7;                           // hidden units padded to a multiple of 8
   cpx_t01<R>* s_t01 = reinterpret_cast<cpx_t01<R>*>(smem_raw);  // [N*M8] (if has_op)
-  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(s_t01 + (has_op ? N * M8 : 0));  // [M*N]
-  cpx<R>* s_b = s_W + M * N;                              // [M]
-  cpx<R>* s_a = s_b + M;                                  // [N]
+  cpx<R>* s_W = reinterpret_cast<cpx<R>*>(s_t01 + (has_op ? N * M8 : 0));  // [M8*N], zero padding
+  cpx<R>* s_b = s_W + M8 * N;                             // [M8]
+  cpx<R>* s_a = s_b + M8;                                 // [N]
   cpx<R>* s_g = s_a + N;                                  // [M8][T], g = 0 on the padding
-  for (int k = threadIdx.x; k < M * N; k += T) s_W[k] = net.W[k];
-  for (int k = threadIdx.x; k < M; k += T) s_b[k] = net.b[k];
+  for (int k = threadIdx.x; k < M8 * N; k += T) {
+    const int h = k % M8, j = k / M8;
+    s_W[k] = h < M ? net.W[h + M * j] : mk(R(0), R(0));
+  }
+  for (int k = threadIdx.x; k < M8; k += T) s_b[k] = k < M ? net.b[k] : mk(R(0), R(0));
   for (int k = threadIdx.x; k < N; k += T) s_a[k] = net.a[k];
   for (int k = threadIdx.x; k < (M8 - M) * T; k += T) s_g[M * T + k] = mk(R(0), R(0));
   if (has_op)
@@ -140,24 +143,24 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
     lp.x += s_a[j].x * v;
     lp.y += s_a[j].y * v;
   }
-  // θ of four hidden units per pass over the sites (one site value per j)
+  // θ of four hidden units per pass over the sites (one site value per j;
+  // the weights are zero-padded to M8 units)
   for (int h0 = 0; h0 < M; h0 += 4) {
     cpx<R> th[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int h = h0 + u;
-      th[u] = h < M ? (theta_in_g ? gout[(size_t)h * Ns + s] : s_b[h]) : mk(R(0), R(0));
+      th[u] = theta_in_g ? (h < M ? gout[(size_t)h * Ns + s] : mk(R(0), R(0))) : s_b[h];
     }
     if (!theta_in_g) {
       for (int j = 0; j < N; ++j) {
         const R v = site_value<R>(bits, j, hilb);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (h0 + u < M) {
-            const cpx<R> w = s_W[h0 + u + M * j];
-            th[u].x += w.x * v;
-            th[u].y += w.y * v;
-          }
+        for (int u = 0; u < 4; ++u) {
+          const cpx<R> w = s_W[h0 + u + M8 * j];
+          th[u].x += w.x * v;
+          th[u].y += w.y * v;
+        }
       }
     }
 #pragma unroll
@@ -244,7 +247,7 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
             int site = __ldg(op.conn_change_site + 8 * c + q);
             R nv = (R)__ldg(op.conn_change_value + 8 * c + q);
             R dv = nv - site_value<R>(bits, site, hilb);
-            cpx<R> w = s_W[h + M * site];
+            cpx<R> w = s_W[h + M8 * site];
             dth.x += w.x * dv;
             dth.y += w.y * dv;
           }
@@ -273,7 +276,7 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
 }
 
 template <typename R, int ACT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, DevOp op,
                 int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
                 cpx<R>* __restrict__ eloc, int theta_in_g) {
@@ -538,9 +541,9 @@ cudaError_t launch_rbm_tables(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<
   return cudaGetLastError();
 }
 
-static int eval_threads(int M, size_t csize) {
+static int eval_threads(int M, size_t csize, int Tmax = 128) {
   const size_t M8 = (size_t)(M + 7) & ~(size_t)7;
-  int T = 128;
+  int T = Tmax;
   while (T > 32 && M8 * T * csize > 96 * 1024) T /= 2;
   return T;
 }
@@ -548,11 +551,12 @@ static int eval_threads(int M, size_t csize) {
 template <typename R>
 cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int Ns, const DevOp* op,
                             cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc, cudaStream_t st, int theta_in_g) {
-  const int T = eval_threads(net.M, sizeof(cpx<R>));
+  // up to 256 threads: the per-thread slices of g bound the occupancy, the
+  // shared tables are amortised over more samples
+  const int T = eval_threads(net.M, sizeof(cpx<R>), 256);
   const int has_op = op != nullptr && eloc != nullptr;
   const size_t M8 = (size_t)(net.M + 7) & ~(size_t)7;
-  size_t smem = ((size_t)net.M * net.N + net.M + net.N + M8 * T + (has_op ? 2 * (size_t)net.N * M8 : 0)) *
-                sizeof(cpx<R>);
+  size_t smem = (M8 * net.N + M8 + net.N + M8 * T + (has_op ? 2 * (size_t)net.N * M8 : 0)) * sizeof(cpx<R>);
   DevOp dop;
   if (has_op) dop = *op;
   const int blocks = (Ns + T - 1) / T;
@@ -580,7 +584,7 @@ template <typename R>
 cudaError_t launch_rbm_eval_batch(const EvalJob<R>* jobs, const int* blk_start, int np, int total_blocks,
                                   int M_max, int N_max, int act, int T, cudaStream_t st) {
   const size_t M8 = (size_t)(M_max + 7) & ~(size_t)7;
-  const size_t smem = ((size_t)M_max * N_max + M_max + N_max + M8 * T + 2 * (size_t)N_max * M8) * sizeof(cpx<R>);
+  const size_t smem = (M8 * N_max + M8 + N_max + M8 * T + 2 * (size_t)N_max * M8) * sizeof(cpx<R>);
   if (act == ACT_LOGCOSH) {
     auto kern = rbm_eval_batch_kernel<R, ACT_LOGCOSH>;
     if (smem > 48 * 1024) {
