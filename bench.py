@@ -130,6 +130,9 @@ def s_precision_choice():
 # DRAM bytes (read + write) of one gram_tf32_kernel launch on this workload, from
 # the ncu capture summarised in profiles/gram_tf32_c1.txt
 GRAM_TRAFFIC_BYTES = 701.59e6
+# warp instructions of one production launch of the Metropolis kernel on this
+# workload (ncu smsp__inst_executed.sum, profiles/rbm_sampler_c1.txt)
+SAMPLER_WARP_INSTRUCTIONS = 526.8e6
 
 
 def effective_samples_per_s(loc, sample_ms):
@@ -221,6 +224,17 @@ def run_gb300(args, barrier=None):
     roof["kernel_ms"] = kernels
     roof["dominant_kernel"] = max(kernels, key=kernels.get)
     roof["share_of_three"] = {k: v / ksum for k, v in kernels.items()}
+    # the sampler, the largest share, moves no HBM bytes and uses no tensor
+    # core: its bound is the instruction issue rate of 152 SMs x 4 schedulers
+    clk_sum = clk.summary()
+    sm_ghz = (clk_sum.get("sm_mhz") or 2070.0) / 1000.0
+    issue_peak = 152 * 4 * sm_ghz * 1e9
+    roof["sampler_issue_bound"] = {
+        "bound": "instruction issue", "warp_instructions_per_launch": SAMPLER_WARP_INSTRUCTIONS,
+        "achieved": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3), "peak": issue_peak,
+        "unit": "warp instructions/s", "frac": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3) / issue_peak,
+        "note": "instruction count from one ncu capture of this workload's launch (profiles/rbm_sampler_c1.txt), "
+                "time from the live CUDA events; HBM traffic of the launch: 62 KB"}
 
     line = {
         "metric": METRIC, "value": value, "unit": "SR steps/s", "n_gpus": args.gpus,
