@@ -485,9 +485,23 @@ def learned_vs_local():
 # --------------------------------------------------------------------------
 def cpu_baseline(max_seconds=20.0, chains=None):
     """Times the oracle's restatement of one reference VMC iteration on a
-    bounded number of chains and scales to the full workload."""
+    bounded number of chains and scales to the full workload, on all host
+    cores and, in a separate process limited to one thread (OpenMP and
+    BLAS), on one core."""
     from oracle import cport
-    return cport.time_baseline(WORKLOAD, max_seconds=max_seconds, chains=chains)
+    res = cport.time_baseline(WORKLOAD, max_seconds=max_seconds, chains=chains)
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    code = ("import json; from oracle import cport; "
+            f"w = json.loads({json.dumps(json.dumps(WORKLOAD))}); "
+            f"print(json.dumps(cport.time_baseline(w, max_seconds={max_seconds / 2!r}, quiet=True)))")
+    try:
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                             timeout=max(120.0, 6 * max_seconds), cwd=os.path.dirname(os.path.abspath(__file__)))
+        one = json.loads(out.stdout.strip().splitlines()[-1])
+        res["single_core"] = {"value": one["value"], "unit": one["unit"], "cores": 1, "sample": one["sample"]}
+    except (subprocess.SubprocessError, ValueError, IndexError, KeyError) as e:
+        res["single_core"] = {"unavailable": f"{type(e).__name__}"}
+    return res
 
 
 def run_reference(args):
