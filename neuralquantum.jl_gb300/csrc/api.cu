@@ -449,6 +449,11 @@ nq_status upload_op(nq_handle* h, const nq_op_table* t, DevOp* out, std::vector<
   if ((s = upload(h, t->op_row_offset, t->n_ops, &d.op_row_offset, allocs)) != NQ_OK) return s;
   if ((s = upload(h, t->row_conn_offset, (size_t)t->n_rows + 1, &d.row_conn_offset, allocs)) != NQ_OK) return s;
   if ((s = upload(h, t->conn_mel, 2 * (size_t)t->n_conns, &d.conn_mel, allocs)) != NQ_OK) return s;
+  {
+    std::vector<float2> mf(std::max(1, t->n_conns));
+    for (int c = 0; c < t->n_conns; ++c) mf[c] = make_float2((float)t->conn_mel[2 * c], (float)t->conn_mel[2 * c + 1]);
+    if ((s = upload(h, (const float2*)mf.data(), mf.size(), &d.conn_mel_f, allocs)) != NQ_OK) return s;
+  }
   if ((s = upload(h, t->conn_n_changes, (size_t)t->n_conns, &d.conn_n_changes, allocs)) != NQ_OK) return s;
   if ((s = upload(h, t->conn_change_site, 8 * (size_t)t->n_conns, &d.conn_change_site, allocs)) != NQ_OK) return s;
   if ((s = upload(h, (const signed char*)t->conn_change_value, 8 * (size_t)t->n_conns, &d.conn_change_value,

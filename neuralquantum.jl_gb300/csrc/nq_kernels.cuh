@@ -12,6 +12,7 @@ struct DevOp {
   const int* op_row_offset = nullptr;   // [n_ops]
   const int* row_conn_offset = nullptr; // [n_rows+1]
   const double* conn_mel = nullptr;     // [2*n_conns]
+  const float2* conn_mel_f = nullptr;   // [n_conns] the same elements in FP32 (FP32 estimators)
   const int* conn_n_changes = nullptr;  // [n_conns]
   const int* conn_change_site = nullptr;// [8*n_conns]
   const signed char* conn_change_value = nullptr; // [8*n_conns]

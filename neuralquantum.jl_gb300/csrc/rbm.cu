@@ -7,6 +7,8 @@
 // (sampler), src/IterativeInterface/Accumulators/AccumulatorObsScalar.jl:52-137
 // (estimator), src/IterativeInterface/Samplers/CostFun/BatchedValSampler.jl:97-115
 // and BaseIterativeSampler.jl:19-26 (centring and force).
+#include <type_traits>
+
 #include "nq_kernels.cuh"
 
 namespace {
@@ -195,9 +197,14 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
     const int row = __ldg(op.op_row_offset + o) + r;
     const int c0 = __ldg(op.row_conn_offset + row), c1 = __ldg(op.row_conn_offset + row + 1);
     for (int c = c0; c < c1; ++c) {
-      const double mre = __ldg(op.conn_mel + 2 * c), mim = __ldg(op.conn_mel + 2 * c + 1);
-      if (mre == 0.0 && mim == 0.0) continue;
-      const cpx<R> mel = mk((R)mre, (R)mim);
+      cpx<R> mel;
+      if constexpr (std::is_same<R, float>::value) {
+        const float2 m = __ldg(op.conn_mel_f + c);       // FP32 copy: no FP64 compare or conversion
+        mel = mk(m.x, m.y);
+      } else {
+        mel = mk((R)__ldg(op.conn_mel + 2 * c), (R)__ldg(op.conn_mel + 2 * c + 1));
+      }
+      if (mel.x == R(0) && mel.y == R(0)) continue;
       const int nch = __ldg(op.conn_n_changes + c);
       if (nch == 0) { E = E + mel; continue; }
       // exp(aᵀΔσ)
