@@ -451,8 +451,30 @@ nq_status upload_op(nq_handle* h, const nq_op_table* t, DevOp* out, std::vector<
   if ((s = upload(h, t->conn_mel, 2 * (size_t)t->n_conns, &d.conn_mel, allocs)) != NQ_OK) return s;
   {
     std::vector<float2> mf(std::max(1, t->n_conns));
-    for (int c = 0; c < t->n_conns; ++c) mf[c] = make_float2((float)t->conn_mel[2 * c], (float)t->conn_mel[2 * c + 1]);
+    std::vector<int4> cp(std::max(1, t->n_conns));
+    for (int c = 0; c < t->n_conns; ++c) {
+      mf[c] = make_float2((float)t->conn_mel[2 * c], (float)t->conn_mel[2 * c + 1]);
+      int4 q;
+      memcpy(&q.x, &mf[c].x, 4);
+      memcpy(&q.y, &mf[c].y, 4);
+      q.z = t->conn_n_changes[c];
+      q.w = q.z > 0 ? ((t->conn_change_site[8 * c] & 0xff) | ((int)(unsigned char)t->conn_change_value[8 * c] << 8))
+                    : 0;
+      cp[c] = q;
+    }
     if ((s = upload(h, (const float2*)mf.data(), mf.size(), &d.conn_mel_f, allocs)) != NQ_OK) return s;
+    if ((s = upload(h, (const int4*)cp.data(), cp.size(), &d.conn_pack, allocs)) != NQ_OK) return s;
+    std::vector<int4> om(std::max(1, t->n_ops));
+    for (int o = 0; o < t->n_ops; ++o) {
+      int lo = 0, hi = 0;
+      for (int k = 0; k < t->op_n_sites[o]; ++k) {
+        const int site = t->op_sites[8 * o + k] & 0xff;
+        if (k < 4) lo |= site << (8 * k);
+        else hi |= site << (8 * (k - 4));
+      }
+      om[o] = make_int4(t->op_n_sites[o], t->op_row_offset[o], lo, hi);
+    }
+    if ((s = upload(h, (const int4*)om.data(), om.size(), &d.op_meta, allocs)) != NQ_OK) return s;
   }
   if ((s = upload(h, t->conn_n_changes, (size_t)t->n_conns, &d.conn_n_changes, allocs)) != NQ_OK) return s;
   if ((s = upload(h, t->conn_change_site, 8 * (size_t)t->n_conns, &d.conn_change_site, allocs)) != NQ_OK) return s;

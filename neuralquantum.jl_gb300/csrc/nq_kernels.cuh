@@ -13,6 +13,12 @@ struct DevOp {
   const int* row_conn_offset = nullptr; // [n_rows+1]
   const double* conn_mel = nullptr;     // [2*n_conns]
   const float2* conn_mel_f = nullptr;   // [n_conns] the same elements in FP32 (FP32 estimators)
+  // packed copies for the RBM estimator's walk (one load per operator / connection):
+  // op_meta[o] = {n_sites, row_offset, sites 0-3, sites 4-7} (one byte per site);
+  // conn_pack[c] = {FP32 mel re, FP32 mel im (bit patterns), n_changes,
+  //                 first changed site | (its new value as a byte) << 8}
+  const int4* op_meta = nullptr;        // [n_ops]
+  const int4* conn_pack = nullptr;      // [n_conns]
   const int* conn_n_changes = nullptr;  // [n_conns]
   const int* conn_change_site = nullptr;// [8*n_conns]
   const signed char* conn_change_value = nullptr; // [8*n_conns]

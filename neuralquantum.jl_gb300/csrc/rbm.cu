@@ -188,31 +188,31 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
   const R dmag = hilb == HILB_SPIN ? R(2) : R(1);
   cpx<R> E = mk(R(0), R(0));
   for (int o = 0; o < op.n_ops; ++o) {
-    const int ns_o = __ldg(op.op_n_sites + o);
+    const int4 om = __ldg(op.op_meta + o);             // {n_sites, row_offset, sites 0-3, sites 4-7}
     int r = 0;
-    for (int d = 0; d < ns_o; ++d) {
-      int site = __ldg(op.op_sites + 8 * o + d);
+    for (int d = 0; d < om.x; ++d) {
+      const int site = ((d < 4 ? om.z : om.w) >> (8 * (d & 3))) & 0xff;
       r |= (int)((bits >> site) & 1ull) << d;
     }
-    const int row = __ldg(op.op_row_offset + o) + r;
+    const int row = om.y + r;
     const int c0 = __ldg(op.row_conn_offset + row), c1 = __ldg(op.row_conn_offset + row + 1);
     for (int c = c0; c < c1; ++c) {
+      const int4 cp = __ldg(op.conn_pack + c);          // {mel re, mel im, n_changes, first change}
       cpx<R> mel;
       if constexpr (std::is_same<R, float>::value) {
-        const float2 m = __ldg(op.conn_mel_f + c);       // FP32 copy: no FP64 compare or conversion
-        mel = mk(m.x, m.y);
+        mel = mk(__int_as_float(cp.x), __int_as_float(cp.y));   // FP32 copy: no FP64 compare or conversion
       } else {
         mel = mk((R)__ldg(op.conn_mel + 2 * c), (R)__ldg(op.conn_mel + 2 * c + 1));
       }
       if (mel.x == R(0) && mel.y == R(0)) continue;
-      const int nch = __ldg(op.conn_n_changes + c);
+      const int nch = cp.z;
       if (nch == 0) { E = E + mel; continue; }
       // exp(aᵀΔσ)
       cpx<R> aexp = mk(R(0), R(0));
       int i1 = -1; R dv1 = 0;
       for (int q = 0; q < nch; ++q) {
-        int site = __ldg(op.conn_change_site + 8 * c + q);
-        R nv = (R)__ldg(op.conn_change_value + 8 * c + q);
+        const int site = q == 0 ? (cp.w & 0xff) : __ldg(op.conn_change_site + 8 * c + q);
+        const R nv = q == 0 ? (R)(signed char)((cp.w >> 8) & 0xff) : (R)__ldg(op.conn_change_value + 8 * c + q);
         R dv = nv - site_value<R>(bits, site, hilb);
         aexp.x += s_a[site].x * dv;
         aexp.y += s_a[site].y * dv;
