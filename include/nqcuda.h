@@ -108,7 +108,8 @@ typedef enum {
 
 /* Precision of the S = O_c O_c† accumulation. */
 typedef enum {
-  NQ_S_F32 = 0,            /* FP32 CUDA cores */
+  NQ_S_F32 = 0,            /* FP32 accuracy: 3xTF32 on tcgen05 when X and its low part fit 16 GB,
+                              else FP32 CUDA cores (no X buffers) */
   NQ_S_TF32 = 1,           /* tcgen05 kind::tf32, FP32 accumulate */
   NQ_S_TF32X3 = 2,         /* tcgen05 kind::tf32 with hi/lo split (3 products) */
   NQ_S_F64 = 3,            /* FP64 CUDA cores (not provided) */
@@ -255,6 +256,19 @@ nq_status nq_sample(nq_handle* h, uint64_t call_index, int8_t* samples_out,
                     uint8_t* accept_bits);
 /* Replace the sample buffer (N x B x L int8), e.g. to evaluate given states. */
 nq_status nq_set_samples(nq_handle* h, const int8_t* samples);
+/* Read the current sample buffer (N x B x L int8, doubled: 2N x B x L): the
+ * samples of the last nq_sample / nq_vmc_step / batched step, or of
+ * nq_set_samples.  The reference keeps them in the sampler's `samples` field
+ * (BaseIterativeSampler.jl:5-17) for the user to read. */
+nq_status nq_get_samples(nq_handle* h, int8_t* samples_out);
+/* Read the results of the last estimate and solve on this handle without
+ * recomputing anything (all outputs nullable): loc_out B x L complex128 local
+ * values, force_out P values and dw_out P values (complex128, real
+ * parameters float64) of the force F and the update Δw.  After a batched step
+ * (nq_batch_vmc_step) they are that step's values for this problem.  The
+ * reference holds the same quantities in its accumulator and SR cache
+ * (BatchedValSampler.jl:117-139, SRDirect.jl:51-90). */
+nq_status nq_get_estimates(nq_handle* h, double* loc_out, double* force_out, double* dw_out);
 
 /* ---- logψ! / logψ_and_∇logψ! on arbitrary host batches --------------------
  * sigma: n configurations, int8, column-major (N x n; doubled: row block
@@ -290,16 +304,26 @@ nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
 /* Iterative SR settings (NQ_SR_CG): relative residual tolerance |r|/|F|
  * (SR(precision=...), default 1e-4) and the iteration cap (default 10 P as
  * SRIterative.jl:99).  nq_sr_info returns [iterations, |r|/|F|] of the last
- * iterative solve. */
+ * iterative solve; for the direct solve (NQ_SR_DIRECT) it returns
+ * [FP64-residual corrections, |Δx|/|x| of the last correction] of the last
+ * single-problem solve (the corrections stop below 1e-13 |x|, at most 12). */
 nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter);
 nq_status nq_sr_info(nq_handle* h, double* out2);
+/* Limit, in nanoseconds, of every grid-barrier wait in this handle's SR solve
+ * kernels (the cooperative inversion, the refinement and the conjugate
+ * gradients; 0 restores the default of 1 s).  A wait that runs out ends its
+ * kernel early and the call reports NQ_ERR_TIMEOUT; the handle stays usable.
+ * No counterpart in the reference (its solve runs on the host). */
+nq_status nq_set_wait_limit(nq_handle* h, uint64_t limit_ns);
 
 /* ---- precondition!(prec, SR, iter) ----------------------------------------
  * kind: 0 = sr_shift (S_ii += eps), 1 = sr_multiplicative
  * (S + max(lam0*b^iter, lam_min) diag S), 2 = sr_none.  The reference's
  * Cholesky solve of S Δw = F becomes an FP32 inverse of the shifted S (block
- * Gauss–Jordan) with FP64-residual refinement.  dw_out (nullable) receives Δw
- * (complex128 or float64). */
+ * Gauss–Jordan) with FP64-residual refinement iterated until the correction
+ * is below 1e-13 of Δw: Δw solves the FP64 system.  dw_out (nullable)
+ * receives Δw (complex128 or float64).  NQ_ERR_NOT_PD: a non-positive pivot
+ * (the shifted S is not positive definite); NQ_ERR_NAN: non-finite Δw. */
 nq_status nq_precondition(nq_handle* h, int32_t kind, double eps, double lam0,
                           double b, double lam_min, int32_t iter, double* dw_out);
 
@@ -427,14 +451,16 @@ nq_status nq_proposal_stats(nq_handle* h, uint64_t* out2);
  *   stream   : cudaStream_t the two kernels are queued on (NULL = default);
  *              the call returns without waiting for them.
  *   err      : optional buffer for a message when the status is not NQ_OK.
- * Limit: n_chains <= NQ_NOALLOC_MAX_CHAINS.  The per-chain scratch (3 doubles
- * per chain, 1.5 MiB) is one fixed device array shared by every call on a
- * device; nothing in it needs to start at zero.  Calls whose kernels can
- * overlap in time (different streams, or several host threads) race on that
- * array: order them on one stream or with events.  The first call on each
- * device looks the array's address up once (cudaGetSymbolAddress), which may
- * load the library's device code on that device; make that first call before
- * any stream capture begins. */
+ * Limit: n_chains <= NQ_NOALLOC_MAX_CHAINS.  The scratch (5 doubles per
+ * block of 64 chains: 40 KiB at the limit) is one fixed device array, held
+ * by every device that loads the library until the process exits, and shared
+ * by every call on a device; nothing in it needs to start at zero.  Calls
+ * whose kernels can overlap in time (different streams, or several host
+ * threads) race on that array: order them on one stream or with events.  The
+ * first call on each device (and again after the device's context was reset)
+ * looks the array's address up (cudaGetSymbolAddress), which may load the
+ * library's device code on that device; make that first call before any
+ * stream capture begins. */
 #define NQ_NOALLOC_MAX_CHAINS 65536
 nq_status nq_measurement_noalloc(const void* d_values, int32_t dtype, int32_t n_chains,
                                  int32_t chain_length, int32_t kind, double* d_out6, void* stream,

@@ -7,7 +7,14 @@ namespace {
 
 // FP64-residual corrections after the first solve with the FP32 inverse; each
 // gains about -log10(cond(S + shift) * 6e-8) digits
-constexpr int kSolveRefine = 3;
+// FP64-residual corrections of the shifted solve: at most kSolveRefine in the
+// single-problem cooperative refinement (it stops once a correction is below
+// kRefineTol of the solution), exactly kSolveRefineBatch in the many-problem
+// step's per-problem graph branches
+constexpr int kSolveRefine = 12;
+// largest X + Xlo (bytes) for which an NQ_S_F32 request runs as 3xTF32 on tcgen05
+constexpr double kSf32TensorBytes = 16e9;
+constexpr int kSolveRefineBatch = 5;
 
 
 template <typename R>
@@ -368,8 +375,10 @@ nq_status check_status_word(nq_handle* h) {
   if (st != 0) {
     CK(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st));
     CK(cudaStreamSynchronize(h->st));
-    if (st & 0x10) return fail(h, NQ_ERR_TIMEOUT, "a bounded device-side wait gave up (status 0x%x)", st);
-    return fail(h, NQ_ERR_NOT_PD, "SR matrix is not positive definite after the diagonal shift");
+    if (st & NQ_DEVERR_TIMEOUT) return fail(h, NQ_ERR_TIMEOUT, "a bounded device-side wait gave up (status 0x%x)", st);
+    if (st & 1) return fail(h, NQ_ERR_NOT_PD, "SR matrix is not positive definite after the diagonal shift");
+    if (st & NQ_DEVERR_NONFINITE) return fail(h, NQ_ERR_NAN, "the SR solve produced a non-finite update");
+    return fail(h, NQ_ERR_CUDA, "device status word 0x%x", st);
   }
   return NQ_OK;
 }
@@ -701,7 +710,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   step(dalloc(&h->fb.force, 2 * (size_t)P), "force");
   step(dalloc(&h->fb.meanE, 2), "meanE");
   step(dalloc(&h->d_stats, 8), "stats");
-  step(dalloc(&h->d_chainstats, 3 * (size_t)h->B + 4), "chain stats");
+  step(dalloc(&h->d_chainstats, stats_scratch_doubles(h->B)), "chain stats");
   step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
   h->cg = c.sr_algorithm == NQ_SR_CG;
   h->exact = c.sampler_kind == NQ_SAMPLER_EXACT;
@@ -711,6 +720,14 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   const bool sr_bufs = !h->cg && !h->diag;
   const int rows = 2 * P;
   const int rp = ((rows + 127) / 128) * 128;
+  // NQ_S_F32 asks for S with FP32 accuracy.  Where the tensor-core Gram is
+  // available and X with its low part fits kSf32TensorBytes, S is accumulated
+  // as 3xTF32 on tcgen05 (hi/lo split, FP32-level error); otherwise in FP32 on
+  // CUDA cores, which needs no X buffers.
+  if (sr_bufs && c.s_precision == NQ_S_F32 && gram_tc_supported() &&
+      2.0 * rows * (double)(((h->Ns + 127) / 128) * 128) * sizeof(float) <= kSf32TensorBytes)
+    h->cfg.s_precision = NQ_S_TF32X3;
+  const int s_prec = h->cfg.s_precision;
   if (h->cg) {
     // matrix-free SR: O(P) vectors and per-CTA partials only
     const int G = sr_cg_grid();
@@ -746,15 +763,15 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   if (sr_bufs) step(dalloc(&h->d_G, (size_t)rows * rows), "G");
   if (sr_bufs) step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
   if (!sr_bufs) {
-  } else if (c.s_precision == NQ_S_TF32 || c.s_precision == NQ_S_TF32X3 || c.s_precision == NQ_S_BF16) {
-    const int bf16 = c.s_precision == NQ_S_BF16 ? 1 : 0;
+  } else if (s_prec == NQ_S_TF32 || s_prec == NQ_S_TF32X3 || s_prec == NQ_S_BF16) {
+    const int bf16 = s_prec == NQ_S_BF16 ? 1 : 0;
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad, bf16);
     cudaFree(h->d_Gpart);
     h->d_Gpart = nullptr;
     step(dalloc(&h->d_Gpart, gram_tc_partial_elems(rows, h->Ns_pad, bf16)), "G partial");
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad / (bf16 ? 2 : 1)), "X");     // BF16 X: half the bytes
-    if (c.s_precision == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
+    if (s_prec == NQ_S_TF32X3) step(dalloc(&h->d_Xlo, (size_t)rows * h->Ns_pad), "Xlo");
   } else if (h->ndm || h->chain) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
@@ -769,6 +786,8 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
     step(cudaMalloc(&h->sb.ctl, sweep_ctl_bytes()), "sweep ctl");
     step(dalloc(&h->sb.work, sweep_work_elems(P)), "sweep work");
     step(dalloc(&h->sb.yf, (size_t)P), "yf");
+    step(dalloc(&h->sb.norms, refine_norm_doubles()), "refinement norms");
+    step(dalloc(&h->sb.info, 2), "refinement info");
   }
   if (h->diag) step(dalloc(&h->sb.status, 1), "status");
   if (h->tc_theta) step(dalloc(&h->d_theta_img, theta_tc_image_elems(h->M, h->theta_terms)), "theta image");
@@ -819,7 +838,7 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->d_theta_img, h->d_exact, h->d_pairs, h->d_xtab[0],
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->sb.norms, h->sb.info, h->d_theta_img, h->d_exact, h->d_pairs, h->d_xtab[0],
                   h->d_xtab[1], h->d_xtab[2], h->d_xW, h->d_xare, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial,
                   h->d_diag[0], h->d_diag[1], h->d_diag[2], h->d_bare, h->d_perms};
@@ -1161,7 +1180,7 @@ nq_status nq_observable(nq_handle* h, const nq_op_table* obs, nq_measurement* st
   nq_status s = upload_op(h, obs, &d, &allocs);
   if (s != NQ_OK) return cleanup(s);
   if (cudaMalloc(&d_lp, (size_t)h->Ns * csz) != cudaSuccess || cudaMalloc(&d_loc, (size_t)h->Ns * csz) != cudaSuccess ||
-      cudaMalloc((void**)&d_cs, ((size_t)h->B * 3 + 4) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&d_cs, stats_scratch_doubles(h->B) * sizeof(double)) != cudaSuccess ||
       cudaMalloc((void**)&d_st, 8 * sizeof(double)) != cudaSuccess)
     return cleanup(fail(h, NQ_ERR_CUDA, "observable buffers"));
   cudaError_t e;
@@ -1260,6 +1279,46 @@ nq_status nq_set_samples(nq_handle* h, const int8_t* samples) {
   return NQ_OK;
 }
 
+nq_status nq_get_samples(nq_handle* h, int8_t* samples_out) {
+  if (!h || !samples_out) return NQ_ERR_ARG;
+  signed char* d_v = nullptr;
+  CK(cudaMalloc(&d_v, (size_t)h->Ns * h->nst));
+  ++h->launches;
+  CK(launch_unpack_int8(h->d_samples, h->nst, h->Ns, h->hilb, d_v, h->st));
+  CK(cudaMemcpyAsync(samples_out, d_v, (size_t)h->Ns * h->nst, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  cudaFree(d_v);
+  return NQ_OK;
+}
+
+nq_status nq_get_estimates(nq_handle* h, double* loc_out, double* force_out, double* dw_out) {
+  if (!h) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_get_estimates");
+  CK(cudaStreamSynchronize(h->st));
+  if (loc_out) {
+    const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
+    std::vector<char> buf((size_t)h->Ns * csz);
+    CK(cudaMemcpy(buf.data(), h->d_eloc, buf.size(), cudaMemcpyDeviceToHost));
+    if (h->f64) memcpy(loc_out, buf.data(), buf.size());
+    else {
+      const float* f = (const float*)buf.data();
+      for (size_t i = 0; i < 2 * (size_t)h->Ns; ++i) loc_out[i] = f[i];
+    }
+  }
+  double* srcs[2] = {h->fb.force, h->cg ? h->cga.x : h->sb.x};
+  double* outs[2] = {force_out, dw_out};
+  for (int k = 0; k < 2; ++k) {
+    if (!outs[k]) continue;
+    if (!srcs[k]) return fail(h, NQ_ERR_STATE, "no %s buffer on this handle", k ? "update" : "force");
+    std::vector<double> f(2 * (size_t)h->P);
+    CK(cudaMemcpy(f.data(), srcs[k], f.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->complex_params) memcpy(outs[k], f.data(), f.size() * sizeof(double));
+    else
+      for (int i = 0; i < h->P; ++i) outs[k][i] = f[2 * i];
+  }
+  return NQ_OK;
+}
+
 static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, double* out, double* grad) {
   if (!h || !sigma || !out || n < 1) return NQ_ERR_ARG;
   if (h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
@@ -1348,6 +1407,8 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, doub
   h->stage_ms[3] = elapsed_ms(h->ev[3], h->ev[4]);
   h->stage_ms[7] = elapsed_ms(h->kev[2], h->kev[3]);
   fill_measurement(h, stats);
+  if (!std::isfinite(h->h_stats[0]) || !std::isfinite(h->h_stats[1]))
+    return fail(h, NQ_ERR_NAN, "non-finite local estimator mean");
   const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
   if (loc_out) {
     std::vector<char> buf((size_t)h->Ns * csz);
@@ -1368,6 +1429,15 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, doub
   return NQ_OK;
 }
 
+nq_status nq_set_wait_limit(nq_handle* h, uint64_t limit_ns) {
+  if (!h) return NQ_ERR_ARG;
+  const uint64_t v = limit_ns ? limit_ns : kNqWaitNs;
+  h->sb.wait_ns = v;
+  h->cga.wait_ns = v;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NQ_OK;
+}
+
 nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter) {
   if (!h || !(tol > 0.0) || maxiter < 1) return NQ_ERR_ARG;
   h->cg_tol = tol;
@@ -1378,8 +1448,11 @@ nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter) {
 
 nq_status nq_sr_info(nq_handle* h, double* out2) {
   if (!h || !out2) return NQ_ERR_ARG;
-  if (!h->cg) return fail(h, NQ_ERR_STATE, "the handle uses the direct SR solve");
-  CK(cudaMemcpyAsync(h->h_cginfo, h->cga.info, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  NQ_REJECT_DIAG(h, "nq_sr_info");
+  if (!h->h_cginfo) CK(cudaMallocHost((void**)&h->h_cginfo, 2 * sizeof(double)));
+  const double* src = h->cg ? h->cga.info : h->sb.info;
+  if (!src) return fail(h, NQ_ERR_STATE, "no SR solve on this handle");
+  CK(cudaMemcpyAsync(h->h_cginfo, src, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   out2[0] = h->h_cginfo[0];
   out2[1] = h->h_cginfo[1];
@@ -1482,8 +1555,10 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
   CK(cudaMemcpyAsync(h->h_acc, h->d_accepted, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   nq_status s = check_status_word(h);
-  if (s != NQ_OK) return s;
   fill_measurement(h, stats);
+  if (s != NQ_OK) return s;
+  if (!std::isfinite(h->h_stats[0]) || !std::isfinite(h->h_stats[1]))
+    return fail(h, NQ_ERR_NAN, "non-finite local estimator mean");
   return NQ_OK;
 }
 
@@ -1773,9 +1848,9 @@ nq_status batch_capture(nq_batch* b, double eps, double lr) {
     nq_handle* h = b->hs[p];
     ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch 2");
     if (s == NQ_OK) {
-      ck(launch_sr_finish(h->sb, h->P, h->fb.force, 0, eps, 0.0, !h->complex_params, kSolveRefine, h->st),
+      ck(launch_sr_finish(h->sb, h->P, h->fb.force, 0, eps, 0.0, !h->complex_params, kSolveRefineBatch, h->st),
          "solve");
-      h->launches += 2 + 3 * (kSolveRefine + 1);
+      h->launches += 2 + 3 * (kSolveRefineBatch + 1);
     }
     if (s == NQ_OK) s = stage_update(h, lr);
     ck(cudaEventRecord(b->join[p], h->st), "join 2");

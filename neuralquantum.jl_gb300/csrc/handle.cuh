@@ -63,7 +63,7 @@ struct nq_handle {
   ForceBufs fb;
   int force_nblk = 0;
   double* d_stats = nullptr;       // 6 doubles
-  double* d_chainstats = nullptr;  // [B][3] chain mean (re, im) and variance
+  double* d_chainstats = nullptr;  // statistics block summaries, stats_scratch_doubles(B)
   float* d_G = nullptr;
   float* d_Gpart = nullptr;
   int gram_ksplit = 1;

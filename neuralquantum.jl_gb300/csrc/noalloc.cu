@@ -14,14 +14,52 @@ namespace {
 constexpr int kMaxChains = NQ_NOALLOC_MAX_CHAINS;
 constexpr int kMaxDevices = 64;
 
-// Scratch of the statistics kernels (4 doubles per 64 chains; sized by the
-// 3B + 4 bound that launch_stats documents, 1.5 MiB per device).  Every word
-// a call reads is written earlier in the same call, so nothing has to start
-// at zero.
-static __device__ __align__(256) double g_chain_scratch[3 * kMaxChains];
+// Scratch of the statistics kernels: the per-block summaries of launch_stats
+// (5 doubles per block of 64 chains), 40 KiB per device at the maximum chain
+// count.  Every word a call reads is written earlier in the same call, so
+// nothing has to start at zero.
+constexpr size_t kScratchDoubles = stats_scratch_doubles(kMaxChains);
+static_assert(kScratchDoubles == 5 * ((kMaxChains + 63) / 64), "scratch follows launch_stats' block layout");
+static __device__ __align__(256) double g_chain_scratch[kScratchDoubles];
 
+// Device address of g_chain_scratch, looked up once per device and context.
+// The address belongs to the module loaded in the device's current context:
+// after cudaDeviceReset (or any teardown of the primary context) the module is
+// loaded again and the symbol may move, so the cache is keyed by the context's
+// unique id (cuCtxGetId, reached through the runtime's driver entry points);
+// without that entry point the address is looked up on every call.
+struct ScratchSlot {
+  unsigned long long ctx_id = 0;
+  double* ptr = nullptr;
+};
 std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
+ScratchSlot g_slot[kMaxDevices];
+
+typedef int (*PFN_ctx_get_current)(void** ctx);
+typedef int (*PFN_ctx_get_id)(void* ctx, unsigned long long* id);
+
+bool current_context_id(unsigned long long* id) {
+  static PFN_ctx_get_current get_current = nullptr;
+  static PFN_ctx_get_id get_id = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_ctx_get_current>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_ctx_get_id>(p);
+    cudaGetLastError();
+  }
+  if (!get_current || !get_id) return false;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx) return false;
+  return get_id(ctx, id) == 0;
+}
 
 void set_err(char* err, size_t len, const char* msg) {
   if (err && len > 0) snprintf(err, len, "%s", msg);
@@ -85,7 +123,10 @@ extern "C" nq_status nq_measurement_noalloc(const void* d_values, int32_t dtype,
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    unsigned long long ctx_id = 0;
+    const bool have_id = current_context_id(&ctx_id);
+    ScratchSlot& slot = g_slot[dev];
+    if (!have_id || !slot.ptr || slot.ctx_id != ctx_id) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_chain_scratch);
       if (e != cudaSuccess) {
@@ -93,9 +134,10 @@ extern "C" nq_status nq_measurement_noalloc(const void* d_values, int32_t dtype,
         set_err(err, err_len, msg);
         return NQ_ERR_CUDA;
       }
-      g_scratch_ptr[dev] = static_cast<double*>(p);
+      slot.ptr = static_cast<double*>(p);
+      slot.ctx_id = have_id ? ctx_id : 0;
     }
-    scratch = g_scratch_ptr[dev];
+    scratch = slot.ptr;
   }
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (dtype == NQ_DTYPE_C64)

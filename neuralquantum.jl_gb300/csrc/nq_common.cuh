@@ -8,6 +8,14 @@
 #define NQ_HD __host__ __device__ __forceinline__
 #define NQ_D __device__ __forceinline__
 
+// Bits of a handle's device status word beyond the solve's non-positive pivot
+// (bit 0): a bounded wait gave up (host: NQ_ERR_TIMEOUT); the solve produced
+// a non-finite update (host: NQ_ERR_NAN).
+#define NQ_DEVERR_TIMEOUT 0x10
+#define NQ_DEVERR_NONFINITE 0x20
+// Default limit of a bounded device-side wait.
+constexpr uint64_t kNqWaitNs = 1000000000ull;
+
 // ---------------------------------------------------------------------------
 // complex numbers as (re, im) pairs, templated on the real type
 // ---------------------------------------------------------------------------

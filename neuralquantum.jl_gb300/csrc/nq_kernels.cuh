@@ -259,13 +259,20 @@ NQ_D double sr_diag_shift(const double* S, int P, int i, int kind, double eps, d
   if (kind == 1) return lam * S[2 * ((size_t)i + (size_t)P * i)];
   return 0.0;
 }
-// the FP64-residual refinement of launch_sr_finish (x0 = A⁻¹F, then `iters`
-// corrections, last residual in r) as one cooperative launch; ctl: sweep_ctl_bytes()
+// the FP64-residual refinement (x0 = A⁻¹F, then corrections until
+// |Δx| <= tol |x| or max_corr of them, last residual in r) as one cooperative
+// launch of at most kRefineMaxCtas CTAs; ctl: sweep_ctl_bytes(); norms:
+// refine_norm_doubles(); info (nullable): [corrections, last |Δx|/|x|]
+constexpr int kRefineMaxCtas = 256;
+constexpr double kRefineTol = 1e-13;
+constexpr size_t refine_norm_doubles() { return 2 * (size_t)kRefineMaxCtas * 8; }
 cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const double* F, int kind, double eps,
-                               double lam, bool real_params, int iters, double* x, double* r, float2* rf, void* ctl,
-                               int* status, cudaStream_t st);
+                               double lam, bool real_params, int max_corr, double tol, double* x, double* r,
+                               float2* rf, double* norms, double* info, void* ctl, int* status, cudaStream_t st,
+                               uint64_t wait_ns);
 size_t sweep_work_elems(int P);
-cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st);
+cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st,
+                               uint64_t wait_ns = kNqWaitNs);
 // many matrices in one cooperative launch (one CTA group per matrix, groups
 // of total_ctas <= SMs); every job's ctl lies in ctl_base (zeroed here).
 // The Hermitian fill is left to launch_herm_fill per matrix.
@@ -303,6 +310,7 @@ struct SrCgArgs {
   void* ctl = nullptr;             // sr_cg_ctl_bytes()
   int* status = nullptr;
   double* info = nullptr;          // [2]
+  uint64_t wait_ns = kNqWaitNs;    // limit of every grid-barrier wait
 };
 int sr_cg_grid();
 size_t sr_cg_ctl_bytes();
@@ -322,15 +330,20 @@ struct SolveBufs {
   float2* yf = nullptr;       // [P] complex float correction
   int* status = nullptr;      // device status word
   void* ctl = nullptr;        // grid-barrier control block of the cooperative sweep
+  double* norms = nullptr;    // refinement: per-warp |y|², |x|² (refine_norm_doubles())
+  double* info = nullptr;     // refinement: [corrections, |y|/|x| of the last correction]
+  uint64_t wait_ns = kNqWaitNs;   // limit of every grid-barrier wait of the solve
   cudaEvent_t* ev = nullptr;  // optional [6] events: copy, inversion, fill+rhs, first solve, refinement, end
 };
 // shifted solve (S + shift) x = F: FP32 explicit inverse, then x_0 = A^-1 F and
-// refine_iters corrections x += A^-1 (F - A x) with the residual in FP64;
+// corrections x += A^-1 (F - A x) with the residual in FP64 until the
+// correction is below kRefineTol |x| (at most refine_iters of them);
 // a pivot <= 0 sets bit 0 of status
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st);
 // the two halves around the inversion, for callers that invert several matrices in one launch:
-// W = S + shift; then (after the inversion) fill, x_0 and the refinement steps
+// W = S + shift; then (after the inversion) fill, x_0 and refine_iters
+// correction steps (a fixed count: these kernels run inside a graph)
 cudaError_t launch_sr_shift(const SolveBufs& sb, int P, int kind, double eps, double lam, cudaStream_t st);
 cudaError_t launch_sr_finish(const SolveBufs& sb, int P, const double* F, int kind, double eps, double lam,
                              bool real_params, int refine_iters, cudaStream_t st);
@@ -346,8 +359,9 @@ cudaError_t launch_gram_simt_x(const float* X, int ldx, int ns, int rows, float*
 
 // Measurement statistics (stats.jl:26-50) of a chains x samples matrix stored
 // sample-major (value index s = chain + B*slot); mode 0: complex values,
-// mode 1: |value|^2 (the Liouvillian cost).  chain_scratch: 4 ceil(B/64)
-// doubles (at most 3B + 4).
+// mode 1: |value|^2 (the Liouvillian cost).  chain_scratch:
+// stats_scratch_doubles(B) doubles (5 per block of 64 chains).
+constexpr size_t stats_scratch_doubles(long B) { return 5 * (size_t)((B + 63) / 64); }
 template <typename R>
 cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* chain_scratch,
                          double* out6, cudaStream_t st);

@@ -18,6 +18,8 @@
 // sweep_group.  The grid barrier is a generation counter with a bounded spin
 // (1 s, sticky abort flag): a stalled barrier ends the kernel with a status
 // bit.
+#include <algorithm>
+
 #include "nq_kernels.cuh"
 #include "tc_common.cuh"
 
@@ -33,7 +35,7 @@ struct SweepCtl {
 };
 
 // Barrier over the `n` CTAs that share ctl (the whole grid, or one group).
-__device__ bool group_barrier(SweepCtl* ctl, unsigned n, int* err) {
+__device__ bool group_barrier(SweepCtl* ctl, unsigned n, int* err, uint64_t limit_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -50,7 +52,8 @@ __device__ bool group_barrier(SweepCtl* ctl, unsigned n, int* err) {
       unsigned it = 0;
       while (*vgen == g) {
         if (*(volatile int*)&ctl->abort) { s_ok = 0; break; }
-        if ((++it & 255u) == 0 && globaltimer_ns() - t0 > 1000000000ull) {
+        // the timer is read every 256 polls, every poll under a sub-0.1 ms limit
+        if (((++it & 255u) == 0 || limit_ns < 100000u) && globaltimer_ns() - t0 > limit_ns) {
           atomicOr(err, NQ_DEVERR_TIMEOUT);
           atomicExch(&ctl->abort, 1);
           s_ok = 0;
@@ -191,7 +194,7 @@ NQ_D float2 herm_block_elem(const float2* __restrict__ W, int P, int bi, int bj,
 // barrier per step instead of two, and the serial 32-step pivot inverse runs
 // beside the rank-32 update instead of before it.
 NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status, float2* __restrict__ work,
-                      int rank, int nranks) {
+                      int rank, int nranks, uint64_t limit_ns) {
   __shared__ float2 Dt[CB][CB + 1];
   __shared__ float2 Ut[CB][CB + 1];
   __shared__ float2 Vt[CB][CB + 1];
@@ -358,13 +361,13 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
         }
       }
     }
-    if (k + 1 < nblk && !group_barrier(ctl, (unsigned)nranks, status)) return;
+    if (k + 1 < nblk && !group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
   }
 }
 
 __global__ void __launch_bounds__(256, 2) sweep_coop_kernel(float2* __restrict__ W, int P, SweepCtl* ctl,
-                                                         int* status, float2* __restrict__ work) {
-  sweep_group(W, P, ctl, status, work, blockIdx.x, gridDim.x);
+                                                         int* status, float2* __restrict__ work, uint64_t limit_ns) {
+  sweep_group(W, P, ctl, status, work, blockIdx.x, gridDim.x, limit_ns);
 }
 
 // Many matrices in one cooperative launch: matrix p is swept by CTAs
@@ -379,7 +382,7 @@ __global__ void __launch_bounds__(256, 2) sweep_batch_kernel(const SweepJob* __r
   }
   const SweepJob& j = jobs[lo];
   const int r0 = __ldg(cta_start + lo), n = __ldg(cta_start + lo + 1) - r0;
-  sweep_group(j.W, j.P, reinterpret_cast<SweepCtl*>(j.ctl), j.status, j.work, b - r0, n);
+  sweep_group(j.W, j.P, reinterpret_cast<SweepCtl*>(j.ctl), j.status, j.work, b - r0, n, kNqWaitNs);
 }
 
 // W upper = conj(W lower) so that column i holds row i of the Hermitian matrix
@@ -426,22 +429,35 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
 }
 
 // FP64-residual refinement of the shifted solve in one cooperative launch
-// (one CTA per SM): rf = F, then for it = 0..iters: x (+)= A⁻¹ rf (Hermitian
-// GEMV with W = -A⁻¹, one warp per row, the same warp adds its row into x),
-// grid barrier, r = F - A x in FP64 from the FP64 S and the shift (one warp
-// per row; rf = FP32 copy of r), grid barrier.  The last residual stays in r.
-// Same arithmetic per element as herm_gemv_neg_kernel + refine_update_kernel +
-// residual_kernel; 2 grid barriers per pass instead of three launches.
+// (one CTA per SM).  rf = F, then pass it = 0, 1, ...:
+//   y = A⁻¹ rf (Hermitian GEMV with W = -A⁻¹ in FP32, one warp per row),
+//   x = y (it = 0) or x + y (the same warp adds its row into x, in FP64),
+//   grid barrier,
+//   r = F - A x in FP64 from the FP64 S and the shift (one warp per row;
+//   rf = FP32 copy of r),
+// until the correction is negligible, |y| <= tol |x|, or after max_corr
+// corrections; a grid barrier separates the passes.  Every CTA sums the
+// per-warp |y|² and |x|² partials of the pass in the same fixed order, so all
+// CTAs take the same decision.  Each correction shrinks the error by the
+// FP32 inverse's error ‖I - A⁻¹₃₂ A‖, so x converges to the FP64 solution of
+// the shifted system (limited by the FP64 residual, about cond(A) 1e-16).
+// The last residual stays in r; info = [corrections, |y|/|x| of the last one].
+// A non-finite x sets NQ_DEVERR_NONFINITE in the status word.
 __global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restrict__ W, const double* __restrict__ S,
                                                           int P, const double* __restrict__ F, int kind, double eps,
-                                                          double lam, int real_params, int iters, double* x, double* r,
-                                                          float2* rf, SweepCtl* ctl, int* status) {
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), nw = gridDim.x * (blockDim.x >> 5);
+                                                          double lam, int real_params, int max_corr, double tol,
+                                                          double* x, double* r, float2* rf, double* norms,
+                                                          double* info, SweepCtl* ctl, int* status,
+                                                          uint64_t limit_ns) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib, nw = gridDim.x * (blockDim.x >> 5);
+  __shared__ double s_red[2][8];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x)
     rf[i] = make_float2((float)F[2 * i], real_params ? 0.f : (float)F[2 * i + 1]);
-  if (!group_barrier(ctl, gridDim.x, status)) return;
-  for (int it = 0; it <= iters; ++it) {
+  if (!group_barrier(ctl, gridDim.x, status, limit_ns)) return;
+  for (int it = 0;; ++it) {
+    double yy = 0.0, xx = 0.0;
+    bool finite = true;
     for (int i = gw; i < P; i += nw) {
       const float2* col = W + (size_t)P * i;
       float sx = 0.f, sy = 0.f;
@@ -457,17 +473,52 @@ __global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restri
         sy += __shfl_xor_sync(0xffffffffu, sy, off);
       }
       if (lane == 0) {
-        const float yx = -sx, yy = -sy;
-        if (it == 0) {
-          x[2 * i] = (double)yx;
-          x[2 * i + 1] = (double)yy;
-        } else {
-          x[2 * i] += (double)yx;
-          x[2 * i + 1] += (double)yy;
+        const double yx = -(double)sx, yyv = -(double)sy;
+        double nx = yx, ny = yyv;
+        if (it > 0) {
+          nx += x[2 * i];
+          ny += x[2 * i + 1];
         }
+        x[2 * i] = nx;
+        x[2 * i + 1] = ny;
+        yy += yx * yx + yyv * yyv;
+        xx += nx * nx + ny * ny;
+        finite = finite && isfinite(nx) && isfinite(ny);
       }
     }
-    if (!group_barrier(ctl, gridDim.x, status)) return;
+    if (lane == 0) {
+      norms[2 * gw] = yy;
+      norms[2 * gw + 1] = xx;
+      if (!finite) atomicOr(status, NQ_DEVERR_NONFINITE);
+    }
+    if (!group_barrier(ctl, gridDim.x, status, limit_ns)) return;
+    // |y|² and |x|² of this pass, summed by every CTA in the same order
+    double ty = 0.0, tx = 0.0;
+    for (int w = threadIdx.x; w < nw; w += blockDim.x) {
+      ty += __ldcg(norms + 2 * w);
+      tx += __ldcg(norms + 2 * w + 1);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      ty += __shfl_xor_sync(0xffffffffu, ty, off);
+      tx += __shfl_xor_sync(0xffffffffu, tx, off);
+    }
+    if (lane == 0) {
+      s_red[0][wib] = ty;
+      s_red[1][wib] = tx;
+    }
+    __syncthreads();
+    ty = 0.0;
+    tx = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      ty += s_red[0][w];
+      tx += s_red[1][w];
+    }
+    const bool last = (it > 0 && ty <= tol * tol * tx) || it >= max_corr || !(tx == tx);
+    if (last && blockIdx.x == 0 && threadIdx.x == 0 && info) {
+      info[0] = (double)it;
+      info[1] = tx > 0.0 ? sqrt(ty / tx) : 0.0;
+    }
     for (int k = gw; k < P; k += nw) {
       // (S x)_k = Σ_l conj(S[l][k]) x_l (Hermitian; column k contiguous)
       const double* col = S + 2 * (size_t)P * k;
@@ -494,7 +545,8 @@ __global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restri
         rf[k] = make_float2((float)rx, (float)ry);
       }
     }
-    if (it < iters && !group_barrier(ctl, gridDim.x, status)) return;
+    if (last) break;
+    if (!group_barrier(ctl, gridDim.x, status, limit_ns)) return;
   }
 }
 
@@ -504,7 +556,8 @@ size_t sweep_ctl_bytes() { return sizeof(SweepCtl); }
 // C and G of every block and the pivot inverse, each twice (step parity)
 size_t sweep_work_elems(int P) { return (size_t)(4 * ((P + CB - 1) / CB) + 2) * CB * CB; }
 
-cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st) {
+cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2* work, cudaStream_t st,
+                               uint64_t wait_ns) {
   static int grid = 0;
   if (grid == 0) {
     int dev = 0, sms = 0, per = 0;
@@ -534,7 +587,7 @@ cudaError_t launch_spd_inverse(float2* W, int P, void* ctl, int* status, float2*
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   SweepCtl* c = reinterpret_cast<SweepCtl*>(ctl);
-  return cudaLaunchKernelEx(&cfg, sweep_coop_kernel, W, P, c, status, work);
+  return cudaLaunchKernelEx(&cfg, sweep_coop_kernel, W, P, c, status, work, wait_ns);
 }
 
 cudaError_t launch_herm_gemv_neg(const float2* W, int P, const float2* x, float2* y, cudaStream_t st) {
@@ -567,8 +620,9 @@ cudaError_t launch_herm_fill(float2* W, int P, cudaStream_t st) {
 }
 
 cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const double* F, int kind, double eps,
-                               double lam, bool real_params, int iters, double* x, double* r, float2* rf, void* ctl,
-                               int* status, cudaStream_t st) {
+                               double lam, bool real_params, int max_corr, double tol, double* x, double* r,
+                               float2* rf, double* norms, double* info, void* ctl, int* status, cudaStream_t st,
+                               uint64_t wait_ns) {
   static int grid = 0;
   if (grid == 0) {
     int dev = 0, sms = 0, per = 0;
@@ -579,7 +633,7 @@ cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const do
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, refine_coop_kernel, 256, 0);
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorCooperativeLaunchTooLarge;
-    grid = sms;
+    grid = std::min(sms, kRefineMaxCtas);
   }
   cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(SweepCtl), st);
   if (e != cudaSuccess) return e;
@@ -593,6 +647,6 @@ cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const do
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, refine_coop_kernel, W, S, P, F, kind, eps, lam, real_params ? 1 : 0, iters, x, r,
-                            rf, reinterpret_cast<SweepCtl*>(ctl), status);
+  return cudaLaunchKernelEx(&cfg, refine_coop_kernel, W, S, P, F, kind, eps, lam, real_params ? 1 : 0, max_corr, tol,
+                            x, r, rf, norms, info, reinterpret_cast<SweepCtl*>(ctl), status, wait_ns);
 }

@@ -317,16 +317,21 @@ __device__ __forceinline__ cpx<double> stat_val(const cpx<R>* v, long i, int mod
 }
 
 
-// pass 1 (one thread per chain): chain mean μ_c and unbiased variance var_c
+// pass 1 (one thread per chain, 64 chains per block): chain mean μ_c and
+// unbiased variance var_c from two passes over the chain's L values; per
+// block, with n_b valid chains, the block mean m_b = Σ μ_c / n_b, the centred
+// sum M2_b = Σ |μ_c - m_b|² and Σ var_c, written as
+// part[5 b ..] = [n_b, Re m_b, Im m_b, M2_b, Σ var_c] (fixed shuffle order).
+// Centring inside the block keeps the spread of the chain means exact when
+// it is tiny next to the mean itself (a local energy of -40 with a spread of
+// 1e-6), where Σ|μ_c|² - B|μ|² would cancel to rounding noise.
 template <typename R>
 __global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
                                                          double* __restrict__ part) {
-  // per chain (one thread): μ_c and var_c (two passes over its L values);
-  // per block (64 chains, fixed shuffle/smem order): Σ Re μ_c, Σ Im μ_c,
-  // Σ var_c, Σ |μ_c|² into part[4 blockIdx.x ..]
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = c < B;
   double mx = 0, my = 0, var = 0;
-  if (c < B) {
+  if (valid) {
     for (int l = 0; l < L; ++l) { cpx<double> x = stat_val(v, c + (long)B * l, mode); mx += x.x; my += x.y; }
     mx /= L; my /= L;
     double vv = 0;
@@ -336,39 +341,83 @@ __global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restric
     }
     var = L > 1 ? vv / (L - 1) : 0.0;
   }
-  double q[4] = {mx, my, var, mx * mx + my * my};
+  __shared__ double sh[2][3];
+  double q[3] = {valid ? mx : 0.0, valid ? my : 0.0, var};
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < 3; ++k)
     for (int off = 16; off > 0; off >>= 1) q[k] += __shfl_xor_sync(0xffffffffu, q[k], off);
-  __shared__ double sh[2][4];
   if ((threadIdx.x & 31) == 0)
-    for (int k = 0; k < 4; ++k) sh[threadIdx.x >> 5][k] = q[k];
+    for (int k = 0; k < 3; ++k) sh[threadIdx.x >> 5][k] = q[k];
   __syncthreads();
-  if (threadIdx.x < 4) part[4 * blockIdx.x + threadIdx.x] = sh[0][threadIdx.x] + sh[1][threadIdx.x];
+  const int nb = min(64, B - blockIdx.x * 64);
+  const double bx = (sh[0][0] + sh[1][0]) / nb, by = (sh[0][1] + sh[1][1]) / nb;
+  const double vsum = sh[0][2] + sh[1][2];
+  double d2 = valid ? (mx - bx) * (mx - bx) + (my - by) * (my - by) : 0.0;
+  for (int off = 16; off > 0; off >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, off);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][0] = d2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* o = part + 5 * (size_t)blockIdx.x;
+    o[0] = (double)nb;
+    o[1] = bx;
+    o[2] = by;
+    o[3] = sh[0][0] + sh[1][0];
+    o[4] = vsum;
+  }
 }
 
-// pass 2 (one warp, fixed order): μ = Σμ_c / B;
-// Σ|μ_c-μ|² = Σ|μ_c|² - B|μ|²; var_μ_ch = Σ|μ_c-μ|²/(B-1);
-// var_μ = [(L-1) Σ var_c + L Σ|μ_c-μ|²]/(BL-1) (= var of all values about μ);
-// variance = mean var_c; t = var_μ_ch/var_μ (stats.jl:26-50)
+// merge two (n, mean, M2) summaries of chain means (Chan, Golub and LeVeque's
+// pairwise update), plus the summed chain variances
+struct ChainSummary {
+  double n, mx, my, m2, vs;
+};
+__device__ __forceinline__ ChainSummary merge_summary(const ChainSummary& a, const ChainSummary& b) {
+  if (a.n == 0.0) return b;
+  if (b.n == 0.0) return a;
+  ChainSummary r;
+  r.n = a.n + b.n;
+  const double dx = b.mx - a.mx, dy = b.my - a.my, f = b.n / r.n;
+  r.mx = a.mx + dx * f;
+  r.my = a.my + dy * f;
+  r.m2 = a.m2 + b.m2 + (dx * dx + dy * dy) * a.n * f;
+  r.vs = a.vs + b.vs;
+  return r;
+}
+
+// pass 2 (one warp, fixed order): lane l merges blocks l, l + 32, ... in
+// order, then the lanes merge pairwise down a fixed tree.  With μ the mean of
+// the chain means and Σ|μ_c - μ|² = M2:
+// var_μ_ch = M2/(B-1); var_μ = [(L-1) Σ var_c + L M2]/(BL-1) (= the variance
+// of all values about μ); variance = mean var_c; t = var_μ_ch/var_μ
+// (stats.jl:26-50)
 __global__ void __launch_bounds__(32) stats_final_kernel(const double* __restrict__ part, int nblk, int B, int L,
                                                          double* __restrict__ out) {
-  double q[4] = {0, 0, 0, 0};
-  for (int b = threadIdx.x; b < nblk; b += 32)
-    for (int k = 0; k < 4; ++k) q[k] += part[4 * b + k];
+  ChainSummary s = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nblk; b += 32) {
+    const double* p = part + 5 * (size_t)b;
+    const ChainSummary t = {p[0], p[1], p[2], p[3], p[4]};
+    s = merge_summary(s, t);
+  }
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    for (int off = 16; off > 0; off >>= 1) q[k] += __shfl_xor_sync(0xffffffffu, q[k], off);
+  for (int off = 1; off < 32; off <<= 1) {
+    ChainSummary o;
+    o.n = __shfl_down_sync(0xffffffffu, s.n, off);
+    o.mx = __shfl_down_sync(0xffffffffu, s.mx, off);
+    o.my = __shfl_down_sync(0xffffffffu, s.my, off);
+    o.m2 = __shfl_down_sync(0xffffffffu, s.m2, off);
+    o.vs = __shfl_down_sync(0xffffffffu, s.vs, off);
+    if ((threadIdx.x & (2 * off - 1)) == 0 && threadIdx.x + off < 32) s = merge_summary(s, o);
+  }
   if (threadIdx.x == 0) {
-    const double mux = q[0] / B, muy = q[1] / B;
-    const double dev = fmax(0.0, q[3] - B * (mux * mux + muy * muy));   // Σ|μ_c - μ|²
-    const double var_mu_ch = dev / (B - 1);
-    const double var_mu = ((L - 1) * q[2] + L * dev) / ((double)B * L - 1);
-    const double t = var_mu_ch / var_mu;
-    out[0] = mux;
-    out[1] = muy;
+    const double dev = s.m2;                       // Σ|μ_c - μ|²
+    const double var_mu_ch = B > 1 ? dev / (B - 1) : 0.0;
+    const double var_mu = ((L - 1) * s.vs + L * dev) / ((double)B * L - 1);
+    const double t = var_mu > 0.0 ? var_mu_ch / var_mu : 0.0;
+    out[0] = s.mx;
+    out[1] = s.my;
     out[2] = sqrt(var_mu_ch / B);
-    out[3] = q[2] / B;
+    out[3] = s.vs / B;
     out[4] = fmax(0.0, 0.5 * (t * L - 1.0));
     out[5] = sqrt((double)(L - 1) / L + t);
   }
@@ -465,7 +514,7 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   cudaError_t e = launch_sr_shift(sb, P, kind, eps, lam, st);
   if (e != cudaSuccess) return e;
   mark(1);
-  e = launch_spd_inverse(sb.W, P, sb.ctl, sb.status, sb.work, st);
+  e = launch_spd_inverse(sb.W, P, sb.ctl, sb.status, sb.work, st, sb.wait_ns);
   if (e != cudaSuccess) return e;
   // one problem on the GPU: the refinement as one cooperative launch (the
   // many-problem step keeps launch_sr_finish, whose small kernels run side by
@@ -475,8 +524,8 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   mark(2);
   mark(3);
   mark(4);
-  e = launch_refine_coop(sb.W, sb.S, P, F, kind, eps, lam, real_params, refine_iters, sb.x, sb.r, sb.rf, sb.ctl,
-                         sb.status, st);
+  e = launch_refine_coop(sb.W, sb.S, P, F, kind, eps, lam, real_params, refine_iters, kRefineTol, sb.x, sb.r,
+                         sb.rf, sb.norms, sb.info, sb.ctl, sb.status, st, sb.wait_ns);
   if (e != cudaSuccess) return e;
   mark(5);
   return cudaSuccess;
@@ -492,7 +541,7 @@ template <typename R>
 cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* chain_scratch, double* out6,
                          cudaStream_t st) {
   const int nblk = (B + 63) / 64;
-  chain_stats_kernel<R><<<nblk, 64, 0, st>>>(vals, B, L, mode, chain_scratch);
+  chain_stats_kernel<R><<<nblk, 64, 0, st>>>(vals, B, L, mode, chain_scratch);   // 5 nblk doubles
   stats_final_kernel<<<1, 32, 0, st>>>(chain_scratch, nblk, B, L, out6);
   return cudaGetLastError();
 }

@@ -27,7 +27,7 @@ struct CgCtl {
   int abort, pad;
 };
 
-__device__ bool cg_barrier(CgCtl* ctl, int* err) {
+__device__ bool cg_barrier(CgCtl* ctl, int* err, uint64_t limit_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -44,7 +44,8 @@ __device__ bool cg_barrier(CgCtl* ctl, int* err) {
       unsigned it = 0;
       while (*vgen == g) {
         if (*(volatile int*)&ctl->abort) { s_ok = 0; break; }
-        if ((++it & 255u) == 0 && globaltimer_ns() - t0 > 1000000000ull) {
+        // the timer is read every 256 polls, every poll under a sub-0.1 ms limit
+        if (((++it & 255u) == 0 || limit_ns < 100000u) && globaltimer_ns() - t0 > limit_ns) {
           atomicOr(err, NQ_DEVERR_TIMEOUT);
           atomicExch(&ctl->abort, 1);
           s_ok = 0;
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     block_sum2d(rr, ff);
     if (tid == 0) { a.dots[4 * b] = rr; a.dots[4 * b + 1] = 0.0; }
   }
-  if (!cg_barrier(ctl, a.status)) return;
+  if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
   double rr = 0.0;
   for (int k = 0; k < G; ++k) rr += __ldcg(a.dots + 4 * k);
   const double rr0 = rr;
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
       }
       a.t[s] = make_float2(tx, ty);
     }
-    if (!cg_barrier(ctl, a.status)) return;
+    if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     // ---- adjoint partials over this CTA's sample chunk ----
     double2 acc[EMAX];
 #pragma unroll
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
       }
     }
     if (tid == 0) { a.tsum[2 * b] = tsx; a.tsum[2 * b + 1] = tsy; }
-    if (!cg_barrier(ctl, a.status)) return;
+    if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     // ---- w = S p + shift p on this CTA's slice; p·w partial ----
     double tx = 0.0, ty = 0.0;
     for (int k = 0; k < G; ++k) { tx += __ldcg(a.tsum + 2 * k); ty += __ldcg(a.tsum + 2 * k + 1); }
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     }
     block_sum2d(pw, dummy);
     if (tid == 0) a.dots[4 * b + 1] = pw;
-    if (!cg_barrier(ctl, a.status)) return;
+    if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     double pwt = 0.0;
     for (int k = 0; k < G; ++k) pwt += __ldcg(a.dots + 4 * k + 1);
     if (!(pwt > 0.0)) {
@@ -264,7 +265,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     }
     block_sum2d(rr_new, dummy);
     if (tid == 0) a.dots[4 * b + 2] = rr_new;
-    if (!cg_barrier(ctl, a.status)) return;
+    if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     double rrn = 0.0;
     for (int k = 0; k < G; ++k) rrn += __ldcg(a.dots + 4 * k + 2);
     const double beta = rrn / rr;
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
       a.pv[2 * p] = a.r[2 * p] + beta * a.pv[2 * p];
       a.pv[2 * p + 1] = a.r[2 * p + 1] + beta * a.pv[2 * p + 1];
     }
-    if (!cg_barrier(ctl, a.status)) return;
+    if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
   }
   if (b == 0 && tid == 0) {
     a.info[0] = (double)it;

@@ -7,8 +7,6 @@
 
 #include "nq_common.cuh"
 
-// Error word written when a bounded wait gives up (host maps it to NQ_ERR_TIMEOUT).
-#define NQ_DEVERR_TIMEOUT 0x10
 
 NQ_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -45,7 +43,7 @@ NQ_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // check sit in one asm block: written as a C++ loop, the divergent loop made
 // every tcgen05.mma issued by the same thread about 2.5x slower (measured on
 // GB300, one wait per four 128x256x16 MMAs: 66 -> 165 ns per MMA).
-NQ_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns = 1000000000ull) {
+NQ_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns = kNqWaitNs) {
   uint32_t ok;
   asm volatile(
       "{\n"

@@ -96,6 +96,9 @@ EXPORTS = {
     "nq_create_chain": (ctypes.c_int, [_P(NqConfig), ctypes.c_int32, _P(NqLayer), _P(ctypes.c_void_p)]),
     "nq_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]),
     "nq_set_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "nq_get_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "nq_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "nq_get_estimates": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "nq_logpsi": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "nq_logpsi_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                       ctypes.c_void_p, ctypes.c_void_p]),

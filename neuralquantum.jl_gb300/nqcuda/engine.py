@@ -177,6 +177,22 @@ class Engine:
             raise ValueError("samples must hold L x B x nsites values")
         self._check(self.lib.nq_set_samples(self.h, v.ctypes.data))
 
+    def get_samples(self):
+        """The current sample buffer, (L, B, nsites) int8."""
+        out = np.empty((self.L, self.B, self.nsites), np.int8)
+        self._check(self.lib.nq_get_samples(self.h, out.ctypes.data))
+        return out
+
+    def get_estimates(self):
+        """(local values (L, B), force F, update Δw) of the last estimate and
+        solve on this handle, read back without recomputation."""
+        loc = np.empty((self.L, self.B), np.complex128)
+        dt = np.complex128 if self.complex_params else np.float64
+        force = np.empty(self.P, dt)
+        dw = np.empty(self.P, dt)
+        self._check(self.lib.nq_get_estimates(self.h, loc.ctypes.data, force.ctypes.data, dw.ctypes.data))
+        return loc, force, dw
+
     def logpsi(self, sigma, with_grad=False):
         """sigma: (n, nsites) site values -> logψ (n,) [, grad (n, P)]."""
         v = np.ascontiguousarray(sigma, dtype=np.int8)
@@ -213,8 +229,13 @@ class Engine:
     def set_sr_tolerance(self, tol, maxiter):
         self._check(self.lib.nq_set_sr_tolerance(self.h, float(tol), int(maxiter)))
 
+    def set_wait_limit(self, ns):
+        """Limit of every grid-barrier wait of the solve kernels (0 = 1 s)."""
+        self._check(self.lib.nq_set_wait_limit(self.h, int(ns)))
+
     def sr_info(self):
-        """[iterations, |r|/|F|] of the last matrix-free SR solve."""
+        """[iterations, |r|/|F|] of the last matrix-free SR solve, or
+        [FP64-residual corrections, last |Δx|/|x|] of the last direct solve."""
         v = (ctypes.c_double * 2)()
         self._check(self.lib.nq_sr_info(self.h, v))
         return int(v[0]), float(v[1])

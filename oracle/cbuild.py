@@ -1,22 +1,23 @@
-"""Builds the oracle's C restatement (test infrastructure, see
-``oracle/__init__``) into oracle/_build/libnqport.so with gcc -O3 -fopenmp.
-No reference sources are compiled: the reference is Julia and has no
-C/C++ path."""
+"""Builds the oracle's C code (test infrastructure, see ``oracle/__init__``)
+into oracle/_build/libnqport.so with gcc -O3 -fopenmp: cport.c (the C
+restatement of the reference VMC iteration) and lanczos.c (the matrix-free
+Lanczos recurrence that pins the 2D Ising convention).  No reference sources
+are compiled: the reference is Julia and has no C/C++ path."""
 import ctypes
 import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "cport.c")
+SRCS = [os.path.join(HERE, "cport.c"), os.path.join(HERE, "lanczos.c")]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnqport.so")
 
 
 def build(force=False):
     os.makedirs(OUT_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRCS):
         return LIB
-    cmd = ["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-std=c11", SRC, "-o", LIB + ".tmp", "-lm"]
+    cmd = ["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-std=c11", *SRCS, "-o", LIB + ".tmp", "-lm"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -37,5 +38,7 @@ def lib():
         L.port_eval.argtypes = [i, i, i, vp, i, vp, vp, vp]
         L.port_eloc.restype = None
         L.port_eloc.argtypes = [i, i, i, i, vp, i, vp, vp, i] + [vp] * 8 + [vp]
+        L.tfim2d_lanczos.restype = i
+        L.tfim2d_lanczos.argtypes = [i, i, d, d, i, i, vp, vp]
         _lib = L
     return _lib

@@ -123,3 +123,28 @@ def exact_local_energy_expectation(net, H):
     psi = np.exp(psi_vector(net, hilb))
     Hd = ops.to_matrix(H)
     return np.vdot(psi, Hd @ psi) / np.vdot(psi, psi)
+
+
+def tfim_ground_energy_2d(Lx, Ly, h, J, z2=True, iters=300, tol=1e-11):
+    """Ground energy of ``tfim_2d(Lx, Ly, h, J)`` by the matrix-free Lanczos
+    recurrence of oracle/lanczos.c (even sector of the global spin flip when
+    ``z2``): the lowest eigenvalue of the tridiagonal Lanczos matrix, taken
+    once it changes by less than ``tol`` between 20-step checkpoints."""
+    import scipy.linalg as sla
+    from . import cbuild
+    lib = cbuild.lib()
+    alpha = np.zeros(iters)
+    beta = np.zeros(iters)
+    k = lib.tfim2d_lanczos(int(Lx), int(Ly), float(h), float(J), 1 if z2 else 0, int(iters),
+                           alpha.ctypes.data, beta.ctypes.data)
+    if k <= 0:
+        raise MemoryError("tfim2d_lanczos failed")
+    prev = None
+    e = None
+    for m in list(range(20, k, 20)) + [k]:
+        e = float(sla.eigh_tridiagonal(alpha[:m], beta[:m - 1], eigvals_only=True,
+                                       select="i", select_range=(0, 0))[0])
+        if prev is not None and abs(e - prev) < tol:
+            return e
+        prev = e
+    return e

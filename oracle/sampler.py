@@ -72,7 +72,9 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
     n_sweeps = burn + n_record
     if stale_last_slot and L == 1:
         n_sweeps = burn
-    info = {"ambiguous": 0, "mismatch": 0, "accepted": 0, "steps": 0}
+    # max_tie_gap: the largest |log u - Δ| of a decision the device took the
+    # other way (0 when every decision agrees)
+    info = {"ambiguous": 0, "mismatch": 0, "accepted": 0, "steps": 0, "max_tie_gap": 0.0}
     t = 0
     for sweep in range(n_sweeps):
         for _ in range(passes):
@@ -104,9 +106,13 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
                 logu = np.log(np.maximum(u, 1e-300))
             if gpu_accept_bits is not None:
                 g = np.asarray(gpu_accept_bits[t], dtype=bool)
-                amb = np.abs(logu - delta) < tie_tol
-                info["ambiguous"] += int(np.sum(amb & (g != acc)))
-                info["mismatch"] += int(np.sum(~amb & (g != acc)))
+                gap = np.abs(logu - delta)
+                amb = gap < tie_tol
+                dis = g != acc
+                info["ambiguous"] += int(np.sum(amb & dis))
+                info["mismatch"] += int(np.sum(~amb & dis))
+                if dis.any():
+                    info["max_tie_gap"] = max(info["max_tie_gap"], float(gap[dis].max()))
                 acc = np.where(amb, g, acc)
             sigma = np.where(acc[:, None], new, sigma)
             lp = np.where(acc, lpn, lp)

@@ -66,6 +66,24 @@ def test_known_ground_energy_1d():
     assert abs(e / 20 - kat["tfim1d_N20_h1_J1_energy_per_site"]) < 1e-9
 
 
+def test_known_ground_energy_2d():
+    """examples/ising2d.jl:55 quotes E0 = -80.13310152422413 for the 5 x 5
+    periodic TFIM at h = 3.  The matrix-free Lanczos on the oracle's tfim_2d
+    convention reproduces it to 1e-9 with the coupling sign J = -1
+    (ferromagnetic, H = -h Σσx - Σσzσz); the example's code adds +J σzσz,
+    whose frustrated (odd L) ground energy is -79.6241413371 instead.  The
+    convention itself is pinned by dense diagonalisation of the oracle's
+    operator tables at 3 x 3 for both signs."""
+    kat = json.load(open(os.path.join(GOLDEN, "known_answers.json")))
+    h9 = Hilbert(9, SPIN)
+    for J in (1.0, -1.0):
+        e_dense = np.linalg.eigvalsh(ops.to_matrix(exact.tfim_2d(h9, 3, 3, 3.0, J)).real)[0]
+        assert abs(exact.tfim_ground_energy_2d(3, 3, 3.0, J) - e_dense) < 1e-9
+        assert abs(exact.tfim_ground_energy_2d(3, 3, 3.0, J, z2=False) - e_dense) < 1e-9
+    e = exact.tfim_ground_energy_2d(5, 5, 3.0, -1.0, iters=80)
+    assert abs(e - kat["tfim2d_5x5_h3_J1_energy"]) < 1e-9
+
+
 def test_oracle_hamiltonian_matches_lanczos_convention():
     N = 8
     h = Hilbert(N, SPIN)
@@ -439,3 +457,71 @@ def test_exact_sampler_oracle_chi_square():
     prev = np.full((5, 8), -7)
     idx2, _ = osm.exact_run(p, 8, 5, seed=9, call=3, stale_last_slot=True, prev_samples=prev)
     assert np.all(idx2[4] == -7) and np.array_equal(idx2[:4], osm.exact_run(p, 8, 5, seed=9, call=3)[0][:4])
+
+
+def test_batched_estimators_match_per_sample_forms():
+    """The sample-batched estimators (used on the full-size sample sets) visit
+    the same connections as the per-sample restatements: E_loc, F and S of a
+    TFIM ket, L_loc, the cost, F and <O> of a dissipative Liouvillian."""
+    rng = np.random.default_rng(12)
+    N = 6
+    h = Hilbert(N, SPIN)
+    r = nw.RBM(N, 12, nw.LOGCOSH)
+    nw.init_random_pars(r, rng, sigma=0.2 ** 2)
+    H = exact.tfim_1d(h, 0.7, 1.0)
+    samples = h.value(rng.integers(0, 2, size=(300, N)))
+    E = oest.local_energy(r, H, samples)
+    Eb = oest.local_energy_batched(r, H, samples, chunk=97)
+    np.testing.assert_allclose(Eb, E, rtol=0, atol=1e-12)
+    _, O = r.logpsi_and_grad(samples)
+    gf = lambda a, b: r.logpsi_and_grad(samples[a:b])[1]
+    np.testing.assert_allclose(oest.force_ket_batched(E, gf, 300, chunk=64), oest.force_ket(E, O),
+                               rtol=0, atol=1e-12)
+    Sb, _ = oest.sr_matrix_batched(gf, 300, False, chunk=64)
+    np.testing.assert_allclose(Sb, osr.build_S(oest.center(O)[0], False), rtol=0, atol=1e-12)
+
+    hf = Hilbert(4, FOCK)
+    n = nw.NDM(4, 1, 1, nw.SOFTPLUS)
+    nw.init_random_pars(n, rng, sigma=0.3 ** 2)
+    Hd, Ls = exact.dissipative_ising(hf, 1.0, 2.0)
+    lv = ops.liouvillian(Hd, Ls)
+    sr = hf.value(rng.integers(0, 2, size=(200, 4)))
+    sc = hf.value(rng.integers(0, 2, size=(200, 4)))
+    L, dL = oest.local_liouvillian(n, lv, sr, sc)
+    _, On = n.logpsi_and_grad(sr, sc)
+    C, F = oest.force_liouvillian(L, dL, On)
+    Lb, Cb, Fb, mOb = oest.liouvillian_force_batched(n, lv, sr, sc, chunk=77)
+    np.testing.assert_allclose(Lb, L, rtol=0, atol=1e-12)
+    assert abs(Cb - C) < 1e-12 * max(1.0, C)
+    np.testing.assert_allclose(Fb, F, rtol=0, atol=1e-11)
+    np.testing.assert_allclose(mOb, On.mean(axis=0), rtol=0, atol=1e-12)
+
+
+def test_stats_centred_merge_matches_formula_at_large_offset():
+    """The block-centred merge of chain means (Chan et al.) that the device
+    statistics follow gives stats.jl's variance of the chain means also when
+    the spread (1e-6) is tiny next to the mean (-40), where Σ|μ_c|² - B|μ|²
+    cancels."""
+    rng = np.random.default_rng(3)
+    B, L = 1000, 9
+    v = -40.0 + 1e-6 * (rng.standard_normal((B, L)) + 1j * rng.standard_normal((B, L)))
+    mu_c = v.mean(axis=1)
+    blocks = [mu_c[i:i + 64] for i in range(0, B, 64)]
+    n, m, m2 = 0.0, 0.0 + 0j, 0.0
+    for blk in blocks:
+        nb, mb = len(blk), blk.mean()
+        m2b = np.sum(np.abs(blk - mb) ** 2)
+        if n == 0:
+            n, m, m2 = nb, mb, m2b
+            continue
+        tot = n + nb
+        d = mb - m
+        m = m + d * nb / tot
+        m2 = m2 + m2b + abs(d) ** 2 * n * nb / tot
+        n = tot
+    direct = np.sum(np.abs(mu_c - mu_c.mean()) ** 2)
+    assert abs(m2 - direct) < 1e-9 * direct
+    naive = np.sum(np.abs(mu_c) ** 2) - B * abs(mu_c.mean()) ** 2
+    assert abs(naive - direct) > 1e-3 * direct          # the cancelling form is visibly off
+    st = ost.stat_analysis(v)
+    assert abs(st["error"] - np.sqrt(direct / (B - 1) / B)) < 1e-9 * st["error"]
