@@ -133,6 +133,14 @@ GRAM_TRAFFIC_BYTES = 701.59e6
 # warp instructions of one production launch of the Metropolis kernel on this
 # workload (ncu smsp__inst_executed.sum, profiles/rbm_sampler_c1.txt)
 SAMPLER_WARP_INSTRUCTIONS = 526.8e6
+# DRAM bytes (read + write) of one sampler launch (same capture)
+SAMPLER_TRAFFIC_BYTES = 62e3
+# algorithmic FP32 flops of one Metropolis proposal per hidden unit: the ratio
+# t0 + g t1 (complex FMA, 8), |r|^2 (3) and the running product (1); and per
+# hidden unit of an accepted flip: θ += W dv (4), num = g + τ (2),
+# den = 1 + g τ (8), |den|^2 (3), 1/|den|^2 (1), num conj(den) (6), scaling (2)
+SAMPLER_FLOPS_RATIO = 12
+SAMPLER_FLOPS_ACCEPT = 26
 
 
 def effective_samples_per_s(loc, sample_ms):
@@ -163,7 +171,7 @@ def run_gb300(args, barrier=None):
         ms = eng.bench_steps(args.warmup, args.steps, w["eps"], w["lr"], L2_FLUSH_BYTES)   # synchronises
     if barrier:
         barrier()
-    launches = eng.kernel_launches() - launches0 - eng_graph_kernels(eng)
+    launches = eng.kernel_launches() - launches0
     total_ms = float(np.sum(ms))
     ms_step = total_ms / args.steps
     value = 1e3 / ms_step
@@ -206,35 +214,46 @@ def run_gb300(args, barrier=None):
     e2e = {"value": args.steps / e2e_s, "unit": "SR steps/s", "h2d_bytes_per_step": 16 * P,
            "d2h_bytes_per_step": 16 * P + 8 * 7}
 
-    # roofline of the tensor-core kernel; shares of the three largest kernels
+    # roofline: the dominant kernel (the Metropolis sampler, FP32 CUDA cores)
+    # with its algorithmic flops; the tensor-core S accumulation as a second entry
     Ns = w["chains"] * w["chain_length"]
     kernels = {"sampler": st[6], "S_accumulation": st[7], "inversion": st[8]}
     ksum = sum(kernels.values())
     stages = {"sample": st[0], "eval_estimator": st[1], "force_stats": st[2], "S": st[3],
               "solve": st[4], "update": st[5]}
+    clk_sum = clk.summary()
+    sm_ghz = (clk_sum.get("sm_mhz") or 2070.0) / 1000.0
+    M = w["alpha"] * w["N"]
+    proposals = w["chains"] * (w["passes"] + 1) * (w["burn"] + w["chain_length"])
+    flops_per_proposal = SAMPLER_FLOPS_RATIO * M + m.acceptance * SAMPLER_FLOPS_ACCEPT * M
+    fp32_peak = 152 * 128 * 2 * sm_ghz * 1e9 / 1e12
+    samp_tflops = proposals * flops_per_proposal / (st[6] * 1e-3) / 1e12
+    roof = {"kernel": "rbm_sampler_kernel (Metropolis, θ-cache)", "bound": "fp32", "unit": "TFLOP/s",
+            "achieved": samp_tflops, "peak": fp32_peak, "frac": samp_tflops / fp32_peak,
+            "traffic": SAMPLER_TRAFFIC_BYTES,
+            "algorithmic_flops_per_launch": proposals * flops_per_proposal,
+            "note": (f"algorithmic flops per proposal = {SAMPLER_FLOPS_RATIO} M (ratio t0 + g t1, |.|^2, product) "
+                     f"+ acceptance x {SAMPLER_FLOPS_ACCEPT} M (θ update and Möbius update of g), M = {M}, "
+                     f"acceptance {m.acceptance:.3f}; {proposals} proposals per launch; peak = FP32 FMA rate of "
+                     f"152 SMs x 128 lanes at the sampled SM clock ({sm_ghz:.3f} GHz), derived (MEASURED_PEAKS.json "
+                     f"has no FP32 figure); the kernel keeps θ, g and σ on chip (traffic from ncu)"),
+            "kernel_ms": kernels, "dominant_kernel": max(kernels, key=kernels.get),
+            "share_of_three": {k: v / ksum for k, v in kernels.items()}}
     s_kernel_ms = st[7]
     s_flops = 2.0 * (2 * P) ** 2 * Ns / 2.0        # upper triangle of the 2P x 2P real Gram
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
-    roof = {"kernel": "S accumulation (G = X Xᵀ, upper tiles)", "bound": "tensor",
-            "achieved": s_flops / (s_kernel_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
-            "frac": None, "traffic": GRAM_TRAFFIC_BYTES,
-            "note": "peak = measured dense bf16 burst (of measured); algorithmic flops = 2*(2P)^2*Ns/2 "
-                    "per launch; TF32 operands, so the bf16 peak is an upper bound twice the TF32 rate"}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["kernel_ms"] = kernels
-    roof["dominant_kernel"] = max(kernels, key=kernels.get)
-    roof["share_of_three"] = {k: v / ksum for k, v in kernels.items()}
-    # the sampler, the largest share, moves no HBM bytes and uses no tensor
-    # core: its bound is the instruction issue rate of 152 SMs x 4 schedulers
-    clk_sum = clk.summary()
-    sm_ghz = (clk_sum.get("sm_mhz") or 2070.0) / 1000.0
-    issue_peak = 152 * 4 * sm_ghz * 1e9
+    roof["tensor_kernel"] = {
+        "kernel": "gram_tf32_kernel (S = X Xᵀ, upper tiles)", "bound": "tensor",
+        "achieved": s_flops / (s_kernel_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+        "frac": s_flops / (s_kernel_ms * 1e-3) / 1e12 / bf16_peak, "traffic": GRAM_TRAFFIC_BYTES,
+        "note": "peak = measured dense bf16 burst (of measured); algorithmic flops = 2*(2P)^2*Ns/2 per launch; "
+                "TF32 operands issue at half the bf16 rate"}
     roof["sampler_issue_bound"] = {
         "bound": "instruction issue", "warp_instructions_per_launch": SAMPLER_WARP_INSTRUCTIONS,
-        "achieved": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3), "peak": issue_peak,
-        "unit": "warp instructions/s", "frac": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3) / issue_peak,
-        "note": "instruction count from one ncu capture of this workload's launch (profiles/rbm_sampler_c1.txt), "
-                "time from the live CUDA events; HBM traffic of the launch: 62 KB"}
+        "achieved": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3), "peak": 152 * 4 * sm_ghz * 1e9,
+        "unit": "warp instructions/s",
+        "frac": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3) / (152 * 4 * sm_ghz * 1e9),
+        "note": "executed (not algorithmic) instructions from one ncu capture of this workload's launch"}
 
     line = {
         "metric": METRIC, "value": value, "unit": "SR steps/s", "n_gpus": args.gpus,
@@ -258,10 +277,6 @@ def run_gb300(args, barrier=None):
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(max_seconds=args.cpu_seconds)
     return line
-
-
-def eng_graph_kernels(eng):
-    return 0
 
 
 # --------------------------------------------------------------------------
@@ -334,6 +349,14 @@ def precision_modes():
     d0, d1 = ref.precondition(0, c["eps"]), fast.precondition(0, c["eps"])
     out["relative_error_vs_fp64_eval"] = {"L_loc": rel(l1, l0), "cost": abs(m1.mean_re - m0.mean_re) / abs(m0.mean_re),
                                           "F": rel(f1, f0), "S": rel(s1, s0), "dw": rel(d1, d0)}
+    # the solve's own error: Δw against the FP64 solve of each engine's own S and F
+    eye = np.eye(s0.shape[0])
+    out["solve_error_vs_fp64_solve_of_own_S"] = {
+        "fp64_eval": rel(d0, np.linalg.solve(s0 + c["eps"] * eye, f0)),
+        "precision_mode": rel(d1, np.linalg.solve(s1 + c["eps"] * eye, f1))}
+    out["dw_error_from_S"] = rel(np.linalg.solve(s1 + c["eps"] * eye, f1), np.linalg.solve(s0 + c["eps"] * eye, f1))
+    out["solve_corrections"] = {"fp64_eval": ref.sr_info()[0],
+                                "precision_mode": fast.sr_info()[0]}
     del ref, fast
     curves = {}
     for name, sp in (("tf32", nq._lib.NQ_S_TF32), ("fp32", nq._lib.NQ_S_F32)):
@@ -489,11 +512,14 @@ def cpu_baseline(max_seconds=20.0, chains=None):
     cores and, in a separate process limited to one thread (OpenMP and
     BLAS), on one core."""
     from oracle import cport
-    res = cport.time_baseline(WORKLOAD, max_seconds=max_seconds, chains=chains)
+    res = cport.time_baseline(WORKLOAD, max_seconds=max_seconds, chains=chains, precision="f32")
+    f64 = cport.time_baseline(WORKLOAD, max_seconds=max_seconds / 2, chains=chains, precision="f64")
+    res["fp64"] = {"value": f64["value"], "unit": f64["unit"], "cores": f64["cores"], "sample": f64["sample"]}
     env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
     code = ("import json; from oracle import cport; "
             f"w = json.loads({json.dumps(json.dumps(WORKLOAD))}); "
-            f"print(json.dumps(cport.time_baseline(w, max_seconds={max_seconds / 2!r}, quiet=True)))")
+            f"print(json.dumps(cport.time_baseline(w, max_seconds={max_seconds / 2!r}, quiet=True, "
+            f"precision='f32')))")
     try:
         out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                              timeout=max(120.0, 6 * max_seconds), cwd=os.path.dirname(os.path.abspath(__file__)))
@@ -506,17 +532,20 @@ def cpu_baseline(max_seconds=20.0, chains=None):
 
 def run_reference(args):
     from oracle import cport
+    # each step is a bounded sample of the workload, sized so that the whole
+    # run stays within about three minutes
+    per_step = min(args.cpu_seconds, max(2.0, 180.0 / (args.steps + args.warmup)))
     res = []
     for _ in range(args.warmup):
-        cport.time_baseline(WORKLOAD, max_seconds=args.cpu_seconds / 4, quiet=True)
+        cport.time_baseline(WORKLOAD, max_seconds=per_step / 4, quiet=True, precision="f32")
     for _ in range(args.steps):
-        res.append(cport.time_baseline(WORKLOAD, max_seconds=args.cpu_seconds))
+        res.append(cport.time_baseline(WORKLOAD, max_seconds=per_step, precision="f32"))
     v = float(np.median([r["value"] for r in res]))
     base = res[-1]
     base["value"] = v
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "SR steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": workload_config(), "cpu_baseline": base,
             "e2e": {"value": v, "unit": "SR steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

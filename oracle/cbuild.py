@@ -1,6 +1,7 @@
 """Builds the oracle's C code (test infrastructure, see ``oracle/__init__``)
 into oracle/_build/libnqport.so with gcc -O3 -fopenmp: cport.c (the C
-restatement of the reference VMC iteration) and lanczos.c (the matrix-free
+restatement of the reference VMC iteration, compiled in FP64 and in FP32) and
+lanczos.c (the matrix-free
 Lanczos recurrence that pins the 2D Ising convention).  No reference sources
 are compiled: the reference is Julia and has no C/C++ path."""
 import ctypes
@@ -17,7 +18,17 @@ def build(force=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRCS):
         return LIB
-    cmd = ["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-std=c11", *SRCS, "-o", LIB + ".tmp", "-lm"]
+    # cport.c twice: FP64 (port_*) and FP32 (port_*_f32, -DPORT_F32)
+    units = [(SRCS[0], "cport64.o", []), (SRCS[0], "cport32.o", ["-DPORT_F32"]), (SRCS[1], "lanczos.o", [])]
+    objs = []
+    for src, obj, extra in units:
+        out = os.path.join(OUT_DIR, obj)
+        cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-std=c11", *extra, "-c", src, "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"gcc failed for {src}:\n{r.stderr}")
+        objs.append(out)
+    cmd = ["gcc", "-shared", "-fopenmp", *objs, "-o", LIB + ".tmp", "-lm"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -32,12 +43,13 @@ def lib():
         build()
         L = ctypes.CDLL(LIB)
         d, i, u64, u32, vp = ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p
-        L.port_sample.restype = ctypes.c_long
-        L.port_sample.argtypes = [i, i, i, i, vp, i, i, i, i, u64, u32, i, vp]
-        L.port_eval.restype = None
-        L.port_eval.argtypes = [i, i, i, vp, i, vp, vp, vp]
-        L.port_eloc.restype = None
-        L.port_eloc.argtypes = [i, i, i, i, vp, i, vp, vp, i] + [vp] * 8 + [vp]
+        for sfx in ("", "_f32"):
+            getattr(L, "port_sample" + sfx).restype = ctypes.c_long
+            getattr(L, "port_sample" + sfx).argtypes = [i, i, i, i, vp, i, i, i, i, u64, u32, i, vp]
+            getattr(L, "port_eval" + sfx).restype = None
+            getattr(L, "port_eval" + sfx).argtypes = [i, i, i, vp, i, vp, vp, vp]
+            getattr(L, "port_eloc" + sfx).restype = None
+            getattr(L, "port_eloc" + sfx).argtypes = [i, i, i, i, vp, i, vp, vp, i] + [vp] * 8 + [vp]
         L.tfim2d_lanczos.restype = i
         L.tfim2d_lanczos.argtypes = [i, i, d, d, i, i, vp, vp]
         _lib = L

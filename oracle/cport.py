@@ -50,12 +50,23 @@ def _ptr(a):
 
 
 class PortRBM:
-    def __init__(self, N, M, activation, hilb_kind, H):
+    """One reference VMC iteration in the C restatement.  ``precision`` "f64"
+    runs complex128 throughout; "f32" runs the network, sampler and
+    estimator in complex64 (the reference's default STD_REAL_PREC = Float32,
+    src/NeuralQuantum.jl:57, with FP32 weights) and O, S, F and the Cholesky
+    solve in complex64 as Julia would on ComplexF32 arrays."""
+
+    def __init__(self, N, M, activation, hilb_kind, H, precision="f64"):
         self.N, self.M = N, M
         self.act = 0 if activation == nw.LOGCOSH else 1
         self.hilb = 0 if hilb_kind == SPIN else 1
         self.tab = flatten_ket_operator(H, N)
         self.L = cbuild.lib()
+        self.precision = precision
+        sfx = "_f32" if precision == "f32" else ""
+        self.f_sample = getattr(self.L, "port_sample" + sfx)
+        self.f_eval = getattr(self.L, "port_eval" + sfx)
+        self.f_eloc = getattr(self.L, "port_eloc" + sfx)
 
     def iteration(self, params, B, L, burn, passes, seed, call, eps, lr, timings=None):
         N, M = self.N, self.M
@@ -64,16 +75,18 @@ class PortRBM:
         ns = B * L
         t0 = time.perf_counter()
         samples = np.empty((L, B, N), np.float64)
-        self.L.port_sample(N, M, self.act, self.hilb, _ptr(params), B, L, burn, passes, seed, call, 0,
-                           _ptr(samples))
+        self.f_sample(N, M, self.act, self.hilb, _ptr(params), B, L, burn, passes, seed, call, 0, _ptr(samples))
         t1 = time.perf_counter()
         flat = samples.reshape(ns, N)
         lp = np.empty(ns, np.complex128)
         O = np.empty((ns, P), np.complex128)
-        self.L.port_eval(N, M, self.act, _ptr(params), ns, _ptr(flat), _ptr(lp), _ptr(O))
+        self.f_eval(N, M, self.act, _ptr(params), ns, _ptr(flat), _ptr(lp), _ptr(O))
         E = np.empty(ns, np.complex128)
-        self.L.port_eloc(N, M, self.act, self.hilb, _ptr(params), ns, _ptr(flat), _ptr(lp),
-                         len(self.tab[0]), *[_ptr(a) for a in self.tab], _ptr(E))
+        self.f_eloc(N, M, self.act, self.hilb, _ptr(params), ns, _ptr(flat), _ptr(lp),
+                    len(self.tab[0]), *[_ptr(a) for a in self.tab], _ptr(E))
+        if self.precision == "f32":
+            O = O.astype(np.complex64)
+            E = E.astype(np.complex64)
         t2 = time.perf_counter()
         mean = O.mean(axis=0)
         O -= mean
@@ -82,20 +95,20 @@ class PortRBM:
         t3 = time.perf_counter()
         S[np.diag_indices_from(S)] += eps
         dw = sla.cho_solve(sla.cho_factor(S, lower=False, check_finite=False), F, check_finite=False)
-        newp = params - lr * dw
+        newp = params - lr * dw.astype(np.complex128)
         t4 = time.perf_counter()
         if timings is not None:
             timings.update(sample=t1 - t0, eval_eloc=t2 - t1, S=t3 - t2, solve=t4 - t3)
         return newp, samples, E, dw
 
 
-def time_baseline(w, max_seconds=15.0, chains=None, quiet=False):
+def time_baseline(w, max_seconds=15.0, chains=None, quiet=False, precision="f32"):
     """Runs the reference iteration on a bounded number of chains and scales
     the chain-proportional stages to the full workload."""
     N, alpha = w["N"], w["alpha"]
     h = Hilbert(N, SPIN)
     H = exact.tfim_1d(h, w["h"], w["J"])
-    port = PortRBM(N, alpha * N, nw.LOGCOSH, SPIN, H)
+    port = PortRBM(N, alpha * N, nw.LOGCOSH, SPIN, H, precision=precision)
     net = nw.RBM(N, alpha * N, nw.LOGCOSH)
     nw.init_random_pars(net, np.random.default_rng(w["seed"]), sigma=1e-4)
     passes = w["passes"] + 1 if w["passes"] % 2 == 0 else w["passes"]
@@ -114,6 +127,8 @@ def time_baseline(w, max_seconds=15.0, chains=None, quiet=False):
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     return {"value": 1.0 / per_step, "unit": "SR steps/s", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
             "kind": "port",
+            "precision": precision,
             "sample": (f"{B} of {full} chains x {w['chain_length']} samples (C restatement of the reference "
-                       f"path, FP64, OpenMP + OpenBLAS), chain-proportional stages scaled x{scale:g}"),
+                       f"path, {'FP32' if precision == 'f32' else 'FP64'} complex, OpenMP + OpenBLAS), "
+                       f"chain-proportional stages scaled x{scale:g}"),
             "stage_s_measured": {k: round(v, 4) for k, v in tm.items()}}

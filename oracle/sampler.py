@@ -38,7 +38,7 @@ def init_configs(hilb, seed, call, chains, n_sites_total):
 
 def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
         doubled=False, stale_last_slot=False, prev_samples=None,
-        gpu_accept_bits=None, tie_tol=1e-3, chain_offset=0, couplings=None, move_op=None):
+        gpu_accept_bits=None, tie_tol=1e-6, chain_offset=0, couplings=None, move_op=None):
     """Replays one ``_sample_state!`` call.
 
     ``couplings`` (list of 0-based site pairs) selects ExchangeRule
@@ -54,8 +54,9 @@ def run(log_prob, hilb, n_chains, chain_length, burn, passes, seed, call=0,
 
     ``log_prob(batch)`` maps (B, nsites_total) configurations to 2 Re log psi.
     ``gpu_accept_bits`` (optional, (steps, B) bool) resolves near-tie
-    decisions (|log u - Δ| < tie_tol) the way the GPU took them; all other
-    decisions must agree.  Returns (samples (L, B, nsites_total), info)."""
+    decisions (|log u - Δ| < tie_tol, default 1e-6: the FP32 rounding of the
+    device's Δ) the way the GPU took them and counts them; all other decisions
+    must agree.  Returns (samples (L, B, nsites_total), info)."""
     N = hilb.n_sites
     nt = 2 * N if doubled else N
     chains = np.arange(n_chains) + chain_offset

@@ -2,7 +2,7 @@
 (src/Networks/Chains/) on the GPU against the FP64 oracle, through the C-ABI.
 
 Tolerances: logψ, ∇logψ, E_loc relative 2e-5 (FP32) / 1e-10 (FP64); chains
-bit-exact against the Philox replay (near-ties |log u - Δ| < 1e-3 follow the
+bit-exact against the Philox replay (near-ties |log u - Δ| < 1e-6 follow the
 device); F 1e-4; S 1e-4 (FP32 S); Δw 2e-3; χ² p > 1e-3; the chain of
 examples/ising1d_ffnn.jl lowers the TFIM energy.
 """

@@ -2,7 +2,7 @@
 GPU against the oracle, through the C-ABI.
 
 * the diagonal chains are the Metropolis replay of p(σ) ∝ ρ(σ,σ) on the N
-  physical sites, bit-exact (near-ties |log u - Δ| < 1e-3 follow the
+  physical sites, bit-exact (near-ties |log u - Δ| < 1e-6 follow the
   device, none may disagree elsewhere);
 * logρ(σ,σ) of N-site configurations (nq_logpsi on the diagonal handle):
   relative 2e-5 (FP32) / 1e-10 (FP64);

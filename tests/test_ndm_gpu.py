@@ -3,7 +3,9 @@ the FP64 oracle, through the C-ABI.
 
 Tolerances: logρ, ∇logρ, L_loc: relative 2e-5 (FP32 evaluation) / 1e-10
 (FP64); sampler configurations bit-exact against the Philox replay (near-ties
-|log u - Δ| < 1e-3 follow the device); F: 1e-4; S: 1e-4 (FP32 S); Δw: 2e-3.
+|log u - Δ| < 1e-6 follow the device); F: 1e-4; S: 1e-4 (FP32 S); Δw: 1e-9
+against the FP64 solve of the engine's own S and F, 2e-3 against the
+oracle's Δw (adds the S error).
 """
 import numpy as np
 import pytest
@@ -97,6 +99,8 @@ def test_liouvillian_estimator_force_S_solve(nqlib, prec):
     dw = is_.engine.precondition(0, 0.01)
     dwo = osr.precondition(S, F, 0.01, real_params=True)
     assert rel(dw, dwo) < 2e-3
+    Sg = is_.engine.sr_matrix()
+    assert rel(dw, np.linalg.solve(Sg + 0.01 * np.eye(Sg.shape[0]), force)) < 1e-9
     p0 = is_.engine.get_params()
     is_.engine.update_descent(0.01)
     np.testing.assert_allclose(is_.engine.get_params(), p0 - 0.01 * dw, rtol=0, atol=1e-12)

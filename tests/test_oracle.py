@@ -525,3 +525,20 @@ def test_stats_centred_merge_matches_formula_at_large_offset():
     assert abs(naive - direct) > 1e-3 * direct          # the cancelling form is visibly off
     st = ost.stat_analysis(v)
     assert abs(st["error"] - np.sqrt(direct / (B - 1) / B)) < 1e-9 * st["error"]
+
+
+def test_c_port_fp32_matches_oracle_within_fp32():
+    """The FP32 build of the C restatement (the reference's default complex64
+    precision) gives the oracle's chains and E_loc within FP32 rounding."""
+    from oracle import cport
+    N, M, B, L, burn, passes, seed = 6, 12, 32, 3, 4, 7, 99
+    h = Hilbert(N, SPIN)
+    H = exact.tfim_1d(h, 1.0, 1.0)
+    r = nw.RBM(N, M, nw.LOGCOSH)
+    nw.init_random_pars(r, np.random.default_rng(8), sigma=0.2 ** 2)
+    port = cport.PortRBM(N, M, nw.LOGCOSH, SPIN, H, precision="f32")
+    newp, samples, E, dw = port.iteration(r.flat(), B, L, burn, passes, seed, 3, 0.01, 0.1)
+    ref, info = osm.run(r.log_prob, h, B, L, burn, passes, seed, call=3)
+    np.testing.assert_array_equal(samples, ref)
+    Eo = oest.local_energy(r, H, ref.reshape(-1, N))
+    assert np.max(np.abs(E - Eo)) < 2e-5 * np.max(np.abs(Eo))

@@ -3,7 +3,7 @@ the doubled-space path against the FP64 oracle, through the C-ABI.
 
 Tolerances: logρ, ∇logρ, L_loc relative 2e-5 (FP32) / 1e-10 (FP64); the
 doubled-space chains bit-exact against the Philox replay (near-ties
-|log u - Δ| < 1e-3 follow the device); F 1e-4; S 1e-4 (FP32 S, complex
+|log u - Δ| < 1e-6 follow the device); F 1e-4; S 1e-4 (FP32 S, complex
 parameters: S = conj(O_c O_c†)/Ns, SRDirect.jl:38-44); Δw 2e-3; the
 diagonal observables as for the NDM (2e-5 FP32 per sample, dense trace
 within 5 error bars).
