@@ -202,6 +202,11 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
           }
         }
       }
+      // on an abort the drain warps may stop before the last segment: wait
+      // (bounded) for the MMAs already issued, tracked by the commit of the
+      // last stage, so that no MMA still reads shared memory or writes TMEM
+      // when the CTA frees them
+      if (stop && k > 0) mbar_wait_bounded(&empty[(k - 1) % stages], (uint32_t)((k - 1) / stages) & 1u, err);
     }
     __syncwarp();
   } else {

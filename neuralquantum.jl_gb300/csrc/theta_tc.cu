@@ -111,7 +111,9 @@ theta_bf16x2_kernel(const uint4* __restrict__ img, int NPr, int nterms, int tmem
       }
       mma_commit(bar);
     }
-    if (!mbar_wait_bounded(bar, phase, err)) ok = false;
+    bool landed = mbar_wait_bounded(bar, phase, err);
+    if (!landed && tid == 0) landed = mbar_wait_bounded(bar, phase, err);   // issued MMAs before TMEM is freed
+    if (!landed) ok = false;
     phase ^= 1u;
     ok = __syncthreads_and(ok ? 1 : 0) != 0;      // uniform: the TMEM loads below are warp-collective
     tc_fence_after();
