@@ -1,6 +1,8 @@
 // C-ABI of libnqcuda: handle lifecycle, device buffers, the stage sequence of
 // one VMC iteration and its CUDA-graph replay.  See include/nqcuda.h for the
 // mapping of every entry point onto the reference interface it replaces.
+#include <type_traits>
+
 #include "handle.cuh"
 
 namespace {
@@ -55,6 +57,8 @@ nq_status ndm_refresh(nq_handle* h) {
   }
   RbmDev<R> d = rbm_dev<R>(h);
   CKL(launch_rbm_tables<R>(d, (cpx<R>*)h->d_tab[0], (cpx<R>*)h->d_tab[1], (cpx<R>*)h->d_tab[2], h->st));
+  if constexpr (std::is_same<R, float>::value)
+    if (h->tc_theta) CKL(launch_theta_pack(b.C, h->U, h->N2, h->theta_terms, h->d_theta_img, h->st));
   return NQ_OK;
 }
 
@@ -207,9 +211,24 @@ nq_status stage_sample(nq_handle* h, uint32_t call, unsigned char* accept_bits_d
   return NQ_OK;
 }
 
+// θ of the sample buffer's doubled configurations on tcgen05 (density
+// matrices with NQ_EVAL_TC_BF16X2 / X3), read by the evaluation, estimator and
+// gradient kernels instead of forming θ on CUDA cores
+template <typename R>
+nq_status ndm_tc_theta(nq_handle* h, NdmEff<R>* e) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (!h->tc_theta) return NQ_OK;
+    CKL(launch_theta_bf16x2(h->d_theta_img, h->theta_terms, h->U, h->N2, e->b, h->d_samples, h->Ns, h->hilb,
+                            h->d_ndm_theta, h->sb.status, h->st));
+    e->theta = h->d_ndm_theta;
+  }
+  return NQ_OK;
+}
+
 template <typename R>
 nq_status ndm_stage_eval(nq_handle* h) {
-  const NdmEff<R> e = ndm_eff<R>(h);
+  NdmEff<R> e = ndm_eff<R>(h);
+  if (nq_status s = ndm_tc_theta<R>(h, &e)) return s;
   const int sp = h->cfg.s_precision;
   const bool tc = sp == NQ_S_TF32 || sp == NQ_S_TF32X3;
   CKL(launch_ndm_eval<R>(e, h->act, h->d_samples, h->Ns, h->hilb, (cpx<R>*)h->d_logpsi, h->d_X, h->Ns_pad,
@@ -257,9 +276,13 @@ __global__ void g64_to_32_kernel(const double* g, long n, float2* out) {
 
 template <typename R>
 nq_status ndm_stage_force(nq_handle* h) {
-  // cost C = mean |L_loc|^2 with its statistics, then F
+  // cost C = mean |L_loc|^2 with its statistics, then F (θ of the samples from
+  // the evaluation stage when it ran on tcgen05)
+  NdmEff<R> e = ndm_eff<R>(h);
+  if constexpr (std::is_same<R, float>::value)
+    if (h->tc_theta) e.theta = h->d_ndm_theta;
   CKL(launch_stats<R>((cpx<R>*)h->d_eloc, h->B, h->L, 1, h->d_chainstats, h->d_stats, h->st));
-  CKL(launch_ndm_grad<R>(ndm_eff<R>(h), h->act, h->op, h->d_samples, h->Ns, h->hilb, h->maxc,
+  CKL(launch_ndm_grad<R>(e, h->act, h->op, h->d_samples, h->Ns, h->hilb, h->maxc,
                          (const cpx<R>*)h->d_eloc, (const cpx<R>*)h->d_w, h->d_wconn, h->d_nconn,
                          h->d_ndm_partial, h->fb.meanO, h->d_stats, h->fb.force, h->st));
   return NQ_OK;
@@ -581,12 +604,21 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
   if (!h->chain && (c.n_hidden < 1 || c.n_hidden > 256)) return bad("n_hidden must be in 1..256");
   if (c.n_chains < 2 || c.chain_length < 1 || c.burn < 0 || c.passes < 1) return bad("bad sampler sizes");
-  if (c.eval_precision != NQ_EVAL_F32 && c.eval_precision != NQ_EVAL_F64 &&
-      !((c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3) &&
-        c.network == NQ_NET_RBM &&
-        theta_tc_supported(c.n_sites, c.n_hidden) && gram_tc_supported())) {
-    delete h;
-    return NQ_ERR_UNSUPPORTED;
+  if (c.eval_precision != NQ_EVAL_F32 && c.eval_precision != NQ_EVAL_F64) {
+    // θ on tcgen05: the RBM ket (θ = Wσ + b), and the density matrices on the
+    // doubled space (the units of their effective network, θ_u = b_u + C_u·(σ, η))
+    const bool tc = c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3;
+    const int eff_units = c.network == NQ_NET_RBM_SPLIT ? c.n_hidden
+                          : 4 * c.n_hidden * (c.network == NQ_NET_NDM_SYMM ? std::max(1, c.n_symm) : 1) +
+                                c.n_ancilla * (c.network == NQ_NET_NDM_SYMM ? std::max(1, c.n_symm) : 1);
+    const bool ok = tc && gram_tc_supported() &&
+                    ((c.network == NQ_NET_RBM && theta_tc_supported(c.n_sites, c.n_hidden)) ||
+                     (matrix_net && c.sampler_space == NQ_SPACE_NETWORK &&
+                      theta_tc_supported(2 * c.n_sites, eff_units)));
+    if (!ok) {
+      delete h;
+      return NQ_ERR_UNSUPPORTED;
+    }
   }
   if (c.s_precision == NQ_S_F64) { delete h; return NQ_ERR_UNSUPPORTED; }
   if (c.sr_algorithm != NQ_SR_DIRECT && c.sr_algorithm != NQ_SR_CG) return bad("unknown sr_algorithm");
@@ -790,7 +822,10 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
     step(dalloc(&h->sb.info, 2), "refinement info");
   }
   if (h->diag) step(dalloc(&h->sb.status, 1), "status");
-  if (h->tc_theta) step(dalloc(&h->d_theta_img, theta_tc_image_elems(h->M, h->theta_terms)), "theta image");
+  if (h->tc_theta) {
+    step(dalloc(&h->d_theta_img, theta_tc_image_elems(h->ndm ? h->U : h->M, h->theta_terms)), "theta image");
+    if (h->ndm) step(dalloc(&h->d_ndm_theta, (size_t)h->U * h->Ns), "unit pre-activations");
+  }
   h->sb.S = h->d_S;
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
@@ -838,7 +873,7 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->sb.norms, h->sb.info, h->d_theta_img, h->d_exact, h->d_pairs, h->d_xtab[0],
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->sb.norms, h->sb.info, h->d_theta_img, h->d_ndm_theta, h->d_exact, h->d_pairs, h->d_xtab[0],
                   h->d_xtab[1], h->d_xtab[2], h->d_xW, h->d_xare, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial,
                   h->d_diag[0], h->d_diag[1], h->d_diag[2], h->d_bare, h->d_perms};
@@ -1349,7 +1384,16 @@ static nq_status eval_host_batch(nq_handle* h, const int8_t* sigma, int64_t n, d
   } else if (h->ndm) {
     if (grad) CK(cudaMalloc(&d_out, (size_t)2 * h->P * n * sizeof(double)));
     if (h->f64) CKL(launch_ndm_eval<double>(ndm_eff<double>(h), h->act, d_bits, (int)n, h->hilb, (cpx<double>*)d_lp, nullptr, 0, d_out, h->st));
-    else CKL(launch_ndm_eval<float>(ndm_eff<float>(h), h->act, d_bits, (int)n, h->hilb, (cpx<float>*)d_lp, nullptr, 0, d_out, h->st));
+    else {
+      NdmEff<float> e = ndm_eff<float>(h);
+      if (h->tc_theta) {        // θ of the given configurations on tcgen05, as in the estimator
+        CK(cudaMalloc(&d_g, (size_t)n * h->U * sizeof(cpx<float>)));
+        CKL(launch_theta_bf16x2(h->d_theta_img, h->theta_terms, h->U, h->N2, e.b, d_bits, (int)n, h->hilb,
+                                (cpx<float>*)d_g, h->sb.status, h->st));
+        e.theta = (const cpx<float>*)d_g;
+      }
+      CKL(launch_ndm_eval<float>(e, h->act, d_bits, (int)n, h->hilb, (cpx<float>*)d_lp, nullptr, 0, d_out, h->st));
+    }
   } else if (h->f64) CKL(launch_rbm_eval<double>(rbm_dev<double>(h), d_bits, (int)n, nullptr, (cpx<double>*)d_lp, (cpx<double>*)d_g, nullptr, h->st));
   else if (h->tc_theta) {
     const RbmDev<float> d = rbm_dev<float>(h);

@@ -133,16 +133,23 @@ NQ_D cpx<R> ndm_O_train(const NdmEff<R>& e, int k, const cpx<R>* g, int gstride,
 
 // unit pre-activations x_u and derivatives g_u at configuration `bits`
 // into per-thread slices of shared memory (stride T)
+// (θ read from e.theta[u n + s] when the tensor-core θ of the n samples is given)
 template <typename R, int ACT>
-NQ_D cpx<R> ndm_units(const NdmEff<R>& e, uint64_t bits, int hilb, cpx<R>* x, cpx<R>* g, int T) {
+NQ_D cpx<R> ndm_units(const NdmEff<R>& e, uint64_t bits, int hilb, cpx<R>* x, cpx<R>* g, int T, int s = 0,
+                      int n = 0) {
   const int U = e.U, N2 = e.N2;
   cpx<R> lp = mk(R(0), R(0));
   for (int i = 0; i < N2; ++i) lp = lp + site_value<R>(bits, i, hilb) * e.a[i];
   for (int u = 0; u < U; ++u) {
-    cpx<R> t = e.b[u];
-    for (int i = 0; i < N2; ++i) {
-      const R v = site_value<R>(bits, i, hilb);
-      if (v != R(0)) { const cpx<R> c = e.C[u + (size_t)U * i]; t.x += c.x * v; t.y += c.y * v; }
+    cpx<R> t;
+    if (e.theta) {
+      t = e.theta[(size_t)u * n + s];
+    } else {
+      t = e.b[u];
+      for (int i = 0; i < N2; ++i) {
+        const R v = site_value<R>(bits, i, hilb);
+        if (v != R(0)) { const cpx<R> c = e.C[u + (size_t)U * i]; t.x += c.x * v; t.y += c.y * v; }
+      }
     }
     x[(size_t)u * T] = t;
     g[(size_t)u * T] = act_df<ACT>(t);
@@ -167,7 +174,7 @@ ndm_eval_kernel(NdmEff<R> e, const uint64_t* __restrict__ samples, int n, int hi
   const int s = blockIdx.x * T + threadIdx.x;
   if (s >= n) return;
   const uint64_t bits = samples[s];
-  const cpx<R> lp = ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
+  const cpx<R> lp = ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T, s, n);
   logrho[s] = lp;
   for (int k = 0; k < e.P; ++k) {
     const cpx<R> o = ndm_O_train<R>(e, k, sg + threadIdx.x, T, bits, hilb);
@@ -226,7 +233,7 @@ ndm_loc_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int 
   const int s = blockIdx.x * T + threadIdx.x;
   if (s >= n) return;
   const uint64_t bits = samples[s];
-  ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T);
+  ndm_units<R, ACT>(e, bits, hilb, sx + threadIdx.x, sg + threadIdx.x, T, s, n);
   cpx<R> acc = mk(R(0), R(0));
   int cnt = 0;
   for (int o = 0; o < op.n_ops; ++o) {
@@ -453,10 +460,15 @@ ndm_grad_kernel(NdmEff<R> e, DevOp op, const uint64_t* __restrict__ samples, int
       const int cc = wconn[(size_t)s * maxc + s_list_c[m]];
       const uint64_t bits = samples[s];
       // x_u at σ, then add the connection's change
-      cpx<R> xu = e.b[u];
-      for (int i = 0; i < e.N2; ++i) {
-        const R v = site_value<R>(bits, i, hilb);
-        if (v != R(0)) { const cpx<R> c = e.C[u + (size_t)U * i]; xu.x += c.x * v; xu.y += c.y * v; }
+      cpx<R> xu;
+      if (e.theta) {
+        xu = e.theta[(size_t)u * n + s];
+      } else {
+        xu = e.b[u];
+        for (int i = 0; i < e.N2; ++i) {
+          const R v = site_value<R>(bits, i, hilb);
+          if (v != R(0)) { const cpx<R> c = e.C[u + (size_t)U * i]; xu.x += c.x * v; xu.y += c.y * v; }
+        }
       }
       uint64_t nb = bits;
       const int nch = __ldg(op.conn_n_changes + cc);
@@ -624,9 +636,11 @@ cudaError_t launch_ndm_loc(const NdmEff<R>& e, int act, const DevOp& op, const u
 }
 
 template <typename R>
-cudaError_t launch_ndm_diag_obs(const NdmEff<R>& e, int act, const DevOp& op, const uint64_t* samples, int n,
+cudaError_t launch_ndm_diag_obs(const NdmEff<R>& e_in, int act, const DevOp& op, const uint64_t* samples, int n,
                                 int hilb, cpx<R>* logrho, cpx<R>* O, cudaStream_t st) {
   if (n < 1) return cudaSuccess;
+  NdmEff<R> e = e_in;
+  e.theta = nullptr;              // the (σ, σ) configurations are formed in the kernel
   const int T = ndm_threads<R>(e.U);
   const size_t smem = unit_smem<R>(e.U, T);
   cudaError_t err;

@@ -41,6 +41,10 @@ template <typename R> struct NdmEff {
   const cpx<R>* C = nullptr;   // [U x N2] column-major
   const cpx<R>* b = nullptr;   // [U]
   const cpx<R>* a = nullptr;   // [N2]
+  // optional [U][n] unit pre-activations θ_u = b_u + Σ_i C[u][i] v_i of the
+  // n samples being evaluated (the tensor-core θ of NQ_EVAL_TC_BF16X2/X3);
+  // null: the kernels form θ on CUDA cores
+  const cpx<R>* theta = nullptr;
 };
 
 template <typename R> struct NdmEffBufs {
