@@ -357,15 +357,31 @@ def precision_modes():
     out["dw_error_from_S"] = rel(np.linalg.solve(s1 + c["eps"] * eye, f1), np.linalg.solve(s0 + c["eps"] * eye, f1))
     out["solve_corrections"] = {"fp64_eval": ref.sr_info()[0],
                                 "precision_mode": fast.sr_info()[0]}
+    # θ of the density matrix on tcgen05: BF16 hi + lo (x2) and hi + mid + lo (x3)
+    for name, prec in (("theta_bf16x2", nq._lib.NQ_EVAL_TC_BF16X2), ("theta_bf16x3", nq._lib.NQ_EVAL_TC_BF16X3)):
+        e = engine(prec, nq._lib.NQ_S_TF32)
+        e.set_samples(samples)
+        mt, lt, ft = e.estimate(want_loc=True, want_force=True)
+        st_ = e.sr_matrix()
+        dt = e.precondition(0, c["eps"])
+        out["relative_error_vs_fp64_eval_" + name] = {
+            "L_loc": rel(lt, l0), "cost": abs(mt.mean_re - m0.mean_re) / abs(m0.mean_re), "F": rel(ft, f0),
+            "S": rel(st_, s0), "dw": rel(dt, d0)}
+        del e
     del ref, fast
     curves = {}
-    for name, sp in (("tf32", nq._lib.NQ_S_TF32), ("fp32", nq._lib.NQ_S_F32)):
-        e = engine(nq._lib.NQ_EVAL_F32, sp)
+    for name, prec, sp in (("tf32", nq._lib.NQ_EVAL_F32, nq._lib.NQ_S_TF32),
+                           ("fp32", nq._lib.NQ_EVAL_F32, nq._lib.NQ_S_F32),
+                           ("bf16_theta_tf32_S", nq._lib.NQ_EVAL_TC_BF16X2, nq._lib.NQ_S_TF32)):
+        e = engine(prec, sp)
         curves[name] = [e.vmc_step(it, c["eps"], c["lr"]).mean_re for it in range(c["sr_steps"])]
         del e
     out["cost_curve_tf32"] = curves["tf32"]
     out["cost_curve_fp32"] = curves["fp32"]
+    out["cost_curve_bf16_theta_tf32_S"] = curves["bf16_theta_tf32_S"]
     out["final_cost_relative_difference"] = abs(curves["tf32"][-1] - curves["fp32"][-1]) / abs(curves["fp32"][-1])
+    out["final_cost_relative_difference_bf16_theta"] = (abs(curves["bf16_theta_tf32_S"][-1] - curves["fp32"][-1]) /
+                                                        abs(curves["fp32"][-1]))
     return out
 
 
@@ -433,7 +449,7 @@ def learned_vs_local():
     and of |Σσz| per chain; the sampling time is the sampler stage's device
     time.  Energies of both samplers are reported with their difference."""
     import nqcuda as nq
-    from nqcuda.stats import integrated_autocorr_time
+    from nqcuda.stats import integrated_autocorr_time, autocorrelation
     c = LEARNED
     N = c["L"] * c["L"]
     hilb, H = _tfim2d(nq, c["L"], c["h"], c["J"])
@@ -479,12 +495,14 @@ def learned_vs_local():
         mz = np.abs(smp_.sum(axis=2)).astype(np.float64)
         tE = integrated_autocorr_time(loc.T)
         tM = integrated_autocorr_time(mz.T)
+        rhoE = autocorrelation(loc.T, 40)
         r = {"passes": e.passes, "sample_ms": ms, "tau_E": tE, "tau_absM": tM,
              "ess_per_s_E": loc.size / tE / (ms * 1e-3), "ess_per_s_absM": loc.size / tM / (ms * 1e-3),
              "energy_per_site": mm.mean_re / N, "energy_err_per_site": mm.error / N}
         if p_ar > 0:
             a, b = e.proposal_stats()
             r["ar_acceptance"] = b / max(a, 1)
+        r["_rhoE"] = rhoE
         del e
         return r
 
@@ -492,6 +510,31 @@ def learned_vs_local():
     mixed = [measure(c["p_ar"], p) for p in (1, 3)]
     bl = max(local, key=lambda r: r["ess_per_s_E"])
     bm = max(mixed, key=lambda r: r["ess_per_s_E"])
+    # Ceiling of the 50/50 mixture on this configuration, whatever the cost
+    # of an AR move: at one step per sample (the mixture's best spacing) half
+    # of the steps are local moves, so a step costs at least half a local
+    # step; an AR step can at most replace the state by an independent draw,
+    # so ρ_mix(k) >= (1/2)^k ρ_L(k) (every one of the k steps local) and
+    # τ_mix >= 1 + 2 Σ_k (1/2)^k ρ_L(k) ("perfect proposal").  With the trained
+    # proposal's measured τ_mix in place of that bound, the same formula
+    # gives the ceiling of this proposal at zero AR cost.
+    l1 = local[0]
+    ns_e = c["chains"] * c["ess_length"]
+    rho = l1["_rhoE"]
+    tau_perfect = 1.0 + 2.0 * float(sum(0.5 ** k * rho[k] for k in range(1, len(rho))))
+    half_step_s = 0.5 * l1["sample_ms"] * 1e-3
+    steps_per_chain = c["ess_length"] + c["ess_burn"]
+    ceiling = {
+        "tau_E_local_one_step": l1["tau_E"], "tau_E_mixture_measured": mixed[0]["tau_E"],
+        "tau_E_mixture_perfect_proposal_bound": tau_perfect,
+        "ess_ratio_ceiling_zero_ar_cost_measured_proposal": ns_e / mixed[0]["tau_E"] / half_step_s / bl["ess_per_s_E"],
+        "ess_ratio_ceiling_zero_ar_cost_perfect_proposal": ns_e / tau_perfect / half_step_s / bl["ess_per_s_E"],
+        "local_step_ns": l1["sample_ms"] * 1e6 / (c["chains"] * steps_per_chain),
+        "mixture_step_ns": mixed[0]["sample_ms"] * 1e6 / (c["chains"] * steps_per_chain),
+    }
+    ceiling["ar_move_ns"] = 2 * ceiling["mixture_step_ns"] - ceiling["local_step_ns"]
+    for r in local + mixed:
+        r.pop("_rhoE", None)
     return {"workload": "tfim2d_6x6_h3.04_rbm_alpha4_8192_chains", "sr_ms_per_step": sr_ms,
             "sr_steps_per_s": 1e3 / sr_ms,
             "matrix_free_cg": {"sr_ms_per_step": cg_ms, "sr_steps_per_s": 1e3 / cg_ms, "iterations": cg_iters,
@@ -500,6 +543,7 @@ def learned_vs_local():
             "made_nll_after_each_training": nll, "local": local, "learned_mixture": mixed,
             "best_local_ess_per_s_E": bl["ess_per_s_E"], "best_learned_ess_per_s_E": bm["ess_per_s_E"],
             "learned_over_local_ess_ratio": bm["ess_per_s_E"] / bl["ess_per_s_E"],
+            "mixture_ceiling": ceiling,
             "abs_dE_per_site_learned_vs_local": abs(bm["energy_per_site"] - bl["energy_per_site"])}
 
 

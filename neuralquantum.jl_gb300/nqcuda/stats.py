@@ -41,6 +41,22 @@ def integrated_autocorr_time(x, window=5.0):
     return max(tau, 1.0)
 
 
+def autocorrelation(x, max_lag):
+    """Chain-averaged normalised autocorrelation ρ(0..max_lag) of a
+    (chains, samples) series (ρ(0) = 1)."""
+    import numpy as np
+    v = np.asarray(x, dtype=np.complex128)
+    v = v - v.mean(axis=1, keepdims=True)
+    n = v.shape[1]
+    spec = np.fft.fft(v, n=2 * n, axis=1)
+    acov = np.fft.ifft(np.abs(spec) ** 2, axis=1)[:, :n].real.mean(axis=0)
+    if not acov[0] > 0:
+        out = np.zeros(max_lag + 1)
+        out[0] = 1.0
+        return out
+    return acov[:max_lag + 1] / acov[0]
+
+
 def effective_sample_size(x, window=5.0):
     """Number of samples divided by the integrated autocorrelation time."""
     import numpy as np
