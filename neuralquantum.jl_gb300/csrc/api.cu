@@ -864,6 +864,7 @@ nq_status nq_create_chain(const nq_config* cfg, int32_t n_layers, const nq_layer
 void nq_destroy(nq_handle* h) {
   if (!h) return;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->x_borrowed) { h->d_X = nullptr; h->d_Xlo = nullptr; }   // owned by the batch
   if (h->graph) cudaGraphExecDestroy(h->graph);
   proposal_destroy(h);
   free_op(h);
@@ -1685,6 +1686,19 @@ struct nq_batch {
   double* d_gather = nullptr;           // [np][8]
   double* h_gather = nullptr;           // pinned [np][8]
   int64_t launches = 0;
+  // grouped SR stages (every stage of all problems one launch): equal sample
+  // counts and S on tcgen05 (TF32 or 3xTF32)
+  bool grouped = false;
+  int split3 = 0;
+  float* d_Xall = nullptr;              // stacked X of all problems [Σ 2P][Ns_pad]
+  float* d_Xlo_all = nullptr;           // its 3xTF32 low part
+  int rows_total = 0, Ns_pad = 0;
+  float* d_slots = nullptr;             // Gram partial blocks of all problems
+  void* d_geom = nullptr;               // Gram geometry
+  GramGroupPlan gplan;
+  SrJob* d_jobs = nullptr;
+  int* d_prefix = nullptr;              // the prefix arrays of SrGroup, 9 x (np + 1)
+  SrGroup grp;
 };
 
 namespace {
@@ -1735,6 +1749,99 @@ void split_ctas(const std::vector<int>& P, int total, std::vector<int>& start) {
     extra = std::min(extra, std::max(0, nb - 1));
     start[p + 1] = start[p] + 1 + extra;
   }
+}
+
+// Grouped SR stages: one stacked X for all problems (each handle's X becomes
+// a row slice of it), the problem table and the prefix arrays of every
+// grouped kernel.  Needs equal sample counts and S on tcgen05 (TF32 or
+// 3xTF32); otherwise the step keeps one graph branch per problem.
+nq_status batch_setup_grouped(nq_batch* b) {
+  const int np = (int)b->hs.size();
+  const int sp = b->hs[0]->cfg.s_precision;
+  if (sp != NQ_S_TF32 && sp != NQ_S_TF32X3) return NQ_OK;
+  for (nq_handle* h : b->hs)
+    if (h->Ns != b->hs[0]->Ns || h->cfg.s_precision != sp || h->Ns_pad != b->hs[0]->Ns_pad) return NQ_OK;
+  b->split3 = sp == NQ_S_TF32X3 ? 1 : 0;
+  b->Ns_pad = b->hs[0]->Ns_pad;
+  std::vector<int> rows(np), off(np);
+  int tot = 0;
+  for (int p = 0; p < np; ++p) {
+    rows[p] = 2 * b->hs[p]->P;
+    off[p] = tot;
+    tot += rows[p];
+  }
+  b->rows_total = tot;
+  BCK(cudaMalloc(&b->d_Xall, (size_t)tot * b->Ns_pad * sizeof(float) + 16));
+  if (b->split3) BCK(cudaMalloc(&b->d_Xlo_all, (size_t)tot * b->Ns_pad * sizeof(float) + 16));
+  b->gplan = gram_group_plan(rows, b->Ns_pad);
+  BCK(cudaMalloc(&b->d_slots, gram_group_partial_elems(b->gplan) * sizeof(float) + 16));
+  BCK(cudaMalloc(&b->d_geom, gram_group_geom_bytes(np)));
+  BCK(gram_group_upload(b->gplan, b->d_geom, b->st));
+  std::vector<SrJob> jobs(np);
+  std::vector<int> pre(9 * (size_t)(np + 1), 0);
+  auto P_ = [&](int k, int p) -> int& { return pre[(size_t)k * (np + 1) + p]; };
+  size_t fsmem = 0;
+  for (int p = 0; p < np; ++p) {
+    nq_handle* h = b->hs[p];
+    // the handle's own X is replaced by its slice of the stacked X
+    if (!h->x_borrowed) {
+      cudaFree(h->d_X);
+      if (h->d_Xlo) cudaFree(h->d_Xlo);
+    }
+    h->d_X = b->d_Xall + (size_t)off[p] * b->Ns_pad;
+    h->d_Xlo = b->split3 ? b->d_Xlo_all + (size_t)off[p] * b->Ns_pad : nullptr;
+    h->x_borrowed = true;
+    SrJob& j = jobs[p];
+    j.N = h->N; j.M = h->M; j.P = h->P; j.hilb = h->hilb; j.act = h->act; j.Ns = h->Ns; j.B = h->B; j.L = h->L;
+    j.Ns_pad = h->Ns_pad;
+    j.force_CH = rbm_force_chunk(h->N, h->M);
+    j.force_nblk = (h->Ns + j.force_CH - 1) / j.force_CH;
+    fsmem = std::max(fsmem, rbm_force_smem(h->N, h->M));
+    j.samples = h->d_samples;
+    j.g = reinterpret_cast<const float2*>(h->d_g);
+    j.eloc = reinterpret_cast<const float2*>(h->d_eloc);
+    j.fb = h->fb;
+    j.chainstats = h->d_chainstats;
+    j.stats = h->d_stats;
+    j.X = h->d_X;
+    j.Xlo = h->d_Xlo;
+    j.G = h->d_G;
+    j.S = h->d_S;
+    j.W = h->sb.W;
+    j.x = h->sb.x;
+    j.r = h->sb.r;
+    j.rf = h->sb.rf;
+    j.norms = h->sb.norms;
+    j.status = h->sb.status;
+    j.master = h->d_master;
+    j.p32 = h->d_p32;
+    j.t0 = reinterpret_cast<float2*>(h->d_tab[0]);
+    j.t1 = reinterpret_cast<float2*>(h->d_tab[1]);
+    j.t2 = reinterpret_cast<float2*>(h->d_tab[2]);
+    const int units[9] = {j.force_nblk, h->P + 1, h->P, (h->B + 63) / 64, ((h->Ns_pad + 1023) / 1024) * (h->M + 1),
+                          h->P * h->P, ((h->P + 31) / 32) * ((h->P + 31) / 32), 2 * h->P, h->N * h->M};
+    for (int k = 0; k < 9; ++k) P_(k, p + 1) = P_(k, p) + units[k];
+  }
+  BCK(cudaMalloc((void**)&b->d_jobs, np * sizeof(SrJob)));
+  BCK(cudaMalloc((void**)&b->d_prefix, pre.size() * sizeof(int)));
+  BCK(cudaMemcpy(b->d_jobs, jobs.data(), np * sizeof(SrJob), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_prefix, pre.data(), pre.size() * sizeof(int), cudaMemcpyHostToDevice));
+  SrGroup& g = b->grp;
+  g.np = np;
+  g.jobs = b->d_jobs;
+  const int* d = b->d_prefix;
+  auto dp = [&](int k) { return d + (size_t)k * (np + 1); };
+  g.force_blk = dp(0); g.force_blocks = P_(0, np); g.force_smem = fsmem;
+  g.force_warp = dp(1); g.force_warps = P_(1, np);
+  g.pelem = dp(2); g.pelems = P_(2, np);
+  g.stat_blk = dp(3); g.stat_blocks = P_(3, np);
+  g.x_blk = dp(4); g.x_blocks = P_(4, np);
+  g.pp_elem = dp(5); g.pp_elems = P_(5, np);
+  g.fill_blk = dp(6); g.fill_blocks = P_(6, np);
+  g.master_elem = dp(7); g.master_elems = P_(7, np);
+  g.tab_elem = dp(8); g.tab_elems = P_(8, np);
+  b->grouped = true;
+  return NQ_OK;
 }
 
 nq_status batch_build_tables(nq_batch* b) {
@@ -1869,36 +1976,53 @@ nq_status batch_capture(nq_batch* b, double eps, double lr) {
   ck(launch_rbm_eval_batch<float>(b->d_ejobs, b->d_eblk, np, b->e_blocks, b->M_max, b->N_max, b->act, b->eval_T,
                                   b->st), "batched estimator");
   b->launches += 2;
-  // branches: force + statistics, S, shifted copy
-  ck(cudaEventRecord(b->fork, b->st), "fork");
-  for (int p = 0; p < np && s == NQ_OK; ++p) {
-    nq_handle* h = b->hs[p];
-    ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch");
-    if (s == NQ_OK) s = stage_force(h);
-    if (s == NQ_OK) s = stage_S(h);
-    if (s == NQ_OK) {
-      ck(launch_sr_shift(h->sb, h->P, 0, eps, 0.0, h->st), "shift");
-      ++h->launches;
+  if (b->grouped) {
+    // every SR stage of all problems as one launch (one kernel per stage)
+    const SrGroup& gp = b->grp;
+    ck(launch_force_group(gp, b->st), "grouped force");
+    ck(launch_stats_group(gp, b->st), "grouped statistics");
+    ck(launch_build_X_group(gp, b->split3, b->st), "grouped X");
+    ck(launch_gram_group(b->d_Xall, b->d_Xlo_all, b->rows_total, b->Ns_pad, b->split3, b->gplan, b->d_geom, gp,
+                         b->d_slots, b->hs[0]->sb.status, b->st), "grouped S accumulation");
+    ck(launch_assemble_shift_group(gp, eps, b->st), "grouped S and shift");
+    ck(launch_spd_inverse_batch(b->d_wjobs, b->d_wcta, np, b->w_ctas, b->d_ctl, (size_t)np * 64, b->st),
+       "batched inversion");
+    ck(launch_fill_group(gp, b->st), "grouped fill");
+    ck(launch_refine_group(gp, b->d_wcta, b->w_ctas, b->d_ctl, eps, kSolveRefine, b->st), "grouped refinement");
+    ck(launch_update_group(gp, lr, b->st), "grouped update");
+    b->launches += 14;
+  } else {
+    // branches: force + statistics, S, shifted copy
+    ck(cudaEventRecord(b->fork, b->st), "fork");
+    for (int p = 0; p < np && s == NQ_OK; ++p) {
+      nq_handle* h = b->hs[p];
+      ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch");
+      if (s == NQ_OK) s = stage_force(h);
+      if (s == NQ_OK) s = stage_S(h);
+      if (s == NQ_OK) {
+        ck(launch_sr_shift(h->sb, h->P, 0, eps, 0.0, h->st), "shift");
+        ++h->launches;
+      }
+      ck(cudaEventRecord(b->join[p], h->st), "join");
+      ck(cudaStreamWaitEvent(b->st, b->join[p], 0), "join wait");
     }
-    ck(cudaEventRecord(b->join[p], h->st), "join");
-    ck(cudaStreamWaitEvent(b->st, b->join[p], 0), "join wait");
-  }
-  // one cooperative launch inverts every problem's shifted S
-  ck(launch_spd_inverse_batch(b->d_wjobs, b->d_wcta, np, b->w_ctas, b->d_ctl, (size_t)np * 64, b->st),
-     "batched inversion");
-  ++b->launches;
-  ck(cudaEventRecord(b->fork, b->st), "fork 2");
-  for (int p = 0; p < np && s == NQ_OK; ++p) {
-    nq_handle* h = b->hs[p];
-    ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch 2");
-    if (s == NQ_OK) {
-      ck(launch_sr_finish(h->sb, h->P, h->fb.force, 0, eps, 0.0, !h->complex_params, kSolveRefineBatch, h->st),
-         "solve");
-      h->launches += 2 + 3 * (kSolveRefineBatch + 1);
+    // one cooperative launch inverts every problem's shifted S
+    ck(launch_spd_inverse_batch(b->d_wjobs, b->d_wcta, np, b->w_ctas, b->d_ctl, (size_t)np * 64, b->st),
+       "batched inversion");
+    ++b->launches;
+    ck(cudaEventRecord(b->fork, b->st), "fork 2");
+    for (int p = 0; p < np && s == NQ_OK; ++p) {
+      nq_handle* h = b->hs[p];
+      ck(cudaStreamWaitEvent(h->st, b->fork, 0), "branch 2");
+      if (s == NQ_OK) {
+        ck(launch_sr_finish(h->sb, h->P, h->fb.force, 0, eps, 0.0, !h->complex_params, kSolveRefineBatch, h->st),
+           "solve");
+        h->launches += 2 + 3 * (kSolveRefineBatch + 1);
+      }
+      if (s == NQ_OK) s = stage_update(h, lr);
+      ck(cudaEventRecord(b->join[p], h->st), "join 2");
+      ck(cudaStreamWaitEvent(b->st, b->join[p], 0), "join wait 2");
     }
-    if (s == NQ_OK) s = stage_update(h, lr);
-    ck(cudaEventRecord(b->join[p], h->st), "join 2");
-    ck(cudaStreamWaitEvent(b->st, b->join[p], 0), "join wait 2");
   }
   if (s == NQ_OK) {
     batch_gather_kernel<<<(np + 63) / 64, 64, 0, b->st>>>(np, b->d_stat_src, b->d_status_src, b->d_acc,
@@ -1972,6 +2096,7 @@ nq_status nq_batch_create(const nq_config* cfgs, int32_t n, nq_batch** out) {
                   cudaMalloc((void**)&b->d_status_src, n * sizeof(int*)) == cudaSuccess &&
                   cudaMalloc((void**)&b->d_gather, (size_t)n * 8 * sizeof(double)) == cudaSuccess;
   if (!ok) return cleanup(NQ_ERR_CUDA);
+  if (nq_status s = batch_setup_grouped(b)) return cleanup(s);
   *out = b;
   return NQ_OK;
 }
@@ -1982,7 +2107,8 @@ void nq_batch_destroy(nq_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (nq_handle* h : b->hs) nq_destroy(h);
   void* bufs[] = {b->d_call, b->d_sjobs, b->d_ejobs, b->d_wjobs, b->d_sblk, b->d_eblk, b->d_wcta, b->d_ctl,
-                  b->d_acc, b->d_stat_src, b->d_status_src, b->d_gather};
+                  b->d_acc, b->d_stat_src, b->d_status_src, b->d_gather, b->d_Xall, b->d_Xlo_all, b->d_slots,
+                  b->d_geom, b->d_jobs, b->d_prefix};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->h_call) cudaFreeHost(b->h_call);

@@ -110,6 +110,7 @@ struct nq_handle {
   double* h_cginfo = nullptr;      // pinned [2]
   bool tc_theta = false;           // NQ_EVAL_TC_BF16X2 / X3: θ = Wσ + b on tcgen05
   int theta_terms = 2;             // BF16 terms of W (2 or 3)
+  bool x_borrowed = false;         // d_X / d_Xlo are row slices of a batch's stacked X
   __nv_bfloat16* d_theta_img = nullptr;   // packed BF16 hi/lo image of W (density matrices: of C)
   cpx<float>* d_ndm_theta = nullptr;      // density matrices with θ on tcgen05: [U][Ns] θ of the samples
 };

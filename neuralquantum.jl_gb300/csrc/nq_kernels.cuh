@@ -2,6 +2,9 @@
 // libnqcuda.  Every launcher returns a cudaError_t and enqueues on `st`.
 #pragma once
 #include <cuda_bf16.h>
+
+#include <vector>
+
 #include "nq_common.cuh"
 
 // Flattened operator on the device (see nq_op_table in include/nqcuda.h).
@@ -375,3 +378,99 @@ cudaError_t launch_unpack_int8(const uint64_t* bits, int nsites, long n, int hil
 template <typename R>
 cudaError_t launch_rbm_grad_matrix(const uint64_t* samples, int n, int N, int M, int hilb,
                                    const cpx<R>* g, double* out, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Grouped SR stages of the many-problem step: every stage of all problems is
+// one launch.  A grouped kernel's work units (blocks, warps or elements) are
+// split over the problems by a prefix array start[0..np] in device memory:
+// problem p owns units [start[p], start[p+1]).
+// ---------------------------------------------------------------------------
+NQ_D int group_of(int unit, const int* __restrict__ start, int np) {
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {                       // last p with start[p] <= unit
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(start + mid) <= unit) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One problem of a grouped FP32 RBM SR step: its sizes and device buffers
+// (the problem handle's own, except X, which is a row slice of the batch's
+// stacked X).
+struct SrJob {
+  int N, M, P, hilb, act, Ns, B, L, Ns_pad;
+  int force_CH, force_nblk;                 // force partial sums: samples per block, blocks
+  const uint64_t* samples;
+  const float2* g;                          // [M][Ns] f'(θ)
+  const float2* eloc;                       // [Ns]
+  ForceBufs fb;
+  double* chainstats;                       // stats_scratch_doubles(B)
+  double* stats;                            // [6]
+  float* X;                                 // [2P][Ns_pad] row slice of the stacked X
+  float* Xlo;                               // 3xTF32 low part (or null)
+  float* G;                                 // [2P][2P]
+  double* S;                                // [P][P] complex
+  float2* W;                                // shifted S, then -(S + shift)^-1
+  double* x;                                // [P] complex solution
+  double* r;                                // [P] complex residual
+  float2* rf;                               // [P] FP32 right-hand side
+  double* norms;                            // refine_norm_doubles()
+  int* status;
+  double* master;                           // FP64 parameters (complex)
+  float* p32;                               // FP32 parameters
+  float2* t0;                               // per-flip tables [N*M]
+  float2* t1;
+  float2* t2;
+};
+
+// Prefix arrays (device, np + 1 entries) and totals of the grouped stages.
+struct SrGroup {
+  int np = 0;
+  const SrJob* jobs = nullptr;
+  const int* force_blk = nullptr; int force_blocks = 0; size_t force_smem = 0;
+  const int* force_warp = nullptr; int force_warps = 0;       // P + 1 warps per problem
+  const int* pelem = nullptr; int pelems = 0;                 // P elements per problem
+  const int* stat_blk = nullptr; int stat_blocks = 0;         // ceil(B / 64) blocks
+  const int* x_blk = nullptr; int x_blocks = 0;               // ceil(Ns_pad / 1024) * (M + 1) blocks
+  const int* pp_elem = nullptr; int pp_elems = 0;             // P * P elements
+  const int* fill_blk = nullptr; int fill_blocks = 0;         // ceil(P / 32)^2 tiles
+  const int* master_elem = nullptr; int master_elems = 0;     // 2P doubles
+  const int* tab_elem = nullptr; int tab_elems = 0;           // N * M table entries
+};
+// force partial sums, their reductions and F of every problem
+cudaError_t launch_force_group(const SrGroup& g, cudaStream_t st);
+// FP32 force-kernel geometry of one problem: samples per block, shared memory
+int rbm_force_chunk(int N, int M);
+size_t rbm_force_smem(int N, int M);
+// Measurement statistics of every problem's E_loc
+cudaError_t launch_stats_group(const SrGroup& g, cudaStream_t st);
+// X of every problem (TF32-rounded; Xlo when split3)
+cudaError_t launch_build_X_group(const SrGroup& g, int split3, cudaStream_t st);
+// S = conj(G)/Ns per problem, then the shifted copy W = S + eps I
+cudaError_t launch_assemble_shift_group(const SrGroup& g, double eps, cudaStream_t st);
+// Hermitian fill of every inverted W
+cudaError_t launch_fill_group(const SrGroup& g, cudaStream_t st);
+// FP64-residual refinement of every problem in one cooperative launch: problem
+// p runs on CTAs [cta_start[p], cta_start[p+1]) with barrier block p of
+// ctl_base (64 bytes each, zeroed here); max_corr corrections at most, each
+// problem stopping once its correction is below kRefineTol of its solution
+cudaError_t launch_refine_group(const SrGroup& g, const int* cta_start, int total_ctas, void* ctl_base,
+                                double eps, int max_corr, cudaStream_t st);
+// w -= lr Δw on the FP64 master, its FP32 copy and the per-flip tables
+cudaError_t launch_update_group(const SrGroup& g, double lr, cudaStream_t st);
+// G = X Xᵀ of every problem on tcgen05 from one stacked X (rows_total x Ns_pad,
+// problem p's 2P_p rows starting at row_off[p]; Ns_pad equal for all).
+// split3: 3xTF32 from X and Xlo.  The host plan lives in `plan` (built by
+// gram_group_plan); slots: gram_group_partial_elems floats; geom: device
+// buffer of gram_group_geom_bytes.  G of problem p goes to jobs[p].G.
+struct GramGroupPlan {
+  int np = 0, ks = 1, per = 0, nch = 0, items = 0, ncta = 0, tiles = 0;
+  std::vector<int> rows, row_off, nblocks, item0, tile0;
+};
+GramGroupPlan gram_group_plan(const std::vector<int>& rows, int Ns_pad);
+size_t gram_group_partial_elems(const GramGroupPlan& p);
+size_t gram_group_geom_bytes(int np);
+cudaError_t gram_group_upload(const GramGroupPlan& p, void* geom_dev, cudaStream_t st);
+cudaError_t launch_gram_group(const float* X, const float* Xlo, int rows_total, int Ns_pad, int split3,
+                              const GramGroupPlan& p, const void* geom_dev, const SrGroup& g, float* slots,
+                              int* err, cudaStream_t st);

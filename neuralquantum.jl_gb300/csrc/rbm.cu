@@ -23,8 +23,7 @@ __global__ void master_to_f32_kernel(const double* m, long n, float* out) {
 }
 
 template <typename R>
-__global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;   // idx = i*M + h
+NQ_D void rbm_tables_elem(const RbmDev<R>& net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2, int idx) {   // idx = i*M + h
   if (idx >= net.N * net.M) return;
   int i = idx / net.M, h = idx % net.M;
   // compute in double for accuracy, store as R
@@ -45,6 +44,27 @@ __global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>*
   t0[idx] = mk((R)c0.x, (R)c0.y);
   t1[idx] = mk((R)c1.x, (R)c1.y);
   t2[idx] = mk((R)c2.x, (R)c2.y);
+}
+
+template <typename R>
+__global__ void rbm_tables_kernel(RbmDev<R> net, cpx<R>* t0, cpx<R>* t1, cpx<R>* t2) {
+  rbm_tables_elem<R>(net, t0, t1, t2, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// per-flip tables of every problem of a grouped step from its FP32 parameters
+__global__ void tables_group_kernel(SrGroup g) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.tab_elems) return;
+  const int p = group_of(e, g.tab_elem, g.np);
+  const SrJob& j = g.jobs[p];
+  RbmDev<float> net;
+  net.N = j.N; net.M = j.M; net.act = j.act; net.hilb = j.hilb;
+  const cpx<float>* base = reinterpret_cast<const cpx<float>*>(j.p32);
+  net.a = base;
+  net.b = base + j.N;
+  net.W = base + j.N + j.M;
+  rbm_tables_elem<float>(net, reinterpret_cast<cpx<float>*>(j.t0), reinterpret_cast<cpx<float>*>(j.t1),
+                         reinterpret_cast<cpx<float>*>(j.t2), e - __ldg(g.tab_elem + p));
 }
 
 template <typename R>
@@ -325,14 +345,13 @@ NQ_D void kahan_add(cpx<R>& s, cpx<R>& c, cpx<R> x) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256)
-rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ samples, int Ns,
-                         const cpx<R>* __restrict__ g, const cpx<R>* __restrict__ eloc, int CH,
-                         double* __restrict__ partial, double* __restrict__ partialE) {
+NQ_D void force_partial_block(int N, int M, int hilb, const uint64_t* __restrict__ samples, int Ns,
+                              const cpx<R>* __restrict__ g, const cpx<R>* __restrict__ eloc, int CH,
+                              double* __restrict__ partial, double* __restrict__ partialE, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int P = N + M + M * N;
   const int NJ = (N + 3) & ~3;                         // sites padded to groups of 4
-  const int s0 = blockIdx.x * CH;
+  const int s0 = blk * CH;
   const int n = min(CH, Ns - s0);
   cpx<R>* s_g = reinterpret_cast<cpx<R>*>(smem_raw);   // [CH][M]: consecutive h conflict-free
   cpx<R>* s_e = s_g + (size_t)M * CH;                  // [CH]
@@ -347,7 +366,7 @@ rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ sa
     for (int j = 0; j < NJ; ++j) s_v[t * NJ + j] = (t < n && j < N) ? site_value<R>(bits, j, hilb) : R(0);
   }
   __syncthreads();
-  double* dst = partial + (size_t)blockIdx.x * 4 * P;
+  double* dst = partial + (size_t)blk * 4 * P;
   const int nW = M * (NJ / 4);
   for (int item = threadIdx.x; item < nW + M + N; item += blockDim.x) {
     if (item < nW) {
@@ -421,18 +440,24 @@ rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ sa
   if (threadIdx.x == 0) {
     double ex = 0, ey = 0;
     for (int t = 0; t < n; ++t) { ex += (double)s_e[t].x; ey += (double)s_e[t].y; }
-    partialE[2 * blockIdx.x] = ex;
-    partialE[2 * blockIdx.x + 1] = ey;
+    partialE[2 * blk] = ex;
+    partialE[2 * blk + 1] = ey;
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ samples, int Ns,
+                         const cpx<R>* __restrict__ g, const cpx<R>* __restrict__ eloc, int CH,
+                         double* __restrict__ partial, double* __restrict__ partialE) {
+  force_partial_block<R>(N, M, hilb, samples, Ns, g, eloc, CH, partial, partialE, blockIdx.x);
 }
 
 // Deterministic FP64 reduction of the per-chunk partials: one warp per
 // parameter (index P carries ΣE), lanes stride over chunks, fixed-order
 // shuffle tree.  sums[0..2P) = ΣO, [2P..4P) = ΣE conj(O), [4P..4P+2) = ΣE.
-__global__ void force_sums_kernel(int P, int nblk, const double* __restrict__ partial,
-                                  const double* __restrict__ partialE, double* __restrict__ sums) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w > P) return;
+NQ_D void force_sums_warp(int P, int nblk, const double* __restrict__ partial, const double* __restrict__ partialE,
+                          double* __restrict__ sums, int w, int lane) {
   double a = 0, b = 0, c = 0, d = 0;
   if (w < P) {
     for (int k = lane; k < nblk; k += 32) {
@@ -459,10 +484,16 @@ __global__ void force_sums_kernel(int P, int nblk, const double* __restrict__ pa
   }
 }
 
+__global__ void force_sums_kernel(int P, int nblk, const double* __restrict__ partial,
+                                  const double* __restrict__ partialE, double* __restrict__ sums) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w > P) return;
+  force_sums_warp(P, nblk, partial, partialE, sums, w, lane);
+}
+
 // <O> = ΣO/Ns, <E> = ΣE/Ns, F = ΣE conj(O)/Ns - <E> conj(<O>)
-__global__ void force_finalize_kernel(int P, int Ns, const double* __restrict__ sums, double* meanO,
-                                      double* force, double* meanE) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+NQ_D void force_finalize_elem(int P, int Ns, const double* __restrict__ sums, double* meanO, double* force,
+                              double* meanE, int p) {
   const double ex = sums[4 * P] / Ns, ey = sums[4 * P + 1] / Ns;
   if (p == 0) { meanE[0] = ex; meanE[1] = ey; }
   if (p >= P) return;
@@ -472,6 +503,48 @@ __global__ void force_finalize_kernel(int P, int Ns, const double* __restrict__ 
   fx -= ex * ox + ey * oy;
   fy -= ey * ox - ex * oy;
   force[2 * p] = fx; force[2 * p + 1] = fy;
+}
+
+__global__ void force_finalize_kernel(int P, int Ns, const double* __restrict__ sums, double* meanO,
+                                      double* force, double* meanE) {
+  force_finalize_elem(P, Ns, sums, meanO, force, meanE, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ---- grouped forms (many-problem step, FP32): the problem of a unit from the prefix arrays
+__global__ void __launch_bounds__(256) force_partial_group_kernel(SrGroup g) {
+  const int p = group_of(blockIdx.x, g.force_blk, g.np);
+  const SrJob& j = g.jobs[p];
+  force_partial_block<float>(j.N, j.M, j.hilb, j.samples, j.Ns, reinterpret_cast<const cpx<float>*>(j.g),
+                             reinterpret_cast<const cpx<float>*>(j.eloc), j.force_CH, j.fb.partial,
+                             j.fb.partialE, blockIdx.x - __ldg(g.force_blk + p));
+}
+
+__global__ void force_sums_group_kernel(SrGroup g) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= g.force_warps) return;
+  const int p = group_of(w, g.force_warp, g.np);
+  const SrJob& j = g.jobs[p];
+  force_sums_warp(j.P, j.force_nblk, j.fb.partial, j.fb.partialE, j.fb.sums, w - __ldg(g.force_warp + p), lane);
+}
+
+__global__ void force_finalize_group_kernel(SrGroup g) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.pelems) return;
+  const int p = group_of(e, g.pelem, g.np);
+  const SrJob& j = g.jobs[p];
+  force_finalize_elem(j.P, j.Ns, j.fb.sums, j.fb.meanO, j.fb.force, j.fb.meanE, e - __ldg(g.pelem + p));
+}
+
+// w -= lr Δw on the FP64 master (complex parameters, 2P doubles) and its FP32 copy
+__global__ void update_group_kernel(SrGroup g, double lr) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.master_elems) return;
+  const int p = group_of(e, g.master_elem, g.np);
+  const SrJob& j = g.jobs[p];
+  const int i = e - __ldg(g.master_elem + p);
+  const double w = j.master[i] - lr * j.x[i];
+  j.master[i] = w;
+  j.p32[i] = (float)w;
 }
 
 template <typename R>
@@ -679,3 +752,30 @@ template cudaError_t launch_rbm_force<float>(const RbmDev<float>&, const uint64_
 template cudaError_t launch_rbm_force<double>(const RbmDev<double>&, const uint64_t*, int, const cpx<double>*, const cpx<double>*, const ForceBufs&, cudaStream_t);
 template cudaError_t launch_rbm_grad_matrix<float>(const uint64_t*, int, int, int, int, const cpx<float>*, double*, cudaStream_t);
 template cudaError_t launch_rbm_grad_matrix<double>(const uint64_t*, int, int, int, int, const cpx<double>*, double*, cudaStream_t);
+
+cudaError_t launch_force_group(const SrGroup& g, cudaStream_t st) {
+  if (g.force_smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(force_partial_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)g.force_smem);
+    if (e != cudaSuccess) return e;
+  }
+  force_partial_group_kernel<<<g.force_blocks, 256, g.force_smem, st>>>(g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  force_sums_group_kernel<<<(g.force_warps + 7) / 8, 256, 0, st>>>(g);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  force_finalize_group_kernel<<<(g.pelems + 255) / 256, 256, 0, st>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update_group(const SrGroup& g, double lr, cudaStream_t st) {
+  update_group_kernel<<<(g.master_elems + 255) / 256, 256, 0, st>>>(g, lr);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  tables_group_kernel<<<(g.tab_elems + 127) / 128, 128, 0, st>>>(g);
+  return cudaGetLastError();
+}
+
+int rbm_force_chunk(int N, int M) { return force_chunk(N, M, (int)sizeof(cpx<float>)); }
+size_t rbm_force_smem(int N, int M) { return force_smem(N, M, rbm_force_chunk(N, M), (int)sizeof(cpx<float>)); }

@@ -386,9 +386,8 @@ __global__ void __launch_bounds__(256, 2) sweep_batch_kernel(const SweepJob* __r
 }
 
 // W upper = conj(W lower) so that column i holds row i of the Hermitian matrix
-__global__ void herm_fill_kernel(float2* __restrict__ W, int P) {
-  __shared__ float2 t[32][33];
-  const int bi = blockIdx.y, bj = blockIdx.x;       // source tile (bi, bj), bi > bj, lower
+NQ_D void herm_fill_tile(float2* __restrict__ W, int P, int bi, int bj) {
+  __shared__ float2 t[32][33];                      // source tile (bi, bj), bi > bj, lower
   if (bi < bj) return;
   const int r = threadIdx.x, c0 = threadIdx.y;
   for (int c = c0; c < 32; c += blockDim.y) {
@@ -404,6 +403,15 @@ __global__ void herm_fill_kernel(float2* __restrict__ W, int P) {
       W[(size_t)gi + (size_t)P * gj] = make_float2(v.x, -v.y);
     }
   }
+}
+
+__global__ void herm_fill_kernel(float2* __restrict__ W, int P) { herm_fill_tile(W, P, blockIdx.y, blockIdx.x); }
+
+__global__ void herm_fill_group_kernel(SrGroup g) {
+  const int p = group_of(blockIdx.x, g.fill_blk, g.np);
+  const SrJob& j = g.jobs[p];
+  const int nb = (j.P + 31) / 32, local = blockIdx.x - __ldg(g.fill_blk + p);
+  herm_fill_tile(j.W, j.P, local / nb, local % nb);
 }
 
 // y = -W x for the full Hermitian W (= A^-1 after the sweep): one warp per
@@ -443,18 +451,17 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
 // the shifted system (limited by the FP64 residual, about cond(A) 1e-16).
 // The last residual stays in r; info = [corrections, |y|/|x| of the last one].
 // A non-finite x sets NQ_DEVERR_NONFINITE in the status word.
-__global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restrict__ W, const double* __restrict__ S,
-                                                          int P, const double* __restrict__ F, int kind, double eps,
-                                                          double lam, int real_params, int max_corr, double tol,
-                                                          double* x, double* r, float2* rf, double* norms,
-                                                          double* info, SweepCtl* ctl, int* status,
-                                                          uint64_t limit_ns) {
+// The refinement of one matrix on the CTAs rank = 0..nranks-1 that share ctl.
+NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restrict__ S, int P,
+                            const double* __restrict__ F, int kind, double eps, double lam, int real_params,
+                            int max_corr, double tol, double* x, double* r, float2* rf, double* norms, double* info,
+                            SweepCtl* ctl, int* status, uint64_t limit_ns, int rank, int nranks) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + wib, nw = gridDim.x * (blockDim.x >> 5);
+  const int gw = rank * (blockDim.x >> 5) + wib, nw = nranks * (blockDim.x >> 5);
   __shared__ double s_red[2][8];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x)
+  for (int i = rank * blockDim.x + threadIdx.x; i < P; i += nranks * blockDim.x)
     rf[i] = make_float2((float)F[2 * i], real_params ? 0.f : (float)F[2 * i + 1]);
-  if (!group_barrier(ctl, gridDim.x, status, limit_ns)) return;
+  if (!group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
   for (int it = 0;; ++it) {
     double yy = 0.0, xx = 0.0;
     bool finite = true;
@@ -491,7 +498,7 @@ __global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restri
       norms[2 * gw + 1] = xx;
       if (!finite) atomicOr(status, NQ_DEVERR_NONFINITE);
     }
-    if (!group_barrier(ctl, gridDim.x, status, limit_ns)) return;
+    if (!group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
     // |y|² and |x|² of this pass, summed by every CTA in the same order
     double ty = 0.0, tx = 0.0;
     for (int w = threadIdx.x; w < nw; w += blockDim.x) {
@@ -515,7 +522,7 @@ __global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restri
       tx += s_red[1][w];
     }
     const bool last = (it > 0 && ty <= tol * tol * tx) || it >= max_corr || !(tx == tx);
-    if (last && blockIdx.x == 0 && threadIdx.x == 0 && info) {
+    if (last && rank == 0 && threadIdx.x == 0 && info) {
       info[0] = (double)it;
       info[1] = tx > 0.0 ? sqrt(ty / tx) : 0.0;
     }
@@ -546,8 +553,30 @@ __global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restri
       }
     }
     if (last) break;
-    if (!group_barrier(ctl, gridDim.x, status, limit_ns)) return;
+    if (!group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
   }
+}
+
+__global__ void __launch_bounds__(256) refine_coop_kernel(const float2* __restrict__ W, const double* __restrict__ S,
+                                                          int P, const double* __restrict__ F, int kind, double eps,
+                                                          double lam, int real_params, int max_corr, double tol,
+                                                          double* x, double* r, float2* rf, double* norms,
+                                                          double* info, SweepCtl* ctl, int* status,
+                                                          uint64_t limit_ns) {
+  refine_group_body(W, S, P, F, kind, eps, lam, real_params, max_corr, tol, x, r, rf, norms, info, ctl, status,
+                    limit_ns, blockIdx.x, gridDim.x);
+}
+
+// every problem of a grouped step: problem p on CTAs [cta_start[p], cta_start[p+1])
+// with barrier block p (64 bytes) of ctl_base; sr_shift (eps), complex parameters
+__global__ void __launch_bounds__(256) refine_group_kernel(SrGroup g, const int* __restrict__ cta_start,
+                                                           char* ctl_base, double eps, int max_corr) {
+  const int p = group_of(blockIdx.x, cta_start, g.np);
+  const SrJob& j = g.jobs[p];
+  const int r0 = __ldg(cta_start + p), n = __ldg(cta_start + p + 1) - r0;
+  refine_group_body(j.W, j.S, j.P, j.fb.force, 0, eps, 0.0, 0, max_corr, kRefineTol, j.x, j.r, j.rf, j.norms,
+                    nullptr, reinterpret_cast<SweepCtl*>(ctl_base + (size_t)p * 64), j.status, kNqWaitNs,
+                    blockIdx.x - r0, n);
 }
 
 }  // namespace
@@ -649,4 +678,27 @@ cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const do
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, refine_coop_kernel, W, S, P, F, kind, eps, lam, real_params ? 1 : 0, max_corr, tol,
                             x, r, rf, norms, info, reinterpret_cast<SweepCtl*>(ctl), status, wait_ns);
+}
+
+cudaError_t launch_fill_group(const SrGroup& g, cudaStream_t st) {
+  herm_fill_group_kernel<<<g.fill_blocks, dim3(32, 8), 0, st>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine_group(const SrGroup& g, const int* cta_start, int total_ctas, void* ctl_base, double eps,
+                                int max_corr, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(ctl_base, 0, (size_t)g.np * 64, st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(total_ctas);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, refine_group_kernel, g, cta_start, reinterpret_cast<char*>(ctl_base), eps,
+                            max_corr);
 }

@@ -154,11 +154,10 @@ __device__ __forceinline__ void put_x_row(float* X, float* Xlo, int row, int Ns_
 // stores coalesced across the warp: the kernel is bound by the X writes
 // (4 rows Ns_pad bytes, twice with Xlo, half with BF16), not by re-reads.
 template <bool BF16>
-__global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int Ns_pad, float* __restrict__ X,
-                                                      float* __restrict__ Xlo) {
-  const int u = blockIdx.y;
+NQ_D void build_X_block(const RbmOSource& src, int Ns_pad, float* __restrict__ X, float* __restrict__ Xlo, int bx,
+                        int u) {
   const int N = src.N, M = src.M, Ns = src.Ns, hilb = src.hilb;
-  const int s0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  const int s0 = (bx * blockDim.x + threadIdx.x) * 4;
   if (s0 >= Ns_pad) return;
   uint64_t bits[4];
   float2 g[4];
@@ -210,6 +209,25 @@ __global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int Ns_pad
   }
 }
 
+template <bool BF16>
+__global__ void __launch_bounds__(256) build_X_kernel(RbmOSource src, int Ns_pad, float* __restrict__ X,
+                                                      float* __restrict__ Xlo) {
+  build_X_block<BF16>(src, Ns_pad, X, Xlo, blockIdx.x, blockIdx.y);
+}
+
+// grouped: problem p owns blocks [x_blk[p], x_blk[p+1]) = (M + 1) units x
+// ceil(Ns_pad / 1024) sample ranges, unit-major
+__global__ void __launch_bounds__(256) build_X_group_kernel(SrGroup g, int split3) {
+  const int p = group_of(blockIdx.x, g.x_blk, g.np);
+  const SrJob& j = g.jobs[p];
+  const int local = blockIdx.x - __ldg(g.x_blk + p);
+  const int nbx = (j.Ns_pad + 1023) / 1024;
+  RbmOSource src;
+  src.N = j.N; src.M = j.M; src.hilb = j.hilb; src.Ns = j.Ns;
+  src.samples = j.samples; src.g = j.g; src.meanO = j.fb.meanO;
+  build_X_block<false>(src, j.Ns_pad, j.X, split3 ? j.Xlo : nullptr, local % nbx, local / nbx);
+}
+
 __device__ __forceinline__ float gsym(const float* G, int rows, int a, int b) {
   return a <= b ? G[(size_t)a * rows + b] : G[(size_t)b * rows + a];
 }
@@ -247,6 +265,23 @@ __global__ void shift_copy_kernel(const double* __restrict__ S, int P, int kind,
   double re = S[2 * idx], im = S[2 * idx + 1];
   if (i == j) { re += diag_shift(S, P, i, kind, eps, lam); im = 0.0; }
   W[idx] = make_float2((float)re, (float)im);
+}
+
+// grouped: S = conj(G)/Ns (complex parameters) and W = S + eps I of every
+// problem, one element (k, l) per thread
+__global__ void assemble_shift_group_kernel(SrGroup g, double eps) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= g.pp_elems) return;
+  const int p = group_of(e, g.pp_elem, g.np);
+  const SrJob& j = g.jobs[p];
+  const int idx = e - __ldg(g.pp_elem + p), P = j.P, rows = 2 * P;
+  const int k = idx % P, l = idx / P;
+  const double inv_ns = 1.0 / j.Ns;
+  const double re = ((double)gsym(j.G, rows, 2 * k, 2 * l) + (double)gsym(j.G, rows, 2 * k + 1, 2 * l + 1)) * inv_ns;
+  const double im = ((double)gsym(j.G, rows, 2 * k, 2 * l + 1) - (double)gsym(j.G, rows, 2 * k + 1, 2 * l)) * inv_ns;
+  j.S[2 * (size_t)idx] = re;
+  j.S[2 * (size_t)idx + 1] = im;
+  j.W[idx] = k == l ? make_float2((float)(re + eps), 0.f) : make_float2((float)re, (float)im);
 }
 
 
@@ -326,9 +361,9 @@ __device__ __forceinline__ cpx<double> stat_val(const cpx<R>* v, long i, int mod
 // it is tiny next to the mean itself (a local energy of -40 with a spread of
 // 1e-6), where Σ|μ_c|² - B|μ|² would cancel to rounding noise.
 template <typename R>
-__global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
-                                                         double* __restrict__ part) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+NQ_D void chain_stats_block(const cpx<R>* __restrict__ v, int B, int L, int mode, double* __restrict__ part,
+                            int blk) {
+  const int c = blk * blockDim.x + threadIdx.x;
   const bool valid = c < B;
   double mx = 0, my = 0, var = 0;
   if (valid) {
@@ -349,7 +384,7 @@ __global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restric
   if ((threadIdx.x & 31) == 0)
     for (int k = 0; k < 3; ++k) sh[threadIdx.x >> 5][k] = q[k];
   __syncthreads();
-  const int nb = min(64, B - blockIdx.x * 64);
+  const int nb = min(64, B - blk * 64);
   const double bx = (sh[0][0] + sh[1][0]) / nb, by = (sh[0][1] + sh[1][1]) / nb;
   const double vsum = sh[0][2] + sh[1][2];
   double d2 = valid ? (mx - bx) * (mx - bx) + (my - by) * (my - by) : 0.0;
@@ -358,7 +393,7 @@ __global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restric
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][0] = d2;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double* o = part + 5 * (size_t)blockIdx.x;
+    double* o = part + 5 * (size_t)blk;
     o[0] = (double)nb;
     o[1] = bx;
     o[2] = by;
@@ -391,8 +426,13 @@ __device__ __forceinline__ ChainSummary merge_summary(const ChainSummary& a, con
 // var_μ_ch = M2/(B-1); var_μ = [(L-1) Σ var_c + L M2]/(BL-1) (= the variance
 // of all values about μ); variance = mean var_c; t = var_μ_ch/var_μ
 // (stats.jl:26-50)
-__global__ void __launch_bounds__(32) stats_final_kernel(const double* __restrict__ part, int nblk, int B, int L,
-                                                         double* __restrict__ out) {
+template <typename R>
+__global__ void __launch_bounds__(64) chain_stats_kernel(const cpx<R>* __restrict__ v, int B, int L, int mode,
+                                                         double* __restrict__ part) {
+  chain_stats_block<R>(v, B, L, mode, part, blockIdx.x);
+}
+
+NQ_D void stats_final_warp(const double* __restrict__ part, int nblk, int B, int L, double* __restrict__ out) {
   ChainSummary s = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < nblk; b += 32) {
     const double* p = part + 5 * (size_t)b;
@@ -421,6 +461,24 @@ __global__ void __launch_bounds__(32) stats_final_kernel(const double* __restric
     out[4] = fmax(0.0, 0.5 * (t * L - 1.0));
     out[5] = sqrt((double)(L - 1) / L + t);
   }
+}
+
+__global__ void __launch_bounds__(32) stats_final_kernel(const double* __restrict__ part, int nblk, int B, int L,
+                                                         double* __restrict__ out) {
+  stats_final_warp(part, nblk, B, L, out);
+}
+
+// ---- grouped forms (many-problem step, FP32)
+__global__ void __launch_bounds__(64) chain_stats_group_kernel(SrGroup g) {
+  const int p = group_of(blockIdx.x, g.stat_blk, g.np);
+  const SrJob& j = g.jobs[p];
+  chain_stats_block<float>(reinterpret_cast<const cpx<float>*>(j.eloc), j.B, j.L, 0, j.chainstats,
+                           blockIdx.x - __ldg(g.stat_blk + p));
+}
+
+__global__ void __launch_bounds__(32) stats_final_group_kernel(SrGroup g) {
+  const SrJob& j = g.jobs[blockIdx.x];
+  stats_final_warp(j.chainstats, (j.B + 63) / 64, j.B, j.L, j.stats);
 }
 
 }  // namespace
@@ -547,3 +605,21 @@ cudaError_t launch_stats(const cpx<R>* vals, int B, int L, int mode, double* cha
 }
 template cudaError_t launch_stats<float>(const cpx<float>*, int, int, int, double*, double*, cudaStream_t);
 template cudaError_t launch_stats<double>(const cpx<double>*, int, int, int, double*, double*, cudaStream_t);
+
+cudaError_t launch_stats_group(const SrGroup& g, cudaStream_t st) {
+  chain_stats_group_kernel<<<g.stat_blocks, 64, 0, st>>>(g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  stats_final_group_kernel<<<g.np, 32, 0, st>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_X_group(const SrGroup& g, int split3, cudaStream_t st) {
+  build_X_group_kernel<<<g.x_blocks, 256, 0, st>>>(g, split3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_shift_group(const SrGroup& g, double eps, cudaStream_t st) {
+  assemble_shift_group_kernel<<<(g.pp_elems + 255) / 256, 256, 0, st>>>(g, eps);
+  return cudaGetLastError();
+}

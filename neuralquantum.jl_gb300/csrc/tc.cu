@@ -58,6 +58,34 @@ __device__ __forceinline__ void block_coords(int p, int nj, int* ti, int* J) {
   *ti = i; *J = first_block(i) + rem;
 }
 
+// Geometry of the many-problem Gram: per problem 8 ints {row offset in the
+// stacked X, rows, nt, nj, nblocks, first item, first reduction tile, 0},
+// then the item starts [np + 1] and the tile starts [np + 1].
+constexpr int GEOM_INTS = 8;
+
+// Work item q -> k-split y, block (ti, J) and the first row of its problem in
+// X.  Single problem: geom == nullptr.
+__device__ __forceinline__ void resolve_item(int q, int nj, int nblocks, const int* __restrict__ geom, int np,
+                                             int* y, int* ti, int* J, int* roff) {
+  int local = q, nbl = nblocks, njj = nj;
+  *roff = 0;
+  if (geom) {
+    const int* item_start = geom + GEOM_INTS * np;
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(item_start + mid) <= q) lo = mid; else hi = mid - 1;
+    }
+    const int* gm = geom + GEOM_INTS * lo;
+    *roff = __ldg(gm + 0);
+    njj = __ldg(gm + 3);
+    nbl = __ldg(gm + 4);
+    local = q - __ldg(gm + 5);
+  }
+  *y = local / nbl;
+  block_coords(local - *y * nbl, njj, ti, J);
+}
+
 // chunk range of k-split y: [y * per, min(nch, (y + 1) * per))
 __device__ __forceinline__ int item_chunks(int y, int per, int nch) { return min(nch, (y + 1) * per) - y * per; }
 
@@ -71,7 +99,7 @@ template <int KIND>
 __global__ void __launch_bounds__(THREADS, 1)
 gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap xlomap,
                  int nj, int nblocks, int nch, int per, int items, float* __restrict__ slots,
-                 int* __restrict__ err) {
+                 int* __restrict__ err, const int* __restrict__ geom, int np) {
   constexpr bool split3 = KIND == GRAM_TF32X3;
   constexpr bool bf16 = KIND == GRAM_BF16;
   constexpr int stages = split3 ? 2 : 4;
@@ -113,9 +141,8 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
       int k = 0;                      // stage counter across items
       bool stop = false;
       for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
-        const int y = q / nblocks;
-        int ti, J;
-        block_coords(q - y * nblocks, nj, &ti, &J);
+        int y, ti, J, roff;
+        resolve_item(q, nj, nblocks, geom, np, &y, &ti, &J, &roff);
         const bool a_in_b = first_block(ti) == J;
         const int n = item_chunks(y, per, nch);
         const uint32_t bytes = (uint32_t)TILE_BYTES * (a_in_b ? 2u : 3u) * (split3 ? 2u : 1u);
@@ -131,14 +158,14 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
           uint8_t* buf = ring + (size_t)s * stage_bytes;
           const int kx = (y * per + c) * (bf16 ? 2 * KC : KC);     // elements of 128-byte rows
           mbar_arrive_expect_tx(&full[s], bytes);
-          tma_load_2d(buf, &xmap, kx, J * NW, &full[s]);
-          tma_load_2d(buf + TILE_BYTES, &xmap, kx, J * NW + TM, &full[s]);
-          if (!a_in_b) tma_load_2d(buf + 2 * TILE_BYTES, &xmap, kx, ti * TM, &full[s]);
+          tma_load_2d(buf, &xmap, kx, roff + J * NW, &full[s]);
+          tma_load_2d(buf + TILE_BYTES, &xmap, kx, roff + J * NW + TM, &full[s]);
+          if (!a_in_b) tma_load_2d(buf + 2 * TILE_BYTES, &xmap, kx, roff + ti * TM, &full[s]);
           if (split3) {
             uint8_t* lb = buf + 3 * TILE_BYTES;
-            tma_load_2d(lb, &xlomap, kx, J * NW, &full[s]);
-            tma_load_2d(lb + TILE_BYTES, &xlomap, kx, J * NW + TM, &full[s]);
-            if (!a_in_b) tma_load_2d(lb + 2 * TILE_BYTES, &xlomap, kx, ti * TM, &full[s]);
+            tma_load_2d(lb, &xlomap, kx, roff + J * NW, &full[s]);
+            tma_load_2d(lb + TILE_BYTES, &xlomap, kx, roff + J * NW + TM, &full[s]);
+            if (!a_in_b) tma_load_2d(lb + 2 * TILE_BYTES, &xlomap, kx, roff + ti * TM, &full[s]);
           }
         }
       }
@@ -157,9 +184,8 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
       int k = 0, seg = 0;
       bool stop = false;
       for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
-        const int y = q / nblocks;
-        int ti, J;
-        block_coords(q - y * nblocks, nj, &ti, &J);
+        int y, ti, J, roff;
+        resolve_item(q, nj, nblocks, geom, np, &y, &ti, &J, &roff);
         const bool a_in_b = first_block(ti) == J;
         const uint64_t a_off = a_in_b ? (uint64_t)((ti * TM - J * NW) / TM) * desc_box : 2u * desc_box;
         const int n = item_chunks(y, per, nch);
@@ -217,7 +243,8 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
     int seg = 0;
     bool stop = false;
     for (int q = blockIdx.x; q < items && !stop; q += gridDim.x) {
-      const int y = q / nblocks;
+      int y, ti_, J_, roff_;
+      resolve_item(q, nj, nblocks, geom, np, &y, &ti_, &J_, &roff_);
       const int nseg = (item_chunks(y, per, nch) + SEG - 1) / SEG;
       float acc[TM];
 #pragma unroll
@@ -258,11 +285,11 @@ gram_tf32_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant
 // column-major partial blocks; 32 x 32 sub-blocks transposed through shared
 // memory so that both the partial reads and the G writes are coalesced.
 // blockIdx.x: upper tile t = (ti, tj) in row-major order, blockIdx.y: sub-block.
-__global__ void __launch_bounds__(256) gram_slot_reduce_kernel(const float* __restrict__ slots, int rows, int nt,
-                                                               int nj, int nblocks, int ks, float* __restrict__ G) {
+NQ_D void slot_reduce_tile(const float* __restrict__ slots, int rows, int nt, int nj, int nblocks, int ks,
+                           float* __restrict__ G, int tile) {
   __shared__ float buf[32][33];
   const int sr = (blockIdx.y >> 2) * 32, sc = (blockIdx.y & 3) * 32;
-  int ti = 0, rem = blockIdx.x;
+  int ti = 0, rem = tile;
   while (rem >= nt - ti) { rem -= nt - ti; ++ti; }
   const int tj = ti + rem;
   const int J = (tj * TM) / NW;
@@ -279,6 +306,27 @@ __global__ void __launch_bounds__(256) gram_slot_reduce_kernel(const float* __re
     const int gr = ti * TM + sr + rl, gc = tj * TM + sc + threadIdx.x;
     if (gr < rows && gc < rows) G[(size_t)gr * rows + gc] = buf[threadIdx.x][rl];
   }
+}
+
+__global__ void __launch_bounds__(256) gram_slot_reduce_kernel(const float* __restrict__ slots, int rows, int nt,
+                                                               int nj, int nblocks, int ks, float* __restrict__ G) {
+  slot_reduce_tile(slots, rows, nt, nj, nblocks, ks, G, blockIdx.x);
+}
+
+// many problems: problem p owns the reduction tiles [tile_start[p], tile_start[p+1])
+// and the partial blocks from its first item on; its G goes to jobs[p].G
+__global__ void __launch_bounds__(256) gram_slot_reduce_group_kernel(const float* __restrict__ slots,
+                                                                     const int* __restrict__ geom, int np, int ks,
+                                                                     const SrJob* __restrict__ jobs) {
+  const int* tile_start = geom + GEOM_INTS * np + np + 1;
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(tile_start + mid) <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const int* gm = geom + GEOM_INTS * lo;
+  slot_reduce_tile(slots + (size_t)__ldg(gm + 5) * BLOCK_ELEMS, __ldg(gm + 1), __ldg(gm + 2), __ldg(gm + 3),
+                   __ldg(gm + 4), ks, jobs[lo].G, blockIdx.x - __ldg(gm + 6));
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -390,11 +438,100 @@ cudaError_t launch_gram_tc(const void* X, const float* Xlo, int rows, int Ns_pad
   auto kernel = split3 ? gram_tf32_kernel<GRAM_TF32X3> : bf16 ? gram_tf32_kernel<GRAM_BF16> : gram_tf32_kernel<GRAM_TF32>;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kernel<<<p.ncta, THREADS, smem, st>>>(xmap, xlomap, p.nj, p.nblocks, p.nch, p.per, p.items, partial, err);
+  kernel<<<p.ncta, THREADS, smem, st>>>(xmap, xlomap, p.nj, p.nblocks, p.nch, p.per, p.items, partial, err,
+                                         nullptr, 0);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int tiles = p.nt * (p.nt + 1) / 2;
   gram_slot_reduce_kernel<<<dim3((unsigned)tiles, 16), dim3(32, 8), 0, st>>>(partial, rows, p.nt, p.nj, p.nblocks,
                                                                               p.ks, G);
+  return cudaGetLastError();
+}
+
+// ---- many problems: one launch over the upper blocks of every problem's Gram
+GramGroupPlan gram_group_plan(const std::vector<int>& rows, int Ns_pad) {
+  GramGroupPlan p;
+  p.np = (int)rows.size();
+  p.rows = rows;
+  p.nch = Ns_pad / KC;
+  int total_blocks = 0, off = 0;
+  p.row_off.resize(p.np);
+  p.nblocks.resize(p.np);
+  for (int i = 0; i < p.np; ++i) {
+    const int nt = (rows[i] + TM - 1) / TM, nj = (rows[i] + NW - 1) / NW;
+    p.nblocks[i] = blocks_before(nt, nj);
+    p.row_off[i] = off;
+    off += rows[i];
+    total_blocks += p.nblocks[i];
+  }
+  // k-split as for one problem: stages of the busiest CTA plus a charge per split
+  const int nsm = sm_count();
+  long best = -1;
+  for (int ks = 1; ks <= 32 && ks <= p.nch; ++ks) {
+    const int per = (p.nch + ks - 1) / ks;
+    if ((p.nch + per - 1) / per != ks) continue;
+    if (ks > 1 && per < 16) break;
+    const long items = (long)total_blocks * ks;
+    const long rounds = (items + nsm - 1) / nsm;
+    const long cost = 6L * rounds * per + (long)ks * total_blocks;
+    if (best < 0 || cost < best) { best = cost; p.ks = ks; }
+  }
+  p.per = (p.nch + p.ks - 1) / p.ks;
+  p.item0.assign(p.np + 1, 0);
+  p.tile0.assign(p.np + 1, 0);
+  for (int i = 0; i < p.np; ++i) {
+    const int nt = (rows[i] + TM - 1) / TM;
+    p.item0[i + 1] = p.item0[i] + p.nblocks[i] * p.ks;
+    p.tile0[i + 1] = p.tile0[i] + nt * (nt + 1) / 2;
+  }
+  p.items = p.item0[p.np];
+  p.tiles = p.tile0[p.np];
+  p.ncta = std::min(nsm, p.items);
+  return p;
+}
+
+size_t gram_group_partial_elems(const GramGroupPlan& p) { return (size_t)p.items * BLOCK_ELEMS; }
+size_t gram_group_geom_bytes(int np) { return sizeof(int) * ((size_t)GEOM_INTS * np + 2 * (np + 1)); }
+
+cudaError_t gram_group_upload(const GramGroupPlan& p, void* geom_dev, cudaStream_t st) {
+  std::vector<int> h((size_t)GEOM_INTS * p.np + 2 * (p.np + 1), 0);
+  for (int i = 0; i < p.np; ++i) {
+    int* g = h.data() + GEOM_INTS * i;
+    g[0] = p.row_off[i];
+    g[1] = p.rows[i];
+    g[2] = (p.rows[i] + TM - 1) / TM;
+    g[3] = (p.rows[i] + NW - 1) / NW;
+    g[4] = p.nblocks[i];
+    g[5] = p.item0[i];
+    g[6] = p.tile0[i];
+  }
+  for (int i = 0; i <= p.np; ++i) {
+    h[(size_t)GEOM_INTS * p.np + i] = p.item0[i];
+    h[(size_t)GEOM_INTS * p.np + p.np + 1 + i] = p.tile0[i];
+  }
+  cudaError_t e = cudaMemcpyAsync(geom_dev, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
+}
+
+cudaError_t launch_gram_group(const float* X, const float* Xlo, int rows_total, int Ns_pad, int split3,
+                              const GramGroupPlan& p, const void* geom_dev, const SrGroup& g, float* slots,
+                              int* err, cudaStream_t st) {
+  if (Ns_pad % KC != 0 || ((uintptr_t)X & 15u) != 0) return cudaErrorInvalidValue;
+  if (split3 && (!Xlo || ((uintptr_t)Xlo & 15u) != 0)) return cudaErrorInvalidValue;
+  CUtensorMap xmap, xlomap;
+  if (!encode_rowmajor(&xmap, X, rows_total, Ns_pad, 0)) return cudaErrorInvalidValue;
+  if (!encode_rowmajor(&xlomap, split3 ? (const void*)Xlo : (const void*)X, rows_total, Ns_pad, 0))
+    return cudaErrorInvalidValue;
+  const int stages = split3 ? 2 : 4;
+  const size_t smem = (size_t)stages * (split3 ? 6 : 3) * TILE_BYTES + 1024 + 256;
+  auto kernel = split3 ? gram_tf32_kernel<GRAM_TF32X3> : gram_tf32_kernel<GRAM_TF32>;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int* geom = static_cast<const int*>(geom_dev);
+  kernel<<<p.ncta, THREADS, smem, st>>>(xmap, xlomap, 0, 1, p.nch, p.per, p.items, slots, err, geom, p.np);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  gram_slot_reduce_group_kernel<<<dim3((unsigned)p.tiles, 16), dim3(32, 8), 0, st>>>(slots, geom, p.np, p.ks, g.jobs);
   return cudaGetLastError();
 }
