@@ -76,7 +76,8 @@ typedef enum {
  * symmetric NDM's (real, NDM order, sizes n_hidden and n_ancilla).  The
  * density matrices sample the doubled space (σ, η) and take the Liouvillian
  * cost function. */
-typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_SYMM = 3, NQ_NET_CHAIN = 4 } nq_network;
+typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_SYMM = 3, NQ_NET_CHAIN = 4,
+               NQ_NET_MIXED_CHAIN = 5 } nq_network;
 
 /* Layers of a feed-forward ket, PureStateAnsatz(Chain(layers...), N)
  * (src/Networks/Chains/Chain.jl, Layers/Dense.jl, Layers/WeightedSum.jl,
@@ -85,8 +86,15 @@ typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_
  * NQ_LAYER_SUM: logψ = Σ_i x_i (sum_autobatch).  A chain is 1..7 Dense
  * layers (the first with n_in = n_sites, widths <= 256) closed by one WSUM or
  * SUM.  Complex parameters in the functor order: per Dense layer W
- * (column-major) then b, then c. */
-typedef enum { NQ_LAYER_DENSE = 0, NQ_LAYER_WSUM = 1, NQ_LAYER_SUM = 2 } nq_layer_kind;
+ * (column-major) then b, then c.
+ * A density-matrix chain, MixedStateAnsatz(Chain(DenseSplit(N, out, f),
+ * Dense..., WSum | sum_autobatch), N) (MixedDensityMatrix/MixedChainWrapper.jl,
+ * Layers/DenseSplit.jl): network NQ_NET_MIXED_CHAIN, first layer
+ * NQ_LAYER_DENSE_SPLIT (n_in = N, θ = Wr σ + Wc η + b on the row and column
+ * configurations, parameters Wr, Wc (out x N, column-major), b), then as a
+ * ket chain; it samples |ρ(σ,η)|² on the doubled space and takes the
+ * Liouvillian cost function like the NDM. */
+typedef enum { NQ_LAYER_DENSE = 0, NQ_LAYER_WSUM = 1, NQ_LAYER_SUM = 2, NQ_LAYER_DENSE_SPLIT = 3 } nq_layer_kind;
 typedef struct {
   int32_t kind;            /* nq_layer_kind */
   int32_t n_in;
@@ -232,9 +240,11 @@ typedef struct nq_handle nq_handle;
 const char* nq_version(void);
 int32_t nq_abi_version(void);
 nq_status nq_create(const nq_config* cfg, nq_handle** out);
-/* A handle for PureStateAnsatz(Chain(layers...)): cfg->network =
- * NQ_NET_CHAIN (n_hidden, n_ancilla and activation are not used), local-flip
- * Metropolis sampler, direct SR with NQ_S_F32 / NQ_S_TF32 / NQ_S_TF32X3. */
+/* A handle for PureStateAnsatz(Chain(layers...)) (cfg->network =
+ * NQ_NET_CHAIN) or MixedStateAnsatz(Chain(DenseSplit, layers...))
+ * (NQ_NET_MIXED_CHAIN); n_hidden, n_ancilla and activation are not used;
+ * local-flip Metropolis sampler, direct SR with NQ_S_F32 / NQ_S_TF32 /
+ * NQ_S_TF32X3. */
 nq_status nq_create_chain(const nq_config* cfg, int32_t n_layers, const nq_layer* layers, nq_handle** out);
 void nq_destroy(nq_handle* h);
 nq_status nq_last_error(const nq_handle* h, char* buf, size_t len);

@@ -293,7 +293,20 @@ nq_status stage_force(nq_handle* h) {
   if (h->chain) {
     const int sp = h->cfg.s_precision;
     const bool tc = sp == NQ_S_TF32 || sp == NQ_S_TF32X3;
-    if (h->f64) {
+    if (h->mixed) {
+      // density matrix: the cost C = mean |L_loc|² with its statistics, then F
+      if (h->f64) {
+        CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 1, h->d_chainstats, h->d_stats, h->st));
+        CKL(launch_chain_liouv_force<double>(chain_dev<double>(h), h->d_samples, h->Ns, h->op,
+                                             (const cpx<double>*)h->d_eloc, h->d_X, h->Ns_pad, h->d_stats,
+                                             h->d_cgrad, h->fb.force, h->st));
+      } else {
+        CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 1, h->d_chainstats, h->d_stats, h->st));
+        CKL(launch_chain_liouv_force<float>(chain_dev<float>(h), h->d_samples, h->Ns, h->op,
+                                            (const cpx<float>*)h->d_eloc, h->d_X, h->Ns_pad, h->d_stats,
+                                            h->d_cgrad, h->fb.force, h->st));
+      }
+    } else if (h->f64) {
       CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
       CKL(launch_chain_force<double>(h->d_X, h->Ns_pad, h->P, h->Ns, (const cpx<double>*)h->d_eloc, h->d_stats,
                                      h->fb.force, h->st));
@@ -539,21 +552,33 @@ int32_t nq_abi_version(void) { return NQCUDA_ABI_VERSION; }
 namespace {
 
 // validated layer list of a chain into spec; "" or the reason it is refused
+// A density-matrix chain's DenseSplit layer (θ = Wr σ + Wc η + b) is stored
+// as a Dense layer on the 2N doubled sites: W = [Wr Wc] column-major is Wr
+// then Wc, so the parameter vector is unchanged.
 const char* chain_layers(const nq_config& c, int n_layers, const nq_layer* layers, ChainDev<float>* spec) {
   if (!layers || n_layers < 2 || n_layers > 8) return "a chain has 2..8 layers";
+  const bool mixed = c.network == NQ_NET_MIXED_CHAIN;
   int off = 0, n_theta = 0, max_w = 0, prev = c.n_sites;
   for (int l = 0; l < n_layers; ++l) {
     const nq_layer& y = layers[l];
     ChainLayerDev d;
     d.kind = y.kind; d.in = y.n_in; d.out = y.n_out; d.act = y.activation;
     if (y.n_in != prev) return "layer input width differs from the previous output";
+    if (mixed != (l == 0 && y.kind == NQ_LAYER_DENSE_SPLIT) && l == 0)
+      return mixed ? "a density-matrix chain starts with DenseSplit" : "DenseSplit starts a density-matrix chain";
+    if (l > 0 && y.kind == NQ_LAYER_DENSE_SPLIT) return "DenseSplit is the first layer only";
+    const bool dense = y.kind == NQ_LAYER_DENSE || y.kind == NQ_LAYER_DENSE_SPLIT;
+    if (y.kind == NQ_LAYER_DENSE_SPLIT) {
+      d.kind = NQ_LAYER_DENSE;
+      d.in = 2 * y.n_in;
+    }
     const bool closing = l == n_layers - 1;
-    if (closing != (y.kind != NQ_LAYER_DENSE)) return "Dense layers, then exactly one closing WSum or sum";
-    if (y.kind == NQ_LAYER_DENSE) {
+    if (closing != !dense) return "Dense layers, then exactly one closing WSum or sum";
+    if (dense) {
       if (y.n_out < 1 || y.n_out > 256) return "Dense widths must be in 1..256";
       if (y.activation != NQ_ACT_LOGCOSH && y.activation != NQ_ACT_SOFTPLUS && y.activation != NQ_ACT_IDENTITY)
         return "unknown Dense activation";
-      d.w_off = off; off += y.n_out * y.n_in;
+      d.w_off = off; off += y.n_out * d.in;
       d.b_off = off; off += y.n_out;
       n_theta += y.n_out;
       max_w = std::max(max_w, y.n_out);
@@ -568,7 +593,8 @@ const char* chain_layers(const nq_config& c, int n_layers, const nq_layer* layer
     }
     spec->L[l] = d;
   }
-  spec->N = c.n_sites; spec->hilb = c.hilbert; spec->n_layers = n_layers; spec->P = off;
+  spec->N = mixed ? 2 * c.n_sites : c.n_sites;
+  spec->hilb = c.hilbert; spec->n_layers = n_layers; spec->P = off;
   spec->n_theta = n_theta; spec->max_w = max_w;
   if (off > 256 * 24) return "too many chain parameters (max 6144)";
   return "";
@@ -585,17 +611,19 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
     delete h;
     return NQ_ERR_ARG;
   };
-  if (c.network == NQ_NET_CHAIN) {
+  if (c.network == NQ_NET_CHAIN || c.network == NQ_NET_MIXED_CHAIN) {
     if (!layers) return bad("chains are created with nq_create_chain");
-    if (c.n_sites < 1 || c.n_sites > 64) return bad("n_sites must be in 1..64");
+    if (c.n_sites < 1 || c.n_sites > (c.network == NQ_NET_MIXED_CHAIN ? 32 : 64))
+      return bad("n_sites must be in 1..64 (1..32 for a density-matrix chain)");
     const char* why = chain_layers(c, n_layers, layers, &h->chain_spec);
     if (*why) return bad(why);
     if (c.sampler_kind != NQ_SAMPLER_METROPOLIS || c.rule != NQ_RULE_LOCAL || c.sampler_space != NQ_SPACE_NETWORK)
       return bad("chains sample with the local-flip Metropolis rule");
     h->chain = true;
+    h->mixed = c.network == NQ_NET_MIXED_CHAIN;
   }
   if (c.network != NQ_NET_RBM && c.network != NQ_NET_NDM && c.network != NQ_NET_RBM_SPLIT &&
-      c.network != NQ_NET_NDM_SYMM && c.network != NQ_NET_CHAIN)
+      c.network != NQ_NET_NDM_SYMM && c.network != NQ_NET_CHAIN && c.network != NQ_NET_MIXED_CHAIN)
     return bad("unknown network");
   const bool matrix_net = c.network == NQ_NET_NDM || c.network == NQ_NET_RBM_SPLIT || c.network == NQ_NET_NDM_SYMM;
   if (c.network == NQ_NET_NDM_SYMM && (c.n_symm < 1 || c.n_symm > 64)) return bad("NDMSymm: n_symm must be in 1..64");
@@ -672,7 +700,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
     if (h->Ms > 320) return bad("2*n_hidden + n_ancilla must be <= 320");
     if (h->P > 256 * 24) return bad("too many density-matrix parameters (max 6144)");
   } else if (h->chain) {
-    h->nst = h->N;
+    h->nst = h->mixed ? 2 * h->N : h->N;
     h->M = h->chain_spec.L[0].out;
     h->P = h->chain_spec.P;
   } else {
@@ -743,6 +771,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   step(dalloc(&h->fb.meanE, 2), "meanE");
   step(dalloc(&h->d_stats, 8), "stats");
   step(dalloc(&h->d_chainstats, stats_scratch_doubles(h->B)), "chain stats");
+  if (h->mixed) step(dalloc(&h->d_cgrad, (size_t)h->P * h->Ns), "Liouvillian gradient");
   step(dalloc(&h->fb.sums, 4 * (size_t)P + 2), "force sums");
   h->cg = c.sr_algorithm == NQ_SR_CG;
   h->exact = c.sampler_kind == NQ_SAMPLER_EXACT;
@@ -874,7 +903,7 @@ void nq_destroy(nq_handle* h) {
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
                   h->d_stats, h->d_G, h->d_Gpart, h->d_X, h->d_Xlo, h->d_S, h->sb.W, h->sb.work, h->sb.x, h->sb.r,
-                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->sb.norms, h->sb.info, h->d_theta_img, h->d_ndm_theta, h->d_exact, h->d_pairs, h->d_xtab[0],
+                  h->sb.rf, h->sb.yf, h->sb.status, h->sb.ctl, h->sb.norms, h->sb.info, h->d_theta_img, h->d_ndm_theta, h->d_cgrad, h->d_exact, h->d_pairs, h->d_xtab[0],
                   h->d_xtab[1], h->d_xtab[2], h->d_xW, h->d_xare, h->d_dw, h->d_eff[0], h->d_eff[1],
                   h->d_eff[2], h->d_eff[3], h->d_eff[4], h->d_w, h->d_wconn, h->d_nconn, h->d_ndm_partial,
                   h->d_diag[0], h->d_diag[1], h->d_diag[2], h->d_bare, h->d_perms};

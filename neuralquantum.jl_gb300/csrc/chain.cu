@@ -232,6 +232,104 @@ __global__ void chain_force_kernel(const float* __restrict__ X, int ldx, int P, 
 }
 
 // ---------------------------------------------------------------------------
+// Density-matrix chains (MixedStateAnsatz on the doubled sites): the
+// gradient of the local Liouvillian, AccumulatorObsGrad.jl:62-113 --
+// ∇L_loc(σ) = Σ_c w_c O(σ'_c), w_c = mel_c ρ(σ'_c)/ρ(σ), over every non-zero
+// connection including those without changes, with no -O(σ) term.  One
+// thread per sample writes G[k n + s] = conj(∇L_loc,k(σ_s)) (FP32 complex,
+// accumulated over the connections); the force is reduced from it below.
+// Each connection restarts the forward pass from θ_1' = θ_1 + Σ_q W_1[:, s_q] dv_q
+// with its pre-activations kept for the backward pass at σ'.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(128)
+chain_liouv_grad_kernel(ChainDev<R> c, const uint64_t* __restrict__ samples, int n, DevOp op,
+                        float2* __restrict__ G) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = blockDim.x;
+  cpx<R>* th = reinterpret_cast<cpx<R>*>(smem_raw) + threadIdx.x;          // [n_theta][T] at σ
+  cpx<R>* th2 = th + (size_t)c.n_theta * T;                                 // [n_theta][T] at σ'
+  cpx<R>* xa = th2 + (size_t)c.n_theta * T;
+  cpx<R>* xb = xa + (size_t)c.max_w * T;
+  cpx<R>* xc = xb + (size_t)c.max_w * T;
+  const int s = blockIdx.x * T + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t bits = samples[s];
+  chain_theta0<R>(c, bits, th, T);
+  const cpx<R> lp = chain_forward_from0<R>(c, th, th, xa, xb, T);
+  for (int k = 0; k < c.P; ++k) G[(size_t)k * n + s] = make_float2(0.f, 0.f);
+  const ChainLayerDev& L0 = c.L[0];
+  for (int o = 0; o < op.n_ops; ++o) {
+    const int ns_o = __ldg(op.op_n_sites + o);
+    int r = 0;
+    for (int dd = 0; dd < ns_o; ++dd) r |= (int)((bits >> __ldg(op.op_sites + 8 * o + dd)) & 1ull) << dd;
+    const int row = __ldg(op.op_row_offset + o) + r;
+    const int c0 = __ldg(op.row_conn_offset + row), c1 = __ldg(op.row_conn_offset + row + 1);
+    for (int cc = c0; cc < c1; ++cc) {
+      const double mre = __ldg(op.conn_mel + 2 * cc), mim = __ldg(op.conn_mel + 2 * cc + 1);
+      if (mre == 0.0 && mim == 0.0) continue;
+      const int nch = __ldg(op.conn_n_changes + cc);
+      for (int q = 0; q < L0.out; ++q) th2[(size_t)q * T] = th[(size_t)q * T];
+      uint64_t nb = bits;
+      for (int k = 0; k < nch; ++k) {
+        const int site = __ldg(op.conn_change_site + 8 * cc + k);
+        const R nv = (R)__ldg(op.conn_change_value + 8 * cc + k);
+        const R dv = nv - site_value<R>(bits, site, c.hilb);
+        for (int q = 0; q < L0.out; ++q) {
+          const cpx<R> w = c.p[L0.w_off + q + L0.out * site];
+          th2[(size_t)q * T].x += w.x * dv;
+          th2[(size_t)q * T].y += w.y * dv;
+        }
+        const uint64_t bit = (c.hilb == HILB_SPIN) ? (nv > 0 ? 1ull : 0ull) : (nv != R(0) ? 1ull : 0ull);
+        nb = (nb & ~(1ull << site)) | (bit << site);
+      }
+      const cpx<R> lq = chain_forward_from0<R>(c, th2, th2, xa, xb, T);
+      const cpx<R> w = mk((R)mre, (R)mim) * cexpc(lq - lp);
+      const cpx<R> cw = conjc(w);
+      chain_backprop<R>(c, nb, th2, xa, xb, xc, T, [&](int k, cpx<R> v) {
+        const cpx<R> add = cw * conjc(v);
+        float2* gk = G + (size_t)k * n + s;
+        gk->x += (float)add.x;
+        gk->y += (float)add.y;
+      });
+    }
+  }
+}
+
+// F_k = conj(Σ_s L_s G_ks)/Ns - C <O_k> with C = mean |L_loc|² (stats[0])
+// and <O> from the uncentred rows of X (BatchedGradSampler.jl:99-120); one
+// warp per parameter, FP64 sums in a fixed order.
+template <typename R>
+__global__ void chain_liouv_force_kernel(const float* __restrict__ X, int ldx, int P, int ns,
+                                         const cpx<R>* __restrict__ L, const float2* __restrict__ G,
+                                         const double* __restrict__ stats, double* __restrict__ force) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (k >= P) return;
+  const float* xr = X + (size_t)(2 * k) * ldx;
+  const float* xi = X + (size_t)(2 * k + 1) * ldx;
+  const float2* gk = G + (size_t)k * ns;
+  double ar = 0, ai = 0, sr = 0, si = 0;
+  for (int s = lane; s < ns; s += 32) {
+    const double lr = (double)L[s].x, li = (double)L[s].y, gr = gk[s].x, gi = gk[s].y;
+    ar += lr * gr - li * gi;
+    ai += lr * gi + li * gr;
+    sr += xr[s];
+    si += xi[s];
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    ar += __shfl_xor_sync(0xffffffffu, ar, off);
+    ai += __shfl_xor_sync(0xffffffffu, ai, off);
+    sr += __shfl_xor_sync(0xffffffffu, sr, off);
+    si += __shfl_xor_sync(0xffffffffu, si, off);
+  }
+  if (lane == 0) {
+    const double C = stats[0];
+    force[2 * k] = ar / ns - C * sr / ns;
+    force[2 * k + 1] = -ai / ns - C * si / ns;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Metropolis sampler (Metropolis.jl:101-167 with LocalRule, the Philox schema
 // of the RBM sampler): one thread per chain keeps θ_1 and logψ; a proposal
 // flipping site i evaluates the chain from θ_1 + W_1[:, i] dv.
@@ -329,6 +427,25 @@ cudaError_t launch_chain_force(const float* X, int ldx, int P, int ns, const cpx
 }
 
 template <typename R>
+cudaError_t launch_chain_liouv_force(const ChainDev<R>& c, const uint64_t* samples, int n, const DevOp& op,
+                                     const cpx<R>* L, const float* X, int ldx, const double* stats, float2* G,
+                                     double* force, cudaStream_t st) {
+  if (n < 1) return cudaSuccess;
+  int T = 128;
+  auto need = [&](int t) { return (size_t)(2 * c.n_theta + 3 * c.max_w) * t * sizeof(cpx<R>); };
+  while (T > 32 && need(T) > 96 * 1024) T /= 2;
+  const size_t smem = need(T);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = set_smem(chain_liouv_grad_kernel<R>, smem);
+  if (e != cudaSuccess) return e;
+  chain_liouv_grad_kernel<R><<<(n + T - 1) / T, T, smem, st>>>(c, samples, n, op, G);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  chain_liouv_force_kernel<R><<<(32 * c.P + 255) / 256, 256, 0, st>>>(X, ldx, c.P, n, L, G, stats, force);
+  return cudaGetLastError();
+}
+
+template <typename R>
 cudaError_t launch_chain_sampler(const ChainDev<R>& c, const SamplerRun& run, cudaStream_t st) {
   if (c.N > 64 || c.n_layers < 2) return cudaErrorInvalidValue;
   const int T = chain_threads(c, 2) < 128 ? chain_threads(c, 2) : 128;
@@ -350,3 +467,9 @@ template cudaError_t launch_chain_force<double>(const float*, int, int, int, con
                                                 double*, cudaStream_t);
 template cudaError_t launch_chain_sampler<float>(const ChainDev<float>&, const SamplerRun&, cudaStream_t);
 template cudaError_t launch_chain_sampler<double>(const ChainDev<double>&, const SamplerRun&, cudaStream_t);
+template cudaError_t launch_chain_liouv_force<float>(const ChainDev<float>&, const uint64_t*, int, const DevOp&,
+                                                     const cpx<float>*, const float*, int, const double*, float2*,
+                                                     double*, cudaStream_t);
+template cudaError_t launch_chain_liouv_force<double>(const ChainDev<double>&, const uint64_t*, int, const DevOp&,
+                                                      const cpx<double>*, const float*, int, const double*, float2*,
+                                                      double*, cudaStream_t);

@@ -24,7 +24,9 @@ struct nq_handle {
   int n_record = 0, write_last = 0;
   bool doubled = false, complex_params = true, f64 = false, ndm = false;
   int Mh = 0, Ma = 0, U = 0, Ms = 0, N2 = 0;   // NDM sizes (effective units, doubled sites)
-  bool chain = false;              // feed-forward ket chain (chain_dev)
+  bool chain = false;              // feed-forward chain (chain_dev)
+  bool mixed = false;              // density-matrix chain over the doubled sites (Liouvillian cost)
+  float2* d_cgrad = nullptr;       // density-matrix chain: conj ∇L_loc per sample, [P][Ns]
   ChainDev<float> chain_spec;      // its layers (the parameter pointer is set per precision)
   bool split = false;              // RBMSplit on the doubled-space path (complex parameters)
   bool symm = false;               // NDMSymm: trainable symmetric NDM, evaluated as its bare NDM

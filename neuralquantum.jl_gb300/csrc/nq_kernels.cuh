@@ -140,6 +140,13 @@ template <typename R> struct ChainDev {
 template <typename R>
 cudaError_t launch_chain_eval(const ChainDev<R>& c, const uint64_t* samples, int n, const DevOp* op, cpx<R>* logpsi,
                               cpx<R>* eloc, float* X, int ldx, double* Oout, cudaStream_t st);
+// density-matrix chains: G = conj(∇L_loc) per sample ([P][n] FP32 complex),
+// then F = conj(Σ_s L_s G_s)/Ns - C <O> with C = stats[0] and <O> from the
+// uncentred rows of X
+template <typename R>
+cudaError_t launch_chain_liouv_force(const ChainDev<R>& c, const uint64_t* samples, int n, const DevOp& op,
+                                     const cpx<R>* L, const float* X, int ldx, const double* stats, float2* G,
+                                     double* force, cudaStream_t st);
 // F = E O_c† / Ns from the uncentred rows of X and the mean of E in stats[0..1]
 template <typename R>
 cudaError_t launch_chain_force(const float* X, int ldx, int P, int ns, const cpx<R>* E, const double* stats,

@@ -5,7 +5,8 @@ import numpy as np
 
 from . import _lib
 from .hilbert import SuperOpSpace, physical
-from .networks import RBM, NDM, NDMSymm, RBMSplit, PureStateAnsatz, Dense, WSum, af_logcosh, af_softplus
+from .networks import RBM, NDM, NDMSymm, RBMSplit, PureStateAnsatz, MixedStateAnsatz, Dense, DenseSplit, WSum, \
+    af_logcosh, af_softplus
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
@@ -28,6 +29,10 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
         cfg.network = _lib.NQ_NET_NDM
         cfg.n_hidden = net.Mh
         cfg.n_ancilla = net.Ma
+    elif isinstance(net, MixedStateAnsatz):
+        cfg.network = _lib.NQ_NET_MIXED_CHAIN
+        cfg.n_hidden = net.chain.layers[0].n_out
+        cfg.n_ancilla = 0
     elif isinstance(net, PureStateAnsatz):
         cfg.network = _lib.NQ_NET_CHAIN
         cfg.n_hidden = net.chain.layers[0].n_out
@@ -59,13 +64,16 @@ def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_prec
 
 
 def chain_layers(net):
-    """nq_layer array of a PureStateAnsatz's chain."""
+    """nq_layer array of a PureStateAnsatz's or MixedStateAnsatz's chain."""
     acts = {af_logcosh: _lib.NQ_ACT_LOGCOSH, af_softplus: _lib.NQ_ACT_SOFTPLUS, "identity": _lib.NQ_ACT_IDENTITY}
     layers = net.chain.layers
     arr = (_lib.NqLayer * len(layers))()
     width = net.N
     for k, l in enumerate(layers):
-        if isinstance(l, Dense):
+        if isinstance(l, DenseSplit):
+            arr[k] = _lib.NqLayer(_lib.NQ_LAYER_DENSE_SPLIT, l.n_in, l.n_out, acts[l.f])
+            width = l.n_out
+        elif isinstance(l, Dense):
             arr[k] = _lib.NqLayer(_lib.NQ_LAYER_DENSE, l.n_in, l.n_out, acts[l.f])
             width = l.n_out
         elif isinstance(l, WSum):
@@ -83,14 +91,14 @@ class Engine:
         L = _lib.lib()
         cfg = make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision,
                           s_precision, quirks, sampler_lanes, sr_algorithm, sampler_kind, rule, sampler_space)
-        self.complex_params = isinstance(net, (RBM, RBMSplit, PureStateAnsatz))
+        self.complex_params = isinstance(net, (RBM, RBMSplit, PureStateAnsatz, MixedStateAnsatz))
         self.cfg = cfg
         self.lib = L
         self._owned = _handle is None
         self._owner = _owner                  # keeps a batch alive while its problem handles are used
         if _handle is None:
             self.h = ctypes.c_void_p()
-            if isinstance(net, PureStateAnsatz):
+            if isinstance(net, (PureStateAnsatz, MixedStateAnsatz)):
                 st = L.nq_create_chain(ctypes.byref(cfg), len(net.chain.layers), chain_layers(net),
                                        ctypes.byref(self.h))
             else:

@@ -173,6 +173,23 @@ class Dense:
         return [self.W, self.b]
 
 
+class DenseSplit:
+    """``DenseSplit(T, in, out, σ=identity)`` (Chains/Layers/DenseSplit.jl:3-19):
+    the first layer of a density-matrix chain, y = σ.(Wr σr .+ Wc σc .+ b) on
+    the row and column configurations, Wr and Wc out x in, glorot-uniform
+    initialisation; functor order Wr, Wc, b."""
+
+    def __init__(self, T, n_in, n_out, f=identity, rng=None):
+        self.dtype = np.dtype(T)
+        self.n_in, self.n_out, self.f = int(n_in), int(n_out), f
+        self.Wr = glorot_uniform(self.dtype, self.n_out, self.n_in, rng=rng)
+        self.Wc = glorot_uniform(self.dtype, self.n_out, self.n_in, rng=rng)
+        self.b = glorot_uniform(self.dtype, self.n_out, rng=rng)
+
+    def arrays(self):
+        return [self.Wr, self.Wc, self.b]
+
+
 class WSum:
     """``WSum(T, in)`` (Chains/Layers/WeightedSum.jl): logψ = Σ_i c_i x_i."""
 
@@ -254,6 +271,55 @@ class PureStateAnsatz:
 
     def __repr__(self):
         return f"PureStateAnsatz(Chain of {len(self.chain.layers)} layers, N={self.N})"
+
+
+class MixedStateAnsatz:
+    """``MixedStateAnsatz(chain, N)`` (MixedDensityMatrix/MixedChainWrapper.jl:
+    3-37): a density matrix whose logρ(σ, η) is the chain's output for the
+    pair of configurations; the chain is DenseSplit(N, out) followed by Dense
+    layers and closed by WSum or sum_autobatch.  Complex parameters in the
+    functor order (DenseSplit: Wr, Wc, b; Dense: W, b; WSum: c).  Since
+    DenseSplit's θ = Wr σ + Wc η + b is a Dense layer on the 2N doubled sites
+    with W = [Wr Wc], whose column-major storage is Wr then Wc, the flat
+    vector is that of a chain over the doubled sites."""
+
+    def __init__(self, chain, n_sites):
+        self.N = n_sites if isinstance(n_sites, int) else n_sites.n_sites
+        self.chain = chain if isinstance(chain, Chain) else Chain(*chain)
+        layers = self.chain.layers
+        if len(layers) < 2 or not isinstance(layers[0], DenseSplit) or \
+                not all(isinstance(l, Dense) for l in layers[1:-1]) or not isinstance(layers[-1], (WSum, _SumAutobatch)):
+            raise ValueError("the chain is DenseSplit, then Dense layers, closed by WSum or sum_autobatch")
+        if layers[0].n_in != self.N:
+            raise ValueError("DenseSplit's input width must be the number of sites")
+        width = layers[0].n_out
+        for l in layers[1:-1]:
+            if l.n_in != width:
+                raise ValueError("layer widths do not match")
+            width = l.n_out
+        if isinstance(layers[-1], WSum) and layers[-1].n_in != width:
+            raise ValueError("WSum width does not match the last Dense layer")
+        self.dtype = np.result_type(*[a.dtype for l in layers for a in l.arrays()])
+
+    @property
+    def n_params(self):
+        return sum(a.size for l in self.chain.layers for a in l.arrays())
+
+    def flat(self):
+        return np.concatenate([a.reshape(-1, order="F") for l in self.chain.layers for a in l.arrays()]).astype(
+            np.complex128)
+
+    def set_flat(self, v):
+        v = np.asarray(v)
+        o = 0
+        for l in self.chain.layers:
+            for name in {DenseSplit: ("Wr", "Wc", "b"), Dense: ("W", "b"), WSum: ("c",)}.get(type(l), ()):
+                a = getattr(l, name)
+                setattr(l, name, v[o:o + a.size].reshape(a.shape, order="F").astype(l.dtype))
+                o += a.size
+
+    def __repr__(self):
+        return f"MixedStateAnsatz(Chain of {len(self.chain.layers)} layers, N={self.N})"
 
 
 def PureChain(N, *layers):

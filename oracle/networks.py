@@ -423,3 +423,46 @@ def init_random_pars(net, rng, sigma=1e-4):
         v = rng.standard_normal(p.size)
     net.set_flat(v * np.sqrt(sigma))
     return net
+
+
+class MixedChain:
+    """``MixedStateAnsatz(Chain(DenseSplit(N, M, f), Dense..., sum | WSum), N)``
+    (MixedDensityMatrix/MixedChainWrapper.jl:3-37, Layers/DenseSplit.jl:11):
+    logρ(σ, η) is the chain's output with the first layer
+    θ = Wr σ + Wc η + b.  That layer is a Dense layer on the concatenated
+    (σ, η) with W = [Wr Wc], whose column-major storage is Wr then Wc, so the
+    flat vector (Wr, Wc, b, later layers) is the ``Chain`` over 2N inputs
+    with layers[0] = ("dense", 2N, M, f).  ``layers`` lists the DenseSplit as
+    ("dense_split", N, M, f)."""
+
+    def __init__(self, n, layers):
+        self.N = int(n)
+        first = layers[0]
+        assert first[0] == "dense_split" and first[1] == self.N
+        self.chain = Chain(2 * self.N, [("dense", 2 * self.N, first[2], first[3])] + list(layers[1:]))
+
+    @property
+    def n_params(self):
+        return self.chain.n_params
+
+    def flat(self):
+        return self.chain.flat()
+
+    def set_flat(self, v):
+        self.chain.set_flat(v)
+
+    def dense_split(self):
+        """(Wr, Wc, b) of the first layer."""
+        W, b = self.chain.params[0]
+        return W[:, :self.N], W[:, self.N:], b
+
+    def logpsi(self, sr, sc):
+        sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
+        return self.chain.logpsi(np.concatenate([sr, sc], axis=1))
+
+    def logpsi_and_grad(self, sr, sc):
+        sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
+        return self.chain.logpsi_and_grad(np.concatenate([sr, sc], axis=1))
+
+    def log_prob(self, sr, sc):
+        return 2.0 * np.real(self.logpsi(sr, sc))

@@ -542,3 +542,30 @@ def test_c_port_fp32_matches_oracle_within_fp32():
     np.testing.assert_array_equal(samples, ref)
     Eo = oest.local_energy(r, H, ref.reshape(-1, N))
     assert np.max(np.abs(E - Eo)) < 2e-5 * np.max(np.abs(Eo))
+
+
+def test_mixed_chain_is_the_dense_split_formula():
+    """The density-matrix chain MixedStateAnsatz(Chain(DenseSplit(N, M, f),
+    sum_autobatch), N) of test/Machines/test_grad.jl:49-50: logρ(σ, η) =
+    Σ_h f(Wr_h·σ + Wc_h·η + b_h) (DenseSplit.jl:11 with sum.jl), and the
+    analytic gradient against central finite differences."""
+    rng = np.random.default_rng(21)
+    N, M = 4, 8
+    mc = nw.MixedChain(N, [("dense_split", N, M, nw.SOFTPLUS), ("sum", M)])
+    p = (rng.standard_normal(mc.n_params) + 1j * rng.standard_normal(mc.n_params)) * 0.3
+    mc.set_flat(p)
+    Wr, Wc, b = mc.dense_split()
+    h = Hilbert(N, SPIN)
+    sr = h.value(rng.integers(0, 2, size=(20, N)))
+    sc = h.value(rng.integers(0, 2, size=(20, N)))
+    direct = nw.softplus(sr @ Wr.T + sc @ Wc.T + b[None, :]).sum(axis=1)
+    np.testing.assert_allclose(mc.logpsi(sr, sc), direct, rtol=0, atol=1e-12)
+    lp, g = mc.logpsi_and_grad(sr, sc)
+    eps = 1e-6
+    for k in range(0, mc.n_params, 5):
+        q = p.copy(); q[k] += eps
+        mc.set_flat(q); up = mc.logpsi(sr, sc)
+        q[k] -= 2 * eps
+        mc.set_flat(q); dn = mc.logpsi(sr, sc)
+        np.testing.assert_allclose(g[:, k], (up - dn) / (2 * eps), rtol=0, atol=1e-7)
+    mc.set_flat(p)
