@@ -886,7 +886,7 @@ extern "C" {
 nq_status nq_create(const nq_config* cfg, nq_handle** out) { return create_impl(cfg, 0, nullptr, out); }
 
 nq_status nq_create_chain(const nq_config* cfg, int32_t n_layers, const nq_layer* layers, nq_handle** out) {
-  if (!cfg || cfg->network != NQ_NET_CHAIN) return NQ_ERR_ARG;
+  if (!cfg || (cfg->network != NQ_NET_CHAIN && cfg->network != NQ_NET_MIXED_CHAIN)) return NQ_ERR_ARG;
   return create_impl(cfg, n_layers, layers, out);
 }
 
@@ -1923,10 +1923,13 @@ nq_status batch_build_tables(nq_batch* b) {
   int sms = 0, dev = 0;
   BCK(cudaGetDevice(&dev));
   BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // the grouped step's inversion and refinement are throughput-bound: up to
+  // two co-resident CTAs per SM
+  const int slots = sms * (b->grouped ? batch_solve_ctas_per_sm() : 1);
   std::vector<int> wcta;
-  split_ctas(Ps, sms, wcta);
-  if (wcta[np] > sms)
-    return bfail(b, NQ_ERR_UNSUPPORTED, "%d problems exceed the %d SMs of the inversion launch", np, sms);
+  split_ctas(Ps, slots, wcta);
+  if (wcta[np] > slots)
+    return bfail(b, NQ_ERR_UNSUPPORTED, "%d problems exceed the %d CTAs of the inversion launch", np, slots);
   b->s_blocks = sblk[np];
   b->e_blocks = eblk[np];
   b->w_ctas = wcta[np];

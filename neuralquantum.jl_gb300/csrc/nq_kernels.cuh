@@ -463,6 +463,8 @@ cudaError_t launch_fill_group(const SrGroup& g, cudaStream_t st);
 // problem stopping once its correction is below kRefineTol of its solution
 cudaError_t launch_refine_group(const SrGroup& g, const int* cta_start, int total_ctas, void* ctl_base,
                                 double eps, int max_corr, cudaStream_t st);
+// CTAs per SM of the many-problem inversion and refinement (1 or 2)
+int batch_solve_ctas_per_sm();
 // w -= lr Δw on the FP64 master, its FP32 copy and the per-flip tables
 cudaError_t launch_update_group(const SrGroup& g, double lr, cudaStream_t st);
 // G = X Xᵀ of every problem on tcgen05 from one stacked X (rows_total x Ns_pad,

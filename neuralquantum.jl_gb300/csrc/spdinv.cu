@@ -702,3 +702,17 @@ cudaError_t launch_refine_group(const SrGroup& g, const int* cta_start, int tota
   return cudaLaunchKernelEx(&cfg, refine_group_kernel, g, cta_start, reinterpret_cast<char*>(ctl_base), eps,
                             max_corr);
 }
+
+// CTAs per SM that the many-problem inversion and refinement can keep
+// co-resident (both run as cooperative launches over the same CTA split);
+// at most two: the grouped step is throughput-bound, unlike the single
+// problem, whose sweep runs fastest at one CTA per SM
+int batch_solve_ctas_per_sm() {
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, sweep_batch_kernel, 256, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, refine_group_kernel, 256, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return std::max(1, std::min(2, std::min(a, b)));
+}
