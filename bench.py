@@ -389,14 +389,9 @@ BATCH = dict(n_problems=64, sizes=(3, 4, 5), h_range=(2.0, 4.0), J=1.0, alpha=1,
              burn=50, eps=0.01, lr=0.01, seed=1, steps=10)
 
 
-def batched_vs_sequential():
-    """64 independent 2D TFIM ground-state problems (L in {3,4,5}, h in
-    U[2,4] from seed 1, J = 1, complex RBM alpha = 1, 1024 chains x 20
-    samples): one batched SR step (one sampler, one estimator and one
-    inversion launch for all problems, per-problem stages as parallel graph
-    branches) against the same 64 problems stepped one after the other, each
-    replaying its own single-problem graph."""
-    import nqcuda as nq
+def _batch_problems(nq):
+    """The 64 problems of the many-problem workload: (network, Hilbert space,
+    Hamiltonian) per problem, drawn from the workload's seed."""
     c = BATCH
     rng = np.random.default_rng(c["seed"])
     spec = [(int(rng.choice(c["sizes"])), float(rng.uniform(*c["h_range"]))) for _ in range(c["n_problems"])]
@@ -406,14 +401,35 @@ def batched_vs_sequential():
         net = nq.RBM(np.complex64, L * L, c["alpha"], nq.af_logcosh)
         nq.init_random_pars_(net, sigma=0.01, rng=np.random.default_rng(100 + k))
         probs.append((net, hilb, H))
+    return spec, probs
+
+
+def batched_step(probs):
+    """One batched SR step for all problems: device ms per step (10 timed
+    steps after 3 + 10 warm-up steps), kernels per step and the tuning."""
+    import nqcuda as nq
+    c = BATCH
     batch = nq.ProblemBatch(probs, c["chains"], c["chain_length"], c["burn"])
     for i in range(3):
         batch.vmc_step(i, c["eps"], c["lr"])
     l0 = batch.kernel_launches()
-    ms_b = batch.bench_steps(10, c["steps"], c["eps"], c["lr"])
-    launches_b = (batch.kernel_launches() - l0) / c["steps"]
+    ms_b = batch.bench_steps(10, c["steps"], c["eps"], c["lr"])     # one untimed step, then the timed ones
+    launches_b = (batch.kernel_launches() - l0) / (c["steps"] + 1)
     tuning = batch.tuning()
     del batch
+    return float(np.mean(ms_b)), launches_b, tuning
+
+
+def batched_vs_sequential():
+    """64 independent 2D TFIM ground-state problems (L in {3,4,5}, h in
+    U[2,4] from seed 1, J = 1, complex RBM alpha = 1, 1024 chains x 20
+    samples): one batched SR step (every stage of all problems one grouped
+    launch, 17 kernels) against the same 64 problems stepped one after the
+    other, each replaying its own single-problem graph."""
+    import nqcuda as nq
+    c = BATCH
+    spec, probs = _batch_problems(nq)
+    ms_bat, launches_b, tuning = batched_step(probs)
     engines = []
     for k, (net, hilb, H) in enumerate(probs):
         smp = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], hilb.n_sites, burn=c["burn"],
@@ -429,7 +445,6 @@ def batched_vs_sequential():
         for e in engines:
             e.vmc_step(100 + it, c["eps"], c["lr"])
     wall_seq = (time.perf_counter() - t0) / c["steps"] * 1e3
-    ms_bat = float(np.mean(ms_b))
     return {"workload": "64 x tfim2d L in {3,4,5}, h~U[2,4], rbm alpha=1, 1024 chains x 20",
             "sizes": [L for L, _ in spec], "batched_ms_per_step": ms_bat,
             "batched_problem_steps_per_s": c["n_problems"] * 1e3 / ms_bat,
@@ -623,11 +638,20 @@ def main():
                     help="skip the precision-mode comparison (NDM N=12)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-proposal vs local Metropolis comparison (6x6 TFIM)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="time only the batched step of the 64-problem workload (for launch lists)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.batch_only:
+        import nqcuda as nq
+        _, probs = _batch_problems(nq)
+        ms, kernels, tuning = batched_step(probs)
+        print(json.dumps({"workload": "64 x tfim2d batched step", "batched_ms_per_step": ms,
+                          "batched_kernels_per_step": kernels, "tuning": tuning}))
+        return
     if args.impl == "reference":
         if rank != 0:
             return
