@@ -1889,8 +1889,20 @@ nq_status batch_build_tables(nq_batch* b) {
   }
   b->eval_T = rbm_eval_threads(b->M_max);
   const int cpb = 256 / b->lanes;          // chains per sampler block
+  // sampler jobs longest first (steps per chain x units per lane, the narrower
+  // loop of the batch kernel included), so the last wave holds short blocks
+  const int hpl_max = (b->M_max + b->lanes - 1) / b->lanes, hpl_lo = (hpl_max + 1) / 2;
+  std::vector<int> order(np);
+  std::vector<double> work(np);
   for (int p = 0; p < np; ++p) {
     nq_handle* h = b->hs[p];
+    const int hpl = (hpl_lo < hpl_max && h->M <= b->lanes * hpl_lo) ? hpl_lo : hpl_max;
+    work[p] = (double)h->passes * (h->cfg.burn + h->n_record) * (hpl + 2);
+    order[p] = p;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+  for (int q = 0; q < np; ++q) {
+    nq_handle* h = b->hs[order[q]];
     SamplerRun run;
     run.B = h->B; run.L = h->L; run.burn = h->cfg.burn; run.passes = h->passes;
     run.n_record = h->n_record; run.write_last_at_end = h->write_last;
@@ -1898,10 +1910,13 @@ nq_status batch_build_tables(nq_batch* b) {
     run.k1 = (uint32_t)(h->cfg.seed >> 32);
     run.call_ptr = b->d_call;
     run.samples = h->d_samples;
-    run.accepted = b->d_acc + p;
-    sj[p].net = rbm_dev<float>(h);
-    sj[p].run = run;
-    sblk[p + 1] = sblk[p] + (h->B + cpb - 1) / cpb;
+    run.accepted = b->d_acc + order[q];
+    sj[q].net = rbm_dev<float>(h);
+    sj[q].run = run;
+    sblk[q + 1] = sblk[q] + (h->B + cpb - 1) / cpb;
+  }
+  for (int p = 0; p < np; ++p) {
+    nq_handle* h = b->hs[p];
     ej[p].net = rbm_dev<float>(h);
     ej[p].samples = h->d_samples;
     ej[p].Ns = h->Ns;

@@ -44,7 +44,10 @@ template <typename R> struct alignas(4 * sizeof(R)) cpx_pair {
 // EXCH: the exchange rule (ExchangeRule.jl:38-68): a move draws a coupling
 // (i, j) and swaps the two values; equal values leave the state unchanged
 // (ratio 1, accepted).  The move tables are then per coupling.
-template <typename R, int G, int HPL, int ACT, bool EXCH = false, bool HALF = false>
+// PRE: read the table rows one step ahead (below); the many-problem kernel
+// runs without it, since there the extra registers cost more resident warps
+// than the hidden latency gains.
+template <typename R, int G, int HPL, int ACT, bool EXCH = false, bool HALF = false, bool PRE = true>
 NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int MP = G * HPL;
@@ -118,42 +121,71 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
   }
   const R dmag = hilb == HILB_SPIN ? R(2) : R(1);
 
-  unsigned long long naccept = 0;
-  const int nsweeps = run.burn + run.n_record;
+  uint32_t naccept = 0;
+  const bool rec_bits = run.accept_bits && active && lane == 0;
+  const uint32_t nsteps = (uint32_t)(run.burn + run.n_record) * (uint32_t)run.passes;
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
-  uint32_t t = 0;
   int my_site = 0;
   R my_lu = 0;
-  for (int sweep = 0; sweep < nsweeps; ++sweep) {
-    for (int pass = 0; pass < run.passes; ++pass, ++t) {
-      const int slot = (int)(t & (G - 1));
-      if (slot == 0) {
-        const u32x4 r = philox4x32_10(t + (uint32_t)lane, run.call, (uint32_t)chain, TAG_MH, run.k0, run.k1);
-        my_site = (int)uniform_site(r.x, (uint32_t)NR);
-        my_lu = fast_log2((R)uniform24(r.y));       // log2 u; u = 0 -> -inf (always accept)
-      }
-      const int i = __shfl_sync(gmask, my_site, slot, G);
-      const R lu = __shfl_sync(gmask, my_lu, slot, G);
-      uint64_t fmask = 1ull << i;
-      int site_i = i;
-      if (EXCH) {
-        const int2 pr = s_pairs[i];
-        site_i = pr.x;
-        fmask = (1ull << pr.x) | (1ull << pr.y);
-        if (((bits >> pr.x) & 1ull) == ((bits >> pr.y) & 1ull)) {
-          // swap of equal values: the same state, ratio 1 (u < 1 always accepts)
-          ++naccept;
-          if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = 1;
-          continue;
-        }
-      }
+  int pass = 0, sweep = 0;
+
+  // Operands of one step, read one step ahead: the site and the uniform of
+  // step t depend only on the Philox counter, never on the chain's state, so
+  // the table rows of step t+1 are loaded while step t decides.  Two buffers
+  // alternate (the loop below is unrolled by two), so nothing is copied.
+  // The rows stay in shared memory where the buffers would not fit the
+  // register file.
+  constexpr bool PRE_T = PRE && HPL * sizeof(R) <= 40;       // {t0, t1} rows
+  constexpr bool PRE_W = PRE && HPL * sizeof(R) <= 20;       // {t2, W} rows (accepted flips)
+  struct Pre {
+    cpx_pair<R> t01[PRE_T ? HPL : 1];
+    cpx_pair<R> t2w[PRE_W ? HPL : 1];
+    R are, lu;
+    int i;
+    int2 pr;
+  };
+  auto fetch = [&](uint32_t tn, Pre& p) {
+    const int slot = (int)(tn & (G - 1));
+    if (slot == 0) {
+      // lane l draws the (site, u) of step tn + l
+      const u32x4 r = philox4x32_10(tn + (uint32_t)lane, run.call, (uint32_t)chain, TAG_MH, run.k0, run.k1);
+      my_site = (int)uniform_site(r.x, (uint32_t)NR);
+      my_lu = fast_log2((R)uniform24(r.y));       // log2 u; u = 0 -> -inf (always accept)
+    }
+    p.i = __shfl_sync(gmask, my_site, slot, G);
+    p.lu = __shfl_sync(gmask, my_lu, slot, G);
+    if constexpr (EXCH) p.pr = s_pairs[p.i];
+    if constexpr (PRE_T) {
+#pragma unroll
+      for (int k = 0; k < HPL; ++k) p.t01[k] = s_t01[p.i * MP + lane + G * k];
+    }
+    if constexpr (PRE_W) {
+#pragma unroll
+      for (int k = 0; k < HPL; ++k) p.t2w[k] = s_t2w[p.i * MP + lane + G * k];
+    }
+    p.are = s_are[p.i];
+  };
+
+  auto step = [&](uint32_t t, const Pre& p, Pre& nxt) {
+    fetch(t + 1, nxt);
+    const int i = p.i;
+    uint64_t fmask = 1ull << i;
+    int site_i = i;
+    bool flip = true;
+    if constexpr (EXCH) {
+      site_i = p.pr.x;
+      fmask = (1ull << p.pr.x) | (1ull << p.pr.y);
+      // a swap of equal values is the same state: ratio 1, accepted (u < 1)
+      flip = ((bits >> p.pr.x) & 1ull) != ((bits >> p.pr.y) & 1ull);
+    }
+    bool acc = true;
+    if (flip) {
       const bool pos = !((bits >> site_i) & 1ull);
       const R dv = pos ? dmag : -dmag;
-      const cpx_pair<R>* trow = s_t01 + i * MP + lane;
       R prod = R(1), prod_half = R(1);
 #pragma unroll
       for (int k = 0; k < HPL; ++k) {
-        const cpx_pair<R> tt = trow[G * k];
+        const cpx_pair<R> tt = PRE_T ? p.t01[k] : s_t01[i * MP + lane + G * k];
         cpx<R> rr;
         if (ACT == ACT_LOGCOSH) {
           cpx<R> c1 = tt.b;
@@ -170,12 +202,12 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
       if (HALF) lsum += R(0.5) * fast_log2(prod_half);
 #pragma unroll
       for (int off = G / 2; off > 0; off >>= 1) lsum += __shfl_xor_sync(gmask, lsum, off, G);
-      const R logA = s_are[i] * dv + lsum;                  // log2 of the acceptance ratio
-      const bool acc = lu < logA;
+      const R logA = p.are * dv + lsum;                    // log2 of the acceptance ratio
+      acc = p.lu < logA;
       if (acc) {
 #pragma unroll
         for (int k = 0; k < HPL; ++k) {
-          const cpx_pair<R> tw = s_t2w[i * MP + lane + G * k];
+          const cpx_pair<R> tw = PRE_W ? p.t2w[k] : s_t2w[i * MP + lane + G * k];
           const cpx<R> w = tw.b;
           th[k].x += w.x * dv;
           th[k].y += w.y * dv;
@@ -186,7 +218,7 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
             num = g[k] + tau;
             den = cfma(g[k], tau, mk(R(1), R(0)));
           } else {
-            const cpx_pair<R> tt = trow[G * k];
+            const cpx_pair<R> tt = PRE_T ? p.t01[k] : s_t01[i * MP + lane + G * k];
             const cpx<R> bb = pos ? tt.a : tt.b;
             num = g[k] * mk(R(1) + bb.x, bb.y);
             den = cfma(g[k], bb, mk(R(1), R(0)));
@@ -195,18 +227,33 @@ NQ_D void sampler_block(const RbmDev<R>& net, SamplerRun run, int blk) {
           g[k] = inv * (num * conjc(den));
         }
         bits ^= fmask;
-        ++naccept;
       }
-      if (run.accept_bits && active && lane == 0) run.accept_bits[(size_t)t * run.B + chain] = acc ? 1 : 0;
     }
-    // end of sweep: record and resynchronise g with θ
-    const int slot = sweep - run.burn;
-    if (slot >= 0 && active && lane == 0) run.samples[(size_t)slot * run.B + chain] = bits;
+    naccept += acc ? 1u : 0u;
+    if (rec_bits) run.accept_bits[(size_t)t * run.B + chain] = acc ? 1 : 0;
+    if (++pass == run.passes) {
+      // end of sweep: record and resynchronise g with θ
+      pass = 0;
+      const int slot = sweep - run.burn;
+      if (slot >= 0 && active && lane == 0) run.samples[(size_t)slot * run.B + chain] = bits;
 #pragma unroll
-    for (int k = 0; k < HPL; ++k) g[k] = act_df<ACT>(th[k]);
+      for (int k = 0; k < HPL; ++k) g[k] = act_df<ACT>(th[k]);
+      ++sweep;
+    }
+  };
+
+  if (nsteps > 0) {
+    Pre pa, pb;
+    fetch(0, pa);
+    uint32_t t = 0;
+    for (; t + 1 < nsteps; t += 2) {
+      step(t, pa, pb);
+      step(t + 1, pb, pa);
+    }
+    if (t < nsteps) step(t, pa, pb);
   }
   if (run.write_last_at_end && active && lane == 0) run.samples[chain] = bits;
-  if (active && lane == 0) atomicAdd(run.accepted, naccept);
+  if (active && lane == 0) atomicAdd(run.accepted, (unsigned long long)naccept);
 }
 
 template <typename R, int G, int HPL, int ACT, bool EXCH, bool HALF>
@@ -214,8 +261,10 @@ __global__ void __launch_bounds__(256) rbm_sampler_kernel(RbmDev<R> net, Sampler
   sampler_block<R, G, HPL, ACT, EXCH, HALF>(net, run, blockIdx.x);
 }
 
-// Many independent problems in one launch: problem p owns blocks
+// Many independent problems in one launch: job p owns blocks
 // [blk_start[p], blk_start[p+1]); every block loads its own problem's tables.
+// A problem whose hidden units fit in half the units per lane of the largest
+// one runs the narrower loop (its blocks lay out their tables for it).
 template <typename R, int G, int HPL, int ACT>
 __global__ void __launch_bounds__(256)
 rbm_sampler_batch_kernel(const SamplerJob<R>* __restrict__ jobs, const int* __restrict__ blk_start, int np) {
@@ -226,7 +275,12 @@ rbm_sampler_batch_kernel(const SamplerJob<R>* __restrict__ jobs, const int* __re
     if (__ldg(blk_start + mid) <= b) lo = mid; else hi = mid - 1;
   }
   const SamplerJob<R> job = jobs[lo];
-  sampler_block<R, G, HPL, ACT>(job.net, job.run, b - __ldg(blk_start + lo));
+  const int blk = b - __ldg(blk_start + lo);
+  constexpr int HLO = (HPL + 1) / 2;
+  if (HLO < HPL && job.net.M <= G * HLO)
+    sampler_block<R, G, HLO, ACT, false, false, false>(job.net, job.run, blk);
+  else
+    sampler_block<R, G, HPL, ACT, false, false, false>(job.net, job.run, blk);
 }
 
 }  // namespace
