@@ -315,8 +315,11 @@ nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
  * (SR(precision=...), default 1e-4) and the iteration cap (default 10 P as
  * SRIterative.jl:99).  nq_sr_info returns [iterations, |r|/|F|] of the last
  * iterative solve; for the direct solve (NQ_SR_DIRECT) it returns
- * [FP64-residual corrections, |Δx|/|x| of the last correction] of the last
- * single-problem solve (the corrections stop below 1e-13 |x|, at most 12). */
+ * [FP64-residual corrections, relative error bound] of the last
+ * single-problem solve: the corrections stop once the last one, or the error
+ * it leaves (|Δx_k|²/|Δx_{k-1}| while each correction shrinks the previous by
+ * more than half), is below 1e-13 |x|, at most 12; the bound is the smaller of
+ * the two. */
 nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter);
 nq_status nq_sr_info(nq_handle* h, double* out2);
 /* Limit, in nanoseconds, of every grid-barrier wait in this handle's SR solve
@@ -330,7 +333,7 @@ nq_status nq_set_wait_limit(nq_handle* h, uint64_t limit_ns);
  * kind: 0 = sr_shift (S_ii += eps), 1 = sr_multiplicative
  * (S + max(lam0*b^iter, lam_min) diag S), 2 = sr_none.  The reference's
  * Cholesky solve of S Δw = F becomes an FP32 inverse of the shifted S (block
- * Gauss–Jordan) with FP64-residual refinement iterated until the correction
+ * Gauss–Jordan) with FP64-residual refinement iterated until the error left
  * is below 1e-13 of Δw: Δw solves the FP64 system.  dw_out (nullable)
  * receives Δw (complex128 or float64).  NQ_ERR_NOT_PD: a non-positive pivot
  * (the shifted S is not positive definite); NQ_ERR_NAN: non-finite Δw. */

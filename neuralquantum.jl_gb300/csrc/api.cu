@@ -10,9 +10,9 @@ namespace {
 // FP64-residual corrections after the first solve with the FP32 inverse; each
 // gains about -log10(cond(S + shift) * 6e-8) digits
 // FP64-residual corrections of the shifted solve: at most kSolveRefine in the
-// single-problem cooperative refinement (it stops once a correction is below
-// kRefineTol of the solution), exactly kSolveRefineBatch in the many-problem
-// step's per-problem graph branches
+// single-problem cooperative refinement and at most kSolveRefineBatch in the
+// grouped many-problem refinement (both stop once a correction, or the error
+// it leaves, is below kRefineTol of the solution)
 constexpr int kSolveRefine = 12;
 // largest X + Xlo (bytes) for which an NQ_S_F32 request runs as 3xTF32 on tcgen05
 constexpr double kSf32TensorBytes = 16e9;
@@ -1869,6 +1869,8 @@ nq_status batch_setup_grouped(nq_batch* b) {
   g.fill_blk = dp(6); g.fill_blocks = P_(6, np);
   g.master_elem = dp(7); g.master_elems = P_(7, np);
   g.tab_elem = dp(8); g.tab_elems = P_(8, np);
+  g.P_max = 0;
+  for (nq_handle* h : b->hs) g.P_max = std::max(g.P_max, h->P);
   b->grouped = true;
   return NQ_OK;
 }

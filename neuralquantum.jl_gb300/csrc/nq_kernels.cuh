@@ -269,12 +269,20 @@ NQ_D double sr_diag_shift(const double* S, int P, int i, int kind, double eps, d
   if (kind == 1) return lam * S[2 * ((size_t)i + (size_t)P * i)];
   return 0.0;
 }
-// the FP64-residual refinement (x0 = A⁻¹F, then corrections until
-// |Δx| <= tol |x| or max_corr of them, last residual in r) as one cooperative
-// launch of at most kRefineMaxCtas CTAs; ctl: sweep_ctl_bytes(); norms:
-// refine_norm_doubles(); info (nullable): [corrections, last |Δx|/|x|]
+// the FP64-residual refinement (x0 = A⁻¹F, then corrections until |Δx_k|,
+// or the error |Δx_k|²/|Δx_{k-1}| it leaves while the iteration contracts,
+// is <= tol |x|, or max_corr of them) as one cooperative launch of at most
+// kRefineMaxCtas CTAs; ctl: sweep_ctl_bytes(); norms: refine_norm_doubles();
+// info (nullable): [corrections, the smaller of the last |Δx|/|x| and the
+// estimated relative error after it]
 constexpr int kRefineMaxCtas = 256;
 constexpr double kRefineTol = 1e-13;
+// shared memory of a refinement CTA: the GEMV vector (P complex doubles) when
+// it fits the default 48 KiB, else none (the vector is read from L2)
+constexpr size_t kRefineStageMax = 48 * 1024;
+constexpr size_t refine_stage_bytes(int P) {
+  return (size_t)16 * P <= kRefineStageMax ? (size_t)16 * P : (P > 0 ? kRefineStageMax : 0);
+}
 constexpr size_t refine_norm_doubles() { return 2 * (size_t)kRefineMaxCtas * 8; }
 cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const double* F, int kind, double eps,
                                double lam, bool real_params, int max_corr, double tol, double* x, double* r,
@@ -347,7 +355,8 @@ struct SolveBufs {
 };
 // shifted solve (S + shift) x = F: FP32 explicit inverse, then x_0 = A^-1 F and
 // corrections x += A^-1 (F - A x) with the residual in FP64 until the
-// correction is below kRefineTol |x| (at most refine_iters of them);
+// correction, or the error it leaves, is below kRefineTol |x| (at most
+// refine_iters of them);
 // a pivot <= 0 sets bit 0 of status
 cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kind, double eps,
                             double lam, bool real_params, int refine_iters, cudaStream_t st);
@@ -443,6 +452,7 @@ struct SrGroup {
   const int* fill_blk = nullptr; int fill_blocks = 0;         // ceil(P / 32)^2 tiles
   const int* master_elem = nullptr; int master_elems = 0;     // 2P doubles
   const int* tab_elem = nullptr; int tab_elems = 0;           // N * M table entries
+  int P_max = 0;                                              // largest P of the group
 };
 // force partial sums, their reductions and F of every problem
 cudaError_t launch_force_group(const SrGroup& g, cudaStream_t st);

@@ -443,13 +443,15 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
 //   grid barrier,
 //   r = F - A x in FP64 from the FP64 S and the shift (one warp per row;
 //   rf = FP32 copy of r),
-// until the correction is negligible, |y| <= tol |x|, or after max_corr
-// corrections; a grid barrier separates the passes.  Every CTA sums the
-// per-warp |y|² and |x|² partials of the pass in the same fixed order, so all
-// CTAs take the same decision.  Each correction shrinks the error by the
+// until the correction, or the error it leaves, is below tol |x|, or after
+// max_corr corrections; a grid barrier separates the passes.  Every CTA sums
+// the per-warp |y|² and |x|² partials of the pass in the same fixed order, so
+// all CTAs take the same decision.  Each correction shrinks the error by the
 // FP32 inverse's error ‖I - A⁻¹₃₂ A‖, so x converges to the FP64 solution of
 // the shifted system (limited by the FP64 residual, about cond(A) 1e-16).
-// The last residual stays in r; info = [corrections, |y|/|x| of the last one].
+// info = [corrections, relative error bound of the last one].  Each CTA
+// copies the vector of a GEMV (rf, then x) into shared memory once per pass
+// when P fits (refine_stage_bytes), instead of every warp reading it from L2.
 // A non-finite x sets NQ_DEVERR_NONFINITE in the status word.
 // The refinement of one matrix on the CTAs rank = 0..nranks-1 that share ctl.
 NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restrict__ S, int P,
@@ -459,18 +461,27 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = rank * (blockDim.x >> 5) + wib, nw = nranks * (blockDim.x >> 5);
   __shared__ double s_red[2][8];
+  extern __shared__ __align__(16) unsigned char s_vec[];
+  const bool stage = (size_t)16 * P <= kRefineStageMax;
+  float2* const s_rf = reinterpret_cast<float2*>(s_vec);
+  double2* const s_x = reinterpret_cast<double2*>(s_vec);
   for (int i = rank * blockDim.x + threadIdx.x; i < P; i += nranks * blockDim.x)
     rf[i] = make_float2((float)F[2 * i], real_params ? 0.f : (float)F[2 * i + 1]);
   if (!group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
+  double ty_prev = 0.0;
   for (int it = 0;; ++it) {
     double yy = 0.0, xx = 0.0;
     bool finite = true;
+    if (stage) {
+      for (int j = threadIdx.x; j < P; j += blockDim.x) s_rf[j] = __ldcg(rf + j);
+      __syncthreads();
+    }
     for (int i = gw; i < P; i += nw) {
       const float2* col = W + (size_t)P * i;
       float sx = 0.f, sy = 0.f;
 #pragma unroll 8
       for (int j = lane; j < P; j += 32) {
-        const float2 w = __ldcg(col + j), v = __ldcg(rf + j);
+        const float2 w = __ldcg(col + j), v = stage ? s_rf[j] : __ldcg(rf + j);
         sx += w.x * v.x + w.y * v.y;
         sy += w.x * v.y - w.y * v.x;
       }
@@ -521,21 +532,38 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
       ty += s_red[0][w];
       tx += s_red[1][w];
     }
-    const bool last = (it > 0 && ty <= tol * tol * tx) || it >= max_corr || !(tx == tx);
+    // Stop when the correction just applied, or the error it leaves, is below
+    // tol |x|.  The iteration contracts by ρ ≈ |Δx_k| / |Δx_{k-1}|, so the
+    // error after Δx_k is about ρ |Δx_k| = |Δx_k|² / |Δx_{k-1}| (trusted
+    // when ρ < 1/2).  The residual of the final x is not formed.
+    const bool small = it > 0 && ty <= tol * tol * tx;
+    const bool contracting = it > 1 && ty < 0.25 * ty_prev;
+    const bool est = contracting && ty * ty <= tol * tol * tx * ty_prev;
+    const bool last = small || est || it >= max_corr || !(tx == tx);
     if (last && rank == 0 && threadIdx.x == 0 && info) {
       info[0] = (double)it;
-      info[1] = tx > 0.0 ? sqrt(ty / tx) : 0.0;
+      // the smaller of |Δx_k| / |x| and the estimated error after it
+      double rel = tx > 0.0 ? sqrt(ty / tx) : 0.0;
+      if (contracting && tx > 0.0 && ty_prev > 0.0) rel = fmin(rel, ty / sqrt(tx * ty_prev));
+      info[1] = rel;
+    }
+    ty_prev = ty;
+    if (last) break;
+    if (stage) {
+      for (int l = threadIdx.x; l < P; l += blockDim.x) s_x[l] = make_double2(__ldcg(x + 2 * l), __ldcg(x + 2 * l + 1));
+      __syncthreads();
     }
     for (int k = gw; k < P; k += nw) {
       // (S x)_k = Σ_l conj(S[l][k]) x_l (Hermitian; column k contiguous)
-      const double* col = S + 2 * (size_t)P * k;
+      const double2* col = reinterpret_cast<const double2*>(S + 2 * (size_t)P * k);
       double sx = 0.0, sy = 0.0;
 #pragma unroll 8
       for (int l = lane; l < P; l += 32) {
-        const double ar = col[2 * l], ai = l == k ? 0.0 : -col[2 * l + 1];
-        const double xr = __ldcg(x + 2 * l), xi = __ldcg(x + 2 * l + 1);
-        sx += ar * xr - ai * xi;
-        sy += ar * xi + ai * xr;
+        const double2 a = __ldg(col + l);
+        const double ar = a.x, ai = l == k ? 0.0 : -a.y;
+        const double2 xv = stage ? s_x[l] : make_double2(__ldcg(x + 2 * l), __ldcg(x + 2 * l + 1));
+        sx += ar * xv.x - ai * xv.y;
+        sy += ar * xv.y + ai * xv.x;
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
@@ -552,7 +580,6 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
         rf[k] = make_float2((float)rx, (float)ry);
       }
     }
-    if (last) break;
     if (!group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
   }
 }
@@ -669,7 +696,7 @@ cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const do
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = refine_stage_bytes(P);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -692,7 +719,7 @@ cudaError_t launch_refine_group(const SrGroup& g, const int* cta_start, int tota
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(total_ctas);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = refine_stage_bytes(g.P_max);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
