@@ -348,7 +348,7 @@ struct SolveBufs {
   float2* yf = nullptr;       // [P] complex float correction
   int* status = nullptr;      // device status word
   void* ctl = nullptr;        // grid-barrier control block of the cooperative sweep
-  double* norms = nullptr;    // refinement: per-warp |y|², |x|² (refine_norm_doubles())
+  double* norms = nullptr;    // refinement: per-CTA |y|², |x|² (refine_norm_doubles())
   double* info = nullptr;     // refinement: [corrections, |y|/|x| of the last correction]
   uint64_t wait_ns = kNqWaitNs;   // limit of every grid-barrier wait of the solve
   cudaEvent_t* ev = nullptr;  // optional [6] events: copy, inversion, fill+rhs, first solve, refinement, end

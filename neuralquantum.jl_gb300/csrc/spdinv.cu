@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(256) herm_gemv_neg_kernel(const float2* __rest
 //   rf = FP32 copy of r),
 // until the correction, or the error it leaves, is below tol |x|, or after
 // max_corr corrections; a grid barrier separates the passes.  Every CTA sums
-// the per-warp |y|² and |x|² partials of the pass in the same fixed order, so
+// the per-CTA |y|² and |x|² partials of the pass in the same fixed order, so
 // all CTAs take the same decision.  Each correction shrinks the error by the
 // FP32 inverse's error ‖I - A⁻¹₃₂ A‖, so x converges to the FP64 solution of
 // the shifted system (limited by the FP64 residual, about cond(A) 1e-16).
@@ -479,11 +479,26 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
     for (int i = gw; i < P; i += nw) {
       const float2* col = W + (size_t)P * i;
       float sx = 0.f, sy = 0.f;
+      if (stage && !(P & 1)) {
+        // two elements per 16-byte load (the column starts 16-byte aligned
+        // when P is even): all of a column's loads are in flight at once
+        const float4* col4 = reinterpret_cast<const float4*>(col);
+#pragma unroll 16
+        for (int j2 = lane; 2 * j2 < P; j2 += 32) {
+          const float4 w = __ldcg(col4 + j2);
+          const float2 v0 = s_rf[2 * j2], v1 = s_rf[2 * j2 + 1];
+          sx += w.x * v0.x + w.y * v0.y;
+          sy += w.x * v0.y - w.y * v0.x;
+          sx += w.z * v1.x + w.w * v1.y;
+          sy += w.z * v1.y - w.w * v1.x;
+        }
+      } else {
 #pragma unroll 8
-      for (int j = lane; j < P; j += 32) {
-        const float2 w = __ldcg(col + j), v = stage ? s_rf[j] : __ldcg(rf + j);
-        sx += w.x * v.x + w.y * v.y;
-        sy += w.x * v.y - w.y * v.x;
+        for (int j = lane; j < P; j += 32) {
+          const float2 w = __ldcg(col + j), v = stage ? s_rf[j] : __ldcg(rf + j);
+          sx += w.x * v.x + w.y * v.y;
+          sy += w.x * v.y - w.y * v.x;
+        }
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
@@ -504,15 +519,26 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
         finite = finite && isfinite(nx) && isfinite(ny);
       }
     }
+    // the CTA's |y|² and |x|² partials, its warps summed in a fixed order
     if (lane == 0) {
-      norms[2 * gw] = yy;
-      norms[2 * gw + 1] = xx;
+      s_red[0][wib] = yy;
+      s_red[1][wib] = xx;
       if (!finite) atomicOr(status, NQ_DEVERR_NONFINITE);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double cy = 0.0, cx = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        cy += s_red[0][w];
+        cx += s_red[1][w];
+      }
+      norms[2 * rank] = cy;
+      norms[2 * rank + 1] = cx;
     }
     if (!group_barrier(ctl, (unsigned)nranks, status, limit_ns)) return;
     // |y|² and |x|² of this pass, summed by every CTA in the same order
     double ty = 0.0, tx = 0.0;
-    for (int w = threadIdx.x; w < nw; w += blockDim.x) {
+    for (int w = threadIdx.x; w < nranks; w += blockDim.x) {
       ty += __ldcg(norms + 2 * w);
       tx += __ldcg(norms + 2 * w + 1);
     }
@@ -556,15 +582,24 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
     for (int k = gw; k < P; k += nw) {
       // (S x)_k = Σ_l conj(S[l][k]) x_l (Hermitian; column k contiguous)
       const double2* col = reinterpret_cast<const double2*>(S + 2 * (size_t)P * k);
-      double sx = 0.0, sy = 0.0;
-#pragma unroll 8
-      for (int l = lane; l < P; l += 32) {
+      // four independent FP64 accumulators per lane
+      double sx0 = 0.0, sy0 = 0.0, sx1 = 0.0, sy1 = 0.0;
+#pragma unroll 4
+      for (int l = lane; l < P; l += 64) {
+        const int l1 = l + 32;
         const double2 a = __ldg(col + l);
+        const double2 b = l1 < P ? __ldg(col + l1) : make_double2(0.0, 0.0);
         const double ar = a.x, ai = l == k ? 0.0 : -a.y;
-        const double2 xv = stage ? s_x[l] : make_double2(__ldcg(x + 2 * l), __ldcg(x + 2 * l + 1));
-        sx += ar * xv.x - ai * xv.y;
-        sy += ar * xv.y + ai * xv.x;
+        const double br = b.x, bi = l1 == k ? 0.0 : -b.y;
+        const double2 xa = stage ? s_x[l] : make_double2(__ldcg(x + 2 * l), __ldcg(x + 2 * l + 1));
+        const double2 xb = l1 >= P ? make_double2(0.0, 0.0)
+                           : stage ? s_x[l1] : make_double2(__ldcg(x + 2 * l1), __ldcg(x + 2 * l1 + 1));
+        sx0 += ar * xa.x - ai * xa.y;
+        sy0 += ar * xa.y + ai * xa.x;
+        sx1 += br * xb.x - bi * xb.y;
+        sy1 += br * xb.y + bi * xb.x;
       }
+      double sx = sx0 + sx1, sy = sy0 + sy1;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
         sx += __shfl_xor_sync(0xffffffffu, sx, off);
