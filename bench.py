@@ -130,9 +130,13 @@ def s_precision_choice():
 # DRAM bytes (read + write) of one gram_tf32_kernel launch on this workload, from
 # the ncu capture summarised in profiles/gram_tf32_c1.txt
 GRAM_TRAFFIC_BYTES = 701.59e6
-# warp instructions of one production launch of the Metropolis kernel on this
-# workload (ncu smsp__inst_executed.sum, profiles/rbm_sampler_c1.txt)
-SAMPLER_WARP_INSTRUCTIONS = 526.8e6
+# one ncu capture of a production launch of the Metropolis kernel on this
+# workload (profiles/rbm_sampler_c1.txt): warp instructions
+# (smsp__inst_executed.sum), the capture's duration, its issue-active share and
+# the acceptance of that launch (the accepted-flip update is most of the
+# difference between launches)
+SAMPLER_NCU = {"warp_instructions": 534.2e6, "duration_us": 726.0, "issue_active_pct": 65.7, "acceptance": 0.888,
+               "warp_instructions_per_warp_step": 177.4}
 # DRAM bytes (read + write) of one sampler launch (same capture)
 SAMPLER_TRAFFIC_BYTES = 62e3
 # algorithmic FP32 flops of one Metropolis proposal per hidden unit: the ratio
@@ -248,12 +252,15 @@ def run_gb300(args, barrier=None):
         "frac": s_flops / (s_kernel_ms * 1e-3) / 1e12 / bf16_peak, "traffic": GRAM_TRAFFIC_BYTES,
         "note": "peak = measured dense bf16 burst (of measured); algorithmic flops = 2*(2P)^2*Ns/2 per launch; "
                 "TF32 operands issue at half the bf16 rate"}
+    issue_rate = SAMPLER_NCU["warp_instructions"] / (SAMPLER_NCU["duration_us"] * 1e-6)
     roof["sampler_issue_bound"] = {
-        "bound": "instruction issue", "warp_instructions_per_launch": SAMPLER_WARP_INSTRUCTIONS,
-        "achieved": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3), "peak": 152 * 4 * sm_ghz * 1e9,
-        "unit": "warp instructions/s",
-        "frac": SAMPLER_WARP_INSTRUCTIONS / (st[6] * 1e-3) / (152 * 4 * sm_ghz * 1e9),
-        "note": "executed (not algorithmic) instructions from one ncu capture of this workload's launch"}
+        "bound": "instruction issue", "warp_instructions_per_launch": SAMPLER_NCU["warp_instructions"],
+        "achieved": issue_rate, "peak": 152 * 4 * 2.07e9, "unit": "warp instructions/s",
+        "frac": issue_rate / (152 * 4 * 2.07e9), "issue_active_pct": SAMPLER_NCU["issue_active_pct"],
+        "note": (f"executed (not algorithmic) instructions over the duration of one ncu capture of this "
+                 f"workload's launch (acceptance {SAMPLER_NCU['acceptance']}, "
+                 f"{SAMPLER_NCU['warp_instructions_per_warp_step']} warp instructions per warp and step); "
+                 f"peak = 152 SMs x 4 schedulers x 2.07 GHz")}
 
     line = {
         "metric": METRIC, "value": value, "unit": "SR steps/s", "n_gpus": args.gpus,
