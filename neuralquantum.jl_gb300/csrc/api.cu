@@ -1823,9 +1823,12 @@ nq_status batch_setup_grouped(nq_batch* b) {
     SrJob& j = jobs[p];
     j.N = h->N; j.M = h->M; j.P = h->P; j.hilb = h->hilb; j.act = h->act; j.Ns = h->Ns; j.B = h->B; j.L = h->L;
     j.Ns_pad = h->Ns_pad;
-    j.force_CH = rbm_force_chunk(h->N, h->M);
+    j.force_CH = rbm_force_chunk(h->N, h->M, h->Ns);
     j.force_nblk = (h->Ns + j.force_CH - 1) / j.force_CH;
-    fsmem = std::max(fsmem, rbm_force_smem(h->N, h->M));
+    if (j.force_nblk > h->force_nblk)      // the handle's partial buffers hold force_nblk blocks
+      return bfail(b, NQ_ERR_STATE, "problem %d: grouped force needs %d partial blocks, %d allocated", p,
+                   j.force_nblk, h->force_nblk);
+    fsmem = std::max(fsmem, rbm_force_smem(h->N, h->M, h->Ns));
     j.samples = h->d_samples;
     j.g = reinterpret_cast<const float2*>(h->d_g);
     j.eloc = reinterpret_cast<const float2*>(h->d_eloc);

@@ -457,8 +457,8 @@ struct SrGroup {
 // force partial sums, their reductions and F of every problem
 cudaError_t launch_force_group(const SrGroup& g, cudaStream_t st);
 // FP32 force-kernel geometry of one problem: samples per block, shared memory
-int rbm_force_chunk(int N, int M);
-size_t rbm_force_smem(int N, int M);
+int rbm_force_chunk(int N, int M, int Ns);
+size_t rbm_force_smem(int N, int M, int Ns);
 // Measurement statistics of every problem's E_loc
 cudaError_t launch_stats_group(const SrGroup& g, cudaStream_t st);
 // X of every problem (TF32-rounded; Xlo when split3)

@@ -7,6 +7,9 @@
 // (sampler), src/IterativeInterface/Accumulators/AccumulatorObsScalar.jl:52-137
 // (estimator), src/IterativeInterface/Samplers/CostFun/BatchedValSampler.jl:97-115
 // and BaseIterativeSampler.jl:19-26 (centring and force).
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 
 #include "nq_kernels.cuh"
@@ -302,8 +305,12 @@ NQ_D void eval_block(const RbmDev<R>& net, const uint64_t* __restrict__ samples,
   eloc[s] = E;
 }
 
+// largest block of the single-problem estimator: 512 threads in FP32; FP64
+// keeps 256 (its 78 registers per thread would spill under a 512 bound)
+template <typename R> constexpr int kEvalMaxThreads = sizeof(R) == 4 ? 512 : 256;
+
 template <typename R, int ACT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kEvalMaxThreads<R>)
 rbm_eval_kernel(RbmDev<R> net, const uint64_t* __restrict__ samples, int Ns, DevOp op,
                 int has_op, cpx<R>* __restrict__ logpsi, cpx<R>* __restrict__ gout,
                 cpx<R>* __restrict__ eloc, int theta_in_g) {
@@ -446,7 +453,7 @@ NQ_D void force_partial_block(int N, int M, int hilb, const uint64_t* __restrict
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 rbm_force_partial_kernel(int N, int M, int hilb, const uint64_t* __restrict__ samples, int Ns,
                          const cpx<R>* __restrict__ g, const cpx<R>* __restrict__ eloc, int CH,
                          double* __restrict__ partial, double* __restrict__ partialE) {
@@ -628,15 +635,68 @@ static int eval_threads(int M, size_t csize, int Tmax = 128) {
   return T;
 }
 
+static size_t eval_smem(int N, int M, int T, bool has_op, size_t csize) {
+  const size_t M8 = (size_t)(M + 7) & ~(size_t)7;
+  return (M8 * N + M8 + N + M8 * T + (has_op ? 2 * (size_t)N * M8 : 0)) * csize;
+}
+
+// Threads per block of the single-problem estimator: one thread per sample,
+// and the per-thread slices of g in shared memory bound the blocks per SM, so
+// a fixed block size can leave a short second wave (81920 samples at 256
+// threads: 320 blocks for 304 slots).  The block size (a multiple of 32 up to
+// kEvalMaxThreads) with the fewest waves wins, then the one with the most
+// resident threads per SM.  Cached per (N, M, Ns, operator, activation, precision).
+template <typename R, typename K>
+static int eval_block_threads(K kern, int N, int M, int Ns, bool has_op, int act) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int, int>, int> cache;
+  const auto key = std::make_tuple(N, M, Ns, has_op ? 1 : 0, act, (int)sizeof(R));
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 0;
+  int best = eval_threads(M, sizeof(cpx<R>), 256);
+  long best_waves = -1;
+  int best_res = 0;
+  for (int T = 64; sms > 0 && T <= kEvalMaxThreads<R>; T += 32) {
+    const size_t smem = eval_smem(N, M, T, has_op, sizeof(cpx<R>));
+    if (smem > 227 * 1024) break;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaGetLastError();
+      break;
+    }
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, T, smem) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (bps < 1) continue;
+    const long blocks = (Ns + T - 1) / T, slots = (long)sms * bps;
+    const long waves = (blocks + slots - 1) / slots;
+    const int res = bps * T;
+    if (best_waves < 0 || waves < best_waves || (waves == best_waves && res > best_res)) {
+      best_waves = waves;
+      best_res = res;
+      best = T;
+    }
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = best;
+  return best;
+}
+
 template <typename R>
 cudaError_t launch_rbm_eval(const RbmDev<R>& net, const uint64_t* samples, int Ns, const DevOp* op,
                             cpx<R>* logpsi, cpx<R>* g, cpx<R>* eloc, cudaStream_t st, int theta_in_g) {
-  // up to 256 threads: the per-thread slices of g bound the occupancy, the
-  // shared tables are amortised over more samples
-  const int T = eval_threads(net.M, sizeof(cpx<R>), 256);
   const int has_op = op != nullptr && eloc != nullptr;
-  const size_t M8 = (size_t)(net.M + 7) & ~(size_t)7;
-  size_t smem = (M8 * net.N + M8 + net.N + M8 * T + (has_op ? 2 * (size_t)net.N * M8 : 0)) * sizeof(cpx<R>);
+  const int T = net.act == ACT_LOGCOSH
+                    ? eval_block_threads<R>(rbm_eval_kernel<R, ACT_LOGCOSH>, net.N, net.M, Ns, has_op, net.act)
+                    : eval_block_threads<R>(rbm_eval_kernel<R, ACT_SOFTPLUS>, net.N, net.M, Ns, has_op, net.act);
+  const size_t smem = eval_smem(net.N, net.M, T, has_op, sizeof(cpx<R>));
   DevOp dop;
   if (has_op) dop = *op;
   const int blocks = (Ns + T - 1) / T;
@@ -696,15 +756,70 @@ static int force_chunk(int N, int M, int csize) {
   return CH;
 }
 
+// Geometry of the force partial sums: one thread per work item (M ceil(N/4)
+// blocks of W, M of b, N of a) in one round, and the samples per block (CH, a
+// multiple of 8) that put every block in one wave with the most resident
+// threads per SM, counted up to 1024 (32 warps hide the latency), then the
+// largest CH (fewer partials to write and reduce).  The grouped many-problem
+// force uses the same CH per problem.  Cached per (N, M, Ns, precision).
+struct ForceGeom { int CH, T; };
+template <typename R>
+static ForceGeom force_geom(int N, int M, int Ns) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int>, ForceGeom> cache;
+  const auto key = std::make_tuple(N, M, Ns, (int)sizeof(R));
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const int csize = (int)sizeof(cpx<R>);
+  const int items = M * (((N + 3) & ~3) / 4) + M + N;
+  ForceGeom best{force_chunk(N, M, csize), 256};
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 0;
+  const int T = std::min(512, std::max(64, (items + 31) & ~31));
+  long best_waves = -1;
+  int best_res = 0;
+  auto kern = rbm_force_partial_kernel<R>;
+  for (int CH = 32; sms > 0 && CH <= 256; CH += 8) {
+    const size_t smem = force_smem(N, M, CH, csize);
+    if (smem > 227 * 1024) break;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaGetLastError();
+      break;
+    }
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, T, smem) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (bps < 1) continue;
+    const long blocks = (Ns + CH - 1) / CH, slots = (long)sms * bps;
+    const long waves = (blocks + slots - 1) / slots;
+    const int res = std::min(bps * T, 1024);
+    if (best_waves < 0 || waves < best_waves || (waves == best_waves && res >= best_res)) {
+      best_waves = waves;
+      best_res = res;
+      best = ForceGeom{CH, T};
+    }
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = best;
+  return best;
+}
+
 int rbm_force_nblocks(int Ns, int N, int M, int csize) {
-  int CH = force_chunk(N, M, csize);
+  const int CH = csize == (int)sizeof(cpx<float>) ? force_geom<float>(N, M, Ns).CH : force_geom<double>(N, M, Ns).CH;
   return (Ns + CH - 1) / CH;
 }
 
 template <typename R>
 cudaError_t launch_rbm_force(const RbmDev<R>& net, const uint64_t* samples, int Ns, const cpx<R>* g,
                              const cpx<R>* eloc, const ForceBufs& fb, cudaStream_t st) {
-  const int CH = force_chunk(net.N, net.M, (int)sizeof(cpx<R>));
+  const ForceGeom fg = force_geom<R>(net.N, net.M, Ns);
+  const int CH = fg.CH;
   const int nblk = (Ns + CH - 1) / CH;
   const size_t smem = force_smem(net.N, net.M, CH, (int)sizeof(cpx<R>));
   auto kern = rbm_force_partial_kernel<R>;
@@ -712,8 +827,8 @@ cudaError_t launch_rbm_force(const RbmDev<R>& net, const uint64_t* samples, int 
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  kern<<<nblk, 256, smem, st>>>(net.N, net.M, net.hilb, samples, Ns, g, eloc, CH, fb.partial,
-                                fb.partialE);
+  kern<<<nblk, fg.T, smem, st>>>(net.N, net.M, net.hilb, samples, Ns, g, eloc, CH, fb.partial,
+                                 fb.partialE);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int P = net.N + net.M + net.M * net.N;
@@ -777,5 +892,9 @@ cudaError_t launch_update_group(const SrGroup& g, double lr, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-int rbm_force_chunk(int N, int M) { return force_chunk(N, M, (int)sizeof(cpx<float>)); }
-size_t rbm_force_smem(int N, int M) { return force_smem(N, M, rbm_force_chunk(N, M), (int)sizeof(cpx<float>)); }
+// the grouped force uses the single-problem chunking, so a handle's partial
+// buffers (sized by rbm_force_nblocks) fit it and both give the same F
+int rbm_force_chunk(int N, int M, int Ns) { return force_geom<float>(N, M, Ns).CH; }
+size_t rbm_force_smem(int N, int M, int Ns) {
+  return force_smem(N, M, rbm_force_chunk(N, M, Ns), (int)sizeof(cpx<float>));
+}
