@@ -240,19 +240,34 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
         const int sa = max(i, kn), sb = min(i, kn);
         const bool v_from_c = k >= 0 && i == k;          // stored (kn, k) after step k is C_kn
         const bool v_update = k >= 0 && nblk > 1 && !v_from_c;
+        // every global load of the five tiles is issued before the first
+        // shared-memory store, so the phase costs one L2 round trip
+        float2 ld[5][CB * CB / 256];
+        const float2 z2 = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int e0 = 0; e0 < CB * CB; e0 += 256) {
-          const int e = e0 + threadIdx.x, r = e & 31, c = e >> 5;
-          Dt[r][c] = herm_block_elem(W, P, kn, kn, r, c);
+        for (int q = 0; q < CB * CB / 256; ++q) {
+          const int e = q * 256 + threadIdx.x, r = e & 31, c = e >> 5;
+          ld[0][q] = herm_block_elem(W, P, kn, kn, r, c);
+          ld[1][q] = k >= 0 ? __ldcg(Cc + (size_t)kn * tile + e) : z2;
+          ld[2][q] = k >= 0 ? __ldcg(Gc + (size_t)kn * tile + e) : z2;
+          const int gi = sa * CB + r, gj = sb * CB + c;
+          ld[3][q] = nblk <= 1 ? z2
+                     : v_from_c ? __ldcg(Cc + (size_t)kn * tile + e)
+                     : (gi < P && gj < P) ? __ldcg(W + (size_t)gi + (size_t)P * gj) : z2;
+          ld[4][q] = (nblk > 1 && v_update) ? __ldcg(i > kn ? Cc + (size_t)sa * tile + e : Gc + (size_t)sb * tile + e)
+                                             : z2;
+        }
+#pragma unroll
+        for (int q = 0; q < CB * CB / 256; ++q) {
+          const int e = q * 256 + threadIdx.x, r = e & 31, c = e >> 5;
+          Dt[r][c] = ld[0][q];
           if (k >= 0) {
-            Ut[r][c] = __ldcg(Cc + (size_t)kn * tile + e);
-            Vt[r][c] = __ldcg(Gc + (size_t)kn * tile + e);
+            Ut[r][c] = ld[1][q];
+            Vt[r][c] = ld[2][q];
           }
           if (nblk > 1) {
-            const int gi = sa * CB + r, gj = sb * CB + c;
-            Xt[r][c] = v_from_c ? __ldcg(Cc + (size_t)kn * tile + e)
-                                : (gi < P && gj < P) ? __ldcg(W + (size_t)gi + (size_t)P * gj) : make_float2(0.f, 0.f);
-            if (v_update) Yt[r][c] = __ldcg(i > kn ? Cc + (size_t)sa * tile + e : Gc + (size_t)sb * tile + e);
+            Xt[r][c] = ld[3][q];
+            if (v_update) Yt[r][c] = ld[4][q];
           }
         }
         __syncthreads();
