@@ -15,9 +15,9 @@
 // W = -A^-1.  Each step is one phase between grid barriers: the rank-32
 // update of step k runs beside the preparation of step k+1 (its pivot
 // inverse, a 32x32 Gauss–Jordan held in registers, and its C and G), see
-// sweep_group.  The grid barrier is a generation counter with a bounded spin
-// (1 s, sticky abort flag): a stalled barrier ends the kernel with a status
-// bit.
+// sweep_group.  The grid barrier is a ticket counter (ticket_grid_barrier)
+// with a bounded spin (1 s by default, sticky abort flag): a stalled barrier
+// ends the kernel with a status bit.
 #include <algorithm>
 
 #include "nq_kernels.cuh"
@@ -28,43 +28,15 @@ namespace {
 constexpr int CB = 32;
 
 struct SweepCtl {
-  unsigned count;      // arrivals at the current barrier
-  unsigned gen;        // barrier generation
+  unsigned count;      // arrivals since the launch (tickets)
+  unsigned gen;        // barriers completed
   int abort;           // sticky abort flag
   int pad;
 };
 
 // Barrier over the `n` CTAs that share ctl (the whole grid, or one group).
 __device__ bool group_barrier(SweepCtl* ctl, unsigned n, int* err, uint64_t limit_ns) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_ok = 1;
-    volatile unsigned* vgen = &ctl->gen;
-    const unsigned g = *vgen;
-    __threadfence();
-    if (atomicAdd(&ctl->count, 1u) == n - 1) {
-      atomicExch(&ctl->count, 0u);
-      __threadfence();
-      atomicAdd(&ctl->gen, 1u);
-    } else {
-      const uint64_t t0 = globaltimer_ns();
-      unsigned it = 0;
-      while (*vgen == g) {
-        if (*(volatile int*)&ctl->abort) { s_ok = 0; break; }
-        // the timer is read every 256 polls, every poll under a sub-0.1 ms limit
-        if (((++it & 255u) == 0 || limit_ns < 100000u) && globaltimer_ns() - t0 > limit_ns) {
-          atomicOr(err, NQ_DEVERR_TIMEOUT);
-          atomicExch(&ctl->abort, 1);
-          s_ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return s_ok != 0;
+  return ticket_grid_barrier(&ctl->count, &ctl->gen, &ctl->abort, n, err, limit_ns);
 }
 
 NQ_D float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }

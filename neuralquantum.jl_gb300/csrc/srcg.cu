@@ -28,35 +28,7 @@ struct CgCtl {
 };
 
 __device__ bool cg_barrier(CgCtl* ctl, int* err, uint64_t limit_ns) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_ok = 1;
-    volatile unsigned* vgen = &ctl->gen;
-    const unsigned g = *vgen;
-    __threadfence();
-    if (atomicAdd(&ctl->count, 1u) == gridDim.x - 1) {
-      atomicExch(&ctl->count, 0u);
-      __threadfence();
-      atomicAdd(&ctl->gen, 1u);
-    } else {
-      const uint64_t t0 = globaltimer_ns();
-      unsigned it = 0;
-      while (*vgen == g) {
-        if (*(volatile int*)&ctl->abort) { s_ok = 0; break; }
-        // the timer is read every 256 polls, every poll under a sub-0.1 ms limit
-        if (((++it & 255u) == 0 || limit_ns < 100000u) && globaltimer_ns() - t0 > limit_ns) {
-          atomicOr(err, NQ_DEVERR_TIMEOUT);
-          atomicExch(&ctl->abort, 1);
-          s_ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return s_ok != 0;
+  return ticket_grid_barrier(&ctl->count, &ctl->gen, &ctl->abort, gridDim.x, err, limit_ns);
 }
 
 // fixed-order block sum of two doubles; result valid in every thread

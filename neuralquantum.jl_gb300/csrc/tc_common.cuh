@@ -16,6 +16,48 @@ NQ_D uint64_t globaltimer_ns() {
   return t;
 }
 
+// Barrier over the n CTAs that share (count, gen, abort), by tickets.  The
+// counter only grows within a launch (it is zeroed before the launch), so the
+// arrival with ticket t belongs to barrier t / n and the last arrival of
+// barrier e publishes gen = e + 1.  Thread 0 arrives with an acquire-release
+// add and waits with acquire loads (no separate fences), so the CTA's writes
+// before the barrier are visible to every CTA after it; data written by other
+// CTAs is read with L2 (.cg) loads.  The wait is bounded by limit_ns
+// (%globaltimer, read every 256 polls or every poll under 0.1 ms): on timeout
+// it sets NQ_DEVERR_TIMEOUT in *err and the abort flag, which ends the other
+// waiters.  Returns false on abort.
+NQ_D bool ticket_grid_barrier(unsigned* count, unsigned* gen, int* abort, unsigned n, int* err,
+                              uint64_t limit_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    unsigned t;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(t) : "l"(count) : "memory");
+    const unsigned target = t / n + 1;
+    if (t % n == n - 1) {
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(target) : "memory");
+    } else {
+      const uint64_t t0 = globaltimer_ns();
+      unsigned it = 0;
+      for (;;) {
+        unsigned g;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(gen) : "memory");
+        if ((int)(g - target) >= 0) break;
+        if (*(volatile int*)abort) { s_ok = 0; break; }
+        if (((++it & 255u) == 0 || limit_ns < 100000u) && globaltimer_ns() - t0 > limit_ns) {
+          atomicOr(err, NQ_DEVERR_TIMEOUT);
+          atomicExch(abort, 1);
+          s_ok = 0;
+          break;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 NQ_D void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
