@@ -446,7 +446,9 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
                             int max_corr, double tol, double* x, double* r, float2* rf, double* norms, double* info,
                             SweepCtl* ctl, int* status, uint64_t limit_ns, int rank, int nranks) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int gw = rank * (blockDim.x >> 5) + wib, nw = nranks * (blockDim.x >> 5);
+  // warps numbered across CTAs first, so the rows of both GEMVs spread over
+  // every CTA (and SM) when there are fewer rows than warps
+  const int gw = wib * nranks + rank, nw = nranks * (blockDim.x >> 5);
   __shared__ double s_red[2][8];
   extern __shared__ __align__(16) unsigned char s_vec[];
   const bool stage = (size_t)16 * P <= kRefineStageMax;
