@@ -277,12 +277,12 @@ NQ_D double sr_diag_shift(const double* S, int P, int i, int kind, double eps, d
 // estimated relative error after it]
 constexpr int kRefineMaxCtas = 256;
 constexpr double kRefineTol = 1e-13;
-// shared memory of a refinement CTA: the GEMV vector (P complex doubles) when
-// it fits the default 48 KiB, else none (the vector is read from L2)
-constexpr size_t kRefineStageMax = 48 * 1024;
-constexpr size_t refine_stage_bytes(int P) {
-  return (size_t)16 * P <= kRefineStageMax ? (size_t)16 * P : (P > 0 ? kRefineStageMax : 0);
-}
+// dynamic shared memory of a refinement CTA: the GEMV vector (P complex
+// doubles) when it fits 40 KiB (under the 48 KiB default with the kernel's
+// static shared memory), else none and the vector is read from L2; the kernel
+// stages a problem's vector only when it fits the launch's allocation
+constexpr size_t kRefineStageMax = 40 * 1024;
+constexpr size_t refine_stage_bytes(int P) { return (size_t)16 * P <= kRefineStageMax ? (size_t)16 * P : 0; }
 constexpr size_t refine_norm_doubles() { return 2 * (size_t)kRefineMaxCtas * 8; }
 cudaError_t launch_refine_coop(const float2* W, const double* S, int P, const double* F, int kind, double eps,
                                double lam, bool real_params, int max_corr, double tol, double* x, double* r,

@@ -451,7 +451,9 @@ NQ_D void refine_group_body(const float2* __restrict__ W, const double* __restri
   const int gw = wib * nranks + rank, nw = nranks * (blockDim.x >> 5);
   __shared__ double s_red[2][8];
   extern __shared__ __align__(16) unsigned char s_vec[];
-  const bool stage = (size_t)16 * P <= kRefineStageMax;
+  unsigned dyn_smem;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_smem));
+  const bool stage = (size_t)16 * P <= dyn_smem;
   float2* const s_rf = reinterpret_cast<float2*>(s_vec);
   double2* const s_x = reinterpret_cast<double2*>(s_vec);
   for (int i = rank * blockDim.x + threadIdx.x; i < P; i += nranks * blockDim.x)
@@ -743,7 +745,8 @@ cudaError_t launch_refine_group(const SrGroup& g, const int* cta_start, int tota
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(total_ctas);
   cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = refine_stage_bytes(g.P_max);
+  // up to 40 KiB: the problems whose vector fits stage it
+  cfg.dynamicSmemBytes = std::min((size_t)16 * g.P_max, kRefineStageMax);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

@@ -248,3 +248,23 @@ def test_sr_algorithms_and_reference_multiplicative_quirk(nqlib):
                 # the engine's own S and F, solved in FP64 by the oracle: the solve's own error
                 dwo = osr.precondition(S, force, 0.01, kind=okind, it=3, algorithm=oalg)
                 assert rel(dw, dwo) < 1e-9, (quirks, alg, okind)
+
+
+@pytest.mark.parametrize("alpha", [1, 2])
+def test_solve_at_large_P(nqlib, alpha):
+    """The direct solve at P = 36 + 36 alpha + 36^2 alpha (1368 and 2700):
+    the refinement stages its vectors in shared memory up to P = 2560 and
+    reads them from L2 beyond; either way Δw matches the FP64 solve of the
+    engine's own S and F to 1e-9."""
+    N, B, L = 36, 256, 4
+    is_, net, onet, oH, ohilb = make(N=N, alpha=alpha, B=B, L=L, burn=4, sigma=0.02 ** 2)
+    eng = is_.engine
+    assert eng.P == N + alpha * N + alpha * N * N
+    eng.sample(2, want_samples=False)
+    _, _, F = eng.estimate(want_force=True)
+    S = eng.sr_matrix()
+    dw = eng.precondition(0, 0.01)
+    x = np.linalg.solve(S + 0.01 * np.eye(S.shape[0]), F)
+    assert rel(dw, x) < 1e-9
+    corr, bound = eng.sr_info()
+    assert 1 <= corr <= 12 and bound <= 1e-13
