@@ -115,8 +115,18 @@ def build_sampler(s_precision=None):
     smp = nq.MetropolisSampler(nq.LocalRule(), w["chain_length"], w["passes"], burn=w["burn"],
                                seed=w["seed"])
     sp = nq._lib.NQ_S_TF32 if s_precision is None else s_precision
-    is_ = nq.BatchedSampler(net, smp, H, nq.SR(eps=w["eps"]), batch_sz=w["chains"], s_precision=sp)
+    is_ = nq.BatchedSampler(net, smp, H, nq.SR(eps=w["eps"]), batch_sz=w["chains"], s_precision=sp,
+                            eval_precision=eval_precision_choice())
     return nq, net, is_
+
+
+def eval_precision_choice():
+    """Evaluation precision of the bench workload: FP32 on CUDA cores unless
+    NQ_BENCH_EVAL_PRECISION names another nq_eval_precision (for example
+    NQ_EVAL_TC_BF16X2, θ on tcgen05, for a profile of that kernel)."""
+    import nqcuda as nq
+    env = os.environ.get("NQ_BENCH_EVAL_PRECISION")
+    return getattr(nq._lib, env) if env else nq._lib.NQ_EVAL_F32
 
 
 def s_precision_choice():
@@ -267,7 +277,9 @@ def run_gb300(args, barrier=None):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (random-init RBM weights, Philox-seeded chains)",
-        "config": workload_config({"s_precision": int(sp)}),
+        "config": workload_config(),
+        "precision": {"s": int(sp), "eval": int(eval_precision_choice()),
+                      "note": "nq_s_precision / nq_eval_precision of the timed step (1 = TF32 S, 0 = FP32 evaluation)"},
         "clocks": clk.summary(), "e2e": e2e, "gpu_launches": int(launches),
         "effective_samples_per_s": ess, "tau_int_eloc": tau, "energy_per_site": m.mean_re / w["N"],
         "stage_ms": stages, "kernel_ms": kernels,
