@@ -319,14 +319,26 @@ nq_status stage_force(nq_handle* h) {
                         tc ? 1 : 0, h->st));
     return NQ_OK;
   }
+  // the statistics of E_loc feed only the step's measurement: inside the
+  // captured step they run on the side branch, joined at its end
+  const bool side = h->capturing && h->side_ok && h->st_side;
+  cudaStream_t sst = side ? h->st_side : h->st;
+  if (side) {
+    CK(cudaEventRecord(h->ev_fork, h->st));
+    CK(cudaStreamWaitEvent(h->st_side, h->ev_fork, 0));
+  }
   if (h->f64) {
+    CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, sst));
     CKL(launch_rbm_force<double>(rbm_dev<double>(h), h->d_samples, h->Ns, (cpx<double>*)h->d_g,
                                  (cpx<double>*)h->d_eloc, h->fb, h->st));
-    CKL(launch_stats<double>((cpx<double>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
   } else {
+    CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, sst));
     CKL(launch_rbm_force<float>(rbm_dev<float>(h), h->d_samples, h->Ns, (cpx<float>*)h->d_g,
                                 (cpx<float>*)h->d_eloc, h->fb, h->st));
-    CKL(launch_stats<float>((cpx<float>*)h->d_eloc, h->B, h->L, 0, h->d_chainstats, h->d_stats, h->st));
+  }
+  if (side) {
+    CK(cudaEventRecord(h->ev_join, h->st_side));
+    h->side_pending = true;
   }
   return NQ_OK;
 }
@@ -739,6 +751,9 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
     }
   };
   step(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking), "stream");
+  step(cudaStreamCreateWithFlags(&h->st_side, cudaStreamNonBlocking), "side stream");
+  step(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming), "fork event");
+  step(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming), "join event");
   const size_t csz = h->f64 ? sizeof(cpx<double>) : sizeof(cpx<float>);
   const int P = h->P;
   step(dalloc(&h->d_master, 2 * (size_t)P), "params");
@@ -927,6 +942,9 @@ void nq_destroy(nq_handle* h) {
   for (int k = 0; k < 6; ++k)
     if (h->sev[k]) cudaEventDestroy(h->sev[k]);
   if (h->d_flush) cudaFree(h->d_flush);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->st_side) cudaStreamDestroy(h->st_side);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -1602,6 +1620,7 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     h->capturing = true;
+    h->side_ok = true;
     const int64_t before = h->launches;
     nq_status s = NQ_OK;
     cudaError_t ce = cudaMemcpyAsync(h->d_call, h->h_call, sizeof(uint32_t), cudaMemcpyHostToDevice, h->st);
@@ -1612,6 +1631,12 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
     if (s == NQ_OK) s = stage_S(h);
     if (s == NQ_OK) s = stage_solve(h, 0, eps, 0.0);
     if (s == NQ_OK) s = stage_update(h, lr);
+    if (h->side_pending) {           // join the side branch before the capture ends
+      cudaError_t je = cudaStreamWaitEvent(h->st, h->ev_join, 0);
+      if (je != cudaSuccess && s == NQ_OK) s = fail(h, NQ_ERR_CUDA, "capture join: %s", cudaGetErrorString(je));
+      h->side_pending = false;
+    }
+    h->side_ok = false;
     cudaError_t e = cudaStreamEndCapture(h->st, &g);
     h->capturing = false;
     h->graph_kernels = h->launches - before;

@@ -49,6 +49,11 @@ struct nq_handle {
   double* d_ndm_partial = nullptr; // [nblk][2P]
   int hilb = 0, act = 0;
   cudaStream_t st = nullptr;
+  // side branch of the captured step: the ket path's measurement statistics
+  // run beside the force, S and solve stages (they are read only at the end)
+  cudaStream_t st_side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool side_ok = false, side_pending = false;     // side_ok: set by nq_vmc_step's capture only
   std::string err;
   int64_t launches = 0;
 
