@@ -198,6 +198,9 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
     // few ranks everything is dealt round-robin
     const bool split = nranks > ncol;
     const int nunits = ncol + nlight;
+    // a CTA with several column units in this phase forms and inverts the
+    // pivot tile once: Dt keeps the inverse for its later units
+    bool piv_ready = false;
     for (int u0 = split ? (rank < ncol ? rank : ncol + (rank - ncol)) : rank; u0 < nunits;
          u0 += split ? (rank < ncol ? nunits : nranks - ncol) : nranks) {
       const int u = u0;
@@ -219,7 +222,7 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
 #pragma unroll
         for (int q = 0; q < CB * CB / 256; ++q) {
           const int e = q * 256 + threadIdx.x, r = e & 31, c = e >> 5;
-          ld[0][q] = herm_block_elem(W, P, kn, kn, r, c);
+          ld[0][q] = piv_ready ? z2 : herm_block_elem(W, P, kn, kn, r, c);
           ld[1][q] = k >= 0 ? __ldcg(Cc + (size_t)kn * tile + e) : z2;
           ld[2][q] = k >= 0 ? __ldcg(Gc + (size_t)kn * tile + e) : z2;
           const int gi = sa * CB + r, gj = sb * CB + c;
@@ -232,7 +235,7 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
 #pragma unroll
         for (int q = 0; q < CB * CB / 256; ++q) {
           const int e = q * 256 + threadIdx.x, r = e & 31, c = e >> 5;
-          Dt[r][c] = ld[0][q];
+          if (!piv_ready) Dt[r][c] = ld[0][q];
           if (k >= 0) {
             Ut[r][c] = ld[1][q];
             Vt[r][c] = ld[2][q];
@@ -243,7 +246,7 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
           }
         }
         __syncthreads();
-        if (k >= 0) {
+        if (k >= 0 && !piv_ready) {
           // updated pivot tile W_kn,kn - C_kn G_knᴴ on the stored lower triangle
           // (the lower part of Dt holds the stored values; the diagonal is
           // real), then mirrored
@@ -263,7 +266,21 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
           __syncthreads();
         }
         bool ok = true;
-        if (threadIdx.x < 128) {
+        if (piv_ready) {
+          if (v_update) {
+            // the pivot is inverted already: V on all 8 warps
+            float2 o[4];
+            tile_mm<1>(i > kn ? Yt : Ut, i > kn ? Vt : Yt, o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int c = cg + q;
+              if (sa * CB + tr < P && sb * CB + c < P) {
+                Xt[tr][c].x -= o[q].x;
+                Xt[tr][c].y -= o[q].y;
+              }
+            }
+          }
+        } else if (threadIdx.x < 128) {
           ok = hpd_inverse_32_w4(Dt, colbuf);
         } else if (v_update) {
           // V = stored (sa, sb) - C_sa G_sbᴴ (the rank-32 update of that tile)
@@ -279,6 +296,7 @@ NQ_D void sweep_group(float2* __restrict__ W, int P, SweepCtl* ctl, int* status,
           }
         }
         __syncthreads();
+        piv_ready = true;
         if (u == 0) {
           if (!ok && threadIdx.x == 0) atomicOr(status, 1);
           for (int e = threadIdx.x; e < CB * CB; e += blockDim.x) pn[e] = Dt[e & 31][e >> 5];
