@@ -1731,7 +1731,8 @@ struct nq_batch {
   int* d_sblk = nullptr;                // [np+1] sampler block starts
   int* d_eblk = nullptr;                // [np+1] estimator block starts
   int* d_wcta = nullptr;                // [np+1] inversion CTA starts
-  int s_blocks = 0, e_blocks = 0, w_ctas = 0, M_max = 0, N_max = 0, act = 0;
+  int* d_rcta = nullptr;                // [np+1] refinement CTA starts
+  int s_blocks = 0, e_blocks = 0, w_ctas = 0, r_ctas = 0, M_max = 0, N_max = 0, act = 0;
   int lanes = 0, eval_T = 0;
   void* d_ctl = nullptr;                // per-problem barrier blocks, 64 B each
   unsigned long long* d_acc = nullptr;  // [np] accepted-move counters
@@ -1801,6 +1802,26 @@ void split_ctas(const std::vector<int>& P, int total, std::vector<int>& start) {
     const int nb = (P[p] + 31) / 32;
     int extra = (int)std::floor(spare * w[p] / sum);
     extra = std::min(extra, std::max(0, nb - 1));
+    start[p + 1] = start[p] + 1 + extra;
+  }
+}
+
+// CTAs of the grouped refinement: its passes are GEMVs (the FP64 residual on
+// GB300's few FP64 units dominates), so the split follows P², with at least
+// 8 rows (one per warp) per CTA
+void split_ctas_refine(const std::vector<int>& P, int total, std::vector<int>& start) {
+  const int np = (int)P.size();
+  std::vector<double> w(np);
+  double sum = 0;
+  for (int p = 0; p < np; ++p) {
+    w[p] = (double)P[p] * P[p];
+    sum += w[p];
+  }
+  const int spare = std::max(0, total - np);
+  start.assign(np + 1, 0);
+  for (int p = 0; p < np; ++p) {
+    int extra = (int)std::floor(spare * w[p] / sum);
+    extra = std::min(extra, std::max(0, P[p] / 8 - 1));
     start[p + 1] = start[p] + 1 + extra;
   }
 }
@@ -1978,12 +1999,16 @@ nq_status batch_build_tables(nq_batch* b) {
   b->s_blocks = sblk[np];
   b->e_blocks = eblk[np];
   b->w_ctas = wcta[np];
+  std::vector<int> rcta;
+  split_ctas_refine(Ps, slots, rcta);
+  b->r_ctas = rcta[np];
   BCK(cudaMemcpy(b->d_sjobs, sj.data(), np * sizeof(SamplerJob<float>), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_ejobs, ej.data(), np * sizeof(EvalJob<float>), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_wjobs, wj.data(), np * sizeof(SweepJob), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_sblk, sblk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_eblk, eblk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_wcta, wcta.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_rcta, rcta.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_stat_src, sp.data(), np * sizeof(double*), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_status_src, stp.data(), np * sizeof(int*), cudaMemcpyHostToDevice));
   return NQ_OK;
@@ -2065,7 +2090,7 @@ nq_status batch_capture(nq_batch* b, double eps, double lr) {
     ck(launch_spd_inverse_batch(b->d_wjobs, b->d_wcta, np, b->w_ctas, b->d_ctl, (size_t)np * 64, b->st),
        "batched inversion");
     ck(launch_fill_group(gp, b->st), "grouped fill");
-    ck(launch_refine_group(gp, b->d_wcta, b->w_ctas, b->d_ctl, eps, kSolveRefine, b->st), "grouped refinement");
+    ck(launch_refine_group(gp, b->d_rcta, b->r_ctas, b->d_ctl, eps, kSolveRefine, b->st), "grouped refinement");
     ck(launch_update_group(gp, lr, b->st), "grouped update");
     b->launches += 14;
   } else {
@@ -2167,6 +2192,7 @@ nq_status nq_batch_create(const nq_config* cfgs, int32_t n, nq_batch** out) {
                   cudaMalloc((void**)&b->d_sblk, (n + 1) * sizeof(int)) == cudaSuccess &&
                   cudaMalloc((void**)&b->d_eblk, (n + 1) * sizeof(int)) == cudaSuccess &&
                   cudaMalloc((void**)&b->d_wcta, (n + 1) * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc((void**)&b->d_rcta, (n + 1) * sizeof(int)) == cudaSuccess &&
                   cudaMalloc(&b->d_ctl, (size_t)n * 64) == cudaSuccess &&
                   cudaMalloc((void**)&b->d_acc, n * sizeof(unsigned long long)) == cudaSuccess &&
                   cudaMalloc((void**)&b->d_stat_src, n * sizeof(double*)) == cudaSuccess &&
@@ -2183,7 +2209,7 @@ void nq_batch_destroy(nq_batch* b) {
   if (b->st) cudaStreamSynchronize(b->st);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (nq_handle* h : b->hs) nq_destroy(h);
-  void* bufs[] = {b->d_call, b->d_sjobs, b->d_ejobs, b->d_wjobs, b->d_sblk, b->d_eblk, b->d_wcta, b->d_ctl,
+  void* bufs[] = {b->d_call, b->d_sjobs, b->d_ejobs, b->d_wjobs, b->d_sblk, b->d_eblk, b->d_wcta, b->d_rcta, b->d_ctl,
                   b->d_acc, b->d_stat_src, b->d_status_src, b->d_gather, b->d_Xall, b->d_Xlo_all, b->d_slots,
                   b->d_geom, b->d_jobs, b->d_prefix};
   for (void* p : bufs)
