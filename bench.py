@@ -475,6 +475,27 @@ def batched_vs_sequential():
             "speedup_vs_sequential_device": dev_ms / ms_bat}
 
 
+def cg_step():
+    """The matrix-free CG SR step (tolerance 1e-4) on the 6x6 TFIM workload
+    of the learned-proposal comparison, from its random start: device ms per
+    step over 5 timed steps after 3 + 10 warm-up steps, CG iterations."""
+    import nqcuda as nq
+    c = LEARNED
+    N = c["L"] * c["L"]
+    hilb, H = _tfim2d(nq, c["L"], c["h"], c["J"])
+    net = nq.RBM(np.complex64, N, c["alpha"], nq.af_logcosh)
+    nq.init_random_pars_(net, sigma=0.01, rng=np.random.default_rng(c["seed"]))
+    smp = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], N, burn=c["burn"], seed=c["seed"])
+    eng = nq.BatchedSampler(net, smp, H, nq.SR(eps=c["eps"], algorithm=nq.sr_cg, precision=1e-4),
+                            batch_sz=c["chains"], s_precision=nq._lib.NQ_S_TF32).engine
+    for i in range(3):
+        eng.vmc_step(i, c["eps"], c["lr"])
+    ms = float(np.mean(eng.bench_steps(10, 5, c["eps"], c["lr"], 0)))
+    it, res = eng.sr_info()
+    return {"workload": "tfim2d_6x6_h3.04_rbm_alpha4_8192_chains matrix-free CG", "ms_per_step": ms,
+            "cg_iterations": it, "relative_residual": res}
+
+
 def learned_vs_local():
     """SR on the 6x6 TFIM (h = 3.04) with the MADE proposal trained online on
     the chains' samples every 10 SR steps, then effective samples/s of local
@@ -659,11 +680,16 @@ def main():
                     help="skip the learned-proposal vs local Metropolis comparison (6x6 TFIM)")
     ap.add_argument("--batch-only", action="store_true",
                     help="time only the batched step of the 64-problem workload (for launch lists)")
+    ap.add_argument("--cg-only", action="store_true",
+                    help="time only the matrix-free CG SR step of the 6x6 TFIM workload (for profiles)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.cg_only:
+        print(json.dumps(cg_step()))
+        return
     if args.batch_only:
         import nqcuda as nq
         _, probs = _batch_problems(nq)

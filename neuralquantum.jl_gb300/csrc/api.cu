@@ -674,7 +674,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
     return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM's doubled space) <= 26");
   if (c.sr_algorithm == NQ_SR_CG &&
       (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64 ||
-       !sr_cg_supported(c.n_sites + c.n_hidden + c.n_sites * c.n_hidden))) {
+       !sr_cg_supported(c.n_sites, c.n_hidden))) {
     delete h;
     return NQ_ERR_UNSUPPORTED;
   }

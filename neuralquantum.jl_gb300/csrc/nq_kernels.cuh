@@ -332,7 +332,7 @@ struct SrCgArgs {
 };
 int sr_cg_grid();
 size_t sr_cg_ctl_bytes();
-bool sr_cg_supported(int P);
+bool sr_cg_supported(int N, int M);   // the CG kernel's shared memory fits
 cudaError_t launch_sr_cg(const SrCgArgs& args, int kind, double lam, cudaStream_t st);
 
 // y = -W x for the full Hermitian W

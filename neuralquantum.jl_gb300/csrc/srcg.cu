@@ -19,8 +19,18 @@
 namespace {
 
 constexpr int THREADS = 256;
-constexpr int EMAX = 24;          // parameters per thread in the adjoint: P <= 6144
 constexpr int TS = 32;            // samples per shared-memory tile of the adjoint
+constexpr int TSP = TS + 1;       // row stride of the z tile (odd: fewer bank conflicts)
+constexpr int FH = 8;             // forward: hidden units per register chunk
+constexpr int AH = 4, AJ = 8;     // adjoint: register tile of hidden units x sites
+
+NQ_D int pad8(int n) { return (n + 7) & ~7; }
+// dynamic shared memory of the CG kernel (bytes)
+NQ_HD size_t cg_smem_bytes(int N, int M) {
+  const size_t P = (size_t)N + M + (size_t)N * M;
+  return 2 * P * sizeof(float2) + (size_t)M * TSP * sizeof(float2) + (size_t)TS * (((N + 7) & ~7)) * sizeof(float) +
+         TS * sizeof(float2) + TS * sizeof(uint64_t) + 16;
+}
 
 struct CgCtl {
   unsigned count, gen;
@@ -52,9 +62,13 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CgCtl* ctl = reinterpret_cast<CgCtl*>(a.ctl);
   const int N = a.N, M = a.M, P = a.P, Ns = a.Ns, hilb = a.hilb;
+  const int NP8 = pad8(N);
   float2* s_v = reinterpret_cast<float2*>(smem_raw);                 // [P] direction, FP32
-  float2* s_g = s_v + P;                                              // [M][TS] g tile
-  float2* s_t = s_g + (size_t)M * TS;                                 // [TS]
+  float2* s_acc = s_v + P;                                            // [P] this CTA's adjoint sums
+  float2* s_z = s_acc + P;                                            // [M][TSP] conj(g) t of a tile
+  float* s_sig = reinterpret_cast<float*>(
+      (reinterpret_cast<uintptr_t>(s_z + (size_t)M * TSP) + 15) & ~(uintptr_t)15);   // [TS][NP8] σ of a tile
+  float2* s_t = reinterpret_cast<float2*>(s_sig + (size_t)TS * NP8); // [TS]
   uint64_t* s_bits = reinterpret_cast<uint64_t*>(s_t + TS);          // [TS]
   __shared__ double s_c[2];
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
@@ -107,6 +121,8 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     }
     __syncthreads();
     const float cx = (float)s_c[0], cy = (float)s_c[1];
+    // one thread per sample; the hidden units in register chunks of FH, so a
+    // site value serves FH units: u_h = v_b,h + Σ_j v_W,hj σ_j, t += g_h u_h
     for (int s = b * THREADS + tid; s < Ns; s += G * THREADS) {
       const uint64_t bits = a.samples[s];
       float tx = -cx, ty = -cy;
@@ -115,78 +131,112 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
         tx += s_v[j].x * sv;
         ty += s_v[j].y * sv;
       }
-      for (int h = 0; h < M; ++h) {
-        float zx = s_v[N + h].x, zy = s_v[N + h].y;
-        const float2* vw = s_v + N + M + h;
+      for (int h0 = 0; h0 < M; h0 += FH) {
+        float2 z[FH];
+#pragma unroll
+        for (int u = 0; u < FH; ++u) z[u] = h0 + u < M ? s_v[N + h0 + u] : make_float2(0.f, 0.f);
         for (int j = 0; j < N; ++j) {
           const float sv = site_valuef(bits, j, hilb);
-          zx += vw[(size_t)M * j].x * sv;
-          zy += vw[(size_t)M * j].y * sv;
+          const float2* vw = s_v + N + M + (size_t)M * j + h0;
+#pragma unroll
+          for (int u = 0; u < FH; ++u)
+            if (h0 + u < M) {
+              z[u].x += vw[u].x * sv;
+              z[u].y += vw[u].y * sv;
+            }
         }
-        const float2 gh = a.g[(size_t)h * Ns + s];
-        tx += gh.x * zx - gh.y * zy;
-        ty += gh.x * zy + gh.y * zx;
+#pragma unroll
+        for (int u = 0; u < FH; ++u)
+          if (h0 + u < M) {
+            const float2 gh = a.g[(size_t)(h0 + u) * Ns + s];
+            tx += gh.x * z[u].x - gh.y * z[u].y;
+            ty += gh.x * z[u].y + gh.y * z[u].x;
+          }
       }
       a.t[s] = make_float2(tx, ty);
     }
     if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     // ---- adjoint partials over this CTA's sample chunk ----
-    double2 acc[EMAX];
-#pragma unroll
-    for (int e = 0; e < EMAX; ++e) acc[e] = make_double2(0.0, 0.0);
+    // y_a,j = Σ_s σ_sj t_s, y_b,h = Σ_s z_sh, y_W,hj = Σ_s σ_sj z_sh with
+    // z_sh = conj(g_sh) t_s: per tile of TS samples, z and σ are staged in
+    // shared memory and the W block is a register-tiled (AH x AJ) contraction
+    // over the tile; FP32 sums per tile, added into this CTA's FP32 totals.
+    for (int p = tid; p < P; p += THREADS) s_acc[p] = make_float2(0.f, 0.f);
+    const int HT = (M + AH - 1) / AH, JT = (N + AJ - 1) / AJ, ntile = HT * JT;
     float tsx = 0.f, tsy = 0.f;
     for (int c0 = s0; c0 < s1; c0 += TS) {
       const int nt = min(TS, s1 - c0);
       __syncthreads();
-      for (int e = tid; e < M * TS; e += THREADS) {
-        const int h = e / TS, q = e % TS;
-        s_g[e] = q < nt ? a.g[(size_t)h * Ns + c0 + q] : make_float2(0.f, 0.f);
-      }
       for (int q = tid; q < TS; q += THREADS) {
         s_t[q] = q < nt ? __ldcg(reinterpret_cast<const float2*>(a.t) + c0 + q) : make_float2(0.f, 0.f);
         s_bits[q] = q < nt ? a.samples[c0 + q] : 0ull;
       }
       __syncthreads();
+      for (int e = tid; e < TS * NP8; e += THREADS) {
+        const int q = e / NP8, j = e % NP8;
+        s_sig[e] = (q < nt && j < N) ? site_valuef(s_bits[q], j, hilb) : 0.f;
+      }
+      for (int e = tid; e < M * TS; e += THREADS) {
+        const int h = e / TS, q = e % TS;
+        const float2 gv = q < nt ? a.g[(size_t)h * Ns + c0 + q] : make_float2(0.f, 0.f);
+        const float2 tv = s_t[q];
+        s_z[h * TSP + q] = make_float2(gv.x * tv.x + gv.y * tv.y, gv.x * tv.y - gv.y * tv.x);
+      }
       if (tid == 0)
         for (int q = 0; q < nt; ++q) { tsx += s_t[q].x; tsy += s_t[q].y; }
-#pragma unroll
-      for (int e = 0; e < EMAX; ++e) {
-        const int p = tid + e * THREADS;
-        if (p < P) {
-          float ax = 0.f, ay = 0.f;
-          if (p < N) {
-            for (int q = 0; q < nt; ++q) {
-              const float sv = site_valuef(s_bits[q], p, hilb);
-              ax += sv * s_t[q].x;
-              ay += sv * s_t[q].y;
-            }
-          } else if (p < N + M) {
-            const float2* gr = s_g + (size_t)(p - N) * TS;
-            for (int q = 0; q < nt; ++q) {      // conj(g) t
-              ax += gr[q].x * s_t[q].x + gr[q].y * s_t[q].y;
-              ay += gr[q].x * s_t[q].y - gr[q].y * s_t[q].x;
-            }
-          } else {
-            const int k = p - N - M, h = k % M, j = k / M;
-            const float2* gr = s_g + (size_t)h * TS;
-            for (int q = 0; q < nt; ++q) {
-              const float sv = site_valuef(s_bits[q], j, hilb);
-              ax += sv * (gr[q].x * s_t[q].x + gr[q].y * s_t[q].y);
-              ay += sv * (gr[q].x * s_t[q].y - gr[q].y * s_t[q].x);
-            }
+      __syncthreads();
+      for (int p = tid; p < N + M; p += THREADS) {
+        float ax = 0.f, ay = 0.f;
+        if (p < N) {
+          for (int q = 0; q < nt; ++q) {
+            const float sv = s_sig[q * NP8 + p];
+            ax += sv * s_t[q].x;
+            ay += sv * s_t[q].y;
           }
-          acc[e].x += ax;
-          acc[e].y += ay;
+        } else {
+          const float2* zr = s_z + (size_t)(p - N) * TSP;
+          for (int q = 0; q < nt; ++q) { ax += zr[q].x; ay += zr[q].y; }
         }
+        s_acc[p].x += ax;
+        s_acc[p].y += ay;
+      }
+      for (int T = tid; T < ntile; T += THREADS) {
+        const int j0 = AJ * (T % JT), h0 = AH * (T / JT);
+        float2 acc[AH][AJ];
+#pragma unroll
+        for (int u = 0; u < AH; ++u)
+#pragma unroll
+          for (int v = 0; v < AJ; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        for (int q = 0; q < nt; ++q) {
+          float2 z[AH];
+#pragma unroll
+          for (int u = 0; u < AH; ++u) z[u] = h0 + u < M ? s_z[(h0 + u) * TSP + q] : make_float2(0.f, 0.f);
+          const float4 sa = *reinterpret_cast<const float4*>(s_sig + q * NP8 + j0);
+          const float4 sb = *reinterpret_cast<const float4*>(s_sig + q * NP8 + j0 + 4);
+          const float sg[AJ] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+#pragma unroll
+          for (int u = 0; u < AH; ++u)
+#pragma unroll
+            for (int v = 0; v < AJ; ++v) {
+              acc[u][v].x += z[u].x * sg[v];
+              acc[u][v].y += z[u].y * sg[v];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < AH; ++u)
+#pragma unroll
+          for (int v = 0; v < AJ; ++v)
+            if (h0 + u < M && j0 + v < N) {
+              float2& d = s_acc[N + M + (h0 + u) + (size_t)M * (j0 + v)];
+              d.x += acc[u][v].x;
+              d.y += acc[u][v].y;
+            }
       }
     }
-#pragma unroll
-    for (int e = 0; e < EMAX; ++e) {
-      const int p = tid + e * THREADS;
-      if (p < P) {
-        a.part[((size_t)b * P + p) * 2] = acc[e].x;
-        a.part[((size_t)b * P + p) * 2 + 1] = acc[e].y;
-      }
+    __syncthreads();
+    for (int p = tid; p < P; p += THREADS) {
+      a.part[((size_t)b * P + p) * 2] = (double)s_acc[p].x;
+      a.part[((size_t)b * P + p) * 2 + 1] = (double)s_acc[p].y;
     }
     if (tid == 0) { a.tsum[2 * b] = tsx; a.tsum[2 * b + 1] = tsy; }
     if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
@@ -298,17 +348,16 @@ int sr_cg_grid() {
 }
 
 size_t sr_cg_ctl_bytes() { return sizeof(CgCtl); }
-bool sr_cg_supported(int P) { return P <= EMAX * THREADS; }
+bool sr_cg_supported(int N, int M) { return cg_smem_bytes(N, M) <= 220 * 1024; }
 
 cudaError_t launch_sr_cg(const SrCgArgs& args, int kind, double lam, cudaStream_t st) {
-  if (!sr_cg_supported(args.P)) return cudaErrorInvalidValue;
+  if (!sr_cg_supported(args.N, args.M)) return cudaErrorInvalidValue;
   sr_diag_kernel<<<(args.P + 255) / 256, 256, 0, st>>>(args, lam, kind);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(args.ctl, 0, sizeof(CgCtl), st);
   if (e != cudaSuccess) return e;
-  const size_t smem = (size_t)args.P * sizeof(float2) + (size_t)args.M * TS * sizeof(float2) + TS * sizeof(float2) +
-                      TS * sizeof(uint64_t);
+  const size_t smem = cg_smem_bytes(args.N, args.M);
   e = cudaFuncSetAttribute(sr_cg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
