@@ -416,10 +416,16 @@ nq_status stage_update(nq_handle* h, double lr) {
   return refresh_params(h);
 }
 
-nq_status check_status_word(nq_handle* h) {
+// st_read: the status word already copied to the host after the last
+// synchronisation (nq_vmc_step reads it with the measurement), else null
+nq_status check_status_word(nq_handle* h, const int* st_read = nullptr) {
   int st = 0;
-  CK(cudaMemcpyAsync(&st, h->sb.status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
+  if (st_read) {
+    st = *st_read;
+  } else {
+    CK(cudaMemcpyAsync(&st, h->sb.status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
   if (st != 0) {
     CK(cudaMemsetAsync(h->sb.status, 0, sizeof(int), h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -874,6 +880,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   step(cudaMallocHost((void**)&h->h_call, sizeof(uint32_t)), "pinned");
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
   step(cudaMallocHost((void**)&h->h_acc, sizeof(unsigned long long)), "pinned");
+  step(cudaMallocHost((void**)&h->h_status, sizeof(int)), "pinned");
   for (int k = 0; k < 7; ++k) step(cudaEventCreate(&h->ev[k]), "event");
   for (int k = 0; k < 4; ++k) step(cudaEventCreate(&h->kev[k]), "event");
   for (int k = 0; k < 6; ++k) step(cudaEventCreate(&h->sev[k]), "event");
@@ -934,6 +941,7 @@ void nq_destroy(nq_handle* h) {
   }
   if (h->h_call) cudaFreeHost(h->h_call);
   if (h->h_stats) cudaFreeHost(h->h_stats);
+  if (h->h_status) cudaFreeHost(h->h_status);
   if (h->h_acc) cudaFreeHost(h->h_acc);
   for (int k = 0; k < 7; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);
@@ -977,11 +985,10 @@ nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype
   }
   for (double v : buf)
     if (!std::isfinite(v)) return fail(h, NQ_ERR_NAN, "non-finite parameter");
+  // the copy from pageable memory has left buf when it returns; the refresh
+  // kernels stay queued on the handle's stream ahead of its next call
   CK(cudaMemcpyAsync(h->d_master, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  nq_status s = refresh_params(h);
-  if (s != NQ_OK) return s;
-  CK(cudaStreamSynchronize(h->st));
-  return NQ_OK;
+  return refresh_params(h);
 }
 
 nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
@@ -1609,11 +1616,13 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
   NQ_REJECT_DIAG(h, "nq_vmc_step");
   if (h->symm && !h->sym_ready) return fail(h, NQ_ERR_STATE, "NDMSymm: no permutations (nq_set_symmetry)");
   if (!h->has_op) return fail(h, NQ_ERR_STATE, "no operator set (nq_set_operator)");
+  // every graph launch of this handle ends with a synchronisation, so no
+  // graph is in flight here and the pinned call word is free; work queued by
+  // asynchronous calls (nq_set_params) runs ahead of the graph on the stream
   if (h->graph && (h->graph_eps != eps || h->graph_lr != lr)) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
-  CK(cudaStreamSynchronize(h->st));
   if (nq_status ts = ensure_tuned(h)) return ts;
   *h->h_call = (uint32_t)call_index;
   if (!h->graph) {
@@ -1652,8 +1661,9 @@ nq_status nq_vmc_step(nq_handle* h, uint64_t call_index, double eps, double lr, 
   h->launches += h->graph_kernels;
   CK(cudaMemcpyAsync(h->h_stats, h->d_stats, 6 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->h_acc, h->d_accepted, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_status, h->sb.status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  nq_status s = check_status_word(h);
+  nq_status s = check_status_word(h, h->h_status);
   fill_measurement(h, stats);
   if (s != NQ_OK) return s;
   if (!std::isfinite(h->h_stats[0]) || !std::isfinite(h->h_stats[1]))

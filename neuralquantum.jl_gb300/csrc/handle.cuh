@@ -51,6 +51,7 @@ struct nq_handle {
   cudaStream_t st = nullptr;
   // side branch of the captured step: the ket path's measurement statistics
   // run beside the force, S and solve stages (they are read only at the end)
+  int* h_status = nullptr;           // pinned copy of the device status word (nq_vmc_step)
   cudaStream_t st_side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side_ok = false, side_pending = false;     // side_ok: set by nq_vmc_step's capture only
