@@ -2,7 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product (the ``nqcuda`` host package
 or ``libnqcuda``) imports this package; only ``tests/``, the smoke entry point
-and the CPU-baseline leg of ``bench.py`` use it, and only as the checker.
+and the CPU-baseline and reference legs of ``bench.py`` use it, to check and
+to time the GPU path, never as part of it.
 
 Each module restates one part of the reference algorithm in plain numpy
 (float64 / complex128) and cites the reference file:line it follows:
@@ -25,10 +26,12 @@ Each module restates one part of the reference algorithm in plain numpy
 * ``stats``       -- ``Measurement`` statistics (src/utils/stats.jl).
 * ``exact``       -- exact enumeration helpers for small systems.
 
-Parity pinning: the reference is Julia and cannot be executed in this build
-environment (no Julia runtime), and it stores no golden numeric vectors.  The
-oracle is pinned instead to the reference's own known answers and test
-properties: the exact ground-state energy quoted in examples/ising1d.jl:46-47,
+Parity pinning: the reference is Julia and cannot be executed here (no Julia
+runtime), and it stores no golden numeric vectors.  The oracle is pinned
+instead to the reference's own known answers and test properties: the exact
+ground-state energies quoted in examples/ising1d.jl:46-47 and
+examples/ising2d.jl:55 (the 5 x 5 lattice, by the Lanczos recurrence of
+lanczos.c),
 the operator/Liouvillian matrix conventions of test/Operators/ising.jl:28-42
 (rebuilt here from independent Kronecker products), hand-written gradients
 against numerical differentiation (test/Machines/test_grad.jl:108-138), and
