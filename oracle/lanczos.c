@@ -2,8 +2,9 @@
  * Matrix-free Lanczos recurrence for the ground energy of the transverse-field
  * Ising model on an Lx x Ly periodic square lattice (test infrastructure:
  * it pins the oracle's 2D Hamiltonian convention to the exact energy quoted by
- * the reference, examples/ising2d.jl:55, for the 5 x 5 lattice at h = 3,
- * J = 1).  Never linked into libnqcuda.
+ * the reference, examples/ising2d.jl:55, for the 5 x 5 lattice at h = 3; the
+ * quoted value is the ferromagnetic coupling's, J = -1 here).  Never linked
+ * into libnqcuda.
  *
  * H = -h Σ_p σx_p + J Σ_p (σz_p σz_{right(p)} + σz_p σz_{up(p)}) with the site
  * numbering of examples/ising2d.jl:16-26 (0-based: p = i + j Ly, right(p) =
