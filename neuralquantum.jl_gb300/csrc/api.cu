@@ -1066,7 +1066,7 @@ nq_status nq_set_symmetry(nq_handle* h, int32_t n_perm, const int32_t* perms) {
   auto put = [&](int bare, double c) { idx.push_back(bare); coef.push_back(c); };
   for (int f9 = 0; f9 < 9; ++f9) {
     const bool isb = f9 == 0 || f9 == 4, ish = f9 == 1 || f9 == 5, isd = f9 == 6;
-    const bool isw = f9 == 2 || f9 == 7, isu = f9 == 3 || f9 == 8;
+    const bool isw = f9 == 2 || f9 == 7;            // otherwise (f9 = 3, 8): the ancilla weights
     const int n = isb ? N : (ish ? ah : (isd ? aa : (isw ? ah * N : aa * N)));
     for (int k = 0; k < n; ++k) {
       if (isb) {
