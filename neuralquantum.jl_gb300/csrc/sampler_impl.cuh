@@ -19,7 +19,8 @@ namespace {
 // at the end of every sweep, so rounding drift is bounded by one sweep.
 // Random draws are software-pipelined: every G steps each lane evaluates the
 // Philox block of one upcoming step and the chain's lanes broadcast (site, u)
-// by shuffle when the step is reached.
+// by shuffle one step ahead, together with the table rows of that site, so
+// the loads of step t+1 overlap the decision of step t.
 // ---------------------------------------------------------------------------
 template <typename R> NQ_D R fast_log2(R x) { return log2(x); }
 template <> NQ_D float fast_log2<float>(float x) { return __log2f(x); }
