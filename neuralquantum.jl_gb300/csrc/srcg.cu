@@ -7,11 +7,12 @@
 //                = σ·v_a + Σ_h g_h (v_b,h + Σ_j v_W,hj σ_j) − ⟨O⟩·v
 //   adjoint  y_p = (Σ_s conj(O_p(s)) t_s − conj⟨O_p⟩ Σ_s t_s) / Ns
 // Conjugate gradients in FP64 vectors in ONE persistent cooperative launch:
-// per iteration a forward pass (thread per sample, v in shared memory), an
-// adjoint pass (CTA b accumulates its chunk of samples for every parameter in
-// registers, FP32 inside 32-sample tiles, FP64 across), a fixed-order
-// reduction of the CTA partials and the CG recurrences, separated by bounded
-// grid barriers.  Every dot product is reduced in a fixed order, so the result
+// per iteration a forward pass (thread per sample, v in shared memory, the
+// hidden units in register chunks), an adjoint pass (CTA b works through its
+// chunk of samples in tiles of 32: σ and z = conj(g) t staged in shared
+// memory, the W block as a register-tiled contraction; FP32 sums per tile and
+// per CTA, FP64 across CTAs), a fixed-order reduction of the CTA partials and
+// the CG recurrences, separated by bounded grid barriers.  Every dot product is reduced in a fixed order, so the result
 // does not depend on timing.  Memory: O(P · CTAs + Ns), no P x P matrix.
 #include "nq_kernels.cuh"
 #include "tc_common.cuh"
