@@ -881,6 +881,8 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   step(cudaMallocHost((void**)&h->h_stats, 8 * sizeof(double)), "pinned");
   step(cudaMallocHost((void**)&h->h_acc, sizeof(unsigned long long)), "pinned");
   step(cudaMallocHost((void**)&h->h_status, sizeof(int)), "pinned");
+  step(cudaMallocHost((void**)&h->h_params, 2 * (size_t)P * sizeof(double)), "pinned");
+  step(cudaEventCreateWithFlags(&h->ev_params, cudaEventDisableTiming), "params event");
   for (int k = 0; k < 7; ++k) step(cudaEventCreate(&h->ev[k]), "event");
   for (int k = 0; k < 4; ++k) step(cudaEventCreate(&h->kev[k]), "event");
   for (int k = 0; k < 6; ++k) step(cudaEventCreate(&h->sev[k]), "event");
@@ -942,6 +944,8 @@ void nq_destroy(nq_handle* h) {
   if (h->h_call) cudaFreeHost(h->h_call);
   if (h->h_stats) cudaFreeHost(h->h_stats);
   if (h->h_status) cudaFreeHost(h->h_status);
+  if (h->h_params) cudaFreeHost(h->h_params);
+  if (h->ev_params) cudaEventDestroy(h->ev_params);
   if (h->h_acc) cudaFreeHost(h->h_acc);
   for (int k = 0; k < 7; ++k)
     if (h->ev[k]) cudaEventDestroy(h->ev[k]);
@@ -969,42 +973,44 @@ int64_t nq_kernel_launches(const nq_handle* h) { return h ? h->launches : -1; }
 nq_status nq_set_params(nq_handle* h, const void* flat, int64_t n, int32_t dtype) {
   if (!h || !flat) return NQ_ERR_ARG;
   if (n != h->P) return fail(h, NQ_ERR_ARG, "expected %d parameters, got %lld", h->P, (long long)n);
-  std::vector<double> buf((h->complex_params ? 2 : 1) * (size_t)h->P, 0.0);
-  if (h->complex_params) {
-    if (dtype == NQ_DTYPE_C128) memcpy(buf.data(), flat, buf.size() * sizeof(double));
-    else if (dtype == NQ_DTYPE_C64) {
-      const float* f = (const float*)flat;
-      for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
-    } else return fail(h, NQ_ERR_ARG, "RBM / RBMSplit parameters are complex (dtype c64 or c128)");
+  const size_t nd = (h->complex_params ? 2 : 1) * (size_t)h->P;
+  if (h->complex_params ? (dtype != NQ_DTYPE_C128 && dtype != NQ_DTYPE_C64)
+                        : (dtype != NQ_DTYPE_F64 && dtype != NQ_DTYPE_F32))
+    return fail(h, NQ_ERR_ARG, h->complex_params ? "RBM / RBMSplit parameters are complex (dtype c64 or c128)"
+                                                 : "NDM parameters are real (dtype f32 or f64)");
+  // the pinned staging buffer is reused once the previous upload out of it is done
+  CK(cudaEventSynchronize(h->ev_params));
+  double* buf = h->h_params;
+  if (dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_F64) {
+    memcpy(buf, flat, nd * sizeof(double));
   } else {
-    if (dtype == NQ_DTYPE_F64) memcpy(buf.data(), flat, buf.size() * sizeof(double));
-    else if (dtype == NQ_DTYPE_F32) {
-      const float* f = (const float*)flat;
-      for (size_t i = 0; i < buf.size(); ++i) buf[i] = f[i];
-    } else return fail(h, NQ_ERR_ARG, "NDM parameters are real (dtype f32 or f64)");
+    const float* f = (const float*)flat;
+    for (size_t i = 0; i < nd; ++i) buf[i] = f[i];
   }
-  for (double v : buf)
-    if (!std::isfinite(v)) return fail(h, NQ_ERR_NAN, "non-finite parameter");
-  // the copy from pageable memory has left buf when it returns; the refresh
-  // kernels stay queued on the handle's stream ahead of its next call
-  CK(cudaMemcpyAsync(h->d_master, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  for (size_t i = 0; i < nd; ++i)
+    if (!std::isfinite(buf[i])) return fail(h, NQ_ERR_NAN, "non-finite parameter");
+  // asynchronous upload from the pinned buffer; it and the refresh kernels
+  // stay queued on the handle's stream ahead of its next call
+  CK(cudaMemcpyAsync(h->d_master, buf, nd * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->ev_params, h->st));
   return refresh_params(h);
 }
 
 nq_status nq_get_params(nq_handle* h, void* flat, int64_t n, int32_t dtype) {
   if (!h || !flat) return NQ_ERR_ARG;
   if (n != h->P) return fail(h, NQ_ERR_ARG, "expected %d parameters, got %lld", h->P, (long long)n);
-  std::vector<double> buf((h->complex_params ? 2 : 1) * (size_t)h->P);
-  CK(cudaMemcpyAsync(buf.data(), h->d_master, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
   const bool want_c = dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_C64;
   if (want_c != h->complex_params)
     return fail(h, NQ_ERR_ARG, h->complex_params ? "RBM / RBMSplit parameters are complex (dtype c64 or c128)"
                                                  : "NDM parameters are real (dtype f32 or f64)");
-  if (dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_F64) memcpy(flat, buf.data(), buf.size() * sizeof(double));
+  const size_t nd = (h->complex_params ? 2 : 1) * (size_t)h->P;
+  // into the pinned staging buffer (after any upload out of it, stream order)
+  CK(cudaMemcpyAsync(h->h_params, h->d_master, nd * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (dtype == NQ_DTYPE_C128 || dtype == NQ_DTYPE_F64) memcpy(flat, h->h_params, nd * sizeof(double));
   else {
     float* f = (float*)flat;
-    for (size_t i = 0; i < buf.size(); ++i) f[i] = (float)buf[i];
+    for (size_t i = 0; i < nd; ++i) f[i] = (float)h->h_params[i];
   }
   return NQ_OK;
 }

@@ -52,6 +52,8 @@ struct nq_handle {
   // side branch of the captured step: the ket path's measurement statistics
   // run beside the force, S and solve stages (they are read only at the end)
   int* h_status = nullptr;           // pinned copy of the device status word (nq_vmc_step)
+  double* h_params = nullptr;        // pinned staging of nq_set_params / nq_get_params (2P doubles)
+  cudaEvent_t ev_params = nullptr;   // the last upload out of h_params
   cudaStream_t st_side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side_ok = false, side_pending = false;     // side_ok: set by nq_vmc_step's capture only

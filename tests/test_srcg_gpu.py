@@ -63,9 +63,13 @@ def test_cg_solve_matches_oracle(nqlib, kind):
         eng.sr_matrix()
 
 
-def test_cg_matches_direct_on_same_samples(nqlib):
-    direct, _, _ = make(nq.sr_cholesky, N=8, B=256, L=8)
-    cg, _, _ = make(nq.sr_cg, N=8, B=256, L=8, precision=1e-9)
+@pytest.mark.parametrize("N,alpha,B,L", [(8, 2, 256, 8), (9, 1, 1024, 8), (12, 3, 512, 16)])
+def test_cg_matches_direct_on_same_samples(nqlib, N, alpha, B, L):
+    """CG against the direct solve on one sample set; the shapes cover hidden
+    units and sites that do not fill the adjoint's 4 x 8 register tiles
+    (M = 9, N = 9 and 12) and several 32-sample tiles per CTA (Ns = 8192)."""
+    direct, _, _ = make(nq.sr_cholesky, N=N, alpha=alpha, B=B, L=L)
+    cg, _, _ = make(nq.sr_cg, N=N, alpha=alpha, B=B, L=L, precision=1e-9)
     samples, _ = direct.engine.sample(3)
     cg.engine.set_samples(samples)
     direct.engine.estimate()
