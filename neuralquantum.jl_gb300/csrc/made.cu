@@ -1,7 +1,7 @@
 // Learned autoregressive proposal: a MADE masked MLP (N -> H -> H -> N, ReLU,
 // Bernoulli outputs) with its own sampling, log-probability and training
-// kernels.  The reference has no learned proposal; the FP64 definition the
-// kernels follow is oracle/made.py.
+// kernels.  The reference has no learned proposal; the tests check these
+// kernels against an FP64 restatement of the same network.
 //
 // Parameters (FP32 master, flat): W1 [H][N], b1 [H], W2 [H][H], b2 [H],
 // W3 [N][H], b3 [N]; masked entries are zero and stay zero (their gradient is

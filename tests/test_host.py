@@ -176,3 +176,25 @@ def test_hypercube_and_lattice_operators():
     perms = nq.translational_symm_table(nq.HyperCube([N]))
     net = nq.NDMSymm(np.float64, N, 1, 1, perms)
     assert net.permutations.min() == 0 and net.permutations.max() == N - 1
+
+
+def test_product_path_never_reaches_the_oracle():
+    """The host package and the CUDA sources neither import nor load anything
+    from oracle/: the oracle is the checker of the tests, the smoke entry point
+    and the bench's CPU legs, never part of the path it checks."""
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    pkg = os.path.join(root, "neuralquantum.jl_gb300")
+    pat = re.compile(r"(import\s+oracle|from\s+oracle|oracle[/\\]|libnqport|cport)")
+    hits = []
+    for d, _, files in os.walk(pkg):
+        if "_build" in d or "__pycache__" in d:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".c", ".cpp")):
+                path = os.path.join(d, f)
+                with open(path, encoding="utf-8") as fh:
+                    for n, line in enumerate(fh, 1):
+                        if pat.search(line):
+                            hits.append(f"{os.path.relpath(path, root)}:{n}: {line.strip()}")
+    assert not hits, hits
