@@ -93,8 +93,19 @@ typedef enum { NQ_NET_RBM = 0, NQ_NET_NDM = 1, NQ_NET_RBM_SPLIT = 2, NQ_NET_NDM_
  * NQ_LAYER_DENSE_SPLIT (n_in = N, θ = Wr σ + Wc η + b on the row and column
  * configurations, parameters Wr, Wc (out x N, column-major), b), then as a
  * ket chain; it samples |ρ(σ,η)|² on the doubled space and takes the
- * Liouvillian cost function like the NDM. */
-typedef enum { NQ_LAYER_DENSE = 0, NQ_LAYER_WSUM = 1, NQ_LAYER_SUM = 2, NQ_LAYER_DENSE_SPLIT = 3 } nq_layer_kind;
+ * Liouvillian cost function like the NDM.
+ * NQ_LAYER_POSITIVE_DEF_R may open a density-matrix chain instead of
+ * DenseSplit (Layers/PositiveDefR.jl, PositiveDefRBatched.jl):
+ * θ = Wr (σ + η) + i Wi (σ − η) + b, parameters Wr, Wi (out x N,
+ * column-major) and b, real in the reference and passed here as complex
+ * values with zero imaginary part; ∇Wr = δθ (σ + η)ᵀ, ∇Wi = i δθ (σ − η)ᵀ,
+ * ∇b = δθ.  With that first layer the chain's first trainable array is real,
+ * so SR runs in the reference's real mode (Algorithms/SR/SRDirect.jl:11-38):
+ * S = Re(O_c O_c†)/Ns, F = Re(F) (nq_estimate returns F with zero imaginary
+ * parts), a real Δw, and the Descent update moves only the real parts of
+ * every parameter, later complex Dense and WSum weights included. */
+typedef enum { NQ_LAYER_DENSE = 0, NQ_LAYER_WSUM = 1, NQ_LAYER_SUM = 2, NQ_LAYER_DENSE_SPLIT = 3,
+               NQ_LAYER_POSITIVE_DEF_R = 4 } nq_layer_kind;
 typedef struct {
   int32_t kind;            /* nq_layer_kind */
   int32_t n_in;

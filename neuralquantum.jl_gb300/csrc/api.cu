@@ -65,7 +65,10 @@ nq_status ndm_refresh(nq_handle* h) {
 // refresh FP32 copies and the per-flip tables after a parameter change
 nq_status refresh_params(nq_handle* h) {
   if (h->chain) {
-    if (!h->f64) CKL(launch_master_to_f32(h->d_master, 2L * h->P, h->d_p32, h->st));
+    if (h->chain_spec.pdr)
+      CKL(launch_chain_pdr_params(h->d_master, h->P, h->chain_spec.L[0].out, h->N, h->f64 ? nullptr : h->d_p32,
+                                  h->f64 ? h->d_pexp : nullptr, h->st));
+    else if (!h->f64) CKL(launch_master_to_f32(h->d_master, 2L * h->P, h->d_p32, h->st));
     return NQ_OK;
   }
   if (h->ndm) {
@@ -355,7 +358,7 @@ nq_status stage_S(nq_handle* h) {
       CKL(launch_gram_simt_x(h->d_X, h->Ns_pad, h->Ns, 2 * h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
     }
     if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
-    CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, !h->complex_params, h->d_S, h->st));
+    CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, h->real_sr, h->d_S, h->st));
     return NQ_OK;
   }
   RbmOSource src;
@@ -384,7 +387,7 @@ nq_status stage_S(nq_handle* h) {
     CKL(launch_gram_simt(src, h->P, h->d_G, h->d_Gpart, h->gram_ksplit, h->st));
     if (!h->capturing) CK(cudaEventRecord(h->kev[3], h->st));
   }
-  CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, !h->complex_params, h->d_S, h->st));
+  CKL(launch_assemble_S(h->d_G, h->P, 1.0 / h->Ns, h->real_sr, h->d_S, h->st));
   return NQ_OK;
 }
 
@@ -394,7 +397,7 @@ nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
     a.eps = eps;
     a.tol = h->cg_tol;
     a.maxiter = h->cg_maxiter;
-    a.real_params = h->complex_params ? 0 : 1;
+    a.real_params = h->real_sr ? 1 : 0;
     if (!h->capturing) CK(cudaEventRecord(h->sev[0], h->st));
     CKL(launch_sr_cg(a, kind, lam, h->st));
     ++h->launches;
@@ -405,7 +408,7 @@ nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
   }
   SolveBufs sb = h->sb;
   sb.ev = h->capturing ? nullptr : h->sev;
-  CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, !h->complex_params, kSolveRefine, h->st));
+  CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, h->real_sr, kSolveRefine, h->st));
   h->launches += 8;
   return NQ_OK;
 }
@@ -572,7 +575,9 @@ namespace {
 // validated layer list of a chain into spec; "" or the reason it is refused
 // A density-matrix chain's DenseSplit layer (θ = Wr σ + Wc η + b) is stored
 // as a Dense layer on the 2N doubled sites: W = [Wr Wc] column-major is Wr
-// then Wc, so the parameter vector is unchanged.
+// then Wc, so the parameter vector is unchanged.  A PositiveDefR first layer
+// (Wr, Wi, b) has the same sizes and runs as that Dense layer with
+// W = [Wr + i Wi, Wr − i Wi] (spec->pdr).
 const char* chain_layers(const nq_config& c, int n_layers, const nq_layer* layers, ChainDev<float>* spec) {
   if (!layers || n_layers < 2 || n_layers > 8) return "a chain has 2..8 layers";
   const bool mixed = c.network == NQ_NET_MIXED_CHAIN;
@@ -582,13 +587,16 @@ const char* chain_layers(const nq_config& c, int n_layers, const nq_layer* layer
     ChainLayerDev d;
     d.kind = y.kind; d.in = y.n_in; d.out = y.n_out; d.act = y.activation;
     if (y.n_in != prev) return "layer input width differs from the previous output";
-    if (mixed != (l == 0 && y.kind == NQ_LAYER_DENSE_SPLIT) && l == 0)
-      return mixed ? "a density-matrix chain starts with DenseSplit" : "DenseSplit starts a density-matrix chain";
-    if (l > 0 && y.kind == NQ_LAYER_DENSE_SPLIT) return "DenseSplit is the first layer only";
-    const bool dense = y.kind == NQ_LAYER_DENSE || y.kind == NQ_LAYER_DENSE_SPLIT;
-    if (y.kind == NQ_LAYER_DENSE_SPLIT) {
+    const bool split = y.kind == NQ_LAYER_DENSE_SPLIT || y.kind == NQ_LAYER_POSITIVE_DEF_R;
+    if (mixed != (l == 0 && split) && l == 0)
+      return mixed ? "a density-matrix chain starts with DenseSplit or PositiveDefR"
+                   : "DenseSplit and PositiveDefR start a density-matrix chain";
+    if (l > 0 && split) return "DenseSplit and PositiveDefR are the first layer only";
+    const bool dense = y.kind == NQ_LAYER_DENSE || split;
+    if (split) {
       d.kind = NQ_LAYER_DENSE;
       d.in = 2 * y.n_in;
+      spec->pdr = y.kind == NQ_LAYER_POSITIVE_DEF_R ? 1 : 0;
     }
     const bool closing = l == n_layers - 1;
     if (closing != !dense) return "Dense layers, then exactly one closing WSum or sum";
@@ -738,6 +746,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   h->tc_theta = c.eval_precision == NQ_EVAL_TC_BF16X2 || c.eval_precision == NQ_EVAL_TC_BF16X3;
   h->theta_terms = c.eval_precision == NQ_EVAL_TC_BF16X3 ? 3 : 2;
   h->complex_params = !h->ndm || h->split;      // RBM, RBMSplit and chains
+  h->real_sr = !h->complex_params || (h->chain && h->chain_spec.pdr);
   const int sampler_M = h->diag ? h->Md : (h->ndm ? h->Ms : h->M), sampler_N = h->nst;
   if (c.sampler_lanes != 0 && !h->chain) {
     int cand[4];
@@ -764,6 +773,7 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   const int P = h->P;
   step(dalloc(&h->d_master, 2 * (size_t)P), "params");
   step(dalloc(&h->d_p32, 2 * (size_t)P), "params32");
+  if (h->chain && h->chain_spec.pdr && h->f64) step(dalloc(&h->d_pexp, 2 * (size_t)P), "PositiveDefR params");
   for (int k = 0; k < 3; ++k) step(cudaMalloc(&h->d_tab[k], (size_t)sampler_N * sampler_M * csz + 16), "tables");
   if (h->ndm) {
     const size_t ne[5] = {(size_t)h->U * h->N2, (size_t)h->U, (size_t)h->N2, (size_t)h->Ms * h->N2, (size_t)h->Ms};
@@ -922,7 +932,7 @@ void nq_destroy(nq_handle* h) {
   proposal_destroy(h);
   free_op(h);
   free_rule_operator(h);
-  void* bufs[] = {h->d_master, h->d_p32, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
+  void* bufs[] = {h->d_master, h->d_p32, h->d_pexp, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
                   h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
@@ -1408,6 +1418,8 @@ nq_status nq_get_estimates(nq_handle* h, double* loc_out, double* force_out, dou
     if (!srcs[k]) return fail(h, NQ_ERR_STATE, "no %s buffer on this handle", k ? "update" : "force");
     std::vector<double> f(2 * (size_t)h->P);
     CK(cudaMemcpy(f.data(), srcs[k], f.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->complex_params && h->real_sr)         // PositiveDefR chain: F and Δw are real
+      for (int i = 0; i < h->P; ++i) f[2 * i + 1] = 0.0;
     if (h->complex_params) memcpy(outs[k], f.data(), f.size() * sizeof(double));
     else
       for (int i = 0; i < h->P; ++i) outs[k][i] = f[2 * i];
@@ -1527,6 +1539,8 @@ nq_status nq_estimate(nq_handle* h, nq_measurement* stats, double* loc_out, doub
   if (force_out) {
     std::vector<double> f(2 * (size_t)h->P);
     CK(cudaMemcpy(f.data(), h->fb.force, f.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->complex_params && h->real_sr)         // PositiveDefR chain: F is real
+      for (int i = 0; i < h->P; ++i) f[2 * i + 1] = 0.0;
     if (h->complex_params) memcpy(force_out, f.data(), f.size() * sizeof(double));
     else
       for (int i = 0; i < h->P; ++i) force_out[i] = f[2 * i];

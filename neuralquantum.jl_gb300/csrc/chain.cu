@@ -15,6 +15,12 @@
 // every Dense layer (Σ out) and three vectors of the widest layer; a
 // proposal or a connection changes only θ_1 (θ_1' = θ_1 + Σ_q W_1[:, s_q] dv_q),
 // so the forward pass restarts from θ_1'.
+//
+// Density-matrix chains run the same kernels on the 2N doubled sites (σ, η):
+// DenseSplit (Layers/DenseSplit.jl) is the Dense layer W = [Wr Wc], and
+// PositiveDefR (Layers/PositiveDefR.jl) the Dense layer W = [Wr + i Wi,
+// Wr − i Wi] written by chain_pdr_params_kernel, whose gradient entries
+// chain_backprop takes with respect to (Wr, Wi).
 #include "nq_kernels.cuh"
 
 namespace {
@@ -116,6 +122,19 @@ NQ_D void chain_backprop(const ChainDev<R>& c, uint64_t bits, const cpx<R>* th, 
     if (l > 0)
       for (int i = 0; i < Ly.in; ++i)
         x[(size_t)i * T] = chain_act<R>(c.L[l - 1].act, th[(size_t)(thoff[l - 1] + i) * T]);
+    if (l == 0 && c.pdr) {
+      // PositiveDefRBatched.jl backprop: ∇Wr = δθ (σ + η)ᵀ, ∇Wi = i δθ (σ − η)ᵀ
+      const int n = Ly.in / 2;
+      for (int i = 0; i < n; ++i) {
+        const R sr = site_value<R>(bits, i, c.hilb), sc = site_value<R>(bits, n + i, c.hilb);
+        for (int q = 0; q < Ly.out; ++q) {
+          const cpx<R> dq = d[(size_t)q * T];
+          out(Ly.w_off + q + Ly.out * i, mk(dq.x * (sr + sc), dq.y * (sr + sc)));
+          out(Ly.w_off + q + Ly.out * (n + i), mk(-dq.y * (sr - sc), dq.x * (sr - sc)));
+        }
+      }
+      break;
+    }
     for (int i = 0; i < Ly.in; ++i) {
       const cpx<R> xi = l > 0 ? x[(size_t)i * T] : mk(site_value<R>(bits, i, c.hilb), R(0));
       cpx<R> back = mk(R(0), R(0));
@@ -402,7 +421,37 @@ cudaError_t set_smem(K kern, size_t smem) {
   return cudaSuccess;
 }
 
+// PositiveDefR's θ = Wr (σ + η) + i Wi (σ − η) + b (PositiveDefR.jl:11-12)
+// is the Dense layer W_σ σ + W_η η + b with W_σ = Wr + i Wi, W_η = Wr − i Wi;
+// the later layers are copied.  One thread per complex entry k < P.
+template <typename T>
+__global__ void chain_pdr_params_kernel(const double* __restrict__ master, int P, int nw, T* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P) return;
+  double re = master[2 * k], im = master[2 * k + 1];
+  if (k < 2 * nw) {
+    const int j = k < nw ? k : k - nw;                     // the same (unit, site) of Wr and Wi
+    const double ar = master[2 * j], ai = master[2 * j + 1];
+    const double br = master[2 * (nw + j)], bi = master[2 * (nw + j) + 1];
+    const double s = k < nw ? 1.0 : -1.0;                  // Wr ± i Wi
+    re = ar - s * bi;
+    im = ai + s * br;
+  }
+  out[2 * k] = (T)re;
+  out[2 * k + 1] = (T)im;
+}
+
 }  // namespace
+
+cudaError_t launch_chain_pdr_params(const double* master, int P, int n_out, int n_sites, float* p32, double* p64,
+                                    cudaStream_t st) {
+  const int nw = n_out * n_sites;
+  if (P < 2 * nw + n_out || (p32 == nullptr) == (p64 == nullptr)) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)((P + 255) / 256);
+  if (p32) chain_pdr_params_kernel<float><<<grid, 256, 0, st>>>(master, P, nw, p32);
+  else chain_pdr_params_kernel<double><<<grid, 256, 0, st>>>(master, P, nw, p64);
+  return cudaGetLastError();
+}
 
 template <typename R>
 cudaError_t launch_chain_eval(const ChainDev<R>& c, const uint64_t* samples, int n, const DevOp* op, cpx<R>* logpsi,

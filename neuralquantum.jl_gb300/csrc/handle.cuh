@@ -62,6 +62,8 @@ struct nq_handle {
 
   double* d_master = nullptr;      // FP64 master parameters (complex interleaved or real)
   float* d_p32 = nullptr;          // FP32 working copy (RBM, complex)
+  double* d_pexp = nullptr;        // FP64 working copy of a PositiveDefR chain (Dense form)
+  bool real_sr = false;            // S, F and Δw real: real parameters, or a PositiveDefR chain
   void* d_tab[3] = {nullptr, nullptr, nullptr};
   uint64_t* d_samples = nullptr;   // [L][B]
   unsigned long long* d_accepted = nullptr;
@@ -224,7 +226,10 @@ ChainDev<R> chain_dev(nq_handle* h) {
   const ChainDev<float>& s = h->chain_spec;
   c.N = s.N; c.hilb = s.hilb; c.n_layers = s.n_layers; c.P = s.P; c.n_theta = s.n_theta; c.max_w = s.max_w;
   for (int l = 0; l < 8; ++l) c.L[l] = s.L[l];
-  c.p = h->f64 ? reinterpret_cast<const cpx<R>*>(h->d_master) : reinterpret_cast<const cpx<R>*>(h->d_p32);
+  c.pdr = s.pdr;
+  c.p = !h->f64     ? reinterpret_cast<const cpx<R>*>(h->d_p32)
+        : s.pdr     ? reinterpret_cast<const cpx<R>*>(h->d_pexp)
+                    : reinterpret_cast<const cpx<R>*>(h->d_master);
   return c;
 }
 

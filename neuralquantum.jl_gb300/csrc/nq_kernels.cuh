@@ -133,6 +133,10 @@ template <typename R> struct ChainDev {
   int n_theta = 0;             // Σ out over the Dense layers (stored pre-activations)
   int max_w = 0;               // widest Dense output
   ChainLayerDev L[8];
+  // first layer PositiveDefR: p holds it in the Dense form over the doubled
+  // sites (W_σ = Wr + i Wi, W_η = Wr − i Wi, b) and the gradient entries of
+  // that layer are taken with respect to (Wr, Wi, b)
+  int pdr = 0;
   const cpx<R>* p = nullptr;
 };
 // logψ, E_loc (op nullable) and O into X (uncentred FP32 rows 2k, 2k+1) and/or
@@ -153,6 +157,12 @@ cudaError_t launch_chain_force(const float* X, int ldx, int P, int ns, const cpx
                                double* force, cudaStream_t st);
 template <typename R>
 cudaError_t launch_chain_sampler(const ChainDev<R>& c, const SamplerRun& run, cudaStream_t st);
+// the working parameters of a chain that opens with PositiveDefR (n_out x
+// n_sites weights): master (Wr, Wi, b, later layers; complex interleaved, P
+// entries) into the Dense form (W_σ, W_η, b, later layers) as FP32 (p32) or
+// FP64 (p64), whichever is non-null
+cudaError_t launch_chain_pdr_params(const double* master, int P, int n_out, int n_sites, float* p32, double* p64,
+                                    cudaStream_t st);
 
 // Exact sampler (Exact.jl): all 2^N configurations of the sampler's space
 // (N <= 26), FP64 CDF, inverse-CDF draws into run.samples (n_record draws per

@@ -12,7 +12,7 @@ from .operators import (LocalOperator, KLocalOperator, KLocalOperatorSum, KLocal
                         sigmax, sigmay, sigmaz, sigmam, sigmap, liouvillian, op_table)
 from .networks import RBM, NDM, NDMSymm, RBMSplit, af_logcosh, af_softplus, init_random_pars_  # noqa: F401
 from .networks import Dense, WSum, Chain, PureStateAnsatz, PureChain, sum_autobatch, identity  # noqa: F401
-from .networks import DenseSplit, MixedStateAnsatz  # noqa: F401
+from .networks import DenseSplit, PositiveDefR, MixedStateAnsatz  # noqa: F401
 from .samplers import MetropolisSampler, ExactSampler, LocalRule, ExchangeRule, OperatorRule  # noqa: F401
 from .stats import Measurement  # noqa: F401
 from .iterative import (BatchedSampler, BatchedObsKetSampler, BatchedObsDMSampler, add_observable_,  # noqa: F401

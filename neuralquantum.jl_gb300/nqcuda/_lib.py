@@ -29,7 +29,7 @@ NQ_OK, NQ_ERR_ARG, NQ_ERR_CUDA, NQ_ERR_NOT_PD, NQ_ERR_TIMEOUT, NQ_ERR_NAN, NQ_ER
 STATUS_NAMES = ["NQ_OK", "NQ_ERR_ARG", "NQ_ERR_CUDA", "NQ_ERR_NOT_PD", "NQ_ERR_TIMEOUT",
                 "NQ_ERR_NAN", "NQ_ERR_STATE", "NQ_ERR_UNSUPPORTED"]
 NQ_NET_RBM, NQ_NET_NDM, NQ_NET_RBM_SPLIT, NQ_NET_NDM_SYMM, NQ_NET_CHAIN, NQ_NET_MIXED_CHAIN = 0, 1, 2, 3, 4, 5
-NQ_LAYER_DENSE, NQ_LAYER_WSUM, NQ_LAYER_SUM, NQ_LAYER_DENSE_SPLIT = 0, 1, 2, 3
+NQ_LAYER_DENSE, NQ_LAYER_WSUM, NQ_LAYER_SUM, NQ_LAYER_DENSE_SPLIT, NQ_LAYER_POSITIVE_DEF_R = 0, 1, 2, 3, 4
 NQ_ACT_LOGCOSH, NQ_ACT_SOFTPLUS, NQ_ACT_IDENTITY = 0, 1, 2
 NQ_HILB_SPIN, NQ_HILB_FOCK = 0, 1
 NQ_DTYPE_C64, NQ_DTYPE_C128, NQ_DTYPE_F32, NQ_DTYPE_F64 = 0, 1, 2, 3

@@ -5,8 +5,8 @@ import numpy as np
 
 from . import _lib
 from .hilbert import SuperOpSpace, physical
-from .networks import RBM, NDM, NDMSymm, RBMSplit, PureStateAnsatz, MixedStateAnsatz, Dense, DenseSplit, WSum, \
-    af_logcosh, af_softplus
+from .networks import RBM, NDM, NDMSymm, RBMSplit, PureStateAnsatz, MixedStateAnsatz, Dense, DenseSplit, \
+    PositiveDefR, WSum, af_logcosh, af_softplus
 
 
 def make_config(net, hilb, n_chains, chain_length, burn, passes, seed, eval_precision=_lib.NQ_EVAL_F32,
@@ -72,6 +72,9 @@ def chain_layers(net):
     for k, l in enumerate(layers):
         if isinstance(l, DenseSplit):
             arr[k] = _lib.NqLayer(_lib.NQ_LAYER_DENSE_SPLIT, l.n_in, l.n_out, acts[l.f])
+            width = l.n_out
+        elif isinstance(l, PositiveDefR):
+            arr[k] = _lib.NqLayer(_lib.NQ_LAYER_POSITIVE_DEF_R, l.n_in, l.n_out, acts[l.f])
             width = l.n_out
         elif isinstance(l, Dense):
             arr[k] = _lib.NqLayer(_lib.NQ_LAYER_DENSE, l.n_in, l.n_out, acts[l.f])

@@ -190,6 +190,26 @@ class DenseSplit:
         return [self.Wr, self.Wc, self.b]
 
 
+class PositiveDefR:
+    """``PositiveDefR(T, in, out, σ=identity)`` (Chains/Layers/PositiveDefR.jl):
+    the first layer of a density-matrix chain,
+    y = σ.(Wr (σr .+ σc) .+ im Wi (σr .- σc) .+ b), with real Wr, Wi (out x in)
+    and b, glorot-uniform initialisation; functor order Wr, Wi, b.  T is the
+    real element type (STD_REAL_PREC = Float32 by default)."""
+
+    def __init__(self, T=np.float32, n_in=None, n_out=None, f=identity, rng=None):
+        self.dtype = np.dtype(T)
+        if self.dtype.kind == "c":
+            raise ValueError("PositiveDefR takes real weights (Float32 / Float64)")
+        self.n_in, self.n_out, self.f = int(n_in), int(n_out), f
+        self.Wr = glorot_uniform(self.dtype, self.n_out, self.n_in, rng=rng)
+        self.Wi = glorot_uniform(self.dtype, self.n_out, self.n_in, rng=rng)
+        self.b = glorot_uniform(self.dtype, self.n_out, rng=rng)
+
+    def arrays(self):
+        return [self.Wr, self.Wi, self.b]
+
+
 class WSum:
     """``WSum(T, in)`` (Chains/Layers/WeightedSum.jl): logψ = Σ_i c_i x_i."""
 
@@ -276,22 +296,28 @@ class PureStateAnsatz:
 class MixedStateAnsatz:
     """``MixedStateAnsatz(chain, N)`` (MixedDensityMatrix/MixedChainWrapper.jl:
     3-37): a density matrix whose logρ(σ, η) is the chain's output for the
-    pair of configurations; the chain is DenseSplit(N, out) followed by Dense
-    layers and closed by WSum or sum_autobatch.  Complex parameters in the
-    functor order (DenseSplit: Wr, Wc, b; Dense: W, b; WSum: c).  Since
-    DenseSplit's θ = Wr σ + Wc η + b is a Dense layer on the 2N doubled sites
-    with W = [Wr Wc], whose column-major storage is Wr then Wc, the flat
-    vector is that of a chain over the doubled sites."""
+    pair of configurations; the chain is DenseSplit(N, out) or
+    PositiveDefR(N, out) followed by Dense layers and closed by WSum or
+    sum_autobatch.  Parameters in the functor order (DenseSplit: Wr, Wc, b;
+    PositiveDefR: Wr, Wi, b; Dense: W, b; WSum: c), as a complex vector.
+    Since DenseSplit's θ = Wr σ + Wc η + b is a Dense layer on the 2N doubled
+    sites with W = [Wr Wc], whose column-major storage is Wr then Wc, the flat
+    vector is that of a chain over the doubled sites.  PositiveDefR's
+    parameters are real: the vector holds them with zero imaginary part, and
+    ``real_sr`` is set, since the reference's SR takes its element type from
+    the first trainable array (SRDirect.jl:11-38)."""
 
     def __init__(self, chain, n_sites):
         self.N = n_sites if isinstance(n_sites, int) else n_sites.n_sites
         self.chain = chain if isinstance(chain, Chain) else Chain(*chain)
         layers = self.chain.layers
-        if len(layers) < 2 or not isinstance(layers[0], DenseSplit) or \
+        if len(layers) < 2 or not isinstance(layers[0], (DenseSplit, PositiveDefR)) or \
                 not all(isinstance(l, Dense) for l in layers[1:-1]) or not isinstance(layers[-1], (WSum, _SumAutobatch)):
-            raise ValueError("the chain is DenseSplit, then Dense layers, closed by WSum or sum_autobatch")
+            raise ValueError("the chain is DenseSplit or PositiveDefR, then Dense layers, closed by WSum or "
+                             "sum_autobatch")
         if layers[0].n_in != self.N:
-            raise ValueError("DenseSplit's input width must be the number of sites")
+            raise ValueError("the first layer's input width must be the number of sites")
+        self.real_sr = isinstance(layers[0], PositiveDefR)
         width = layers[0].n_out
         for l in layers[1:-1]:
             if l.n_in != width:
@@ -313,9 +339,12 @@ class MixedStateAnsatz:
         v = np.asarray(v)
         o = 0
         for l in self.chain.layers:
-            for name in {DenseSplit: ("Wr", "Wc", "b"), Dense: ("W", "b"), WSum: ("c",)}.get(type(l), ()):
+            names = {DenseSplit: ("Wr", "Wc", "b"), PositiveDefR: ("Wr", "Wi", "b"), Dense: ("W", "b"),
+                     WSum: ("c",)}.get(type(l), ())
+            for name in names:
                 a = getattr(l, name)
-                setattr(l, name, v[o:o + a.size].reshape(a.shape, order="F").astype(l.dtype))
+                x = v[o:o + a.size].reshape(a.shape, order="F")
+                setattr(l, name, (np.real(x) if l.dtype.kind != "c" else x).astype(l.dtype))
                 o += a.size
 
     def __repr__(self):
@@ -332,6 +361,17 @@ def init_random_pars_(net, sigma=0.01, rng=None):
     from randn * sqrt(sigma); complex draws have variance 1/2 per part."""
     rng = np.random.default_rng() if rng is None else rng
     p = net.flat()
+    chain = getattr(net, "chain", None)
+    if chain is not None and any(a.dtype.kind != "c" for l in chain.layers for a in l.arrays()):
+        # a chain holding real arrays (PositiveDefR): each array drawn in its own type
+        parts = []
+        for a in (a for l in chain.layers for a in l.arrays()):
+            if a.dtype.kind == "c":
+                parts.append((rng.standard_normal(a.size) + 1j * rng.standard_normal(a.size)) / np.sqrt(2.0))
+            else:
+                parts.append(rng.standard_normal(a.size) + 0j)
+        net.set_flat(np.concatenate(parts) * np.sqrt(sigma))
+        return net
     if np.iscomplexobj(p):
         v = (rng.standard_normal(p.size) + 1j * rng.standard_normal(p.size)) / np.sqrt(2.0)
     else:

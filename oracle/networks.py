@@ -433,22 +433,41 @@ class MixedChain:
     (σ, η) with W = [Wr Wc], whose column-major storage is Wr then Wc, so the
     flat vector (Wr, Wc, b, later layers) is the ``Chain`` over 2N inputs
     with layers[0] = ("dense", 2N, M, f).  ``layers`` lists the DenseSplit as
-    ("dense_split", N, M, f)."""
+    ("dense_split", N, M, f).
+
+    ``("positive_def_r", N, M, f)`` opens the chain with PositiveDefR
+    (Layers/PositiveDefR.jl:11-12): θ = Wr (σ + η) + i Wi (σ − η) + b, flat
+    vector (Wr, Wi, b, later layers).  It is the Dense layer above with
+    W = [Wr + i Wi, Wr − i Wi]; the gradient of PositiveDefRBatched.jl's
+    backprop, ∇Wr = δθ (σ + η)ᵀ and ∇Wi = i δθ (σ − η)ᵀ, is
+    ∇Wr = ∇W_σ + ∇W_η and ∇Wi = i (∇W_σ − ∇W_η) of that Dense layer.  Its
+    parameters are real in the reference, so SR takes S and F real
+    (``real_sr``; SRDirect.jl:11-38)."""
 
     def __init__(self, n, layers):
         self.N = int(n)
         first = layers[0]
-        assert first[0] == "dense_split" and first[1] == self.N
+        assert first[0] in ("dense_split", "positive_def_r") and first[1] == self.N
+        self.pdr = first[0] == "positive_def_r"
+        self.real_sr = self.pdr
         self.chain = Chain(2 * self.N, [("dense", 2 * self.N, first[2], first[3])] + list(layers[1:]))
+        self._v = self.chain.flat()
 
     @property
     def n_params(self):
         return self.chain.n_params
 
     def flat(self):
-        return self.chain.flat()
+        return self._v.copy() if self.pdr else self.chain.flat()
 
     def set_flat(self, v):
+        v = np.asarray(v).astype(np.complex128)
+        self._v = v.copy()
+        if self.pdr:
+            nw = self.chain.params[0][0].size // 2         # Wr (M x N) of W = [W_σ W_η]
+            v = v.copy()
+            wr, wi = self._v[:nw], self._v[nw:2 * nw]
+            v[:nw], v[nw:2 * nw] = wr + 1j * wi, wr - 1j * wi
         self.chain.set_flat(v)
 
     def dense_split(self):
@@ -462,7 +481,12 @@ class MixedChain:
 
     def logpsi_and_grad(self, sr, sc):
         sr = np.atleast_2d(sr); sc = np.atleast_2d(sc)
-        return self.chain.logpsi_and_grad(np.concatenate([sr, sc], axis=1))
+        out, g = self.chain.logpsi_and_grad(np.concatenate([sr, sc], axis=1))
+        if self.pdr:
+            nw = self.chain.params[0][0].size // 2         # Wr (M x N) of W = [W_σ W_η]
+            gs, ge = g[:, :nw].copy(), g[:, nw:2 * nw].copy()
+            g[:, :nw], g[:, nw:2 * nw] = gs + ge, 1j * (gs - ge)
+        return out, g
 
     def log_prob(self, sr, sc):
         return 2.0 * np.real(self.logpsi(sr, sc))

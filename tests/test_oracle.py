@@ -569,3 +569,49 @@ def test_mixed_chain_is_the_dense_split_formula():
         mc.set_flat(q); dn = mc.logpsi(sr, sc)
         np.testing.assert_allclose(g[:, k], (up - dn) / (2 * eps), rtol=0, atol=1e-7)
     mc.set_flat(p)
+
+
+def test_mixed_chain_positive_def_r_formula_and_gradient():
+    """PositiveDefR opening a density-matrix chain (Layers/PositiveDefR.jl:11-12):
+    logρ(σ, η) = Σ_h f(Wr_h·(σ + η) + i Wi_h·(σ − η) + b_h) with real Wr, Wi,
+    b, then a complex Dense layer and WSum; the gradient with respect to each
+    parameter (real for PositiveDefR, holomorphic for the later complex
+    layers) against central finite differences."""
+    rng = np.random.default_rng(23)
+    N, M = 4, 6
+    mc = nw.MixedChain(N, [("positive_def_r", N, M, nw.LOGCOSH), ("sum", M)])
+    nw_ = M * N
+    p = np.zeros(mc.n_params, np.complex128)
+    p[:] = rng.standard_normal(mc.n_params) * 0.3
+    mc.set_flat(p)
+    Wr = p[:nw_].real.reshape(M, N, order="F")
+    Wi = p[nw_:2 * nw_].real.reshape(M, N, order="F")
+    b = p[2 * nw_:].real
+    h = Hilbert(N, SPIN)
+    sr = h.value(rng.integers(0, 2, size=(20, N)))
+    sc = h.value(rng.integers(0, 2, size=(20, N)))
+    direct = nw.logcosh((sr + sc) @ Wr.T + 1j * ((sr - sc) @ Wi.T) + b[None, :]).sum(axis=1)
+    np.testing.assert_allclose(mc.logpsi(sr, sc), direct, rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(mc.flat(), p)
+    lp, g = mc.logpsi_and_grad(sr, sc)
+    eps = 1e-6
+    for k in range(mc.n_params):
+        q = p.copy(); q[k] += eps
+        mc.set_flat(q); up = mc.logpsi(sr, sc)
+        q[k] -= 2 * eps
+        mc.set_flat(q); dn = mc.logpsi(sr, sc)
+        np.testing.assert_allclose(g[:, k], (up - dn) / (2 * eps), rtol=1e-6, atol=1e-7)
+    mc.set_flat(p)
+    # later complex layers: holomorphic derivative
+    mc2 = nw.MixedChain(N, [("positive_def_r", N, M, nw.SOFTPLUS), ("dense", M, 3, nw.LOGCOSH), ("wsum", 3)])
+    p2 = rng.standard_normal(mc2.n_params) * 0.3 + 0j
+    n1 = 2 * nw_ + M
+    p2[n1:] += 1j * rng.standard_normal(mc2.n_params - n1) * 0.3
+    mc2.set_flat(p2)
+    _, g2 = mc2.logpsi_and_grad(sr, sc)
+    for k in range(0, mc2.n_params, 3):
+        q = p2.copy(); q[k] += eps
+        mc2.set_flat(q); up = mc2.logpsi(sr, sc)
+        q[k] -= 2 * eps
+        mc2.set_flat(q); dn = mc2.logpsi(sr, sc)
+        np.testing.assert_allclose(g2[:, k], (up - dn) / (2 * eps), rtol=1e-6, atol=1e-7)
