@@ -199,7 +199,11 @@ typedef enum { NQ_SAMPLER_METROPOLIS = 0, NQ_SAMPLER_EXACT = 1 } nq_sampler_kind
  * gradients on the operator v -> conj(O_c) O_cᵀ v / Ns + shift v
  * (SRIterative.jl with SR_notfull.jl's SrMatrixC), for the reference's
  * iterative algorithms (sr_cg; sr_minres / sr_qlp / sr_lsq solve the same
- * system to the same tolerance).  RBM, FP32 evaluation; no P x P storage. */
+ * system to the same tolerance); no P x P storage.  The RBM (FP32
+ * evaluation) forms O from (σ, f'(θ)) each iteration; the other networks
+ * (NDM family, feed-forward and density-matrix chains, FP32 or FP64
+ * evaluation) read the centred O rows they materialise for the force, with
+ * P up to 28,000. */
 typedef enum { NQ_SR_DIRECT = 0, NQ_SR_CG = 1 } nq_sr_algorithm;
 
 /* Statistics of the local estimator (src/utils/stats.jl:1-50). */

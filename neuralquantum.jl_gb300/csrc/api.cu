@@ -686,9 +686,10 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   if (c.sampler_kind == NQ_SAMPLER_EXACT &&
       (matrix_net && c.sampler_space == NQ_SPACE_NETWORK ? 2 * c.n_sites : c.n_sites) > 26)
     return bad("the exact sampler enumerates 2^N configurations: N (2N for the NDM's doubled space) <= 26");
-  if (c.sr_algorithm == NQ_SR_CG &&
-      (c.network != NQ_NET_RBM || c.eval_precision == NQ_EVAL_F64 ||
-       !sr_cg_supported(c.n_sites, c.n_hidden))) {
+  // matrix-free SR: the RBM forms O from (σ, g) in FP32 evaluation; the other
+  // networks read the centred O rows of X (size checked once P is known)
+  if (c.sr_algorithm == NQ_SR_CG && c.network == NQ_NET_RBM &&
+      (c.eval_precision == NQ_EVAL_F64 || !sr_cg_supported(c.n_sites, c.n_hidden))) {
     delete h;
     return NQ_ERR_UNSUPPORTED;
   }
@@ -747,6 +748,10 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   h->theta_terms = c.eval_precision == NQ_EVAL_TC_BF16X3 ? 3 : 2;
   h->complex_params = !h->ndm || h->split;      // RBM, RBMSplit and chains
   h->real_sr = !h->complex_params || (h->chain && h->chain_spec.pdr);
+  if (c.sr_algorithm == NQ_SR_CG && c.network != NQ_NET_RBM && !sr_cg_x_supported(h->P)) {
+    delete h;
+    return NQ_ERR_UNSUPPORTED;
+  }
   const int sampler_M = h->diag ? h->Md : (h->ndm ? h->Ms : h->M), sampler_N = h->nst;
   if (c.sampler_lanes != 0 && !h->chain) {
     int cand[4];
@@ -819,6 +824,10 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   if (sr_bufs && c.s_precision == NQ_S_F32 && gram_tc_supported() &&
       2.0 * rows * (double)(((h->Ns + 127) / 128) * 128) * sizeof(float) <= kSf32TensorBytes)
     h->cfg.s_precision = NQ_S_TF32X3;
+  // matrix-free SR over X (NDM family, chains): S is never formed, so X stays
+  // plain FP32 (no TF32 rounding, no low part)
+  const bool cg_x = h->cg && (h->ndm || h->chain) && !h->diag;
+  if (cg_x) h->cfg.s_precision = NQ_S_F32;
   const int s_prec = h->cfg.s_precision;
   if (h->cg) {
     // matrix-free SR: O(P) vectors and per-CTA partials only
@@ -854,8 +863,8 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   }
   if (sr_bufs) step(dalloc(&h->d_G, (size_t)rows * rows), "G");
   if (sr_bufs) step(dalloc(&h->d_Gpart, (size_t)h->gram_ksplit * rp * rp), "G partial");
-  if (!sr_bufs) {
-  } else if (s_prec == NQ_S_TF32 || s_prec == NQ_S_TF32X3 || s_prec == NQ_S_BF16) {
+  if (!sr_bufs && !cg_x) {
+  } else if (sr_bufs && (s_prec == NQ_S_TF32 || s_prec == NQ_S_TF32X3 || s_prec == NQ_S_BF16)) {
     const int bf16 = s_prec == NQ_S_BF16 ? 1 : 0;
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     h->gram_ksplit = gram_tc_ksplit(rows, h->Ns_pad, bf16);
@@ -867,6 +876,10 @@ nq_status create_impl(const nq_config* cfg, int n_layers, const nq_layer* layers
   } else if (h->ndm || h->chain) {
     h->Ns_pad = ((h->Ns + 127) / 128) * 128;
     step(dalloc(&h->d_X, (size_t)rows * h->Ns_pad), "X");
+  }
+  if (cg_x) {
+    h->cga.X = h->d_X;
+    h->cga.ldx = h->Ns_pad;
   }
   if (sr_bufs) {
     step(dalloc(&h->d_S, 2 * (size_t)P * P), "S");

@@ -339,10 +339,16 @@ struct SrCgArgs {
   int* status = nullptr;
   double* info = nullptr;          // [2]
   uint64_t wait_ns = kNqWaitNs;    // limit of every grid-barrier wait
+  // O of the other networks (NDM family, chains): the centred O_c rows of X
+  // (Re O_p at row 2p, Im O_p at row 2p + 1, FP32, row stride ldx); null
+  // for the RBM, whose O is formed from (σ, g, ⟨O⟩)
+  const float* X = nullptr;
+  int ldx = 0;
 };
 int sr_cg_grid();
 size_t sr_cg_ctl_bytes();
-bool sr_cg_supported(int N, int M);   // the CG kernel's shared memory fits
+bool sr_cg_supported(int N, int M);   // the CG kernel's shared memory fits (RBM)
+bool sr_cg_x_supported(int P);        // the same with O read from X
 cudaError_t launch_sr_cg(const SrCgArgs& args, int kind, double lam, cudaStream_t st);
 
 // y = -W x for the full Hermitian W

@@ -14,6 +14,12 @@
 // per CTA, FP64 across CTAs), a fixed-order reduction of the CTA partials and
 // the CG recurrences, separated by bounded grid barriers.  Every dot product is reduced in a fixed order, so the result
 // does not depend on timing.  Memory: O(P · CTAs + Ns), no P x P matrix.
+//
+// The other networks (NDM family, feed-forward and density-matrix chains)
+// have O materialised as the centred rows of X (FP32, the SrMatrix's Ô):
+// the forward pass is a thread per sample over the P complex rows, the
+// adjoint a warp per parameter row over the CTA's sample chunk (fixed-order
+// shuffle sums), and everything after the partials is shared.
 #include "nq_kernels.cuh"
 #include "tc_common.cuh"
 
@@ -59,6 +65,9 @@ __device__ void block_sum2d(double& a, double& b) {
 
 NQ_D double2 ldcg2(const double* p) { return make_double2(__ldcg(p), __ldcg(p + 1)); }
 
+// dynamic shared memory of the CG kernel with O read from X (bytes)
+NQ_HD size_t cg_x_smem_bytes(int P) { return (size_t)P * sizeof(float2) + 16; }
+
 __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CgCtl* ctl = reinterpret_cast<CgCtl*>(a.ctl);
@@ -78,6 +87,8 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
   // sample chunk of this CTA for the adjoint
   const int chunk = (Ns + G - 1) / G, s0 = min(Ns, b * chunk), s1 = min(Ns, s0 + chunk);
   const double inv_ns = 1.0 / Ns;
+  const bool xs = a.X != nullptr;      // O from the centred rows of X
+  const size_t ldx = (size_t)a.ldx;
 
   // shift_p (multiplicative: lam * S_pp, with S_pp from a pass over the samples)
   // x = 0, r = F, p = F
@@ -110,8 +121,8 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
       s_v[p] = make_float2((float)v.x, (float)v.y);
     }
     {
-      double cx = 0.0, cy = 0.0;      // ⟨O⟩·p, same fixed order in every CTA
-      for (int p = tid; p < P; p += THREADS) {
+      double cx = 0.0, cy = 0.0;      // ⟨O⟩·p, same fixed order in every CTA (X is centred: 0)
+      for (int p = tid; p < (xs ? 0 : P); p += THREADS) {
         const double ox = a.meanO[2 * p], oy = a.meanO[2 * p + 1];
         const double2 v = ldcg2(a.pv + 2 * p);
         cx += ox * v.x - oy * v.y;
@@ -122,9 +133,22 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     }
     __syncthreads();
     const float cx = (float)s_c[0], cy = (float)s_c[1];
-    // one thread per sample; the hidden units in register chunks of FH, so a
+    // X: one thread per sample, t_s = Σ_p O_c,p(s) v_p over the rows of X
+    for (int s = b * THREADS + tid; xs && s < Ns; s += G * THREADS) {
+      const float* xc = a.X + s;
+      float tx = 0.f, ty = 0.f;
+#pragma unroll 4
+      for (int p = 0; p < P; ++p) {
+        const float ore = __ldg(xc + (size_t)(2 * p) * ldx), oim = __ldg(xc + (size_t)(2 * p + 1) * ldx);
+        const float2 v = s_v[p];
+        tx += ore * v.x - oim * v.y;
+        ty += ore * v.y + oim * v.x;
+      }
+      a.t[s] = make_float2(tx, ty);
+    }
+    // RBM: one thread per sample; the hidden units in register chunks of FH, so a
     // site value serves FH units: u_h = v_b,h + Σ_j v_W,hj σ_j, t += g_h u_h
-    for (int s = b * THREADS + tid; s < Ns; s += G * THREADS) {
+    for (int s = b * THREADS + tid; !xs && s < Ns; s += G * THREADS) {
       const uint64_t bits = a.samples[s];
       float tx = -cx, ty = -cy;
       for (int j = 0; j < N; ++j) {
@@ -158,14 +182,39 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     }
     if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     // ---- adjoint partials over this CTA's sample chunk ----
+    if (xs) {
+      // y_p = Σ_s conj(O_c,p(s)) t_s: a warp per row of X, lanes over the chunk
+      const int lane = tid & 31;
+      for (int p = tid >> 5; p < P; p += THREADS / 32) {
+        const float* xr = a.X + (size_t)(2 * p) * ldx;
+        const float* xi = xr + ldx;
+        float ax = 0.f, ay = 0.f;
+        for (int s = s0 + lane; s < s1; s += 32) {
+          const float ore = __ldg(xr + s), oim = __ldg(xi + s);
+          const float2 t = __ldcg(reinterpret_cast<const float2*>(a.t) + s);
+          ax += ore * t.x + oim * t.y;
+          ay += ore * t.y - oim * t.x;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          ax += __shfl_xor_sync(0xffffffffu, ax, o);
+          ay += __shfl_xor_sync(0xffffffffu, ay, o);
+        }
+        if (lane == 0) {
+          a.part[((size_t)b * P + p) * 2] = (double)ax;
+          a.part[((size_t)b * P + p) * 2 + 1] = (double)ay;
+        }
+      }
+      if (tid == 0) { a.tsum[2 * b] = 0.0; a.tsum[2 * b + 1] = 0.0; }
+    }
     // y_a,j = Σ_s σ_sj t_s, y_b,h = Σ_s z_sh, y_W,hj = Σ_s σ_sj z_sh with
     // z_sh = conj(g_sh) t_s: per tile of TS samples, z and σ are staged in
     // shared memory and the W block is a register-tiled (AH x AJ) contraction
     // over the tile; FP32 sums per tile, added into this CTA's FP32 totals.
-    for (int p = tid; p < P; p += THREADS) s_acc[p] = make_float2(0.f, 0.f);
+    for (int p = tid; !xs && p < P; p += THREADS) s_acc[p] = make_float2(0.f, 0.f);
     const int HT = (M + AH - 1) / AH, JT = (N + AJ - 1) / AJ, ntile = HT * JT;
     float tsx = 0.f, tsy = 0.f;
-    for (int c0 = s0; c0 < s1; c0 += TS) {
+    for (int c0 = s0; !xs && c0 < s1; c0 += TS) {
       const int nt = min(TS, s1 - c0);
       __syncthreads();
       for (int q = tid; q < TS; q += THREADS) {
@@ -235,11 +284,11 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
       }
     }
     __syncthreads();
-    for (int p = tid; p < P; p += THREADS) {
+    for (int p = tid; !xs && p < P; p += THREADS) {
       a.part[((size_t)b * P + p) * 2] = (double)s_acc[p].x;
       a.part[((size_t)b * P + p) * 2 + 1] = (double)s_acc[p].y;
     }
-    if (tid == 0) { a.tsum[2 * b] = tsx; a.tsum[2 * b + 1] = tsy; }
+    if (tid == 0 && !xs) { a.tsum[2 * b] = tsx; a.tsum[2 * b + 1] = tsy; }
     if (!cg_barrier(ctl, a.status, a.wait_ns)) return;
     // ---- w = S p + shift p on this CTA's slice; p·w partial ----
     double tx = 0.0, ty = 0.0;
@@ -335,6 +384,27 @@ __global__ void sr_diag_kernel(SrCgArgs a, double lam, int kind) {
   a.shift[p] = lam * (acc / Ns - (ox * ox + oy * oy));
 }
 
+// the same from the centred rows of X: S_pp = mean |O_c,p|², a warp per row
+__global__ void sr_diag_x_kernel(SrCgArgs a, double lam, int kind) {
+  const int lane = threadIdx.x & 31;
+  const int p = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (p >= a.P) return;                 // p is uniform across the warp
+  if (kind != 1) {
+    if (lane == 0) a.shift[p] = kind == 0 ? a.eps : 0.0;
+    return;
+  }
+  const float* xr = a.X + (size_t)(2 * p) * a.ldx;
+  const float* xi = xr + a.ldx;
+  double acc = 0.0;
+  for (int s = lane; s < a.Ns; s += 32) {
+    const double r = xr[s], i = xi[s];
+    acc += r * r + i * i;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) a.shift[p] = lam * (acc / a.Ns);
+}
+
 }  // namespace
 
 int sr_cg_grid() {
@@ -350,15 +420,19 @@ int sr_cg_grid() {
 
 size_t sr_cg_ctl_bytes() { return sizeof(CgCtl); }
 bool sr_cg_supported(int N, int M) { return cg_smem_bytes(N, M) <= 220 * 1024; }
+bool sr_cg_x_supported(int P) { return P >= 1 && cg_x_smem_bytes(P) <= 220 * 1024; }
 
 cudaError_t launch_sr_cg(const SrCgArgs& args, int kind, double lam, cudaStream_t st) {
-  if (!sr_cg_supported(args.N, args.M)) return cudaErrorInvalidValue;
-  sr_diag_kernel<<<(args.P + 255) / 256, 256, 0, st>>>(args, lam, kind);
+  const bool xs = args.X != nullptr;
+  if (xs ? (!sr_cg_x_supported(args.P) || args.ldx < args.Ns) : !sr_cg_supported(args.N, args.M))
+    return cudaErrorInvalidValue;
+  if (xs) sr_diag_x_kernel<<<(args.P + 7) / 8, 256, 0, st>>>(args, lam, kind);
+  else sr_diag_kernel<<<(args.P + 255) / 256, 256, 0, st>>>(args, lam, kind);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(args.ctl, 0, sizeof(CgCtl), st);
   if (e != cudaSuccess) return e;
-  const size_t smem = cg_smem_bytes(args.N, args.M);
+  const size_t smem = xs ? cg_x_smem_bytes(args.P) : cg_smem_bytes(args.N, args.M);
   e = cudaFuncSetAttribute(sr_cg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};

@@ -2,10 +2,13 @@
 solve on the same samples.
 
 The conjugate-gradient solve never forms S: it applies conj(O_c) O_cᵀ / Ns
-from (σ, g, ⟨O⟩) each iteration.  With a tight tolerance (1e-10 relative
-residual) Δw agrees with the oracle's direct solve of the FP64 S to the FP32
-precision of the operator (relative 2e-3, as the direct path's test), and
-the reported residual meets the tolerance.
+each iteration, from (σ, g, ⟨O⟩) for the RBM and from the centred O rows of X
+for the other networks (feed-forward chains, the NDM, density-matrix chains
+with complex DenseSplit or real PositiveDefR parameters).  With a tight
+tolerance Δw agrees with the oracle's direct solve of the FP64 S, and with
+the engine's direct solve on the same samples, to the FP32 precision of the
+operator (relative 2e-3, as the direct path's test), and the reported
+residual meets the tolerance.
 """
 import numpy as np
 import pytest
@@ -88,3 +91,123 @@ def test_cg_vmc_steps(nqlib):
     assert abs(a.mean_re - b.mean_re) < 5e-3 * abs(a.mean_re)
     iters, res = cg.engine.sr_info()
     assert res <= 1e-6 and iters > 0
+
+
+def _tfim(hilb, N):
+    H = nq.LocalOperator(hilb)
+    for i in range(1, N + 1):
+        H = H - nq.sigmax(hilb, i)
+        H = H + nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i % N + 1)
+    return H
+
+
+def _dissipative(hilb, N, g=1.0, V=2.0, gamma=1.0):
+    H = nq.LocalOperator(hilb)
+    Ls = []
+    for i in range(1, N + 1):
+        H = H + (g / 2) * nq.sigmax(hilb, i)
+        Ls.append(float(np.sqrt(gamma)) * nq.sigmam(hilb, i))
+    for i in range(1, N):
+        H = H + (V / 4) * nq.sigmaz(hilb, i) * nq.sigmaz(hilb, i + 1)
+    return nq.liouvillian(H, Ls)
+
+
+def make_x(network, algorithm, B=128, L=8, seed=5, precision=1e-9):
+    """The networks whose O the CG solve reads from X, with the oracle twin."""
+    if network == "chain":          # examples/ising1d_ffnn.jl
+        N = 8
+        hilb = nq.HomogeneousSpin(N)
+        net = nq.PureChain(N, nq.Dense(np.complex64, N, 2 * N, nq.af_logcosh), nq.sum_autobatch)
+        nq.init_random_pars_(net, sigma=0.1 ** 2, rng=np.random.default_rng(seed))
+        onet = onw.Chain(N, [("dense", N, 2 * N, onw.LOGCOSH), ("sum", 2 * N)])
+        prob, nst, real = _tfim(hilb, N), N, False
+    elif network == "ndm":          # examples/dissipative_ising1d.jl
+        N = 4
+        hilb = nq.HomogeneousSpin(N)
+        net = nq.NDM(np.float64, N, 1, 1, nq.af_softplus)
+        nq.init_random_pars_(net, sigma=0.1 ** 2, rng=np.random.default_rng(seed))
+        onet = onw.NDM(N, 1, 1, onw.SOFTPLUS)
+        prob, nst, real = _dissipative(hilb, N), 2 * N, True
+    else:                           # density-matrix chains
+        N = 4
+        hilb = nq.HomogeneousSpin(N)
+        if network == "mixed_pdr":
+            first, ofirst = nq.PositiveDefR(np.float32, N, 2 * N, nq.af_logcosh), "positive_def_r"
+        else:
+            first, ofirst = nq.DenseSplit(np.complex64, N, 2 * N, nq.af_logcosh), "dense_split"
+        net = nq.MixedStateAnsatz(nq.Chain(first, nq.sum_autobatch), N)
+        nq.init_random_pars_(net, sigma=0.15 ** 2, rng=np.random.default_rng(seed))
+        onet = onw.MixedChain(N, [(ofirst, N, 2 * N, onw.LOGCOSH), ("sum", 2 * N)])
+        prob, nst, real = _dissipative(hilb, N), 2 * N, network == "mixed_pdr"
+    onet.set_flat(net.flat())
+    smp = nq.MetropolisSampler(nq.LocalRule(), L, nst, burn=10, seed=seed * 3 + 1)
+    is_ = nq.BatchedSampler(net, smp, prob, nq.SR(eps=0.01, algorithm=algorithm, precision=precision),
+                            batch_sz=B)
+    return is_, onet, real
+
+
+@pytest.mark.parametrize("network", ["chain", "ndm", "mixed_split", "mixed_pdr"])
+def test_cg_over_X_matches_direct_on_same_samples(nqlib, network):
+    direct, onet, real = make_x(network, nq.sr_cholesky)
+    cg, _, _ = make_x(network, nq.sr_cg)
+    samples, _ = direct.engine.sample(2)
+    cg.engine.set_samples(samples)
+    _, _, f1 = direct.engine.estimate(want_force=True)
+    _, _, f2 = cg.engine.estimate(want_force=True)
+    assert rel(f2, f1) < 1e-6
+    d1 = direct.engine.precondition(0, 0.01)
+    d2 = cg.engine.precondition(0, 0.01)
+    assert rel(d2, d1) < 2e-3
+    if real:
+        assert np.all(np.imag(d2) == 0)
+    iters, res = cg.engine.sr_info()
+    assert 0 < iters <= 10 * cg.engine.P and res <= 1e-9
+    with pytest.raises(nq._lib.NqError):
+        cg.engine.sr_matrix()
+
+
+@pytest.mark.parametrize("network", ["chain", "ndm"])
+def test_cg_over_X_matches_oracle(nqlib, network):
+    """Δw of the shift and the multiplicative shift against the oracle's FP64
+    solve on the engine's samples."""
+    is_, onet, real = make_x(network, nq.sr_cg, precision=1e-10)
+    eng = is_.engine
+    samples, _ = eng.sample(1)
+    _, _, force = eng.estimate(want_force=True)
+    if network == "chain":
+        flat = samples.reshape(-1, eng.N).astype(np.float64)
+        _, O = onet.logpsi_and_grad(flat)
+    else:
+        flat = samples.reshape(-1, 2 * eng.N).astype(np.float64)
+        _, O = onet.logpsi_and_grad(flat[:, :eng.N], flat[:, eng.N:])
+    S = osr.build_S(oest.center(O)[0], real_params=real)
+    for kind in (0, 1):
+        if kind == 0:
+            dw = eng.precondition(0, 0.01)
+            A = S + 0.01 * np.eye(S.shape[0])
+        else:
+            lam = max(100.0 * 0.95 ** 7, 1e-4)
+            dw = eng.precondition(1, 0.0, 100.0, 0.95, 1e-4, 7)
+            A = S + lam * np.diag(np.diag(S))
+        dwo = np.linalg.solve(A, np.real(force) if real else force)
+        assert rel(dw, dwo) < 2e-3, kind
+
+
+def test_cg_ffnn_example_lowers_energy(nqlib):
+    """examples/ising1d_ffnn.jl's solver, SR(ϵ=0.1, algorithm=sr_cg,
+    precision=1e-3), on its Chain(Dense(N, 2N, af_logcosh), sum_autobatch)."""
+    N = 8
+    hilb = nq.HomogeneousSpin(N)
+    net = nq.PureChain(N, nq.Dense(np.complex64, N, 2 * N, nq.af_logcosh), nq.sum_autobatch)
+    nq.init_random_pars_(net, sigma=0.05 ** 2, rng=np.random.default_rng(3))
+    smp = nq.MetropolisSampler(nq.LocalRule(), 8, N + 1, burn=10, seed=20)
+    is_ = nq.BatchedSampler(net, smp, _tfim(hilb, N), nq.SR(eps=0.1, algorithm=nq.sr_cg, precision=1e-3),
+                            batch_sz=512)
+    e0 = oex.tfim_ground_energy_1d(N, 1.0, 1.0)
+    first = is_.step(0.05)
+    for _ in range(60):
+        m = is_.step(0.05)
+    assert m.mean.real < first.mean.real - 0.05 * abs(e0)
+    assert m.mean.real > e0 - 5 * max(m.error, 1e-3)
+    iters, res = is_.engine.sr_info()
+    assert iters > 0 and res <= 1e-3
