@@ -198,3 +198,44 @@ def test_product_path_never_reaches_the_oracle():
                         if pat.search(line):
                             hits.append(f"{os.path.relpath(path, root)}:{n}: {line.strip()}")
     assert not hits, hits
+
+
+def test_positive_def_r_host_layer_and_chain_validation():
+    """PositiveDefR (Layers/PositiveDefR.jl): real Wr, Wi, b; the chain's flat
+    vector carries them with zero imaginary part, later complex layers keep
+    theirs; the layer is nq_layer kind 4 and opens density-matrix chains only
+    (checked by the Python mirror and by nq_create_chain before any device
+    call)."""
+    N, M = 4, 6
+    l0 = nq.PositiveDefR(np.float32, N, M, nq.af_logcosh, rng=np.random.default_rng(1))
+    assert l0.Wr.dtype == np.float32 and l0.Wi.shape == (M, N) and l0.b.shape == (M,)
+    with pytest.raises(ValueError):
+        nq.PositiveDefR(np.complex64, N, M)
+    net = nq.MixedStateAnsatz(nq.Chain(l0, nq.Dense(np.complex64, M, 3, nq.af_softplus), nq.WSum(np.complex64, 3)),
+                              N)
+    assert net.real_sr
+    nq.init_random_pars_(net, sigma=0.1, rng=np.random.default_rng(2))
+    p = net.flat()
+    n1 = 2 * M * N + M
+    assert p.dtype == np.complex128 and np.all(p[:n1].imag == 0) and np.any(p[n1:].imag != 0)
+    assert np.all(p[:n1].real != 0)
+    net.set_flat(p + 1j)
+    np.testing.assert_array_equal(net.flat()[:n1], p[:n1])
+    arr = nq.engine.chain_layers(net)
+    assert [a.kind for a in arr] == [_lib.NQ_LAYER_POSITIVE_DEF_R, _lib.NQ_LAYER_DENSE, _lib.NQ_LAYER_WSUM]
+    with pytest.raises(ValueError):
+        nq.MixedStateAnsatz(nq.Chain(nq.Dense(np.complex64, N, M), l0, nq.sum_autobatch), N)
+    lib = nq.lib()
+    cases = [
+        (_lib.NQ_NET_MIXED_CHAIN, [(_lib.NQ_LAYER_DENSE_SPLIT, N, M, 0), (_lib.NQ_LAYER_POSITIVE_DEF_R, M, M, 0),
+                                   (_lib.NQ_LAYER_SUM, M, 1, 0)]),
+        (_lib.NQ_NET_CHAIN, [(_lib.NQ_LAYER_POSITIVE_DEF_R, N, M, 0), (_lib.NQ_LAYER_SUM, M, 1, 0)]),
+    ]
+    for network, layers in cases:
+        cfg = _lib.NqConfig()
+        cfg.network, cfg.hilbert = network, _lib.NQ_HILB_SPIN
+        cfg.n_sites, cfg.n_chains, cfg.chain_length, cfg.passes = N, 16, 2, 1
+        arr = (_lib.NqLayer * len(layers))(*[_lib.NqLayer(*l) for l in layers])
+        h = ctypes.c_void_p()
+        assert lib.nq_create_chain(ctypes.byref(cfg), len(layers), arr, ctypes.byref(h)) == _lib.NQ_ERR_ARG
+        assert not h.value
