@@ -337,6 +337,12 @@ nq_status nq_get_sr_matrix(nq_handle* h, double* s_out);
  * the two. */
 nq_status nq_set_sr_tolerance(nq_handle* h, double tol, int32_t maxiter);
 nq_status nq_sr_info(nq_handle* h, double* out2);
+/* SR(time_evo=true) (SR.jl:51-57; setup_algorithm! in SRDirect.jl:26-48 and
+ * SRIterative.jl:32-65): the solves of this handle (nq_precondition,
+ * nq_vmc_step) take α F with α = i instead of F, Re(i F) for real
+ * parameters, so that Δw drives real-time evolution; on = 0 restores α = 1.
+ * The force that nq_estimate and nq_get_estimates return stays ∇C. */
+nq_status nq_set_time_evolution(nq_handle* h, int32_t on);
 /* Limit, in nanoseconds, of every grid-barrier wait in this handle's SR solve
  * kernels (the cooperative inversion, the refinement and the conjugate
  * gradients; 0 restores the default of 1 s).  A wait that runs out ends its

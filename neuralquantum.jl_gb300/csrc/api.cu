@@ -392,8 +392,16 @@ nq_status stage_S(nq_handle* h) {
 }
 
 nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
+  // SR(time_evo=true): α F with α = i (SRDirect.jl:27, SRIterative.jl:33)
+  const double* F = h->fb.force;
+  if (h->time_evo) {
+    CKL(launch_times_i(h->fb.force, h->P, h->d_frhs, h->st));
+    ++h->launches;
+    F = h->d_frhs;
+  }
   if (h->cg) {
     SrCgArgs a = h->cga;
+    a.F = F;
     a.eps = eps;
     a.tol = h->cg_tol;
     a.maxiter = h->cg_maxiter;
@@ -408,7 +416,7 @@ nq_status stage_solve(nq_handle* h, int kind, double eps, double lam) {
   }
   SolveBufs sb = h->sb;
   sb.ev = h->capturing ? nullptr : h->sev;
-  CKL(launch_sr_solve(sb, h->P, h->fb.force, kind, eps, lam, h->real_sr, kSolveRefine, h->st));
+  CKL(launch_sr_solve(sb, h->P, F, kind, eps, lam, h->real_sr, kSolveRefine, h->st));
   h->launches += 8;
   return NQ_OK;
 }
@@ -945,7 +953,7 @@ void nq_destroy(nq_handle* h) {
   proposal_destroy(h);
   free_op(h);
   free_rule_operator(h);
-  void* bufs[] = {h->d_master, h->d_p32, h->d_pexp, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
+  void* bufs[] = {h->d_master, h->d_p32, h->d_pexp, h->d_frhs, h->d_tab[0], h->d_tab[1], h->d_tab[2], h->d_samples,
                   h->d_accepted, h->d_call, h->d_logpsi, h->d_g, h->d_eloc, h->d_g32,
                   h->fb.partial, h->fb.partialE, h->fb.meanO, h->fb.force, h->fb.meanE, h->fb.sums,
                   h->d_chainstats,
@@ -1567,6 +1575,18 @@ nq_status nq_set_wait_limit(nq_handle* h, uint64_t limit_ns) {
   h->sb.wait_ns = v;
   h->cga.wait_ns = v;
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NQ_OK;
+}
+
+nq_status nq_set_time_evolution(nq_handle* h, int32_t on) {
+  if (!h) return NQ_ERR_ARG;
+  NQ_REJECT_DIAG(h, "nq_set_time_evolution");
+  if (on && !h->d_frhs) CK(cudaMalloc(&h->d_frhs, 2 * sizeof(double) * (size_t)h->P));
+  if ((on != 0) != h->time_evo && h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  h->time_evo = on != 0;
   return NQ_OK;
 }
 

@@ -64,6 +64,8 @@ struct nq_handle {
   float* d_p32 = nullptr;          // FP32 working copy (RBM, complex)
   double* d_pexp = nullptr;        // FP64 working copy of a PositiveDefR chain (Dense form)
   bool real_sr = false;            // S, F and Δw real: real parameters, or a PositiveDefR chain
+  bool time_evo = false;           // SR(time_evo=true): the solves take i F (d_frhs)
+  double* d_frhs = nullptr;        // [P] complex right-hand side i F
   void* d_tab[3] = {nullptr, nullptr, nullptr};
   uint64_t* d_samples = nullptr;   // [L][B]
   unsigned long long* d_accepted = nullptr;

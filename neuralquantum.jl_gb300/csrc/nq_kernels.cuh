@@ -161,6 +161,8 @@ cudaError_t launch_chain_sampler(const ChainDev<R>& c, const SamplerRun& run, cu
 // n_sites weights): master (Wr, Wi, b, later layers; complex interleaved, P
 // entries) into the Dense form (W_σ, W_η, b, later layers) as FP32 (p32) or
 // FP64 (p64), whichever is non-null
+// out = i F (P complex): the right-hand side of SR with time evolution
+cudaError_t launch_times_i(const double* F, int P, double* out, cudaStream_t st);
 cudaError_t launch_chain_pdr_params(const double* master, int P, int n_out, int n_sites, float* p32, double* p64,
                                     cudaStream_t st);
 

@@ -589,6 +589,19 @@ cudaError_t launch_sr_solve(const SolveBufs& sb, int P, const double* F, int kin
   return cudaSuccess;
 }
 
+__global__ void times_i_kernel(const double* __restrict__ F, int P, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P) return;
+  const double x = F[2 * k], y = F[2 * k + 1];
+  out[2 * k] = -y;          // i (x + i y) = -y + i x; its real part is what a real solve reads
+  out[2 * k + 1] = x;
+}
+
+cudaError_t launch_times_i(const double* F, int P, double* out, cudaStream_t st) {
+  times_i_kernel<<<(P + 255) / 256, 256, 0, st>>>(F, P, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_descent(double* master, const double* dw, long n_doubles, int stride, double lr,
                            cudaStream_t st) {
   descent_kernel<<<(unsigned)((n_doubles + 255) / 256), 256, 0, st>>>(master, dw, n_doubles, stride, lr);

@@ -106,6 +106,7 @@ EXPORTS = {
                                    ctypes.c_void_p]),
     "nq_observable": (ctypes.c_int, [ctypes.c_void_p, _P(NqOpTable), _P(NqMeasurement), ctypes.c_void_p]),
     "nq_set_sr_tolerance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32]),
+    "nq_set_time_evolution": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "nq_sr_info": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_double)]),
     "nq_get_sr_matrix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "nq_precondition": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,

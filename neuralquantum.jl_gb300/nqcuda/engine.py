@@ -240,6 +240,10 @@ class Engine:
     def set_sr_tolerance(self, tol, maxiter):
         self._check(self.lib.nq_set_sr_tolerance(self.h, float(tol), int(maxiter)))
 
+    def set_time_evolution(self, on):
+        """SR(time_evo=...): the solves take i F instead of F."""
+        self._check(self.lib.nq_set_time_evolution(self.h, 1 if on else 0))
+
     def set_wait_limit(self, ns):
         """Limit of every grid-barrier wait of the solve kernels (0 = 1 s)."""
         self._check(self.lib.nq_set_wait_limit(self.h, int(ns)))

@@ -29,7 +29,9 @@ _DIRECT = (sr_cholesky, sr_diag, sr_div)
 
 class SR:
     """``SR(T; ϵ=0.001, precision=1e-4, precondition_type=sr_shift,
-    algorithm=sr_cholesky, λ0=100, b=0.95, λmin=1e-4)`` (SR.jl:41-50).
+    algorithm=sr_cholesky, λ0=100, b=0.95, λmin=1e-4, time_evo=false)``
+    (SR.jl:41-57).  ``time_evo`` solves with i F instead of F
+    (SRDirect.jl:27, SRIterative.jl:33), Re(i F) for real parameters.
     sr_cholesky, sr_diag (pinv) and sr_div form S and solve the preconditioned
     system directly (the shifted S is positive definite, where the three
     agree; a singular S with sr_none is refused, not pseudo-inverted); the
@@ -39,9 +41,10 @@ class SR:
     either (SRDirect.jl:84-86)."""
 
     def __init__(self, eps=0.001, precondition_type=sr_shift, algorithm=sr_cholesky,
-                 lam0=100.0, b=0.95, lam_min=1e-4, precision=1e-4):
+                 lam0=100.0, b=0.95, lam_min=1e-4, precision=1e-4, time_evo=False):
         if algorithm not in _DIRECT and algorithm not in _ITERATIVE:
             raise NotImplementedError(f"unknown SR algorithm {algorithm}")
+        self.time_evo = bool(time_evo)
         self.eps, self.precondition_type = float(eps), precondition_type
         self.lam0, self.b, self.lam_min = float(lam0), float(b), float(lam_min)
         self.algorithm, self.precision = algorithm, float(precision)
@@ -100,6 +103,8 @@ class BatchedSampler:
             self.engine.set_rule_operator(op_table(move_op))
         if self.algo.iterative:
             self.engine.set_sr_tolerance(self.algo.precision, 10 * self.engine.P)
+        if getattr(self.algo, "time_evo", False):
+            self.engine.set_time_evolution(True)
         self.engine.set_params(net.flat())
         self.engine.set_operator(op_table(prob))
         self.calls = 0

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import nqcuda as nq
-from oracle import networks as onw, estimators as oest, exact as oex, sr as osr
+from oracle import networks as onw, estimators as oest, exact as oex, sr as osr, operators as oops
 from oracle.hilbert import Hilbert, SPIN
 
 pytestmark = pytest.mark.gpu
@@ -211,3 +211,43 @@ def test_cg_ffnn_example_lowers_energy(nqlib):
     assert m.mean.real > e0 - 5 * max(m.error, 1e-3)
     iters, res = is_.engine.sr_info()
     assert iters > 0 and res <= 1e-3
+
+
+@pytest.mark.parametrize("algorithm", [nq.sr_cholesky, nq.sr_cg])
+def test_time_evolution_solves_with_i_force(nqlib, algorithm):
+    """SR(time_evo=true) (SRDirect.jl:27, SRIterative.jl:33): the solve takes
+    i F.  Direct: against the FP64 solve of the engine's own S with i F; both
+    solvers: i times the solve with F; switching it off restores Δw."""
+    is_, onet, oH = make(algorithm, precision=1e-10)
+    eng = is_.engine
+    eng.sample(1)
+    _, _, force = eng.estimate(want_force=True)
+    dw0 = eng.precondition(0, 0.01)
+    eng.set_time_evolution(True)
+    dw1 = eng.precondition(0, 0.01)
+    assert rel(dw1, 1j * dw0) < 1e-6
+    if algorithm == nq.sr_cholesky:
+        Sg = eng.sr_matrix()
+        assert rel(dw1, np.linalg.solve(Sg + 0.01 * np.eye(Sg.shape[0]), 1j * force)) < 1e-9
+    eng.set_time_evolution(False)
+    assert rel(eng.precondition(0, 0.01), dw0) < 1e-12
+
+
+def test_time_evolution_real_parameters(nqlib):
+    """Real parameters (NDM): the solve takes Re(i F) = -Im F, F from the
+    oracle on the engine's samples (|Im F| is ~7% of |F| here, hence 1e-2)."""
+    is_, onet, real = make_x("ndm", nq.sr_cholesky)
+    eng = is_.engine
+    samples, _ = eng.sample(1)
+    eng.estimate()
+    N = eng.N
+    flat = samples.reshape(-1, 2 * N).astype(np.float64)
+    oH, oL = oex.dissipative_ising(Hilbert(N, SPIN), 1.0, 2.0)
+    Lo, dL = oest.local_liouvillian(onet, oops.liouvillian(oH, oL), flat[:, :N], flat[:, N:])
+    _, O = onet.logpsi_and_grad(flat[:, :N], flat[:, N:])
+    _, F = oest.force_liouvillian(Lo, dL, O)
+    eng.set_time_evolution(True)
+    dw = eng.precondition(0, 0.01)
+    Sg = eng.sr_matrix()
+    assert np.isrealobj(dw)
+    assert rel(dw, np.linalg.solve(Sg + 0.01 * np.eye(Sg.shape[0]), -np.imag(F))) < 1e-2
