@@ -496,6 +496,43 @@ def cg_step():
             "cg_iterations": it, "relative_residual": res}
 
 
+def cg_ndm_step():
+    """The matrix-free CG SR solve over the materialised O rows (X) against the
+    direct solve on the dissipative Ising NDM workload (N = 12, α = β = 2,
+    P = 1248 real parameters, 16384 chains x 8, FP32 evaluation, SR
+    tolerance 1e-4): Δw of both on one sample set, then device ms per whole
+    SR step over 5 timed steps after 3 + 10 warm-up steps, CG iterations."""
+    import nqcuda as nq
+    c = PRECISION
+    N = c["N"]
+    hilb = nq.HomogeneousSpin(N)
+    lv = _dissipative(nq, hilb, N, c["g"], c["V"], c["gamma"])
+
+    def engine(algorithm):
+        net = nq.NDM(np.float64, N, c["alpha"], c["beta"], nq.af_softplus)
+        nq.init_random_pars_(net, sigma=1e-4, rng=np.random.default_rng(c["seed"]))
+        smp = nq.MetropolisSampler(nq.LocalRule(), c["chain_length"], 2 * N, burn=c["burn"], seed=c["seed"])
+        return nq.BatchedSampler(net, smp, lv, nq.SR(eps=c["eps"], algorithm=algorithm, precision=1e-4),
+                                 batch_sz=c["chains"]).engine
+
+    direct, cg = engine(nq.sr_cholesky), engine(nq.sr_cg)
+    samples, _ = direct.sample(3)
+    cg.set_samples(samples)
+    direct.estimate()
+    cg.estimate()
+    d0, d1 = direct.precondition(0, c["eps"]), cg.precondition(0, c["eps"])
+    out = {"workload": "ndm_dissipative_ising_N12_alpha2_beta2_16384x8 SR step, direct vs matrix-free CG over X",
+           "n_params": direct.P,
+           "dw_relative_difference": float(np.max(np.abs(d1 - d0)) / np.max(np.abs(d0)))}
+    for name, eng in (("direct", direct), ("cg", cg)):
+        for i in range(3):
+            eng.vmc_step(i, c["eps"], c["lr"])
+        out[name + "_ms_per_step"] = float(np.mean(eng.bench_steps(10, 5, c["eps"], c["lr"], 0)))
+    it, res = cg.sr_info()
+    out["cg_iterations"], out["relative_residual"] = it, res
+    return out
+
+
 def learned_vs_local():
     """SR on the 6x6 TFIM (h = 3.04) with the MADE proposal trained online on
     the chains' samples every 10 SR steps, then effective samples/s of local
@@ -682,6 +719,8 @@ def main():
                     help="time only the batched step of the 64-problem workload (for launch lists)")
     ap.add_argument("--cg-only", action="store_true",
                     help="time only the matrix-free CG SR step of the 6x6 TFIM workload (for profiles)")
+    ap.add_argument("--cg-ndm-only", action="store_true",
+                    help="time only the direct and the matrix-free CG SR steps of the N=12 NDM workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -689,6 +728,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.cg_only:
         print(json.dumps(cg_step()))
+        return
+    if args.cg_ndm_only:
+        print(json.dumps(cg_ndm_step()))
         return
     if args.batch_only:
         import nqcuda as nq

@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
     for (int s = b * THREADS + tid; xs && s < Ns; s += G * THREADS) {
       const float* xc = a.X + s;
       float tx = 0.f, ty = 0.f;
-#pragma unroll 4
+#pragma unroll 16          // 32 independent loads in flight per thread
       for (int p = 0; p < P; ++p) {
         const float ore = __ldg(xc + (size_t)(2 * p) * ldx), oim = __ldg(xc + (size_t)(2 * p + 1) * ldx);
         const float2 v = s_v[p];
@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(THREADS, 1) sr_cg_kernel(SrCgArgs a) {
         const float* xr = a.X + (size_t)(2 * p) * ldx;
         const float* xi = xr + ldx;
         float ax = 0.f, ay = 0.f;
+#pragma unroll 4
         for (int s = s0 + lane; s < s1; s += 32) {
           const float ore = __ldg(xr + s), oim = __ldg(xi + s);
           const float2 t = __ldcg(reinterpret_cast<const float2*>(a.t) + s);
